@@ -1,0 +1,207 @@
+"""ctypes front-end of the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline legs of bench.py.  The product path (ugcore_gb300) never imports
+this module.  The C sources cite the ugcore files they restate.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+ORC_QUAD, ORC_HEX, ORC_TET = 0, 1, 2
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("elem_type", C.c_int), ("mx", C.c_int), ("my", C.c_int), ("mz", C.c_int), ("nref", C.c_int),
+        ("seed", C.c_uint64),
+        ("coef_kind", C.c_int), ("coef_modes", C.c_int), ("coef_kmax", C.c_double),
+        ("vel_kind", C.c_int), ("vel_modes", C.c_int),
+        ("vel_kmax", C.c_double), ("diffusion", C.c_double), ("peclet", C.c_double),
+        ("solver", C.c_int), ("smoother", C.c_int), ("damp", C.c_double),
+        ("nu1", C.c_int), ("nu2", C.c_int), ("cycle", C.c_int), ("base", C.c_int),
+        ("maxit", C.c_int), ("rel_red", C.c_double), ("min_defect", C.c_double),
+    ]
+
+
+def build():
+    """Compile liboracle.so in place (plain C, seconds)."""
+    subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+        ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+        L.orc_prob_create.restype = P
+        L.orc_prob_create.argtypes = [C.POINTER(Params), P, P]
+        for name in ("orc_prob_num_levels",):
+            getattr(L, name).argtypes = [P]
+        L.orc_prob_level_nv.argtypes = [P, C.c_int]
+        L.orc_prob_level_ne.argtypes = [P, C.c_int]
+        L.orc_prob_level_nnz.argtypes = [P, C.c_int]
+        L.orc_prob_level_nnz.restype = C.c_int64
+        L.orc_prob_level_matrix.argtypes = [P, C.c_int, ip, ip, dp]
+        L.orc_prob_level_coef.argtypes = [P, C.c_int, dp]
+        L.orc_prob_level_elems.argtypes = [P, C.c_int, P, P, P]
+        L.orc_prob_rhs.argtypes = [P, dp]
+        L.orc_prob_source.argtypes = [P, dp]
+        L.orc_prob_transfer_nnz.argtypes = [P, C.c_int, C.c_int]
+        L.orc_prob_transfer_nnz.restype = C.c_int64
+        L.orc_prob_transfer.argtypes = [P, C.c_int, C.c_int, ip, ip, dp]
+        L.orc_prob_apply_gmg.argtypes = [P, dp, dp]
+        L.orc_prob_solve.argtypes = [P, dp, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), P, C.c_int]
+        L.orc_prob_adjoint.argtypes = [P, dp, dp, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double)]
+        L.orc_prob_grad_logk.argtypes = [P, dp, dp, dp]
+        L.orc_prob_grad_source.argtypes = [P, dp, dp]
+        L.orc_prob_free.argtypes = [P]
+        L.orc_transpose_nnz.argtypes = [C.c_int, C.c_int, ip, ip, dp, C.c_int]
+        L.orc_transpose_nnz.restype = C.c_int64
+        L.orc_geometry.argtypes = [C.c_int, dp, dp, dp, dp, ip, ip]
+        _LIB = L
+    return _LIB
+
+
+def make_params(elem_type=ORC_QUAD, mx=2, my=2, mz=2, nref=6, seed=1, coef_kind=0, coef_modes=64,
+                coef_kmax=8.0, vel_kind=0, vel_modes=16, vel_kmax=2.0, diffusion=1.0, peclet=10.0,
+                solver=0, smoother=0, damp=0.6, nu1=2, nu2=2, cycle=1, base=0, maxit=200,
+                rel_red=1e-10, min_defect=1e-300):
+    return Params(elem_type, mx, my, mz, nref, seed, coef_kind, coef_modes, coef_kmax, vel_kind,
+                  vel_modes, vel_kmax, diffusion, peclet, solver, smoother, damp, nu1, nu2, cycle,
+                  base, maxit, rel_red, min_defect)
+
+
+class Problem:
+    """One assemble-and-solve problem held by the oracle."""
+
+    def __init__(self, params, m_top=None, f_top=None):
+        L = lib()
+        self.params = params
+        self._m = None if m_top is None else np.ascontiguousarray(m_top, dtype=np.float64)
+        self._f = None if f_top is None else np.ascontiguousarray(f_top, dtype=np.float64)
+        self.h = L.orc_prob_create(C.byref(params),
+                                   None if self._m is None else self._m.ctypes.data,
+                                   None if self._f is None else self._f.ctypes.data)
+        if not self.h:
+            raise RuntimeError("oracle problem setup failed")
+        self.nlev = L.orc_prob_num_levels(self.h)
+        self.top = self.nlev - 1
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_prob_free(self.h)
+            self.h = None
+
+    def nv(self, l=None):
+        return lib().orc_prob_level_nv(self.h, self.top if l is None else l)
+
+    def ne(self, l=None):
+        return lib().orc_prob_level_ne(self.h, self.top if l is None else l)
+
+    def matrix(self, l=None):
+        l = self.top if l is None else l
+        L = lib()
+        n = self.nv(l)
+        nnz = L.orc_prob_level_nnz(self.h, l)
+        rp = np.zeros(n + 1, np.int32)
+        ci = np.zeros(nnz, np.int32)
+        va = np.zeros(nnz, np.float64)
+        L.orc_prob_level_matrix(self.h, l, rp, ci, va)
+        return rp, ci, va
+
+    def transfer(self, l, which):
+        """which = 0: P (fine l x coarse l-1), 1: R."""
+        L = lib()
+        nnz = L.orc_prob_transfer_nnz(self.h, l, which)
+        nrow = self.nv(l) if which == 0 else self.nv(l - 1)
+        rp = np.zeros(nrow + 1, np.int32)
+        ci = np.zeros(nnz, np.int32)
+        va = np.zeros(nnz, np.float64)
+        L.orc_prob_transfer(self.h, l, which, rp, ci, va)
+        return rp, ci, va
+
+    def coef(self, l=None):
+        l = self.top if l is None else l
+        K = np.zeros(self.ne(l))
+        lib().orc_prob_level_coef(self.h, l, K)
+        return K
+
+    def rhs(self):
+        b = np.zeros(self.nv())
+        lib().orc_prob_rhs(self.h, b)
+        return b
+
+    def source(self):
+        f = np.zeros(self.nv())
+        lib().orc_prob_source(self.h, f)
+        return f
+
+    def apply_gmg(self, d):
+        c = np.zeros(self.nv())
+        rc = lib().orc_prob_apply_gmg(self.h, c, np.ascontiguousarray(d, np.float64))
+        if rc:
+            raise RuntimeError("gmg init failed %d" % rc)
+        return c
+
+    def solve(self, hist_cap=0):
+        x = np.zeros(self.nv())
+        steps = C.c_int()
+        d0, d1 = C.c_double(), C.c_double()
+        hist = np.zeros(max(hist_cap, 1))
+        rc = lib().orc_prob_solve(self.h, x, C.byref(steps), C.byref(d0), C.byref(d1),
+                                  hist.ctypes.data if hist_cap else None, hist_cap)
+        return dict(x=x, steps=steps.value, d0=d0.value, d1=d1.value, converged=(rc == 0),
+                    history=hist[:min(steps.value + 1, hist_cap)] if hist_cap else None)
+
+    def adjoint(self, g):
+        lam = np.zeros(self.nv())
+        steps = C.c_int()
+        d0, d1 = C.c_double(), C.c_double()
+        rc = lib().orc_prob_adjoint(self.h, np.ascontiguousarray(g, np.float64), lam, C.byref(steps),
+                                    C.byref(d0), C.byref(d1))
+        return dict(lam=lam, steps=steps.value, d0=d0.value, d1=d1.value, converged=(rc == 0))
+
+    def grad_logk(self, u, lam):
+        g = np.zeros(self.ne())
+        lib().orc_prob_grad_logk(self.h, np.ascontiguousarray(u, np.float64),
+                                 np.ascontiguousarray(lam, np.float64), g)
+        return g
+
+    def grad_source(self, lam):
+        g = np.zeros(self.nv())
+        lib().orc_prob_grad_source(self.h, np.ascontiguousarray(lam, np.float64), g)
+        return g
+
+
+def transpose_nnz(rowptr, col, val, n_cols, keep_zeros):
+    rowptr = np.ascontiguousarray(rowptr, np.int32)
+    return lib().orc_transpose_nnz(len(rowptr) - 1, n_cols, rowptr, np.ascontiguousarray(col, np.int32),
+                                   np.ascontiguousarray(val, np.float64), int(keep_zeros))
+
+
+def geometry(elem_type, corners):
+    dim = 2 if elem_type == ORC_QUAD else 3
+    k = 8 if elem_type == ORC_HEX else 4
+    nf = {ORC_QUAD: 4, ORC_HEX: 12, ORC_TET: 6}[elem_type]
+    corners = np.ascontiguousarray(corners, np.float64).reshape(-1)
+    normals = np.zeros(nf * dim)
+    vols = np.zeros(k)
+    grads = np.zeros(nf * k * dim)
+    fr = np.zeros(nf, np.int32)
+    to = np.zeros(nf, np.int32)
+    lib().orc_geometry(elem_type, corners, normals, vols, grads, fr, to)
+    return dict(normals=normals.reshape(nf, dim), vols=vols, grads=grads.reshape(nf, k, dim),
+                frm=fr, to=to)

@@ -1,0 +1,184 @@
+/*
+ * ug4_oracle.h -- CPU restatement of UG4/ugcore's assemble-and-solve path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the correctness oracle for the
+ * GB300 kernels in ugcore_gb300/csrc.  Only tests/, __graft_entry__.smoke()
+ * and the CPU-baseline legs of bench.py may load it; the product path never
+ * does.  Every routine cites the reference file:line whose behaviour it
+ * restates (paths relative to the ugcore source tree, ugbase/...).
+ *
+ * Scope (all FP64, single-threaded like the reference hot path):
+ *   - structured grid hierarchies (quad 2D, hex 3D, Kuhn 6-tet 3D) with
+ *     lexicographic DoF numbering and parent tables;
+ *   - FV1 (box-method) element assembly of -div(K grad u) + div(v u) = f with
+ *     full upwind, Dirichlet rows kept in the pattern;
+ *   - StdTransfer P1 prolongation, R = P^T, Dirichlet adjustment of both;
+ *   - damped Jacobi, multicolour Gauss-Seidel, dense pivoted LU;
+ *   - AssembledMultiGridCycle V/W cycle, CG and BiCGStab with StdConvCheck;
+ *   - the discrete adjoint (transposed solve, element/vertex gradients).
+ */
+#ifndef UG4_ORACLE_H
+#define UG4_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_QUAD = 0, ORC_HEX = 1, ORC_TET = 2 };
+
+typedef struct {
+    int n_rows, n_cols;
+    int64_t nnz;
+    int *rowptr;   /* n_rows + 1 */
+    int *col;      /* nnz, sorted per row */
+    double *val;   /* nnz */
+} orc_crs;
+
+typedef struct {
+    int elem_type, dim, k;      /* k = corners per element */
+    int nx, ny, nz;             /* vertices per axis (nz = 1 in 2D) */
+    int nv, ne;
+    double *coords;             /* nv * dim */
+    int *elems;                 /* ne * k, corners in reference order */
+    unsigned char *bnd;         /* nv: 1 = Dirichlet boundary vertex */
+    int *npar;                  /* nv: number of coarse parents (level > 0) */
+    int *par;                   /* nv * 8: coarse parent vertex ids, sorted */
+} orc_level;
+
+typedef struct {
+    int nlev;
+    orc_level *lev;
+} orc_hier;
+
+/* random fields (seeded, counter-based) */
+typedef struct {
+    int nmodes;
+    int dim;
+    double amp;          /* sqrt(2/nmodes) * sigma */
+    double *k;           /* nmodes * dim wavevectors */
+    double *phase;       /* nmodes */
+    double *a;           /* nmodes * 3 vector amplitudes (curl field only) */
+    double scale;        /* post-scale (curl field) */
+} orc_field;
+
+uint64_t orc_splitmix64(uint64_t *state);
+double orc_hash_uniform(uint64_t seed, uint64_t i);   /* U[0,1) from (seed,i) */
+void orc_source_uniform(uint64_t seed, int n, double *f); /* U[-1,1] */
+
+int orc_field_scalar_init(orc_field *F, int dim, int nmodes, double kmax, uint64_t seed);
+int orc_field_curl_init(orc_field *F, int nmodes, double kmax, uint64_t seed);
+double orc_field_scalar_eval(const orc_field *F, const double *x);
+void orc_field_curl_eval(const orc_field *F, const double *x, double *v);
+void orc_field_free(orc_field *F);
+
+/* hierarchy */
+int orc_hier_create(orc_hier *H, int elem_type, int mx, int my, int mz, int nref);
+void orc_hier_free(orc_hier *H);
+void orc_level_centroids(const orc_level *L, double *c);
+
+/* CRS */
+void orc_crs_free(orc_crs *A);
+int orc_crs_pattern_from_elems(const orc_level *L, orc_crs *A);
+int orc_crs_transpose(const orc_crs *B, int keep_zeros, orc_crs *T);
+void orc_crs_axpy(const orc_crs *A, double *dest, double alpha1, const double *v1,
+                  double beta1, const double *w1);
+void orc_crs_matmul_minus(const orc_crs *A, double *res, const double *x);
+void orc_crs_apply_ignore_zero_rows(const orc_crs *A, double *dest, double beta, const double *w);
+int orc_crs_find(const orc_crs *A, int r, int c);
+
+/* FV1 element geometry (one element, arbitrary corner coords) */
+typedef struct {
+    int nscv, nscvf;
+    int from[12], to[12];
+    double normal[12][3];
+    double gip[12][3];       /* global SCVF integration points */
+    double grad[12][8][3];   /* global shape gradients at SCVF ips */
+    double vol[8];           /* SCV volumes */
+} orc_fv1geom;
+
+int orc_fv1_geometry(int elem_type, const double *corner, orc_fv1geom *G);
+
+/* assembly: K per element (NULL = 1), vel per element per scvf ip (NULL = 0)
+   or velocity field F (if vel == NULL and F != NULL), f per vertex (NULL = 0). */
+typedef struct {
+    const double *K;         /* ne */
+    const double *vel;       /* ne * nscvf * dim */
+    const orc_field *vfield; /* evaluated at scvf ips if vel == NULL */
+    const double *f;         /* nv */
+    int upwind;              /* 0 = none (no convection), 1 = full upwind */
+    int dirichlet;           /* 1 = zero Dirichlet on the boundary */
+} orc_disc;
+
+int orc_assemble(const orc_level *L, const orc_disc *D, orc_crs *A, double *b);
+void orc_scv_volume_sum(const orc_level *L, double *vol);
+int orc_element_matrix(const orc_level *L, int e, double K, const orc_field *vf, int upwind,
+                       double *Aloc, double *vol);
+int orc_grad_logk(const orc_level *L, const double *K, const double *u, const double *lam, double *g);
+
+/* transfers */
+int orc_prolongation(const orc_level *fine, const orc_level *coarse, orc_crs *P);
+int orc_restriction(const orc_level *fine, const orc_level *coarse, const orc_crs *P, orc_crs *R);
+
+/* dense LU (no-LAPACK path) */
+typedef struct { int n; double *LU; int *piv; } orc_lu;
+int orc_lu_init(orc_lu *F, const orc_crs *A);
+void orc_lu_apply(const orc_lu *F, double *x, const double *b);
+void orc_lu_free(orc_lu *F);
+
+/* GMG */
+enum { ORC_SMOOTH_JACOBI = 0, ORC_SMOOTH_MCGS = 1 };
+typedef struct {
+    int nlev, base, cycle, nu1, nu2, smoother;
+    double damp;
+    orc_crs *A;          /* per level */
+    orc_crs *P, *R;      /* per level (index = fine level) */
+    double **diaginv;
+    int **color;         /* multicolour GS: colour of each row */
+    int *ncolor;
+    double **sc, **sd, **st;
+    orc_lu lu;
+} orc_gmg;
+
+int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, double damp,
+                 int nu1, int nu2, int cycle, int base);
+void orc_gmg_apply(orc_gmg *G, double *c, const double *d);
+void orc_gmg_free(orc_gmg *G);
+
+/* Krylov with StdConvCheck(maxit, minDefect, relReduction) */
+typedef struct {
+    int maxit;
+    double min_defect, rel_red;
+    int steps;
+    double initial_defect, final_defect;
+    double *history;     /* optional, capacity hist_cap */
+    int hist_cap;
+    int converged;
+} orc_conv;
+
+int orc_cg(const orc_crs *A, orc_gmg *M, double *x, double *b, orc_conv *C);
+int orc_bicgstab(const orc_crs *A, orc_gmg *M, double *x, double *b, orc_conv *C);
+
+/* full forward problem helper used by the tests */
+typedef struct {
+    int elem_type, mx, my, mz, nref;
+    uint64_t seed;
+    int coef_kind;          /* 0: K=1, 1: K=exp(2g) lognormal field, 2: K=exp(m) per element given */
+    int coef_modes; double coef_kmax;
+    const double *m_top;    /* coef_kind 2: log-coefficient per top element */
+    int vel_kind;           /* 0: none, 1: curl field */
+    int vel_modes; double vel_kmax; double diffusion; double peclet;
+    int solver;             /* 0 CG, 1 BiCGStab */
+    int smoother; double damp; int nu1, nu2, cycle, base;
+    int maxit; double rel_red;
+    const double *f_top;    /* optional source override (nv top) */
+} orc_problem;
+
+/* coefficient per element on every level (coarse levels: mean of children's log K) */
+int orc_problem_coefficients(const orc_problem *P, const orc_hier *H, double **Klev);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

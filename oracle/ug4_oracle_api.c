@@ -1,0 +1,293 @@
+/*
+ * ug4_oracle_api.c -- oracle: flat problem-level API for the tests (ctypes).
+ *
+ * TEST INFRASTRUCTURE ONLY (see ug4_oracle.h).
+ *
+ * A "problem" bundles what a ugcore Lua script sets up for this path
+ * (util.solver.SolveLinearProblem, scripts/util/solver_util.lua:1182):
+ * domain hierarchy, DomainDiscretization with the FV1 convection-diffusion
+ * element disc and a zero DirichletBoundary, assemble_linear on the top
+ * level, GMG (re-assembled level operators, StdTransfer, Jacobi/GS, LU base),
+ * and a CG or BiCGStab solve from x = 0 with StdConvCheck.
+ * The adjoint part (no reference counterpart) solves A^T lambda = g with the
+ * same GMG on the transposed level operators (Dirichlet rows reset to
+ * identity) and forms dJ/d(log K) per element and dJ/d(f) per vertex.
+ */
+#include "ug4_oracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+int orc_grad_logk(const orc_level *L, const double *K, const double *u, const double *lam, double *g);
+
+typedef struct {
+    int elem_type, mx, my, mz, nref;
+    uint64_t seed;
+    int coef_kind;      /* 0: K=1, 1: exp(2g) field, 2: exp(m) given, 3: constant `diffusion` */
+    int coef_modes;
+    double coef_kmax;
+    int vel_kind;       /* 0: none, 1: curl of a random vector potential */
+    int vel_modes;
+    double vel_kmax, diffusion, peclet;
+    int solver;         /* 0: CG, 1: BiCGStab */
+    int smoother;       /* 0: Jacobi, 1: multicolour GS */
+    double damp;
+    int nu1, nu2, cycle, base;
+    int maxit;
+    double rel_red, min_defect;
+} orc_params;
+
+typedef struct {
+    orc_params p;
+    orc_hier H;
+    double **K;          /* per level per element */
+    orc_field vf;
+    int has_vf;
+    double *f;           /* top-level source */
+    orc_crs *A;          /* per level */
+    double *b;           /* top rhs */
+    orc_gmg G;
+    int gmg_ready;
+    orc_crs *AT;         /* transposed level operators (adjoint) */
+    orc_gmg GT;
+    int gmgT_ready;
+} orc_prob;
+
+static int assemble_all(orc_prob *P)
+{
+    int nl = P->H.nlev, top = nl - 1;
+    P->A = (orc_crs *)calloc((size_t)nl, sizeof(orc_crs));
+    P->b = (double *)calloc((size_t)P->H.lev[top].nv, sizeof(double));
+    for (int l = 0; l < nl; ++l) {
+        orc_disc D;
+        memset(&D, 0, sizeof(D));
+        D.K = P->K[l];
+        D.upwind = P->has_vf ? 1 : 0;
+        D.vfield = P->has_vf ? &P->vf : NULL;
+        D.f = (l == top) ? P->f : NULL;
+        D.dirichlet = 1;
+        if (orc_assemble(&P->H.lev[l], &D, &P->A[l], (l == top) ? P->b : NULL)) return -1;
+    }
+    return 0;
+}
+
+orc_prob *orc_prob_create(const orc_params *p, const double *m_top, const double *f_top)
+{
+    orc_prob *P = (orc_prob *)calloc(1, sizeof(orc_prob));
+    if (!P) return NULL;
+    P->p = *p;
+    if (orc_hier_create(&P->H, p->elem_type, p->mx, p->my, p->mz, p->nref)) { free(P); return NULL; }
+    int nl = P->H.nlev, top = nl - 1;
+    P->K = (double **)calloc((size_t)nl, sizeof(double *));
+    if (p->coef_kind == 3) {
+        for (int l = 0; l < nl; ++l) {
+            P->K[l] = (double *)malloc(sizeof(double) * (size_t)P->H.lev[l].ne);
+            for (int e = 0; e < P->H.lev[l].ne; ++e) P->K[l][e] = p->diffusion;
+        }
+    } else {
+        orc_problem pr;
+        memset(&pr, 0, sizeof(pr));
+        pr.seed = p->seed; pr.coef_kind = p->coef_kind; pr.coef_modes = p->coef_modes;
+        pr.coef_kmax = p->coef_kmax; pr.m_top = m_top;
+        orc_problem_coefficients(&pr, &P->H, P->K);
+    }
+    if (p->vel_kind == 1) {
+        orc_field_curl_init(&P->vf, p->vel_modes, p->vel_kmax, p->seed ^ 0x7E10C17ULL);
+        P->vf.scale *= p->peclet * 2.0 * p->diffusion * (double)(P->H.lev[top].nx - 1);
+        P->has_vf = 1;
+    }
+    int nv = P->H.lev[top].nv;
+    P->f = (double *)malloc(sizeof(double) * (size_t)nv);
+    if (f_top) memcpy(P->f, f_top, sizeof(double) * (size_t)nv);
+    else orc_source_uniform(p->seed, nv, P->f);
+    if (assemble_all(P)) return NULL;
+    return P;
+}
+
+int orc_prob_num_levels(const orc_prob *P) { return P->H.nlev; }
+int orc_prob_level_nv(const orc_prob *P, int l) { return P->H.lev[l].nv; }
+int orc_prob_level_ne(const orc_prob *P, int l) { return P->H.lev[l].ne; }
+int64_t orc_prob_level_nnz(const orc_prob *P, int l) { return P->A[l].nnz; }
+
+static void crs_out(const orc_crs *A, int *rowptr, int *col, double *val)
+{
+    if (rowptr) memcpy(rowptr, A->rowptr, sizeof(int) * ((size_t)A->n_rows + 1));
+    if (col) memcpy(col, A->col, sizeof(int) * (size_t)A->nnz);
+    if (val) memcpy(val, A->val, sizeof(double) * (size_t)A->nnz);
+}
+
+void orc_prob_level_matrix(const orc_prob *P, int l, int *rowptr, int *col, double *val)
+{
+    crs_out(&P->A[l], rowptr, col, val);
+}
+
+void orc_prob_level_coef(const orc_prob *P, int l, double *K)
+{
+    memcpy(K, P->K[l], sizeof(double) * (size_t)P->H.lev[l].ne);
+}
+
+void orc_prob_level_elems(const orc_prob *P, int l, int *elems, double *coords, unsigned char *bnd)
+{
+    const orc_level *L = &P->H.lev[l];
+    if (elems) memcpy(elems, L->elems, sizeof(int) * (size_t)L->ne * L->k);
+    if (coords) memcpy(coords, L->coords, sizeof(double) * (size_t)L->nv * L->dim);
+    if (bnd) memcpy(bnd, L->bnd, (size_t)L->nv);
+}
+
+void orc_prob_rhs(const orc_prob *P, double *b)
+{
+    memcpy(b, P->b, sizeof(double) * (size_t)P->H.lev[P->H.nlev - 1].nv);
+}
+
+void orc_prob_source(const orc_prob *P, double *f)
+{
+    memcpy(f, P->f, sizeof(double) * (size_t)P->H.lev[P->H.nlev - 1].nv);
+}
+
+static int ensure_gmg(orc_prob *P)
+{
+    if (P->gmg_ready) return 0;
+    const orc_params *p = &P->p;
+    int rc = orc_gmg_init(&P->G, &P->H, P->A, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base);
+    if (rc) return rc;
+    P->gmg_ready = 1;
+    return 0;
+}
+
+int64_t orc_prob_transfer_nnz(orc_prob *P, int l, int which)
+{
+    if (ensure_gmg(P)) return -1;
+    return which ? P->G.R[l].nnz : P->G.P[l].nnz;
+}
+
+void orc_prob_transfer(orc_prob *P, int l, int which, int *rowptr, int *col, double *val)
+{
+    if (ensure_gmg(P)) return;
+    crs_out(which ? &P->G.R[l] : &P->G.P[l], rowptr, col, val);
+}
+
+int orc_prob_apply_gmg(orc_prob *P, double *c, const double *d)
+{
+    if (ensure_gmg(P)) return -1;
+    orc_gmg_apply(&P->G, c, d);
+    return 0;
+}
+
+static int run_solver(const orc_params *p, const orc_crs *A, orc_gmg *G, double *x, double *rhs,
+                      int *steps, double *d0, double *d1, double *hist, int hist_cap)
+{
+    orc_conv C;
+    memset(&C, 0, sizeof(C));
+    C.maxit = p->maxit; C.min_defect = p->min_defect; C.rel_red = p->rel_red;
+    C.history = hist; C.hist_cap = hist_cap;
+    int ok = (p->solver == 0) ? orc_cg(A, G, x, rhs, &C) : orc_bicgstab(A, G, x, rhs, &C);
+    if (steps) *steps = C.steps;
+    if (d0) *d0 = C.initial_defect;
+    if (d1) *d1 = C.final_defect;
+    return ok ? 0 : 1;
+}
+
+/* forward solve from x = 0; returns 0 if converged */
+int orc_prob_solve(orc_prob *P, double *x, int *steps, double *d0, double *d1, double *hist, int hist_cap)
+{
+    if (ensure_gmg(P)) return -1;
+    int top = P->H.nlev - 1, nv = P->H.lev[top].nv;
+    double *rhs = (double *)malloc(sizeof(double) * (size_t)nv);
+    memcpy(rhs, P->b, sizeof(double) * (size_t)nv);
+    memset(x, 0, sizeof(double) * (size_t)nv);
+    int rc = run_solver(&P->p, &P->A[top], &P->G, x, rhs, steps, d0, d1, hist, hist_cap);
+    free(rhs);
+    return rc;
+}
+
+/* transposed operator with Dirichlet rows reset to identity */
+static int transpose_dirichlet(const orc_crs *A, const orc_level *L, orc_crs *T)
+{
+    if (orc_crs_transpose(A, 1, T)) return -1;
+    for (int v = 0; v < L->nv; ++v) {
+        if (!L->bnd[v]) continue;
+        for (int a = T->rowptr[v]; a < T->rowptr[v + 1]; ++a) T->val[a] = 0.0;
+        T->val[orc_crs_find(T, v, v)] = 1.0;
+    }
+    return 0;
+}
+
+int orc_prob_adjoint(orc_prob *P, const double *g, double *lam, int *steps, double *d0, double *d1)
+{
+    int nl = P->H.nlev, top = nl - 1, nv = P->H.lev[top].nv;
+    if (!P->gmgT_ready) {
+        P->AT = (orc_crs *)calloc((size_t)nl, sizeof(orc_crs));
+        for (int l = 0; l < nl; ++l)
+            if (transpose_dirichlet(&P->A[l], &P->H.lev[l], &P->AT[l])) return -1;
+        const orc_params *p = &P->p;
+        int rc = orc_gmg_init(&P->GT, &P->H, P->AT, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base);
+        if (rc) return rc;
+        P->gmgT_ready = 1;
+    }
+    double *rhs = (double *)malloc(sizeof(double) * (size_t)nv);
+    for (int i = 0; i < nv; ++i) rhs[i] = P->H.lev[top].bnd[i] ? 0.0 : g[i];
+    memset(lam, 0, sizeof(double) * (size_t)nv);
+    int rc = run_solver(&P->p, &P->AT[top], &P->GT, lam, rhs, steps, d0, d1, NULL, 0);
+    free(rhs);
+    return rc;
+}
+
+void orc_prob_grad_logk(const orc_prob *P, const double *u, const double *lam, double *grad)
+{
+    int top = P->H.nlev - 1;
+    orc_grad_logk(&P->H.lev[top], P->K[top], u, lam, grad);
+}
+
+void orc_prob_grad_source(const orc_prob *P, const double *lam, double *grad)
+{
+    int top = P->H.nlev - 1;
+    const orc_level *L = &P->H.lev[top];
+    orc_scv_volume_sum(L, grad);
+    for (int i = 0; i < L->nv; ++i) grad[i] = L->bnd[i] ? 0.0 : grad[i] * lam[i];
+}
+
+void orc_prob_free(orc_prob *P)
+{
+    if (!P) return;
+    int nl = P->H.nlev;
+    if (P->gmg_ready) orc_gmg_free(&P->G);
+    if (P->gmgT_ready) orc_gmg_free(&P->GT);
+    for (int l = 0; l < nl; ++l) {
+        if (P->A) orc_crs_free(&P->A[l]);
+        if (P->AT) orc_crs_free(&P->AT[l]);
+        if (P->K) free(P->K[l]);
+    }
+    free(P->A); free(P->AT); free(P->K); free(P->b); free(P->f);
+    if (P->has_vf) orc_field_free(&P->vf);
+    orc_hier_free(&P->H);
+    free(P);
+}
+
+/* standalone transpose on caller CRS arrays (pins set_as_transpose_of[2]) */
+int64_t orc_transpose_nnz(int n_rows, int n_cols, const int *rowptr, const int *col, const double *val,
+                          int keep_zeros)
+{
+    orc_crs B = {n_rows, n_cols, rowptr[n_rows], (int *)rowptr, (int *)col, (double *)val};
+    orc_crs T;
+    if (orc_crs_transpose(&B, keep_zeros, &T)) return -1;
+    int64_t nnz = T.nnz;
+    orc_crs_free(&T);
+    return nnz;
+}
+
+/* FV1 geometry of one element (for geometry unit tests) */
+int orc_geometry(int elem_type, const double *corner, double *normals, double *vols, double *grads,
+                 int *from, int *to)
+{
+    orc_fv1geom G;
+    orc_fv1_geometry(elem_type, corner, &G);
+    int dim = (elem_type == ORC_QUAD) ? 2 : 3;
+    for (int i = 0; i < G.nscvf; ++i) {
+        from[i] = G.from[i]; to[i] = G.to[i];
+        for (int d = 0; d < dim; ++d) normals[i * dim + d] = G.normal[i][d];
+        for (int s = 0; s < G.nscv; ++s)
+            for (int d = 0; d < dim; ++d) grads[(i * G.nscv + s) * dim + d] = G.grad[i][s][d];
+    }
+    for (int s = 0; s < G.nscv; ++s) vols[s] = G.vol[s];
+    return G.nscvf;
+}
