@@ -1,0 +1,224 @@
+/*
+ * ug4gb.h -- C ABI of libug4gb, the GB300 (sm_103a) assemble-and-solve engine
+ * for UG4/ugcore's FV1 + geometric-multigrid + Krylov hot path.
+ *
+ * Conventions
+ *   - Every function returns an int status: UG4GB_OK (0) or a negative error
+ *     code; ug4gb_last_error(ctx) returns the message of the last failure.
+ *     No C++ exception crosses this boundary.
+ *   - Array arguments may be host or device pointers (the library detects
+ *     which); the caller owns them.  The library owns all device memory of a
+ *     handle and frees it in the matching *_destroy.
+ *   - One CUDA stream per context; calls on one context are not thread-safe
+ *     (ugcore's hot path is single-threaded per process).
+ *   - Indices are 0-based 32-bit ints; DoF numbering is lexicographic per
+ *     level (i + nx*(j + ny*k)).
+ * Each entry point names the ugcore interface it stands in for
+ * (paths relative to ugcore's ugbase/).
+ */
+#ifndef UG4GB_H
+#define UG4GB_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define UG4GB_API __attribute__((visibility("default")))
+#else
+#define UG4GB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UG4GB_OK 0
+#define UG4GB_ERR_INVALID (-1)      /* bad argument / handle */
+#define UG4GB_ERR_CUDA (-2)         /* a CUDA runtime call failed */
+#define UG4GB_ERR_NOMEM (-3)        /* device allocation failed */
+#define UG4GB_ERR_SINGULAR (-4)     /* base-level LU found a pivot < 1e-10 */
+#define UG4GB_ERR_NOT_CONVERGED (-5)/* Krylov solver stopped without convergence */
+#define UG4GB_ERR_BREAKDOWN (-6)    /* CG lambda == 0 / BiCGStab rho, alpha, tt, omega == 0 */
+#define UG4GB_ERR_STATE (-7)        /* call order (e.g. apply before init) */
+
+/* element types of a grid hierarchy */
+#define UG4GB_QUAD 0                /* 2D quadrilaterals (ROID_QUADRILATERAL) */
+#define UG4GB_HEX 1                 /* 3D hexahedra (ROID_HEXAHEDRON) */
+#define UG4GB_TET 2                 /* 3D tetrahedra, 6 per hex, Kuhn split */
+
+/* smoothers, precisions, solvers */
+#define UG4GB_SMOOTHER_JACOBI 0     /* damped Jacobi (lib_algebra/operator/preconditioner/jacobi.h:90) */
+#define UG4GB_SMOOTHER_MCGS 1       /* multicolour Gauss-Seidel (opt-in; no ugcore counterpart) */
+#define UG4GB_PREC_FP64 0           /* whole preconditioner in FP64 */
+#define UG4GB_PREC_MIXED 1          /* FP32 smoother/transfers/SpMV, FP64 outer Krylov and base LU */
+#define UG4GB_SOLVER_CG 0           /* lib_algebra/operator/linear_solver/cg.h:59 */
+#define UG4GB_SOLVER_BICGSTAB 1     /* lib_algebra/operator/linear_solver/bicgstab.h:59 */
+#define UG4GB_UPWIND_NONE 0
+#define UG4GB_UPWIND_FULL 1         /* ConvectionShapesFullUpwind (lib_disc/spatial_disc/disc_util/conv_shape.h:277) */
+
+typedef struct ug4gb_ctx ug4gb_ctx;
+typedef struct ug4gb_grid ug4gb_grid;
+typedef struct ug4gb_vector ug4gb_vector;
+typedef struct ug4gb_matrix ug4gb_matrix;
+typedef struct ug4gb_disc ug4gb_disc;
+typedef struct ug4gb_gmg ug4gb_gmg;
+typedef struct ug4gb_solver ug4gb_solver;
+
+/* ------------------------------------------------------------- context -- */
+/* Replaces the process-level setup of ugcore (ug::UGInit, ug.cpp) for one GPU. */
+UG4GB_API int ug4gb_create(int device, ug4gb_ctx **out);
+UG4GB_API void ug4gb_destroy(ug4gb_ctx *ctx);
+UG4GB_API const char *ug4gb_last_error(const ug4gb_ctx *ctx);
+UG4GB_API int ug4gb_synchronize(ug4gb_ctx *ctx);
+/* the context's cudaStream_t, for callers that order their own work on it */
+UG4GB_API void *ug4gb_stream(ug4gb_ctx *ctx);
+/* number of kernels this context has launched so far (instrumentation) */
+UG4GB_API int64_t ug4gb_kernel_launches(const ug4gb_ctx *ctx);
+
+/* ------------------------------------------------------ grid hierarchy -- */
+/* Replaces MultiGrid + GlobalMultiGridRefiner::perform_refinement
+   (lib_grid/refinement/global_multi_grid_refiner.cpp:135) and the level
+   DoFDistribution (lib_disc/dof_manager/dof_distribution.cpp:1339) for
+   structured boxes: the unit square/cube split into mx*my(*mz) coarse cells,
+   refined num_refinements times. */
+UG4GB_API int ug4gb_grid_create_structured(ug4gb_ctx *ctx, int elem_type, int mx, int my, int mz,
+                                 int num_refinements, ug4gb_grid **out);
+UG4GB_API int ug4gb_grid_num_levels(const ug4gb_grid *g);
+UG4GB_API int ug4gb_grid_level_info(const ug4gb_grid *g, int level, int *num_vertices, int *num_elements,
+                          int *corners_per_element, int *dim);
+/* copies level geometry out (any pointer may be NULL) */
+UG4GB_API int ug4gb_grid_level_export(const ug4gb_grid *g, int level, double *coords, int *elems,
+                            unsigned char *boundary);
+UG4GB_API void ug4gb_grid_destroy(ug4gb_grid *g);
+
+/* ------------------------------------------------------------- vectors -- */
+/* Replaces ug::Vector<double> (lib_algebra/cpu_algebra/vector.h:54). */
+UG4GB_API int ug4gb_vector_create(ug4gb_ctx *ctx, int n, ug4gb_vector **out);
+/* non-owning view of caller device memory (e.g. a torch tensor) */
+UG4GB_API int ug4gb_vector_wrap(ug4gb_ctx *ctx, double *device_ptr, int n, ug4gb_vector **out);
+UG4GB_API int ug4gb_vector_size(const ug4gb_vector *v);
+UG4GB_API double *ug4gb_vector_data(ug4gb_vector *v);
+UG4GB_API int ug4gb_vector_set(ug4gb_vector *v, double value);                  /* vector.h set */
+UG4GB_API int ug4gb_vector_copy_from(ug4gb_vector *v, const double *src);       /* host or device */
+UG4GB_API int ug4gb_vector_copy_to(const ug4gb_vector *v, double *dst);         /* host or device */
+UG4GB_API int ug4gb_vector_norm(const ug4gb_vector *v, double *out);            /* vector_impl.h:323 */
+UG4GB_API int ug4gb_vector_dot(const ug4gb_vector *a, const ug4gb_vector *b, double *out); /* vector_impl.h:72 */
+/* dest = alpha*a + beta*b (VecScaleAdd, lib_algebra/cpu_algebra/operations_vec.h:55) */
+UG4GB_API int ug4gb_vector_scale_add(ug4gb_vector *dest, double alpha, const ug4gb_vector *a, double beta,
+                           const ug4gb_vector *b);
+UG4GB_API void ug4gb_vector_destroy(ug4gb_vector *v);
+
+/* ------------------------------------------------------------ matrices -- */
+/* Replaces ug::SparseMatrix<double> (lib_algebra/cpu_algebra/sparsematrix.h:98)
+   in its defragmented CRS form (columns sorted per row). */
+UG4GB_API int ug4gb_matrix_create(ug4gb_ctx *ctx, ug4gb_matrix **out);
+UG4GB_API int ug4gb_matrix_set_csr(ug4gb_matrix *A, int num_rows, int num_cols, int64_t nnz, const int *rowptr,
+                         const int *col, const double *val);
+UG4GB_API int ug4gb_matrix_info(const ug4gb_matrix *A, int *num_rows, int *num_cols, int64_t *nnz);
+UG4GB_API int ug4gb_matrix_export_csr(const ug4gb_matrix *A, int *rowptr, int *col, double *val);
+/* dest = alpha1*v1 + beta1*A*w1 (SparseMatrix::axpy, sparsematrix_impl.h:294) */
+UG4GB_API int ug4gb_matrix_axpy(const ug4gb_matrix *A, ug4gb_vector *dest, double alpha1, const ug4gb_vector *v1,
+                      double beta1, const ug4gb_vector *w1);
+/* dest = alpha1*v1 + beta1*A^T*w1 (SparseMatrix::axpy_transposed, sparsematrix_impl.h:344) */
+UG4GB_API int ug4gb_matrix_axpy_transposed(const ug4gb_matrix *A, ug4gb_vector *dest, double alpha1,
+                                 const ug4gb_vector *v1, double beta1, const ug4gb_vector *w1);
+/* T = B^T; keep_zeros=1 as set_as_transpose_of, 0 as set_as_transpose_of2
+   (sparsematrix_impl.h:149,186) */
+UG4GB_API int ug4gb_matrix_set_as_transpose_of(ug4gb_matrix *T, const ug4gb_matrix *B, int keep_zeros);
+UG4GB_API void ug4gb_matrix_destroy(ug4gb_matrix *A);
+
+/* ------------------------------------------------------ discretisation -- */
+/* Replaces DomainDiscretization (lib_disc/spatial_disc/domain_disc.h) with one
+   FV1 convection-diffusion IElemDisc (elem_disc_interface.h:797; the
+   ConvectionDiffusionFV1 plugin) and a zero DirichletBoundary on the whole
+   boundary (lagrange_dirichlet_boundary_impl.h:754-870). */
+UG4GB_API int ug4gb_disc_create(ug4gb_ctx *ctx, const ug4gb_grid *g, ug4gb_disc **out);
+UG4GB_API int ug4gb_disc_set_diffusion_constant(ug4gb_disc *d, double K);
+/* K = exp(factor * g(centroid)), g(x) = amp * sum_m cos(k_m . x + phase_m)
+   (LognormalRandomField::eval_K form, lognormal_random_field_impl.h);
+   k: nmodes*dim wavevectors, evaluated on every level */
+UG4GB_API int ug4gb_disc_set_diffusion_fourier(ug4gb_disc *d, int nmodes, const double *k, const double *phase,
+                                     double amp, double factor);
+/* K = exp(m) per top-level element; coarse levels use the children's mean m */
+UG4GB_API int ug4gb_disc_set_log_diffusion_elements(ug4gb_disc *d, const double *m_top);
+/* v(x) = scale * sum_m -sin(k_m . x + phase_m) c_m (3D), evaluated at SCVF ips */
+UG4GB_API int ug4gb_disc_set_velocity_fourier_curl(ug4gb_disc *d, int nmodes, const double *k, const double *c,
+                                         const double *phase, double scale);
+UG4GB_API int ug4gb_disc_set_upwind(ug4gb_disc *d, int upwind);
+/* f per top-level vertex (host or device array) */
+UG4GB_API int ug4gb_disc_set_source_vertices(ug4gb_disc *d, const double *f_top);
+/* f_i = 2*u(seed,i) - 1, u = splitmix64 counter hash (seeded synthetic source) */
+UG4GB_API int ug4gb_disc_set_source_uniform(ug4gb_disc *d, uint64_t seed);
+/* DomainDiscretizationBase::assemble_linear (domain_disc_impl.h:837) */
+UG4GB_API int ug4gb_disc_assemble_linear(ug4gb_disc *d, int level, ug4gb_matrix *A, ug4gb_vector *b);
+/* DomainDiscretizationBase::assemble_jacobian (domain_disc_impl.h:471) */
+UG4GB_API int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matrix *A);
+/* AT = A^T with the Dirichlet rows of `level` reset to identity: the operator
+   of the adjoint (transposed) solve.  No ugcore counterpart (ugcore has
+   SparseMatrix::set_as_transpose_of, sparsematrix_impl.h:149, and
+   SetDirichletRow, sparsematrix_util.h:850, but no adjoint). */
+UG4GB_API int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A, ug4gb_matrix *AT);
+/* element coefficient K of a level (host or device out array, num_elements) */
+UG4GB_API int ug4gb_disc_export_coefficients(ug4gb_disc *d, int level, double *K);
+UG4GB_API void ug4gb_disc_destroy(ug4gb_disc *d);
+
+/* ----------------------------------------------------------------- GMG -- */
+/* Replaces AssembledMultiGridCycle (lib_disc/operator/linear_operator/
+   multi_grid_solver/mg_solver.h:82) with StdTransfer (std_transfer.h:57),
+   Jacobi smoothing and an LU base solver (lu.h:50).  Defaults follow the
+   constructor (mg_solver_impl.hpp:78): V-cycle, 2/2 smoothing steps, base
+   level 0; Jacobi damping 0.6 as in the configured scripts. */
+UG4GB_API int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out);
+UG4GB_API int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp);            /* set_smoother */
+UG4GB_API int ug4gb_gmg_set_cycle_type(ug4gb_gmg *m, int cycle);                      /* 1 = V, 2 = W */
+UG4GB_API int ug4gb_gmg_set_num_presmooth(ug4gb_gmg *m, int n);
+UG4GB_API int ug4gb_gmg_set_num_postsmooth(ug4gb_gmg *m, int n);
+UG4GB_API int ug4gb_gmg_set_base_level(ug4gb_gmg *m, int level);
+UG4GB_API int ug4gb_gmg_set_precision(ug4gb_gmg *m, int precision);
+/* transposed = 1 builds the cycle on A^T of every level (Dirichlet rows reset
+   to identity): the preconditioner of the adjoint solve */
+UG4GB_API int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed);
+/* AssembledMultiGridCycle::init (mg_solver_impl.hpp:380): copies the top
+   operator, re-assembles coarser levels, builds P/R, smoothers and the LU */
+UG4GB_API int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top);
+/* c = B d (AssembledMultiGridCycle::apply, mg_solver_impl.hpp:176) */
+UG4GB_API int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *c, const ug4gb_vector *d);
+/* transfer operators of fine level `level`: which = 0 P, 1 R */
+UG4GB_API int ug4gb_gmg_transfer_info(const ug4gb_gmg *m, int level, int which, int *num_rows, int *num_cols,
+                            int64_t *nnz);
+UG4GB_API int ug4gb_gmg_export_transfer(const ug4gb_gmg *m, int level, int which, int *rowptr, int *col, double *val);
+UG4GB_API void ug4gb_gmg_destroy(ug4gb_gmg *m);
+
+/* ------------------------------------------------------------- Krylov -- */
+/* Replaces CG / BiCGStab with StdConvCheck (convergence_check_impl.h:85-172) */
+UG4GB_API int ug4gb_solver_create(ug4gb_ctx *ctx, int kind, ug4gb_solver **out);
+UG4GB_API int ug4gb_solver_set_preconditioner(ug4gb_solver *s, ug4gb_gmg *m);
+UG4GB_API int ug4gb_solver_set_convergence_check(ug4gb_solver *s, int max_steps, double min_defect,
+                                       double rel_reduction);
+/* ILinearOperatorInverse::init (preconditioned_linear_operator_inverse.h:123) */
+UG4GB_API int ug4gb_solver_init(ug4gb_solver *s, const ug4gb_matrix *A);
+/* apply_return_defect (cg.h:103, bicgstab.h:112): x is the start iterate and
+   the result, b is overwritten by the final defect */
+UG4GB_API int ug4gb_solver_apply_return_defect(ug4gb_solver *s, ug4gb_vector *x, ug4gb_vector *b);
+/* apply (preconditioned_linear_operator_inverse.h:150): b is kept */
+UG4GB_API int ug4gb_solver_apply(ug4gb_solver *s, ug4gb_vector *x, const ug4gb_vector *b);
+/* host-buffer solve: copies b in, solves from x = 0, copies x out */
+UG4GB_API int ug4gb_solver_solve_host(ug4gb_solver *s, const double *b_host, double *x_host);
+UG4GB_API int ug4gb_solver_get_stats(const ug4gb_solver *s, int *steps, double *initial_defect,
+                           double *final_defect, int *converged);
+/* defect history: hist[0] = initial defect, hist[i] = defect after step i */
+UG4GB_API int ug4gb_solver_get_history(const ug4gb_solver *s, double *hist, int capacity);
+UG4GB_API void ug4gb_solver_destroy(ug4gb_solver *s);
+
+/* ------------------------------------------------------------ adjoint -- */
+/* No ugcore counterpart.  Gradients of J(u) with A(m) u = b(f), K = exp(m):
+   dJ/dm_e = -K_e * sum_{i not Dirichlet} lambda_i (A1_e u_e)_i   (per element)
+   dJ/df_i = lambda_i * |SCV(i)|                                  (per vertex)
+   where A^T lambda = dJ/du, A1_e the unit-coefficient element matrix.
+   u, lambda: top-level vectors; grad: host or device array. */
+UG4GB_API int ug4gb_disc_grad_logk(ug4gb_disc *d, const ug4gb_vector *u, const ug4gb_vector *lambda, double *grad);
+UG4GB_API int ug4gb_disc_grad_source(ug4gb_disc *d, const ug4gb_vector *lambda, double *grad);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -30,7 +30,15 @@ class Params(C.Structure):
 
 
 def build():
-    """Compile liboracle.so in place (plain C, seconds)."""
+    """Compile liboracle.so in place (plain C, seconds); a library left from
+    another host architecture is rebuilt."""
+    import platform
+    stamp = os.path.join(_HERE, ".build_arch")
+    arch = platform.machine()
+    if not os.path.exists(stamp) or open(stamp).read().strip() != arch:
+        subprocess.check_call(["make", "-s", "-C", _HERE, "clean"])
+        with open(stamp, "w") as fh:
+            fh.write(arch)
     subprocess.check_call(["make", "-s", "-C", _HERE, "liboracle.so"])
 
 

@@ -275,6 +275,22 @@ int64_t orc_transpose_nnz(int n_rows, int n_cols, const int *rowptr, const int *
     return nnz;
 }
 
+/* parameters of the seeded fields (kind 0 scalar, 1 curl); for the tests that
+   pin the product's host-side generator to the oracle's */
+int orc_field_params(int kind, int dim, int nmodes, double kmax, uint64_t seed, double *k, double *phase, double *c,
+                     double *amp_scale)
+{
+    orc_field F;
+    if (kind == 0) orc_field_scalar_init(&F, dim, nmodes, kmax, seed);
+    else orc_field_curl_init(&F, nmodes, kmax, seed);
+    memcpy(k, F.k, sizeof(double) * (size_t)nmodes * F.dim);
+    memcpy(phase, F.phase, sizeof(double) * (size_t)nmodes);
+    if (kind == 1) memcpy(c, F.a, sizeof(double) * (size_t)nmodes * 3);
+    *amp_scale = (kind == 0) ? F.amp : F.scale;
+    orc_field_free(&F);
+    return 0;
+}
+
 /* FV1 geometry of one element (for geometry unit tests) */
 int orc_geometry(int elem_type, const double *corner, double *normals, double *vols, double *grads,
                  int *from, int *to)

@@ -1,0 +1,34 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built libug4gb.so")
+    config.addinivalue_line("markers", "slow: full-size configurations")
+
+
+@pytest.fixture(scope="session")
+def oracle_lib():
+    from oracle import oracle as orc
+    orc.build()
+    return orc
+
+
+@pytest.fixture(scope="session")
+def built_lib():
+    from ugcore_gb300 import build
+    return build.build()
+
+
+@pytest.fixture(scope="session")
+def ctx(built_lib):
+    import ugcore_gb300 as ug
+    c = ug.Context(0)
+    yield c
+    c.close()

@@ -1,0 +1,49 @@
+"""Shared helpers of the parity tests: map a problems.py configuration onto
+the oracle's parameters, compare CRS matrices, read golden fixtures."""
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# Tolerances stated by the benchmark spec for this path:
+#   CRS row pointers / column indices: bit-exact
+#   matrix values: 1e-13 relative in FP64 (relative to the largest |a_ij| of
+#     the row, so that entries that cancel to ~0 are judged against the row)
+#   solution: 1e-10 relative residual, iteration count within +-1
+VAL_RTOL = 1e-13
+
+
+def oracle_params(orc, cfg):
+    et = {"quad": orc.ORC_QUAD, "hex": orc.ORC_HEX, "tet": orc.ORC_TET}[cfg["elem"]]
+    if cfg["coef"] == "const":
+        ck = 0 if (cfg["diffusion"] == 1.0) else 3
+    else:
+        ck = {"lognormal": 1, "logk": 2}[cfg["coef"]]
+    return orc.make_params(
+        elem_type=et, mx=cfg["mx"], my=cfg["my"], mz=cfg["mz"], nref=cfg["nref"], seed=cfg["seed"], coef_kind=ck,
+        coef_modes=cfg["coef_modes"], coef_kmax=cfg["coef_kmax"], vel_kind=1 if cfg["vel"] else 0,
+        vel_modes=cfg["vel_modes"], vel_kmax=cfg["vel_kmax"], diffusion=cfg["diffusion"], peclet=cfg["peclet"],
+        solver=0 if cfg["solver"] == "cg" else 1, smoother=0 if cfg["smoother"] == "jacobi" else 1,
+        damp=cfg["damp"], nu1=cfg["nu1"], nu2=cfg["nu2"], cycle=cfg["cycle"], base=cfg["base"], maxit=cfg["maxit"],
+        rel_red=cfg["rel_red"], min_defect=cfg["min_defect"])
+
+
+def assert_crs_equal(a, b, rtol=VAL_RTOL, what="matrix"):
+    """a, b = (rowptr, col, val); pattern bit-exact, values row-relative."""
+    rpa, cia, vaa = a
+    rpb, cib, vab = b
+    assert np.array_equal(rpa, rpb), what + ": row pointers differ"
+    assert np.array_equal(cia, cib), what + ": column indices differ"
+    n = len(rpa) - 1
+    rowmax = np.maximum.reduceat(np.abs(vab), rpb[:-1]) if len(vab) else np.zeros(n)
+    scale = np.repeat(rowmax, np.diff(rpb))
+    err = np.abs(vaa - vab)
+    bad = err > rtol * np.maximum(scale, 1e-300)
+    assert not bad.any(), "%s: %d values beyond %.0e (max rel %.3e)" % (
+        what, int(bad.sum()), rtol, float((err / np.maximum(scale, 1e-300)).max()))
+
+
+def load_golden(name):
+    path = os.path.join(GOLDEN, name + ".npz")
+    return dict(np.load(path)) if os.path.exists(path) else None

@@ -1,0 +1,177 @@
+"""GPU parity: the CUDA path against the oracle and against fixtures from
+ugcore's own algebra, at sizes the oracle finishes in seconds.
+
+Bars (stated by the benchmark spec for this path):
+  CRS row pointers / columns bit-exact; matrix values 1e-13 relative (to the
+  row's largest entry); transfers P, R bit-exact (their weights are exact);
+  FP64 GMG application 1e-12 relative; solve: same iteration count +-1 and
+  the GPU solution's relative residual < 1e-10 (plus the difference to the
+  oracle solution stated per case); mixed precision: relative residual
+  < 1e-10 in FP64 and error against the FP64 oracle solution reported.
+"""
+import numpy as np
+import pytest
+
+from helpers import assert_crs_equal, load_golden, oracle_params
+
+pytestmark = pytest.mark.gpu
+
+SMALL = [
+    ("c0", dict(nref=5)),
+    ("c1", dict(nref=3)),
+    ("c2", dict(nref=2, precision="fp64")),
+    ("c3", dict(nref=4)),
+    ("c4", dict(nref=2, precision="fp64")),
+]
+
+
+def _problem(ctx, name, over):
+    from ugcore_gb300 import problems
+    cfg = problems.config(name, **over)
+    return cfg, problems.Problem(ctx, cfg)
+
+
+def _oracle(orc, cfg, p):
+    return orc.Problem(oracle_params(orc, cfg), m_top=getattr(p, "m_top", None))
+
+
+def _rel_residual(p, x):
+    import ugcore_gb300 as ug
+    r = ug.GPUVector(p.ctx, p.n)
+    xv = ug.GPUVector(p.ctx, p.n).copy_from(x)
+    p.A.axpy(r, 1.0, p.b, -1.0, xv)
+    return r.norm() / p.b.norm()
+
+
+@pytest.mark.parametrize("name,over", SMALL)
+def test_assembly_matches_oracle(ctx, oracle_lib, name, over):
+    cfg, p = _problem(ctx, name, over)
+    op = _oracle(oracle_lib, cfg, p)
+    assert_crs_equal(p.A.export_csr(), op.matrix(), what="top operator")
+    b = p.b.numpy()
+    ob = op.rhs()
+    assert np.abs(b - ob).max() <= 1e-13 * np.abs(ob).max()
+
+
+@pytest.mark.parametrize("name,over", SMALL)
+def test_transfers_match_oracle(ctx, oracle_lib, name, over):
+    cfg, p = _problem(ctx, name, over)
+    op = _oracle(oracle_lib, cfg, p)
+    for l in range(1, p.hier.num_levels):
+        for which in (0, 1):
+            assert_crs_equal(p.gmg.transfer(l, which), op.transfer(l, which), rtol=0.0,
+                             what="%s level %d" % ("PR"[which], l))
+
+
+@pytest.mark.parametrize("name,over", SMALL)
+def test_gmg_apply_matches_oracle(ctx, oracle_lib, name, over):
+    import ugcore_gb300 as ug
+    cfg, p = _problem(ctx, name, over)
+    op = _oracle(oracle_lib, cfg, p)
+    d = np.random.default_rng(0).standard_normal(p.n)
+    _, _, bnd = p.hier.export()
+    d[bnd.astype(bool)] = 0.0
+    c_ref = op.apply_gmg(d)
+    dv = ug.GPUVector(ctx, p.n).copy_from(d)
+    cv = ug.GPUVector(ctx, p.n)
+    p.gmg.apply(cv, dv)
+    err = np.abs(cv.numpy() - c_ref).max() / np.abs(c_ref).max()
+    assert err < 1e-12, err
+
+
+@pytest.mark.parametrize("name,over", SMALL)
+def test_solve_matches_oracle(ctx, oracle_lib, name, over):
+    cfg, p = _problem(ctx, name, over)
+    st = p.solve()
+    op = _oracle(oracle_lib, cfg, p)
+    ref = op.solve(hist_cap=400)
+    assert st["converged"]
+    assert abs(st["steps"] - ref["steps"]) <= 1, (st["steps"], ref["steps"])
+    x = p.x.numpy()
+    assert _rel_residual(p, x) < 1e-10
+    assert np.abs(x - ref["x"]).max() <= 1e-8 * np.abs(ref["x"]).max()
+    h = p.solver.history()
+    n = min(len(h), len(ref["history"]))
+    assert np.allclose(h[:n], ref["history"][:n], rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("name,over", [("c1", dict(nref=3, precision="mixed")),
+                                       ("c2", dict(nref=2)),
+                                       ("c4", dict(nref=2))])
+def test_mixed_precision_converges_to_fp64_oracle(ctx, oracle_lib, name, over):
+    cfg, p = _problem(ctx, name, over)
+    assert cfg["precision"] == "mixed"
+    st = p.solve()
+    ref = _oracle(oracle_lib, cfg, p).solve()
+    x = p.x.numpy()
+    assert st["converged"] and _rel_residual(p, x) < 1e-10
+    # the FP32 preconditioner changes iterates, not the converged solution
+    err = np.abs(x - ref["x"]).max() / np.abs(ref["x"]).max()
+    assert err < 1e-7, err
+    assert st["steps"] <= ref["steps"] + 3
+
+
+def test_mcgs_smoother_matches_oracle(ctx, oracle_lib):
+    cfg, p = _problem(ctx, "c1", dict(nref=3, smoother="mcgs", damp=1.0))
+    st = p.solve()
+    op = _oracle(oracle_lib, cfg, p)
+    ref = op.solve()
+    assert abs(st["steps"] - ref["steps"]) <= 1
+    assert np.abs(p.x.numpy() - ref["x"]).max() <= 1e-8 * np.abs(ref["x"]).max()
+
+
+@pytest.mark.parametrize("name", ["quad_2x2_r4", "hex_2x2x2_r2", "tet_4x4x4_r1_lognormal", "hex_3x3x3_r1_convection"])
+def test_gpu_against_ugcore_algebra_golden(ctx, name):
+    """fixtures written by ugcore's own SparseMatrix/Jacobi/LU/CG/BiCGStab"""
+    from ugcore_gb300 import problems
+    g = load_golden(name)
+    e, mx, my, mz, nref, seed, ck, solver, vk, diff, pe = g["params"]
+    cfg = problems.config("golden", elem=["quad", "hex", "tet"][int(e)], mx=int(mx), my=int(my), mz=int(mz),
+                          nref=int(nref), seed=int(seed),
+                          coef={0: "const", 1: "lognormal", 3: "const"}[int(ck)], diffusion=diff,
+                          vel="curl" if vk else None, solver="cg" if solver == 0 else "bicgstab", peclet=pe)
+    p = problems.Problem(ctx, cfg)
+    nl = int(g["nlev"])
+    assert_crs_equal(p.A.export_csr(), (g["A%d_rowptr" % (nl - 1)], g["A%d_col" % (nl - 1)],
+                                        g["A%d_val" % (nl - 1)]), what="top operator vs ugcore")
+    assert_crs_equal(p.gmg.transfer(nl - 1, 0), (g["P_rowptr"], g["P_col"], g["P_val"]), rtol=0.0, what="P")
+    assert_crs_equal(p.gmg.transfer(nl - 1, 1), (g["R_rowptr"], g["R_col"], g["R_val"]), rtol=0.0, what="R")
+    st = p.solve()
+    assert abs(st["steps"] - int(g["steps"])) <= 1
+    x = p.x.numpy()
+    assert np.abs(x - g["x"]).max() <= 1e-8 * np.abs(g["x"]).max()
+
+
+def test_edge_cases(ctx):
+    """zero rhs (converged at step 0), single-level hierarchy (base == top),
+    W-cycle, no pre-smoothing, base level above 0"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    cfg = problems.config("c0", nref=3)
+    p = problems.Problem(ctx, cfg)
+    p.b.set(0.0)
+    st = p.solve()
+    assert st["steps"] == 0 and np.all(p.x.numpy() == 0.0)
+    for over in [dict(nref=0), dict(nref=4, cycle=2), dict(nref=4, nu1=0), dict(nref=4, base=2),
+                 dict(nref=4, nu1=1, nu2=3)]:
+        cfg = problems.config("c0", **over)
+        p = problems.Problem(ctx, cfg)
+        st = p.solve()
+        assert st["converged"], over
+        assert _rel_residual(p, p.x.numpy()) < 1e-10
+
+
+def test_error_reporting(ctx):
+    import ugcore_gb300 as ug
+    with pytest.raises(ug.UG4GBError):
+        ug.StructuredHierarchy(ctx, "hex", 0, 1, 1, 1)
+    from ugcore_gb300 import problems
+    p = problems.Problem(ctx, problems.config("c0", nref=3, maxit=2))
+    with pytest.raises(ug.UG4GBError) as ei:
+        p.solve()
+    assert ei.value.code == -5
+    g = ug.GeometricMultiGrid(p.disc)
+    c = ug.GPUVector(ctx, p.n)
+    with pytest.raises(ug.UG4GBError) as ei:
+        g.apply(c, p.b)
+    assert ei.value.code == -7

@@ -1,0 +1,226 @@
+"""Pins the CPU oracle: against ugcore's own golden data (the transpose test
+log) and against fixtures produced by ugcore's own algebra (tests/golden),
+plus geometry and generator properties.  CPU only."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, assert_crs_equal, load_golden, oracle_params
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+# ---- ugcore tests/sm_transpose.cc + tests/ref/sm_transpose.out -------------
+def _sm_test0(N, M):
+    """matrix of test0() (tests/sm_transpose.cc:77-95)"""
+    ent = {}
+    for i in range(1, min(N, M)):
+        ent[(i, i)] = 2.0
+        ent[(i, i - 1)] = 1.0
+        ent[(i - 1, i)] = 1.0
+    if N > 6 and M > 6:
+        ent[(5, 5)] = 0.0
+        ent[(5, 0)] = 0.0
+        ent[(1, 6)] = 1.0
+    return ent, N, M
+
+
+def _sm_test3(N):
+    """matrix of test3() (tests/sm_transpose.cc:118-131)"""
+    return {(i, j): float(i + j) for i in range(N) for j in range(N)}, N, N
+
+
+def _to_crs(ent, N):
+    rows = [[] for _ in range(N)]
+    for (i, j), v in ent.items():
+        rows[i].append((j, v))
+    rp, ci, va = [0], [], []
+    for r in rows:
+        for j, v in sorted(r):
+            ci.append(j)
+            va.append(v)
+        rp.append(len(ci))
+    return np.array(rp, np.int32), np.array(ci, np.int32), np.array(va)
+
+
+# (matrix, nnz of set_as_transpose_of, nnz of set_as_transpose_of2) from
+# tests/ref/sm_transpose.out:1-30
+SM_GOLDEN = [
+    (lambda: _sm_test0(2, 2), 3, 3),
+    (lambda: _sm_test0(10000, 10000), 29999, 29997),
+    (lambda: _sm_test0(7, 10), 20, 18),
+    (lambda: _sm_test0(10, 7), 20, 18),
+    (lambda: _sm_test3(10), 100, 99),
+    (lambda: _sm_test3(300), 90000, 89999),
+]
+
+
+@pytest.mark.parametrize("case", range(len(SM_GOLDEN)))
+def test_transpose_matches_ugcore_golden(oracle_lib, case):
+    make, nnz_keep, nnz_drop = SM_GOLDEN[case]
+    ent, N, M = make()
+    rp, ci, va = _to_crs(ent, N)
+    assert oracle_lib.transpose_nnz(rp, ci, va, M, keep_zeros=True) == nnz_keep
+    assert oracle_lib.transpose_nnz(rp, ci, va, M, keep_zeros=False) == nnz_drop
+
+
+# ---- fixtures from ugcore's algebra (tests/golden/make_golden.py) ----------
+GOLDEN_CASES = ["quad_2x2_r4", "hex_2x2x2_r2", "tet_4x4x4_r1_lognormal", "hex_3x3x3_r1_convection"]
+
+
+def _golden_problem(orc, g):
+    e, mx, my, mz, nref, seed, ck, solver, vk, diff, pe = g["params"]
+    p = orc.make_params(elem_type=int(e), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
+                        coef_kind=int(ck), solver=int(solver), vel_kind=int(vk), diffusion=diff, peclet=pe)
+    return orc.Problem(p)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_oracle_reproduces_ugcore_algebra(oracle_lib, name):
+    g = load_golden(name)
+    assert g is not None, "missing fixture " + name
+    P = _golden_problem(oracle_lib, g)
+    nl = int(g["nlev"])
+    assert P.nlev == nl
+    for l in range(nl):
+        got = P.matrix(l)
+        ref = (g["A%d_rowptr" % l], g["A%d_col" % l], g["A%d_val" % l])
+        assert_crs_equal(got, ref, rtol=0.0, what="level %d operator" % l)
+    assert_crs_equal(P.transfer(nl - 1, 0), (g["P_rowptr"], g["P_col"], g["P_val"]), rtol=0.0, what="P")
+    assert_crs_equal(P.transfer(nl - 1, 1), (g["R_rowptr"], g["R_col"], g["R_val"]), rtol=0.0, what="R")
+    assert np.array_equal(P.rhs(), g["b"])
+    s = P.solve(hist_cap=400)
+    assert s["steps"] == int(g["steps"])
+    assert np.array_equal(s["x"], g["x"])
+    assert np.array_equal(s["history"], g["hist"])
+
+
+def test_reference_driver_live(oracle_lib, tmp_path):
+    """When the reference tree is present, rebuild the driver and compare live."""
+    drv = os.path.join(ROOT, "oracle", "_ref", "ref_driver")
+    if not os.path.exists(drv):
+        pytest.skip("oracle/_ref not built (no reference tree on this machine)")
+    out = str(tmp_path / "r.bin")
+    subprocess.check_call([drv, out, "1", "2", "2", "2", "2", "7", "0", "0", "0"], stdout=subprocess.DEVNULL)
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mg", os.path.join(GOLDEN, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    R = mg.read_ref(out)
+    P = oracle_lib.Problem(oracle_lib.make_params(elem_type=1, mx=2, my=2, mz=2, nref=2, seed=7))
+    s = P.solve(hist_cap=100)
+    assert s["steps"] == R["steps"] and np.array_equal(s["x"], R["x"])
+
+
+# ---- geometry -------------------------------------------------------------
+def test_fv1_geometry_unit_elements(oracle_lib):
+    o = oracle_lib
+    g = o.geometry(o.ORC_QUAD, [[0, 0], [1, 0], [1, 1], [0, 1]])
+    assert np.allclose(g["vols"], 0.25)
+    assert np.allclose(g["normals"], [[0.5, 0], [0, 0.5], [-0.5, 0], [0, -0.5]])
+    hexc = [[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]]
+    g = o.geometry(o.ORC_HEX, hexc)
+    assert np.allclose(g["vols"], 0.125)
+    # every SCVF normal points from -> to with area 1/4
+    c = np.array(hexc, float)
+    for i in range(12):
+        d = c[g["to"][i]] - c[g["frm"][i]]
+        assert np.isclose(g["normals"][i] @ d, 0.25)
+    g = o.geometry(o.ORC_TET, [[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]])
+    assert np.allclose(g["vols"], 1.0 / 24.0, rtol=1e-14)
+
+
+def test_fv1_gradients_reproduce_linear_functions(oracle_lib):
+    """sum_sh u(x_sh) grad phi_sh = grad u for linear u, on distorted elements"""
+    o = oracle_lib
+    rng = np.random.default_rng(3)
+    a = np.array([0.3, -1.2, 0.7])
+    for et, base in [(o.ORC_QUAD, [[0, 0], [1, 0], [1, 1], [0, 1]]),
+                     (o.ORC_HEX, [[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1],
+                                  [0, 1, 1]]),
+                     (o.ORC_TET, [[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]])]:
+        X = np.array(base, float) + 0.1 * rng.standard_normal((len(base), len(base[0])))
+        if et == o.ORC_HEX:
+            X = np.array(base, float) * [1.0, 0.8, 1.3]   # trilinear maps keep linear exact on parallelepipeds
+        g = o.geometry(et, X)
+        dim = X.shape[1]
+        u = X @ a[:dim]
+        for ip in range(g["grads"].shape[0]):
+            assert np.allclose(g["grads"][ip].T @ u, a[:dim], atol=1e-12)
+
+
+# ---- seeded generators: product host code == oracle --------------------------
+def test_field_generators_match_oracle(oracle_lib):
+    import ctypes as C
+    from ugcore_gb300 import fields
+    L = oracle_lib.lib()
+    L.orc_field_params.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.POINTER(C.c_double)]
+    for dim, nm, kmax, seed in [(3, 64, 8.0, 1 ^ fields.COEF_SEED_XOR), (2, 32, 8.0, 5)]:
+        k = np.zeros(nm * dim)
+        ph = np.zeros(nm)
+        amp = C.c_double()
+        L.orc_field_params(0, dim, nm, kmax, seed, k.ctypes.data, ph.ctypes.data, None, C.byref(amp))
+        f = fields.ScalarField(dim, nm, kmax, seed)
+        assert np.array_equal(f.k.ravel(), k) and np.array_equal(f.phase, ph) and f.amp == amp.value
+    nm = 16
+    k, ph, c = np.zeros(nm * 3), np.zeros(nm), np.zeros(nm * 3)
+    sc = C.c_double()
+    L.orc_field_params(1, 3, nm, 2.0, 1 ^ fields.VEL_SEED_XOR, k.ctypes.data, ph.ctypes.data, c.ctypes.data,
+                       C.byref(sc))
+    f = fields.CurlField(nm, 2.0, 1 ^ fields.VEL_SEED_XOR)
+    assert np.array_equal(f.k.ravel(), k) and np.array_equal(f.phase, ph) and np.array_equal(f.c.ravel(), c)
+    assert f.scale == sc.value
+
+
+def test_curl_field_is_divergence_free():
+    from ugcore_gb300 import fields
+    f = fields.CurlField(16, 2.0, 11)
+    x = np.random.default_rng(0).random((50, 3))
+    h = 1e-5
+    div = sum((f(x + h * e)[:, i] - f(x - h * e)[:, i]) / (2 * h) for i, e in enumerate(np.eye(3)))
+    assert np.abs(div).max() < 1e-6
+
+
+def test_source_hash_matches_oracle(oracle_lib):
+    from ugcore_gb300 import fields
+    P = oracle_lib.Problem(oracle_lib.make_params(elem_type=0, nref=3, seed=42))
+    assert np.array_equal(P.source(), fields.source_uniform(42, P.nv()))
+
+
+# ---- solver-level properties of the oracle ----------------------------------
+def test_tet_refinement_nests(oracle_lib):
+    """every coarse Kuhn tet receives exactly 8 children when log K is coarsened"""
+    o = oracle_lib
+    P = o.Problem(o.make_params(elem_type=o.ORC_TET, mx=2, my=2, mz=2, nref=2, coef_kind=2),
+                  m_top=np.ones(6 * 8 * 8 * 8 * 8))
+    for l in range(P.nlev):
+        assert np.allclose(np.log(P.coef(l)), 1.0)
+
+
+def test_mcgs_oracle_converges(oracle_lib):
+    o = oracle_lib
+    P = o.Problem(o.make_params(elem_type=o.ORC_HEX, nref=3, smoother=1, damp=1.0))
+    s = P.solve()
+    assert s["converged"] and s["steps"] < 10
+
+
+def test_adjoint_oracle_matches_finite_differences(oracle_lib):
+    o = oracle_lib
+    rng = np.random.default_rng(1)
+    base = o.make_params(elem_type=o.ORC_QUAD, nref=3, coef_kind=2, rel_red=1e-14, maxit=400)
+    ne = 2 * 2 * 64
+    m = 0.3 * rng.standard_normal(ne)
+    P = o.Problem(base, m_top=m)
+    u = P.solve()["x"]
+    uobs = 0.5 * u
+    lam = P.adjoint(u - uobs)["lam"]
+    g = P.grad_logk(u, lam)
+    J = lambda mm: 0.5 * np.sum((o.Problem(base, m_top=mm).solve()["x"] - uobs) ** 2)
+    h = 1e-6
+    for _ in range(3):
+        d = rng.standard_normal(ne)
+        fd = (J(m + h * d) - J(m - h * d)) / (2 * h)
+        assert abs(fd - g @ d) <= 1e-6 * max(abs(fd), 1e-30) + 1e-12

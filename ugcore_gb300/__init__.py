@@ -1,0 +1,14 @@
+"""ugcore_gb300 -- GB300-native (sm_103a) FV1 assembly + geometric-multigrid
+Krylov solve for UG4/ugcore, behind a C ABI (include/ug4gb.h, libug4gb.so).
+
+The Python layer mirrors ugcore's object model (algebra.py) and hosts the
+adjoint autograd binding (adjoint.py).  Every numerical step runs in the
+CUDA library; importing works without a GPU, but creating a Context needs one
+and there is no CPU fallback.
+"""
+from ._lib import UG4GBError, exported_symbols, LIB_PATH  # noqa: F401
+from .algebra import (BiCGStab, CG, Context, DomainDiscretization, GaussSeidel, GeometricMultiGrid,  # noqa: F401
+                      GPUSparseMatrix, GPUVector, Jacobi, StdConvCheck, StructuredHierarchy)
+
+__all__ = ["UG4GBError", "Context", "StructuredHierarchy", "GPUVector", "GPUSparseMatrix", "DomainDiscretization",
+           "GeometricMultiGrid", "Jacobi", "GaussSeidel", "StdConvCheck", "CG", "BiCGStab", "exported_symbols"]

@@ -1,0 +1,140 @@
+"""ctypes binding of libug4gb.so (the C ABI declared in include/ug4gb.h).
+
+Loading fails loudly when the library has not been built: there is no CPU
+fallback anywhere in this package.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libug4gb.so")
+
+OK = 0
+ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_SINGULAR, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_STATE = -1, -2, -3, -4, -5, -6, -7
+QUAD, HEX, TET = 0, 1, 2
+SMOOTHER_JACOBI, SMOOTHER_MCGS = 0, 1
+PREC_FP64, PREC_MIXED = 0, 1
+SOLVER_CG, SOLVER_BICGSTAB = 0, 1
+UPWIND_NONE, UPWIND_FULL = 0, 1
+
+_ERRNAMES = {ERR_INVALID: "invalid argument", ERR_CUDA: "CUDA error", ERR_NOMEM: "out of device memory",
+             ERR_SINGULAR: "singular base matrix", ERR_NOT_CONVERGED: "not converged",
+             ERR_BREAKDOWN: "Krylov breakdown", ERR_STATE: "wrong call order"}
+
+
+class UG4GBError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (_ERRNAMES.get(code, "error"), code, msg))
+        self.code = code
+
+
+P = C.c_void_p
+I = C.c_int
+D = C.c_double
+I64 = C.c_int64
+PP = C.POINTER(C.c_void_p)
+PI = C.POINTER(C.c_int)
+PD = C.POINTER(C.c_double)
+PI64 = C.POINTER(C.c_int64)
+
+# name: (restype, argtypes)
+_SIGS = {
+    "ug4gb_create": (I, [I, PP]),
+    "ug4gb_destroy": (None, [P]),
+    "ug4gb_last_error": (C.c_char_p, [P]),
+    "ug4gb_synchronize": (I, [P]),
+    "ug4gb_stream": (P, [P]),
+    "ug4gb_kernel_launches": (I64, [P]),
+    "ug4gb_grid_create_structured": (I, [P, I, I, I, I, I, PP]),
+    "ug4gb_grid_num_levels": (I, [P]),
+    "ug4gb_grid_level_info": (I, [P, I, PI, PI, PI, PI]),
+    "ug4gb_grid_level_export": (I, [P, I, P, P, P]),
+    "ug4gb_grid_destroy": (None, [P]),
+    "ug4gb_vector_create": (I, [P, I, PP]),
+    "ug4gb_vector_wrap": (I, [P, P, I, PP]),
+    "ug4gb_vector_size": (I, [P]),
+    "ug4gb_vector_data": (P, [P]),
+    "ug4gb_vector_set": (I, [P, D]),
+    "ug4gb_vector_copy_from": (I, [P, P]),
+    "ug4gb_vector_copy_to": (I, [P, P]),
+    "ug4gb_vector_norm": (I, [P, PD]),
+    "ug4gb_vector_dot": (I, [P, P, PD]),
+    "ug4gb_vector_scale_add": (I, [P, D, P, D, P]),
+    "ug4gb_vector_destroy": (None, [P]),
+    "ug4gb_matrix_create": (I, [P, PP]),
+    "ug4gb_matrix_set_csr": (I, [P, I, I, I64, P, P, P]),
+    "ug4gb_matrix_info": (I, [P, PI, PI, PI64]),
+    "ug4gb_matrix_export_csr": (I, [P, P, P, P]),
+    "ug4gb_matrix_axpy": (I, [P, P, D, P, D, P]),
+    "ug4gb_matrix_axpy_transposed": (I, [P, P, D, P, D, P]),
+    "ug4gb_matrix_set_as_transpose_of": (I, [P, P, I]),
+    "ug4gb_matrix_destroy": (None, [P]),
+    "ug4gb_disc_create": (I, [P, P, PP]),
+    "ug4gb_disc_set_diffusion_constant": (I, [P, D]),
+    "ug4gb_disc_set_diffusion_fourier": (I, [P, I, P, P, D, D]),
+    "ug4gb_disc_set_log_diffusion_elements": (I, [P, P]),
+    "ug4gb_disc_set_velocity_fourier_curl": (I, [P, I, P, P, P, D]),
+    "ug4gb_disc_set_upwind": (I, [P, I]),
+    "ug4gb_disc_set_source_vertices": (I, [P, P]),
+    "ug4gb_disc_set_source_uniform": (I, [P, C.c_uint64]),
+    "ug4gb_disc_assemble_linear": (I, [P, I, P, P]),
+    "ug4gb_disc_assemble_jacobian": (I, [P, I, P]),
+    "ug4gb_disc_export_coefficients": (I, [P, I, P]),
+    "ug4gb_disc_adjoint_operator": (I, [P, I, P, P]),
+    "ug4gb_disc_destroy": (None, [P]),
+    "ug4gb_gmg_create": (I, [P, P, PP]),
+    "ug4gb_gmg_set_smoother": (I, [P, I, D]),
+    "ug4gb_gmg_set_cycle_type": (I, [P, I]),
+    "ug4gb_gmg_set_num_presmooth": (I, [P, I]),
+    "ug4gb_gmg_set_num_postsmooth": (I, [P, I]),
+    "ug4gb_gmg_set_base_level": (I, [P, I]),
+    "ug4gb_gmg_set_precision": (I, [P, I]),
+    "ug4gb_gmg_set_transposed": (I, [P, I]),
+    "ug4gb_gmg_init": (I, [P, P]),
+    "ug4gb_gmg_apply": (I, [P, P, P]),
+    "ug4gb_gmg_transfer_info": (I, [P, I, I, PI, PI, PI64]),
+    "ug4gb_gmg_export_transfer": (I, [P, I, I, P, P, P]),
+    "ug4gb_gmg_destroy": (None, [P]),
+    "ug4gb_solver_create": (I, [P, I, PP]),
+    "ug4gb_solver_set_preconditioner": (I, [P, P]),
+    "ug4gb_solver_set_convergence_check": (I, [P, I, D, D]),
+    "ug4gb_solver_init": (I, [P, P]),
+    "ug4gb_solver_apply_return_defect": (I, [P, P, P]),
+    "ug4gb_solver_apply": (I, [P, P, P]),
+    "ug4gb_solver_solve_host": (I, [P, P, P]),
+    "ug4gb_solver_get_stats": (I, [P, PI, PD, PD, PI]),
+    "ug4gb_solver_get_history": (I, [P, P, I]),
+    "ug4gb_solver_destroy": (None, [P]),
+    "ug4gb_disc_grad_logk": (I, [P, P, P, P]),
+    "ug4gb_disc_grad_source": (I, [P, P, P]),
+}
+
+_lib = None
+
+
+def exported_symbols():
+    """Names the C header declares (for the symbol-export test)."""
+    return sorted(_SIGS)
+
+
+def lib():
+    """Load libug4gb.so; raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libug4gb.so not built: run __graft_entry__.build() or "
+                              "python -m ugcore_gb300.build")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc, ctx=None):
+    if rc != OK and rc is not None:
+        msg = lib().ug4gb_last_error(ctx).decode() if ctx else ""
+        raise UG4GBError(rc, msg)
+    return rc

@@ -1,0 +1,485 @@
+"""Python mirror of ugcore's assemble-and-solve interface over libug4gb.
+
+Class and method names follow the ugcore objects a Lua script drives through
+the registry (bridge/algebra_bridges/solver_bridge.cpp, preconditioner_bridge.cpp,
+disc_bridges/multigrid_bridge.cpp, domain_disc_bridge.cpp):
+
+    ugcore (Lua)                          here
+    ------------------------------------  -------------------------------------
+    InitUG(dim, AlgebraType("GPU", 1))    Context(device)
+    util.CreateDomain + refinement        StructuredHierarchy(ctx, "hex", 2, 2, 2, 6)
+    DomainDiscretization + FV1 ConvDiff   DomainDiscretization(hier) .set_* ...
+    + DirichletBoundary (0 on boundary)
+    GridFunction / Vector                 GPUVector
+    AssembledLinearOperator / matrix      GPUSparseMatrix
+    GeometricMultiGrid(approxSpace)       GeometricMultiGrid(disc)
+    Jacobi(0.6) / GaussSeidel()           Jacobi(0.6) / GaussSeidel() (multicolour)
+    StdTransfer                           built in (P1 prolongation, R = P^T)
+    LU                                    built in (dense base solver)
+    CG() / BiCGStab()                     CG() / BiCGStab()
+    ConvCheck(maxit, minDef, red)         StdConvCheck(maxit, minDef, red)
+
+All work happens on the GPU; errors raised by the C ABI become UG4GBError.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, lib
+
+_ELEM = {"quad": _lib.QUAD, "quadrilateral": _lib.QUAD, "hex": _lib.HEX, "hexahedron": _lib.HEX,
+         "tet": _lib.TET, "tetrahedron": _lib.TET}
+
+
+def _ptr(a):
+    """data pointer of a numpy array or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    return C.c_void_p(a.ctypes.data)
+
+
+def _f64(a):
+    if hasattr(a, "data_ptr"):
+        return a
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class Context:
+    """One GPU, one stream (InitUG with the GPU algebra)."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        rc = lib().ug4gb_create(device, C.byref(h))
+        if rc != 0:
+            raise _lib.UG4GBError(rc, "cannot create context on device %d" % device)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def synchronize(self):
+        check(lib().ug4gb_synchronize(self.h), self.h)
+
+    def kernel_launches(self):
+        return lib().ug4gb_kernel_launches(self.h)
+
+    @property
+    def stream(self):
+        return lib().ug4gb_stream(self.h)
+
+
+class StructuredHierarchy:
+    """Uniformly refined unit square/cube: levels 0..num_refinements."""
+
+    def __init__(self, ctx, elem, mx, my, mz=1, num_refinements=0):
+        self.ctx = ctx
+        self.elem_type = _ELEM[elem] if isinstance(elem, str) else int(elem)
+        h = C.c_void_p()
+        check(lib().ug4gb_grid_create_structured(ctx.h, self.elem_type, mx, my, mz, num_refinements, C.byref(h)),
+              ctx.h)
+        self.h = h
+        self.num_levels = lib().ug4gb_grid_num_levels(h)
+        self.top = self.num_levels - 1
+        self.dim = 2 if self.elem_type == _lib.QUAD else 3
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_grid_destroy(self.h)
+            self.h = None
+
+    def level_info(self, level=None):
+        level = self.top if level is None else level
+        nv, ne, k, dim = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(lib().ug4gb_grid_level_info(self.h, level, C.byref(nv), C.byref(ne), C.byref(k), C.byref(dim)))
+        return dict(num_vertices=nv.value, num_elements=ne.value, corners=k.value, dim=dim.value)
+
+    def num_vertices(self, level=None):
+        return self.level_info(level)["num_vertices"]
+
+    def num_elements(self, level=None):
+        return self.level_info(level)["num_elements"]
+
+    def export(self, level=None):
+        level = self.top if level is None else level
+        info = self.level_info(level)
+        coords = np.zeros((info["num_vertices"], info["dim"]))
+        elems = np.zeros((info["num_elements"], info["corners"]), np.int32)
+        bnd = np.zeros(info["num_vertices"], np.uint8)
+        check(lib().ug4gb_grid_level_export(self.h, level, _ptr(coords), _ptr(elems), _ptr(bnd)), self.ctx.h)
+        return coords, elems, bnd
+
+
+class GPUVector:
+    """Device vector of doubles (ug::Vector<double>)."""
+
+    def __init__(self, ctx, n=None, wrap=None):
+        self.ctx = ctx
+        h = C.c_void_p()
+        if wrap is not None:
+            # wrap a CUDA torch tensor (float64, contiguous) without copying
+            self._keep = wrap
+            check(lib().ug4gb_vector_wrap(ctx.h, C.c_void_p(wrap.data_ptr()), wrap.numel(), C.byref(h)), ctx.h)
+        else:
+            check(lib().ug4gb_vector_create(ctx.h, int(n), C.byref(h)), ctx.h)
+        self.h = h
+        self.n = lib().ug4gb_vector_size(h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_vector_destroy(self.h)
+            self.h = None
+
+    def __len__(self):
+        return self.n
+
+    def size(self):
+        return self.n
+
+    def data_ptr(self):
+        return lib().ug4gb_vector_data(self.h)
+
+    def set(self, value):
+        check(lib().ug4gb_vector_set(self.h, float(value)), self.ctx.h)
+        return self
+
+    def copy_from(self, src):
+        src = _f64(src)
+        check(lib().ug4gb_vector_copy_from(self.h, _ptr(src)), self.ctx.h)
+        return self
+
+    def copy_to(self, dst=None):
+        if dst is None:
+            dst = np.zeros(self.n)
+        check(lib().ug4gb_vector_copy_to(self.h, _ptr(dst)), self.ctx.h)
+        return dst
+
+    def numpy(self):
+        return self.copy_to()
+
+    def norm(self):
+        out = C.c_double()
+        check(lib().ug4gb_vector_norm(self.h, C.byref(out)), self.ctx.h)
+        return out.value
+
+    def dot(self, other):
+        out = C.c_double()
+        check(lib().ug4gb_vector_dot(self.h, other.h, C.byref(out)), self.ctx.h)
+        return out.value
+
+    def scale_add(self, alpha, a, beta, b):
+        check(lib().ug4gb_vector_scale_add(self.h, alpha, a.h, beta, b.h), self.ctx.h)
+        return self
+
+    def clone(self):
+        v = GPUVector(self.ctx, self.n)
+        v.scale_add(1.0, self, 0.0, self)
+        return v
+
+    def clone_without_values(self):
+        return GPUVector(self.ctx, self.n)
+
+
+class GPUSparseMatrix:
+    """Device CRS matrix (ug::SparseMatrix<double>, defragmented form)."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(lib().ug4gb_matrix_create(ctx.h, C.byref(h)), ctx.h)
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_matrix_destroy(self.h)
+            self.h = None
+
+    def info(self):
+        r, c, nnz = C.c_int(), C.c_int(), C.c_int64()
+        check(lib().ug4gb_matrix_info(self.h, C.byref(r), C.byref(c), C.byref(nnz)))
+        return r.value, c.value, nnz.value
+
+    def num_rows(self):
+        return self.info()[0]
+
+    def num_cols(self):
+        return self.info()[1]
+
+    def total_num_connections(self):
+        return self.info()[2]
+
+    def set_csr(self, rowptr, col, val, num_cols=None):
+        rowptr = np.ascontiguousarray(rowptr, np.int32)
+        col = np.ascontiguousarray(col, np.int32)
+        val = np.ascontiguousarray(val, np.float64)
+        n = len(rowptr) - 1
+        check(lib().ug4gb_matrix_set_csr(self.h, n, n if num_cols is None else num_cols, len(col), _ptr(rowptr),
+                                         _ptr(col), _ptr(val)), self.ctx.h)
+        return self
+
+    def export_csr(self):
+        r, _, nnz = self.info()
+        rp = np.zeros(r + 1, np.int32)
+        ci = np.zeros(nnz, np.int32)
+        va = np.zeros(nnz)
+        check(lib().ug4gb_matrix_export_csr(self.h, _ptr(rp), _ptr(ci), _ptr(va)), self.ctx.h)
+        return rp, ci, va
+
+    def axpy(self, dest, alpha1, v1, beta1, w1):
+        """dest = alpha1*v1 + beta1*A*w1"""
+        check(lib().ug4gb_matrix_axpy(self.h, dest.h, alpha1, v1.h if v1 is not None else None, beta1, w1.h),
+              self.ctx.h)
+
+    def axpy_transposed(self, dest, alpha1, v1, beta1, w1):
+        check(lib().ug4gb_matrix_axpy_transposed(self.h, dest.h, alpha1, v1.h if v1 is not None else None, beta1,
+                                                 w1.h), self.ctx.h)
+
+    def apply(self, f, u):
+        """f = A u"""
+        self.axpy(f, 0.0, None, 1.0, u)
+
+    def apply_transposed(self, f, u):
+        self.axpy_transposed(f, 0.0, None, 1.0, u)
+
+    def matmul_minus(self, res, x):
+        """res -= A x"""
+        self.axpy(res, 1.0, res, -1.0, x)
+
+    def set_as_transpose_of(self, B, keep_zeros=True):
+        check(lib().ug4gb_matrix_set_as_transpose_of(self.h, B.h, 1 if keep_zeros else 0), self.ctx.h)
+        return self
+
+
+class DomainDiscretization:
+    """DomainDiscretization with one FV1 convection-diffusion element disc
+    (-div(K grad u) + div(v u) = f) and zero Dirichlet values on the whole
+    boundary."""
+
+    def __init__(self, hier):
+        self.ctx = hier.ctx
+        self.hier = hier
+        h = C.c_void_p()
+        check(lib().ug4gb_disc_create(self.ctx.h, hier.h, C.byref(h)), self.ctx.h)
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_disc_destroy(self.h)
+            self.h = None
+
+    def set_diffusion(self, K):
+        check(lib().ug4gb_disc_set_diffusion_constant(self.h, float(K)), self.ctx.h)
+
+    def set_diffusion_field(self, field, factor=2.0):
+        """K = exp(factor * g(centroid)) for a fields.ScalarField g."""
+        self._kk = np.ascontiguousarray(field.k, np.float64)
+        self._kp = np.ascontiguousarray(field.phase, np.float64)
+        check(lib().ug4gb_disc_set_diffusion_fourier(self.h, field.nmodes, _ptr(self._kk), _ptr(self._kp),
+                                                     field.amp, factor), self.ctx.h)
+
+    def set_log_diffusion(self, m_top):
+        """K = exp(m) per top-level element (host array or CUDA tensor)."""
+        m_top = _f64(m_top)
+        check(lib().ug4gb_disc_set_log_diffusion_elements(self.h, _ptr(m_top)), self.ctx.h)
+
+    def set_velocity_field(self, field, scale):
+        """v = scale * field(x) for a fields.CurlField (already normalised to |v| <= 1)."""
+        self._vk = np.ascontiguousarray(field.k, np.float64)
+        self._vc = np.ascontiguousarray(field.c, np.float64)
+        self._vp = np.ascontiguousarray(field.phase, np.float64)
+        check(lib().ug4gb_disc_set_velocity_fourier_curl(self.h, field.nmodes, _ptr(self._vk), _ptr(self._vc),
+                                                         _ptr(self._vp), field.scale * scale), self.ctx.h)
+
+    def set_upwind(self, upwind="full"):
+        check(lib().ug4gb_disc_set_upwind(self.h, _lib.UPWIND_FULL if upwind in ("full", 1, True) else
+                                          _lib.UPWIND_NONE), self.ctx.h)
+
+    def set_source(self, f_top):
+        f_top = _f64(f_top)
+        check(lib().ug4gb_disc_set_source_vertices(self.h, _ptr(f_top)), self.ctx.h)
+
+    def set_source_uniform(self, seed):
+        check(lib().ug4gb_disc_set_source_uniform(self.h, int(seed)), self.ctx.h)
+
+    def assemble_linear(self, A, b, level=None):
+        level = self.hier.top if level is None else level
+        check(lib().ug4gb_disc_assemble_linear(self.h, level, A.h, b.h), self.ctx.h)
+
+    def assemble_jacobian(self, A, level=None):
+        level = self.hier.top if level is None else level
+        check(lib().ug4gb_disc_assemble_jacobian(self.h, level, A.h), self.ctx.h)
+
+    def adjoint_operator(self, A, AT, level=None):
+        """AT = A^T with Dirichlet rows reset to identity."""
+        level = self.hier.top if level is None else level
+        check(lib().ug4gb_disc_adjoint_operator(self.h, level, A.h, AT.h), self.ctx.h)
+        return AT
+
+    def coefficients(self, level=None):
+        level = self.hier.top if level is None else level
+        K = np.zeros(self.hier.num_elements(level))
+        check(lib().ug4gb_disc_export_coefficients(self.h, level, _ptr(K)), self.ctx.h)
+        return K
+
+    def grad_logk(self, u, lam, out=None):
+        if out is None:
+            out = np.zeros(self.hier.num_elements())
+        check(lib().ug4gb_disc_grad_logk(self.h, u.h, lam.h, _ptr(out)), self.ctx.h)
+        return out
+
+    def grad_source(self, lam, out=None):
+        if out is None:
+            out = np.zeros(self.hier.num_vertices())
+        check(lib().ug4gb_disc_grad_source(self.h, lam.h, _ptr(out)), self.ctx.h)
+        return out
+
+
+class Jacobi:
+    """damped Jacobi smoother (jacobi.h); damp is the ugcore damping factor"""
+
+    def __init__(self, damp=1.0):
+        self.kind, self.damp = _lib.SMOOTHER_JACOBI, float(damp)
+
+
+class GaussSeidel:
+    """multicolour Gauss-Seidel smoother (opt-in GPU variant of gauss_seidel.h)"""
+
+    def __init__(self, relax=1.0):
+        self.kind, self.damp = _lib.SMOOTHER_MCGS, float(relax)
+
+
+class GeometricMultiGrid:
+    """AssembledMultiGridCycle: V/W cycle, re-assembled level operators,
+    StdTransfer, LU base solver."""
+
+    def __init__(self, disc):
+        self.ctx = disc.ctx
+        self.disc = disc
+        h = C.c_void_p()
+        check(lib().ug4gb_gmg_create(self.ctx.h, disc.h, C.byref(h)), self.ctx.h)
+        self.h = h
+        self.set_smoother(Jacobi(0.6))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_gmg_destroy(self.h)
+            self.h = None
+
+    def set_smoother(self, sm):
+        check(lib().ug4gb_gmg_set_smoother(self.h, sm.kind, sm.damp), self.ctx.h)
+
+    def set_cycle_type(self, cycle):
+        c = {"V": 1, "W": 2, 1: 1, 2: 2}[cycle]
+        check(lib().ug4gb_gmg_set_cycle_type(self.h, c), self.ctx.h)
+
+    def set_num_presmooth(self, n):
+        check(lib().ug4gb_gmg_set_num_presmooth(self.h, n), self.ctx.h)
+
+    def set_num_postsmooth(self, n):
+        check(lib().ug4gb_gmg_set_num_postsmooth(self.h, n), self.ctx.h)
+
+    def set_base_level(self, level):
+        check(lib().ug4gb_gmg_set_base_level(self.h, level), self.ctx.h)
+
+    def set_precision(self, prec):
+        p = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, 0: 0, 1: 1}[prec]
+        check(lib().ug4gb_gmg_set_precision(self.h, p), self.ctx.h)
+
+    def set_transposed(self, flag=True):
+        check(lib().ug4gb_gmg_set_transposed(self.h, 1 if flag else 0), self.ctx.h)
+
+    def init(self, A):
+        check(lib().ug4gb_gmg_init(self.h, A.h), self.ctx.h)
+
+    def apply(self, c, d):
+        check(lib().ug4gb_gmg_apply(self.h, c.h, d.h), self.ctx.h)
+
+    def transfer(self, level, which):
+        """(rowptr, col, val) of P (which=0) or R (which=1) of fine level `level`."""
+        r, cc, nnz = C.c_int(), C.c_int(), C.c_int64()
+        check(lib().ug4gb_gmg_transfer_info(self.h, level, which, C.byref(r), C.byref(cc), C.byref(nnz)),
+              self.ctx.h)
+        rp = np.zeros(r.value + 1, np.int32)
+        ci = np.zeros(nnz.value, np.int32)
+        va = np.zeros(nnz.value)
+        check(lib().ug4gb_gmg_export_transfer(self.h, level, which, _ptr(rp), _ptr(ci), _ptr(va)), self.ctx.h)
+        return rp, ci, va
+
+
+class StdConvCheck:
+    def __init__(self, max_steps=100, min_defect=1e-300, rel_reduction=1e-10):
+        self.max_steps, self.min_defect, self.rel_reduction = int(max_steps), float(min_defect), float(rel_reduction)
+
+
+class _Krylov:
+    KIND = None
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(lib().ug4gb_solver_create(ctx.h, self.KIND, C.byref(h)), ctx.h)
+        self.h = h
+        self.pre = None
+        self.set_convergence_check(StdConvCheck())
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_solver_destroy(self.h)
+            self.h = None
+
+    def set_preconditioner(self, gmg):
+        self.pre = gmg
+        check(lib().ug4gb_solver_set_preconditioner(self.h, gmg.h if gmg is not None else None), self.ctx.h)
+
+    def set_convergence_check(self, cc):
+        self.conv = cc
+        check(lib().ug4gb_solver_set_convergence_check(self.h, cc.max_steps, cc.min_defect, cc.rel_reduction),
+              self.ctx.h)
+
+    def init(self, A):
+        self.A = A
+        check(lib().ug4gb_solver_init(self.h, A.h), self.ctx.h)
+
+    def apply_return_defect(self, x, b, raise_on_failure=True):
+        rc = lib().ug4gb_solver_apply_return_defect(self.h, x.h, b.h)
+        return self._finish(rc, raise_on_failure)
+
+    def apply(self, x, b, raise_on_failure=True):
+        rc = lib().ug4gb_solver_apply(self.h, x.h, b.h)
+        return self._finish(rc, raise_on_failure)
+
+    def solve_host(self, b_host, x_host, raise_on_failure=True):
+        """b, x: host arrays (numpy or pinned torch); x = A^{-1} b from x0 = 0."""
+        rc = lib().ug4gb_solver_solve_host(self.h, _ptr(b_host), _ptr(x_host))
+        return self._finish(rc, raise_on_failure)
+
+    def _finish(self, rc, raise_on_failure):
+        if rc != 0 and (raise_on_failure or rc not in (_lib.ERR_NOT_CONVERGED, _lib.ERR_BREAKDOWN)):
+            check(rc, self.ctx.h)
+        return rc == 0
+
+    def stats(self):
+        steps, d0, d1, conv = C.c_int(), C.c_double(), C.c_double(), C.c_int()
+        check(lib().ug4gb_solver_get_stats(self.h, C.byref(steps), C.byref(d0), C.byref(d1), C.byref(conv)))
+        return dict(steps=steps.value, initial_defect=d0.value, defect=d1.value, converged=bool(conv.value))
+
+    def history(self):
+        cap = self.conv.max_steps + 2
+        buf = np.zeros(cap)
+        n = lib().ug4gb_solver_get_history(self.h, _ptr(buf), cap)
+        return buf[:max(n, 0)]
+
+
+class CG(_Krylov):
+    KIND = _lib.SOLVER_CG
+
+
+class BiCGStab(_Krylov):
+    KIND = _lib.SOLVER_BICGSTAB

@@ -1,0 +1,308 @@
+// api_disc.cu -- C ABI: FV1 convection-diffusion discretisation (assembly,
+// coefficients, Dirichlet rows) and the adjoint gradients.
+#include <cstring>
+
+#include "disc.cuh"
+#include "gmg.cuh"
+
+using namespace ug4gb;
+
+namespace ug4gb {
+
+
+
+// element coefficients of a level (cached until the coefficient changes)
+const double *disc_coefficients(ug4gb_disc *d, int level)
+{
+    DiscImpl &D = d->d;
+    Ctx &c = d->ctx->c;
+    const auto &lev = d->g->lev;
+    int nl = (int)lev.size();
+    if ((int)D.Klev.size() != nl) {
+        D.Klev.clear();
+        D.Klev.resize(nl);
+        D.Kvalid.assign(nl, false);
+    }
+    if (D.Kvalid[level]) return D.Klev[level].p;
+    if (D.coef_kind == COEF_LOG_ELEMS) {
+        // log K on every level from the top: children's mean, then exp
+        std::vector<DevBuf<double>> logk(nl);
+        logk[nl - 1].alloc(lev[nl - 1].ne);
+        UG_CUDA(cudaMemcpyAsync(logk[nl - 1].p, D.m_top.p, D.m_top.bytes(), cudaMemcpyDeviceToDevice, c.stream));
+        for (int l = nl - 2; l >= 0; --l) {
+            logk[l].alloc(lev[l].ne);
+            coarsen_log(c, lev[l + 1], lev[l], logk[l + 1].p, logk[l].p);
+        }
+        for (int l = 0; l < nl; ++l) {
+            D.Klev[l].alloc(lev[l].ne);
+            exp_elements(c, logk[l].p, lev[l].ne, D.Klev[l].p);
+            D.Kvalid[l] = true;
+        }
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        return D.Klev[level].p;
+    }
+    D.Klev[level].alloc(lev[level].ne);
+    if (D.coef_kind == COEF_CONST) fill_double(c, D.Klev[level].p, lev[level].ne, D.K_const);
+    else launch_coef_fourier(c, lev[level], D.kmodes, D.kk.p, D.kphase.p, D.kamp, D.kfactor, D.Klev[level].p);
+    D.Kvalid[level] = true;
+    return D.Klev[level].p;
+}
+
+// assemble the FV1 operator of `level` into A (and the rhs into b if given)
+void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b)
+{
+    Ctx &c = d->ctx->c;
+    const Level &L = d->g->lev[level];
+    const double *K = disc_coefficients(d, level);
+    if (A->pattern_grid != (const void *)d->g || A->pattern_level != level) {
+        csr_from_elements(c, L, A->A);
+        A->pattern_grid = d->g;
+        A->pattern_level = level;
+    } else {
+        UG_CUDA(cudaMemsetAsync(A->A.val.p, 0, sizeof(double) * (size_t)A->A.nnz, c.stream));
+    }
+    A->sell_valid = false;
+    if (b) UG_CUDA(cudaMemsetAsync(b, 0, sizeof(double) * (size_t)L.nv, c.stream));
+    const DiscImpl &D = d->d;
+    bool top = (level == (int)d->g->lev.size() - 1);
+    AsmArgs a;
+    a.coords = L.coords.p;
+    a.elems = L.elems.p;
+    a.ne = L.ne;
+    a.K = K;
+    a.f = (top && D.f_kind == 1) ? D.f_top.p : nullptr;
+    a.f_seed = D.f_seed;
+    a.use_seed = (top && D.f_kind == 2) ? 1 : 0;
+    a.vmodes = D.upwind ? D.vmodes : 0;
+    a.vk = D.vk.p;
+    a.vc = D.vc.p;
+    a.vphase = D.vphase.p;
+    a.vscale = D.vscale;
+    a.rowptr = A->A.rowptr.p;
+    a.col = A->A.col.p;
+    a.val = A->A.val.p;
+    a.b = b;
+    launch_assemble(c, L, a);
+    launch_dirichlet(c, L, A->A, b);
+}
+
+}  // namespace ug4gb
+
+template <class F>
+static int guarded(ug4gb_ctx *ctx, F &&f)
+{
+    try {
+        f();
+        return UG4GB_OK;
+    } catch (const Error &e) {
+        if (ctx) ctx->c.err = e.msg;
+        return e.code;
+    } catch (const std::exception &e) {
+        if (ctx) ctx->c.err = e.what();
+        return UG4GB_ERR_INVALID;
+    }
+}
+
+static void invalidate(ug4gb_disc *d)
+{
+    d->d.Kvalid.assign(d->g->lev.size(), false);
+}
+
+extern "C" {
+
+int ug4gb_disc_create(ug4gb_ctx *ctx, const ug4gb_grid *g, ug4gb_disc **out)
+{
+    if (!ctx || !g || !out) return UG4GB_ERR_INVALID;
+    ug4gb_disc *d = new ug4gb_disc;
+    d->ctx = ctx;
+    d->g = g;
+    invalidate(d);
+    *out = d;
+    return UG4GB_OK;
+}
+
+int ug4gb_disc_set_diffusion_constant(ug4gb_disc *d, double K)
+{
+    if (!d) return UG4GB_ERR_INVALID;
+    d->d.coef_kind = COEF_CONST;
+    d->d.K_const = K;
+    invalidate(d);
+    return UG4GB_OK;
+}
+
+int ug4gb_disc_set_diffusion_fourier(ug4gb_disc *d, int nmodes, const double *k, const double *phase, double amp,
+                                     double factor)
+{
+    if (!d || nmodes < 0 || (nmodes && (!k || !phase))) return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        int dim = d->g->lev[0].dim;
+        DiscImpl &D = d->d;
+        D.coef_kind = COEF_FOURIER;
+        D.kmodes = nmodes;
+        D.kk.alloc((size_t)(nmodes > 0 ? nmodes : 1) * dim);
+        D.kphase.alloc(nmodes > 0 ? nmodes : 1);
+        copy_in(d->ctx->c, D.kk.p, k, sizeof(double) * (size_t)nmodes * dim);
+        copy_in(d->ctx->c, D.kphase.p, phase, sizeof(double) * (size_t)nmodes);
+        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+        D.kamp = amp;
+        D.kfactor = factor;
+        invalidate(d);
+    });
+}
+
+int ug4gb_disc_set_log_diffusion_elements(ug4gb_disc *d, const double *m_top)
+{
+    if (!d || !m_top) return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        DiscImpl &D = d->d;
+        int ne = d->g->lev.back().ne;
+        D.coef_kind = COEF_LOG_ELEMS;
+        D.m_top.alloc(ne);
+        copy_in(d->ctx->c, D.m_top.p, m_top, sizeof(double) * (size_t)ne);
+        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+        invalidate(d);
+    });
+}
+
+int ug4gb_disc_set_velocity_fourier_curl(ug4gb_disc *d, int nmodes, const double *k, const double *cvec,
+                                         const double *phase, double scale)
+{
+    if (!d || nmodes < 0 || (nmodes && (!k || !cvec || !phase))) return UG4GB_ERR_INVALID;
+    if (d->g->lev[0].dim != 3 && nmodes > 0) {
+        d->ctx->c.err = "velocity field: only 3D grids";
+        return UG4GB_ERR_INVALID;
+    }
+    return guarded(d->ctx, [&] {
+        DiscImpl &D = d->d;
+        D.vmodes = nmodes;
+        size_t m = nmodes > 0 ? nmodes : 1;
+        D.vk.alloc(3 * m);
+        D.vc.alloc(3 * m);
+        D.vphase.alloc(m);
+        copy_in(d->ctx->c, D.vk.p, k, sizeof(double) * 3 * (size_t)nmodes);
+        copy_in(d->ctx->c, D.vc.p, cvec, sizeof(double) * 3 * (size_t)nmodes);
+        copy_in(d->ctx->c, D.vphase.p, phase, sizeof(double) * (size_t)nmodes);
+        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+        D.vscale = scale;
+    });
+}
+
+int ug4gb_disc_set_upwind(ug4gb_disc *d, int upwind)
+{
+    if (!d || (upwind != UG4GB_UPWIND_NONE && upwind != UG4GB_UPWIND_FULL)) return UG4GB_ERR_INVALID;
+    d->d.upwind = upwind;
+    return UG4GB_OK;
+}
+
+int ug4gb_disc_set_source_vertices(ug4gb_disc *d, const double *f)
+{
+    if (!d || !f) return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        int nv = d->g->lev.back().nv;
+        d->d.f_top.alloc(nv);
+        copy_in(d->ctx->c, d->d.f_top.p, f, sizeof(double) * (size_t)nv);
+        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+        d->d.f_kind = 1;
+    });
+}
+
+int ug4gb_disc_set_source_uniform(ug4gb_disc *d, uint64_t seed)
+{
+    if (!d) return UG4GB_ERR_INVALID;
+    d->d.f_kind = 2;
+    d->d.f_seed = seed;
+    return UG4GB_OK;
+}
+
+int ug4gb_disc_assemble_linear(ug4gb_disc *d, int level, ug4gb_matrix *A, ug4gb_vector *b)
+{
+    if (!d || !A || !b || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
+    if (b->n != d->g->lev[level].nv) {
+        d->ctx->c.err = "assemble_linear: rhs size mismatch";
+        return UG4GB_ERR_INVALID;
+    }
+    return guarded(d->ctx, [&] {
+        disc_assemble(d, level, A, b->d);
+        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+    });
+}
+
+int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matrix *A)
+{
+    if (!d || !A || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        disc_assemble(d, level, A, nullptr);
+        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+    });
+}
+
+int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A, ug4gb_matrix *AT)
+{
+    if (!d || !A || !AT || A == AT || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
+    if (A->A.nrows != d->g->lev[level].nv) return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        Ctx &c = d->ctx->c;
+        csr_transpose(c, A->A, AT->A, true);
+        launch_dirichlet(c, d->g->lev[level], AT->A, nullptr);
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        AT->sell_valid = false;
+        AT->pattern_grid = nullptr;
+        AT->pattern_level = -1;
+    });
+}
+
+int ug4gb_disc_export_coefficients(ug4gb_disc *d, int level, double *K)
+{
+    if (!d || !K || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        const double *p = disc_coefficients(d, level);
+        copy_out(d->ctx->c, K, p, sizeof(double) * (size_t)d->g->lev[level].ne);
+    });
+}
+
+void ug4gb_disc_destroy(ug4gb_disc *d)
+{
+    if (!d) return;
+    cudaStreamSynchronize(d->ctx->c.stream);
+    delete d;
+}
+
+int ug4gb_disc_grad_logk(ug4gb_disc *d, const ug4gb_vector *u, const ug4gb_vector *lam, double *grad)
+{
+    if (!d || !u || !lam || !grad) return UG4GB_ERR_INVALID;
+    const Level &L = d->g->lev.back();
+    if (u->n != L.nv || lam->n != L.nv) return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        Ctx &c = d->ctx->c;
+        const double *K = disc_coefficients(d, (int)d->g->lev.size() - 1);
+        if (is_device_ptr(grad)) {
+            launch_grad_logk(c, L, K, u->d, lam->d, grad);
+            UG_CUDA(cudaStreamSynchronize(c.stream));
+        } else {
+            DevBuf<double> g;
+            g.alloc(L.ne);
+            launch_grad_logk(c, L, K, u->d, lam->d, g.p);
+            copy_out(c, grad, g.p, g.bytes());
+        }
+    });
+}
+
+int ug4gb_disc_grad_source(ug4gb_disc *d, const ug4gb_vector *lam, double *grad)
+{
+    if (!d || !lam || !grad) return UG4GB_ERR_INVALID;
+    const Level &L = d->g->lev.back();
+    if (lam->n != L.nv) return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        Ctx &c = d->ctx->c;
+        if (is_device_ptr(grad)) {
+            launch_grad_source(c, L, lam->d, grad);
+        } else {
+            DevBuf<double> g;
+            g.alloc(L.nv);
+            launch_grad_source(c, L, lam->d, g.p);
+            copy_out(c, grad, g.p, g.bytes());
+        }
+    });
+}
+
+}  // extern "C"

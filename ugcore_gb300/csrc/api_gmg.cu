@@ -1,0 +1,575 @@
+// api_gmg.cu -- AssembledMultiGridCycle on the GPU: level setup (operator
+// copy / re-assembly, StdTransfer P and R with Dirichlet adjustment, Jacobi
+// or multicolour Gauss-Seidel smoother, dense LU base) and the cycle as a
+// fixed sequence of fused kernels, replayed from a CUDA graph.
+//
+// Reference: lib_disc/operator/linear_operator/multi_grid_solver/
+// mg_solver_impl.hpp (init :380, init_transfer :1078, init_smoother :1137,
+// init_base_solver :1173, apply :176, lmgc :2091, presmooth_and_restriction
+// :1687, prolongation_and_postsmooth :1820, base_solve :1969) for a fully
+// refined hierarchy, where the last defect update after post-smoothing and
+// after the base solve is dead (m_LocalFullRefLevel == top level) except on
+// the top level, where it only feeds the returned correction's defect and
+// is skipped here because apply() returns the correction alone.
+#include <cmath>
+#include <cstring>
+
+#include "disc.cuh"
+#include "gmg.cuh"
+
+using namespace ug4gb;
+
+namespace ug4gb {
+
+void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b);
+
+// ------------------------------------------------------------- helpers ---
+__global__ void k_diag_inv(const int *rowptr, const int *col, const double *val, int n, double damp, int smoother,
+                           double *dinv, double *dfac)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double a = 0.0;
+    for (int q = rowptr[i]; q < rowptr[i + 1]; ++q)
+        if (col[q] == i) a = val[q];
+    if (smoother == UG4GB_SMOOTHER_JACOBI) {
+        // Jacobi::preprocess (jacobi.h:196-208): diagInv = 1 / (a_ii * (1/damp))
+        double m = a * (1. / damp);
+        dinv[i] = 1. / m;
+        dfac[i] = m;
+    } else {
+        dinv[i] = damp / a;
+        dfac[i] = 1.0;
+    }
+}
+
+template <class V>
+__global__ void k_to_v(const double *in, V *out, int n)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (V)in[i];
+}
+
+// P rows from the parent table; Dirichlet fine rows: values 0, and 1 to a
+// vertex parent (DirichletBoundary::adjust_prolongation)
+__global__ void k_build_P(const int *npar, const int *par, const unsigned char *bnd, int nf, int *rowptr_len,
+                          int *col, double *val, const int *rowptr, int mode)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nf) return;
+    int n = npar[i];
+    if (mode == 0) {
+        rowptr_len[i] = n;
+        return;
+    }
+    double w = (n == 1) ? 1.0 : (n == 2 ? 0.5 : (n == 4 ? 0.25 : 0.125));
+    int a0 = rowptr[i];
+    for (int j = 0; j < n; ++j) {
+        col[a0 + j] = par[8 * (size_t)i + j];
+        double v = w;
+        if (bnd[i]) v = (n == 1) ? 1.0 : 0.0;
+        val[a0 + j] = v;
+    }
+}
+
+// rows of coarse Dirichlet vertices in R: 0, and 1 at the fine child
+// (DirichletBoundary::adjust_restriction)
+__global__ void k_adjust_R(const int *npar, const int *par, const unsigned char *bnd, int nf, const int *rowptr,
+                           const int *col, double *val)
+{
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf || !bnd[f] || npar[f] != 1) return;
+    int c = par[8 * (size_t)f];
+    for (int a = rowptr[c]; a < rowptr[c + 1]; ++a) val[a] = (col[a] == f) ? 1.0 : 0.0;
+}
+
+// transposed operator: Dirichlet rows reset to identity
+__global__ void k_dirichlet_identity(const unsigned char *bnd, int n, const int *rowptr, const int *col, double *val)
+{
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n || !bnd[v]) return;
+    for (int a = rowptr[v]; a < rowptr[v + 1]; ++a) val[a] = (col[a] == v) ? 1.0 : 0.0;
+}
+
+__global__ void k_colour_rows(const int *color, int n, int c, int *rows, int *count)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || color[i] != c) return;
+    rows[atomicAdd(count, 1)] = i;
+}
+
+template <class V>
+__global__ void k_vadd(int n, V *a, const V *b, const int *skip)
+{
+    if (skip && *skip) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] += b[i];
+}
+
+template <class V>
+__global__ void k_zero(int n, V *a, const int *skip)
+{
+    if (skip && *skip) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = (V)0;
+}
+
+// dense inverse of the base matrix through a partially pivoted LU, in the
+// order of LUDecomp / SolveLU (lib_algebra/small_algebra/no_lapack/lu_decomp.h)
+static void dense_lu_inverse(int n, std::vector<double> &M, std::vector<double> &inv)
+{
+    std::vector<int> piv(n);
+    for (int k = 0; k < n; ++k) {
+        int big = k;
+        for (int j = k + 1; j < n; ++j)
+            if (std::fabs(M[(size_t)big * n + k]) < std::fabs(M[(size_t)j * n + k])) big = j;
+        if (big != k)
+            for (int j = 0; j < n; ++j) std::swap(M[(size_t)k * n + j], M[(size_t)big * n + j]);
+        piv[k] = big;
+        UG_REQUIRE(std::fabs(M[(size_t)k * n + k]) >= 1e-10, UG4GB_ERR_SINGULAR,
+                   "GMG base solver: LU pivot below 1e-10 (singular base matrix)");
+        for (int i = k + 1; i < n; ++i) {
+            M[(size_t)i * n + k] = M[(size_t)i * n + k] / M[(size_t)k * n + k];
+            for (int j = k + 1; j < n; ++j) M[(size_t)i * n + j] -= M[(size_t)i * n + k] * M[(size_t)k * n + j];
+        }
+    }
+    inv.assign((size_t)n * n, 0.0);
+    std::vector<double> x(n);
+    for (int col = 0; col < n; ++col) {
+        for (int i = 0; i < n; ++i) x[i] = (i == col) ? 1.0 : 0.0;
+        for (int i = 0; i < n; ++i)
+            if (i < piv[i]) std::swap(x[i], x[piv[i]]);
+        for (int i = 0; i < n; ++i) {
+            double s = x[i];
+            for (int k = 0; k < i; ++k) s -= M[(size_t)i * n + k] * x[k];
+            x[i] = s;
+        }
+        for (int i = n - 1; i >= 0; --i) {
+            double s = x[i];
+            for (int k = i + 1; k < n; ++k) s -= M[(size_t)i * n + k] * x[k];
+            x[i] = s / M[(size_t)i * n + i];
+        }
+        for (int i = 0; i < n; ++i) inv[(size_t)i * n + col] = x[i];
+    }
+}
+
+// ---------------------------------------------------------------- GmgT ---
+template <class V>
+struct GmgT : GmgBase {
+    std::vector<GLevel<V>> lev;
+    int base = 0, nu1 = 2, nu2 = 2, cycle = 1, smoother = 0;
+    DevBuf<double> Ainv;
+    int nbase = 0;
+
+    int top() const override { return (int)lev.size() - 1; }
+    bool is_fp32() const override { return sizeof(V) == 4; }
+    void *sc_top() override { return lev.back().sc.p; }
+    const Csr &P(int l) const override { return lev[l].P; }
+    const Csr &R(int l) const override { return lev[l].R; }
+
+    void setup_level(Ctx &c, GLevel<V> &L, const Level &G, int l, double damp, bool is_base)
+    {
+        int n = L.A.nrows;
+        L.n = n;
+        L.sc.alloc(n);
+        L.dA.alloc(n);
+        L.dB.alloc(n);
+        if (is_base) return;
+        L.w.alloc(n);
+        DevBuf<double> dinv64, dfac64;
+        dinv64.alloc(n);
+        dfac64.alloc(n);
+        UG_LAUNCH(c, k_diag_inv, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp, smoother,
+                  dinv64.p, dfac64.p);
+        L.dinv.alloc(n);
+        L.dfac.alloc(n);
+        UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, dinv64.p, L.dinv.p, n);
+        UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, dfac64.p, L.dfac.p, n);
+        if (smoother == UG4GB_SMOOTHER_JACOBI) {
+            sell_from_csr<V>(c, L.A, L.At, dinv64.p);
+        } else {
+            sell_from_csr<V>(c, L.A, L.At, nullptr);
+            L.t.alloc(n);
+            int ncol = 1 << G.dim;
+            L.crow.resize(ncol);
+            L.ncrow.assign(ncol, 0);
+            DevBuf<int> cnt;
+            cnt.alloc(1);
+            for (int q = 0; q < ncol; ++q) {
+                L.crow[q].alloc(n);
+                UG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int), c.stream));
+                UG_LAUNCH(c, k_colour_rows, div_up(n, 256), 256, 0, G.color.p, n, q, L.crow[q].p, cnt.p);
+                UG_CUDA(cudaMemcpyAsync(&L.ncrow[q], cnt.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+                UG_CUDA(cudaStreamSynchronize(c.stream));
+            }
+        }
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        (void)l;
+    }
+
+    void setup_transfers(Ctx &c, GLevel<V> &F, const Level &Gf, const Level &Gc)
+    {
+        Csr &P = F.P;
+        P.nrows = Gf.nv;
+        P.ncols = Gc.nv;
+        DevBuf<int> len;
+        len.alloc(Gf.nv + 1);
+        UG_CUDA(cudaMemsetAsync(len.p, 0, len.bytes(), c.stream));
+        UG_LAUNCH(c, k_build_P, div_up(Gf.nv, 256), 256, 0, Gf.npar.p, Gf.par.p, Gf.bnd.p, Gf.nv, len.p, (int *)nullptr,
+                  (double *)nullptr, (const int *)nullptr, 0);
+        P.rowptr.alloc(Gf.nv + 1);
+        int64_t nnz = 0;
+        exclusive_scan_int(c, len.p, P.rowptr.p, Gf.nv + 1, &nnz);
+        P.nnz = nnz;
+        P.col.alloc(nnz);
+        P.val.alloc(nnz);
+        UG_LAUNCH(c, k_build_P, div_up(Gf.nv, 256), 256, 0, Gf.npar.p, Gf.par.p, Gf.bnd.p, Gf.nv, (int *)nullptr, P.col.p,
+                  P.val.p, (const int *)P.rowptr.p, 1);
+        csr_transpose(c, P, F.R, true);
+        UG_LAUNCH(c, k_adjust_R, div_up(Gf.nv, 256), 256, 0, Gf.npar.p, Gf.par.p, Gf.bnd.p, Gf.nv, F.R.rowptr.p,
+                  F.R.col.p, F.R.val.p);
+        sell_from_csr<V>(c, F.P, F.Ps, nullptr);
+        sell_from_csr<V>(c, F.R, F.Rs, nullptr);
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+    }
+
+    void setup_base(Ctx &c)
+    {
+        const Csr &A = lev[base].A;
+        int n = A.nrows;
+        UG_REQUIRE(n <= 4096, UG4GB_ERR_INVALID, "GMG base level larger than 4096 unknowns (dense LU limit)");
+        std::vector<int> rp(n + 1), ci(A.nnz);
+        std::vector<double> va(A.nnz);
+        copy_out(c, rp.data(), A.rowptr.p, sizeof(int) * (n + 1));
+        copy_out(c, ci.data(), A.col.p, sizeof(int) * A.nnz);
+        copy_out(c, va.data(), A.val.p, sizeof(double) * A.nnz);
+        std::vector<double> M((size_t)n * n, 0.0), inv;
+        for (int r = 0; r < n; ++r)
+            for (int a = rp[r]; a < rp[r + 1]; ++a) M[(size_t)r * n + ci[a]] = va[a];
+        dense_lu_inverse(n, M, inv);
+        Ainv.alloc((size_t)n * n);
+        copy_in(c, Ainv.p, inv.data(), sizeof(double) * inv.size());
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        nbase = n;
+    }
+
+    // ------------------------------------------------------------ cycle --
+    // level l; dtop = FP64 defect of the top level (r), first = first visit
+    void lmgc(Ctx &c, int l, const double *dtop, bool first, const int *skip, const double *r_rho, RedArgs *red,
+              int rho_kind, bool &rho_done)
+    {
+        const int T = top();
+        GLevel<V> &L = lev[l];
+        if (l == base) {
+            // top == base: a single-level "cycle" is the base solve
+            UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
+            base_solve<V>(c, Ainv.p, nbase, L.dA.p, L.sc.p, skip);
+            return;
+        }
+        GLevel<V> &C = lev[l - 1];
+        const V *cur = (l == T) ? nullptr : L.dcur;
+        // ---- pre-smoothing
+        if (nu1 == 0) {
+            if (first) UG_LAUNCH(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, skip);
+            if (l == T) {
+                UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
+                cur = L.dA.p;
+            }
+        }
+        for (int k = 0; k < nu1; ++k) {
+            V *out = (cur == L.dA.p) ? L.dB.p : L.dA.p;
+            if (l == T && k == 0) out = L.dB.p;
+            int mode = (k == 0) ? (first ? SC_SET_FROM_BASE : SC_ADD_FROM_BASE) : SC_ADD_FROM_BASE;
+            if (smoother == UG4GB_SMOOTHER_JACOBI) {
+                if (l == T && k == 0)
+                    smooth_step<V, double, double>(c, L.At, dtop, dtop, L.dinv.p, L.sc.p, out, mode, skip, nullptr,
+                                                   nullptr, 0);
+                else
+                    smooth_step<V, V, V>(c, L.At, cur, cur, L.dinv.p, L.sc.p, out, mode, skip, nullptr, nullptr, 0);
+            } else {
+                if (l == T && k == 0) {
+                    gs_sweep(c, L, dtop, skip);
+                    residual_update<V, double>(c, L.At, L.t.p, dtop, out, L.sc.p, mode == SC_SET_FROM_BASE ? 1 : 0,
+                                               skip);
+                } else {
+                    gs_sweep(c, L, cur, skip);
+                    residual_update<V, V>(c, L.At, L.t.p, cur, out, L.sc.p, mode == SC_SET_FROM_BASE ? 1 : 0, skip);
+                }
+            }
+            cur = out;
+        }
+        const V *dpre = cur;
+        // ---- restriction
+        restrict_apply<V>(c, L.Rs, dpre, C.dA.p, skip);
+        C.dcur = C.dA.p;
+        // ---- coarse correction
+        if (l - 1 == base) {
+            base_solve<V>(c, Ainv.p, nbase, C.dA.p, C.sc.p, skip);
+        } else {
+            for (int i = 0; i < cycle; ++i) {
+                bool rd = false;
+                lmgc(c, l - 1, nullptr, i == 0, skip, nullptr, nullptr, 0, rd);
+            }
+        }
+        // ---- prolongation + post-smoothing
+        prolong_apply<V>(c, L.Ps, C.sc.p, L.sc.p, L.dfac.p, nu2 > 0 ? L.w.p : (V *)nullptr, skip);
+        const V *dbase = dpre;
+        if (smoother == UG4GB_SMOOTHER_JACOBI) {
+            for (int k = 0; k < nu2; ++k) {
+                const V *x = (k == 0) ? L.w.p : dbase;
+                bool need_out = (k < nu2 - 1) || (l != T && cycle > 1);
+                V *out = need_out ? ((dbase == L.dA.p) ? L.dB.p : L.dA.p) : nullptr;
+                bool last_top = (l == T && k == nu2 - 1 && r_rho);
+                smooth_step<V, V, V>(c, L.At, x, dbase, L.dinv.p, L.sc.p, out, SC_ADD_FROM_NEW, skip,
+                                     last_top ? r_rho : nullptr, last_top ? red : nullptr, rho_kind);
+                if (last_top) rho_done = true;
+                if (out) dbase = out;
+            }
+        } else {
+            for (int k = 0; k < nu2; ++k) {
+                const V *tprev = (k == 0) ? L.w.p : L.t.p;
+                V *out = (dbase == L.dA.p) ? L.dB.p : L.dA.p;
+                residual_update<V, V>(c, L.At, tprev, dbase, out, L.sc.p, k == 0 ? 2 : 0, skip);
+                gs_sweep(c, L, out, skip);
+                dbase = out;
+            }
+            if (nu2 > 0) UG_LAUNCH(c, k_vadd<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, L.t.p, skip);
+        }
+        L.dcur = const_cast<V *>(dbase);
+    }
+
+    template <class DT>
+    void gs_sweep(Ctx &c, GLevel<V> &L, const DT *d, const int *skip)
+    {
+        const V *dv;
+        if constexpr (sizeof(DT) == sizeof(V)) {
+            dv = (const V *)d;
+        } else {
+            // FP64 top defect into the FP32 level: convert once into w
+            UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, (const double *)d, L.w.p, L.n);
+            dv = L.w.p;
+        }
+        UG_LAUNCH(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.t.p, skip);
+        for (size_t q = 0; q < L.crow.size(); ++q)
+            if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], L.dinv.p, dv, L.t.p, skip);
+    }
+
+    bool apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red, int rho_kind) override
+    {
+        bool rho_done = false;
+        lmgc(c, top(), dtop, true, skip, r_rho, red, rho_kind, rho_done);
+        return rho_done;
+    }
+};
+
+template <class V>
+static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
+{
+    Ctx &c = m->ctx->c;
+    const ug4gb_grid *g = m->disc->g;
+    int nl = (int)g->lev.size();
+    auto *G = new GmgT<V>;
+    std::unique_ptr<GmgT<V>> guard(G);
+    G->base = m->base;
+    G->nu1 = m->nu1;
+    G->nu2 = m->nu2;
+    G->cycle = m->cycle;
+    G->smoother = m->smoother;
+    G->lev.resize(nl);
+    UG_REQUIRE(m->base >= 0 && m->base < nl, UG4GB_ERR_INVALID, "GMG: base level out of range");
+    UG_REQUIRE(A_top->A.nrows == g->lev[nl - 1].nv, UG4GB_ERR_INVALID, "GMG: top operator size != top level");
+    for (int l = m->base; l < nl; ++l) {
+        GLevel<V> &L = G->lev[l];
+        // level operator: copy of the surface operator on the top level,
+        // re-assembled on coarser levels (assemble_level_operator, :528-750)
+        if (l == nl - 1) {
+            csr_copy(c, A_top->A, L.A);
+        } else {
+            ug4gb_matrix tmp;
+            tmp.ctx = m->ctx;
+            disc_assemble(m->disc, l, &tmp, nullptr);
+            L.A = std::move(tmp.A);
+        }
+        if (m->transposed) {
+            Csr T;
+            csr_transpose(c, L.A, T, true);
+            UG_LAUNCH(c, k_dirichlet_identity, div_up(T.nrows, 256), 256, 0, g->lev[l].bnd.p, T.nrows, T.rowptr.p,
+                      T.col.p, T.val.p);
+            L.A = std::move(T);
+        }
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
+        if (l > m->base) G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
+    }
+    G->setup_base(c);
+    return guard.release();
+}
+
+}  // namespace ug4gb
+
+template <class F>
+static int guarded(ug4gb_ctx *ctx, F &&f)
+{
+    try {
+        f();
+        return UG4GB_OK;
+    } catch (const Error &e) {
+        if (ctx) ctx->c.err = e.msg;
+        return e.code;
+    } catch (const std::exception &e) {
+        if (ctx) ctx->c.err = e.what();
+        return UG4GB_ERR_INVALID;
+    }
+}
+
+static void drop_graph(ug4gb_gmg *m)
+{
+    if (m->graph) cudaGraphExecDestroy(m->graph);
+    m->graph = nullptr;
+    m->graph_d = nullptr;
+    m->graph_c = nullptr;
+}
+
+extern "C" {
+
+int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out)
+{
+    if (!ctx || !disc || !out) return UG4GB_ERR_INVALID;
+    ug4gb_gmg *m = new ug4gb_gmg;
+    m->ctx = ctx;
+    m->disc = disc;
+    *out = m;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp)
+{
+    if (!m || (kind != UG4GB_SMOOTHER_JACOBI && kind != UG4GB_SMOOTHER_MCGS) || !(damp > 0.0)) return UG4GB_ERR_INVALID;
+    m->smoother = kind;
+    m->damp = damp;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_cycle_type(ug4gb_gmg *m, int cycle)
+{
+    if (!m || (cycle != 1 && cycle != 2)) return UG4GB_ERR_INVALID;
+    m->cycle = cycle;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_num_presmooth(ug4gb_gmg *m, int n)
+{
+    if (!m || n < 0 || n > 16) return UG4GB_ERR_INVALID;
+    m->nu1 = n;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_num_postsmooth(ug4gb_gmg *m, int n)
+{
+    if (!m || n < 0 || n > 16) return UG4GB_ERR_INVALID;
+    m->nu2 = n;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_base_level(ug4gb_gmg *m, int level)
+{
+    if (!m || level < 0) return UG4GB_ERR_INVALID;
+    m->base = level;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_precision(ug4gb_gmg *m, int precision)
+{
+    if (!m || (precision != UG4GB_PREC_FP64 && precision != UG4GB_PREC_MIXED)) return UG4GB_ERR_INVALID;
+    m->precision = precision;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed)
+{
+    if (!m) return UG4GB_ERR_INVALID;
+    m->transposed = transposed ? 1 : 0;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
+{
+    if (!m || !A_top) return UG4GB_ERR_INVALID;
+    return guarded(m->ctx, [&] {
+        drop_graph(m);
+        m->impl.reset();
+        m->gen++;
+        if (m->precision == UG4GB_PREC_FP64) m->impl.reset(build_gmg<double>(m, A_top));
+        else m->impl.reset(build_gmg<float>(m, A_top));
+        m->n_top = A_top->A.nrows;
+    });
+}
+
+int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
+{
+    if (!m || !cvec || !d) return UG4GB_ERR_INVALID;
+    if (!m->impl) {
+        m->ctx->c.err = "ug4gb_gmg_apply: init() not called";
+        return UG4GB_ERR_STATE;
+    }
+    if (cvec->n != m->n_top || d->n != m->n_top) return UG4GB_ERR_INVALID;
+    return guarded(m->ctx, [&] {
+        Ctx &c = m->ctx->c;
+        if (!m->graph || m->graph_d != d->d || m->graph_c != cvec->d) {
+            drop_graph(m);
+            cudaGraph_t gr;
+            int64_t before = c.launches;
+            UG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                m->impl->apply(c, d->d, nullptr, nullptr, nullptr, 0);
+                if (m->impl->is_fp32()) copy_z<float>(c, m->n_top, (const float *)m->impl->sc_top(), cvec->d, nullptr);
+                else copy_z<double>(c, m->n_top, (const double *)m->impl->sc_top(), cvec->d, nullptr);
+            } catch (...) {
+                cudaStreamEndCapture(c.stream, &gr);
+                throw;
+            }
+            UG_CUDA(cudaStreamEndCapture(c.stream, &gr));
+            m->graph_kernels = c.launches - before;
+            c.launches = before;
+            UG_CUDA(cudaGraphInstantiate(&m->graph, gr, 0));
+            cudaGraphDestroy(gr);
+            m->graph_d = d->d;
+            m->graph_c = cvec->d;
+        }
+        UG_CUDA(cudaGraphLaunch(m->graph, c.stream));
+        c.launches += m->graph_kernels;
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+    });
+}
+
+int ug4gb_gmg_transfer_info(const ug4gb_gmg *m, int level, int which, int *nrows, int *ncols, int64_t *nnz)
+{
+    if (!m || !m->impl || level <= m->base || level > m->impl->top()) return UG4GB_ERR_INVALID;
+    const Csr &A = which ? m->impl->R(level) : m->impl->P(level);
+    if (nrows) *nrows = A.nrows;
+    if (ncols) *ncols = A.ncols;
+    if (nnz) *nnz = A.nnz;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_export_transfer(const ug4gb_gmg *m, int level, int which, int *rowptr, int *col, double *val)
+{
+    if (!m || !m->impl || level <= m->base || level > m->impl->top()) return UG4GB_ERR_INVALID;
+    return guarded(m->ctx, [&] {
+        Ctx &c = m->ctx->c;
+        const Csr &A = which ? m->impl->R(level) : m->impl->P(level);
+        if (rowptr) copy_out(c, rowptr, A.rowptr.p, sizeof(int) * (size_t)(A.nrows + 1));
+        if (col) copy_out(c, col, A.col.p, sizeof(int) * (size_t)A.nnz);
+        if (val) copy_out(c, val, A.val.p, sizeof(double) * (size_t)A.nnz);
+    });
+}
+
+void ug4gb_gmg_destroy(ug4gb_gmg *m)
+{
+    if (!m) return;
+    cudaStreamSynchronize(m->ctx->c.stream);
+    drop_graph(m);
+    delete m;
+}
+
+}  // extern "C"

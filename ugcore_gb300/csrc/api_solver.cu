@@ -1,0 +1,305 @@
+// api_solver.cu -- CG / BiCGStab drivers with StdConvCheck on the device.
+//
+// One Krylov iteration (preconditioner cycle included) is captured once as a
+// CUDA graph and replayed; all scalars (alpha, beta, rho, omega, defects)
+// stay in device memory and every kernel of an iteration returns at once
+// when the convergence flag is set, so the host only reads one int per
+// iteration to decide whether to replay again.  The iteration count, defect
+// history and stopping rule are those of the reference loop
+// (lib_algebra/operator/linear_solver/cg.h:103-230,
+//  lib_algebra/operator/linear_solver/bicgstab.h:112-400,
+//  lib_algebra/operator/convergence_check_impl.h:85-172).
+#include <cstring>
+
+#include "gmg.cuh"
+
+using namespace ug4gb;
+
+template <class F>
+static int guarded(ug4gb_ctx *ctx, F &&f)
+{
+    try {
+        f();
+        return UG4GB_OK;
+    } catch (const Error &e) {
+        if (ctx) ctx->c.err = e.msg;
+        return e.code;
+    } catch (const std::exception &e) {
+        if (ctx) ctx->c.err = e.what();
+        return UG4GB_ERR_INVALID;
+    }
+}
+
+static void drop_graph(ug4gb_solver *s)
+{
+    if (s->iter_graph) cudaGraphExecDestroy(s->iter_graph);
+    s->iter_graph = nullptr;
+    s->graph_x = nullptr;
+}
+
+namespace {
+
+// RedArgs for the solver's scalar block (its own counter slot)
+RedArgs red_of(ug4gb_solver *s)
+{
+    Ctx &c = s->ctx->c;
+    return RedArgs{c.red_partials.p, c.red_counter.p, s->ks.p};
+}
+
+// z = M d (or z = d without preconditioner); rho fused when possible
+template <class ZT>
+const ZT *precond(ug4gb_solver *s, const double *d, const double *r_rho, int rho_kind)
+{
+    Ctx &c = s->ctx->c;
+    RedArgs red = red_of(s);
+    const int *skip = &s->ks.p->done;
+    if (!s->pre) {
+        if (r_rho) rho_dot<double>(c, s->n, d, r_rho, rho_kind, red);
+        return (const ZT *)d;
+    }
+    bool fused = s->pre->impl->apply(c, d, skip, r_rho, &red, rho_kind);
+    const ZT *z = (const ZT *)s->pre->impl->sc_top();
+    if (r_rho && !fused) rho_dot<ZT>(c, s->n, z, r_rho, rho_kind, red);
+    return z;
+}
+
+template <class ZT>
+void cg_iteration(ug4gb_solver *s, double *x, double *r, bool first)
+{
+    Ctx &c = s->ctx->c;
+    RedArgs red = red_of(s);
+    const ZT *z = precond<ZT>(s, r, r, first ? 0 : 1);
+    cg_spmv_dot_t<ZT>(c, s->A->sell, z, s->p.p, s->q.p, first ? 1 : 0, red);
+    cg_update(c, s->n, x, r, s->p.p, s->q.p, red);
+}
+
+template <class ZT>
+void bicg_iteration(ug4gb_solver *s, double *x, double *r)
+{
+    Ctx &c = s->ctx->c;
+    RedArgs red = red_of(s);
+    const int n = s->n;
+    bicg_restart(c, n, r, s->r0.p, s->p.p, s->v.p, red);
+    bicg_rho(c, n, s->r0.p, r, red);
+    bicg_p(c, n, r, s->p.p, s->v.p, red);
+    const ZT *q = precond<ZT>(s, s->p.p, nullptr, 0);
+    bicg_spmv_dot_t<ZT>(c, s->A->sell, q, s->v.p, s->r0.p, red);
+    bicg_x_s<ZT>(c, n, x, q, r, s->v.p, s->s.p, red);
+    bicg_s_to_r(c, n, s->s.p, r, red);
+    q = precond<ZT>(s, s->s.p, nullptr, 0);
+    bicg_spmv_2dot_t<ZT>(c, s->A->sell, q, s->t.p, s->s.p, red);
+    bicg_x_r<ZT>(c, n, x, q, s->s.p, s->t.p, r, red);
+}
+
+bool z_is_fp32(ug4gb_solver *s) { return s->pre && s->pre->impl->is_fp32(); }
+
+void read_flags(ug4gb_solver *s, int *done)
+{
+    Ctx &c = s->ctx->c;
+    UG_CUDA(cudaMemcpyAsync(c.host_pinned, &s->ks.p->done, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    UG_CUDA(cudaStreamSynchronize(c.stream));
+    *done = *(int *)c.host_pinned;
+}
+
+void run(ug4gb_solver *s, double *x, double *r)
+{
+    Ctx &c = s->ctx->c;
+    UG_REQUIRE(s->A, UG4GB_ERR_STATE, "solver: init() not called");
+    UG_REQUIRE(!s->pre || s->pre->impl, UG4GB_ERR_STATE, "solver: preconditioner not initialised");
+    UG_REQUIRE(!s->pre || s->pre->n_top == s->n, UG4GB_ERR_INVALID, "solver: preconditioner size mismatch");
+    // device scalars + history
+    KScal h{};
+    h.maxit = s->maxit;
+    h.min_def = s->min_def;
+    h.rel_red = s->rel_red;
+    h.hist_cap = s->maxit + 2;
+    s->hist.alloc(h.hist_cap);
+    h.hist = s->hist.p;
+    UG_CUDA(cudaMemcpyAsync(s->ks.p, &h, sizeof(KScal), cudaMemcpyHostToDevice, c.stream));
+    RedArgs red = red_of(s);
+    const bool f32 = z_is_fp32(s);
+    // prologue: r = b - A x, start the check; CG also does the first step
+    krylov_start(c, s->A->sell, x, r, red);
+    if (s->kind == UG4GB_SOLVER_CG) {
+        if (f32) cg_iteration<float>(s, x, r, true);
+        else cg_iteration<double>(s, x, r, true);
+    }
+    int done = 0;
+    read_flags(s, &done);
+    if (!done) {
+        int pre_gen = s->pre ? s->pre->gen : -1;
+        if (!s->iter_graph || s->graph_x != x || s->graph_r != r || s->graph_pre_gen != pre_gen) {
+            drop_graph(s);
+            cudaGraph_t gr;
+            int64_t before = c.launches;
+            UG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                if (s->kind == UG4GB_SOLVER_CG) {
+                    if (f32) cg_iteration<float>(s, x, r, false);
+                    else cg_iteration<double>(s, x, r, false);
+                } else {
+                    if (f32) bicg_iteration<float>(s, x, r);
+                    else bicg_iteration<double>(s, x, r);
+                }
+            } catch (...) {
+                cudaStreamEndCapture(c.stream, &gr);
+                throw;
+            }
+            UG_CUDA(cudaStreamEndCapture(c.stream, &gr));
+            s->iter_kernels = c.launches - before;
+            c.launches = before;
+            UG_CUDA(cudaGraphInstantiate(&s->iter_graph, gr, 0));
+            cudaGraphDestroy(gr);
+            s->graph_x = x;
+            s->graph_r = r;
+            s->graph_pre_gen = pre_gen;
+        }
+        while (!done) {
+            UG_CUDA(cudaGraphLaunch(s->iter_graph, c.stream));
+            c.launches += s->iter_kernels;
+            read_flags(s, &done);
+        }
+    }
+    UG_CUDA(cudaMemcpyAsync(&s->host_ks, s->ks.p, sizeof(KScal), cudaMemcpyDeviceToHost, c.stream));
+    UG_CUDA(cudaStreamSynchronize(c.stream));
+    int nh = s->host_ks.step + 1 < h.hist_cap ? s->host_ks.step + 1 : h.hist_cap;
+    s->host_hist.resize(nh);
+    copy_out(c, s->host_hist.data(), s->hist.p, sizeof(double) * nh);
+    const KScal &k = s->host_ks;
+    bool converged = (k.dcur < k.min_def) || (k.dcur / k.d0 < k.rel_red);
+    if (k.fail) {
+        s->last_rc = UG4GB_ERR_BREAKDOWN;
+        throw Error{UG4GB_ERR_BREAKDOWN, "Krylov solver breakdown (zero denominator)"};
+    }
+    if (!converged) {
+        s->last_rc = UG4GB_ERR_NOT_CONVERGED;
+        throw Error{UG4GB_ERR_NOT_CONVERGED, "Krylov solver: maximum number of steps reached without convergence"};
+    }
+    s->last_rc = UG4GB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ug4gb_solver_create(ug4gb_ctx *ctx, int kind, ug4gb_solver **out)
+{
+    if (!ctx || !out || (kind != UG4GB_SOLVER_CG && kind != UG4GB_SOLVER_BICGSTAB)) return UG4GB_ERR_INVALID;
+    ug4gb_solver *s = new ug4gb_solver;
+    s->ctx = ctx;
+    s->kind = kind;
+    int rc = guarded(ctx, [&] { s->ks.alloc(1); });
+    if (rc != UG4GB_OK) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return UG4GB_OK;
+}
+
+int ug4gb_solver_set_preconditioner(ug4gb_solver *s, ug4gb_gmg *m)
+{
+    if (!s) return UG4GB_ERR_INVALID;
+    drop_graph(s);
+    s->pre = m;
+    return UG4GB_OK;
+}
+
+int ug4gb_solver_set_convergence_check(ug4gb_solver *s, int maxit, double min_def, double rel_red)
+{
+    if (!s || maxit < 0) return UG4GB_ERR_INVALID;
+    drop_graph(s);
+    s->maxit = maxit;
+    s->min_def = min_def;
+    s->rel_red = rel_red;
+    return UG4GB_OK;
+}
+
+int ug4gb_solver_init(ug4gb_solver *s, const ug4gb_matrix *A)
+{
+    if (!s || !A || A->A.nrows != A->A.ncols) return UG4GB_ERR_INVALID;
+    return guarded(s->ctx, [&] {
+        drop_graph(s);
+        ug4gb_matrix *Am = const_cast<ug4gb_matrix *>(A);
+        Am->ensure_sell();
+        s->A = A;
+        s->n = A->A.nrows;
+        size_t n = s->n > 0 ? s->n : 1;
+        s->p.alloc(n);
+        s->q.alloc(n);
+        s->r.alloc(n);
+        if (s->kind == UG4GB_SOLVER_BICGSTAB) {
+            s->r0.alloc(n);
+            s->v.alloc(n);
+            s->s.alloc(n);
+            s->t.alloc(n);
+        }
+        UG_CUDA(cudaStreamSynchronize(s->ctx->c.stream));
+    });
+}
+
+int ug4gb_solver_apply_return_defect(ug4gb_solver *s, ug4gb_vector *x, ug4gb_vector *b)
+{
+    if (!s || !x || !b || x->n != s->n || b->n != s->n) return UG4GB_ERR_INVALID;
+    return guarded(s->ctx, [&] { run(s, x->d, b->d); });
+}
+
+int ug4gb_solver_apply(ug4gb_solver *s, ug4gb_vector *x, const ug4gb_vector *b)
+{
+    if (!s || !x || !b || x->n != s->n || b->n != s->n) return UG4GB_ERR_INVALID;
+    return guarded(s->ctx, [&] {
+        UG_CUDA(cudaMemcpyAsync(s->r.p, b->d, sizeof(double) * (size_t)s->n, cudaMemcpyDeviceToDevice,
+                                s->ctx->c.stream));
+        run(s, x->d, s->r.p);
+    });
+}
+
+int ug4gb_solver_solve_host(ug4gb_solver *s, const double *b_host, double *x_host)
+{
+    if (!s || !b_host || !x_host) return UG4GB_ERR_INVALID;
+    return guarded(s->ctx, [&] {
+        Ctx &c = s->ctx->c;
+        if (!s->zcopy.p || (int)s->zcopy.n != s->n) s->zcopy.alloc(s->n > 0 ? s->n : 1);
+        UG_CUDA(cudaMemcpyAsync(s->r.p, b_host, sizeof(double) * (size_t)s->n, cudaMemcpyHostToDevice, c.stream));
+        UG_CUDA(cudaMemsetAsync(s->zcopy.p, 0, sizeof(double) * (size_t)s->n, c.stream));
+        int rc_inner = UG4GB_OK;
+        try {
+            run(s, s->zcopy.p, s->r.p);
+        } catch (const Error &e) {
+            rc_inner = e.code;
+            c.err = e.msg;
+        }
+        UG_CUDA(cudaMemcpyAsync(x_host, s->zcopy.p, sizeof(double) * (size_t)s->n, cudaMemcpyDeviceToHost, c.stream));
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        if (rc_inner != UG4GB_OK) throw Error{rc_inner, c.err};
+    });
+}
+
+int ug4gb_solver_get_stats(const ug4gb_solver *s, int *steps, double *d0, double *d1, int *converged)
+{
+    if (!s) return UG4GB_ERR_INVALID;
+    const KScal &k = s->host_ks;
+    if (steps) *steps = k.step;
+    if (d0) *d0 = k.d0;
+    if (d1) *d1 = k.dcur;
+    if (converged) *converged = (k.dcur < k.min_def) || (k.dcur / k.d0 < k.rel_red);
+    return UG4GB_OK;
+}
+
+int ug4gb_solver_get_history(const ug4gb_solver *s, double *hist, int cap)
+{
+    if (!s || !hist) return UG4GB_ERR_INVALID;
+    int n = (int)s->host_hist.size() < cap ? (int)s->host_hist.size() : cap;
+    std::memcpy(hist, s->host_hist.data(), sizeof(double) * (size_t)n);
+    return n;
+}
+
+void ug4gb_solver_destroy(ug4gb_solver *s)
+{
+    if (!s) return;
+    cudaStreamSynchronize(s->ctx->c.stream);
+    drop_graph(s);
+    delete s;
+}
+
+}  // extern "C"

@@ -1,0 +1,238 @@
+// common.cuh -- internal types and helpers of libug4gb (sm_103a).
+//
+// Device data layout (all levels resident in HBM):
+//   grid level   coords  nv*dim FP64 (AoS), elems ne*k int32 (corners in
+//                reference order), bnd nv uint8, parents nv*8 int32 + npar.
+//   CRS          rowptr (n+1) int32, col nnz int32 (sorted per row),
+//                val nnz FP64 -- the defragmented ug::SparseMatrix form.
+//   SELL-32      slices of 32 consecutive rows; slice s stores width w_s =
+//                max row length, entries column-major inside the slice
+//                (entry k of row 32s+lane at sptr[s] + 32k + lane), padded
+//                with (col = a valid column, val = 0).  Thread-per-row loads
+//                are fully coalesced (32 x 4 or 8 bytes per k).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/ug4gb.h"
+
+namespace ug4gb {
+
+struct Error {
+    int code;
+    std::string msg;
+};
+
+#define UG_CUDA(call)                                                                              \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            throw ::ug4gb::Error{e_ == cudaErrorMemoryAllocation ? UG4GB_ERR_NOMEM : UG4GB_ERR_CUDA, \
+                                 std::string(#call) + ": " + cudaGetErrorString(e_)};              \
+    } while (0)
+
+#define UG_REQUIRE(cond, code, text)                                                               \
+    do {                                                                                           \
+        if (!(cond)) throw ::ug4gb::Error{(code), std::string(text)};                             \
+    } while (0)
+
+// Owning device buffer (move-only).
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf &operator=(DevBuf &&o) noexcept
+    {
+        if (this != &o) { release(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count)
+    {
+        if (count == n && p) return;
+        release();
+        if (count == 0) return;
+        UG_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+        n = count;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+struct Ctx {
+    int device = 0;
+    int num_sms = 152;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int64_t launches = 0;
+    // grid-reduction scratch: partial sums per block and a completion counter
+    DevBuf<double> red_partials;        // kRedMaxBlocks * kRedMaxValues
+    DevBuf<unsigned int> red_counter;   // one counter per reduction slot
+    DevBuf<double> red_result;          // results of plain reductions
+    double *host_pinned = nullptr;      // small pinned readback area
+};
+
+constexpr int kRedMaxBlocks = 16384;
+constexpr int kRedMaxValues = 2;
+constexpr int kSliceH = 32;
+
+// Kernel launch accounting; every launch of the library goes through this.
+#define UG_LAUNCH(ctx, kernel, grid, block, shmem, ...)                                            \
+    do {                                                                                           \
+        kernel<<<(grid), (block), (shmem), (ctx).stream>>>(__VA_ARGS__);                           \
+        (ctx).launches++;                                                                          \
+        UG_CUDA(cudaGetLastError());                                                               \
+    } while (0)
+
+inline unsigned div_up(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
+
+// --------------------------------------------------------------- CRS/SELL --
+struct Csr {
+    int nrows = 0, ncols = 0;
+    int64_t nnz = 0;
+    DevBuf<int> rowptr, col;
+    DevBuf<double> val;
+};
+
+template <class T>
+struct Sell {
+    int nrows = 0, ncols = 0, nslices = 0;
+    int64_t stored = 0;     // padded entry count
+    DevBuf<int> sptr;       // nslices + 1
+    DevBuf<int> swidth;     // nslices
+    DevBuf<int> col;        // stored
+    DevBuf<T> val;          // stored
+};
+
+template <class T>
+struct SellView {
+    int nrows;
+    const int *__restrict__ sptr;
+    const int *__restrict__ swidth;
+    const int *__restrict__ col;
+    const T *__restrict__ val;
+};
+
+template <class T>
+inline SellView<T> view(const Sell<T> &s)
+{
+    return SellView<T>{s.nrows, s.sptr.p, s.swidth.p, s.col.p, s.val.p};
+}
+
+// ------------------------------------------------------------- grid level --
+struct Level {
+    int elem_type = 0, dim = 2, k = 4;
+    int nx = 0, ny = 0, nz = 1, nv = 0, ne = 0;
+    DevBuf<double> coords;
+    DevBuf<int> elems;
+    DevBuf<unsigned char> bnd;
+    DevBuf<int> npar, par;       // parents in the next coarser level
+    DevBuf<int> color;           // parity colour of each vertex
+};
+
+// ------------------------------------------------------ device utilities --
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Streaming loads of matrix data: read once per sweep, keep L1/L2 for vectors.
+__device__ __forceinline__ double ld_stream(const double *p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const float *p) { return __ldcs(p); }
+__device__ __forceinline__ int ld_stream(const int *p) { return __ldcs(p); }
+
+// Deterministic grid-wide sum of NV values per thread.  Each block reduces
+// in a fixed tree, writes its partials, and the last block to finish sums
+// the partials in block order and calls fin(total) with thread 0.
+template <int NT, int NV, class Fin>
+__device__ __forceinline__ void grid_reduce(const double (&v)[NV], double *partials, unsigned int *counter,
+                                            Fin fin)
+{
+    __shared__ double sh[NV][NT / 32];
+    __shared__ bool is_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = warp_sum(v[q]);
+        if (lane == 0) sh[q][warp] = s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = (lane < NT / 32) ? sh[q][lane] : 0.0;
+            s = warp_sum(s);
+            if (lane == 0) partials[q * kRedMaxBlocks + blockIdx.x] = s;
+        }
+        if (lane == 0) {
+            __threadfence();
+            unsigned t = atomicAdd(counter, 1u);
+            is_last = (t == gridDim.x - 1);
+        }
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double tot[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) {
+        double s = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += NT) s += __ldcg(partials + q * kRedMaxBlocks + b);
+        s = warp_sum(s);
+        if (lane == 0) sh[q][warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = 0.0;
+            for (int w = 0; w < NT / 32; ++w) s += sh[q][w];
+            tot[q] = s;
+        }
+        *counter = 0u;
+        fin(tot);
+    }
+}
+
+// splitmix64 counter hash -> U[0,1), identical to the oracle's generator.
+__host__ __device__ __forceinline__ double hash_uniform(uint64_t seed, uint64_t i)
+{
+    uint64_t z = (seed ^ (i * 0xD1B54A32D192ED03ULL)) + 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z = z ^ (z >> 31);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// ----------------------------------------------------- host-side helpers --
+bool is_device_ptr(const void *p);
+// copies n elements from a host-or-device pointer into device memory
+void copy_in(Ctx &c, void *dst_dev, const void *src, size_t bytes);
+void copy_out(Ctx &c, void *dst, const void *src_dev, size_t bytes);
+
+// kernels shared between translation units
+void exclusive_scan_int(Ctx &c, const int *in, int *out, int n, int64_t *total_out);
+void csr_from_elements(Ctx &c, const Level &L, Csr &A);
+void csr_transpose(Ctx &c, const Csr &B, Csr &T, bool keep_zeros);
+void csr_copy(Ctx &c, const Csr &src, Csr &dst);
+template <class T>
+void sell_from_csr(Ctx &c, const Csr &A, Sell<T> &S, const double *col_scale /* nullable */);
+void fill_double(Ctx &c, double *p, size_t n, double v);
+
+}  // namespace ug4gb

@@ -1,0 +1,35 @@
+// disc.cuh -- launch interface of the FV1 assembly / coefficient / gradient
+// kernels (k_fv1.cu) used by the host orchestration.
+#pragma once
+
+#include "common.cuh"
+
+namespace ug4gb {
+
+struct AsmArgs {
+    const double *coords;
+    const int *elems;
+    int ne;
+    const double *K;          // per element
+    const double *f;          // per vertex or null
+    uint64_t f_seed;          // seeded uniform source when use_seed
+    int use_seed;
+    int vmodes;               // velocity field (3D curl form), 0 = none
+    const double *vk, *vc, *vphase;
+    double vscale;
+    const int *rowptr;        // level CRS to scatter into
+    const int *col;
+    double *val;
+    double *b;                // rhs or null
+};
+
+void launch_assemble(Ctx &c, const Level &L, const AsmArgs &a);
+void launch_dirichlet(Ctx &c, const Level &L, Csr &A, double *b);
+void launch_coef_fourier(Ctx &c, const Level &L, int nmodes, const double *k, const double *phase, double amp,
+                         double factor, double *K);
+void coarsen_log(Ctx &c, const Level &F, const Level &Cl, const double *logf, double *logc);
+void exp_elements(Ctx &c, const double *m, int n, double *K);
+void launch_grad_logk(Ctx &c, const Level &L, const double *K, const double *u, const double *lam, double *g);
+void launch_grad_source(Ctx &c, const Level &L, const double *lam, double *g);
+
+}  // namespace ug4gb

@@ -1,0 +1,137 @@
+// gmg.cuh -- host-side objects behind the C ABI handles.
+#pragma once
+
+#include <memory>
+
+#include "common.cuh"
+#include "k_solve.cuh"
+
+struct ug4gb_ctx {
+    ug4gb::Ctx c;
+};
+
+struct ug4gb_grid {
+    ug4gb_ctx *ctx = nullptr;
+    int elem_type = 0;
+    std::vector<ug4gb::Level> lev;
+};
+
+struct ug4gb_vector {
+    ug4gb_ctx *ctx = nullptr;
+    int n = 0;
+    double *d = nullptr;
+    ug4gb::DevBuf<double> own;
+};
+
+struct ug4gb_matrix {
+    ug4gb_ctx *ctx = nullptr;
+    ug4gb::Csr A;
+    ug4gb::Sell<double> sell;
+    bool sell_valid = false;
+    const void *pattern_grid = nullptr;   // grid/level whose element pattern A holds
+    int pattern_level = -1;
+    void ensure_sell()
+    {
+        if (!sell_valid) {
+            ug4gb::sell_from_csr<double>(ctx->c, A, sell, nullptr);
+            sell_valid = true;
+        }
+    }
+};
+
+namespace ug4gb {
+
+enum CoefKind { COEF_CONST = 0, COEF_FOURIER = 1, COEF_LOG_ELEMS = 2 };
+
+struct DiscImpl {
+    int coef_kind = COEF_CONST;
+    double K_const = 1.0;
+    int kmodes = 0;
+    DevBuf<double> kk, kphase;
+    double kamp = 1.0, kfactor = 1.0;
+    DevBuf<double> m_top;                  // COEF_LOG_ELEMS
+    std::vector<DevBuf<double>> Klev;      // cache per level
+    std::vector<bool> Kvalid;
+    int vmodes = 0;
+    DevBuf<double> vk, vc, vphase;
+    double vscale = 1.0;
+    int upwind = 0;
+    DevBuf<double> f_top;
+    int f_kind = 0;                        // 0 none, 1 array, 2 seeded uniform
+    uint64_t f_seed = 0;
+};
+
+template <class V>
+struct GLevel {
+    int n = 0;
+    Csr A;                       // FP64 level operator
+    Sell<V> At;                  // Jacobi: A * diag(dinv); MCGS: A
+    DevBuf<V> dinv, dfac;        // Jacobi: dinv = 1/(a_ii/damp), dfac = a_ii/damp; MCGS: relax/a_ii, 1
+    Csr P, R;                    // P: this x coarse, R: coarse x this (FP64, exportable)
+    Sell<V> Ps, Rs;
+    DevBuf<V> sc, dA, dB, w, t;
+    V *dcur = nullptr;
+    std::vector<DevBuf<int>> crow;   // MCGS colour row lists
+    std::vector<int> ncrow;
+};
+
+struct GmgBase {
+    virtual ~GmgBase() = default;
+    virtual int top() const = 0;
+    virtual bool is_fp32() const = 0;
+    virtual void *sc_top() = 0;
+    // z = M d_top (d_top FP64, device); rho fused with r_rho if possible.
+    // returns true if rho was computed
+    virtual bool apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
+                       int rho_kind) = 0;
+    virtual const Csr &P(int l) const = 0;
+    virtual const Csr &R(int l) const = 0;
+};
+
+}  // namespace ug4gb
+
+struct ug4gb_disc {
+    ug4gb_ctx *ctx = nullptr;
+    const ug4gb_grid *g = nullptr;
+    ug4gb::DiscImpl d;
+};
+
+struct ug4gb_gmg {
+    ug4gb_ctx *ctx = nullptr;
+    ug4gb_disc *disc = nullptr;
+    int smoother = UG4GB_SMOOTHER_JACOBI;
+    double damp = 0.6;
+    int cycle = 1, nu1 = 2, nu2 = 2, base = 0;
+    int precision = UG4GB_PREC_FP64;
+    int transposed = 0;
+    std::unique_ptr<ug4gb::GmgBase> impl;
+    int n_top = 0;
+    int gen = 0;                 // incremented by every init (invalidates captured graphs)
+    // standalone apply graph
+    cudaGraphExec_t graph = nullptr;
+    const double *graph_d = nullptr;
+    double *graph_c = nullptr;
+    int64_t graph_kernels = 0;
+};
+
+struct ug4gb_solver {
+    ug4gb_ctx *ctx = nullptr;
+    int kind = UG4GB_SOLVER_CG;
+    ug4gb_gmg *pre = nullptr;
+    int maxit = 100;
+    double min_def = 1e-300, rel_red = 1e-10;
+    const ug4gb_matrix *A = nullptr;
+    int n = 0;
+    ug4gb::DevBuf<double> r, p, q, r0, v, s, t, zcopy;
+    ug4gb::DevBuf<ug4gb::KScal> ks;
+    ug4gb::DevBuf<double> hist;
+    ug4gb::KScal host_ks{};
+    std::vector<double> host_hist;
+    // captured iteration graph
+    cudaGraphExec_t iter_graph = nullptr;
+    int64_t iter_kernels = 0;
+    const double *graph_x = nullptr;
+    const double *graph_r = nullptr;
+    int graph_pre_gen = -1;
+    int last_rc = 0;
+};

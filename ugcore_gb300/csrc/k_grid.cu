@@ -1,0 +1,440 @@
+// k_grid.cu -- structured hierarchy generation, CRS sparsity build, CRS
+// transpose and CRS -> SELL-32 conversion.
+//
+// The CRS pattern of a level is the union of all element couplings with
+// columns sorted per row and structural zeros kept: the set ugcore grows
+// through SparseMatrix::operator()/get_index while adding element matrices
+// (lib_algebra/cpu_algebra/sparsematrix_impl.h:553-701; AddLocalMatrixToGlobal,
+// lib_disc/common/local_algebra.h:767).  It is built here without a global
+// sort: vertex->element adjacency by counting, then one warp per row gathers
+// the corners of its elements and ranks the distinct ones in shared memory.
+#include "common.cuh"
+
+namespace ug4gb {
+
+// ------------------------------------------------------------ generation --
+__global__ void k_gen_vertices(int nx, int ny, int nz, int dim, double *coords, unsigned char *bnd,
+                               int *color)
+{
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    int nv = nx * ny * nz;
+    if (v >= nv) return;
+    int i = v % nx, j = (v / nx) % ny, k = v / (nx * ny);
+    coords[(size_t)v * dim + 0] = (double)i / (double)(nx - 1);
+    coords[(size_t)v * dim + 1] = (double)j / (double)(ny - 1);
+    int b = (i == 0 || i == nx - 1 || j == 0 || j == ny - 1);
+    if (dim == 3) {
+        coords[(size_t)v * dim + 2] = (double)k / (double)(nz - 1);
+        b = b || (k == 0 || k == nz - 1);
+    }
+    bnd[v] = (unsigned char)b;
+    color[v] = (i & 1) | ((j & 1) << 1) | ((k & 1) << 2);
+}
+
+// quads: corners (i,j),(i+1,j),(i+1,j+1),(i,j+1); hexes: the reference
+// hexahedron order; tets: 6 Kuhn tets per hex, orientation made positive.
+__global__ void k_gen_elements(int elem_type, int nx, int ny, int nz, int *elems)
+{
+    int cx = nx - 1, cy = ny - 1, cz = (elem_type == UG4GB_QUAD) ? 1 : nz - 1;
+    int ncell = cx * cy * cz;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int per = (elem_type == UG4GB_TET) ? 6 : 1;
+    if (t >= ncell * per) return;
+    int h = t / per, p = t % per;
+    int i = h % cx, j = (h / cx) % cy, k = h / (cx * cy);
+    int sx = 1, sy = nx, sz = nx * ny;
+    int v0 = i + nx * (j + ny * k);
+    if (elem_type == UG4GB_QUAD) {
+        int *e = elems + 4 * (size_t)h;
+        e[0] = v0; e[1] = v0 + 1; e[2] = v0 + 1 + nx; e[3] = v0 + nx;
+    } else if (elem_type == UG4GB_HEX) {
+        int *e = elems + 8 * (size_t)h;
+        e[0] = v0; e[1] = v0 + sx; e[2] = v0 + sx + sy; e[3] = v0 + sy;
+        e[4] = v0 + sz; e[5] = v0 + sx + sz; e[6] = v0 + sx + sy + sz; e[7] = v0 + sy + sz;
+    } else {
+        const int perm[6][2] = {{0, 1}, {0, 2}, {1, 0}, {1, 2}, {2, 0}, {2, 1}};
+        int step[3] = {sx, sy, sz};
+        int v1 = v0 + step[perm[p][0]], v2 = v1 + step[perm[p][1]], v3 = v0 + sx + sy + sz;
+        bool odd = (p == 1 || p == 2 || p == 5);
+        int *e = elems + 4 * (size_t)t;
+        e[0] = v0; e[1] = odd ? v2 : v1; e[2] = odd ? v1 : v2; e[3] = v3;
+    }
+}
+
+// parents of fine vertex (i,j,k) in the coarse level: vertex parent if all
+// indices even; otherwise the corners of the coarse edge/face/cell
+// (StdTransfer::assemble_prolongation_p1, std_transfer_impl.h:47-168), or for
+// the Kuhn tet split the two ends of the coarse edge.
+__global__ void k_gen_parents(int elem_type, int nx, int ny, int nz, int cnx, int cny, int *npar, int *par)
+{
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nx * ny * nz) return;
+    int i = v % nx, j = (v / nx) % ny, k = v / (nx * ny);
+    int p0 = i & 1, p1 = j & 1, p2 = k & 1;
+    int b0 = i >> 1, b1 = j >> 1, b2 = k >> 1;
+    int *out = par + 8 * (size_t)v;
+    int n = 0;
+    if (elem_type == UG4GB_TET) {
+        out[n++] = b0 + cnx * (b1 + cny * b2);
+        if (p0 | p1 | p2) out[n++] = (b0 + p0) + cnx * ((b1 + p1) + cny * (b2 + p2));
+    } else {
+        for (int dk = 0; dk <= p2; ++dk)
+            for (int dj = 0; dj <= p1; ++dj)
+                for (int di = 0; di <= p0; ++di) out[n++] = (b0 + di) + cnx * ((b1 + dj) + cny * (b2 + dk));
+    }
+    for (int q = n; q < 8; ++q) out[q] = -1;
+    npar[v] = n;
+}
+
+void gen_level(Ctx &c, Level &L, int elem_type, int cx, int cy, int cz, const Level *coarse)
+{
+    L.elem_type = elem_type;
+    L.dim = (elem_type == UG4GB_QUAD) ? 2 : 3;
+    L.k = (elem_type == UG4GB_HEX) ? 8 : 4;
+    L.nx = cx + 1; L.ny = cy + 1; L.nz = (L.dim == 3) ? cz + 1 : 1;
+    L.nv = L.nx * L.ny * L.nz;
+    int ncell = cx * cy * (L.dim == 3 ? cz : 1);
+    L.ne = (elem_type == UG4GB_TET) ? 6 * ncell : ncell;
+    L.coords.alloc((size_t)L.nv * L.dim);
+    L.elems.alloc((size_t)L.ne * L.k);
+    L.bnd.alloc(L.nv);
+    L.color.alloc(L.nv);
+    UG_LAUNCH(c, k_gen_vertices, div_up(L.nv, 256), 256, 0, L.nx, L.ny, L.nz, L.dim, L.coords.p, L.bnd.p,
+              L.color.p);
+    UG_LAUNCH(c, k_gen_elements, div_up(L.ne, 256), 256, 0, elem_type, L.nx, L.ny, L.nz, L.elems.p);
+    if (coarse) {
+        L.npar.alloc(L.nv);
+        L.par.alloc((size_t)L.nv * 8);
+        UG_LAUNCH(c, k_gen_parents, div_up(L.nv, 256), 256, 0, elem_type, L.nx, L.ny, L.nz, coarse->nx, coarse->ny,
+                  L.npar.p, L.par.p);
+    }
+}
+
+// ----------------------------------------------------------------- scan --
+// Exclusive scan of int32 (with int64 total): block-local scans, a single
+// block scanning the block sums, then a fix-up pass.
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_blocks(const int *in, int *out, int n, long long *block_sums)
+{
+    __shared__ long long sh[kScanBlock];
+    int i = blockIdx.x * kScanBlock + threadIdx.x;
+    long long x = (i < n) ? in[i] : 0;
+    sh[threadIdx.x] = x;
+    __syncthreads();
+    for (int o = 1; o < kScanBlock; o <<= 1) {
+        long long t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+        __syncthreads();
+        sh[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < n) out[i] = (int)(sh[threadIdx.x] - x);
+    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = sh[threadIdx.x];
+}
+
+__global__ void k_scan_sums(long long *block_sums, int nb, long long *total)
+{
+    // single block: sequential over chunks, parallel inside each
+    __shared__ long long sh[kScanBlock];
+    long long carry = 0;
+    for (int base = 0; base < nb; base += kScanBlock) {
+        int i = base + threadIdx.x;
+        long long x = (i < nb) ? block_sums[i] : 0;
+        sh[threadIdx.x] = x;
+        __syncthreads();
+        for (int o = 1; o < kScanBlock; o <<= 1) {
+            long long t = (threadIdx.x >= o) ? sh[threadIdx.x - o] : 0;
+            __syncthreads();
+            sh[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < nb) block_sums[i] = carry + sh[threadIdx.x] - x;
+        long long last = sh[kScanBlock - 1];
+        __syncthreads();
+        carry += last;
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void k_scan_fix(int *out, int n, const long long *block_sums)
+{
+    int i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < n) out[i] = (int)(out[i] + block_sums[blockIdx.x]);
+}
+
+void exclusive_scan_int(Ctx &c, const int *in, int *out, int n, int64_t *total_out)
+{
+    int nb = (int)div_up(n > 0 ? n : 1, kScanBlock);
+    DevBuf<long long> sums;
+    sums.alloc(nb + 1);
+    UG_LAUNCH(c, k_scan_blocks, nb, kScanBlock, 0, in, out, n, sums.p);
+    UG_LAUNCH(c, k_scan_sums, 1, kScanBlock, 0, sums.p, nb, sums.p + nb);
+    UG_LAUNCH(c, k_scan_fix, nb, kScanBlock, 0, out, n, sums.p);
+    if (total_out) {
+        long long t = 0;
+        UG_CUDA(cudaMemcpyAsync(&t, sums.p + nb, sizeof(long long), cudaMemcpyDeviceToHost, c.stream));
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        *total_out = t;
+    }
+}
+
+// ------------------------------------------------------- CRS from elems --
+__global__ void k_count_corners(const int *elems, int nek, int *deg)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < nek) atomicAdd(deg + elems[t], 1);
+}
+
+__global__ void k_fill_adjacency(const int *elems, int nek, int k, const int *vptr, int *cursor, int *adj)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nek) return;
+    int v = elems[t];
+    int pos = atomicAdd(cursor + v, 1);
+    adj[vptr[v] + pos] = t / k;
+}
+
+constexpr int kRowCand = 128;   // max candidate columns per row (96 for Kuhn tets)
+
+// One warp per row: gather corners of adjacent elements into shared memory,
+// keep first occurrences, rank them.  mode 0 counts, mode 1 writes columns.
+__global__ void k_row_pattern(const int *elems, int k, const int *vptr, const int *adj, int nv, int mode,
+                              int *rowlen, const int *rowptr, int *col, int *overflow)
+{
+    __shared__ int cand[8][kRowCand];
+    __shared__ int uniq[8][kRowCand];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * 8 + warp;
+    if (row >= nv) return;
+    int *cd = cand[warp], *uq = uniq[warp];
+    const int a0 = vptr[row], a1 = vptr[row + 1];
+    const int ncand = (a1 - a0) * k;
+    if (ncand > kRowCand) {
+        if (lane == 0) atomicExch(overflow, 1);
+        return;
+    }
+    for (int t = lane; t < ncand; t += 32) cd[t] = elems[(size_t)adj[a0 + t / k] * k + (t % k)];
+    __syncwarp();
+    // keep the first occurrence of every column, mark repeats with INT_MAX
+    for (int t = lane; t < ncand; t += 32) {
+        int v = cd[t];
+        bool first = true;
+        for (int s = 0; s < t; ++s) first = first && (cd[s] != v);
+        uq[t] = first ? v : 0x7fffffff;
+    }
+    __syncwarp();
+    int nfirst_lane = 0;
+    for (int t = lane; t < ncand; t += 32) {
+        int v = uq[t];
+        if (v == 0x7fffffff) continue;
+        ++nfirst_lane;
+        if (mode == 1) {
+            int rank = 0;
+            for (int s = 0; s < ncand; ++s) rank += (uq[s] < v) ? 1 : 0;
+            col[rowptr[row] + rank] = v;
+        }
+    }
+    if (mode == 0) {
+        for (int o = 16; o > 0; o >>= 1) nfirst_lane += __shfl_xor_sync(0xffffffffu, nfirst_lane, o);
+        if (lane == 0) rowlen[row] = nfirst_lane;
+    }
+}
+
+void fill_double_impl(Ctx &c, double *p, size_t n, double v);
+
+void csr_from_elements(Ctx &c, const Level &L, Csr &A)
+{
+    const int nv = L.nv, nek = L.ne * L.k;
+    DevBuf<int> deg, vptr, cursor, adj, rowlen, overflow;
+    deg.alloc(nv + 1);
+    vptr.alloc(nv + 1);
+    cursor.alloc(nv);
+    adj.alloc(nek);
+    rowlen.alloc(nv + 1);
+    overflow.alloc(1);
+    UG_CUDA(cudaMemsetAsync(deg.p, 0, deg.bytes(), c.stream));
+    UG_CUDA(cudaMemsetAsync(cursor.p, 0, cursor.bytes(), c.stream));
+    UG_CUDA(cudaMemsetAsync(overflow.p, 0, overflow.bytes(), c.stream));
+    UG_LAUNCH(c, k_count_corners, div_up(nek, 256), 256, 0, L.elems.p, nek, deg.p);
+    exclusive_scan_int(c, deg.p, vptr.p, nv + 1, nullptr);
+    UG_LAUNCH(c, k_fill_adjacency, div_up(nek, 256), 256, 0, L.elems.p, nek, L.k, vptr.p, cursor.p, adj.p);
+    UG_LAUNCH(c, k_row_pattern, div_up(nv, 8), 256, 0, L.elems.p, L.k, vptr.p, adj.p, nv, 0, rowlen.p,
+              (const int *)nullptr, (int *)nullptr, overflow.p);
+    UG_CUDA(cudaMemsetAsync(rowlen.p + nv, 0, sizeof(int), c.stream));
+    A.nrows = A.ncols = nv;
+    A.rowptr.alloc(nv + 1);
+    int64_t nnz = 0;
+    exclusive_scan_int(c, rowlen.p, A.rowptr.p, nv + 1, &nnz);
+    int ovf = 0;
+    UG_CUDA(cudaMemcpy(&ovf, overflow.p, sizeof(int), cudaMemcpyDeviceToHost));
+    UG_REQUIRE(!ovf, UG4GB_ERR_INVALID, "csr_from_elements: a vertex couples to more than 128 corners");
+    UG_REQUIRE(nnz < (int64_t)1 << 31, UG4GB_ERR_INVALID, "csr_from_elements: nnz exceeds int32 range");
+    A.nnz = nnz;
+    A.col.alloc(nnz);
+    A.val.alloc(nnz);
+    UG_LAUNCH(c, k_row_pattern, div_up(nv, 8), 256, 0, L.elems.p, L.k, vptr.p, adj.p, nv, 1, (int *)nullptr,
+              (const int *)A.rowptr.p, A.col.p, overflow.p);
+    UG_CUDA(cudaMemsetAsync(A.val.p, 0, A.val.bytes(), c.stream));
+}
+
+// ------------------------------------------------------------ transpose --
+__global__ void k_count_cols(const int *rowptr, const int *col, const double *val, int nrows, bool keep_zeros,
+                             int *cnt)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    for (int a = rowptr[r]; a < rowptr[r + 1]; ++a)
+        if (keep_zeros || val[a] != 0.0) atomicAdd(cnt + col[a], 1);
+}
+
+__global__ void k_scatter_transpose(const int *rowptr, const int *col, const double *val, int nrows,
+                                    bool keep_zeros, const int *trow, int *cursor, int *tcol, double *tval)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    for (int a = rowptr[r]; a < rowptr[r + 1]; ++a) {
+        if (!(keep_zeros || val[a] != 0.0)) continue;
+        int cc = col[a];
+        int pos = trow[cc] + atomicAdd(cursor + cc, 1);
+        tcol[pos] = r;
+        tval[pos] = val[a];
+    }
+}
+
+// insertion sort of each (short) row by column
+__global__ void k_sort_rows(const int *rowptr, int *col, double *val, int nrows)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    int a0 = rowptr[r], a1 = rowptr[r + 1];
+    for (int a = a0 + 1; a < a1; ++a) {
+        int cc = col[a];
+        double vv = val[a];
+        int b = a - 1;
+        while (b >= a0 && col[b] > cc) {
+            col[b + 1] = col[b];
+            val[b + 1] = val[b];
+            --b;
+        }
+        col[b + 1] = cc;
+        val[b + 1] = vv;
+    }
+}
+
+void csr_transpose(Ctx &c, const Csr &B, Csr &T, bool keep_zeros)
+{
+    T.nrows = B.ncols;
+    T.ncols = B.nrows;
+    DevBuf<int> cnt, cursor;
+    cnt.alloc(T.nrows + 1);
+    cursor.alloc(T.nrows + 1);
+    UG_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), c.stream));
+    UG_CUDA(cudaMemsetAsync(cursor.p, 0, cursor.bytes(), c.stream));
+    UG_LAUNCH(c, k_count_cols, div_up(B.nrows, 256), 256, 0, B.rowptr.p, B.col.p, B.val.p, B.nrows, keep_zeros,
+              cnt.p);
+    T.rowptr.alloc(T.nrows + 1);
+    int64_t nnz = 0;
+    exclusive_scan_int(c, cnt.p, T.rowptr.p, T.nrows + 1, &nnz);
+    T.nnz = nnz;
+    T.col.alloc(nnz > 0 ? nnz : 1);
+    T.val.alloc(nnz > 0 ? nnz : 1);
+    UG_LAUNCH(c, k_scatter_transpose, div_up(B.nrows, 256), 256, 0, B.rowptr.p, B.col.p, B.val.p, B.nrows,
+              keep_zeros, T.rowptr.p, cursor.p, T.col.p, T.val.p);
+    UG_LAUNCH(c, k_sort_rows, div_up(T.nrows, 256), 256, 0, T.rowptr.p, T.col.p, T.val.p, T.nrows);
+}
+
+void csr_copy(Ctx &c, const Csr &src, Csr &dst)
+{
+    dst.nrows = src.nrows;
+    dst.ncols = src.ncols;
+    dst.nnz = src.nnz;
+    dst.rowptr.alloc(src.nrows + 1);
+    dst.col.alloc(src.nnz);
+    dst.val.alloc(src.nnz);
+    UG_CUDA(cudaMemcpyAsync(dst.rowptr.p, src.rowptr.p, src.rowptr.bytes(), cudaMemcpyDeviceToDevice, c.stream));
+    if (src.nnz) {
+        UG_CUDA(cudaMemcpyAsync(dst.col.p, src.col.p, (size_t)src.nnz * sizeof(int), cudaMemcpyDeviceToDevice,
+                                c.stream));
+        UG_CUDA(cudaMemcpyAsync(dst.val.p, src.val.p, (size_t)src.nnz * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c.stream));
+    }
+}
+
+// ----------------------------------------------------------- CRS -> SELL --
+__global__ void k_slice_width(const int *rowptr, int nrows, int nslices, int *w32)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslices) return;
+    int w = 0;
+    for (int r = s * kSliceH; r < min(nrows, (s + 1) * kSliceH); ++r) w = max(w, rowptr[r + 1] - rowptr[r]);
+    w32[s] = w * kSliceH;
+}
+
+__global__ void k_slice_w_from32(const int *w32, int *w, int nslices)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nslices) w[s] = w32[s] / kSliceH;
+}
+
+template <class T>
+__global__ void k_sell_fill(const int *rowptr, const int *col, const double *val, int nrows, const int *sptr,
+                            const int *sw, const double *col_scale, int *scol, T *sval)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    int s = r / kSliceH, lane = r % kSliceH;
+    if (s * kSliceH >= nrows) return;
+    int w = sw[s];
+    int base = sptr[s] + lane;
+    int a0 = (r < nrows) ? rowptr[r] : 0, len = (r < nrows) ? rowptr[r + 1] - a0 : 0;
+    int pad_col = (len > 0) ? col[a0 + len - 1] : 0;
+    for (int q = 0; q < w; ++q) {
+        int cc = pad_col;
+        double v = 0.0;
+        if (q < len) {
+            cc = col[a0 + q];
+            v = val[a0 + q];
+            if (col_scale) v *= col_scale[cc];
+        }
+        scol[base + q * kSliceH] = cc;
+        sval[base + q * kSliceH] = (T)v;
+    }
+}
+
+template <class T>
+void sell_from_csr(Ctx &c, const Csr &A, Sell<T> &S, const double *col_scale)
+{
+    S.nrows = A.nrows;
+    S.ncols = A.ncols;
+    S.nslices = (int)div_up(A.nrows > 0 ? A.nrows : 1, kSliceH);
+    DevBuf<int> w32;
+    w32.alloc(S.nslices + 1);
+    S.sptr.alloc(S.nslices + 1);
+    S.swidth.alloc(S.nslices);
+    UG_CUDA(cudaMemsetAsync(w32.p, 0, w32.bytes(), c.stream));
+    UG_LAUNCH(c, k_slice_width, div_up(S.nslices, 256), 256, 0, A.rowptr.p, A.nrows, S.nslices, w32.p);
+    UG_LAUNCH(c, k_slice_w_from32, div_up(S.nslices, 256), 256, 0, w32.p, S.swidth.p, S.nslices);
+    int64_t stored = 0;
+    exclusive_scan_int(c, w32.p, S.sptr.p, S.nslices + 1, &stored);
+    S.stored = stored;
+    S.col.alloc(stored > 0 ? stored : 1);
+    S.val.alloc(stored > 0 ? stored : 1);
+    UG_LAUNCH(c, k_sell_fill<T>, div_up((size_t)S.nslices * kSliceH, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p,
+              A.nrows, S.sptr.p, S.swidth.p, col_scale, S.col.p, S.val.p);
+}
+
+template void sell_from_csr<double>(Ctx &, const Csr &, Sell<double> &, const double *);
+template void sell_from_csr<float>(Ctx &, const Csr &, Sell<float> &, const double *);
+
+__global__ void k_fill(double *p, size_t n, double v)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+void fill_double(Ctx &c, double *p, size_t n, double v)
+{
+    if (n == 0) return;
+    UG_LAUNCH(c, k_fill, div_up(n, 256), 256, 0, p, n, v);
+}
+
+}  // namespace ug4gb

@@ -1,0 +1,673 @@
+// k_solve.cu -- SELL-32 SpMV-based multigrid and Krylov kernels.
+//
+// Every kernel is HBM-bound: one thread per row, 32 rows per slice, matrix
+// values/columns streamed with evict-first loads (coalesced 32-wide), the
+// gathered vector kept in L1/L2.  Row-local vector work is fused into the
+// SpMV epilogue so each sweep reads the matrix once:
+//   Jacobi step     t = dinv*d ; d -= A t ; sc += t
+//                   (Jacobi::step, lib_algebra/operator/preconditioner/
+//                    jacobi.h:222; AssembledMultiGridCycle::
+//                    presmooth_and_restriction / prolongation_and_postsmooth,
+//                    mg_solver_impl.hpp:1687-1966) becomes one pass over the
+//                   column-scaled operator At = A*diag(dinv): d_new = d - At x.
+//   prolongation    t = P sc_c ; sc += t ; w = t / dinv (so that A t = At w)
+//                   (StdTransfer::prolongate, std_transfer_impl.h:721)
+//   restriction     d_c = R d (StdTransfer::do_restrict, std_transfer_impl.h:776)
+//   CG              q = A z + beta q, p = z + beta p and lambda = (q,p) in one
+//                   pass (CG::apply_return_defect, cg.h:163-226)
+// Reductions are deterministic (grid_reduce: fixed-order tree per block,
+// block partials summed in block order by the last block).
+#include "k_solve.cuh"
+
+namespace ug4gb {
+
+constexpr int NT = 256;
+
+int row_grid(const Ctx &c, int nrows)
+{
+    int need = (int)div_up(nrows > 0 ? nrows : 1, NT);
+    int cap = c.num_sms * 8;
+    return need < cap ? need : cap;
+}
+
+template <class V, class XT, class ACC>
+__device__ __forceinline__ ACC sell_row(const SellView<V> &A, const XT *__restrict__ x, int row)
+{
+    const int s = row >> 5, lane = row & 31;
+    const int base = __ldg(A.sptr + s) + lane;
+    const int w = __ldg(A.swidth + s);
+    ACC acc = (ACC)0;
+#pragma unroll 4
+    for (int k = 0; k < w; ++k) {
+        const int idx = base + k * kSliceH;
+        acc += (ACC)ld_stream(A.val + idx) * (ACC)x[ld_stream(A.col + idx)];
+    }
+    return acc;
+}
+
+__device__ __forceinline__ bool conv_valid(double v)
+{
+    if (v == 0.0) return true;
+    return v >= 2.2250738585072014e-308 && v <= 1.7976931348623157e308 && v == v && v >= 0.0;
+}
+
+__device__ __forceinline__ bool conv_ended(const KScal *ks)
+{
+    if (!conv_valid(ks->dcur)) return true;
+    if (ks->step >= ks->maxit) return true;
+    if (ks->dcur < ks->min_def) return true;
+    if (ks->dcur / ks->d0 < ks->rel_red) return true;
+    return false;
+}
+
+__device__ __forceinline__ void conv_update(KScal *ks, double d, int done_value)
+{
+    ks->dcur = d;
+    ks->step += 1;
+    if (ks->hist && ks->step < ks->hist_cap) ks->hist[ks->step] = d;
+    if (conv_ended(ks)) ks->done = done_value;
+}
+
+// ------------------------------------------------------- smoothing step --
+template <class V, class XT, class DT, bool RHO>
+__global__ void __launch_bounds__(NT) k_smooth(SellView<V> A, const XT *__restrict__ x, const DT *__restrict__ dbase,
+                                               const V *__restrict__ dinv, V *__restrict__ sc, V *__restrict__ dout,
+                                               int sc_mode, const int *skip, const double *__restrict__ r_rho,
+                                               RedArgs red, int rho_kind)
+{
+    if (skip && *skip) return;
+    double rsum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
+        V acc = sell_row<V, XT, V>(A, x, row);
+        V db = (V)dbase[row];
+        V dn = db - acc;
+        if (dout) dout[row] = dn;
+        V t = dinv[row] * (sc_mode == SC_ADD_FROM_NEW ? dn : db);
+        V s = (sc_mode == SC_SET_FROM_BASE) ? t : sc[row] + t;
+        sc[row] = s;
+        if (RHO) rsum += (double)s * r_rho[row];
+    }
+    if (RHO) {
+        double v[1] = {rsum};
+        KScal *ks = red.ks;
+        grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) {
+            if (rho_kind == 0) {
+                ks->rho_old = tot[0];
+            } else {
+                ks->rho = tot[0];
+                ks->beta = tot[0] / ks->rho_old;
+                ks->rho_old = tot[0];
+            }
+        });
+    }
+}
+
+template <class V, class XT, class DT>
+void smooth_step(Ctx &c, const Sell<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout, int sc_mode,
+                 const int *skip, const double *r_rho, RedArgs *red, int rho_kind)
+{
+    int g = row_grid(c, At.nrows);
+    if (r_rho) {
+        UG_LAUNCH(c, (k_smooth<V, XT, DT, true>), g, NT, 0, view(At), x, dbase, dinv, sc, dout, sc_mode, skip, r_rho,
+                  *red, rho_kind);
+    } else {
+        RedArgs none{nullptr, nullptr, nullptr};
+        UG_LAUNCH(c, (k_smooth<V, XT, DT, false>), g, NT, 0, view(At), x, dbase, dinv, sc, dout, sc_mode, skip,
+                  (const double *)nullptr, none, 0);
+    }
+}
+
+#define INST_SMOOTH(V, XT, DT)                                                                              \
+    template void smooth_step<V, XT, DT>(Ctx &, const Sell<V> &, const XT *, const DT *, const V *, V *, V *, int, \
+                                         const int *, const double *, RedArgs *, int);
+INST_SMOOTH(double, double, double)
+INST_SMOOTH(float, float, float)
+INST_SMOOTH(float, double, double)
+INST_SMOOTH(float, float, double)
+
+// --------------------------------------------------------- transfers -----
+template <class V>
+__global__ void __launch_bounds__(NT) k_restrict(SellView<V> R, const V *__restrict__ d, V *__restrict__ dc,
+                                                 const int *skip)
+{
+    if (skip && *skip) return;
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < R.nrows; row += stride) dc[row] = sell_row<V, V, V>(R, d, row);
+}
+
+template <class V>
+void restrict_apply(Ctx &c, const Sell<V> &R, const V *d, V *dc, const int *skip)
+{
+    UG_LAUNCH(c, k_restrict<V>, row_grid(c, R.nrows), NT, 0, view(R), d, dc, skip);
+}
+
+template <class V>
+__global__ void __launch_bounds__(NT) k_prolong(SellView<V> P, const V *__restrict__ scc, V *__restrict__ sc,
+                                                const V *__restrict__ dfac, V *__restrict__ w, const int *skip)
+{
+    if (skip && *skip) return;
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < P.nrows; row += stride) {
+        V t = sell_row<V, V, V>(P, scc, row);
+        sc[row] += t;
+        if (w) w[row] = t * dfac[row];
+    }
+}
+
+template <class V>
+void prolong_apply(Ctx &c, const Sell<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip)
+{
+    UG_LAUNCH(c, k_prolong<V>, row_grid(c, P.nrows), NT, 0, view(P), scc, sc, dfac, w, skip);
+}
+
+// dense base solve with the LU-factored inverse (one block, FP64)
+template <class V>
+__global__ void k_base_solve(const double *__restrict__ Ainv, int n, const V *__restrict__ d, V *__restrict__ sc,
+                             const int *skip)
+{
+    extern __shared__ double dsh[];
+    if (skip && *skip) return;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) dsh[j] = (double)d[j];
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double s = 0.0;
+        for (int j = 0; j < n; ++j) s += Ainv[(size_t)i * n + j] * dsh[j];
+        sc[i] = (V)s;
+    }
+}
+
+template <class V>
+void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip)
+{
+    UG_LAUNCH(c, k_base_solve<V>, 1, NT, (size_t)n * sizeof(double), Ainv, n, d, sc, skip);
+}
+
+// multicolour Gauss-Seidel: rows of one colour, t_i = relax (d_i - (A t)_i) / a_ii
+// (t_i is still 0 when its colour is processed)
+template <class V>
+__global__ void __launch_bounds__(NT) k_mcgs(SellView<V> A, const int *__restrict__ rows, int nrows_c,
+                                             const V *__restrict__ dr, const V *__restrict__ d, V *__restrict__ t,
+                                             const int *skip)
+{
+    if (skip && *skip) return;
+    const int stride = gridDim.x * NT;
+    for (int q = blockIdx.x * NT + threadIdx.x; q < nrows_c; q += stride) {
+        int row = rows[q];
+        V acc = sell_row<V, V, V>(A, t, row);
+        t[row] = dr[row] * (d[row] - acc);
+    }
+}
+
+template <class V>
+void mcgs_colour(Ctx &c, const Sell<V> &A, const int *rows, int nrows_c, const V *dinv_relax, const V *d, V *t,
+                 const int *skip)
+{
+    UG_LAUNCH(c, k_mcgs<V>, row_grid(c, nrows_c), NT, 0, view(A), rows, nrows_c, dinv_relax, d, t, skip);
+}
+
+// d_out = d_base - A t ; sc (= | +=) t
+template <class V, class DT>
+__global__ void __launch_bounds__(NT) k_resupd(SellView<V> A, const V *__restrict__ t, const DT *__restrict__ dbase,
+                                               V *__restrict__ dout, V *__restrict__ sc, int first, const int *skip)
+{
+    if (skip && *skip) return;
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
+        V acc = sell_row<V, V, V>(A, t, row);
+        dout[row] = (V)dbase[row] - acc;
+        if (first == 1) sc[row] = t[row];
+        else if (first == 0) sc[row] += t[row];
+    }
+}
+
+template <class V, class DT>
+void residual_update(Ctx &c, const Sell<V> &A, const V *t, const DT *dbase, V *dout, V *sc, int first, const int *skip)
+{
+    UG_LAUNCH(c, (k_resupd<V, DT>), row_grid(c, A.nrows), NT, 0, view(A), t, dbase, dout, sc, first, skip);
+}
+
+template void restrict_apply<double>(Ctx &, const Sell<double> &, const double *, double *, const int *);
+template void restrict_apply<float>(Ctx &, const Sell<float> &, const float *, float *, const int *);
+template void prolong_apply<double>(Ctx &, const Sell<double> &, const double *, double *, const double *, double *,
+                                    const int *);
+template void prolong_apply<float>(Ctx &, const Sell<float> &, const float *, float *, const float *, float *,
+                                   const int *);
+template void base_solve<double>(Ctx &, const double *, int, const double *, double *, const int *);
+template void base_solve<float>(Ctx &, const double *, int, const float *, float *, const int *);
+template void mcgs_colour<double>(Ctx &, const Sell<double> &, const int *, int, const double *, const double *,
+                                  double *, const int *);
+template void mcgs_colour<float>(Ctx &, const Sell<float> &, const int *, int, const float *, const float *, float *,
+                                 const int *);
+template void residual_update<double, double>(Ctx &, const Sell<double> &, const double *, const double *, double *,
+                                              double *, int, const int *);
+template void residual_update<float, float>(Ctx &, const Sell<float> &, const float *, const float *, float *,
+                                            float *, int, const int *);
+template void residual_update<float, double>(Ctx &, const Sell<float> &, const float *, const double *, float *,
+                                             float *, int, const int *);
+
+// ------------------------------------------------------------ Krylov -----
+// r = b - A x (r holds b on entry); start the convergence check with |r|
+__global__ void __launch_bounds__(NT) k_krylov_start(SellView<double> A, const double *__restrict__ x,
+                                                     double *__restrict__ r, RedArgs red)
+{
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
+        double ax = sell_row<double, double, double>(A, x, row);
+        double rv = r[row] - ax;
+        r[row] = rv;
+        sum += rv * rv;
+    }
+    double v[1] = {sum};
+    KScal *ks = red.ks;
+    grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) {
+        double d = sqrt(tot[0]);
+        ks->d0 = d;
+        ks->dcur = d;
+        ks->step = 0;
+        ks->done = 0;
+        ks->fail = 0;
+        ks->restart = 1;
+        if (ks->hist && ks->hist_cap > 0) ks->hist[0] = d;
+        if (conv_ended(ks)) ks->done = 1;
+    });
+}
+
+void krylov_start(Ctx &c, const Sell<double> &A, const double *x, double *r, RedArgs red)
+{
+    UG_LAUNCH(c, k_krylov_start, row_grid(c, A.nrows), NT, 0, view(A), x, r, red);
+}
+
+// first: p = z, q = A z ; else p = z + beta p, q = A z + beta q ; lambda = (q,p)
+template <class ZT>
+__global__ void __launch_bounds__(NT) k_cg_spmv_dot(SellView<double> A, const ZT *__restrict__ z,
+                                                    double *__restrict__ p, double *__restrict__ q, int first,
+                                                    RedArgs red)
+{
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    const double beta = first ? 0.0 : ks->beta;
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
+        double az = sell_row<double, ZT, double>(A, z, row);
+        double pn = first ? (double)z[row] : (double)z[row] + beta * p[row];
+        double qn = first ? az : az + beta * q[row];
+        p[row] = pn;
+        q[row] = qn;
+        sum += qn * pn;
+    }
+    double v[1] = {sum};
+    grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) {
+        ks->lambda = tot[0];
+        if (tot[0] == 0.0) {
+            ks->fail = 1;
+            ks->done = 1;
+        }
+        ks->alpha = ks->rho_old / tot[0];
+    });
+}
+
+template <class ZT>
+void cg_spmv_dot_t(Ctx &c, const Sell<double> &A, const ZT *z, double *p, double *q, int first, RedArgs red)
+{
+    UG_LAUNCH(c, k_cg_spmv_dot<ZT>, row_grid(c, A.nrows), NT, 0, view(A), z, p, q, first, red);
+}
+template void cg_spmv_dot_t<double>(Ctx &, const Sell<double> &, const double *, double *, double *, int, RedArgs);
+template void cg_spmv_dot_t<float>(Ctx &, const Sell<double> &, const float *, double *, double *, int, RedArgs);
+
+// x += alpha p ; r -= alpha q ; |r| -> convergence check
+__global__ void __launch_bounds__(NT) k_cg_update(int n, double *__restrict__ x, double *__restrict__ r,
+                                                  const double *__restrict__ p, const double *__restrict__ q,
+                                                  RedArgs red)
+{
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    const double alpha = ks->alpha;
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int i = blockIdx.x * NT + threadIdx.x; i < n; i += stride) {
+        x[i] = x[i] + alpha * p[i];
+        double rv = r[i] + (-alpha) * q[i];
+        r[i] = rv;
+        sum += rv * rv;
+    }
+    double v[1] = {sum};
+    grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) { conv_update(ks, sqrt(tot[0]), 1); });
+}
+
+void cg_update(Ctx &c, int n, double *x, double *r, const double *p, const double *q, RedArgs red)
+{
+    UG_LAUNCH(c, k_cg_update, row_grid(c, n), NT, 0, n, x, r, p, q, red);
+}
+
+// rho = (z, r) when the preconditioner could not fuse it (kind 0: first, 1: loop)
+template <class ZT>
+__global__ void __launch_bounds__(NT) k_rho(int n, const ZT *__restrict__ z, const double *__restrict__ r, int kind,
+                                            RedArgs red)
+{
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int i = blockIdx.x * NT + threadIdx.x; i < n; i += stride) sum += (double)z[i] * r[i];
+    double v[1] = {sum};
+    grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) {
+        if (kind == 0) {
+            ks->rho_old = tot[0];
+        } else {
+            ks->rho = tot[0];
+            ks->beta = tot[0] / ks->rho_old;
+            ks->rho_old = tot[0];
+        }
+    });
+}
+
+template <class ZT>
+void rho_dot(Ctx &c, int n, const ZT *z, const double *r, int kind, RedArgs red)
+{
+    UG_LAUNCH(c, k_rho<ZT>, row_grid(c, n), NT, 0, n, z, r, kind, red);
+}
+template void rho_dot<double>(Ctx &, int, const double *, const double *, int, RedArgs);
+template void rho_dot<float>(Ctx &, int, const float *, const double *, int, RedArgs);
+
+template <class ZT>
+__global__ void k_copy_z(int n, const ZT *__restrict__ z, double *__restrict__ out, const int *skip)
+{
+    if (skip && *skip) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (double)z[i];
+}
+
+template <class ZT>
+void copy_z(Ctx &c, int n, const ZT *z, double *out, const int *skip)
+{
+    UG_LAUNCH(c, k_copy_z<ZT>, div_up(n, NT), NT, 0, n, z, out, skip);
+}
+template void copy_z<double>(Ctx &, int, const double *, double *, const int *);
+template void copy_z<float>(Ctx &, int, const float *, double *, const int *);
+
+// ------------------------------------------------------------ BiCGStab ---
+// (BiCGStab::apply_return_defect, bicgstab.h:158-390; restarts off, minOrtho 0)
+__global__ void k_bicg_restart(int n, const double *__restrict__ r, double *__restrict__ r0, double *__restrict__ p,
+                               double *__restrict__ v, KScal *ks)
+{
+    if (ks->done || !ks->restart) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        r0[i] = r[i];
+        p[i] = 0.0;
+        v[i] = 0.0;
+    }
+}
+
+void bicg_restart(Ctx &c, int n, const double *r, double *r0, double *p, double *v, RedArgs red)
+{
+    UG_LAUNCH(c, k_bicg_restart, div_up(n, NT), NT, 0, n, r, r0, p, v, red.ks);
+}
+
+__global__ void __launch_bounds__(NT) k_bicg_rho(int n, const double *__restrict__ r0, const double *__restrict__ r,
+                                                 RedArgs red)
+{
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int i = blockIdx.x * NT + threadIdx.x; i < n; i += stride) sum += r0[i] * r[i];
+    double v[1] = {sum};
+    grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) {
+        if (ks->restart) {
+            ks->alpha = 0.0;
+            ks->omega = 1.0;
+            ks->rho = 1.0;
+            ks->norm_r0 = ks->dcur;
+            ks->restart = 0;
+        }
+        const double rho_old = ks->rho;
+        ks->rho_old = rho_old;
+        ks->rho = tot[0];
+        if (fabs(tot[0]) / (ks->dcur * ks->norm_r0) <= 0.0) ks->restart = 1;
+        if (rho_old == 0.0) {
+            ks->fail = 1;
+            ks->done = 1;
+        }
+        ks->beta = (tot[0] / rho_old) * (ks->alpha / ks->omega);
+    });
+}
+
+void bicg_rho(Ctx &c, int n, const double *r0, const double *r, RedArgs red)
+{
+    UG_LAUNCH(c, k_bicg_rho, row_grid(c, n), NT, 0, n, r0, r, red);
+}
+
+__global__ void k_bicg_p(int n, const double *__restrict__ r, double *__restrict__ p, const double *__restrict__ v,
+                         const KScal *ks)
+{
+    if (ks->done) return;
+    const double beta = ks->beta, bo = -ks->beta * ks->omega;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = 1.0 * r[i] + beta * p[i] + bo * v[i];
+}
+
+void bicg_p(Ctx &c, int n, const double *r, double *p, const double *v, RedArgs red)
+{
+    UG_LAUNCH(c, k_bicg_p, div_up(n, NT), NT, 0, n, r, p, v, red.ks);
+}
+
+template <class ZT>
+__global__ void __launch_bounds__(NT) k_bicg_spmv_dot(SellView<double> A, const ZT *__restrict__ q,
+                                                      double *__restrict__ v, const double *__restrict__ r0, RedArgs red)
+{
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
+        double av = sell_row<double, ZT, double>(A, q, row);
+        v[row] = av;
+        sum += av * r0[row];
+    }
+    double vv[1] = {sum};
+    grid_reduce<NT, 1>(vv, red.partials, red.counter, [&](const double(&tot)[1]) {
+        if (tot[0] == 0.0) {
+            ks->fail = 1;
+            ks->done = 1;
+        }
+        ks->alpha = ks->rho / tot[0];
+    });
+}
+
+template <class ZT>
+void bicg_spmv_dot_t(Ctx &c, const Sell<double> &A, const ZT *q, double *v, const double *r0, RedArgs red)
+{
+    UG_LAUNCH(c, k_bicg_spmv_dot<ZT>, row_grid(c, A.nrows), NT, 0, view(A), q, v, r0, red);
+}
+template void bicg_spmv_dot_t<double>(Ctx &, const Sell<double> &, const double *, double *, const double *, RedArgs);
+template void bicg_spmv_dot_t<float>(Ctx &, const Sell<double> &, const float *, double *, const double *, RedArgs);
+
+template <class ZT>
+__global__ void __launch_bounds__(NT) k_bicg_x_s(int n, double *__restrict__ x, const ZT *__restrict__ q,
+                                                 const double *__restrict__ r, const double *__restrict__ v,
+                                                 double *__restrict__ s, RedArgs red)
+{
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    const double alpha = ks->alpha;
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int i = blockIdx.x * NT + threadIdx.x; i < n; i += stride) {
+        x[i] = 1.0 * x[i] + alpha * (double)q[i];
+        double sv = 1.0 * r[i] + (-alpha) * v[i];
+        s[i] = sv;
+        sum += sv * sv;
+    }
+    double vv[1] = {sum};
+    grid_reduce<NT, 1>(vv, red.partials, red.counter, [&](const double(&tot)[1]) { conv_update(ks, sqrt(tot[0]), 2); });
+}
+
+template <class ZT>
+void bicg_x_s(Ctx &c, int n, double *x, const ZT *q, const double *r, const double *v, double *s, RedArgs red)
+{
+    UG_LAUNCH(c, k_bicg_x_s<ZT>, row_grid(c, n), NT, 0, n, x, q, r, v, s, red);
+}
+template void bicg_x_s<double>(Ctx &, int, double *, const double *, const double *, const double *, double *, RedArgs);
+template void bicg_x_s<float>(Ctx &, int, double *, const float *, const double *, const double *, double *, RedArgs);
+
+__global__ void k_bicg_s_to_r(int n, const double *__restrict__ s, double *__restrict__ r, const KScal *ks)
+{
+    if (ks->done != 2) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) r[i] = s[i];
+}
+
+void bicg_s_to_r(Ctx &c, int n, const double *s, double *r, RedArgs red)
+{
+    UG_LAUNCH(c, k_bicg_s_to_r, div_up(n, NT), NT, 0, n, s, r, red.ks);
+}
+
+template <class ZT>
+__global__ void __launch_bounds__(NT) k_bicg_spmv_2dot(SellView<double> A, const ZT *__restrict__ q,
+                                                       double *__restrict__ t, const double *__restrict__ s,
+                                                       RedArgs red)
+{
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    double tt = 0.0, st = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
+        double av = sell_row<double, ZT, double>(A, q, row);
+        t[row] = av;
+        tt += av * av;
+        st += s[row] * av;
+    }
+    double vv[2] = {tt, st};
+    grid_reduce<NT, 2>(vv, red.partials, red.counter, [&](const double(&tot)[2]) {
+        if (tot[0] == 0.0) {
+            ks->fail = 1;
+            ks->done = 1;
+        }
+        ks->omega = tot[1] / tot[0];
+    });
+}
+
+template <class ZT>
+void bicg_spmv_2dot_t(Ctx &c, const Sell<double> &A, const ZT *q, double *t, const double *s, RedArgs red)
+{
+    UG_LAUNCH(c, k_bicg_spmv_2dot<ZT>, row_grid(c, A.nrows), NT, 0, view(A), q, t, s, red);
+}
+template void bicg_spmv_2dot_t<double>(Ctx &, const Sell<double> &, const double *, double *, const double *, RedArgs);
+template void bicg_spmv_2dot_t<float>(Ctx &, const Sell<double> &, const float *, double *, const double *, RedArgs);
+
+template <class ZT>
+__global__ void __launch_bounds__(NT) k_bicg_x_r(int n, double *__restrict__ x, const ZT *__restrict__ q,
+                                                 const double *__restrict__ s, const double *__restrict__ t,
+                                                 double *__restrict__ r, RedArgs red)
+{
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    const double omega = ks->omega;
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int i = blockIdx.x * NT + threadIdx.x; i < n; i += stride) {
+        x[i] = 1.0 * x[i] + omega * (double)q[i];
+        double rv = 1.0 * s[i] + (-omega) * t[i];
+        r[i] = rv;
+        sum += rv * rv;
+    }
+    double vv[1] = {sum};
+    grid_reduce<NT, 1>(vv, red.partials, red.counter, [&](const double(&tot)[1]) {
+        conv_update(ks, sqrt(tot[0]), 1);
+        if (ks->omega == 0.0) {
+            ks->fail = 1;
+            ks->done = 1;
+        }
+    });
+}
+
+template <class ZT>
+void bicg_x_r(Ctx &c, int n, double *x, const ZT *q, const double *s, const double *t, double *r, RedArgs red)
+{
+    UG_LAUNCH(c, k_bicg_x_r<ZT>, row_grid(c, n), NT, 0, n, x, q, s, t, r, red);
+}
+template void bicg_x_r<double>(Ctx &, int, double *, const double *, const double *, const double *, double *, RedArgs);
+template void bicg_x_r<float>(Ctx &, int, double *, const float *, const double *, const double *, double *, RedArgs);
+
+// ------------------------------------------------------ vector/matrix API --
+__global__ void __launch_bounds__(NT) k_vec_dot(int n, const double *__restrict__ a, const double *__restrict__ b,
+                                                RedArgs red)
+{
+    double sum = 0.0;
+    const int stride = gridDim.x * NT;
+    for (int i = blockIdx.x * NT + threadIdx.x; i < n; i += stride) sum += a[i] * b[i];
+    double v[1] = {sum};
+    KScal *ks = red.ks;
+    grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) { ks->dot_out[0] = tot[0]; });
+}
+
+void vec_dot(Ctx &c, int n, const double *a, const double *b, RedArgs red)
+{
+    UG_LAUNCH(c, k_vec_dot, row_grid(c, n), NT, 0, n, a, b, red);
+}
+
+__global__ void k_vec_scale_add(int n, double *dest, double alpha, const double *a, double beta, const double *b)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dest[i] = alpha * a[i] + beta * b[i];
+}
+
+void vec_scale_add(Ctx &c, int n, double *dest, double alpha, const double *a, double beta, const double *b)
+{
+    UG_LAUNCH(c, k_vec_scale_add, div_up(n, NT), NT, 0, n, dest, alpha, a, beta, b);
+}
+
+// dest = alpha*v1 + beta*A*w1 (SparseMatrix::axpy, sparsematrix_impl.h:294-342)
+__global__ void __launch_bounds__(NT) k_sell_axpy(SellView<double> A, double *dest, double alpha, const double *v1,
+                                                  double beta, const double *__restrict__ w1)
+{
+    const int stride = gridDim.x * NT;
+    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
+        double aw = sell_row<double, double, double>(A, w1, row);
+        dest[row] = (alpha == 0.0 ? 0.0 : alpha * v1[row]) + beta * aw;
+    }
+}
+
+void sell_axpy(Ctx &c, const Sell<double> &A, double *dest, double alpha, const double *v1, double beta,
+               const double *w1)
+{
+    UG_LAUNCH(c, k_sell_axpy, row_grid(c, A.nrows), NT, 0, view(A), dest, alpha, v1, beta, w1);
+}
+
+// dest += beta * A^T w1 (atomics; API path only)
+__global__ void k_csr_axpy_t(int nrows, const int *rowptr, const int *col, const double *val, double *dest,
+                             double beta, const double *w1)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    double wr = beta * w1[r];
+    for (int a = rowptr[r]; a < rowptr[r + 1]; ++a)
+        if (val[a] != 0.0) atomicAdd(dest + col[a], val[a] * wr);
+}
+
+void csr_axpy_transposed(Ctx &c, const Csr &A, double *dest, double beta, const double *w1)
+{
+    UG_LAUNCH(c, k_csr_axpy_t, div_up(A.nrows, NT), NT, 0, A.nrows, A.rowptr.p, A.col.p, A.val.p, dest, beta, w1);
+}
+
+template <class TO, class TI>
+__global__ void k_convert(int n, const TI *in, TO *out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (TO)in[i];
+}
+
+template <class TO, class TI>
+void convert(Ctx &c, int n, const TI *in, TO *out)
+{
+    UG_LAUNCH(c, (k_convert<TO, TI>), div_up(n, NT), NT, 0, n, in, out);
+}
+template void convert<float, double>(Ctx &, int, const double *, float *);
+template void convert<double, float>(Ctx &, int, const float *, double *);
+template void convert<double, double>(Ctx &, int, const double *, double *);
+
+}  // namespace ug4gb
