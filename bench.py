@@ -1,0 +1,393 @@
+"""Benchmark: DoFs/s of the GMG-preconditioned CG solve to 1e-10 relative
+residual (UG4/ugcore FV1 assemble-and-solve path) on one GB300.
+
+Workload (default): 3D Poisson on the unit cube, 2x2x2 hexahedra refined 6
+times (129^3 = 2,146,689 DoFs, 57,066,625 nonzeros), FV1, zero Dirichlet
+boundary, seeded source f ~ U[-1,1], GMG V(2,2) damped Jacobi (0.6),
+StdTransfer, LU base, CG to ||r||/||r0|| < 1e-10 from x0 = 0, FP64.
+One "step" = one complete solve on device-resident data.  The matrix
+(0.69 GB CRS) is larger than L2 (129 MB), so no L2 flush is needed between
+steps.  The mixed-precision (FP32 GMG inside FP64 CG) solve and the assembly
+are measured as extra fields.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun with N > 1 every rank solves its own replica on its own GPU
+("replicas only": the path has no data exchange at one GPU per problem);
+value = N * DoFs / max-over-ranks time per step.  --impl reference times the
+CPU oracle port of the reference algebra (oracle/, single-threaded like
+ugcore's hot path) on the same workload, rank 0 only.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DoFs/s for GMG-PCG solve to 1e-10 rel (FP64 vs mixed) + adjoint grad time"
+UNIT = "DoFs/s"
+WORKLOAD = "c1: 3D Poisson FP64, unit cube 2x2x2 hex refined 6x (129^3 = 2,146,689 DoFs), GMG V(2,2) Jacobi(0.6)-PCG to 1e-10"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.remove(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for i, nm in enumerate(names):
+                if r[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ----------------------------------------------------- byte accounting ----
+def level_sizes(p):
+    """(N, nnz, nslices, nnz_P, nnz_R) per level, from the device matrices."""
+    import ugcore_gb300 as ug
+    out = []
+    for l in range(p.hier.num_levels):
+        A = ug.GPUSparseMatrix(p.ctx)
+        p.disc.assemble_jacobian(A, l)
+        n, _, nnz = A.info()
+        nP = nR = 0
+        if l > p.cfg["base"]:
+            nP = len(p.gmg.transfer(l, 0)[1])
+            nR = len(p.gmg.transfer(l, 1)[1])
+        out.append(dict(N=n, nnz=nnz, ns=(n + 31) // 32, nP=nP, nR=nR))
+    return out
+
+
+def op_bytes(sz, sv):
+    """algorithmic bytes of one sweep over a level operator.  Structured levels
+    use the constant-offset layout, which needs no column indices: nnz*sv."""
+    return sz["nnz"] * sv
+
+
+def smooth_bytes(sz, sv, top):
+    """algorithmic bytes of the 4 fused Jacobi launches of one V(2,2) visit of a level:
+    operator values once per launch; vectors once per launch."""
+    N, M = sz["N"], op_bytes(sz, sv)
+    din = 8 if top else sv                      # top pre-step reads the FP64 defect r
+    pre1 = M + N * (din + sv + sv + sv)         # x=d_in, dinv, sc w, d_out w
+    pre2 = M + N * (sv + sv + 2 * sv + sv)      # x=d, dinv, sc r/w, d_out w
+    post1 = M + N * (sv + sv + sv + 2 * sv + sv)  # w, d_base, dinv, sc r/w, d_out w
+    post2 = M + N * (sv + sv + 2 * sv + (8 if top else 0))  # d, dinv, sc r/w, (r for rho)
+    return pre1 + pre2 + post1 + post2
+
+
+def iteration_bytes(sizes, sv):
+    """algorithmic bytes of one PCG iteration (V(2,2) cycle + CG kernels)."""
+    L = len(sizes) - 1
+    tot = 0
+    for l in range(1, L + 1):
+        s, c = sizes[l], sizes[l - 1]
+        tot += smooth_bytes(s, sv, l == L)
+        tot += s["nR"] * (sv + 4) + 8 * ((c["N"] + 31) // 32) + s["N"] * sv + c["N"] * sv   # restrict
+        tot += s["nP"] * (sv + 4) + 8 * s["ns"] + c["N"] * sv + s["N"] * (2 * sv + sv + sv)  # prolong
+    b = sizes[0]["N"]
+    tot += b * b * 8 + 2 * b * sv                                  # dense base solve
+    top = sizes[L]
+    tot += op_bytes(top, 8) + top["N"] * (sv + 16 + 16)          # q = A z + beta q, p update, (q,p)
+    tot += top["N"] * 48                                            # x, r updates + norm
+    return tot
+
+
+def assembly_bytes(p, sz):
+    N, E = sz["N"], p.hier.num_elements()
+    k = 8 if p.cfg["elem"] == "hex" else 4
+    dim = p.hier.dim
+    return 8 * dim * N + 4 * k * E + 8 * E + sz["nnz"] * 12 + 4 * (N + 1) + 8 * N
+
+
+def profile_summary(prof, top=14):
+    """largest per-kernel totals of one profiled solve: tag|kernel -> [launches, ms]"""
+    items = sorted(prof.items(), key=lambda kv: -kv[1][1])[:top]
+    return {k.replace("decltype(mv)", "MV"): [v[0], round(v[1], 4)] for k, v in items}
+
+
+def max_over_ranks(v, world):
+    """max of a per-rank float over all ranks (NCCL on GPUs, gloo on CPU)."""
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms_local, n, world):
+    """whole-job DoFs/s of `world` independent replicas of an n-DoF solve:
+    world * n / (max over ranks of ms per step)."""
+    ms = max_over_ranks(ms_local, world)
+    return world * n / (ms * 1e-3), ms
+
+
+# ------------------------------------------------------------ our arm -----
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+
+    torch.cuda.set_device(local_rank)
+    ctx = ug.Context(local_rank)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    cfg = problems.config("c1", precision="fp64")
+    t0 = time.perf_counter()
+    p = problems.Problem(ctx, cfg)
+    ctx.synchronize()
+    setup_s = time.perf_counter() - t0
+    n = p.n
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def timed(fn, steps):
+        barrier()
+        torch.cuda.synchronize()
+        ctx.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+        return e0.elapsed_time(e1) / steps
+
+    for _ in range(args.warmup):
+        st = p.solve()
+    clk = ClockSampler(local_rank)
+    clk.start()
+    k0 = ctx.kernel_launches()
+    ms = timed(p.solve, args.steps)
+    launches = ctx.kernel_launches() - k0
+    clocks = clk.stop()
+    st = p.solve()
+    value, ms_max = replica_value(ms, n, world)
+
+    # ---- e2e: C ABI with host buffers (H2D of b, D2H of x inside the region)
+    b_host = torch.empty(n, dtype=torch.float64).pin_memory()
+    x_host = torch.empty(n, dtype=torch.float64).pin_memory()
+    p.b.copy_to(b_host.numpy())
+    p.solver.solve_host(b_host, x_host)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        p.solver.solve_host(b_host, x_host)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_ms = max_over_ranks(e2e_ms, world)
+
+    # ---- live per-kernel timing (CUDA events on the library stream)
+    sizes = level_sizes(p)
+    ctx.profile_begin()
+    p.solve()
+    prof = ctx.profile_end()
+    iters = st["steps"]
+    top = len(sizes) - 1
+    hbm, peak_kind = peaks()
+    smooth = [(k, v) for k, v in prof.items() if k.startswith("L%d|" % top) and "k_smooth" in k]
+    s_cnt = sum(v[0] for _, v in smooth)
+    s_ms = sum(v[1] for _, v in smooth)
+    visits = s_cnt / 4.0
+    s_bytes = smooth_bytes(sizes[top], 8, True) * visits
+    achieved = s_bytes / (s_ms * 1e-3) / 1e9
+    total_prof_ms = sum(v[1] for v in prof.values())
+    it_bytes = iteration_bytes(sizes, 8)
+    solve_gbs = it_bytes * iters / (ms * 1e-3) / 1e9
+
+    # ---- mixed precision variant of the same workload
+    mixed = None
+    if not args.no_extras:
+        pm = problems.Problem(ctx, problems.config("c1", precision="mixed"))
+        for _ in range(args.warmup):
+            pm.solve()
+        ms_m = max_over_ranks(timed(pm.solve, args.steps), world)
+        ctx.profile_begin()
+        pm.solve()
+        prof_m = ctx.profile_end()
+        stm = pm.solve()
+        xm, x64 = pm.x.numpy(), p.x.numpy()
+        mixed = {"value": world * n / (ms_m * 1e-3), "ms_per_step": ms_m, "steps_pcg": stm["steps"],
+                 "speedup_vs_fp64": ms_max / ms_m,
+                 "rel_residual": stm["defect"] / stm["initial_defect"],
+                 "max_rel_diff_vs_fp64_solution": float(abs(xm - x64).max() / abs(x64).max()),
+                 "hbm_gbs_solve": iteration_bytes(sizes, 4) * stm["steps"] / (ms_m * 1e-3) / 1e9,
+                 "kernel_profile": profile_summary(prof_m)}
+        del pm
+
+    # ---- assembly throughput (top level, FP64 FV1 + CRS values + rhs)
+    asm = None
+    if not args.no_extras:
+        A2 = ug.GPUSparseMatrix(ctx)
+        b2 = ug.GPUVector(ctx, n)
+        p.disc.assemble_linear(A2, b2)   # pattern build (first call)
+        ms_a = timed(lambda: p.disc.assemble_linear(A2, b2), 3)
+        asm = {"ms": ms_a, "dofs_per_s": n / (ms_a * 1e-3),
+               "gbs": assembly_bytes(p, sizes[top]) / (ms_a * 1e-3) / 1e9, "setup_s_all_levels": setup_s}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_sample()
+
+    if rank != 0:
+        return None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded splitmix64 source, structured grid)",
+        "config": {"workload": WORKLOAD, "dofs": n, "nnz": sizes[top]["nnz"], "pcg_steps": iters,
+                   "rel_residual": st["defect"] / st["initial_defect"], "levels": len(sizes),
+                   "l2": "inputs larger than L2 (matrix %.2f GB > 129 MB), no flush" % (sizes[top]["nnz"] * 12e-9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
+                "api": "ug4gb_solver_solve_host (C ABI, pinned host b in, x out)"},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "k_smooth (fused damped-Jacobi SpMV, top level, 4 launches/cycle)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "traffic": None,
+                     "bytes_per_launch": s_bytes / max(s_cnt, 1), "avg_launch_ms": s_ms / max(s_cnt, 1),
+                     "share_of_solve": s_ms / total_prof_ms if total_prof_ms else None},
+        "solve_roofline": {"achieved": solve_gbs, "peak": hbm, "unit": "GB/s", "frac": solve_gbs / hbm,
+                           "bytes_per_iteration": it_bytes},
+        "kernel_profile": profile_summary(prof),
+        "mixed": mixed,
+        "assembly": asm,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    return line
+
+
+def cpu_baseline_sample():
+    """oracle port (restated ugcore algebra, 1 core) on the same workload:
+    one full c1 solve after assembling all levels."""
+    from oracle import oracle as orc
+    orc.build()
+    t0 = time.perf_counter()
+    P = orc.Problem(orc.make_params(elem_type=orc.ORC_HEX, mx=2, my=2, mz=2, nref=6, seed=1))
+    t1 = time.perf_counter()
+    s = P.solve()
+    t2 = time.perf_counter()
+    return {"value": P.nv() / (t2 - t1), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "one full c1 solve (%d DoFs, %d PCG steps, %.1f s) after %.1f s of assembly/setup; "
+                      "single thread like ugcore's hot path" % (P.nv(), s["steps"], t2 - t1, t1 - t0)}
+
+
+# ------------------------------------------------------ reference arm -----
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from oracle import oracle as orc
+    orc.build()
+    P = orc.Problem(orc.make_params(elem_type=orc.ORC_HEX, mx=2, my=2, mz=2, nref=6, seed=1))
+    for _ in range(min(args.warmup, 1)):
+        P.solve()
+    t = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        s = P.solve()
+        t.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(t) / len(t)
+    value = P.nv() / (ms * 1e-3)
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": min(args.warmup, 1), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded splitmix64 source, structured grid)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "dofs": P.nv(), "pcg_steps": s["steps"]},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": "full c1 solve per step; the reference hot path is single-threaded "
+                                       "(OpenMP off, ugcore cmake/ug_includes.cmake:188)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, local_rank)
+    if line is not None:
+        print(json.dumps(line))
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -73,6 +73,19 @@ UG4GB_API int ug4gb_synchronize(ug4gb_ctx *ctx);
 UG4GB_API void *ug4gb_stream(ug4gb_ctx *ctx);
 /* number of kernels this context has launched so far (instrumentation) */
 UG4GB_API int64_t ug4gb_kernel_launches(const ug4gb_ctx *ctx);
+/* solve layout of operators set up after this call: UG4GB_FORMAT_AUTO (the
+   constant-offset "diagonal" layout whenever an operator has <= 27 distinct
+   column offsets, else SELL-32) or UG4GB_FORMAT_SELL (always SELL-32).  The
+   exported CRS never changes; only the copy the kernels stream does. */
+#define UG4GB_FORMAT_AUTO 0
+#define UG4GB_FORMAT_SELL 1
+UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
+/* per-launch CUDA-event timing of every kernel until profile_end, which
+   writes "tag|kernel<TAB>launches<TAB>total_ms" lines into buf.  While it is
+   on, solvers launch kernels directly instead of replaying CUDA graphs.
+   (Stands in for ugcore's PROFILE_BEGIN/END probes, common/profiler/profiler.h.) */
+UG4GB_API int ug4gb_profile_begin(ug4gb_ctx *ctx);
+UG4GB_API int ug4gb_profile_end(ug4gb_ctx *ctx, char *buf, int capacity);
 
 /* ------------------------------------------------------ grid hierarchy -- */
 /* Replaces MultiGrid + GlobalMultiGridRefiner::perform_refinement

@@ -1,0 +1,107 @@
+"""The C-ABI boundary without a GPU: the library builds, loads and exports
+every entry point include/ug4gb.h declares; calls fail with status codes
+(no exception, no crash) when no device is present; the header compiles as
+C; the C++ adapter layer compiles against the header."""
+import ctypes
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "ug4gb.h")
+
+
+def declared():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"UG4GB_API\s+[\w\s\*]*?\b(ug4gb_\w+)\s*\(", txt)))
+
+
+def test_header_declares_entry_points():
+    names = declared()
+    assert len(names) >= 60
+    from ugcore_gb300 import _lib
+    assert set(names) == set(_lib.exported_symbols()), set(names) ^ set(_lib.exported_symbols())
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", built_lib], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\sT\s(ug4gb_\w+)", out))
+    missing = set(declared()) - exported
+    assert not missing, missing
+    lib = ctypes.CDLL(built_lib)
+    for n in declared():
+        assert getattr(lib, n)
+
+
+def test_calls_without_device_return_status(built_lib):
+    from ugcore_gb300 import _lib
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    rc = L.ug4gb_create(0, ctypes.byref(h))
+    assert rc < 0 and not h.value
+    # null handles are rejected, not dereferenced
+    assert L.ug4gb_vector_set(None, 1.0) == _lib.ERR_INVALID
+    assert L.ug4gb_solver_init(None, None) == _lib.ERR_INVALID
+    assert L.ug4gb_gmg_apply(None, None, None) == _lib.ERR_INVALID
+    assert L.ug4gb_last_error(None) == b"null context"
+
+
+def test_header_is_plain_c(tmp_path):
+    cc = shutil.which("gcc") or shutil.which("cc")
+    src = tmp_path / "t.c"
+    src.write_text('#include "ug4gb.h"\nint main(void){ ug4gb_ctx *c = 0; return ug4gb_create(0, &c) == 12345; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-fsyntax-only", "-I" + os.path.join(ROOT, "include"),
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_cpp_adapter_compiles_and_links(built_lib, tmp_path):
+    cxx = shutil.which("g++")
+    src = tmp_path / "a.cpp"
+    src.write_text(r'''
+#include "ug4gb.hpp"
+#include <cstdio>
+int main() {
+    try {
+        ug4gb::Context ctx(0);
+        ug4gb::Grid g(ctx, UG4GB_HEX, 2, 2, 2, 2);
+        ug4gb::Disc d(ctx, g);
+        d.set_diffusion(1.0);
+        d.set_source_uniform(1);
+        int top = g.num_levels() - 1;
+        ug4gb::Matrix A(ctx.get());
+        ug4gb::Vector b(ctx.get(), g.num_vertices(top)), x(ctx.get(), g.num_vertices(top));
+        d.assemble_linear(top, A, b);
+        ug4gb::GMG gmg(ctx, d);
+        gmg.set_smoother(UG4GB_SMOOTHER_JACOBI, 0.6);
+        gmg.init(A);
+        ug4gb::Solver cg(ctx, UG4GB_SOLVER_CG);
+        cg.set_preconditioner(&gmg);
+        cg.set_convergence_check(100, 1e-300, 1e-10);
+        cg.init(A);
+        bool ok = cg.apply(x, b);
+        std::printf("steps %d ok %d\n", cg.steps(), (int)ok);
+        return ok ? 0 : 3;
+    } catch (const ug4gb::Error &e) {
+        std::printf("error %d: %s\n", e.code(), e.what());
+        return 2;
+    }
+}
+''')
+    exe = tmp_path / "a.out"
+    r = subprocess.run([cxx, "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"),
+                        "-I" + os.path.join(ROOT, "ugcore_gb300", "adapters"), str(src), built_lib,
+                        "-Wl,-rpath," + os.path.dirname(built_lib), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    import torch
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    if torch.cuda.is_available():
+        assert r.returncode == 0 and "ok 1" in r.stdout, r.stdout + r.stderr
+    else:
+        assert r.returncode == 2 and "error" in r.stdout

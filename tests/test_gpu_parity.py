@@ -142,6 +142,42 @@ def test_gpu_against_ugcore_algebra_golden(ctx, name):
     assert np.abs(x - g["x"]).max() <= 1e-8 * np.abs(g["x"]).max()
 
 
+@pytest.mark.parametrize("name,over", [("c2", dict(nref=2)), ("c4", dict(nref=2)), ("c3", dict(nref=4))])
+def test_bitwise_reproducible(ctx, name, over):
+    """assembly (coloured, no atomics), reductions and the solve give the same
+    bits in every run"""
+    import ugcore_gb300 as ug
+    cfg, p = _problem(ctx, name, over)
+    a1 = p.A.export_csr()[2]
+    b1 = p.b.numpy()
+    p.solve()
+    x1 = p.x.numpy()
+    A2 = ug.GPUSparseMatrix(ctx)
+    b2 = ug.GPUVector(ctx, p.n)
+    p.disc.assemble_linear(A2, b2)
+    assert np.array_equal(a1, A2.export_csr()[2]) and np.array_equal(b1, b2.numpy())
+    p.solve()
+    assert np.array_equal(x1, p.x.numpy())
+
+
+@pytest.mark.parametrize("name,over", [("c0", dict(nref=4)), ("c1", dict(nref=3)), ("c2", dict(nref=2)),
+                                       ("c4", dict(nref=2)), ("c1", dict(nref=3, smoother="mcgs", damp=1.0))])
+def test_sell_and_diagonal_layouts_agree(ctx, name, over):
+    """the automatic diagonal layout and SELL-32 give the same solve"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    cfg = problems.config(name, **over)
+    c2 = ug.Context(0)
+    c2.set_operator_format("sell")
+    p1 = problems.Problem(ctx, cfg)
+    p2 = problems.Problem(c2, cfg)
+    s1, s2 = p1.solve(), p2.solve()
+    assert s1["steps"] == s2["steps"]
+    x1, x2 = p1.x.numpy(), p2.x.numpy()
+    tol = 1e-13 if cfg["precision"] == "fp64" else 1e-7
+    assert np.abs(x1 - x2).max() <= tol * np.abs(x2).max()
+
+
 def test_edge_cases(ctx):
     """zero rhs (converged at step 0), single-level hierarchy (base == top),
     W-cycle, no pre-smoothing, base level above 0"""

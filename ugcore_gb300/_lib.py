@@ -45,6 +45,9 @@ _SIGS = {
     "ug4gb_synchronize": (I, [P]),
     "ug4gb_stream": (P, [P]),
     "ug4gb_kernel_launches": (I64, [P]),
+    "ug4gb_set_operator_format": (I, [P, I]),
+    "ug4gb_profile_begin": (I, [P]),
+    "ug4gb_profile_end": (I, [P, C.c_char_p, I]),
     "ug4gb_grid_create_structured": (I, [P, I, I, I, I, I, PP]),
     "ug4gb_grid_num_levels": (I, [P]),
     "ug4gb_grid_level_info": (I, [P, I, PI, PI, PI, PI]),

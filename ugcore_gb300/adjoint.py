@@ -1,0 +1,92 @@
+"""Differentiable FV1 solve: u = A(exp(m))^{-1} b(f) as a torch.autograd.Function.
+
+No ugcore counterpart (ugcore has no adjoint).  The forward pass assembles the
+operator for the element log-coefficients m and the vertex source f on the
+GPU, re-initialises the multigrid (coarse levels get the children's mean m)
+and solves with GMG-preconditioned CG/BiCGStab.  The backward pass solves the
+transposed system A^T lambda = dJ/du with the same multigrid built on the
+transposed level operators (Dirichlet rows reset to identity) and forms
+    dJ/dm_e = -K_e * sum_{i not Dirichlet} lambda_i (A1_e u_e)_i
+    dJ/df_i = lambda_i * |SCV_i|
+with element-local kernels.  Level checkpointing: the forward pass keeps only
+u (one vector) for the backward pass; the multigrid hierarchy of the adjoint
+is rebuilt from the stored operators instead of keeping per-level forward
+states, so the memory cost of the backward pass is one extra hierarchy.
+"""
+import torch
+
+from . import problems
+from .algebra import GPUVector
+
+
+class DifferentiableProblem(problems.Problem):
+    """A Problem whose coefficient and source come from torch tensors."""
+
+    def __init__(self, ctx, cfg, m=None, f=None):
+        cfg = dict(cfg)
+        cfg["coef"] = "logk"
+        super().__init__(ctx, cfg, m_top=None if m is None else m.detach().cpu().numpy(),
+                         f_top=None if f is None else f.detach().cpu().numpy())
+        self.num_elements = self.hier.num_elements()
+
+    def update(self, m, f):
+        """re-assemble for new (m, f) (CUDA float64 tensors) and re-initialise."""
+        torch.cuda.synchronize()
+        self.disc.set_log_diffusion(m.detach().contiguous())
+        self.disc.set_source(f.detach().contiguous())
+        self.disc.assemble_linear(self.A, self.b)
+        self.gmg.init(self.A)
+        self.solver.init(self.A)
+        self.AT = None
+
+    def solve_into(self, out):
+        """solve and copy u into the CUDA tensor out"""
+        self.solve()
+        v = GPUVector(self.ctx, wrap=out)
+        v.scale_add(1.0, self.x, 0.0, self.x)
+        self.ctx.synchronize()
+        return out
+
+    def backward(self, u_tensor, grad_u):
+        self.adjoint_setup()
+        if getattr(self, "_interior", None) is None:
+            _, _, bnd = self.hier.export()
+            self._interior = torch.tensor(1.0 - bnd.astype("float64"), device=u_tensor.device)
+        # rhs = dJ/du without its Dirichlet entries
+        rhs_t = (grad_u.detach() * self._interior).contiguous()
+        u_t = u_tensor.detach().contiguous()
+        torch.cuda.synchronize()
+        rhs = GPUVector(self.ctx, wrap=rhs_t)
+        u = GPUVector(self.ctx, wrap=u_t)
+        self.lam.set(0.0)
+        self.solverT.apply(self.lam, rhs)
+        gm = torch.empty(self.num_elements, dtype=torch.float64, device=u_tensor.device)
+        gf = torch.empty(self.n, dtype=torch.float64, device=u_tensor.device)
+        self.disc.grad_logk(u, self.lam, out=gm)
+        self.disc.grad_source(self.lam, out=gf)
+        self.ctx.synchronize()
+        self.last_adjoint_stats = self.solverT.stats()
+        return gm, gf
+
+
+class FV1Solve(torch.autograd.Function):
+    """u = FV1Solve.apply(m, f, problem): differentiable in m and f."""
+
+    @staticmethod
+    def forward(ctx, m, f, problem):
+        problem.update(m, f)
+        u = torch.empty(problem.n, dtype=torch.float64, device=m.device)
+        problem.solve_into(u)
+        ctx.problem = problem
+        ctx.save_for_backward(u)
+        return u
+
+    @staticmethod
+    def backward(ctx, grad_u):
+        (u,) = ctx.saved_tensors
+        gm, gf = ctx.problem.backward(u, grad_u)
+        return gm, gf, None
+
+
+def fv1_solve(m, f, problem):
+    return FV1Solve.apply(m, f, problem)

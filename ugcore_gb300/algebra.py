@@ -71,6 +71,23 @@ class Context:
     def kernel_launches(self):
         return lib().ug4gb_kernel_launches(self.h)
 
+    def set_operator_format(self, fmt):
+        """'auto' (diagonal layout for structured operators) or 'sell'."""
+        check(lib().ug4gb_set_operator_format(self.h, {"auto": 0, "sell": 1}[fmt]), self.h)
+
+    def profile_begin(self):
+        check(lib().ug4gb_profile_begin(self.h), self.h)
+
+    def profile_end(self):
+        """{ 'tag|kernel': (launches, total_ms) } of the launches since profile_begin"""
+        buf = C.create_string_buffer(1 << 20)
+        check(lib().ug4gb_profile_end(self.h, buf, len(buf)), self.h)
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, cnt, ms = line.split("\t")
+            out[name] = (int(cnt), float(ms))
+        return out
+
     @property
     def stream(self):
         return lib().ug4gb_stream(self.h)

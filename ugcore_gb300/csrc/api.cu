@@ -34,6 +34,18 @@ void copy_out(Ctx &c, void *dst, const void *src_dev, size_t bytes)
 
 void gen_level(Ctx &c, Level &L, int elem_type, int cx, int cy, int cz, const Level *coarse);
 
+cudaEvent_t prof_event(Ctx &c)
+{
+    cudaEvent_t e;
+    if (!c.ev_pool.empty()) {
+        e = c.ev_pool.back();
+        c.ev_pool.pop_back();
+    } else {
+        UG_CUDA(cudaEventCreate(&e));
+    }
+    return e;
+}
+
 }  // namespace ug4gb
 
 // Runs f, translating internal errors into status codes (no exception
@@ -83,12 +95,35 @@ int ug4gb_create(int device, ug4gb_ctx **out)
     return UG4GB_OK;
 }
 
+void ug4gb_ctx_retain(ug4gb_ctx *ctx)
+{
+    if (ctx) ctx->refs++;
+}
+
+static void ctx_free(ug4gb_ctx *ctx);
+
+void ug4gb_ctx_release(ug4gb_ctx *ctx)
+{
+    if (ctx && --ctx->refs == 0) ctx_free(ctx);
+}
+
 void ug4gb_destroy(ug4gb_ctx *ctx)
 {
-    if (!ctx) return;
+    if (!ctx || ctx->closed) return;
+    ctx->closed = true;
+    ug4gb_ctx_release(ctx);
+}
+
+static void ctx_free(ug4gb_ctx *ctx)
+{
     cudaSetDevice(ctx->c.device);
     if (ctx->c.stream) cudaStreamSynchronize(ctx->c.stream);
     if (ctx->c.host_pinned) cudaFreeHost(ctx->c.host_pinned);
+    for (auto &r : ctx->c.prof) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : ctx->c.ev_pool) cudaEventDestroy(e);
     ctx->c.red_partials.release();
     ctx->c.red_counter.release();
     ctx->c.red_result.release();
@@ -107,6 +142,60 @@ int ug4gb_synchronize(ug4gb_ctx *ctx)
 void *ug4gb_stream(ug4gb_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
 
 int64_t ug4gb_kernel_launches(const ug4gb_ctx *ctx) { return ctx ? ctx->c.launches : -1; }
+
+int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format)
+{
+    if (!ctx || (format != UG4GB_FORMAT_AUTO && format != UG4GB_FORMAT_SELL)) return UG4GB_ERR_INVALID;
+    ctx->c.allow_dia = (format == UG4GB_FORMAT_AUTO);
+    return UG4GB_OK;
+}
+
+int ug4gb_profile_begin(ug4gb_ctx *ctx)
+{
+    if (!ctx) return UG4GB_ERR_INVALID;
+    return guarded(ctx, [&] {
+        UG_CUDA(cudaStreamSynchronize(ctx->c.stream));
+        for (auto &r : ctx->c.prof) {
+            ctx->c.ev_pool.push_back(r.a);
+            ctx->c.ev_pool.push_back(r.b);
+        }
+        ctx->c.prof.clear();
+        ctx->c.profiling = true;
+    });
+}
+
+int ug4gb_profile_end(ug4gb_ctx *ctx, char *buf, int cap)
+{
+    if (!ctx || !buf || cap <= 0) return UG4GB_ERR_INVALID;
+    return guarded(ctx, [&] {
+        Ctx &c = ctx->c;
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        c.profiling = false;
+        std::vector<std::pair<std::string, std::pair<int, double>>> acc;
+        for (auto &r : c.prof) {
+            float ms = 0.f;
+            UG_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+            size_t i = 0;
+            for (; i < acc.size(); ++i)
+                if (acc[i].first == r.name) break;
+            if (i == acc.size()) acc.push_back({r.name, {0, 0.0}});
+            acc[i].second.first += 1;
+            acc[i].second.second += ms;
+            c.ev_pool.push_back(r.a);
+            c.ev_pool.push_back(r.b);
+        }
+        c.prof.clear();
+        std::string out;
+        for (auto &a : acc) {
+            char line[512];
+            snprintf(line, sizeof(line), "%s\t%d\t%.6f\n", a.first.c_str(), a.second.first, a.second.second);
+            out += line;
+        }
+        int n = (int)out.size() < cap - 1 ? (int)out.size() : cap - 1;
+        memcpy(buf, out.data(), n);
+        buf[n] = 0;
+    });
+}
 
 // ------------------------------------------------------------------ grid --
 int ug4gb_grid_create_structured(ug4gb_ctx *ctx, int elem_type, int mx, int my, int mz, int nref, ug4gb_grid **out)
@@ -135,6 +224,7 @@ int ug4gb_grid_create_structured(ug4gb_ctx *ctx, int elem_type, int mx, int my, 
         delete g;
         return rc;
     }
+    ug4gb_ctx_retain(ctx);
     *out = g;
     return UG4GB_OK;
 }
@@ -167,8 +257,10 @@ int ug4gb_grid_level_export(const ug4gb_grid *g, int level, double *coords, int 
 void ug4gb_grid_destroy(ug4gb_grid *g)
 {
     if (!g) return;
-    cudaStreamSynchronize(g->ctx->c.stream);
+    ug4gb_ctx *ctx = g->ctx;
+    cudaStreamSynchronize(ctx->c.stream);
     delete g;
+    ug4gb_ctx_release(ctx);
 }
 
 // --------------------------------------------------------------- vectors --
@@ -188,6 +280,7 @@ int ug4gb_vector_create(ug4gb_ctx *ctx, int n, ug4gb_vector **out)
         delete v;
         return rc;
     }
+    ug4gb_ctx_retain(ctx);
     *out = v;
     return UG4GB_OK;
 }
@@ -203,6 +296,7 @@ int ug4gb_vector_wrap(ug4gb_ctx *ctx, double *dptr, int n, ug4gb_vector **out)
     v->ctx = ctx;
     v->n = n;
     v->d = dptr;
+    ug4gb_ctx_retain(ctx);
     *out = v;
     return UG4GB_OK;
 }
@@ -266,8 +360,10 @@ int ug4gb_vector_scale_add(ug4gb_vector *dest, double alpha, const ug4gb_vector 
 void ug4gb_vector_destroy(ug4gb_vector *v)
 {
     if (!v) return;
-    cudaStreamSynchronize(v->ctx->c.stream);
+    ug4gb_ctx *ctx = v->ctx;
+    cudaStreamSynchronize(ctx->c.stream);
     delete v;
+    ug4gb_ctx_release(ctx);
 }
 
 // -------------------------------------------------------------- matrices --
@@ -276,6 +372,7 @@ int ug4gb_matrix_create(ug4gb_ctx *ctx, ug4gb_matrix **out)
     if (!ctx || !out) return UG4GB_ERR_INVALID;
     ug4gb_matrix *m = new ug4gb_matrix;
     m->ctx = ctx;
+    ug4gb_ctx_retain(ctx);
     *out = m;
     return UG4GB_OK;
 }
@@ -296,7 +393,7 @@ int ug4gb_matrix_set_csr(ug4gb_matrix *m, int nrows, int ncols, int64_t nnz, con
         copy_in(c, m->A.col.p, col, sizeof(int) * (size_t)nnz);
         copy_in(c, m->A.val.p, val, sizeof(double) * (size_t)nnz);
         UG_CUDA(cudaStreamSynchronize(c.stream));
-        m->sell_valid = false;
+        m->op_valid = false;
         m->pattern_grid = nullptr;
         m->pattern_level = -1;
     });
@@ -329,8 +426,8 @@ int ug4gb_matrix_axpy(const ug4gb_matrix *mc, ug4gb_vector *dest, double alpha1,
     if (!m || !dest || !w1 || dest->n != m->A.nrows || w1->n != m->A.ncols) return UG4GB_ERR_INVALID;
     if (alpha1 != 0.0 && (!v1 || v1->n != m->A.nrows)) return UG4GB_ERR_INVALID;
     return guarded(m->ctx, [&] {
-        m->ensure_sell();
-        sell_axpy(m->ctx->c, m->sell, dest->d, alpha1, alpha1 != 0.0 ? v1->d : dest->d, beta1, w1->d);
+        m->ensure_op();
+        op_axpy(m->ctx->c, m->op, dest->d, alpha1, alpha1 != 0.0 ? v1->d : dest->d, beta1, w1->d);
     });
 }
 
@@ -353,7 +450,7 @@ int ug4gb_matrix_set_as_transpose_of(ug4gb_matrix *T, const ug4gb_matrix *B, int
     return guarded(T->ctx, [&] {
         csr_transpose(T->ctx->c, B->A, T->A, keep_zeros != 0);
         UG_CUDA(cudaStreamSynchronize(T->ctx->c.stream));
-        T->sell_valid = false;
+        T->op_valid = false;
         T->pattern_grid = nullptr;
         T->pattern_level = -1;
     });
@@ -362,8 +459,10 @@ int ug4gb_matrix_set_as_transpose_of(ug4gb_matrix *T, const ug4gb_matrix *B, int
 void ug4gb_matrix_destroy(ug4gb_matrix *m)
 {
     if (!m) return;
-    cudaStreamSynchronize(m->ctx->c.stream);
+    ug4gb_ctx *ctx = m->ctx;
+    cudaStreamSynchronize(ctx->c.stream);
     delete m;
+    ug4gb_ctx_release(ctx);
 }
 
 }  // extern "C"

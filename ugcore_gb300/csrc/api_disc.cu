@@ -61,7 +61,7 @@ void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b)
     } else {
         UG_CUDA(cudaMemsetAsync(A->A.val.p, 0, sizeof(double) * (size_t)A->A.nnz, c.stream));
     }
-    A->sell_valid = false;
+    A->op_valid = false;
     if (b) UG_CUDA(cudaMemsetAsync(b, 0, sizeof(double) * (size_t)L.nv, c.stream));
     const DiscImpl &D = d->d;
     bool top = (level == (int)d->g->lev.size() - 1);
@@ -117,6 +117,7 @@ int ug4gb_disc_create(ug4gb_ctx *ctx, const ug4gb_grid *g, ug4gb_disc **out)
     d->ctx = ctx;
     d->g = g;
     invalidate(d);
+    ug4gb_ctx_retain(ctx);
     *out = d;
     return UG4GB_OK;
 }
@@ -245,7 +246,7 @@ int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A,
         csr_transpose(c, A->A, AT->A, true);
         launch_dirichlet(c, d->g->lev[level], AT->A, nullptr);
         UG_CUDA(cudaStreamSynchronize(c.stream));
-        AT->sell_valid = false;
+        AT->op_valid = false;
         AT->pattern_grid = nullptr;
         AT->pattern_level = -1;
     });
@@ -263,8 +264,10 @@ int ug4gb_disc_export_coefficients(ug4gb_disc *d, int level, double *K)
 void ug4gb_disc_destroy(ug4gb_disc *d)
 {
     if (!d) return;
-    cudaStreamSynchronize(d->ctx->c.stream);
+    ug4gb_ctx *ctx = d->ctx;
+    cudaStreamSynchronize(ctx->c.stream);
     delete d;
+    ug4gb_ctx_release(ctx);
 }
 
 int ug4gb_disc_grad_logk(ug4gb_disc *d, const ug4gb_vector *u, const ug4gb_vector *lam, double *grad)

@@ -186,9 +186,9 @@ struct GmgT : GmgBase {
         UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, dinv64.p, L.dinv.p, n);
         UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, dfac64.p, L.dfac.p, n);
         if (smoother == UG4GB_SMOOTHER_JACOBI) {
-            sell_from_csr<V>(c, L.A, L.At, dinv64.p);
+            op_from_csr<V>(c, L.A, L.At, dinv64.p, c.allow_dia);
         } else {
-            sell_from_csr<V>(c, L.A, L.At, nullptr);
+            op_from_csr<V>(c, L.A, L.At, nullptr, c.allow_dia);
             L.t.alloc(n);
             int ncol = 1 << G.dim;
             L.crow.resize(ncol);
@@ -228,8 +228,8 @@ struct GmgT : GmgBase {
         csr_transpose(c, P, F.R, true);
         UG_LAUNCH(c, k_adjust_R, div_up(Gf.nv, 256), 256, 0, Gf.npar.p, Gf.par.p, Gf.bnd.p, Gf.nv, F.R.rowptr.p,
                   F.R.col.p, F.R.val.p);
-        sell_from_csr<V>(c, F.P, F.Ps, nullptr);
-        sell_from_csr<V>(c, F.R, F.Rs, nullptr);
+        op_from_csr<V>(c, F.P, F.Ps, nullptr, false);
+        op_from_csr<V>(c, F.R, F.Rs, nullptr, false);
         UG_CUDA(cudaStreamSynchronize(c.stream));
     }
 
@@ -260,6 +260,7 @@ struct GmgT : GmgBase {
     {
         const int T = top();
         GLevel<V> &L = lev[l];
+        c.prof_tag = "L" + std::to_string(l);
         if (l == base) {
             // top == base: a single-level "cycle" is the base solve
             UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
@@ -304,6 +305,7 @@ struct GmgT : GmgBase {
         C.dcur = C.dA.p;
         // ---- coarse correction
         if (l - 1 == base) {
+            c.prof_tag = "L" + std::to_string(l - 1);
             base_solve<V>(c, Ainv.p, nbase, C.dA.p, C.sc.p, skip);
         } else {
             for (int i = 0; i < cycle; ++i) {
@@ -311,6 +313,7 @@ struct GmgT : GmgBase {
                 lmgc(c, l - 1, nullptr, i == 0, skip, nullptr, nullptr, 0, rd);
             }
         }
+        c.prof_tag = "L" + std::to_string(l);
         // ---- prolongation + post-smoothing
         prolong_apply<V>(c, L.Ps, C.sc.p, L.sc.p, L.dfac.p, nu2 > 0 ? L.w.p : (V *)nullptr, skip);
         const V *dbase = dpre;
@@ -438,6 +441,7 @@ int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out)
     ug4gb_gmg *m = new ug4gb_gmg;
     m->ctx = ctx;
     m->disc = disc;
+    ug4gb_ctx_retain(ctx);
     *out = m;
     return UG4GB_OK;
 }
@@ -515,6 +519,13 @@ int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
     if (cvec->n != m->n_top || d->n != m->n_top) return UG4GB_ERR_INVALID;
     return guarded(m->ctx, [&] {
         Ctx &c = m->ctx->c;
+        if (c.profiling) {
+            m->impl->apply(c, d->d, nullptr, nullptr, nullptr, 0);
+            if (m->impl->is_fp32()) copy_z<float>(c, m->n_top, (const float *)m->impl->sc_top(), cvec->d, nullptr);
+            else copy_z<double>(c, m->n_top, (const double *)m->impl->sc_top(), cvec->d, nullptr);
+            UG_CUDA(cudaStreamSynchronize(c.stream));
+            return;
+        }
         if (!m->graph || m->graph_d != d->d || m->graph_c != cvec->d) {
             drop_graph(m);
             cudaGraph_t gr;
@@ -567,9 +578,11 @@ int ug4gb_gmg_export_transfer(const ug4gb_gmg *m, int level, int which, int *row
 void ug4gb_gmg_destroy(ug4gb_gmg *m)
 {
     if (!m) return;
-    cudaStreamSynchronize(m->ctx->c.stream);
+    ug4gb_ctx *ctx = m->ctx;
+    cudaStreamSynchronize(ctx->c.stream);
     drop_graph(m);
     delete m;
+    ug4gb_ctx_release(ctx);
 }
 
 }  // extern "C"

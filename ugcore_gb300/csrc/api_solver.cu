@@ -1,10 +1,11 @@
 // api_solver.cu -- CG / BiCGStab drivers with StdConvCheck on the device.
 //
-// One Krylov iteration (preconditioner cycle included) is captured once as a
-// CUDA graph and replayed; all scalars (alpha, beta, rho, omega, defects)
-// stay in device memory and every kernel of an iteration returns at once
-// when the convergence flag is set, so the host only reads one int per
-// iteration to decide whether to replay again.  The iteration count, defect
+// The iteration loop is captured once as a CUDA graph with a conditional
+// WHILE node (body: one Krylov iteration, preconditioner cycle included) and
+// launched once per solve; all scalars (alpha, beta, rho, omega, defects)
+// stay in device memory, the device-side convergence check ends the loop,
+// and every kernel returns at once when the convergence flag is set.  The
+// host synchronises twice per solve.  The iteration count, defect
 // history and stopping rule are those of the reference loop
 // (lib_algebra/operator/linear_solver/cg.h:103-230,
 //  lib_algebra/operator/linear_solver/bicgstab.h:112-400,
@@ -69,7 +70,8 @@ void cg_iteration(ug4gb_solver *s, double *x, double *r, bool first)
     Ctx &c = s->ctx->c;
     RedArgs red = red_of(s);
     const ZT *z = precond<ZT>(s, r, r, first ? 0 : 1);
-    cg_spmv_dot_t<ZT>(c, s->A->sell, z, s->p.p, s->q.p, first ? 1 : 0, red);
+    c.prof_tag = "K";
+    cg_spmv_dot_t<ZT>(c, s->A->op, z, s->p.p, s->q.p, first ? 1 : 0, red);
     cg_update(c, s->n, x, r, s->p.p, s->q.p, red);
 }
 
@@ -79,19 +81,84 @@ void bicg_iteration(ug4gb_solver *s, double *x, double *r)
     Ctx &c = s->ctx->c;
     RedArgs red = red_of(s);
     const int n = s->n;
+    c.prof_tag = "K";
     bicg_restart(c, n, r, s->r0.p, s->p.p, s->v.p, red);
     bicg_rho(c, n, s->r0.p, r, red);
     bicg_p(c, n, r, s->p.p, s->v.p, red);
     const ZT *q = precond<ZT>(s, s->p.p, nullptr, 0);
-    bicg_spmv_dot_t<ZT>(c, s->A->sell, q, s->v.p, s->r0.p, red);
+    c.prof_tag = "K";
+    bicg_spmv_dot_t<ZT>(c, s->A->op, q, s->v.p, s->r0.p, red);
     bicg_x_s<ZT>(c, n, x, q, r, s->v.p, s->s.p, red);
     bicg_s_to_r(c, n, s->s.p, r, red);
     q = precond<ZT>(s, s->s.p, nullptr, 0);
-    bicg_spmv_2dot_t<ZT>(c, s->A->sell, q, s->t.p, s->s.p, red);
+    c.prof_tag = "K";
+    bicg_spmv_2dot_t<ZT>(c, s->A->op, q, s->t.p, s->s.p, red);
     bicg_x_r<ZT>(c, n, x, q, s->s.p, s->t.p, r, red);
 }
 
 bool z_is_fp32(ug4gb_solver *s) { return s->pre && s->pre->impl->is_fp32(); }
+
+// last node of the loop body: keep iterating while the check has not ended
+__global__ void k_loop_cond(cudaGraphConditionalHandle h, const KScal *ks)
+{
+    cudaGraphSetConditional(h, ks->done ? 0u : 1u);
+}
+
+void iteration(ug4gb_solver *s, double *x, double *r, bool f32)
+{
+    if (s->kind == UG4GB_SOLVER_CG) {
+        if (f32) cg_iteration<float>(s, x, r, false);
+        else cg_iteration<double>(s, x, r, false);
+    } else {
+        if (f32) bicg_iteration<float>(s, x, r);
+        else bicg_iteration<double>(s, x, r);
+    }
+}
+
+// The whole iteration loop as one graph: a conditional WHILE node whose body
+// is one Krylov iteration (multigrid cycle included) followed by
+// k_loop_cond.  The loop ends when the device-side StdConvCheck (or a
+// breakdown) sets done, at the latest after max_steps iterations.
+void build_loop_graph(ug4gb_solver *s, double *x, double *r, bool f32)
+{
+    Ctx &c = s->ctx->c;
+    cudaGraph_t g;
+    UG_CUDA(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaGraphExec_t exec = nullptr;
+    int64_t before = c.launches;
+    try {
+        UG_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        UG_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        UG_CUDA(cudaStreamBeginCaptureToGraph(c.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        try {
+            iteration(s, x, r, f32);
+            UG_LAUNCH(c, k_loop_cond, 1, 1, 0, h, (const KScal *)s->ks.p);
+        } catch (...) {
+            cudaGraph_t tmp;
+            cudaStreamEndCapture(c.stream, &tmp);
+            throw;
+        }
+        cudaGraph_t tmp;
+        UG_CUDA(cudaStreamEndCapture(c.stream, &tmp));
+        UG_CUDA(cudaGraphInstantiate(&exec, g, 0));
+    } catch (...) {
+        c.launches = before;
+        cudaGraphDestroy(g);
+        throw;
+    }
+    cudaGraphDestroy(g);
+    s->iter_kernels = c.launches - before;
+    c.launches = before;
+    s->iter_graph = exec;
+}
 
 void read_flags(ug4gb_solver *s, int *done)
 {
@@ -119,49 +186,40 @@ void run(ug4gb_solver *s, double *x, double *r)
     RedArgs red = red_of(s);
     const bool f32 = z_is_fp32(s);
     // prologue: r = b - A x, start the check; CG also does the first step
-    krylov_start(c, s->A->sell, x, r, red);
+    c.prof_tag = "K";
+    krylov_start(c, s->A->op, x, r, red);
     if (s->kind == UG4GB_SOLVER_CG) {
         if (f32) cg_iteration<float>(s, x, r, true);
         else cg_iteration<double>(s, x, r, true);
     }
     int done = 0;
     read_flags(s, &done);
+    if (!done && c.profiling) {
+        // profiled run: direct launches, each one timed with events
+        while (!done) {
+            iteration(s, x, r, f32);
+            read_flags(s, &done);
+        }
+    }
     if (!done) {
         int pre_gen = s->pre ? s->pre->gen : -1;
         if (!s->iter_graph || s->graph_x != x || s->graph_r != r || s->graph_pre_gen != pre_gen) {
             drop_graph(s);
-            cudaGraph_t gr;
-            int64_t before = c.launches;
-            UG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
-            try {
-                if (s->kind == UG4GB_SOLVER_CG) {
-                    if (f32) cg_iteration<float>(s, x, r, false);
-                    else cg_iteration<double>(s, x, r, false);
-                } else {
-                    if (f32) bicg_iteration<float>(s, x, r);
-                    else bicg_iteration<double>(s, x, r);
-                }
-            } catch (...) {
-                cudaStreamEndCapture(c.stream, &gr);
-                throw;
-            }
-            UG_CUDA(cudaStreamEndCapture(c.stream, &gr));
-            s->iter_kernels = c.launches - before;
-            c.launches = before;
-            UG_CUDA(cudaGraphInstantiate(&s->iter_graph, gr, 0));
-            cudaGraphDestroy(gr);
+            build_loop_graph(s, x, r, f32);
             s->graph_x = x;
             s->graph_r = r;
             s->graph_pre_gen = pre_gen;
         }
-        while (!done) {
-            UG_CUDA(cudaGraphLaunch(s->iter_graph, c.stream));
-            c.launches += s->iter_kernels;
-            read_flags(s, &done);
-        }
+        UG_CUDA(cudaGraphLaunch(s->iter_graph, c.stream));
     }
+    int steps_before = s->kind == UG4GB_SOLVER_CG ? 1 : 0;
     UG_CUDA(cudaMemcpyAsync(&s->host_ks, s->ks.p, sizeof(KScal), cudaMemcpyDeviceToHost, c.stream));
     UG_CUDA(cudaStreamSynchronize(c.stream));
+    if (!c.profiling && s->iter_graph && s->host_ks.step > steps_before) {
+        // the loop body ran once per CG step / per BiCGStab pair of half steps
+        int64_t runs = s->kind == UG4GB_SOLVER_CG ? s->host_ks.step - steps_before : (s->host_ks.step + 1) / 2;
+        c.launches += runs * s->iter_kernels;
+    }
     int nh = s->host_ks.step + 1 < h.hist_cap ? s->host_ks.step + 1 : h.hist_cap;
     s->host_hist.resize(nh);
     copy_out(c, s->host_hist.data(), s->hist.p, sizeof(double) * nh);
@@ -193,6 +251,7 @@ int ug4gb_solver_create(ug4gb_ctx *ctx, int kind, ug4gb_solver **out)
         delete s;
         return rc;
     }
+    ug4gb_ctx_retain(ctx);
     *out = s;
     return UG4GB_OK;
 }
@@ -221,7 +280,7 @@ int ug4gb_solver_init(ug4gb_solver *s, const ug4gb_matrix *A)
     return guarded(s->ctx, [&] {
         drop_graph(s);
         ug4gb_matrix *Am = const_cast<ug4gb_matrix *>(A);
-        Am->ensure_sell();
+        Am->ensure_op();
         s->A = A;
         s->n = A->A.nrows;
         size_t n = s->n > 0 ? s->n : 1;
@@ -297,9 +356,11 @@ int ug4gb_solver_get_history(const ug4gb_solver *s, double *hist, int cap)
 void ug4gb_solver_destroy(ug4gb_solver *s)
 {
     if (!s) return;
-    cudaStreamSynchronize(s->ctx->c.stream);
+    ug4gb_ctx *ctx = s->ctx;
+    cudaStreamSynchronize(ctx->c.stream);
     drop_graph(s);
     delete s;
+    ug4gb_ctx_release(ctx);
 }
 
 }  // extern "C"

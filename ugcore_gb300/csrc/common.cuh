@@ -73,12 +73,24 @@ struct DevBuf {
     size_t bytes() const { return n * sizeof(T); }
 };
 
+// Per-launch CUDA-event profiler (off by default; never active while a
+// graph is being captured).  Records (kernel name, rows) -> event pairs.
+struct ProfRec {
+    std::string name;
+    cudaEvent_t a, b;
+};
+
 struct Ctx {
     int device = 0;
     int num_sms = 152;
     cudaStream_t stream = nullptr;
     std::string err;
     int64_t launches = 0;
+    bool profiling = false;
+    bool allow_dia = true;      // operators with <= 27 offsets use the diagonal layout
+    std::string prof_tag;       // set by the orchestration (level / phase)
+    std::vector<ProfRec> prof;
+    std::vector<cudaEvent_t> ev_pool;
     // grid-reduction scratch: partial sums per block and a completion counter
     DevBuf<double> red_partials;        // kRedMaxBlocks * kRedMaxValues
     DevBuf<unsigned int> red_counter;   // one counter per reduction slot
@@ -90,12 +102,24 @@ constexpr int kRedMaxBlocks = 16384;
 constexpr int kRedMaxValues = 2;
 constexpr int kSliceH = 32;
 
+cudaEvent_t prof_event(Ctx &c);
+
 // Kernel launch accounting; every launch of the library goes through this.
 #define UG_LAUNCH(ctx, kernel, grid, block, shmem, ...)                                            \
     do {                                                                                           \
+        cudaEvent_t ev_a_ = nullptr;                                                               \
+        if ((ctx).profiling) {                                                                     \
+            ev_a_ = ::ug4gb::prof_event(ctx);                                                      \
+            UG_CUDA(cudaEventRecord(ev_a_, (ctx).stream));                                         \
+        }                                                                                          \
         kernel<<<(grid), (block), (shmem), (ctx).stream>>>(__VA_ARGS__);                           \
         (ctx).launches++;                                                                          \
         UG_CUDA(cudaGetLastError());                                                               \
+        if ((ctx).profiling) {                                                                     \
+            cudaEvent_t ev_b_ = ::ug4gb::prof_event(ctx);                                          \
+            UG_CUDA(cudaEventRecord(ev_b_, (ctx).stream));                                         \
+            (ctx).prof.push_back(::ug4gb::ProfRec{(ctx).prof_tag + "|" + #kernel, ev_a_, ev_b_});  \
+        }                                                                                          \
     } while (0)
 
 inline unsigned div_up(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }
@@ -132,6 +156,39 @@ inline SellView<T> view(const Sell<T> &s)
 {
     return SellView<T>{s.nrows, s.sptr.p, s.swidth.p, s.col.p, s.val.p};
 }
+
+// Constant-offset (diagonal) layout: row i couples to columns i + off[k],
+// k < S; values stored diagonal-major, val[k*nrows + i]; entries that are
+// absent in the CRS (or fall outside the matrix) are 0 and their column is
+// clamped into range.  Used automatically when a matrix has at most 27
+// distinct column offsets (every level operator of a structured hierarchy:
+// 9, 15 or 27 of them); it carries no column indices at all and its loads do
+// not depend on each other.
+constexpr int kMaxDiag = 32;
+struct Offs {
+    int o[kMaxDiag];
+};
+
+template <class T>
+struct Dia {
+    int nrows = 0, ncols = 0, S = 0;
+    Offs off{};
+    DevBuf<T> val;
+};
+
+// An operator in its solve format: SELL-32 (general) or diagonal.
+template <class T>
+struct OpMat {
+    int kind = 0;   // 0 = SELL-32, 1 = diagonal
+    int nrows = 0, ncols = 0;
+    Sell<T> sell;
+    Dia<T> dia;
+    int64_t stored_bytes() const
+    {
+        if (kind == 1) return (int64_t)dia.S * dia.nrows * (int64_t)sizeof(T);
+        return sell.stored * (int64_t)(sizeof(T) + sizeof(int)) + (int64_t)sell.nslices * 8;
+    }
+};
 
 // ------------------------------------------------------------- grid level --
 struct Level {
@@ -233,6 +290,13 @@ void csr_transpose(Ctx &c, const Csr &B, Csr &T, bool keep_zeros);
 void csr_copy(Ctx &c, const Csr &src, Csr &dst);
 template <class T>
 void sell_from_csr(Ctx &c, const Csr &A, Sell<T> &S, const double *col_scale /* nullable */);
+// distinct column offsets (col - row) of A, sorted; false if more than max_s
+bool csr_offsets(Ctx &c, const Csr &A, int max_s, std::vector<int> &offs);
+template <class T>
+void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs, const double *col_scale);
+// solve format: diagonal when A is square with <= 27 offsets and allow_dia, else SELL-32
+template <class T>
+void op_from_csr(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_scale, bool allow_dia);
 void fill_double(Ctx &c, double *p, size_t n, double v);
 
 }  // namespace ug4gb

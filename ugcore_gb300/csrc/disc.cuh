@@ -21,6 +21,7 @@ struct AsmArgs {
     const int *col;
     double *val;
     double *b;                // rhs or null
+    int cx, cy, cz;           // structured cell counts (set by launch_assemble)
 };
 
 void launch_assemble(Ctx &c, const Level &L, const AsmArgs &a);

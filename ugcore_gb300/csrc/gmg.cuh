@@ -8,7 +8,16 @@
 
 struct ug4gb_ctx {
     ug4gb::Ctx c;
+    int refs = 1;          // the context itself + every live child handle
+    bool closed = false;   // ug4gb_destroy called; freed when refs reaches 0
 };
+
+// Child handles keep their context alive, so handles may be destroyed in any
+// order (e.g. by a garbage collector at interpreter exit).
+extern "C" {
+void ug4gb_ctx_retain(ug4gb_ctx *ctx);
+void ug4gb_ctx_release(ug4gb_ctx *ctx);
+}
 
 struct ug4gb_grid {
     ug4gb_ctx *ctx = nullptr;
@@ -26,15 +35,15 @@ struct ug4gb_vector {
 struct ug4gb_matrix {
     ug4gb_ctx *ctx = nullptr;
     ug4gb::Csr A;
-    ug4gb::Sell<double> sell;
-    bool sell_valid = false;
+    ug4gb::OpMat<double> op;              // solve format of A (SELL-32 or diagonal)
+    bool op_valid = false;
     const void *pattern_grid = nullptr;   // grid/level whose element pattern A holds
     int pattern_level = -1;
-    void ensure_sell()
+    void ensure_op()
     {
-        if (!sell_valid) {
-            ug4gb::sell_from_csr<double>(ctx->c, A, sell, nullptr);
-            sell_valid = true;
+        if (!op_valid) {
+            ug4gb::op_from_csr<double>(ctx->c, A, op, nullptr, ctx->c.allow_dia);
+            op_valid = true;
         }
     }
 };
@@ -65,10 +74,10 @@ template <class V>
 struct GLevel {
     int n = 0;
     Csr A;                       // FP64 level operator
-    Sell<V> At;                  // Jacobi: A * diag(dinv); MCGS: A
+    OpMat<V> At;                 // Jacobi: A * diag(dinv); MCGS: A
     DevBuf<V> dinv, dfac;        // Jacobi: dinv = 1/(a_ii/damp), dfac = a_ii/damp; MCGS: relax/a_ii, 1
     Csr P, R;                    // P: this x coarse, R: coarse x this (FP64, exportable)
-    Sell<V> Ps, Rs;
+    OpMat<V> Ps, Rs;
     DevBuf<V> sc, dA, dB, w, t;
     V *dcur = nullptr;
     std::vector<DevBuf<int>> crow;   // MCGS colour row lists

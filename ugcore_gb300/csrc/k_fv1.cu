@@ -1,6 +1,7 @@
 // k_fv1.cu -- FV1 (vertex-centred box) element assembly on the GPU, FP64.
 //
-// One thread per element.  The element geometry follows FV1Geometry_gen::
+// One thread per cell (a quad, a hex, or the 6 Kuhn tets of a hex), launched
+// once per parity colour.  The element geometry follows FV1Geometry_gen::
 // update (lib_disc/spatial_disc/disc_util/fv1_geom.cpp:331-464): mid points
 // as corner averages, one SCVF per element edge with patch [edge mid, centre]
 // (2D) or [edge mid, side-0 centre, centre, side-1 centre] (3D), area normal
@@ -12,8 +13,9 @@
 // FV1 element disc: F_sh = -(K grad phi_sh).n added to (from, sh) and
 // subtracted from (to, sh); full upwind adds flux = v(ip).n to the upwind
 // column (ConvectionShapesFullUpwind::update, conv_shape.h:277-345); the
-// right-hand side gets f_i |SCV_i|.  Element matrices are scattered with FP64
-// atomics into the level CRS, found by binary search in the sorted row.
+// right-hand side gets f_i |SCV_i|.  Element matrices are added into the
+// level CRS (slots found by binary search in the sorted row) colour by colour,
+// without atomics, so every run assembles the same bits.
 // Reference-element numbering: lib_disc/reference_element/reference_element.cpp
 // (quadrilateral :428, tetrahedron :547, hexahedron :1327).
 #include "common.cuh"
@@ -36,12 +38,25 @@ __device__ __forceinline__ int find_slot(const int *__restrict__ rowptr, const i
 
 
 
+// Cells of one parity colour: cell (i,j,k) with (i&1, j&1, k&1) = colour bits.
+// No two cells of a colour share a vertex, so their element matrices are
+// added with plain read-modify-writes, colour after colour: the assembled
+// values are the same bits in every run (an FP64 atomic scatter would sum in
+// a run-dependent order).  A tet cell is the hexahedron of its 6 Kuhn tets.
+__device__ __forceinline__ int colour_cell(const AsmArgs &a, int t, int colour, int *cell)
+{
+    const int b0 = colour & 1, b1 = (colour >> 1) & 1, b2 = (colour >> 2) & 1;
+    const int n0 = (a.cx - b0 + 1) >> 1, n1 = (a.cy - b1 + 1) >> 1, n2 = (a.cz - b2 + 1) >> 1;
+    if (t >= n0 * n1 * n2) return 0;
+    const int t0 = t % n0, t1 = (t / n0) % n1, t2 = t / (n0 * n1);
+    *cell = (2 * t0 + b0) + a.cx * ((2 * t1 + b1) + a.cy * (2 * t2 + b2));
+    return 1;
+}
+
 template <int T>
-__global__ void __launch_bounds__(128) k_assemble(AsmArgs a)
+__device__ __forceinline__ void assemble_element(const AsmArgs &a, int e)
 {
     using E = Elem<T>;
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= a.ne) return;
     int ev[E::K];
     double X[E::K][E::DIM];
 #pragma unroll
@@ -59,14 +74,26 @@ __global__ void __launch_bounds__(128) k_assemble(AsmArgs a)
 #pragma unroll
         for (int j = 0; j < E::K; ++j) {
             int s = find_slot(a.rowptr, a.col, ev[i], ev[j]);
-            if (s >= 0) atomicAdd(a.val + s, Aloc[i][j]);
+            if (s >= 0) a.val[s] += Aloc[i][j];
         }
     if (a.b) {
 #pragma unroll
         for (int i = 0; i < E::K; ++i) {
             double fi = a.f ? a.f[ev[i]] : (a.use_seed ? 2.0 * hash_uniform(a.f_seed, (uint64_t)ev[i]) - 1.0 : 0.0);
-            atomicAdd(a.b + ev[i], fi * vol[i]);
+            a.b[ev[i]] += fi * vol[i];
         }
+    }
+}
+
+template <int T>
+__global__ void __launch_bounds__(128) k_assemble(AsmArgs a, int colour)
+{
+    int cell;
+    if (!colour_cell(a, blockIdx.x * blockDim.x + threadIdx.x, colour, &cell)) return;
+    if (T == UG4GB_TET) {
+        for (int p = 0; p < 6; ++p) assemble_element<T>(a, 6 * cell + p);
+    } else {
+        assemble_element<T>(a, cell);
     }
 }
 
@@ -81,12 +108,20 @@ __global__ void k_dirichlet_rows(const unsigned char *bnd, int nv, const int *ro
     if (b) b[v] = 0.0;
 }
 
-void launch_assemble(Ctx &c, const Level &L, const AsmArgs &a)
+void launch_assemble(Ctx &c, const Level &L, const AsmArgs &a_in)
 {
-    unsigned g = div_up(L.ne, 128);
-    if (L.elem_type == UG4GB_QUAD) UG_LAUNCH(c, k_assemble<UG4GB_QUAD>, g, 128, 0, a);
-    else if (L.elem_type == UG4GB_HEX) UG_LAUNCH(c, k_assemble<UG4GB_HEX>, g, 128, 0, a);
-    else UG_LAUNCH(c, k_assemble<UG4GB_TET>, g, 128, 0, a);
+    AsmArgs a = a_in;
+    a.cx = L.nx - 1;
+    a.cy = L.ny - 1;
+    a.cz = (L.dim == 3) ? L.nz - 1 : 1;
+    const int ncol = (L.dim == 3) ? 8 : 4;
+    const int per = ((a.cx + 1) / 2) * ((a.cy + 1) / 2) * ((a.cz + 1) / 2);
+    unsigned g = div_up(per, 128);
+    for (int colour = 0; colour < ncol; ++colour) {
+        if (L.elem_type == UG4GB_QUAD) UG_LAUNCH(c, k_assemble<UG4GB_QUAD>, g, 128, 0, a, colour);
+        else if (L.elem_type == UG4GB_HEX) UG_LAUNCH(c, k_assemble<UG4GB_HEX>, g, 128, 0, a, colour);
+        else UG_LAUNCH(c, k_assemble<UG4GB_TET>, g, 128, 0, a, colour);
+    }
 }
 
 void launch_dirichlet(Ctx &c, const Level &L, Csr &A, double *b)
@@ -136,50 +171,68 @@ void launch_coef_fourier(Ctx &c, const Level &L, int nmodes, const double *k, co
         UG_LAUNCH(c, k_coef_fourier<UG4GB_TET>, g, 256, 0, L.coords.p, L.elems.p, L.ne, nmodes, k, phase, amp, factor, K);
 }
 
-// coarse log K = mean of the children's log K (structured children)
-__global__ void k_coarsen_log(int elem_type, const double *fcoords, const int *felems, int fne, int fnx, int fny,
-                              int fnz, int cnx, int cny, const double *logf, double *sumc, int *cntc)
+// coarse log K = mean of the children's log K.  Gather: each coarse element
+// sums its structured children in increasing fine-element order (no atomics,
+// same order as the oracle).  A fine Kuhn tet belongs to the coarse Kuhn tet
+// whose permutation orders its centroid's offsets inside the coarse hex.
+__device__ __forceinline__ int kuhn_perm_of(const double *off)
 {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= fne) return;
-    int fx = fnx - 1, fy = fny - 1;
-    int cx = cnx - 1, cy = cny - 1;
-    int ce;
-    if (elem_type == UG4GB_QUAD) {
-        int i = e % fx, j = e / fx;
-        ce = (i >> 1) + cx * (j >> 1);
-    } else if (elem_type == UG4GB_HEX) {
-        int i = e % fx, j = (e / fx) % fy, k = e / (fx * fy);
-        ce = (i >> 1) + cx * ((j >> 1) + cy * (k >> 1));
-    } else {
-        int h = e / 6;
-        int i = h % fx, j = (h / fx) % fy, k = h / (fx * fy);
-        double cc[3] = {0, 0, 0};
-        for (int a = 0; a < 4; ++a) {
-            int v = felems[4 * (size_t)e + a];
-            for (int d = 0; d < 3; ++d) cc[d] += fcoords[3 * (size_t)v + d];
-        }
-        int ci[3] = {i >> 1, j >> 1, k >> 1};
-        double off[3];
-        for (int d = 0; d < 3; ++d) off[d] = cc[d] * 0.25 * (double)(cnx - 1) - (double)ci[d];
-        int p;
-        if (off[0] >= off[1] && off[1] >= off[2]) p = 0;
-        else if (off[0] >= off[2] && off[2] >= off[1]) p = 1;
-        else if (off[1] >= off[0] && off[0] >= off[2]) p = 2;
-        else if (off[1] >= off[2] && off[2] >= off[0]) p = 3;
-        else if (off[2] >= off[0] && off[0] >= off[1]) p = 4;
-        else p = 5;
-        ce = 6 * (ci[0] + cx * (ci[1] + cy * ci[2])) + p;
-    }
-    (void)fnz;
-    atomicAdd(sumc + ce, logf[e]);
-    atomicAdd(cntc + ce, 1);
+    if (off[0] >= off[1] && off[1] >= off[2]) return 0;
+    if (off[0] >= off[2] && off[2] >= off[1]) return 1;
+    if (off[1] >= off[0] && off[0] >= off[2]) return 2;
+    if (off[1] >= off[2] && off[2] >= off[0]) return 3;
+    if (off[2] >= off[0] && off[0] >= off[1]) return 4;
+    return 5;
 }
 
-__global__ void k_finish_coarse_log(const double *sumc, const int *cntc, int ne, double *logc)
+__global__ void k_coarsen_log(int elem_type, const double *fcoords, const int *felems, int fnx, int fny, int cnx,
+                              int cny, int cne, const double *logf, double *logc)
 {
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < ne) logc[e] = sumc[e] / (double)(cntc[e] ? cntc[e] : 1);
+    int ce = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ce >= cne) return;
+    const int fx = fnx - 1, fy = fny - 1, cx = cnx - 1, cy = cny - 1;
+    double s = 0.0;
+    int n = 0;
+    if (elem_type == UG4GB_QUAD) {
+        int I = ce % cx, J = ce / cx;
+        for (int b = 0; b < 2; ++b)
+            for (int a = 0; a < 2; ++a) {
+                s += logf[(2 * I + a) + fx * (2 * J + b)];
+                ++n;
+            }
+    } else if (elem_type == UG4GB_HEX) {
+        int I = ce % cx, J = (ce / cx) % cy, K = ce / (cx * cy);
+        for (int c = 0; c < 2; ++c)
+            for (int b = 0; b < 2; ++b)
+                for (int a = 0; a < 2; ++a) {
+                    s += logf[(2 * I + a) + fx * ((2 * J + b) + fy * (2 * K + c))];
+                    ++n;
+                }
+    } else {
+        int hc = ce / 6, pc = ce % 6;
+        int I = hc % cx, J = (hc / cx) % cy, K = hc / (cx * cy);
+        for (int c = 0; c < 2; ++c)
+            for (int b = 0; b < 2; ++b)
+                for (int a = 0; a < 2; ++a) {
+                    int hf = (2 * I + a) + fx * ((2 * J + b) + fy * (2 * K + c));
+                    for (int p = 0; p < 6; ++p) {
+                        int e = 6 * hf + p;
+                        double cc[3] = {0, 0, 0};
+                        for (int q = 0; q < 4; ++q) {
+                            int v = felems[4 * (size_t)e + q];
+                            for (int d = 0; d < 3; ++d) cc[d] += fcoords[3 * (size_t)v + d];
+                        }
+                        double off[3];
+                        const int ci[3] = {I, J, K};
+                        for (int d = 0; d < 3; ++d) off[d] = cc[d] * 0.25 * (double)(cnx - 1) - (double)ci[d];
+                        if (kuhn_perm_of(off) == pc) {
+                            s += logf[e];
+                            ++n;
+                        }
+                    }
+                }
+    }
+    logc[ce] = s / (double)(n ? n : 1);
 }
 
 __global__ void k_exp(const double *m, int n, double *K)
@@ -190,15 +243,8 @@ __global__ void k_exp(const double *m, int n, double *K)
 
 void coarsen_log(Ctx &c, const Level &F, const Level &Cl, const double *logf, double *logc)
 {
-    DevBuf<double> sum;
-    DevBuf<int> cnt;
-    sum.alloc(Cl.ne);
-    cnt.alloc(Cl.ne);
-    UG_CUDA(cudaMemsetAsync(sum.p, 0, sum.bytes(), c.stream));
-    UG_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes(), c.stream));
-    UG_LAUNCH(c, k_coarsen_log, div_up(F.ne, 256), 256, 0, F.elem_type, F.coords.p, F.elems.p, F.ne, F.nx, F.ny, F.nz,
-              Cl.nx, Cl.ny, logf, sum.p, cnt.p);
-    UG_LAUNCH(c, k_finish_coarse_log, div_up(Cl.ne, 256), 256, 0, sum.p, cnt.p, Cl.ne, logc);
+    UG_LAUNCH(c, k_coarsen_log, div_up(Cl.ne, 128), 128, 0, F.elem_type, F.coords.p, F.elems.p, F.nx, F.ny, Cl.nx,
+              Cl.ny, Cl.ne, logf, logc);
 }
 
 void exp_elements(Ctx &c, const double *m, int n, double *K)
@@ -251,23 +297,27 @@ void launch_grad_logk(Ctx &c, const Level &L, const double *K, const double *u, 
 
 // sum of SCV volumes per vertex (d rhs_i / d f_i)
 template <int T>
-__global__ void k_scv_volumes(const double *coords, const int *elems, int ne, double *vol)
+__global__ void k_scv_volumes(AsmArgs a, int colour, double *vol)
 {
     using E = Elem<T>;
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= ne) return;
-    int ev[E::K];
-    double X[E::K][E::DIM];
+    int cell;
+    if (!colour_cell(a, blockIdx.x * blockDim.x + threadIdx.x, colour, &cell)) return;
+    const int per = (T == UG4GB_TET) ? 6 : 1;
+    for (int p = 0; p < per; ++p) {
+        const int e = per * cell + p;
+        int ev[E::K];
+        double X[E::K][E::DIM];
 #pragma unroll
-    for (int i = 0; i < E::K; ++i) {
-        ev[i] = elems[(size_t)e * E::K + i];
+        for (int i = 0; i < E::K; ++i) {
+            ev[i] = a.elems[(size_t)e * E::K + i];
 #pragma unroll
-        for (int d = 0; d < E::DIM; ++d) X[i][d] = coords[(size_t)ev[i] * E::DIM + d];
+            for (int d = 0; d < E::DIM; ++d) X[i][d] = a.coords[(size_t)ev[i] * E::DIM + d];
+        }
+        double v[E::K];
+        scv_volumes<T>(X, v);
+#pragma unroll
+        for (int i = 0; i < E::K; ++i) vol[ev[i]] += v[i];
     }
-    double v[E::K];
-    scv_volumes<T>(X, v);
-#pragma unroll
-    for (int i = 0; i < E::K; ++i) atomicAdd(vol + ev[i], v[i]);
 }
 
 __global__ void k_grad_source(const double *vol, const unsigned char *bnd, const double *lam, int nv, double *g)
@@ -281,10 +331,20 @@ void launch_grad_source(Ctx &c, const Level &L, const double *lam, double *g)
     DevBuf<double> vol;
     vol.alloc(L.nv);
     UG_CUDA(cudaMemsetAsync(vol.p, 0, vol.bytes(), c.stream));
-    unsigned gr = div_up(L.ne, 128);
-    if (L.elem_type == UG4GB_QUAD) UG_LAUNCH(c, k_scv_volumes<UG4GB_QUAD>, gr, 128, 0, L.coords.p, L.elems.p, L.ne, vol.p);
-    else if (L.elem_type == UG4GB_HEX) UG_LAUNCH(c, k_scv_volumes<UG4GB_HEX>, gr, 128, 0, L.coords.p, L.elems.p, L.ne, vol.p);
-    else UG_LAUNCH(c, k_scv_volumes<UG4GB_TET>, gr, 128, 0, L.coords.p, L.elems.p, L.ne, vol.p);
+    AsmArgs a{};
+    a.coords = L.coords.p;
+    a.elems = L.elems.p;
+    a.ne = L.ne;
+    a.cx = L.nx - 1;
+    a.cy = L.ny - 1;
+    a.cz = (L.dim == 3) ? L.nz - 1 : 1;
+    const int ncol = (L.dim == 3) ? 8 : 4;
+    unsigned gr = div_up(((a.cx + 1) / 2) * ((a.cy + 1) / 2) * ((a.cz + 1) / 2), 128);
+    for (int colour = 0; colour < ncol; ++colour) {
+        if (L.elem_type == UG4GB_QUAD) UG_LAUNCH(c, k_scv_volumes<UG4GB_QUAD>, gr, 128, 0, a, colour, vol.p);
+        else if (L.elem_type == UG4GB_HEX) UG_LAUNCH(c, k_scv_volumes<UG4GB_HEX>, gr, 128, 0, a, colour, vol.p);
+        else UG_LAUNCH(c, k_scv_volumes<UG4GB_TET>, gr, 128, 0, a, colour, vol.p);
+    }
     UG_LAUNCH(c, k_grad_source, div_up(L.nv, 256), 256, 0, vol.p, L.bnd.p, lam, L.nv, g);
     UG_CUDA(cudaStreamSynchronize(c.stream));
 }

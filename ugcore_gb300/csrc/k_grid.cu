@@ -8,6 +8,8 @@
 // lib_disc/common/local_algebra.h:767).  It is built here without a global
 // sort: vertex->element adjacency by counting, then one warp per row gathers
 // the corners of its elements and ranks the distinct ones in shared memory.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace ug4gb {
@@ -424,6 +426,132 @@ void sell_from_csr(Ctx &c, const Csr &A, Sell<T> &S, const double *col_scale)
 
 template void sell_from_csr<double>(Ctx &, const Csr &, Sell<double> &, const double *);
 template void sell_from_csr<float>(Ctx &, const Csr &, Sell<float> &, const double *);
+
+// ------------------------------------------------------- CRS -> diagonal --
+__global__ void k_offset_range(const int *rowptr, const int *col, int nrows, int *mn, int *mx)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    int lo = 0x7fffffff, hi = -0x7fffffff;
+    for (int a = rowptr[r]; a < rowptr[r + 1]; ++a) {
+        int o = col[a] - r;
+        lo = min(lo, o);
+        hi = max(hi, o);
+    }
+    if (rowptr[r + 1] > rowptr[r]) {
+        atomicMin(mn, lo);
+        atomicMax(mx, hi);
+    }
+}
+
+__global__ void k_offset_mark(const int *rowptr, const int *col, int nrows, int lo, int *mark)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    for (int a = rowptr[r]; a < rowptr[r + 1]; ++a) mark[col[a] - r - lo] = 1;
+}
+
+bool csr_offsets(Ctx &c, const Csr &A, int max_s, std::vector<int> &offs)
+{
+    offs.clear();
+    if (A.nrows == 0 || A.nnz == 0) return false;
+    DevBuf<int> mm;
+    mm.alloc(2);
+    int init[2] = {0x7fffffff, -0x7fffffff};
+    UG_CUDA(cudaMemcpyAsync(mm.p, init, sizeof(init), cudaMemcpyHostToDevice, c.stream));
+    UG_LAUNCH(c, k_offset_range, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.nrows, mm.p, mm.p + 1);
+    int h[2];
+    UG_CUDA(cudaMemcpyAsync(h, mm.p, sizeof(h), cudaMemcpyDeviceToHost, c.stream));
+    UG_CUDA(cudaStreamSynchronize(c.stream));
+    int64_t span = (int64_t)h[1] - h[0] + 1;
+    if (span <= 0 || span > (int64_t)64 << 20) return false;
+    DevBuf<int> mark;
+    mark.alloc(span);
+    UG_CUDA(cudaMemsetAsync(mark.p, 0, mark.bytes(), c.stream));
+    UG_LAUNCH(c, k_offset_mark, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.nrows, h[0], mark.p);
+    std::vector<int> hm(span);
+    UG_CUDA(cudaMemcpyAsync(hm.data(), mark.p, mark.bytes(), cudaMemcpyDeviceToHost, c.stream));
+    UG_CUDA(cudaStreamSynchronize(c.stream));
+    for (int64_t i = 0; i < span; ++i)
+        if (hm[i]) {
+            offs.push_back((int)(i + h[0]));
+            if ((int)offs.size() > max_s) return false;
+        }
+    return true;
+}
+
+template <class T>
+__global__ void k_dia_fill(const int *rowptr, const int *col, const double *val, int nrows, Offs off, int S,
+                           const double *col_scale, T *dval)
+{
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nrows) return;
+    for (int k = 0; k < S; ++k) dval[(size_t)k * nrows + r] = (T)0;
+    for (int a = rowptr[r]; a < rowptr[r + 1]; ++a) {
+        int o = col[a] - r;
+        int k = 0;
+        while (k < S && off.o[k] != o) ++k;
+        if (k == S) continue;   // cannot happen: offs holds every offset of A
+        double v = val[a];
+        if (col_scale) v *= col_scale[col[a]];
+        dval[(size_t)k * nrows + r] = (T)v;
+    }
+}
+
+template <class T>
+void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs, const double *col_scale)
+{
+    UG_REQUIRE((int)offs.size() <= kMaxDiag, UG4GB_ERR_INVALID, "dia_from_csr: too many offsets");
+    D.nrows = A.nrows;
+    D.ncols = A.ncols;
+    D.S = (int)offs.size();
+    for (int k = 0; k < kMaxDiag; ++k) D.off.o[k] = k < D.S ? offs[k] : 0;
+    D.val.alloc((size_t)D.S * D.nrows);
+    UG_LAUNCH(c, k_dia_fill<T>, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows, D.off, D.S,
+              col_scale, D.val.p);
+}
+
+// the diagonal kernels are instantiated for S = 9, 15, 27 (2D quads, Kuhn
+// tets, hexahedra); a smaller offset set is padded with offset 0 (value 0)
+static int dia_width(int s)
+{
+    if (s <= 9) return 9;
+    if (s <= 15) return 15;
+    if (s <= 27) return 27;
+    return 0;
+}
+
+template <class T>
+void op_from_csr(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_scale, bool allow_dia)
+{
+    M.nrows = A.nrows;
+    M.ncols = A.ncols;
+    std::vector<int> offs;
+    if (allow_dia && A.nrows == A.ncols && csr_offsets(c, A, 27, offs)) {
+        int w = dia_width((int)offs.size());
+        // pad with offsets that do not occur (value 0), keeping the set sorted
+        int cand = 1;
+        while ((int)offs.size() < w) {
+            bool have = false;
+            for (int o : offs) have = have || (o == cand);
+            if (!have) offs.push_back(cand);
+            cand = (cand > 0) ? -cand : -cand + 1;
+        }
+        std::sort(offs.begin(), offs.end());
+        M.kind = 1;
+        dia_from_csr<T>(c, A, M.dia, offs, col_scale);
+        M.sell = Sell<T>();
+    } else {
+        M.kind = 0;
+        sell_from_csr<T>(c, A, M.sell, col_scale);
+        M.dia = Dia<T>();
+    }
+}
+
+template void dia_from_csr<double>(Ctx &, const Csr &, Dia<double> &, const std::vector<int> &, const double *);
+template void dia_from_csr<float>(Ctx &, const Csr &, Dia<float> &, const std::vector<int> &, const double *);
+template void op_from_csr<double>(Ctx &, const Csr &, OpMat<double> &, const double *, bool);
+template void op_from_csr<float>(Ctx &, const Csr &, OpMat<float> &, const double *, bool);
 
 __global__ void k_fill(double *p, size_t n, double v)
 {

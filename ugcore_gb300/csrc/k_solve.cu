@@ -1,9 +1,14 @@
-// k_solve.cu -- SELL-32 SpMV-based multigrid and Krylov kernels.
+// k_solve.cu -- SpMV-based multigrid and Krylov kernels (SELL-32 or diagonal).
 //
-// Every kernel is HBM-bound: one thread per row, 32 rows per slice, matrix
-// values/columns streamed with evict-first loads (coalesced 32-wide), the
-// gathered vector kept in L1/L2.  Row-local vector work is fused into the
-// SpMV epilogue so each sweep reads the matrix once:
+// Every kernel is HBM-bound: one thread per row, matrix values streamed with
+// evict-first loads (coalesced 32-wide), the gathered vector kept in L1/L2.
+// Two operator layouts share the kernels through a "matrix view":
+//   SELL-32   general sparsity: 32-row slices, column-major in the slice;
+//   diagonal  <= 27 constant offsets (structured levels): values only, the
+//             column of entry k is row + off[k]; no column stream and no
+//             load that depends on another load.
+// Row-local vector work is fused into the SpMV epilogue so each sweep reads
+// the operator once:
 //   Jacobi step     t = dinv*d ; d -= A t ; sc += t
 //                   (Jacobi::step, lib_algebra/operator/preconditioner/
 //                    jacobi.h:222; AssembledMultiGridCycle::
@@ -30,19 +35,62 @@ int row_grid(const Ctx &c, int nrows)
     return need < cap ? need : cap;
 }
 
-template <class V, class XT, class ACC>
-__device__ __forceinline__ ACC sell_row(const SellView<V> &A, const XT *__restrict__ x, int row)
-{
-    const int s = row >> 5, lane = row & 31;
-    const int base = __ldg(A.sptr + s) + lane;
-    const int w = __ldg(A.swidth + s);
-    ACC acc = (ACC)0;
+// ------------------------------------------------------------ views ------
+template <class V>
+struct SellMV {
+    SellView<V> s;
+    __device__ __forceinline__ int rows() const { return s.nrows; }
+    template <class ACC, class XT>
+    __device__ __forceinline__ ACC dot(const XT *__restrict__ x, int row) const
+    {
+        const int sl = row >> 5, lane = row & 31;
+        const int base = __ldg(s.sptr + sl) + lane;
+        const int w = __ldg(s.swidth + sl);
+        ACC acc = (ACC)0;
 #pragma unroll 4
-    for (int k = 0; k < w; ++k) {
-        const int idx = base + k * kSliceH;
-        acc += (ACC)ld_stream(A.val + idx) * (ACC)x[ld_stream(A.col + idx)];
+        for (int k = 0; k < w; ++k) {
+            const int idx = base + k * kSliceH;
+            acc += (ACC)ld_stream(s.val + idx) * (ACC)x[ld_stream(s.col + idx)];
+        }
+        return acc;
     }
-    return acc;
+};
+
+template <class V, int S>
+struct DiaMV {
+    int n, ncols;
+    const V *__restrict__ val;
+    Offs off;
+    __device__ __forceinline__ int rows() const { return n; }
+    template <class ACC, class XT>
+    __device__ __forceinline__ ACC dot(const XT *__restrict__ x, int i) const
+    {
+        ACC acc = (ACC)0;
+#pragma unroll
+        for (int k = 0; k < S; ++k) {
+            int j = i + off.o[k];
+            j = j < 0 ? 0 : (j >= ncols ? ncols - 1 : j);
+            acc += (ACC)ld_stream(val + (size_t)k * n + i) * (ACC)x[j];
+        }
+        return acc;
+    }
+};
+
+// calls f(view) with the view type matching the operator's layout
+template <class V, class F>
+void with_mv(const OpMat<V> &m, F &&f)
+{
+    if (m.kind == 0) {
+        f(SellMV<V>{view(m.sell)});
+        return;
+    }
+    const Dia<V> &d = m.dia;
+    switch (d.S) {
+    case 9: f(DiaMV<V, 9>{d.nrows, d.ncols, d.val.p, d.off}); break;
+    case 15: f(DiaMV<V, 15>{d.nrows, d.ncols, d.val.p, d.off}); break;
+    case 27: f(DiaMV<V, 27>{d.nrows, d.ncols, d.val.p, d.off}); break;
+    default: throw Error{UG4GB_ERR_INVALID, "diagonal operator with unsupported width"};
+    }
 }
 
 __device__ __forceinline__ bool conv_valid(double v)
@@ -69,17 +117,17 @@ __device__ __forceinline__ void conv_update(KScal *ks, double d, int done_value)
 }
 
 // ------------------------------------------------------- smoothing step --
-template <class V, class XT, class DT, bool RHO>
-__global__ void __launch_bounds__(NT) k_smooth(SellView<V> A, const XT *__restrict__ x, const DT *__restrict__ dbase,
+template <class MV, class V, class XT, class DT, bool RHO>
+__global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, const DT *__restrict__ dbase,
                                                const V *__restrict__ dinv, V *__restrict__ sc, V *__restrict__ dout,
                                                int sc_mode, const int *skip, const double *__restrict__ r_rho,
                                                RedArgs red, int rho_kind)
 {
     if (skip && *skip) return;
     double rsum = 0.0;
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
-        V acc = sell_row<V, XT, V>(A, x, row);
+    const int stride = gridDim.x * NT, n = A.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
+        V acc = A.template dot<V>(x, row);
         V db = (V)dbase[row];
         V dn = db - acc;
         if (dout) dout[row] = dn;
@@ -104,61 +152,66 @@ __global__ void __launch_bounds__(NT) k_smooth(SellView<V> A, const XT *__restri
 }
 
 template <class V, class XT, class DT>
-void smooth_step(Ctx &c, const Sell<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout, int sc_mode,
+void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout, int sc_mode,
                  const int *skip, const double *r_rho, RedArgs *red, int rho_kind)
 {
-    int g = row_grid(c, At.nrows);
-    if (r_rho) {
-        UG_LAUNCH(c, (k_smooth<V, XT, DT, true>), g, NT, 0, view(At), x, dbase, dinv, sc, dout, sc_mode, skip, r_rho,
-                  *red, rho_kind);
-    } else {
-        RedArgs none{nullptr, nullptr, nullptr};
-        UG_LAUNCH(c, (k_smooth<V, XT, DT, false>), g, NT, 0, view(At), x, dbase, dinv, sc, dout, sc_mode, skip,
-                  (const double *)nullptr, none, 0);
-    }
+    const int g = row_grid(c, At.nrows);
+    with_mv(At, [&](auto mv) {
+        using MV = decltype(mv);
+        if (r_rho) {
+            UG_LAUNCH(c, (k_smooth<MV, V, XT, DT, true>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
+                      r_rho, *red, rho_kind);
+        } else {
+            RedArgs none{nullptr, nullptr, nullptr};
+            UG_LAUNCH(c, (k_smooth<MV, V, XT, DT, false>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
+                      (const double *)nullptr, none, 0);
+        }
+    });
 }
 
 #define INST_SMOOTH(V, XT, DT)                                                                              \
-    template void smooth_step<V, XT, DT>(Ctx &, const Sell<V> &, const XT *, const DT *, const V *, V *, V *, int, \
+    template void smooth_step<V, XT, DT>(Ctx &, const OpMat<V> &, const XT *, const DT *, const V *, V *, V *, int, \
                                          const int *, const double *, RedArgs *, int);
 INST_SMOOTH(double, double, double)
 INST_SMOOTH(float, float, float)
 INST_SMOOTH(float, double, double)
-INST_SMOOTH(float, float, double)
 
 // --------------------------------------------------------- transfers -----
-template <class V>
-__global__ void __launch_bounds__(NT) k_restrict(SellView<V> R, const V *__restrict__ d, V *__restrict__ dc,
-                                                 const int *skip)
+template <class MV, class V>
+__global__ void __launch_bounds__(NT) k_restrict(MV R, const V *__restrict__ d, V *__restrict__ dc, const int *skip)
 {
     if (skip && *skip) return;
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < R.nrows; row += stride) dc[row] = sell_row<V, V, V>(R, d, row);
+    const int stride = gridDim.x * NT, n = R.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) dc[row] = R.template dot<V>(d, row);
 }
 
 template <class V>
-void restrict_apply(Ctx &c, const Sell<V> &R, const V *d, V *dc, const int *skip)
+void restrict_apply(Ctx &c, const OpMat<V> &R, const V *d, V *dc, const int *skip)
 {
-    UG_LAUNCH(c, k_restrict<V>, row_grid(c, R.nrows), NT, 0, view(R), d, dc, skip);
+    with_mv(R, [&](auto mv) {
+        UG_LAUNCH(c, (k_restrict<decltype(mv), V>), row_grid(c, R.nrows), NT, 0, mv, d, dc, skip);
+    });
 }
 
-template <class V>
-__global__ void __launch_bounds__(NT) k_prolong(SellView<V> P, const V *__restrict__ scc, V *__restrict__ sc,
+template <class MV, class V>
+__global__ void __launch_bounds__(NT) k_prolong(MV P, const V *__restrict__ scc, V *__restrict__ sc,
                                                 const V *__restrict__ dfac, V *__restrict__ w, const int *skip)
 {
     if (skip && *skip) return;
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < P.nrows; row += stride) {
-        V t = sell_row<V, V, V>(P, scc, row);
+    const int stride = gridDim.x * NT, n = P.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
+        V t = P.template dot<V>(scc, row);
         sc[row] += t;
         if (w) w[row] = t * dfac[row];
     }
 }
 
 template <class V>
-void prolong_apply(Ctx &c, const Sell<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip)
+void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip)
 {
-    UG_LAUNCH(c, k_prolong<V>, row_grid(c, P.nrows), NT, 0, view(P), scc, sc, dfac, w, skip);
+    with_mv(P, [&](auto mv) {
+        UG_LAUNCH(c, (k_prolong<decltype(mv), V>), row_grid(c, P.nrows), NT, 0, mv, scc, sc, dfac, w, skip);
+    });
 }
 
 // dense base solve with the LU-factored inverse (one block, FP64)
@@ -185,8 +238,8 @@ void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int 
 
 // multicolour Gauss-Seidel: rows of one colour, t_i = relax (d_i - (A t)_i) / a_ii
 // (t_i is still 0 when its colour is processed)
-template <class V>
-__global__ void __launch_bounds__(NT) k_mcgs(SellView<V> A, const int *__restrict__ rows, int nrows_c,
+template <class MV, class V>
+__global__ void __launch_bounds__(NT) k_mcgs(MV A, const int *__restrict__ rows, int nrows_c,
                                              const V *__restrict__ dr, const V *__restrict__ d, V *__restrict__ t,
                                              const int *skip)
 {
@@ -194,67 +247,74 @@ __global__ void __launch_bounds__(NT) k_mcgs(SellView<V> A, const int *__restric
     const int stride = gridDim.x * NT;
     for (int q = blockIdx.x * NT + threadIdx.x; q < nrows_c; q += stride) {
         int row = rows[q];
-        V acc = sell_row<V, V, V>(A, t, row);
+        V acc = A.template dot<V>(t, row);
         t[row] = dr[row] * (d[row] - acc);
     }
 }
 
 template <class V>
-void mcgs_colour(Ctx &c, const Sell<V> &A, const int *rows, int nrows_c, const V *dinv_relax, const V *d, V *t,
+void mcgs_colour(Ctx &c, const OpMat<V> &A, const int *rows, int nrows_c, const V *dinv_relax, const V *d, V *t,
                  const int *skip)
 {
-    UG_LAUNCH(c, k_mcgs<V>, row_grid(c, nrows_c), NT, 0, view(A), rows, nrows_c, dinv_relax, d, t, skip);
+    with_mv(A, [&](auto mv) {
+        UG_LAUNCH(c, (k_mcgs<decltype(mv), V>), row_grid(c, nrows_c), NT, 0, mv, rows, nrows_c, dinv_relax, d, t,
+                  skip);
+    });
 }
 
-// d_out = d_base - A t ; sc (= | +=) t
-template <class V, class DT>
-__global__ void __launch_bounds__(NT) k_resupd(SellView<V> A, const V *__restrict__ t, const DT *__restrict__ dbase,
-                                               V *__restrict__ dout, V *__restrict__ sc, int first, const int *skip)
+template <class MV, class V, class DT>
+__global__ void __launch_bounds__(NT) k_resupd(MV A, const V *__restrict__ t, const DT *__restrict__ dbase,
+                                               V *__restrict__ dout, V *__restrict__ sc, int sc_mode, const int *skip)
 {
     if (skip && *skip) return;
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
-        V acc = sell_row<V, V, V>(A, t, row);
+    const int stride = gridDim.x * NT, n = A.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
+        V acc = A.template dot<V>(t, row);
         dout[row] = (V)dbase[row] - acc;
-        if (first == 1) sc[row] = t[row];
-        else if (first == 0) sc[row] += t[row];
+        if (sc_mode == 1) sc[row] = t[row];
+        else if (sc_mode == 0) sc[row] += t[row];
     }
 }
 
 template <class V, class DT>
-void residual_update(Ctx &c, const Sell<V> &A, const V *t, const DT *dbase, V *dout, V *sc, int first, const int *skip)
+void residual_update(Ctx &c, const OpMat<V> &A, const V *t, const DT *dbase, V *dout, V *sc, int sc_mode,
+                     const int *skip)
 {
-    UG_LAUNCH(c, (k_resupd<V, DT>), row_grid(c, A.nrows), NT, 0, view(A), t, dbase, dout, sc, first, skip);
+    with_mv(A, [&](auto mv) {
+        UG_LAUNCH(c, (k_resupd<decltype(mv), V, DT>), row_grid(c, A.nrows), NT, 0, mv, t, dbase, dout, sc, sc_mode,
+                  skip);
+    });
 }
 
-template void restrict_apply<double>(Ctx &, const Sell<double> &, const double *, double *, const int *);
-template void restrict_apply<float>(Ctx &, const Sell<float> &, const float *, float *, const int *);
-template void prolong_apply<double>(Ctx &, const Sell<double> &, const double *, double *, const double *, double *,
+template void restrict_apply<double>(Ctx &, const OpMat<double> &, const double *, double *, const int *);
+template void restrict_apply<float>(Ctx &, const OpMat<float> &, const float *, float *, const int *);
+template void prolong_apply<double>(Ctx &, const OpMat<double> &, const double *, double *, const double *, double *,
                                     const int *);
-template void prolong_apply<float>(Ctx &, const Sell<float> &, const float *, float *, const float *, float *,
+template void prolong_apply<float>(Ctx &, const OpMat<float> &, const float *, float *, const float *, float *,
                                    const int *);
 template void base_solve<double>(Ctx &, const double *, int, const double *, double *, const int *);
 template void base_solve<float>(Ctx &, const double *, int, const float *, float *, const int *);
-template void mcgs_colour<double>(Ctx &, const Sell<double> &, const int *, int, const double *, const double *,
+template void mcgs_colour<double>(Ctx &, const OpMat<double> &, const int *, int, const double *, const double *,
                                   double *, const int *);
-template void mcgs_colour<float>(Ctx &, const Sell<float> &, const int *, int, const float *, const float *, float *,
+template void mcgs_colour<float>(Ctx &, const OpMat<float> &, const int *, int, const float *, const float *, float *,
                                  const int *);
-template void residual_update<double, double>(Ctx &, const Sell<double> &, const double *, const double *, double *,
+template void residual_update<double, double>(Ctx &, const OpMat<double> &, const double *, const double *, double *,
                                               double *, int, const int *);
-template void residual_update<float, float>(Ctx &, const Sell<float> &, const float *, const float *, float *,
+template void residual_update<float, float>(Ctx &, const OpMat<float> &, const float *, const float *, float *,
                                             float *, int, const int *);
-template void residual_update<float, double>(Ctx &, const Sell<float> &, const float *, const double *, float *,
+template void residual_update<float, double>(Ctx &, const OpMat<float> &, const float *, const double *, float *,
                                              float *, int, const int *);
 
 // ------------------------------------------------------------ Krylov -----
 // r = b - A x (r holds b on entry); start the convergence check with |r|
-__global__ void __launch_bounds__(NT) k_krylov_start(SellView<double> A, const double *__restrict__ x,
-                                                     double *__restrict__ r, RedArgs red)
+template <class MV>
+__global__ void __launch_bounds__(NT) k_krylov_start(MV A, const double *__restrict__ x, double *__restrict__ r,
+                                                     RedArgs red)
 {
     double sum = 0.0;
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
-        double ax = sell_row<double, double, double>(A, x, row);
+    const int stride = gridDim.x * NT, n = A.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
+        double ax = A.template dot<double>(x, row);
         double rv = r[row] - ax;
         r[row] = rv;
         sum += rv * rv;
@@ -274,24 +334,25 @@ __global__ void __launch_bounds__(NT) k_krylov_start(SellView<double> A, const d
     });
 }
 
-void krylov_start(Ctx &c, const Sell<double> &A, const double *x, double *r, RedArgs red)
+void krylov_start(Ctx &c, const OpMat<double> &A, const double *x, double *r, RedArgs red)
 {
-    UG_LAUNCH(c, k_krylov_start, row_grid(c, A.nrows), NT, 0, view(A), x, r, red);
+    with_mv(A, [&](auto mv) {
+        UG_LAUNCH(c, k_krylov_start<decltype(mv)>, row_grid(c, A.nrows), NT, 0, mv, x, r, red);
+    });
 }
 
 // first: p = z, q = A z ; else p = z + beta p, q = A z + beta q ; lambda = (q,p)
-template <class ZT>
-__global__ void __launch_bounds__(NT) k_cg_spmv_dot(SellView<double> A, const ZT *__restrict__ z,
-                                                    double *__restrict__ p, double *__restrict__ q, int first,
-                                                    RedArgs red)
+template <class MV, class ZT>
+__global__ void __launch_bounds__(NT) k_cg_spmv_dot(MV A, const ZT *__restrict__ z, double *__restrict__ p,
+                                                    double *__restrict__ q, int first, RedArgs red)
 {
     KScal *ks = red.ks;
     if (ks->done) return;
     const double beta = first ? 0.0 : ks->beta;
     double sum = 0.0;
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
-        double az = sell_row<double, ZT, double>(A, z, row);
+    const int stride = gridDim.x * NT, n = A.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
+        double az = A.template dot<double>(z, row);
         double pn = first ? (double)z[row] : (double)z[row] + beta * p[row];
         double qn = first ? az : az + beta * q[row];
         p[row] = pn;
@@ -310,12 +371,14 @@ __global__ void __launch_bounds__(NT) k_cg_spmv_dot(SellView<double> A, const ZT
 }
 
 template <class ZT>
-void cg_spmv_dot_t(Ctx &c, const Sell<double> &A, const ZT *z, double *p, double *q, int first, RedArgs red)
+void cg_spmv_dot_t(Ctx &c, const OpMat<double> &A, const ZT *z, double *p, double *q, int first, RedArgs red)
 {
-    UG_LAUNCH(c, k_cg_spmv_dot<ZT>, row_grid(c, A.nrows), NT, 0, view(A), z, p, q, first, red);
+    with_mv(A, [&](auto mv) {
+        UG_LAUNCH(c, (k_cg_spmv_dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, z, p, q, first, red);
+    });
 }
-template void cg_spmv_dot_t<double>(Ctx &, const Sell<double> &, const double *, double *, double *, int, RedArgs);
-template void cg_spmv_dot_t<float>(Ctx &, const Sell<double> &, const float *, double *, double *, int, RedArgs);
+template void cg_spmv_dot_t<double>(Ctx &, const OpMat<double> &, const double *, double *, double *, int, RedArgs);
+template void cg_spmv_dot_t<float>(Ctx &, const OpMat<double> &, const float *, double *, double *, int, RedArgs);
 
 // x += alpha p ; r -= alpha q ; |r| -> convergence check
 __global__ void __launch_bounds__(NT) k_cg_update(int n, double *__restrict__ x, double *__restrict__ r,
@@ -455,16 +518,16 @@ void bicg_p(Ctx &c, int n, const double *r, double *p, const double *v, RedArgs 
     UG_LAUNCH(c, k_bicg_p, div_up(n, NT), NT, 0, n, r, p, v, red.ks);
 }
 
-template <class ZT>
-__global__ void __launch_bounds__(NT) k_bicg_spmv_dot(SellView<double> A, const ZT *__restrict__ q,
-                                                      double *__restrict__ v, const double *__restrict__ r0, RedArgs red)
+template <class MV, class ZT>
+__global__ void __launch_bounds__(NT) k_bicg_spmv_dot(MV A, const ZT *__restrict__ q, double *__restrict__ v,
+                                                      const double *__restrict__ r0, RedArgs red)
 {
     KScal *ks = red.ks;
     if (ks->done) return;
     double sum = 0.0;
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
-        double av = sell_row<double, ZT, double>(A, q, row);
+    const int stride = gridDim.x * NT, n = A.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
+        double av = A.template dot<double>(q, row);
         v[row] = av;
         sum += av * r0[row];
     }
@@ -479,12 +542,14 @@ __global__ void __launch_bounds__(NT) k_bicg_spmv_dot(SellView<double> A, const 
 }
 
 template <class ZT>
-void bicg_spmv_dot_t(Ctx &c, const Sell<double> &A, const ZT *q, double *v, const double *r0, RedArgs red)
+void bicg_spmv_dot_t(Ctx &c, const OpMat<double> &A, const ZT *q, double *v, const double *r0, RedArgs red)
 {
-    UG_LAUNCH(c, k_bicg_spmv_dot<ZT>, row_grid(c, A.nrows), NT, 0, view(A), q, v, r0, red);
+    with_mv(A, [&](auto mv) {
+        UG_LAUNCH(c, (k_bicg_spmv_dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, q, v, r0, red);
+    });
 }
-template void bicg_spmv_dot_t<double>(Ctx &, const Sell<double> &, const double *, double *, const double *, RedArgs);
-template void bicg_spmv_dot_t<float>(Ctx &, const Sell<double> &, const float *, double *, const double *, RedArgs);
+template void bicg_spmv_dot_t<double>(Ctx &, const OpMat<double> &, const double *, double *, const double *, RedArgs);
+template void bicg_spmv_dot_t<float>(Ctx &, const OpMat<double> &, const float *, double *, const double *, RedArgs);
 
 template <class ZT>
 __global__ void __launch_bounds__(NT) k_bicg_x_s(int n, double *__restrict__ x, const ZT *__restrict__ q,
@@ -526,17 +591,16 @@ void bicg_s_to_r(Ctx &c, int n, const double *s, double *r, RedArgs red)
     UG_LAUNCH(c, k_bicg_s_to_r, div_up(n, NT), NT, 0, n, s, r, red.ks);
 }
 
-template <class ZT>
-__global__ void __launch_bounds__(NT) k_bicg_spmv_2dot(SellView<double> A, const ZT *__restrict__ q,
-                                                       double *__restrict__ t, const double *__restrict__ s,
-                                                       RedArgs red)
+template <class MV, class ZT>
+__global__ void __launch_bounds__(NT) k_bicg_spmv_2dot(MV A, const ZT *__restrict__ q, double *__restrict__ t,
+                                                       const double *__restrict__ s, RedArgs red)
 {
     KScal *ks = red.ks;
     if (ks->done) return;
     double tt = 0.0, st = 0.0;
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
-        double av = sell_row<double, ZT, double>(A, q, row);
+    const int stride = gridDim.x * NT, n = A.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
+        double av = A.template dot<double>(q, row);
         t[row] = av;
         tt += av * av;
         st += s[row] * av;
@@ -552,12 +616,15 @@ __global__ void __launch_bounds__(NT) k_bicg_spmv_2dot(SellView<double> A, const
 }
 
 template <class ZT>
-void bicg_spmv_2dot_t(Ctx &c, const Sell<double> &A, const ZT *q, double *t, const double *s, RedArgs red)
+void bicg_spmv_2dot_t(Ctx &c, const OpMat<double> &A, const ZT *q, double *t, const double *s, RedArgs red)
 {
-    UG_LAUNCH(c, k_bicg_spmv_2dot<ZT>, row_grid(c, A.nrows), NT, 0, view(A), q, t, s, red);
+    with_mv(A, [&](auto mv) {
+        UG_LAUNCH(c, (k_bicg_spmv_2dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, q, t, s, red);
+    });
 }
-template void bicg_spmv_2dot_t<double>(Ctx &, const Sell<double> &, const double *, double *, const double *, RedArgs);
-template void bicg_spmv_2dot_t<float>(Ctx &, const Sell<double> &, const float *, double *, const double *, RedArgs);
+template void bicg_spmv_2dot_t<double>(Ctx &, const OpMat<double> &, const double *, double *, const double *,
+                                       RedArgs);
+template void bicg_spmv_2dot_t<float>(Ctx &, const OpMat<double> &, const float *, double *, const double *, RedArgs);
 
 template <class ZT>
 __global__ void __launch_bounds__(NT) k_bicg_x_r(int n, double *__restrict__ x, const ZT *__restrict__ q,
@@ -622,20 +689,23 @@ void vec_scale_add(Ctx &c, int n, double *dest, double alpha, const double *a, d
 }
 
 // dest = alpha*v1 + beta*A*w1 (SparseMatrix::axpy, sparsematrix_impl.h:294-342)
-__global__ void __launch_bounds__(NT) k_sell_axpy(SellView<double> A, double *dest, double alpha, const double *v1,
-                                                  double beta, const double *__restrict__ w1)
+template <class MV>
+__global__ void __launch_bounds__(NT) k_op_axpy(MV A, double *dest, double alpha, const double *v1, double beta,
+                                                const double *__restrict__ w1)
 {
-    const int stride = gridDim.x * NT;
-    for (int row = blockIdx.x * NT + threadIdx.x; row < A.nrows; row += stride) {
-        double aw = sell_row<double, double, double>(A, w1, row);
+    const int stride = gridDim.x * NT, n = A.rows();
+    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
+        double aw = A.template dot<double>(w1, row);
         dest[row] = (alpha == 0.0 ? 0.0 : alpha * v1[row]) + beta * aw;
     }
 }
 
-void sell_axpy(Ctx &c, const Sell<double> &A, double *dest, double alpha, const double *v1, double beta,
-               const double *w1)
+void op_axpy(Ctx &c, const OpMat<double> &A, double *dest, double alpha, const double *v1, double beta,
+             const double *w1)
 {
-    UG_LAUNCH(c, k_sell_axpy, row_grid(c, A.nrows), NT, 0, view(A), dest, alpha, v1, beta, w1);
+    with_mv(A, [&](auto mv) {
+        UG_LAUNCH(c, k_op_axpy<decltype(mv)>, row_grid(c, A.nrows), NT, 0, mv, dest, alpha, v1, beta, w1);
+    });
 }
 
 // dest += beta * A^T w1 (atomics; API path only)

@@ -1,5 +1,7 @@
 // k_solve.cuh -- device-side state of the Krylov solvers and the launch
 // wrappers of the multigrid / Krylov kernels (implemented in k_solve.cu).
+// Every operator argument is an OpMat (SELL-32 or diagonal layout); the
+// wrappers dispatch to the kernel instantiated for that layout.
 #pragma once
 
 #include "common.cuh"
@@ -36,26 +38,27 @@ int row_grid(const Ctx &c, int nrows);
 // dnew = dbase - At*x ; sc (=|+=) dinv*(dbase|dnew) ; optional dout = dnew;
 // optional rho = sum sc_i * r_i (final top-level step inside a Krylov solve)
 template <class V, class XT, class DT>
-void smooth_step(Ctx &c, const Sell<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout,
+void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout,
                  int sc_mode, const int *skip, const double *r_rho, RedArgs *red, int rho_kind);
 template <class V>
-void restrict_apply(Ctx &c, const Sell<V> &R, const V *d, V *dc, const int *skip);
+void restrict_apply(Ctx &c, const OpMat<V> &R, const V *d, V *dc, const int *skip);
 template <class V>
-void prolong_apply(Ctx &c, const Sell<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip);
+void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip);
 template <class V>
 void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip);
 template <class V>
-void mcgs_colour(Ctx &c, const Sell<V> &A, const int *rows, int nrows_c, const V *dinv_relax, const V *d, V *t,
+void mcgs_colour(Ctx &c, const OpMat<V> &A, const int *rows, int nrows_c, const V *dinv_relax, const V *d, V *t,
                  const int *skip);
+// d_out = d_base - A t ; sc_mode 1: sc = t, 0: sc += t, 2: sc untouched
 template <class V, class DT>
-void residual_update(Ctx &c, const Sell<V> &A, const V *t, const DT *dbase, V *dout, V *sc, int first,
+void residual_update(Ctx &c, const OpMat<V> &A, const V *t, const DT *dbase, V *dout, V *sc, int sc_mode,
                      const int *skip);
 
 // ---- Krylov kernels (FP64 outer vectors; z may be FP32 in mixed mode) ----
-void krylov_start(Ctx &c, const Sell<double> &A, const double *x, double *r, RedArgs red);
+void krylov_start(Ctx &c, const OpMat<double> &A, const double *x, double *r, RedArgs red);
 // first: p = z, q = A z; else p = z + beta p, q = A z + beta q; lambda = (q,p), alpha = rho_old/lambda
 template <class ZT>
-void cg_spmv_dot_t(Ctx &c, const Sell<double> &A, const ZT *z, double *p, double *q, int first, RedArgs red);
+void cg_spmv_dot_t(Ctx &c, const OpMat<double> &A, const ZT *z, double *p, double *q, int first, RedArgs red);
 void cg_update(Ctx &c, int n, double *x, double *r, const double *p, const double *q, RedArgs red);
 // rho = (z, r); kind 0: rho_old = rho (first), 1: beta = rho/rho_old, rho_old = rho
 template <class ZT>
@@ -67,20 +70,20 @@ void bicg_restart(Ctx &c, int n, const double *r, double *r0, double *p, double 
 void bicg_rho(Ctx &c, int n, const double *r0, const double *r, RedArgs red);
 void bicg_p(Ctx &c, int n, const double *r, double *p, const double *v, RedArgs red);
 template <class ZT>
-void bicg_spmv_dot_t(Ctx &c, const Sell<double> &A, const ZT *q, double *v, const double *r0, RedArgs red);
+void bicg_spmv_dot_t(Ctx &c, const OpMat<double> &A, const ZT *q, double *v, const double *r0, RedArgs red);
 template <class ZT>
 void bicg_x_s(Ctx &c, int n, double *x, const ZT *q, const double *r, const double *v, double *s, RedArgs red);
 void bicg_s_to_r(Ctx &c, int n, const double *s, double *r, RedArgs red);
 template <class ZT>
-void bicg_spmv_2dot_t(Ctx &c, const Sell<double> &A, const ZT *q, double *t, const double *s, RedArgs red);
+void bicg_spmv_2dot_t(Ctx &c, const OpMat<double> &A, const ZT *q, double *t, const double *s, RedArgs red);
 template <class ZT>
 void bicg_x_r(Ctx &c, int n, double *x, const ZT *q, const double *s, const double *t, double *r, RedArgs red);
 
 // ---- BLAS-1 / SpMV for the public vector and matrix API ----
 void vec_dot(Ctx &c, int n, const double *a, const double *b, RedArgs red);
 void vec_scale_add(Ctx &c, int n, double *dest, double alpha, const double *a, double beta, const double *b);
-void sell_axpy(Ctx &c, const Sell<double> &A, double *dest, double alpha, const double *v1, double beta,
-               const double *w1);
+void op_axpy(Ctx &c, const OpMat<double> &A, double *dest, double alpha, const double *v1, double beta,
+             const double *w1);
 void csr_axpy_transposed(Ctx &c, const Csr &A, double *dest, double beta, const double *w1);
 template <class TO, class TI>
 void convert(Ctx &c, int n, const TI *in, TO *out);
