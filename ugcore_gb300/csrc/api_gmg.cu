@@ -159,6 +159,7 @@ struct GmgT : GmgBase {
     std::vector<GLevel<V>> lev;
     int base = 0, nu1 = 2, nu2 = 2, cycle = 1, smoother = 0;
     DevBuf<double> Ainv;
+    DevBuf<double> z64;          // mixed precision: FP64 copy of the top correction
     int nbase = 0;
 
     int top() const override { return (int)lev.size() - 1; }
@@ -254,48 +255,44 @@ struct GmgT : GmgBase {
     }
 
     // ------------------------------------------------------------ cycle --
-    // level l; dtop = FP64 defect of the top level (r), first = first visit
+    // level l; dtop = FP64 defect of the top level (r), first = first visit.
+    // In mixed precision the top defect is converted to FP32 once, and the
+    // last top-level kernel writes the correction back in FP64 (z64): every
+    // float<->double conversion happens once per row, never per nonzero
+    // (conversions issue on GB300's slow FP64 pipe).
     void lmgc(Ctx &c, int l, const double *dtop, bool first, const int *skip, const double *r_rho, RedArgs *red,
               int rho_kind, bool &rho_done)
     {
         const int T = top();
         GLevel<V> &L = lev[l];
         c.prof_tag = "L" + std::to_string(l);
+        const V *top_in = nullptr;
+        if (l == T) {
+            if constexpr (sizeof(V) == sizeof(double)) {
+                top_in = (const V *)dtop;
+            } else {
+                UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
+                top_in = L.dA.p;
+            }
+        }
         if (l == base) {
             // top == base: a single-level "cycle" is the base solve
-            UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
-            base_solve<V>(c, Ainv.p, nbase, L.dA.p, L.sc.p, skip);
+            base_solve<V>(c, Ainv.p, nbase, top_in, L.sc.p, skip);
+            if (z64.p) copy_z<V>(c, L.n, L.sc.p, z64.p, skip);
             return;
         }
         GLevel<V> &C = lev[l - 1];
-        const V *cur = (l == T) ? nullptr : L.dcur;
+        const V *cur = (l == T) ? top_in : L.dcur;
         // ---- pre-smoothing
-        if (nu1 == 0) {
-            if (first) UG_LAUNCH(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, skip);
-            if (l == T) {
-                UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
-                cur = L.dA.p;
-            }
-        }
+        if (nu1 == 0 && first) UG_LAUNCH(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, skip);
         for (int k = 0; k < nu1; ++k) {
             V *out = (cur == L.dA.p) ? L.dB.p : L.dA.p;
-            if (l == T && k == 0) out = L.dB.p;
             int mode = (k == 0) ? (first ? SC_SET_FROM_BASE : SC_ADD_FROM_BASE) : SC_ADD_FROM_BASE;
             if (smoother == UG4GB_SMOOTHER_JACOBI) {
-                if (l == T && k == 0)
-                    smooth_step<V, double, double>(c, L.At, dtop, dtop, L.dinv.p, L.sc.p, out, mode, skip, nullptr,
-                                                   nullptr, 0);
-                else
-                    smooth_step<V, V, V>(c, L.At, cur, cur, L.dinv.p, L.sc.p, out, mode, skip, nullptr, nullptr, 0);
+                smooth_step<V, V, V>(c, L.At, cur, cur, L.dinv.p, L.sc.p, out, mode, skip, nullptr, nullptr, 0);
             } else {
-                if (l == T && k == 0) {
-                    gs_sweep(c, L, dtop, skip);
-                    residual_update<V, double>(c, L.At, L.t.p, dtop, out, L.sc.p, mode == SC_SET_FROM_BASE ? 1 : 0,
-                                               skip);
-                } else {
-                    gs_sweep(c, L, cur, skip);
-                    residual_update<V, V>(c, L.At, L.t.p, cur, out, L.sc.p, mode == SC_SET_FROM_BASE ? 1 : 0, skip);
-                }
+                gs_sweep(c, L, cur, skip);
+                residual_update<V, V>(c, L.At, L.t.p, cur, out, L.sc.p, mode == SC_SET_FROM_BASE ? 1 : 0, skip);
             }
             cur = out;
         }
@@ -317,15 +314,20 @@ struct GmgT : GmgBase {
         // ---- prolongation + post-smoothing
         prolong_apply<V>(c, L.Ps, C.sc.p, L.sc.p, L.dfac.p, nu2 > 0 ? L.w.p : (V *)nullptr, skip);
         const V *dbase = dpre;
+        bool z_written = false;
         if (smoother == UG4GB_SMOOTHER_JACOBI) {
             for (int k = 0; k < nu2; ++k) {
                 const V *x = (k == 0) ? L.w.p : dbase;
                 bool need_out = (k < nu2 - 1) || (l != T && cycle > 1);
                 V *out = need_out ? ((dbase == L.dA.p) ? L.dB.p : L.dA.p) : nullptr;
-                bool last_top = (l == T && k == nu2 - 1 && r_rho);
+                bool last_top = (l == T && k == nu2 - 1);
                 smooth_step<V, V, V>(c, L.At, x, dbase, L.dinv.p, L.sc.p, out, SC_ADD_FROM_NEW, skip,
-                                     last_top ? r_rho : nullptr, last_top ? red : nullptr, rho_kind);
-                if (last_top) rho_done = true;
+                                     last_top ? r_rho : nullptr, last_top ? red : nullptr, rho_kind,
+                                     last_top ? z64.p : nullptr);
+                if (last_top) {
+                    rho_done = (r_rho != nullptr);
+                    z_written = true;
+                }
                 if (out) dbase = out;
             }
         } else {
@@ -338,30 +340,23 @@ struct GmgT : GmgBase {
             }
             if (nu2 > 0) UG_LAUNCH(c, k_vadd<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, L.t.p, skip);
         }
+        if (l == T && z64.p && !z_written) copy_z<V>(c, L.n, L.sc.p, z64.p, skip);
         L.dcur = const_cast<V *>(dbase);
     }
 
-    template <class DT>
-    void gs_sweep(Ctx &c, GLevel<V> &L, const DT *d, const int *skip)
+    void gs_sweep(Ctx &c, GLevel<V> &L, const V *dv, const int *skip)
     {
-        const V *dv;
-        if constexpr (sizeof(DT) == sizeof(V)) {
-            dv = (const V *)d;
-        } else {
-            // FP64 top defect into the FP32 level: convert once into w
-            UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, (const double *)d, L.w.p, L.n);
-            dv = L.w.p;
-        }
         UG_LAUNCH(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.t.p, skip);
         for (size_t q = 0; q < L.crow.size(); ++q)
             if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], L.dinv.p, dv, L.t.p, skip);
     }
 
-    bool apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red, int rho_kind) override
+    const double *apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
+                        int rho_kind, bool &rho_done) override
     {
-        bool rho_done = false;
+        rho_done = false;
         lmgc(c, top(), dtop, true, skip, r_rho, red, rho_kind, rho_done);
-        return rho_done;
+        return z64.p ? z64.p : (const double *)lev.back().sc.p;
     }
 };
 
@@ -405,6 +400,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         if (l > m->base) G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
     }
     G->setup_base(c);
+    if (sizeof(V) != sizeof(double)) G->z64.alloc(g->lev[nl - 1].nv);
     return guard.release();
 }
 
@@ -520,9 +516,9 @@ int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
     return guarded(m->ctx, [&] {
         Ctx &c = m->ctx->c;
         if (c.profiling) {
-            m->impl->apply(c, d->d, nullptr, nullptr, nullptr, 0);
-            if (m->impl->is_fp32()) copy_z<float>(c, m->n_top, (const float *)m->impl->sc_top(), cvec->d, nullptr);
-            else copy_z<double>(c, m->n_top, (const double *)m->impl->sc_top(), cvec->d, nullptr);
+            bool rd = false;
+            const double *z = m->impl->apply(c, d->d, nullptr, nullptr, nullptr, 0, rd);
+            copy_z<double>(c, m->n_top, z, cvec->d, nullptr);
             UG_CUDA(cudaStreamSynchronize(c.stream));
             return;
         }
@@ -532,9 +528,9 @@ int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
             int64_t before = c.launches;
             UG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
             try {
-                m->impl->apply(c, d->d, nullptr, nullptr, nullptr, 0);
-                if (m->impl->is_fp32()) copy_z<float>(c, m->n_top, (const float *)m->impl->sc_top(), cvec->d, nullptr);
-                else copy_z<double>(c, m->n_top, (const double *)m->impl->sc_top(), cvec->d, nullptr);
+                bool rd = false;
+                const double *z = m->impl->apply(c, d->d, nullptr, nullptr, nullptr, 0, rd);
+                copy_z<double>(c, m->n_top, z, cvec->d, nullptr);
             } catch (...) {
                 cudaStreamEndCapture(c.stream, &gr);
                 throw;

@@ -47,35 +47,32 @@ RedArgs red_of(ug4gb_solver *s)
     return RedArgs{c.red_partials.p, c.red_counter.p, s->ks.p};
 }
 
-// z = M d (or z = d without preconditioner); rho fused when possible
-template <class ZT>
-const ZT *precond(ug4gb_solver *s, const double *d, const double *r_rho, int rho_kind)
+// z = M d (or z = d without preconditioner), always FP64; rho fused when possible
+const double *precond(ug4gb_solver *s, const double *d, const double *r_rho, int rho_kind)
 {
     Ctx &c = s->ctx->c;
     RedArgs red = red_of(s);
     const int *skip = &s->ks.p->done;
     if (!s->pre) {
         if (r_rho) rho_dot<double>(c, s->n, d, r_rho, rho_kind, red);
-        return (const ZT *)d;
+        return d;
     }
-    bool fused = s->pre->impl->apply(c, d, skip, r_rho, &red, rho_kind);
-    const ZT *z = (const ZT *)s->pre->impl->sc_top();
-    if (r_rho && !fused) rho_dot<ZT>(c, s->n, z, r_rho, rho_kind, red);
+    bool fused = false;
+    const double *z = s->pre->impl->apply(c, d, skip, r_rho, &red, rho_kind, fused);
+    if (r_rho && !fused) rho_dot<double>(c, s->n, z, r_rho, rho_kind, red);
     return z;
 }
 
-template <class ZT>
 void cg_iteration(ug4gb_solver *s, double *x, double *r, bool first)
 {
     Ctx &c = s->ctx->c;
     RedArgs red = red_of(s);
-    const ZT *z = precond<ZT>(s, r, r, first ? 0 : 1);
+    const double *z = precond(s, r, r, first ? 0 : 1);
     c.prof_tag = "K";
-    cg_spmv_dot_t<ZT>(c, s->A->op, z, s->p.p, s->q.p, first ? 1 : 0, red);
+    cg_spmv_dot_t<double>(c, s->A->op, z, s->p.p, s->q.p, first ? 1 : 0, red);
     cg_update(c, s->n, x, r, s->p.p, s->q.p, red);
 }
 
-template <class ZT>
 void bicg_iteration(ug4gb_solver *s, double *x, double *r)
 {
     Ctx &c = s->ctx->c;
@@ -85,18 +82,16 @@ void bicg_iteration(ug4gb_solver *s, double *x, double *r)
     bicg_restart(c, n, r, s->r0.p, s->p.p, s->v.p, red);
     bicg_rho(c, n, s->r0.p, r, red);
     bicg_p(c, n, r, s->p.p, s->v.p, red);
-    const ZT *q = precond<ZT>(s, s->p.p, nullptr, 0);
+    const double *q = precond(s, s->p.p, nullptr, 0);
     c.prof_tag = "K";
-    bicg_spmv_dot_t<ZT>(c, s->A->op, q, s->v.p, s->r0.p, red);
-    bicg_x_s<ZT>(c, n, x, q, r, s->v.p, s->s.p, red);
+    bicg_spmv_dot_t<double>(c, s->A->op, q, s->v.p, s->r0.p, red);
+    bicg_x_s<double>(c, n, x, q, r, s->v.p, s->s.p, red);
     bicg_s_to_r(c, n, s->s.p, r, red);
-    q = precond<ZT>(s, s->s.p, nullptr, 0);
+    q = precond(s, s->s.p, nullptr, 0);
     c.prof_tag = "K";
-    bicg_spmv_2dot_t<ZT>(c, s->A->op, q, s->t.p, s->s.p, red);
-    bicg_x_r<ZT>(c, n, x, q, s->s.p, s->t.p, r, red);
+    bicg_spmv_2dot_t<double>(c, s->A->op, q, s->t.p, s->s.p, red);
+    bicg_x_r<double>(c, n, x, q, s->s.p, s->t.p, r, red);
 }
-
-bool z_is_fp32(ug4gb_solver *s) { return s->pre && s->pre->impl->is_fp32(); }
 
 // last node of the loop body: keep iterating while the check has not ended
 __global__ void k_loop_cond(cudaGraphConditionalHandle h, const KScal *ks)
@@ -104,22 +99,17 @@ __global__ void k_loop_cond(cudaGraphConditionalHandle h, const KScal *ks)
     cudaGraphSetConditional(h, ks->done ? 0u : 1u);
 }
 
-void iteration(ug4gb_solver *s, double *x, double *r, bool f32)
+void iteration(ug4gb_solver *s, double *x, double *r)
 {
-    if (s->kind == UG4GB_SOLVER_CG) {
-        if (f32) cg_iteration<float>(s, x, r, false);
-        else cg_iteration<double>(s, x, r, false);
-    } else {
-        if (f32) bicg_iteration<float>(s, x, r);
-        else bicg_iteration<double>(s, x, r);
-    }
+    if (s->kind == UG4GB_SOLVER_CG) cg_iteration(s, x, r, false);
+    else bicg_iteration(s, x, r);
 }
 
 // The whole iteration loop as one graph: a conditional WHILE node whose body
 // is one Krylov iteration (multigrid cycle included) followed by
 // k_loop_cond.  The loop ends when the device-side StdConvCheck (or a
 // breakdown) sets done, at the latest after max_steps iterations.
-void build_loop_graph(ug4gb_solver *s, double *x, double *r, bool f32)
+void build_loop_graph(ug4gb_solver *s, double *x, double *r)
 {
     Ctx &c = s->ctx->c;
     cudaGraph_t g;
@@ -139,7 +129,7 @@ void build_loop_graph(ug4gb_solver *s, double *x, double *r, bool f32)
         cudaGraph_t body = cp.conditional.phGraph_out[0];
         UG_CUDA(cudaStreamBeginCaptureToGraph(c.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         try {
-            iteration(s, x, r, f32);
+            iteration(s, x, r);
             UG_LAUNCH(c, k_loop_cond, 1, 1, 0, h, (const KScal *)s->ks.p);
         } catch (...) {
             cudaGraph_t tmp;
@@ -184,20 +174,16 @@ void run(ug4gb_solver *s, double *x, double *r)
     h.hist = s->hist.p;
     UG_CUDA(cudaMemcpyAsync(s->ks.p, &h, sizeof(KScal), cudaMemcpyHostToDevice, c.stream));
     RedArgs red = red_of(s);
-    const bool f32 = z_is_fp32(s);
     // prologue: r = b - A x, start the check; CG also does the first step
     c.prof_tag = "K";
     krylov_start(c, s->A->op, x, r, red);
-    if (s->kind == UG4GB_SOLVER_CG) {
-        if (f32) cg_iteration<float>(s, x, r, true);
-        else cg_iteration<double>(s, x, r, true);
-    }
+    if (s->kind == UG4GB_SOLVER_CG) cg_iteration(s, x, r, true);
     int done = 0;
     read_flags(s, &done);
     if (!done && c.profiling) {
         // profiled run: direct launches, each one timed with events
         while (!done) {
-            iteration(s, x, r, f32);
+            iteration(s, x, r);
             read_flags(s, &done);
         }
     }
@@ -205,7 +191,7 @@ void run(ug4gb_solver *s, double *x, double *r)
         int pre_gen = s->pre ? s->pre->gen : -1;
         if (!s->iter_graph || s->graph_x != x || s->graph_r != r || s->graph_pre_gen != pre_gen) {
             drop_graph(s);
-            build_loop_graph(s, x, r, f32);
+            build_loop_graph(s, x, r);
             s->graph_x = x;
             s->graph_r = r;
             s->graph_pre_gen = pre_gen;

@@ -89,10 +89,10 @@ struct GmgBase {
     virtual int top() const = 0;
     virtual bool is_fp32() const = 0;
     virtual void *sc_top() = 0;
-    // z = M d_top (d_top FP64, device); rho fused with r_rho if possible.
-    // returns true if rho was computed
-    virtual bool apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
-                       int rho_kind) = 0;
+    // z = M d_top (d_top FP64, device); returns z in FP64.  rho = (z, r_rho)
+    // is fused into the last kernel when possible (rho_done tells).
+    virtual const double *apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
+                                int rho_kind, bool &rho_done) = 0;
     virtual const Csr &P(int l) const = 0;
     virtual const Csr &R(int l) const = 0;
 };

@@ -121,7 +121,7 @@ template <class MV, class V, class XT, class DT, bool RHO>
 __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, const DT *__restrict__ dbase,
                                                const V *__restrict__ dinv, V *__restrict__ sc, V *__restrict__ dout,
                                                int sc_mode, const int *skip, const double *__restrict__ r_rho,
-                                               RedArgs red, int rho_kind)
+                                               RedArgs red, int rho_kind, double *__restrict__ z64)
 {
     if (skip && *skip) return;
     double rsum = 0.0;
@@ -134,7 +134,11 @@ __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, c
         V t = dinv[row] * (sc_mode == SC_ADD_FROM_NEW ? dn : db);
         V s = (sc_mode == SC_SET_FROM_BASE) ? t : sc[row] + t;
         sc[row] = s;
-        if (RHO) rsum += (double)s * r_rho[row];
+        if (RHO || z64) {
+            const double s64 = (double)s;   // one conversion per row, only where needed
+            if (z64) z64[row] = s64;
+            if (RHO) rsum += s64 * r_rho[row];
+        }
     }
     if (RHO) {
         double v[1] = {rsum};
@@ -153,28 +157,27 @@ __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, c
 
 template <class V, class XT, class DT>
 void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout, int sc_mode,
-                 const int *skip, const double *r_rho, RedArgs *red, int rho_kind)
+                 const int *skip, const double *r_rho, RedArgs *red, int rho_kind, double *z64)
 {
     const int g = row_grid(c, At.nrows);
     with_mv(At, [&](auto mv) {
         using MV = decltype(mv);
         if (r_rho) {
             UG_LAUNCH(c, (k_smooth<MV, V, XT, DT, true>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
-                      r_rho, *red, rho_kind);
+                      r_rho, *red, rho_kind, z64);
         } else {
             RedArgs none{nullptr, nullptr, nullptr};
             UG_LAUNCH(c, (k_smooth<MV, V, XT, DT, false>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
-                      (const double *)nullptr, none, 0);
+                      (const double *)nullptr, none, 0, z64);
         }
     });
 }
 
 #define INST_SMOOTH(V, XT, DT)                                                                              \
     template void smooth_step<V, XT, DT>(Ctx &, const OpMat<V> &, const XT *, const DT *, const V *, V *, V *, int, \
-                                         const int *, const double *, RedArgs *, int);
+                                         const int *, const double *, RedArgs *, int, double *);
 INST_SMOOTH(double, double, double)
 INST_SMOOTH(float, float, float)
-INST_SMOOTH(float, double, double)
 
 // --------------------------------------------------------- transfers -----
 template <class MV, class V>

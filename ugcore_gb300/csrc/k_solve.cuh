@@ -36,10 +36,12 @@ int row_grid(const Ctx &c, int nrows);
 
 // ---- multigrid level kernels (V = level precision) ----
 // dnew = dbase - At*x ; sc (=|+=) dinv*(dbase|dnew) ; optional dout = dnew;
-// optional rho = sum sc_i * r_i (final top-level step inside a Krylov solve)
+// optional rho = sum sc_i * r_i (final top-level step inside a Krylov solve);
+// optional z64 = (double) sc (mixed precision: FP64 correction for the Krylov loop)
 template <class V, class XT, class DT>
 void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout,
-                 int sc_mode, const int *skip, const double *r_rho, RedArgs *red, int rho_kind);
+                 int sc_mode, const int *skip, const double *r_rho, RedArgs *red, int rho_kind,
+                 double *z64 = nullptr);
 template <class V>
 void restrict_apply(Ctx &c, const OpMat<V> &R, const V *d, V *dc, const int *skip);
 template <class V>
