@@ -46,6 +46,7 @@ __global__ void k_diag_inv(const int *rowptr, const int *col, const double *val,
 template <class V>
 __global__ void k_to_v(const double *in, V *out, int n)
 {
+    PDL_ENTRY();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = (V)in[i];
 }
@@ -101,6 +102,7 @@ __global__ void k_colour_rows(const int *color, int n, int c, int *rows, int *co
 template <class V>
 __global__ void k_vadd(int n, V *a, const V *b, const int *skip)
 {
+    PDL_ENTRY();
     if (skip && *skip) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] += b[i];
@@ -109,6 +111,7 @@ __global__ void k_vadd(int n, V *a, const V *b, const int *skip)
 template <class V>
 __global__ void k_zero(int n, V *a, const int *skip)
 {
+    PDL_ENTRY();
     if (skip && *skip) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = (V)0;
@@ -271,7 +274,7 @@ struct GmgT : GmgBase {
             if constexpr (sizeof(V) == sizeof(double)) {
                 top_in = (const V *)dtop;
             } else {
-                UG_LAUNCH(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
+                UG_LAUNCH_PDL(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
                 top_in = L.dA.p;
             }
         }
@@ -284,7 +287,7 @@ struct GmgT : GmgBase {
         GLevel<V> &C = lev[l - 1];
         const V *cur = (l == T) ? top_in : L.dcur;
         // ---- pre-smoothing
-        if (nu1 == 0 && first) UG_LAUNCH(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, skip);
+        if (nu1 == 0 && first) UG_LAUNCH_PDL(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, skip);
         for (int k = 0; k < nu1; ++k) {
             V *out = (cur == L.dA.p) ? L.dB.p : L.dA.p;
             int mode = (k == 0) ? (first ? SC_SET_FROM_BASE : SC_ADD_FROM_BASE) : SC_ADD_FROM_BASE;
@@ -338,7 +341,7 @@ struct GmgT : GmgBase {
                 gs_sweep(c, L, out, skip);
                 dbase = out;
             }
-            if (nu2 > 0) UG_LAUNCH(c, k_vadd<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, L.t.p, skip);
+            if (nu2 > 0) UG_LAUNCH_PDL(c, k_vadd<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, L.t.p, skip);
         }
         if (l == T && z64.p && !z_written) copy_z<V>(c, L.n, L.sc.p, z64.p, skip);
         L.dcur = const_cast<V *>(dbase);
@@ -346,7 +349,7 @@ struct GmgT : GmgBase {
 
     void gs_sweep(Ctx &c, GLevel<V> &L, const V *dv, const int *skip)
     {
-        UG_LAUNCH(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.t.p, skip);
+        UG_LAUNCH_PDL(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.t.p, skip);
         for (size_t q = 0; q < L.crow.size(); ++q)
             if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], L.dinv.p, dv, L.t.p, skip);
     }

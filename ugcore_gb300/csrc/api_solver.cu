@@ -96,6 +96,7 @@ void bicg_iteration(ug4gb_solver *s, double *x, double *r)
 // last node of the loop body: keep iterating while the check has not ended
 __global__ void k_loop_cond(cudaGraphConditionalHandle h, const KScal *ks)
 {
+    PDL_ENTRY();
     cudaGraphSetConditional(h, ks->done ? 0u : 1u);
 }
 
@@ -130,7 +131,7 @@ void build_loop_graph(ug4gb_solver *s, double *x, double *r)
         UG_CUDA(cudaStreamBeginCaptureToGraph(c.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         try {
             iteration(s, x, r);
-            UG_LAUNCH(c, k_loop_cond, 1, 1, 0, h, (const KScal *)s->ks.p);
+            UG_LAUNCH_PDL(c, k_loop_cond, 1, 1, 0, h, (const KScal *)s->ks.p);
         } catch (...) {
             cudaGraph_t tmp;
             cudaStreamEndCapture(c.stream, &tmp);
@@ -191,7 +192,16 @@ void run(ug4gb_solver *s, double *x, double *r)
         int pre_gen = s->pre ? s->pre->gen : -1;
         if (!s->iter_graph || s->graph_x != x || s->graph_r != r || s->graph_pre_gen != pre_gen) {
             drop_graph(s);
-            build_loop_graph(s, x, r);
+            try {
+                build_loop_graph(s, x, r);
+            } catch (const Error &e) {
+                // a driver that rejects programmatic edges inside a conditional
+                // body: rebuild the loop with plain stream-ordered launches
+                if (e.code != UG4GB_ERR_CUDA || !c.pdl) throw;
+                (void)cudaGetLastError();
+                c.pdl = false;
+                build_loop_graph(s, x, r);
+            }
             s->graph_x = x;
             s->graph_r = r;
             s->graph_pre_gen = pre_gen;

@@ -88,6 +88,7 @@ struct Ctx {
     int64_t launches = 0;
     bool profiling = false;
     bool allow_dia = true;      // operators with <= 27 offsets use the diagonal layout
+    bool pdl = true;            // programmatic dependent launch on the solve path
     std::string prof_tag;       // set by the orchestration (level / phase)
     std::vector<ProfRec> prof;
     std::vector<cudaEvent_t> ev_pool;
@@ -120,6 +121,39 @@ cudaEvent_t prof_event(Ctx &c);
             UG_CUDA(cudaEventRecord(ev_b_, (ctx).stream));                                         \
             (ctx).prof.push_back(::ug4gb::ProfRec{(ctx).prof_tag + "|" + #kernel, ev_a_, ev_b_});  \
         }                                                                                          \
+    } while (0)
+
+// Programmatic dependent launch for the solve-path kernels: the next kernel
+// of the stream is scheduled while the current one still runs, and waits in
+// griddepcontrol.wait until its predecessor has completed and its memory is
+// visible.  Every kernel launched this way starts with PDL_ENTRY(), before
+// it reads anything (including its skip flag): a kernel that could finish
+// without waiting would let its successor overtake its own predecessor.
+__device__ __forceinline__ void pdl_entry()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+#define PDL_ENTRY() ::ug4gb::pdl_entry()
+
+#define UG_LAUNCH_PDL(ctx, kernel, grid, block, shmem, ...)                                        \
+    do {                                                                                           \
+        if (!(ctx).pdl || (ctx).profiling) {                                                       \
+            UG_LAUNCH(ctx, kernel, grid, block, shmem, __VA_ARGS__);                               \
+            break;                                                                                 \
+        }                                                                                          \
+        cudaLaunchConfig_t cfg_ = {};                                                              \
+        cfg_.gridDim = dim3(grid);                                                                 \
+        cfg_.blockDim = dim3(block);                                                               \
+        cfg_.dynamicSmemBytes = (shmem);                                                           \
+        cfg_.stream = (ctx).stream;                                                                \
+        cudaLaunchAttribute at_[1];                                                                \
+        at_[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;                            \
+        at_[0].val.programmaticStreamSerializationAllowed = 1;                                     \
+        cfg_.attrs = at_;                                                                          \
+        cfg_.numAttrs = 1;                                                                         \
+        UG_CUDA(cudaLaunchKernelEx(&cfg_, kernel, __VA_ARGS__));                                   \
+        (ctx).launches++;                                                                          \
     } while (0)
 
 inline unsigned div_up(size_t a, size_t b) { return (unsigned)((a + b - 1) / b); }

@@ -123,6 +123,7 @@ __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, c
                                                int sc_mode, const int *skip, const double *__restrict__ r_rho,
                                                RedArgs red, int rho_kind, double *__restrict__ z64)
 {
+    PDL_ENTRY();
     if (skip && *skip) return;
     double rsum = 0.0;
     const int stride = gridDim.x * NT, n = A.rows();
@@ -163,11 +164,11 @@ void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const
     with_mv(At, [&](auto mv) {
         using MV = decltype(mv);
         if (r_rho) {
-            UG_LAUNCH(c, (k_smooth<MV, V, XT, DT, true>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
+            UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, true>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
                       r_rho, *red, rho_kind, z64);
         } else {
             RedArgs none{nullptr, nullptr, nullptr};
-            UG_LAUNCH(c, (k_smooth<MV, V, XT, DT, false>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
+            UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, false>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
                       (const double *)nullptr, none, 0, z64);
         }
     });
@@ -183,6 +184,7 @@ INST_SMOOTH(float, float, float)
 template <class MV, class V>
 __global__ void __launch_bounds__(NT) k_restrict(MV R, const V *__restrict__ d, V *__restrict__ dc, const int *skip)
 {
+    PDL_ENTRY();
     if (skip && *skip) return;
     const int stride = gridDim.x * NT, n = R.rows();
     for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) dc[row] = R.template dot<V>(d, row);
@@ -192,7 +194,7 @@ template <class V>
 void restrict_apply(Ctx &c, const OpMat<V> &R, const V *d, V *dc, const int *skip)
 {
     with_mv(R, [&](auto mv) {
-        UG_LAUNCH(c, (k_restrict<decltype(mv), V>), row_grid(c, R.nrows), NT, 0, mv, d, dc, skip);
+        UG_LAUNCH_PDL(c, (k_restrict<decltype(mv), V>), row_grid(c, R.nrows), NT, 0, mv, d, dc, skip);
     });
 }
 
@@ -200,6 +202,7 @@ template <class MV, class V>
 __global__ void __launch_bounds__(NT) k_prolong(MV P, const V *__restrict__ scc, V *__restrict__ sc,
                                                 const V *__restrict__ dfac, V *__restrict__ w, const int *skip)
 {
+    PDL_ENTRY();
     if (skip && *skip) return;
     const int stride = gridDim.x * NT, n = P.rows();
     for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
@@ -213,7 +216,7 @@ template <class V>
 void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip)
 {
     with_mv(P, [&](auto mv) {
-        UG_LAUNCH(c, (k_prolong<decltype(mv), V>), row_grid(c, P.nrows), NT, 0, mv, scc, sc, dfac, w, skip);
+        UG_LAUNCH_PDL(c, (k_prolong<decltype(mv), V>), row_grid(c, P.nrows), NT, 0, mv, scc, sc, dfac, w, skip);
     });
 }
 
@@ -222,6 +225,7 @@ template <class V>
 __global__ void k_base_solve(const double *__restrict__ Ainv, int n, const V *__restrict__ d, V *__restrict__ sc,
                              const int *skip)
 {
+    PDL_ENTRY();
     extern __shared__ double dsh[];
     if (skip && *skip) return;
     for (int j = threadIdx.x; j < n; j += blockDim.x) dsh[j] = (double)d[j];
@@ -236,7 +240,7 @@ __global__ void k_base_solve(const double *__restrict__ Ainv, int n, const V *__
 template <class V>
 void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip)
 {
-    UG_LAUNCH(c, k_base_solve<V>, 1, NT, (size_t)n * sizeof(double), Ainv, n, d, sc, skip);
+    UG_LAUNCH_PDL(c, k_base_solve<V>, 1, NT, (size_t)n * sizeof(double), Ainv, n, d, sc, skip);
 }
 
 // multicolour Gauss-Seidel: rows of one colour, t_i = relax (d_i - (A t)_i) / a_ii
@@ -246,6 +250,7 @@ __global__ void __launch_bounds__(NT) k_mcgs(MV A, const int *__restrict__ rows,
                                              const V *__restrict__ dr, const V *__restrict__ d, V *__restrict__ t,
                                              const int *skip)
 {
+    PDL_ENTRY();
     if (skip && *skip) return;
     const int stride = gridDim.x * NT;
     for (int q = blockIdx.x * NT + threadIdx.x; q < nrows_c; q += stride) {
@@ -260,7 +265,7 @@ void mcgs_colour(Ctx &c, const OpMat<V> &A, const int *rows, int nrows_c, const 
                  const int *skip)
 {
     with_mv(A, [&](auto mv) {
-        UG_LAUNCH(c, (k_mcgs<decltype(mv), V>), row_grid(c, nrows_c), NT, 0, mv, rows, nrows_c, dinv_relax, d, t,
+        UG_LAUNCH_PDL(c, (k_mcgs<decltype(mv), V>), row_grid(c, nrows_c), NT, 0, mv, rows, nrows_c, dinv_relax, d, t,
                   skip);
     });
 }
@@ -269,6 +274,7 @@ template <class MV, class V, class DT>
 __global__ void __launch_bounds__(NT) k_resupd(MV A, const V *__restrict__ t, const DT *__restrict__ dbase,
                                                V *__restrict__ dout, V *__restrict__ sc, int sc_mode, const int *skip)
 {
+    PDL_ENTRY();
     if (skip && *skip) return;
     const int stride = gridDim.x * NT, n = A.rows();
     for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
@@ -284,7 +290,7 @@ void residual_update(Ctx &c, const OpMat<V> &A, const V *t, const DT *dbase, V *
                      const int *skip)
 {
     with_mv(A, [&](auto mv) {
-        UG_LAUNCH(c, (k_resupd<decltype(mv), V, DT>), row_grid(c, A.nrows), NT, 0, mv, t, dbase, dout, sc, sc_mode,
+        UG_LAUNCH_PDL(c, (k_resupd<decltype(mv), V, DT>), row_grid(c, A.nrows), NT, 0, mv, t, dbase, dout, sc, sc_mode,
                   skip);
     });
 }
@@ -314,6 +320,7 @@ template <class MV>
 __global__ void __launch_bounds__(NT) k_krylov_start(MV A, const double *__restrict__ x, double *__restrict__ r,
                                                      RedArgs red)
 {
+    PDL_ENTRY();
     double sum = 0.0;
     const int stride = gridDim.x * NT, n = A.rows();
     for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
@@ -340,7 +347,7 @@ __global__ void __launch_bounds__(NT) k_krylov_start(MV A, const double *__restr
 void krylov_start(Ctx &c, const OpMat<double> &A, const double *x, double *r, RedArgs red)
 {
     with_mv(A, [&](auto mv) {
-        UG_LAUNCH(c, k_krylov_start<decltype(mv)>, row_grid(c, A.nrows), NT, 0, mv, x, r, red);
+        UG_LAUNCH_PDL(c, k_krylov_start<decltype(mv)>, row_grid(c, A.nrows), NT, 0, mv, x, r, red);
     });
 }
 
@@ -349,6 +356,7 @@ template <class MV, class ZT>
 __global__ void __launch_bounds__(NT) k_cg_spmv_dot(MV A, const ZT *__restrict__ z, double *__restrict__ p,
                                                     double *__restrict__ q, int first, RedArgs red)
 {
+    PDL_ENTRY();
     KScal *ks = red.ks;
     if (ks->done) return;
     const double beta = first ? 0.0 : ks->beta;
@@ -377,7 +385,7 @@ template <class ZT>
 void cg_spmv_dot_t(Ctx &c, const OpMat<double> &A, const ZT *z, double *p, double *q, int first, RedArgs red)
 {
     with_mv(A, [&](auto mv) {
-        UG_LAUNCH(c, (k_cg_spmv_dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, z, p, q, first, red);
+        UG_LAUNCH_PDL(c, (k_cg_spmv_dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, z, p, q, first, red);
     });
 }
 template void cg_spmv_dot_t<double>(Ctx &, const OpMat<double> &, const double *, double *, double *, int, RedArgs);
@@ -388,6 +396,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(int n, double *__restrict__ x,
                                                   const double *__restrict__ p, const double *__restrict__ q,
                                                   RedArgs red)
 {
+    PDL_ENTRY();
     KScal *ks = red.ks;
     if (ks->done) return;
     const double alpha = ks->alpha;
@@ -405,7 +414,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(int n, double *__restrict__ x,
 
 void cg_update(Ctx &c, int n, double *x, double *r, const double *p, const double *q, RedArgs red)
 {
-    UG_LAUNCH(c, k_cg_update, row_grid(c, n), NT, 0, n, x, r, p, q, red);
+    UG_LAUNCH_PDL(c, k_cg_update, row_grid(c, n), NT, 0, n, x, r, p, q, red);
 }
 
 // rho = (z, r) when the preconditioner could not fuse it (kind 0: first, 1: loop)
@@ -413,6 +422,7 @@ template <class ZT>
 __global__ void __launch_bounds__(NT) k_rho(int n, const ZT *__restrict__ z, const double *__restrict__ r, int kind,
                                             RedArgs red)
 {
+    PDL_ENTRY();
     KScal *ks = red.ks;
     if (ks->done) return;
     double sum = 0.0;
@@ -433,7 +443,7 @@ __global__ void __launch_bounds__(NT) k_rho(int n, const ZT *__restrict__ z, con
 template <class ZT>
 void rho_dot(Ctx &c, int n, const ZT *z, const double *r, int kind, RedArgs red)
 {
-    UG_LAUNCH(c, k_rho<ZT>, row_grid(c, n), NT, 0, n, z, r, kind, red);
+    UG_LAUNCH_PDL(c, k_rho<ZT>, row_grid(c, n), NT, 0, n, z, r, kind, red);
 }
 template void rho_dot<double>(Ctx &, int, const double *, const double *, int, RedArgs);
 template void rho_dot<float>(Ctx &, int, const float *, const double *, int, RedArgs);
@@ -441,6 +451,7 @@ template void rho_dot<float>(Ctx &, int, const float *, const double *, int, Red
 template <class ZT>
 __global__ void k_copy_z(int n, const ZT *__restrict__ z, double *__restrict__ out, const int *skip)
 {
+    PDL_ENTRY();
     if (skip && *skip) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = (double)z[i];
@@ -449,7 +460,7 @@ __global__ void k_copy_z(int n, const ZT *__restrict__ z, double *__restrict__ o
 template <class ZT>
 void copy_z(Ctx &c, int n, const ZT *z, double *out, const int *skip)
 {
-    UG_LAUNCH(c, k_copy_z<ZT>, div_up(n, NT), NT, 0, n, z, out, skip);
+    UG_LAUNCH_PDL(c, k_copy_z<ZT>, div_up(n, NT), NT, 0, n, z, out, skip);
 }
 template void copy_z<double>(Ctx &, int, const double *, double *, const int *);
 template void copy_z<float>(Ctx &, int, const float *, double *, const int *);
@@ -459,6 +470,7 @@ template void copy_z<float>(Ctx &, int, const float *, double *, const int *);
 __global__ void k_bicg_restart(int n, const double *__restrict__ r, double *__restrict__ r0, double *__restrict__ p,
                                double *__restrict__ v, KScal *ks)
 {
+    PDL_ENTRY();
     if (ks->done || !ks->restart) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
@@ -470,12 +482,13 @@ __global__ void k_bicg_restart(int n, const double *__restrict__ r, double *__re
 
 void bicg_restart(Ctx &c, int n, const double *r, double *r0, double *p, double *v, RedArgs red)
 {
-    UG_LAUNCH(c, k_bicg_restart, div_up(n, NT), NT, 0, n, r, r0, p, v, red.ks);
+    UG_LAUNCH_PDL(c, k_bicg_restart, div_up(n, NT), NT, 0, n, r, r0, p, v, red.ks);
 }
 
 __global__ void __launch_bounds__(NT) k_bicg_rho(int n, const double *__restrict__ r0, const double *__restrict__ r,
                                                  RedArgs red)
 {
+    PDL_ENTRY();
     KScal *ks = red.ks;
     if (ks->done) return;
     double sum = 0.0;
@@ -504,12 +517,13 @@ __global__ void __launch_bounds__(NT) k_bicg_rho(int n, const double *__restrict
 
 void bicg_rho(Ctx &c, int n, const double *r0, const double *r, RedArgs red)
 {
-    UG_LAUNCH(c, k_bicg_rho, row_grid(c, n), NT, 0, n, r0, r, red);
+    UG_LAUNCH_PDL(c, k_bicg_rho, row_grid(c, n), NT, 0, n, r0, r, red);
 }
 
 __global__ void k_bicg_p(int n, const double *__restrict__ r, double *__restrict__ p, const double *__restrict__ v,
                          const KScal *ks)
 {
+    PDL_ENTRY();
     if (ks->done) return;
     const double beta = ks->beta, bo = -ks->beta * ks->omega;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -518,13 +532,14 @@ __global__ void k_bicg_p(int n, const double *__restrict__ r, double *__restrict
 
 void bicg_p(Ctx &c, int n, const double *r, double *p, const double *v, RedArgs red)
 {
-    UG_LAUNCH(c, k_bicg_p, div_up(n, NT), NT, 0, n, r, p, v, red.ks);
+    UG_LAUNCH_PDL(c, k_bicg_p, div_up(n, NT), NT, 0, n, r, p, v, red.ks);
 }
 
 template <class MV, class ZT>
 __global__ void __launch_bounds__(NT) k_bicg_spmv_dot(MV A, const ZT *__restrict__ q, double *__restrict__ v,
                                                       const double *__restrict__ r0, RedArgs red)
 {
+    PDL_ENTRY();
     KScal *ks = red.ks;
     if (ks->done) return;
     double sum = 0.0;
@@ -548,7 +563,7 @@ template <class ZT>
 void bicg_spmv_dot_t(Ctx &c, const OpMat<double> &A, const ZT *q, double *v, const double *r0, RedArgs red)
 {
     with_mv(A, [&](auto mv) {
-        UG_LAUNCH(c, (k_bicg_spmv_dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, q, v, r0, red);
+        UG_LAUNCH_PDL(c, (k_bicg_spmv_dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, q, v, r0, red);
     });
 }
 template void bicg_spmv_dot_t<double>(Ctx &, const OpMat<double> &, const double *, double *, const double *, RedArgs);
@@ -559,6 +574,7 @@ __global__ void __launch_bounds__(NT) k_bicg_x_s(int n, double *__restrict__ x, 
                                                  const double *__restrict__ r, const double *__restrict__ v,
                                                  double *__restrict__ s, RedArgs red)
 {
+    PDL_ENTRY();
     KScal *ks = red.ks;
     if (ks->done) return;
     const double alpha = ks->alpha;
@@ -577,13 +593,14 @@ __global__ void __launch_bounds__(NT) k_bicg_x_s(int n, double *__restrict__ x, 
 template <class ZT>
 void bicg_x_s(Ctx &c, int n, double *x, const ZT *q, const double *r, const double *v, double *s, RedArgs red)
 {
-    UG_LAUNCH(c, k_bicg_x_s<ZT>, row_grid(c, n), NT, 0, n, x, q, r, v, s, red);
+    UG_LAUNCH_PDL(c, k_bicg_x_s<ZT>, row_grid(c, n), NT, 0, n, x, q, r, v, s, red);
 }
 template void bicg_x_s<double>(Ctx &, int, double *, const double *, const double *, const double *, double *, RedArgs);
 template void bicg_x_s<float>(Ctx &, int, double *, const float *, const double *, const double *, double *, RedArgs);
 
 __global__ void k_bicg_s_to_r(int n, const double *__restrict__ s, double *__restrict__ r, const KScal *ks)
 {
+    PDL_ENTRY();
     if (ks->done != 2) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) r[i] = s[i];
@@ -591,13 +608,14 @@ __global__ void k_bicg_s_to_r(int n, const double *__restrict__ s, double *__res
 
 void bicg_s_to_r(Ctx &c, int n, const double *s, double *r, RedArgs red)
 {
-    UG_LAUNCH(c, k_bicg_s_to_r, div_up(n, NT), NT, 0, n, s, r, red.ks);
+    UG_LAUNCH_PDL(c, k_bicg_s_to_r, div_up(n, NT), NT, 0, n, s, r, red.ks);
 }
 
 template <class MV, class ZT>
 __global__ void __launch_bounds__(NT) k_bicg_spmv_2dot(MV A, const ZT *__restrict__ q, double *__restrict__ t,
                                                        const double *__restrict__ s, RedArgs red)
 {
+    PDL_ENTRY();
     KScal *ks = red.ks;
     if (ks->done) return;
     double tt = 0.0, st = 0.0;
@@ -622,7 +640,7 @@ template <class ZT>
 void bicg_spmv_2dot_t(Ctx &c, const OpMat<double> &A, const ZT *q, double *t, const double *s, RedArgs red)
 {
     with_mv(A, [&](auto mv) {
-        UG_LAUNCH(c, (k_bicg_spmv_2dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, q, t, s, red);
+        UG_LAUNCH_PDL(c, (k_bicg_spmv_2dot<decltype(mv), ZT>), row_grid(c, A.nrows), NT, 0, mv, q, t, s, red);
     });
 }
 template void bicg_spmv_2dot_t<double>(Ctx &, const OpMat<double> &, const double *, double *, const double *,
@@ -634,6 +652,7 @@ __global__ void __launch_bounds__(NT) k_bicg_x_r(int n, double *__restrict__ x, 
                                                  const double *__restrict__ s, const double *__restrict__ t,
                                                  double *__restrict__ r, RedArgs red)
 {
+    PDL_ENTRY();
     KScal *ks = red.ks;
     if (ks->done) return;
     const double omega = ks->omega;
@@ -658,7 +677,7 @@ __global__ void __launch_bounds__(NT) k_bicg_x_r(int n, double *__restrict__ x, 
 template <class ZT>
 void bicg_x_r(Ctx &c, int n, double *x, const ZT *q, const double *s, const double *t, double *r, RedArgs red)
 {
-    UG_LAUNCH(c, k_bicg_x_r<ZT>, row_grid(c, n), NT, 0, n, x, q, s, t, r, red);
+    UG_LAUNCH_PDL(c, k_bicg_x_r<ZT>, row_grid(c, n), NT, 0, n, x, q, s, t, r, red);
 }
 template void bicg_x_r<double>(Ctx &, int, double *, const double *, const double *, const double *, double *, RedArgs);
 template void bicg_x_r<float>(Ctx &, int, double *, const float *, const double *, const double *, double *, RedArgs);
@@ -667,6 +686,7 @@ template void bicg_x_r<float>(Ctx &, int, double *, const float *, const double 
 __global__ void __launch_bounds__(NT) k_vec_dot(int n, const double *__restrict__ a, const double *__restrict__ b,
                                                 RedArgs red)
 {
+    PDL_ENTRY();
     double sum = 0.0;
     const int stride = gridDim.x * NT;
     for (int i = blockIdx.x * NT + threadIdx.x; i < n; i += stride) sum += a[i] * b[i];
@@ -677,18 +697,19 @@ __global__ void __launch_bounds__(NT) k_vec_dot(int n, const double *__restrict_
 
 void vec_dot(Ctx &c, int n, const double *a, const double *b, RedArgs red)
 {
-    UG_LAUNCH(c, k_vec_dot, row_grid(c, n), NT, 0, n, a, b, red);
+    UG_LAUNCH_PDL(c, k_vec_dot, row_grid(c, n), NT, 0, n, a, b, red);
 }
 
 __global__ void k_vec_scale_add(int n, double *dest, double alpha, const double *a, double beta, const double *b)
 {
+    PDL_ENTRY();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) dest[i] = alpha * a[i] + beta * b[i];
 }
 
 void vec_scale_add(Ctx &c, int n, double *dest, double alpha, const double *a, double beta, const double *b)
 {
-    UG_LAUNCH(c, k_vec_scale_add, div_up(n, NT), NT, 0, n, dest, alpha, a, beta, b);
+    UG_LAUNCH_PDL(c, k_vec_scale_add, div_up(n, NT), NT, 0, n, dest, alpha, a, beta, b);
 }
 
 // dest = alpha*v1 + beta*A*w1 (SparseMatrix::axpy, sparsematrix_impl.h:294-342)
@@ -696,6 +717,7 @@ template <class MV>
 __global__ void __launch_bounds__(NT) k_op_axpy(MV A, double *dest, double alpha, const double *v1, double beta,
                                                 const double *__restrict__ w1)
 {
+    PDL_ENTRY();
     const int stride = gridDim.x * NT, n = A.rows();
     for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
         double aw = A.template dot<double>(w1, row);
@@ -707,7 +729,7 @@ void op_axpy(Ctx &c, const OpMat<double> &A, double *dest, double alpha, const d
              const double *w1)
 {
     with_mv(A, [&](auto mv) {
-        UG_LAUNCH(c, k_op_axpy<decltype(mv)>, row_grid(c, A.nrows), NT, 0, mv, dest, alpha, v1, beta, w1);
+        UG_LAUNCH_PDL(c, k_op_axpy<decltype(mv)>, row_grid(c, A.nrows), NT, 0, mv, dest, alpha, v1, beta, w1);
     });
 }
 
@@ -715,6 +737,7 @@ void op_axpy(Ctx &c, const OpMat<double> &A, double *dest, double alpha, const d
 __global__ void k_csr_axpy_t(int nrows, const int *rowptr, const int *col, const double *val, double *dest,
                              double beta, const double *w1)
 {
+    PDL_ENTRY();
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrows) return;
     double wr = beta * w1[r];
@@ -724,12 +747,13 @@ __global__ void k_csr_axpy_t(int nrows, const int *rowptr, const int *col, const
 
 void csr_axpy_transposed(Ctx &c, const Csr &A, double *dest, double beta, const double *w1)
 {
-    UG_LAUNCH(c, k_csr_axpy_t, div_up(A.nrows, NT), NT, 0, A.nrows, A.rowptr.p, A.col.p, A.val.p, dest, beta, w1);
+    UG_LAUNCH_PDL(c, k_csr_axpy_t, div_up(A.nrows, NT), NT, 0, A.nrows, A.rowptr.p, A.col.p, A.val.p, dest, beta, w1);
 }
 
 template <class TO, class TI>
 __global__ void k_convert(int n, const TI *in, TO *out)
 {
+    PDL_ENTRY();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = (TO)in[i];
 }
@@ -737,7 +761,7 @@ __global__ void k_convert(int n, const TI *in, TO *out)
 template <class TO, class TI>
 void convert(Ctx &c, int n, const TI *in, TO *out)
 {
-    UG_LAUNCH(c, (k_convert<TO, TI>), div_up(n, NT), NT, 0, n, in, out);
+    UG_LAUNCH_PDL(c, (k_convert<TO, TI>), div_up(n, NT), NT, 0, n, in, out);
 }
 template void convert<float, double>(Ctx &, int, const double *, float *);
 template void convert<double, float>(Ctx &, int, const float *, double *);
