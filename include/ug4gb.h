@@ -119,6 +119,18 @@ UG4GB_API int ug4gb_vector_dot(const ug4gb_vector *a, const ug4gb_vector *b, dou
 UG4GB_API int ug4gb_vector_scale_add(ug4gb_vector *dest, double alpha, const ug4gb_vector *a, double beta,
                            const ug4gb_vector *b);
 UG4GB_API void ug4gb_vector_destroy(ug4gb_vector *v);
+/* (a, b) of two FP64 device arrays of the current device, for callers that
+   may not allocate device memory (no context needed; nothing is allocated,
+   not even on first use).  Has no counterpart in the reference.  The result
+   goes to *result, a device pointer, in stream order on `stream`; nothing is
+   synchronised.  Reduction scratch is one static array of the library per
+   device, so n <= UG4GB_DOT_NOALLOC_MAX_N (else UG4GB_ERR_INVALID), and calls
+   that overlap in time on one device race on it: order them on one stream.
+   The first call on a device sets the scratch up; make it before any stream
+   capture.  On failure a message goes to err (may be NULL). */
+#define UG4GB_DOT_NOALLOC_MAX_N 67108864
+UG4GB_API int ug4gb_vector_dot_noalloc(const double *a, const double *b, int64_t n, double *result, void *stream,
+                                       char *err, int err_capacity);
 
 /* ------------------------------------------------------------ matrices -- */
 /* Replaces ug::SparseMatrix<double> (lib_algebra/cpu_algebra/sparsematrix.h:98)

@@ -64,6 +64,7 @@ _SIGS = {
     "ug4gb_vector_dot": (I, [P, P, PD]),
     "ug4gb_vector_scale_add": (I, [P, D, P, D, P]),
     "ug4gb_vector_destroy": (None, [P]),
+    "ug4gb_vector_dot_noalloc": (I, [P, P, I64, P, P, C.c_char_p, I]),
     "ug4gb_matrix_create": (I, [P, PP]),
     "ug4gb_matrix_set_csr": (I, [P, I, I, I64, P, P, P]),
     "ug4gb_matrix_info": (I, [P, PI, PI, PI64]),
