@@ -275,6 +275,11 @@ def run_ours(args, rank, world, local_rank):
                  "kernel_profile": profile_summary(prof_m)}
         del pm
 
+    target = adj = None
+    if not args.no_extras:
+        target = run_target(args, ctx, timed, world, hbm)
+        adj = run_adjoint_grad(args, ctx, timed)
+
     # ---- assembly throughput (top level, FP64 FV1 + CRS values + rhs)
     asm = None
     if not args.no_extras:
@@ -312,11 +317,75 @@ def run_ours(args, rank, world, local_rank):
                            "bytes_per_iteration": it_bytes},
         "kernel_profile": profile_summary(prof),
         "mixed": mixed,
+        "variable_coefficient_tets": target,
+        "adjoint_gradient": adj,
         "assembly": asm,
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
     return line
+
+
+def run_target(args, ctx, timed, world, hbm):
+    """3D variable-coefficient diffusion on Kuhn tetrahedra (4^3 hexes x 6 tets,
+    refined 5 times, K = exp(2 g), g a 64-mode Gaussian field): FP64 GMG-PCG
+    against FP32-GMG-in-FP64-CG, both to 1e-10."""
+    from ugcore_gb300 import problems
+    out = {"workload": "3D variable-coefficient diffusion, tets (4^3 hexes x 6, refined 5x), K=exp(2g), "
+                       "GMG V(2,2) Jacobi(0.6)-PCG to 1e-10"}
+    xs, res = {}, {}
+    for prec in ("fp64", "mixed"):
+        p = problems.Problem(ctx, problems.config("c2", precision=prec))
+        for _ in range(args.warmup):
+            p.solve()
+        ms = max_over_ranks(timed(p.solve, args.steps), world)
+        st = p.solve()
+        sizes = level_sizes(p)
+        sv = 8 if prec == "fp64" else 4
+        gbs = iteration_bytes(sizes, sv) * st["steps"] / (ms * 1e-3) / 1e9
+        xs[prec] = p.x.numpy()
+        res[prec] = {"ms_per_step": ms, "dofs_per_s": world * p.n / (ms * 1e-3), "pcg_steps": st["steps"],
+                     "rel_residual": st["defect"] / st["initial_defect"],
+                     "solve_gbs": gbs, "solve_frac_of_measured_hbm": gbs / hbm}
+        out["dofs"], out["nnz"] = p.n, sizes[-1]["nnz"]
+        del p
+    out.update(res)
+    out["mixed_speedup_vs_fp64"] = res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"]
+    out["max_rel_diff_mixed_vs_fp64"] = float(abs(xs["mixed"] - xs["fp64"]).max() / abs(xs["fp64"]).max())
+    return out
+
+
+def run_adjoint_grad(args, ctx, timed):
+    """time of one full gradient dJ/dm (forward assemble + solve, transposed
+    GMG-PCG solve, element adjoint kernel) through the autograd Function, on
+    the 257x257 quadrilateral inverse problem, FP64 and mixed."""
+    import torch
+    from ugcore_gb300 import adjoint, problems
+    out = {"workload": "2D inverse problem 257x257 quads, J = 0.5||u(m) - u_obs||^2, dJ/dm per element"}
+    for prec in ("fp64", "mixed"):
+        cfg = problems.config("c3", precision=prec)
+        prob = adjoint.DifferentiableProblem(ctx, cfg)
+        m = torch.tensor(prob.m_top, dtype=torch.float64, device="cuda")
+        f = torch.ones(prob.n, dtype=torch.float64, device="cuda")
+        u_obs = torch.zeros(prob.n, dtype=torch.float64, device="cuda")
+
+        def grad():
+            mm = m.clone().requires_grad_(True)
+            u = adjoint.fv1_solve(mm, f, prob)
+            (0.5 * ((u - u_obs) ** 2).sum()).backward()
+            return mm.grad
+
+        for _ in range(args.warmup):
+            grad()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            grad()
+        torch.cuda.synchronize()
+        out[prec + "_ms"] = (time.perf_counter() - t0) * 1e3 / args.steps
+        out["dofs"], out["elements"] = prob.n, prob.num_elements
+        del prob
+    return out
 
 
 def cpu_baseline_sample():

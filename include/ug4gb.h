@@ -80,6 +80,11 @@ UG4GB_API int64_t ug4gb_kernel_launches(const ug4gb_ctx *ctx);
 #define UG4GB_FORMAT_AUTO 0
 #define UG4GB_FORMAT_SELL 1
 UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
+/* performance switches (value 0 or 1) that leave every result bit-identical.
+   UG4GB_TUNE_PDL: programmatic dependent launch of the solve-path kernels,
+   each kernel scheduled while its predecessor still runs (default 1). */
+#define UG4GB_TUNE_PDL 1
+UG4GB_API int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value);
 /* per-launch CUDA-event timing of every kernel until profile_end, which
    writes "tag|kernel<TAB>launches<TAB>total_ms" lines into buf.  While it is
    on, solvers launch kernels directly instead of replaying CUDA graphs.

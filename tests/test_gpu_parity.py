@@ -161,9 +161,12 @@ def test_bitwise_reproducible(ctx, name, over):
 
 
 @pytest.mark.parametrize("name,over", [("c0", dict(nref=4)), ("c1", dict(nref=3)), ("c2", dict(nref=2)),
-                                       ("c4", dict(nref=2)), ("c1", dict(nref=3, smoother="mcgs", damp=1.0))])
+                                       ("c4", dict(nref=2)), ("c1", dict(nref=3, smoother="mcgs", damp=1.0)),
+                                       ("c1", dict(nref=6, precision="mixed")), ("c2", dict(nref=5))])
 def test_sell_and_diagonal_layouts_agree(ctx, name, over):
-    """the automatic diagonal layout and SELL-32 give the same solve"""
+    """the automatic diagonal layout and SELL-32 give the same solve (the
+    full-size mixed cases run the 4-rows-per-thread FP32 smoother on the top
+    level)"""
     import ugcore_gb300 as ug
     from ugcore_gb300 import problems
     cfg = problems.config(name, **over)
@@ -176,6 +179,23 @@ def test_sell_and_diagonal_layouts_agree(ctx, name, over):
     x1, x2 = p1.x.numpy(), p2.x.numpy()
     tol = 1e-13 if cfg["precision"] == "fp64" else 1e-7
     assert np.abs(x1 - x2).max() <= tol * np.abs(x2).max()
+
+
+@pytest.mark.parametrize("name,over", [("c1", dict(nref=4)), ("c2", dict(nref=3, precision="mixed")),
+                                       ("c4", dict(nref=3))])
+def test_programmatic_launch_is_bit_identical(ctx, name, over):
+    """programmatic dependent launch changes scheduling only: the solve with
+    it and without it is bit for bit the same"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    cfg = problems.config(name, **over)
+    c2 = ug.Context(0)
+    c2.set_tuning(pdl=False)
+    p1 = problems.Problem(ctx, cfg)
+    p2 = problems.Problem(c2, cfg)
+    s1, s2 = p1.solve(), p2.solve()
+    assert s1["steps"] == s2["steps"]
+    assert np.array_equal(p1.x.numpy(), p2.x.numpy())
 
 
 def test_edge_cases(ctx):

@@ -16,6 +16,7 @@ SMOOTHER_JACOBI, SMOOTHER_MCGS = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_CG, SOLVER_BICGSTAB = 0, 1
 UPWIND_NONE, UPWIND_FULL = 0, 1
+TUNE_PDL = 1
 
 _ERRNAMES = {ERR_INVALID: "invalid argument", ERR_CUDA: "CUDA error", ERR_NOMEM: "out of device memory",
              ERR_SINGULAR: "singular base matrix", ERR_NOT_CONVERGED: "not converged",
@@ -46,6 +47,7 @@ _SIGS = {
     "ug4gb_stream": (P, [P]),
     "ug4gb_kernel_launches": (I64, [P]),
     "ug4gb_set_operator_format": (I, [P, I]),
+    "ug4gb_set_tuning": (I, [P, I, I]),
     "ug4gb_profile_begin": (I, [P]),
     "ug4gb_profile_end": (I, [P, C.c_char_p, I]),
     "ug4gb_grid_create_structured": (I, [P, I, I, I, I, I, PP]),

@@ -75,6 +75,12 @@ class Context:
         """'auto' (diagonal layout for structured operators) or 'sell'."""
         check(lib().ug4gb_set_operator_format(self.h, {"auto": 0, "sell": 1}[fmt]), self.h)
 
+    def set_tuning(self, pdl=None):
+        """performance switches that leave results bit-identical:
+        programmatic dependent launch of the solve kernels."""
+        if pdl is not None:
+            check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_PDL, int(bool(pdl))), self.h)
+
     def profile_begin(self):
         check(lib().ug4gb_profile_begin(self.h), self.h)
 

@@ -150,6 +150,15 @@ int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format)
     return UG4GB_OK;
 }
 
+int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value)
+{
+    if (!ctx || (value != 0 && value != 1)) return UG4GB_ERR_INVALID;
+    switch (knob) {
+    case UG4GB_TUNE_PDL: ctx->c.pdl = value != 0; return UG4GB_OK;
+    default: ctx->c.err = "ug4gb_set_tuning: unknown knob"; return UG4GB_ERR_INVALID;
+    }
+}
+
 int ug4gb_profile_begin(ug4gb_ctx *ctx)
 {
     if (!ctx) return UG4GB_ERR_INVALID;

@@ -164,6 +164,7 @@ struct GmgT : GmgBase {
     DevBuf<double> Ainv;
     DevBuf<double> z64;          // mixed precision: FP64 copy of the top correction
     int nbase = 0;
+    bool top_converted = false;  // this apply: the FP32 top defect is already in dA of the top level
 
     int top() const override { return (int)lev.size() - 1; }
     bool is_fp32() const override { return sizeof(V) == 4; }
@@ -274,7 +275,7 @@ struct GmgT : GmgBase {
             if constexpr (sizeof(V) == sizeof(double)) {
                 top_in = (const V *)dtop;
             } else {
-                UG_LAUNCH_PDL(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
+                if (!top_converted) UG_LAUNCH_PDL(c, k_to_v<V>, div_up(L.n, 256), 256, 0, dtop, L.dA.p, L.n);
                 top_in = L.dA.p;
             }
         }
@@ -355,11 +356,17 @@ struct GmgT : GmgBase {
     }
 
     const double *apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
-                        int rho_kind, bool &rho_done) override
+                        int rho_kind, bool &rho_done, bool top_ready) override
     {
         rho_done = false;
+        top_converted = top_ready && sizeof(V) == 4;
         lmgc(c, top(), dtop, true, skip, r_rho, red, rho_kind, rho_done);
         return z64.p ? z64.p : (const double *)lev.back().sc.p;
+    }
+    float *top_defect_buffer() override
+    {
+        if constexpr (sizeof(V) == 4) return (float *)lev.back().dA.p;
+        return nullptr;
     }
 };
 

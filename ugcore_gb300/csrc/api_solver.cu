@@ -52,13 +52,19 @@ const double *precond(ug4gb_solver *s, const double *d, const double *r_rho, int
 {
     Ctx &c = s->ctx->c;
     RedArgs red = red_of(s);
-    const int *skip = &s->ks.p->done;
+    // Inside the CG loop body the preconditioner never runs after the check
+    // has ended (the loop condition is tested after cg_update), so only
+    // BiCGStab, whose check runs between its two half steps, needs the
+    // kernels to test the done flag.
+    const int *skip = s->kind == UG4GB_SOLVER_BICGSTAB ? &s->ks.p->done : nullptr;
     if (!s->pre) {
         if (r_rho) rho_dot<double>(c, s->n, d, r_rho, rho_kind, red);
         return d;
     }
     bool fused = false;
-    const double *z = s->pre->impl->apply(c, d, skip, r_rho, &red, rho_kind, fused);
+    // CG: d is r, whose FP32 copy krylov_start / cg_update already wrote
+    const bool ready = s->kind == UG4GB_SOLVER_CG && s->pre->impl->top_defect_buffer() != nullptr;
+    const double *z = s->pre->impl->apply(c, d, skip, r_rho, &red, rho_kind, fused, ready);
     if (r_rho && !fused) rho_dot<double>(c, s->n, z, r_rho, rho_kind, red);
     return z;
 }
@@ -70,7 +76,7 @@ void cg_iteration(ug4gb_solver *s, double *x, double *r, bool first)
     const double *z = precond(s, r, r, first ? 0 : 1);
     c.prof_tag = "K";
     cg_spmv_dot_t<double>(c, s->A->op, z, s->p.p, s->q.p, first ? 1 : 0, red);
-    cg_update(c, s->n, x, r, s->p.p, s->q.p, red);
+    cg_update(c, s->n, x, r, s->p.p, s->q.p, red, s->pre ? s->pre->impl->top_defect_buffer() : nullptr);
 }
 
 void bicg_iteration(ug4gb_solver *s, double *x, double *r)
@@ -177,7 +183,8 @@ void run(ug4gb_solver *s, double *x, double *r)
     RedArgs red = red_of(s);
     // prologue: r = b - A x, start the check; CG also does the first step
     c.prof_tag = "K";
-    krylov_start(c, s->A->op, x, r, red);
+    krylov_start(c, s->A->op, x, r, red,
+                 s->kind == UG4GB_SOLVER_CG && s->pre ? s->pre->impl->top_defect_buffer() : nullptr);
     if (s->kind == UG4GB_SOLVER_CG) cg_iteration(s, x, r, true);
     int done = 0;
     read_flags(s, &done);

@@ -16,6 +16,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -206,6 +207,7 @@ struct Offs {
 template <class T>
 struct Dia {
     int nrows = 0, ncols = 0, S = 0;
+    int ld = 0;       // stride between diagonals: nrows rounded up to 32 (128-byte aligned rows of values)
     Offs off{};
     DevBuf<T> val;
 };
@@ -219,7 +221,7 @@ struct OpMat {
     Dia<T> dia;
     int64_t stored_bytes() const
     {
-        if (kind == 1) return (int64_t)dia.S * dia.nrows * (int64_t)sizeof(T);
+        if (kind == 1) return (int64_t)dia.S * dia.ld * (int64_t)sizeof(T);
         return sell.stored * (int64_t)(sizeof(T) + sizeof(int)) + (int64_t)sell.nslices * 8;
     }
 };
@@ -247,6 +249,36 @@ __device__ __forceinline__ double warp_sum(double v)
 __device__ __forceinline__ double ld_stream(const double *p) { return __ldcs(p); }
 __device__ __forceinline__ float ld_stream(const float *p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int *p) { return __ldcs(p); }
+
+// W values of type T that fill 16 bytes, moved with one vector load/store
+template <class T, int W>
+struct alignas(16) Pack {
+    T v[W];
+};
+template <class T, int W>
+__device__ __forceinline__ Pack<T, W> ld_stream_pack(const T *p)
+{
+    static_assert(sizeof(T) * W == 16, "16-byte packs only");
+    Pack<T, W> r;
+    if constexpr (sizeof(T) == 4) {
+        float4 q = __ldcs(reinterpret_cast<const float4 *>(p));
+        r.v[0] = q.x, r.v[1] = q.y, r.v[2] = q.z, r.v[3] = q.w;
+    } else {
+        double2 q = __ldcs(reinterpret_cast<const double2 *>(p));
+        r.v[0] = q.x, r.v[1] = q.y;
+    }
+    return r;
+}
+template <class T, int W>
+__device__ __forceinline__ Pack<T, W> ld_pack(const T *p)
+{
+    return *reinterpret_cast<const Pack<T, W> *>(p);
+}
+template <class T, int W>
+__device__ __forceinline__ void st_pack(T *p, const Pack<T, W> &v)
+{
+    *reinterpret_cast<Pack<T, W> *>(p) = v;
+}
 
 // Deterministic grid-wide sum of NV values per thread.  Each block reduces
 // in a fixed tree, writes its partials, and the last block to finish sums

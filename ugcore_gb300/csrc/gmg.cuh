@@ -91,8 +91,12 @@ struct GmgBase {
     virtual void *sc_top() = 0;
     // z = M d_top (d_top FP64, device); returns z in FP64.  rho = (z, r_rho)
     // is fused into the last kernel when possible (rho_done tells).
+    // top_ready: the caller already wrote d_top in level precision into
+    // top_defect_buffer() (mixed precision), so no conversion pass is needed.
     virtual const double *apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
-                                int rho_kind, bool &rho_done) = 0;
+                                int rho_kind, bool &rho_done, bool top_ready = false) = 0;
+    // FP32 buffer a producer of d_top may fill (mixed precision), else null
+    virtual float *top_defect_buffer() = 0;
     virtual const Csr &P(int l) const = 0;
     virtual const Csr &R(int l) const = 0;
 };

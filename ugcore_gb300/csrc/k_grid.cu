@@ -481,12 +481,11 @@ bool csr_offsets(Ctx &c, const Csr &A, int max_s, std::vector<int> &offs)
 }
 
 template <class T>
-__global__ void k_dia_fill(const int *rowptr, const int *col, const double *val, int nrows, Offs off, int S,
+__global__ void k_dia_fill(const int *rowptr, const int *col, const double *val, int nrows, int ld, Offs off, int S,
                            const double *col_scale, T *dval)
 {
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrows) return;
-    for (int k = 0; k < S; ++k) dval[(size_t)k * nrows + r] = (T)0;
     for (int a = rowptr[r]; a < rowptr[r + 1]; ++a) {
         int o = col[a] - r;
         int k = 0;
@@ -494,7 +493,7 @@ __global__ void k_dia_fill(const int *rowptr, const int *col, const double *val,
         if (k == S) continue;   // cannot happen: offs holds every offset of A
         double v = val[a];
         if (col_scale) v *= col_scale[col[a]];
-        dval[(size_t)k * nrows + r] = (T)v;
+        dval[(size_t)k * ld + r] = (T)v;
     }
 }
 
@@ -506,9 +505,12 @@ void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs,
     D.ncols = A.ncols;
     D.S = (int)offs.size();
     for (int k = 0; k < kMaxDiag; ++k) D.off.o[k] = k < D.S ? offs[k] : 0;
-    D.val.alloc((size_t)D.S * D.nrows);
-    UG_LAUNCH(c, k_dia_fill<T>, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows, D.off, D.S,
-              col_scale, D.val.p);
+    D.ld = (A.nrows + 31) / 32 * 32;
+    D.val.alloc((size_t)D.S * D.ld);
+    // absent entries and the padding rows stay 0
+    UG_CUDA(cudaMemsetAsync(D.val.p, 0, D.val.bytes(), c.stream));
+    UG_LAUNCH(c, k_dia_fill<T>, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows, D.ld, D.off,
+              D.S, col_scale, D.val.p);
 }
 
 // the diagonal kernels are instantiated for S = 9, 15, 27 (2D quads, Kuhn

@@ -58,7 +58,8 @@ struct SellMV {
 
 template <class V, int S>
 struct DiaMV {
-    int n, ncols;
+    static constexpr int kS = S;
+    int n, ncols, ld;
     const V *__restrict__ val;
     Offs off;
     __device__ __forceinline__ int rows() const { return n; }
@@ -70,9 +71,37 @@ struct DiaMV {
         for (int k = 0; k < S; ++k) {
             int j = i + off.o[k];
             j = j < 0 ? 0 : (j >= ncols ? ncols - 1 : j);
-            acc += (ACC)ld_stream(val + (size_t)k * n + i) * (ACC)x[j];
+            acc += (ACC)ld_stream(val + (size_t)k * ld + i) * (ACC)x[j];
         }
         return acc;
+    }
+    // W consecutive rows i0..i0+W-1 (i0 % W == 0, all < n): one 16-byte
+    // value load per diagonal instead of W scalar ones
+    template <int W, class XT>
+    __device__ __forceinline__ void dot_w(const XT *__restrict__ x, int i0, V (&acc)[W]) const
+    {
+#pragma unroll
+        for (int e = 0; e < W; ++e) acc[e] = (V)0;
+        // diagonals in three batches: S/3 packs in flight per thread keeps
+        // the register count low enough for a full SM
+        constexpr int B = S / 3;
+        static_assert(B * 3 == S, "S must be a multiple of 3");
+#pragma unroll 1
+        for (int kb = 0; kb < S; kb += B) {
+            Pack<V, W> a[B];
+#pragma unroll
+            for (int k = 0; k < B; ++k) a[k] = ld_stream_pack<V, W>(val + (size_t)(kb + k) * ld + i0);
+#pragma unroll
+            for (int k = 0; k < B; ++k) {
+                const int j = i0 + off.o[kb + k];
+#pragma unroll
+                for (int e = 0; e < W; ++e) {
+                    int jj = j + e;
+                    jj = jj < 0 ? 0 : (jj >= ncols ? ncols - 1 : jj);
+                    acc[e] += a[k].v[e] * (V)x[jj];
+                }
+            }
+        }
     }
 };
 
@@ -86,9 +115,9 @@ void with_mv(const OpMat<V> &m, F &&f)
     }
     const Dia<V> &d = m.dia;
     switch (d.S) {
-    case 9: f(DiaMV<V, 9>{d.nrows, d.ncols, d.val.p, d.off}); break;
-    case 15: f(DiaMV<V, 15>{d.nrows, d.ncols, d.val.p, d.off}); break;
-    case 27: f(DiaMV<V, 27>{d.nrows, d.ncols, d.val.p, d.off}); break;
+    case 9: f(DiaMV<V, 9>{d.nrows, d.ncols, d.ld, d.val.p, d.off}); break;
+    case 15: f(DiaMV<V, 15>{d.nrows, d.ncols, d.ld, d.val.p, d.off}); break;
+    case 27: f(DiaMV<V, 27>{d.nrows, d.ncols, d.ld, d.val.p, d.off}); break;
     default: throw Error{UG4GB_ERR_INVALID, "diagonal operator with unsupported width"};
     }
 }
@@ -156,6 +185,102 @@ __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, c
     }
 }
 
+// The same step on the diagonal layout with W = 16/sizeof(V) consecutive rows
+// per thread: every value and row-vector access is one 16-byte load or
+// store (the gathered x stays scalar).  A tail of n % W rows is done by the
+// thread that owns the last, partial group.  Per row the arithmetic is that
+// of k_smooth.
+template <class V, int S, bool RHO>
+__global__ void __launch_bounds__(NT, 4) k_smooth_dia(DiaMV<V, S> A, const V *__restrict__ x, const V *__restrict__ dbase,
+                                                   const V *__restrict__ dinv, V *__restrict__ sc, V *__restrict__ dout,
+                                                   int sc_mode, const int *skip, const double *__restrict__ r_rho,
+                                                   RedArgs red, int rho_kind, double *__restrict__ z64)
+{
+    constexpr int W = 16 / sizeof(V);
+    PDL_ENTRY();
+    if (skip && *skip) return;
+    double rsum = 0.0;
+    const int n = A.rows(), ng = (n + W - 1) / W, stride = gridDim.x * NT;
+    const bool wide64 = (((uintptr_t)z64 | (uintptr_t)r_rho) & 15u) == 0;
+    for (int g = blockIdx.x * NT + threadIdx.x; g < ng; g += stride) {
+        const int r0 = g * W;
+        if (r0 + W <= n) {
+            V acc[W];
+            A.template dot_w<W>(x, r0, acc);
+            Pack<V, W> db = ld_pack<V, W>(dbase + r0), di = ld_pack<V, W>(dinv + r0), s, dn;
+            if (sc_mode != SC_SET_FROM_BASE) s = ld_pack<V, W>(sc + r0);
+#pragma unroll
+            for (int e = 0; e < W; ++e) {
+                dn.v[e] = db.v[e] - acc[e];
+                V t = di.v[e] * (sc_mode == SC_ADD_FROM_NEW ? dn.v[e] : db.v[e]);
+                s.v[e] = (sc_mode == SC_SET_FROM_BASE) ? t : s.v[e] + t;
+            }
+            if (dout) st_pack<V, W>(dout + r0, dn);
+            st_pack<V, W>(sc + r0, s);
+            if (RHO || z64) {
+                double s64[W];
+#pragma unroll
+                for (int e = 0; e < W; ++e) s64[e] = (double)s.v[e];
+                if constexpr (W % 2 == 0) {
+                    // FP64 side in 16-byte pairs when both arrays allow it
+                    if (wide64) {
+#pragma unroll
+                        for (int e = 0; e < W; e += 2) {
+                            if (z64) st_pack<double, 2>(z64 + r0 + e, Pack<double, 2>{{s64[e], s64[e + 1]}});
+                            if (RHO) {
+                                Pack<double, 2> rr = ld_pack<double, 2>(r_rho + r0 + e);
+                                rsum += s64[e] * rr.v[0];
+                                rsum += s64[e + 1] * rr.v[1];
+                            }
+                        }
+                        continue;
+                    }
+                }
+#pragma unroll
+                for (int e = 0; e < W; ++e) {
+                    if (z64) z64[r0 + e] = s64[e];
+                    if (RHO) rsum += s64[e] * r_rho[r0 + e];
+                }
+            }
+        } else {
+            for (int row = r0; row < n; ++row) {
+                V acc = A.template dot<V>(x, row);
+                V db = dbase[row];
+                V dn = db - acc;
+                if (dout) dout[row] = dn;
+                V t = dinv[row] * (sc_mode == SC_ADD_FROM_NEW ? dn : db);
+                V s = (sc_mode == SC_SET_FROM_BASE) ? t : sc[row] + t;
+                sc[row] = s;
+                if (RHO || z64) {
+                    const double s64 = (double)s;
+                    if (z64) z64[row] = s64;
+                    if (RHO) rsum += s64 * r_rho[row];
+                }
+            }
+        }
+    }
+    if (RHO) {
+        double v[1] = {rsum};
+        KScal *ks = red.ks;
+        grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) {
+            if (rho_kind == 0) {
+                ks->rho_old = tot[0];
+            } else {
+                ks->rho = tot[0];
+                ks->beta = tot[0] / ks->rho_old;
+                ks->rho_old = tot[0];
+            }
+        });
+    }
+}
+
+template <class MV>
+struct is_dia : std::false_type {};
+template <class V, int S>
+struct is_dia<DiaMV<V, S>> : std::true_type {};
+
+inline bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
 template <class V, class XT, class DT>
 void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout, int sc_mode,
                  const int *skip, const double *r_rho, RedArgs *red, int rho_kind, double *z64)
@@ -163,6 +288,28 @@ void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const
     const int g = row_grid(c, At.nrows);
     with_mv(At, [&](auto mv) {
         using MV = decltype(mv);
+        if constexpr (is_dia<MV>::value && std::is_same<XT, V>::value && std::is_same<DT, V>::value) {
+            // FP32 levels of at least three full waves of one-row threads:
+            // there the wider loads pay (8-9% per sweep on GB300).  FP64 sweeps
+            // are bound by the FP64 FMA rate and smaller levels by latency;
+            // there the one-row-per-thread kernel is as fast or faster.
+            const bool wide = sizeof(V) == 4 && At.nrows >= c.num_sms * 2048 * 3;
+            if (wide && aligned16(dbase) && aligned16(dinv) && aligned16(sc) && aligned16(dout)) {
+                constexpr int W = 16 / sizeof(V);
+                const int groups = (At.nrows + W - 1) / W;
+                int gv = (int)div_up(groups > 0 ? groups : 1, NT);
+                if (gv > kRedMaxBlocks) gv = kRedMaxBlocks;
+                if (r_rho) {
+                    UG_LAUNCH_PDL(c, (k_smooth_dia<V, MV::kS, true>), gv, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode,
+                                  skip, r_rho, *red, rho_kind, z64);
+                } else {
+                    RedArgs none{nullptr, nullptr, nullptr};
+                    UG_LAUNCH_PDL(c, (k_smooth_dia<V, MV::kS, false>), gv, NT, 0, mv, x, dbase, dinv, sc, dout,
+                                  sc_mode, skip, (const double *)nullptr, none, 0, z64);
+                }
+                return;
+            }
+        }
         if (r_rho) {
             UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, true>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
                       r_rho, *red, rho_kind, z64);
@@ -318,7 +465,7 @@ template void residual_update<float, double>(Ctx &, const OpMat<float> &, const 
 // r = b - A x (r holds b on entry); start the convergence check with |r|
 template <class MV>
 __global__ void __launch_bounds__(NT) k_krylov_start(MV A, const double *__restrict__ x, double *__restrict__ r,
-                                                     RedArgs red)
+                                                     float *__restrict__ r32, RedArgs red)
 {
     PDL_ENTRY();
     double sum = 0.0;
@@ -327,6 +474,7 @@ __global__ void __launch_bounds__(NT) k_krylov_start(MV A, const double *__restr
         double ax = A.template dot<double>(x, row);
         double rv = r[row] - ax;
         r[row] = rv;
+        if (r32) r32[row] = (float)rv;
         sum += rv * rv;
     }
     double v[1] = {sum};
@@ -344,10 +492,10 @@ __global__ void __launch_bounds__(NT) k_krylov_start(MV A, const double *__restr
     });
 }
 
-void krylov_start(Ctx &c, const OpMat<double> &A, const double *x, double *r, RedArgs red)
+void krylov_start(Ctx &c, const OpMat<double> &A, const double *x, double *r, RedArgs red, float *r32)
 {
     with_mv(A, [&](auto mv) {
-        UG_LAUNCH_PDL(c, k_krylov_start<decltype(mv)>, row_grid(c, A.nrows), NT, 0, mv, x, r, red);
+        UG_LAUNCH_PDL(c, k_krylov_start<decltype(mv)>, row_grid(c, A.nrows), NT, 0, mv, x, r, r32, red);
     });
 }
 
@@ -391,10 +539,53 @@ void cg_spmv_dot_t(Ctx &c, const OpMat<double> &A, const ZT *z, double *p, doubl
 template void cg_spmv_dot_t<double>(Ctx &, const OpMat<double> &, const double *, double *, double *, int, RedArgs);
 template void cg_spmv_dot_t<float>(Ctx &, const OpMat<double> &, const float *, double *, double *, int, RedArgs);
 
-// x += alpha p ; r -= alpha q ; |r| -> convergence check
+// x += alpha p ; r -= alpha q ; |r| -> convergence check; optionally
+// r32 = (float) r, the FP32 defect the mixed-precision multigrid starts from.
+// Two entries per thread with 16-byte accesses (all pointers 16-byte
+// aligned; the odd last entry alone).
 __global__ void __launch_bounds__(NT) k_cg_update(int n, double *__restrict__ x, double *__restrict__ r,
                                                   const double *__restrict__ p, const double *__restrict__ q,
-                                                  RedArgs red)
+                                                  float *__restrict__ r32, RedArgs red)
+{
+    PDL_ENTRY();
+    KScal *ks = red.ks;
+    if (ks->done) return;
+    const double alpha = ks->alpha;
+    double sum = 0.0;
+    const int stride = gridDim.x * NT, npair = (n + 1) / 2;
+    for (int k = blockIdx.x * NT + threadIdx.x; k < npair; k += stride) {
+        const int i = 2 * k;
+        if (i + 1 < n) {
+            Pack<double, 2> xv = ld_pack<double, 2>(x + i), pv = ld_pack<double, 2>(p + i);
+            Pack<double, 2> rv = ld_pack<double, 2>(r + i), qv = ld_pack<double, 2>(q + i);
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                xv.v[e] = xv.v[e] + alpha * pv.v[e];
+                rv.v[e] = rv.v[e] + (-alpha) * qv.v[e];
+                sum += rv.v[e] * rv.v[e];
+            }
+            st_pack<double, 2>(x + i, xv);
+            st_pack<double, 2>(r + i, rv);
+            if (r32) {
+                float2 f = make_float2((float)rv.v[0], (float)rv.v[1]);
+                *reinterpret_cast<float2 *>(r32 + i) = f;
+            }
+        } else {
+            x[i] = x[i] + alpha * p[i];
+            double rv = r[i] + (-alpha) * q[i];
+            r[i] = rv;
+            sum += rv * rv;
+            if (r32) r32[i] = (float)rv;
+        }
+    }
+    double v[1] = {sum};
+    grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) { conv_update(ks, sqrt(tot[0]), 1); });
+}
+
+// the same one entry per thread (pointers not 16-byte aligned)
+__global__ void __launch_bounds__(NT) k_cg_update1(int n, double *__restrict__ x, double *__restrict__ r,
+                                                   const double *__restrict__ p, const double *__restrict__ q,
+                                                   float *__restrict__ r32, RedArgs red)
 {
     PDL_ENTRY();
     KScal *ks = red.ks;
@@ -407,14 +598,20 @@ __global__ void __launch_bounds__(NT) k_cg_update(int n, double *__restrict__ x,
         double rv = r[i] + (-alpha) * q[i];
         r[i] = rv;
         sum += rv * rv;
+        if (r32) r32[i] = (float)rv;
     }
     double v[1] = {sum};
     grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) { conv_update(ks, sqrt(tot[0]), 1); });
 }
 
-void cg_update(Ctx &c, int n, double *x, double *r, const double *p, const double *q, RedArgs red)
+static inline bool al16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+void cg_update(Ctx &c, int n, double *x, double *r, const double *p, const double *q, RedArgs red, float *r32)
 {
-    UG_LAUNCH_PDL(c, k_cg_update, row_grid(c, n), NT, 0, n, x, r, p, q, red);
+    if (al16(x) && al16(r) && al16(p) && al16(q) && (!r32 || ((uintptr_t)r32 & 7u) == 0))
+        UG_LAUNCH_PDL(c, k_cg_update, row_grid(c, (n + 1) / 2), NT, 0, n, x, r, p, q, r32, red);
+    else
+        UG_LAUNCH_PDL(c, k_cg_update1, row_grid(c, n), NT, 0, n, x, r, p, q, r32, red);
 }
 
 // rho = (z, r) when the preconditioner could not fuse it (kind 0: first, 1: loop)

@@ -57,11 +57,14 @@ void residual_update(Ctx &c, const OpMat<V> &A, const V *t, const DT *dbase, V *
                      const int *skip);
 
 // ---- Krylov kernels (FP64 outer vectors; z may be FP32 in mixed mode) ----
-void krylov_start(Ctx &c, const OpMat<double> &A, const double *x, double *r, RedArgs red);
+// r -= A x, |r| starts the check; optionally r32 = (float) r
+void krylov_start(Ctx &c, const OpMat<double> &A, const double *x, double *r, RedArgs red, float *r32 = nullptr);
 // first: p = z, q = A z; else p = z + beta p, q = A z + beta q; lambda = (q,p), alpha = rho_old/lambda
 template <class ZT>
 void cg_spmv_dot_t(Ctx &c, const OpMat<double> &A, const ZT *z, double *p, double *q, int first, RedArgs red);
-void cg_update(Ctx &c, int n, double *x, double *r, const double *p, const double *q, RedArgs red);
+// x += alpha p, r -= alpha q, |r| -> check; optionally r32 = (float) r
+void cg_update(Ctx &c, int n, double *x, double *r, const double *p, const double *q, RedArgs red,
+               float *r32 = nullptr);
 // rho = (z, r); kind 0: rho_old = rho (first), 1: beta = rho/rho_old, rho_old = rho
 template <class ZT>
 void rho_dot(Ctx &c, int n, const ZT *z, const double *r, int kind, RedArgs red);

@@ -1,0 +1,52 @@
+"""Solve one named configuration on cuda:0 a few times and print the solver
+statistics as JSON, e.g. to profile one precision or layout in isolation:
+
+    python -m ugcore_gb300.run_case --config c2 --precision mixed --solves 2
+    python -m ugcore_gb300.run_case --config c1 --nref 5 --format sell
+
+Configurations: c0 2D Poisson 129^2 quads, c1 3D Poisson 129^3 hexes,
+c2 3D lognormal diffusion on Kuhn tets (129^3 vertices), c3 2D log-K field
+257^2 quads, c4 3D convection-diffusion 193^3 hexes (BiCGStab).
+"""
+import argparse
+import json
+import time
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="c1")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default=None)
+    ap.add_argument("--nref", type=int, default=None)
+    ap.add_argument("--smoother", choices=["jacobi", "mcgs"], default=None)
+    ap.add_argument("--format", choices=["auto", "sell"], default="auto")
+    ap.add_argument("--solves", type=int, default=1)
+    args = ap.parse_args()
+
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    over = {}
+    if args.precision:
+        over["precision"] = args.precision
+    if args.nref is not None:
+        over["nref"] = args.nref
+    if args.smoother:
+        over["smoother"] = args.smoother
+    ctx = ug.Context(0)
+    ctx.set_operator_format(args.format)
+    t0 = time.perf_counter()
+    p = problems.Problem(ctx, problems.config(args.config, **over))
+    ctx.synchronize()
+    setup = time.perf_counter() - t0
+    out = []
+    for _ in range(args.solves):
+        t0 = time.perf_counter()
+        st = p.solve()
+        ctx.synchronize()
+        out.append({"ms": (time.perf_counter() - t0) * 1e3, "steps": st["steps"],
+                    "rel_residual": st["defect"] / st["initial_defect"]})
+    print(json.dumps({"config": args.config, "dofs": p.n, "setup_s": setup, "solves": out}))
+
+
+if __name__ == "__main__":
+    main()
