@@ -256,6 +256,7 @@ struct GmgT : GmgBase {
         copy_in(c, Ainv.p, inv.data(), sizeof(double) * inv.size());
         UG_CUDA(cudaStreamSynchronize(c.stream));
         nbase = n;
+        base_solve_prepare<V>(n);
     }
 
     // ------------------------------------------------------------ cycle --

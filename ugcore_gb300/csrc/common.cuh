@@ -136,6 +136,11 @@ __device__ __forceinline__ void pdl_entry()
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 #define PDL_ENTRY() ::ug4gb::pdl_entry()
+// The two halves, for kernels that first load data no kernel of the solve
+// writes (operator values, Jacobi factors): those loads overlap the
+// predecessor's tail instead of following it.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 #define UG_LAUNCH_PDL(ctx, kernel, grid, block, shmem, ...)                                        \
     do {                                                                                           \

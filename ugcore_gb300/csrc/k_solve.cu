@@ -38,8 +38,41 @@ int row_grid(const Ctx &c, int nrows)
 // ------------------------------------------------------------ views ------
 template <class V>
 struct SellMV {
+    static constexpr int kCache = 8;   // entries of a row loaded ahead (the rest after the wait)
     SellView<V> s;
+    struct Cache {
+        int base, w;
+        int col[kCache];
+        V val[kCache];
+    };
     __device__ __forceinline__ int rows() const { return s.nrows; }
+    __device__ __forceinline__ void prefetch(int row, Cache &c) const
+    {
+        const int sl = row >> 5, lane = row & 31;
+        c.base = __ldg(s.sptr + sl) + lane;
+        c.w = __ldg(s.swidth + sl);
+#pragma unroll
+        for (int k = 0; k < kCache; ++k) {
+            if (k < c.w) {
+                c.col[k] = __ldg(s.col + c.base + k * kSliceH);
+                c.val[k] = __ldg(s.val + c.base + k * kSliceH);
+            }
+        }
+    }
+    // dot with a prefetched row; same order of operations as dot
+    template <class ACC, class XT>
+    __device__ __forceinline__ ACC dot_cached(const XT *__restrict__ x, int, const Cache &c) const
+    {
+        ACC acc = (ACC)0;
+#pragma unroll
+        for (int k = 0; k < kCache; ++k)
+            if (k < c.w) acc += (ACC)c.val[k] * (ACC)x[c.col[k]];
+        for (int k = kCache; k < c.w; ++k) {
+            const int idx = c.base + k * kSliceH;
+            acc += (ACC)ld_stream(s.val + idx) * (ACC)x[ld_stream(s.col + idx)];
+        }
+        return acc;
+    }
     template <class ACC, class XT>
     __device__ __forceinline__ ACC dot(const XT *__restrict__ x, int row) const
     {
@@ -62,7 +95,27 @@ struct DiaMV {
     int n, ncols, ld;
     const V *__restrict__ val;
     Offs off;
+    struct Cache {
+        V a[S];
+    };
     __device__ __forceinline__ int rows() const { return n; }
+    __device__ __forceinline__ void prefetch(int i, Cache &c) const
+    {
+#pragma unroll
+        for (int k = 0; k < S; ++k) c.a[k] = ld_stream(val + (size_t)k * ld + i);
+    }
+    template <class ACC, class XT>
+    __device__ __forceinline__ ACC dot_cached(const XT *__restrict__ x, int i, const Cache &c) const
+    {
+        ACC acc = (ACC)0;
+#pragma unroll
+        for (int k = 0; k < S; ++k) {
+            int j = i + off.o[k];
+            j = j < 0 ? 0 : (j >= ncols ? ncols - 1 : j);
+            acc += (ACC)c.a[k] * (ACC)x[j];
+        }
+        return acc;
+    }
     template <class ACC, class XT>
     __device__ __forceinline__ ACC dot(const XT *__restrict__ x, int i) const
     {
@@ -152,16 +205,26 @@ __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, c
                                                int sc_mode, const int *skip, const double *__restrict__ r_rho,
                                                RedArgs red, int rho_kind, double *__restrict__ z64)
 {
-    PDL_ENTRY();
+    // this thread's first row of the operator and its Jacobi factor are
+    // loaded before waiting for the predecessor (no solve kernel writes them)
+    pdl_trigger();
+    const int stride = gridDim.x * NT, n = A.rows(), row0 = blockIdx.x * NT + threadIdx.x;
+    typename MV::Cache cache;
+    V dinv0 = (V)0;
+    if (row0 < n) {
+        A.prefetch(row0, cache);
+        dinv0 = dinv[row0];
+    }
+    pdl_wait();
     if (skip && *skip) return;
     double rsum = 0.0;
-    const int stride = gridDim.x * NT, n = A.rows();
-    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
-        V acc = A.template dot<V>(x, row);
+    for (int row = row0; row < n; row += stride) {
+        const bool first = (row == row0);
+        V acc = first ? A.template dot_cached<V>(x, row, cache) : A.template dot<V>(x, row);
         V db = (V)dbase[row];
         V dn = db - acc;
         if (dout) dout[row] = dn;
-        V t = dinv[row] * (sc_mode == SC_ADD_FROM_NEW ? dn : db);
+        V t = (first ? dinv0 : dinv[row]) * (sc_mode == SC_ADD_FROM_NEW ? dn : db);
         V s = (sc_mode == SC_SET_FROM_BASE) ? t : sc[row] + t;
         sc[row] = s;
         if (RHO || z64) {
@@ -331,10 +394,14 @@ INST_SMOOTH(float, float, float)
 template <class MV, class V>
 __global__ void __launch_bounds__(NT) k_restrict(MV R, const V *__restrict__ d, V *__restrict__ dc, const int *skip)
 {
-    PDL_ENTRY();
+    pdl_trigger();
+    const int stride = gridDim.x * NT, n = R.rows(), row0 = blockIdx.x * NT + threadIdx.x;
+    typename MV::Cache cache;
+    if (row0 < n) R.prefetch(row0, cache);
+    pdl_wait();
     if (skip && *skip) return;
-    const int stride = gridDim.x * NT, n = R.rows();
-    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) dc[row] = R.template dot<V>(d, row);
+    for (int row = row0; row < n; row += stride)
+        dc[row] = (row == row0) ? R.template dot_cached<V>(d, row, cache) : R.template dot<V>(d, row);
 }
 
 template <class V>
@@ -349,13 +416,21 @@ template <class MV, class V>
 __global__ void __launch_bounds__(NT) k_prolong(MV P, const V *__restrict__ scc, V *__restrict__ sc,
                                                 const V *__restrict__ dfac, V *__restrict__ w, const int *skip)
 {
-    PDL_ENTRY();
+    pdl_trigger();
+    const int stride = gridDim.x * NT, n = P.rows(), row0 = blockIdx.x * NT + threadIdx.x;
+    typename MV::Cache cache;
+    V dfac0 = (V)0;
+    if (row0 < n) {
+        P.prefetch(row0, cache);
+        if (w) dfac0 = dfac[row0];
+    }
+    pdl_wait();
     if (skip && *skip) return;
-    const int stride = gridDim.x * NT, n = P.rows();
-    for (int row = blockIdx.x * NT + threadIdx.x; row < n; row += stride) {
-        V t = P.template dot<V>(scc, row);
+    for (int row = row0; row < n; row += stride) {
+        const bool first = (row == row0);
+        V t = first ? P.template dot_cached<V>(scc, row, cache) : P.template dot<V>(scc, row);
         sc[row] += t;
-        if (w) w[row] = t * dfac[row];
+        if (w) w[row] = t * (first ? dfac0 : dfac[row]);
     }
 }
 
@@ -368,27 +443,55 @@ void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac
 }
 
 // dense base solve with the LU-factored inverse (one block, FP64)
+// Ainv is staged in shared memory before the wait when it fits (staged != 0)
 template <class V>
 __global__ void k_base_solve(const double *__restrict__ Ainv, int n, const V *__restrict__ d, V *__restrict__ sc,
-                             const int *skip)
+                             const int *skip, int staged)
 {
-    PDL_ENTRY();
     extern __shared__ double dsh[];
+    double *ash = dsh + n;
+    pdl_trigger();
+    if (staged)
+        for (int q = threadIdx.x; q < n * n; q += blockDim.x) ash[q] = Ainv[q];
+    pdl_wait();
     if (skip && *skip) return;
     for (int j = threadIdx.x; j < n; j += blockDim.x) dsh[j] = (double)d[j];
     __syncthreads();
+    const double *M = staged ? ash : Ainv;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
         double s = 0.0;
-        for (int j = 0; j < n; ++j) s += Ainv[(size_t)i * n + j] * dsh[j];
+        for (int j = 0; j < n; ++j) s += M[(size_t)i * n + j] * dsh[j];
         sc[i] = (V)s;
     }
+}
+
+constexpr size_t kBaseStageMax = 160 * 1024;
+
+static size_t base_smem(int n, int &staged)
+{
+    const size_t full = ((size_t)n * n + n) * sizeof(double);
+    staged = full <= kBaseStageMax ? 1 : 0;
+    return staged ? full : (size_t)n * sizeof(double);
+}
+
+template <class V>
+void base_solve_prepare(int n)
+{
+    int staged = 0;
+    const size_t shm = base_smem(n, staged);
+    if (shm > 48 * 1024)
+        UG_CUDA(cudaFuncSetAttribute(k_base_solve<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
 }
 
 template <class V>
 void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip)
 {
-    UG_LAUNCH_PDL(c, k_base_solve<V>, 1, NT, (size_t)n * sizeof(double), Ainv, n, d, sc, skip);
+    int staged = 0;
+    const size_t shm = base_smem(n, staged);
+    UG_LAUNCH_PDL(c, k_base_solve<V>, 1, NT, shm, Ainv, n, d, sc, skip, staged);
 }
+template void base_solve_prepare<double>(int);
+template void base_solve_prepare<float>(int);
 
 // multicolour Gauss-Seidel: rows of one colour, t_i = relax (d_i - (A t)_i) / a_ii
 // (t_i is still 0 when its colour is processed)

@@ -48,6 +48,9 @@ template <class V>
 void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip);
 template <class V>
 void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip);
+// once per base size, outside stream capture: allows the shared-memory copy of Ainv
+template <class V>
+void base_solve_prepare(int n);
 template <class V>
 void mcgs_colour(Ctx &c, const OpMat<V> &A, const int *rows, int nrows_c, const V *dinv_relax, const V *d, V *t,
                  const int *skip);
