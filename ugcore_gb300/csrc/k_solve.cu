@@ -199,27 +199,33 @@ __device__ __forceinline__ void conv_update(KScal *ks, double d, int done_value)
 }
 
 // ------------------------------------------------------- smoothing step --
-template <class MV, class V, class XT, class DT, bool RHO>
+// PF (levels of at most one wave of rows, where latency rules): this
+// thread's first row of the operator and its Jacobi factor are loaded
+// before waiting for the predecessor (no solve kernel writes them).  Large
+// levels skip it: the cached row would cost registers, hence occupancy.
+template <class MV, class V, class XT, class DT, bool RHO, bool PF>
 __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, const DT *__restrict__ dbase,
                                                const V *__restrict__ dinv, V *__restrict__ sc, V *__restrict__ dout,
                                                int sc_mode, const int *skip, const double *__restrict__ r_rho,
                                                RedArgs red, int rho_kind, double *__restrict__ z64)
 {
-    // this thread's first row of the operator and its Jacobi factor are
-    // loaded before waiting for the predecessor (no solve kernel writes them)
-    pdl_trigger();
     const int stride = gridDim.x * NT, n = A.rows(), row0 = blockIdx.x * NT + threadIdx.x;
     typename MV::Cache cache;
     V dinv0 = (V)0;
-    if (row0 < n) {
-        A.prefetch(row0, cache);
-        dinv0 = dinv[row0];
+    if constexpr (PF) {
+        pdl_trigger();
+        if (row0 < n) {
+            A.prefetch(row0, cache);
+            dinv0 = dinv[row0];
+        }
+        pdl_wait();
+    } else {
+        PDL_ENTRY();
     }
-    pdl_wait();
     if (skip && *skip) return;
     double rsum = 0.0;
     for (int row = row0; row < n; row += stride) {
-        const bool first = (row == row0);
+        const bool first = PF && (row == row0);
         V acc = first ? A.template dot_cached<V>(x, row, cache) : A.template dot<V>(x, row);
         V db = (V)dbase[row];
         V dn = db - acc;
@@ -373,13 +379,20 @@ void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const
                 return;
             }
         }
-        if (r_rho) {
-            UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, true>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
-                      r_rho, *red, rho_kind, z64);
+        const bool pf = At.nrows <= c.num_sms * NT;
+        RedArgs none{nullptr, nullptr, nullptr};
+        if (r_rho && pf) {
+            UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, true, true>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode,
+                          skip, r_rho, *red, rho_kind, z64);
+        } else if (r_rho) {
+            UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, true, false>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode,
+                          skip, r_rho, *red, rho_kind, z64);
+        } else if (pf) {
+            UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, false, true>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode,
+                          skip, (const double *)nullptr, none, 0, z64);
         } else {
-            RedArgs none{nullptr, nullptr, nullptr};
-            UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, false>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode, skip,
-                      (const double *)nullptr, none, 0, z64);
+            UG_LAUNCH_PDL(c, (k_smooth<MV, V, XT, DT, false, false>), g, NT, 0, mv, x, dbase, dinv, sc, dout, sc_mode,
+                          skip, (const double *)nullptr, none, 0, z64);
         }
     });
 }
@@ -391,43 +404,54 @@ INST_SMOOTH(double, double, double)
 INST_SMOOTH(float, float, float)
 
 // --------------------------------------------------------- transfers -----
-template <class MV, class V>
+template <class MV, class V, bool PF>
 __global__ void __launch_bounds__(NT) k_restrict(MV R, const V *__restrict__ d, V *__restrict__ dc, const int *skip)
 {
-    pdl_trigger();
     const int stride = gridDim.x * NT, n = R.rows(), row0 = blockIdx.x * NT + threadIdx.x;
     typename MV::Cache cache;
-    if (row0 < n) R.prefetch(row0, cache);
-    pdl_wait();
+    if constexpr (PF) {
+        pdl_trigger();
+        if (row0 < n) R.prefetch(row0, cache);
+        pdl_wait();
+    } else {
+        PDL_ENTRY();
+    }
     if (skip && *skip) return;
     for (int row = row0; row < n; row += stride)
-        dc[row] = (row == row0) ? R.template dot_cached<V>(d, row, cache) : R.template dot<V>(d, row);
+        dc[row] = (PF && row == row0) ? R.template dot_cached<V>(d, row, cache) : R.template dot<V>(d, row);
 }
 
 template <class V>
 void restrict_apply(Ctx &c, const OpMat<V> &R, const V *d, V *dc, const int *skip)
 {
     with_mv(R, [&](auto mv) {
-        UG_LAUNCH_PDL(c, (k_restrict<decltype(mv), V>), row_grid(c, R.nrows), NT, 0, mv, d, dc, skip);
+        if (R.nrows <= c.num_sms * NT)
+            UG_LAUNCH_PDL(c, (k_restrict<decltype(mv), V, true>), row_grid(c, R.nrows), NT, 0, mv, d, dc, skip);
+        else
+            UG_LAUNCH_PDL(c, (k_restrict<decltype(mv), V, false>), row_grid(c, R.nrows), NT, 0, mv, d, dc, skip);
     });
 }
 
-template <class MV, class V>
+template <class MV, class V, bool PF>
 __global__ void __launch_bounds__(NT) k_prolong(MV P, const V *__restrict__ scc, V *__restrict__ sc,
                                                 const V *__restrict__ dfac, V *__restrict__ w, const int *skip)
 {
-    pdl_trigger();
     const int stride = gridDim.x * NT, n = P.rows(), row0 = blockIdx.x * NT + threadIdx.x;
     typename MV::Cache cache;
     V dfac0 = (V)0;
-    if (row0 < n) {
-        P.prefetch(row0, cache);
-        if (w) dfac0 = dfac[row0];
+    if constexpr (PF) {
+        pdl_trigger();
+        if (row0 < n) {
+            P.prefetch(row0, cache);
+            if (w) dfac0 = dfac[row0];
+        }
+        pdl_wait();
+    } else {
+        PDL_ENTRY();
     }
-    pdl_wait();
     if (skip && *skip) return;
     for (int row = row0; row < n; row += stride) {
-        const bool first = (row == row0);
+        const bool first = PF && (row == row0);
         V t = first ? P.template dot_cached<V>(scc, row, cache) : P.template dot<V>(scc, row);
         sc[row] += t;
         if (w) w[row] = t * (first ? dfac0 : dfac[row]);
@@ -438,7 +462,12 @@ template <class V>
 void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip)
 {
     with_mv(P, [&](auto mv) {
-        UG_LAUNCH_PDL(c, (k_prolong<decltype(mv), V>), row_grid(c, P.nrows), NT, 0, mv, scc, sc, dfac, w, skip);
+        if (P.nrows <= c.num_sms * NT)
+            UG_LAUNCH_PDL(c, (k_prolong<decltype(mv), V, true>), row_grid(c, P.nrows), NT, 0, mv, scc, sc, dfac, w,
+                          skip);
+        else
+            UG_LAUNCH_PDL(c, (k_prolong<decltype(mv), V, false>), row_grid(c, P.nrows), NT, 0, mv, scc, sc, dfac, w,
+                          skip);
     });
 }
 
