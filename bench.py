@@ -131,14 +131,16 @@ def smooth_bytes(sz, sv, top):
 
 
 def iteration_bytes(sizes, sv):
-    """algorithmic bytes of one PCG iteration (V(2,2) cycle + CG kernels)."""
+    """algorithmic bytes of one PCG iteration (V(2,2) cycle + CG kernels).
+    The transfers of the structured hierarchy are applied from grid indices
+    (no stored P or R): vectors only."""
     L = len(sizes) - 1
     tot = 0
     for l in range(1, L + 1):
         s, c = sizes[l], sizes[l - 1]
         tot += smooth_bytes(s, sv, l == L)
-        tot += s["nR"] * (sv + 4) + 8 * ((c["N"] + 31) // 32) + s["N"] * sv + c["N"] * sv   # restrict
-        tot += s["nP"] * (sv + 4) + 8 * s["ns"] + c["N"] * sv + s["N"] * (2 * sv + sv + sv)  # prolong
+        tot += s["N"] * sv + c["N"] * sv                       # restrict: d read, coarse d written
+        tot += c["N"] * sv + s["N"] * (2 * sv + sv + sv)       # prolong: coarse sc, sc r/w, dfac, w
     b = sizes[0]["N"]
     tot += b * b * 8 + 2 * b * sv                                  # dense base solve
     top = sizes[L]

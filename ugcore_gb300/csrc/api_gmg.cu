@@ -235,6 +235,10 @@ struct GmgT : GmgBase {
                   F.R.col.p, F.R.val.p);
         op_from_csr<V>(c, F.P, F.Ps, nullptr, false);
         op_from_csr<V>(c, F.R, F.Rs, nullptr, false);
+        // the structured hierarchy's P and R need no stored matrix (AUTO
+        // format); the assembled CSR stays for export and the SELL format
+        F.grid_transfer = c.allow_dia;
+        F.gp = GridPair{Gf.nx, Gf.ny, Gf.nz, Gc.nx, Gc.ny, Gc.nz, Gf.dim, Gf.elem_type == UG4GB_TET ? 1 : 0};
         UG_CUDA(cudaStreamSynchronize(c.stream));
     }
 
@@ -303,7 +307,8 @@ struct GmgT : GmgBase {
         }
         const V *dpre = cur;
         // ---- restriction
-        restrict_apply<V>(c, L.Rs, dpre, C.dA.p, skip);
+        if (L.grid_transfer) restrict_grid<V>(c, L.gp, dpre, C.dA.p, skip);
+        else restrict_apply<V>(c, L.Rs, dpre, C.dA.p, skip);
         C.dcur = C.dA.p;
         // ---- coarse correction
         if (l - 1 == base) {
@@ -317,7 +322,8 @@ struct GmgT : GmgBase {
         }
         c.prof_tag = "L" + std::to_string(l);
         // ---- prolongation + post-smoothing
-        prolong_apply<V>(c, L.Ps, C.sc.p, L.sc.p, L.dfac.p, nu2 > 0 ? L.w.p : (V *)nullptr, skip);
+        if (L.grid_transfer) prolong_grid<V>(c, L.gp, C.sc.p, L.sc.p, L.dfac.p, nu2 > 0 ? L.w.p : (V *)nullptr, skip);
+        else prolong_apply<V>(c, L.Ps, C.sc.p, L.sc.p, L.dfac.p, nu2 > 0 ? L.w.p : (V *)nullptr, skip);
         const V *dbase = dpre;
         bool z_written = false;
         if (smoother == UG4GB_SMOOTHER_JACOBI) {

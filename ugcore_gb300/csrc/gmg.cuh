@@ -78,6 +78,8 @@ struct GLevel {
     DevBuf<V> dinv, dfac;        // Jacobi: dinv = 1/(a_ii/damp), dfac = a_ii/damp; MCGS: relax/a_ii, 1
     Csr P, R;                    // P: this x coarse, R: coarse x this (FP64, exportable)
     OpMat<V> Ps, Rs;
+    bool grid_transfer = false;  // apply P and R from grid indices (structured hierarchy)
+    GridPair gp{};
     DevBuf<V> sc, dA, dB, w, t;
     V *dcur = nullptr;
     std::vector<DevBuf<int>> crow;   // MCGS colour row lists

@@ -471,6 +471,98 @@ void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac
     });
 }
 
+// ------------------------------------------- grid-index transfers ---------
+__device__ __forceinline__ bool on_box_boundary(int i, int j, int k, int nx, int ny, int nz, int dim)
+{
+    return i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (dim == 3 && (k == 0 || k == nz - 1));
+}
+
+// t = P scc for fine vertex f; sc += t; w = t * dfac (k_prolong on the assembled P)
+template <class V>
+__global__ void __launch_bounds__(NT) k_prolong_grid(GridPair g, const V *__restrict__ scc, V *__restrict__ sc,
+                                                     const V *__restrict__ dfac, V *__restrict__ w, const int *skip)
+{
+    PDL_ENTRY();
+    if (skip && *skip) return;
+    const int n = g.nx * g.ny * g.nz, stride = gridDim.x * NT;
+    for (int f = blockIdx.x * NT + threadIdx.x; f < n; f += stride) {
+        const int i = f % g.nx, j = (f / g.nx) % g.ny, k = f / (g.nx * g.ny);
+        const int p0 = i & 1, p1 = j & 1, p2 = k & 1, b0 = i >> 1, b1 = j >> 1, b2 = k >> 1;
+        const bool bnd = on_box_boundary(i, j, k, g.nx, g.ny, g.nz, g.dim);
+        V t = (V)0;
+        if (g.tet) {
+            const bool odd = (p0 | p1 | p2) != 0;
+            const V wt = odd ? (bnd ? (V)0 : (V)0.5) : (V)1;
+            t += wt * scc[b0 + g.cnx * (b1 + g.cny * b2)];
+            if (odd) t += wt * scc[(b0 + p0) + g.cnx * ((b1 + p1) + g.cny * (b2 + p2))];
+        } else {
+            const int np = 1 << (p0 + p1 + p2);
+            const V wt = bnd ? (np == 1 ? (V)1 : (V)0) : (V)(1.0 / np);
+            for (int dk = 0; dk <= p2; ++dk)
+                for (int dj = 0; dj <= p1; ++dj)
+                    for (int di = 0; di <= p0; ++di) t += wt * scc[(b0 + di) + g.cnx * ((b1 + dj) + g.cny * (b2 + dk))];
+        }
+        sc[f] += t;
+        if (w) w[f] = t * dfac[f];
+    }
+}
+
+// dc = R d for coarse vertex c: R = P^T, Dirichlet coarse rows = injection
+// (k_restrict on the assembled R); children in increasing fine index
+template <class V>
+__global__ void __launch_bounds__(NT) k_restrict_grid(GridPair g, const V *__restrict__ d, V *__restrict__ dc,
+                                                      const int *skip)
+{
+    PDL_ENTRY();
+    if (skip && *skip) return;
+    const int n = g.cnx * g.cny * g.cnz, stride = gridDim.x * NT;
+    const int kr = (g.dim == 3) ? 1 : 0;
+    for (int c = blockIdx.x * NT + threadIdx.x; c < n; c += stride) {
+        const int I = c % g.cnx, J = (c / g.cnx) % g.cny, K = c / (g.cnx * g.cny);
+        const int fv = 2 * I + g.nx * (2 * J + g.ny * 2 * K);
+        if (on_box_boundary(I, J, K, g.cnx, g.cny, g.cnz, g.dim)) {
+            dc[c] = (V)0 + (V)1 * d[fv];
+            continue;
+        }
+        V acc = (V)0;
+        for (int dk = -kr; dk <= kr; ++dk)
+            for (int dj = -1; dj <= 1; ++dj)
+                for (int di = -1; di <= 1; ++di) {
+                    const int nodd = (di != 0) + (dj != 0) + (dk != 0);
+                    V wt;
+                    if (g.tet) {
+                        const bool pos = di > 0 || dj > 0 || dk > 0, neg = di < 0 || dj < 0 || dk < 0;
+                        if (pos && neg) continue;   // not a Kuhn edge through this vertex
+                        wt = nodd ? (V)0.5 : (V)1;
+                    } else {
+                        wt = (V)(1.0 / (1 << nodd));
+                    }
+                    acc += wt * d[fv + di + g.nx * (dj + g.ny * dk)];
+                }
+        dc[c] = acc;
+    }
+}
+
+template <class V>
+void prolong_grid(Ctx &c, const GridPair &g, const V *scc, V *sc, const V *dfac, V *w, const int *skip)
+{
+    const int n = g.nx * g.ny * g.nz;
+    UG_LAUNCH_PDL(c, k_prolong_grid<V>, row_grid(c, n), NT, 0, g, scc, sc, dfac, w, skip);
+}
+
+template <class V>
+void restrict_grid(Ctx &c, const GridPair &g, const V *d, V *dc, const int *skip)
+{
+    const int n = g.cnx * g.cny * g.cnz;
+    UG_LAUNCH_PDL(c, k_restrict_grid<V>, row_grid(c, n), NT, 0, g, d, dc, skip);
+}
+template void prolong_grid<double>(Ctx &, const GridPair &, const double *, double *, const double *, double *,
+                                   const int *);
+template void prolong_grid<float>(Ctx &, const GridPair &, const float *, float *, const float *, float *,
+                                  const int *);
+template void restrict_grid<double>(Ctx &, const GridPair &, const double *, double *, const int *);
+template void restrict_grid<float>(Ctx &, const GridPair &, const float *, float *, const int *);
+
 // dense base solve with the LU-factored inverse (one block, FP64)
 // Ainv is staged in shared memory before the wait when it fits (staged != 0)
 template <class V>

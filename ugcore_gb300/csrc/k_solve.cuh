@@ -46,6 +46,19 @@ template <class V>
 void restrict_apply(Ctx &c, const OpMat<V> &R, const V *d, V *dc, const int *skip);
 template <class V>
 void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac, V *w, const int *skip);
+// StdTransfer on a structured hierarchy without a stored matrix: the
+// parents of a fine vertex and the weights (1, 1/2, 1/4, 1/8; Dirichlet rows
+// adjusted as in the assembled P and R) follow from its grid indices.  Same
+// entries, same order of summation as the assembled P and R = P^T.
+struct GridPair {
+    int nx, ny, nz;      // fine level vertices per direction (nz = 1 in 2D)
+    int cnx, cny, cnz;   // coarse level
+    int dim, tet;        // tet: Kuhn split (two parents per edge midpoint)
+};
+template <class V>
+void prolong_grid(Ctx &c, const GridPair &g, const V *scc, V *sc, const V *dfac, V *w, const int *skip);
+template <class V>
+void restrict_grid(Ctx &c, const GridPair &g, const V *d, V *dc, const int *skip);
 template <class V>
 void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip);
 // once per base size, outside stream capture: allows the shared-memory copy of Ainv
