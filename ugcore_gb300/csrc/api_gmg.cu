@@ -48,7 +48,10 @@ __global__ void k_to_v(const double *in, V *out, int n)
 {
     PDL_ENTRY();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = (V)in[i];
+    if (i < n) {
+        if constexpr (sizeof(V) == 4) out[i] = f64_to_f32(in[i]);
+        else out[i] = (V)in[i];
+    }
 }
 
 // P rows from the parent table; Dirichlet fine rows: values 0, and 1 to a

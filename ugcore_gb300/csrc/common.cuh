@@ -255,6 +255,47 @@ __device__ __forceinline__ double ld_stream(const double *p) { return __ldcs(p);
 __device__ __forceinline__ float ld_stream(const float *p) { return __ldcs(p); }
 __device__ __forceinline__ int ld_stream(const int *p) { return __ldcs(p); }
 
+// FP32 <-> FP64 conversions in integer arithmetic, from the IEEE-754 binary
+// formats.  On GB300 the hardware conversions issue on the FP64 pipe at a
+// fraction of the FMA rate, which made them the limiter of the FP64 vector
+// kernels that also produce or consume the FP32 multigrid vectors.  Normal
+// numbers and zeros take the integer path (widening is exact; narrowing
+// rounds to nearest, ties to even, as cvt.rn.f32.f64); subnormal, out-of-
+// range, infinite and NaN inputs fall back to the hardware conversion.
+__device__ __forceinline__ double f32_to_f64(float f)
+{
+    const unsigned int u = __float_as_uint(f);
+    const unsigned int e = (u >> 23) & 0xffu;
+    const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
+    if (e == 0u && (u & 0x7fffffu) == 0u) return __longlong_as_double((long long)sgn);
+    if (e == 0u || e == 0xffu) return (double)f;
+    const unsigned long long bits =
+        sgn | ((unsigned long long)(e + (1023u - 127u)) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ float f64_to_f32(double d)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned int sgn = (unsigned int)(b >> 63) << 31;
+    const int e = (int)((b >> 52) & 0x7ffu);
+    const unsigned long long m = b & 0xfffffffffffffULL;
+    if (e == 0 && m == 0) return __uint_as_float(sgn);
+    int fe = e - 1023 + 127;
+    if (fe <= 0 || fe >= 255) return (float)d;
+    unsigned int mant = (unsigned int)(m >> 29);
+    const unsigned long long rest = m & ((1ULL << 29) - 1), half = 1ULL << 28;
+    if (rest > half || (rest == half && (mant & 1u))) {
+        mant += 1u;
+        if (mant == (1u << 23)) {
+            mant = 0u;
+            fe += 1;
+            if (fe >= 255) return (float)d;
+        }
+    }
+    return __uint_as_float(sgn | ((unsigned int)fe << 23) | mant);
+}
+
 // W values of type T that fill 16 bytes, moved with one vector load/store
 template <class T, int W>
 struct alignas(16) Pack {

@@ -35,6 +35,10 @@ int row_grid(const Ctx &c, int nrows)
     return need < cap ? need : cap;
 }
 
+// widening to FP64 of a level-precision value (identity for FP64)
+__device__ __forceinline__ double f32_to_f64_t(double v) { return v; }
+__device__ __forceinline__ double f32_to_f64_t(float v) { return f32_to_f64(v); }
+
 // ------------------------------------------------------------ views ------
 template <class V>
 struct SellMV {
@@ -234,7 +238,7 @@ __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, c
         V s = (sc_mode == SC_SET_FROM_BASE) ? t : sc[row] + t;
         sc[row] = s;
         if (RHO || z64) {
-            const double s64 = (double)s;   // one conversion per row, only where needed
+            const double s64 = f32_to_f64_t(s);   // one conversion per row, only where needed
             if (z64) z64[row] = s64;
             if (RHO) rsum += s64 * r_rho[row];
         }
@@ -289,7 +293,7 @@ __global__ void __launch_bounds__(NT, 4) k_smooth_dia(DiaMV<V, S> A, const V *__
             if (RHO || z64) {
                 double s64[W];
 #pragma unroll
-                for (int e = 0; e < W; ++e) s64[e] = (double)s.v[e];
+                for (int e = 0; e < W; ++e) s64[e] = f32_to_f64_t(s.v[e]);
                 if constexpr (W % 2 == 0) {
                     // FP64 side in 16-byte pairs when both arrays allow it
                     if (wide64) {
@@ -321,7 +325,7 @@ __global__ void __launch_bounds__(NT, 4) k_smooth_dia(DiaMV<V, S> A, const V *__
                 V s = (sc_mode == SC_SET_FROM_BASE) ? t : sc[row] + t;
                 sc[row] = s;
                 if (RHO || z64) {
-                    const double s64 = (double)s;
+                    const double s64 = f32_to_f64_t(s);
                     if (z64) z64[row] = s64;
                     if (RHO) rsum += s64 * r_rho[row];
                 }
@@ -477,6 +481,13 @@ __device__ __forceinline__ bool on_box_boundary(int i, int j, int k, int nx, int
     return i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (dim == 3 && (k == 0 || k == nz - 1));
 }
 
+// StdTransfer weight of a parent along `nodd` odd directions: 1, 1/2, 1/4, 1/8
+template <class V>
+__device__ __forceinline__ V grid_weight(int nodd)
+{
+    return nodd == 0 ? (V)1 : (nodd == 1 ? (V)0.5 : (nodd == 2 ? (V)0.25 : (V)0.125));
+}
+
 // t = P scc for fine vertex f; sc += t; w = t * dfac (k_prolong on the assembled P)
 template <class V>
 __global__ void __launch_bounds__(NT) k_prolong_grid(GridPair g, const V *__restrict__ scc, V *__restrict__ sc,
@@ -497,7 +508,7 @@ __global__ void __launch_bounds__(NT) k_prolong_grid(GridPair g, const V *__rest
             if (odd) t += wt * scc[(b0 + p0) + g.cnx * ((b1 + p1) + g.cny * (b2 + p2))];
         } else {
             const int np = 1 << (p0 + p1 + p2);
-            const V wt = bnd ? (np == 1 ? (V)1 : (V)0) : (V)(1.0 / np);
+            const V wt = bnd ? (np == 1 ? (V)1 : (V)0) : grid_weight<V>(p0 + p1 + p2);
             for (int dk = 0; dk <= p2; ++dk)
                 for (int dj = 0; dj <= p1; ++dj)
                     for (int di = 0; di <= p0; ++di) t += wt * scc[(b0 + di) + g.cnx * ((b1 + dj) + g.cny * (b2 + dk))];
@@ -535,7 +546,7 @@ __global__ void __launch_bounds__(NT) k_restrict_grid(GridPair g, const V *__res
                         if (pos && neg) continue;   // not a Kuhn edge through this vertex
                         wt = nodd ? (V)0.5 : (V)1;
                     } else {
-                        wt = (V)(1.0 / (1 << nodd));
+                        wt = grid_weight<V>(nodd);
                     }
                     acc += wt * d[fv + di + g.nx * (dj + g.ny * dk)];
                 }
@@ -698,7 +709,7 @@ __global__ void __launch_bounds__(NT) k_krylov_start(MV A, const double *__restr
         double ax = A.template dot<double>(x, row);
         double rv = r[row] - ax;
         r[row] = rv;
-        if (r32) r32[row] = (float)rv;
+        if (r32) r32[row] = f64_to_f32(rv);
         sum += rv * rv;
     }
     double v[1] = {sum};
@@ -791,7 +802,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(int n, double *__restrict__ x,
             st_pack<double, 2>(x + i, xv);
             st_pack<double, 2>(r + i, rv);
             if (r32) {
-                float2 f = make_float2((float)rv.v[0], (float)rv.v[1]);
+                float2 f = make_float2(f64_to_f32(rv.v[0]), f64_to_f32(rv.v[1]));
                 *reinterpret_cast<float2 *>(r32 + i) = f;
             }
         } else {
@@ -799,7 +810,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(int n, double *__restrict__ x,
             double rv = r[i] + (-alpha) * q[i];
             r[i] = rv;
             sum += rv * rv;
-            if (r32) r32[i] = (float)rv;
+            if (r32) r32[i] = f64_to_f32(rv);
         }
     }
     double v[1] = {sum};
@@ -822,7 +833,7 @@ __global__ void __launch_bounds__(NT) k_cg_update1(int n, double *__restrict__ x
         double rv = r[i] + (-alpha) * q[i];
         r[i] = rv;
         sum += rv * rv;
-        if (r32) r32[i] = (float)rv;
+        if (r32) r32[i] = f64_to_f32(rv);
     }
     double v[1] = {sum};
     grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) { conv_update(ks, sqrt(tot[0]), 1); });
@@ -875,7 +886,7 @@ __global__ void k_copy_z(int n, const ZT *__restrict__ z, double *__restrict__ o
     PDL_ENTRY();
     if (skip && *skip) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = (double)z[i];
+    if (i < n) out[i] = f32_to_f64_t(z[i]);
 }
 
 template <class ZT>
