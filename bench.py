@@ -31,6 +31,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "DoFs/s for GMG-PCG solve to 1e-10 rel (FP64 vs mixed) + adjoint grad time"
+# DRAM bytes (read + write) per launch of the top-level FP64 smoothing kernel,
+# mean of the two launches captured by
+#   ncu --set full --clock-control none -k regex:k_smooth -c 2 -o prof \
+#       python bench.py --steps 2 --warmup 3 --no-extras --no-cpu
+# (summary in profiles/k_smooth_fp64_poisson129.md); the FP64 pipe was 82 % busy.
+NCU_TRAFFIC_TOP_SMOOTH = 512.1e6
+NCU_FP64_PIPE_TOP_SMOOTH = 0.82
 UNIT = "DoFs/s"
 WORKLOAD = "c1: 3D Poisson FP64, unit cube 2x2x2 hex refined 6x (129^3 = 2,146,689 DoFs), GMG V(2,2) Jacobi(0.6)-PCG to 1e-10"
 
@@ -312,7 +319,8 @@ def run_ours(args, rank, world, local_rank):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "kernel": "k_smooth (fused damped-Jacobi SpMV, top level, 4 launches/cycle)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_kind": peak_kind, "traffic": None,
+                     "peak_kind": peak_kind, "traffic": NCU_TRAFFIC_TOP_SMOOTH,
+                     "limiter": "FP64 FMA pipe (%.0f%% busy in ncu): 27 FP64 FMAs per row" % (100 * NCU_FP64_PIPE_TOP_SMOOTH),
                      "bytes_per_launch": s_bytes / max(s_cnt, 1), "avg_launch_ms": s_ms / max(s_cnt, 1),
                      "share_of_solve": s_ms / total_prof_ms if total_prof_ms else None},
         "solve_roofline": {"achieved": solve_gbs, "peak": hbm, "unit": "GB/s", "frac": solve_gbs / hbm,
