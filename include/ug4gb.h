@@ -80,10 +80,20 @@ UG4GB_API int64_t ug4gb_kernel_launches(const ug4gb_ctx *ctx);
 #define UG4GB_FORMAT_AUTO 0
 #define UG4GB_FORMAT_SELL 1
 UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
-/* performance switches (value 0 or 1) that leave every result bit-identical.
-   UG4GB_TUNE_PDL: programmatic dependent launch of the solve-path kernels,
-   each kernel scheduled while its predecessor still runs (default 1). */
+/* performance switches that leave every result bit-identical.
+   UG4GB_TUNE_PDL (0 or 1): programmatic dependent launch of the solve-path
+   kernels, each kernel scheduled while its predecessor still runs (default 1).
+   UG4GB_TUNE_SWEEP_FUSION (bit mask, 0..3): two consecutive damped-Jacobi
+   steps of a structured 3D FP32 level in one pass over its operator.  Bit 1:
+   on; bit 2: levels of every size (else only levels of at least 2^18
+   vertices).  Default 0.  Smoothed corrections and defects are
+   bit-identical; inside a Krylov solve only the summation order of the
+   fused (z, r) product changes.  Applies to multigrids set up after the call. */
 #define UG4GB_TUNE_PDL 1
+#define UG4GB_TUNE_SWEEP_FUSION 2
+/* UG4GB_TUNE_SWEEP_PLANES (2..128): z planes a block of the fused sweeps
+   marches through (default 16). */
+#define UG4GB_TUNE_SWEEP_PLANES 3
 UG4GB_API int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value);
 /* per-launch CUDA-event timing of every kernel until profile_end, which
    writes "tag|kernel<TAB>launches<TAB>total_ms" lines into buf.  While it is

@@ -17,6 +17,8 @@ PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_CG, SOLVER_BICGSTAB = 0, 1
 UPWIND_NONE, UPWIND_FULL = 0, 1
 TUNE_PDL = 1
+TUNE_SWEEP_FUSION = 2
+TUNE_SWEEP_PLANES = 3
 
 _ERRNAMES = {ERR_INVALID: "invalid argument", ERR_CUDA: "CUDA error", ERR_NOMEM: "out of device memory",
              ERR_SINGULAR: "singular base matrix", ERR_NOT_CONVERGED: "not converged",

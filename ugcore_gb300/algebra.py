@@ -75,11 +75,18 @@ class Context:
         """'auto' (diagonal layout for structured operators) or 'sell'."""
         check(lib().ug4gb_set_operator_format(self.h, {"auto": 0, "sell": 1}[fmt]), self.h)
 
-    def set_tuning(self, pdl=None):
+    def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None):
         """performance switches that leave results bit-identical:
-        programmatic dependent launch of the solve kernels."""
+        pdl: programmatic dependent launch of the solve kernels;
+        sweep_fusion: bit mask (1 on, 2 every level size) of the
+        two-Jacobi-steps-per-pass smoother of structured 3D FP32 levels;
+        sweep_planes: z planes per block of that smoother."""
         if pdl is not None:
             check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_PDL, int(bool(pdl))), self.h)
+        if sweep_fusion is not None:
+            check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_SWEEP_FUSION, int(sweep_fusion)), self.h)
+        if sweep_planes is not None:
+            check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_SWEEP_PLANES, int(sweep_planes)), self.h)
 
     def profile_begin(self):
         check(lib().ug4gb_profile_begin(self.h), self.h)

@@ -152,9 +152,20 @@ int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format)
 
 int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value)
 {
-    if (!ctx || (value != 0 && value != 1)) return UG4GB_ERR_INVALID;
+    if (!ctx) return UG4GB_ERR_INVALID;
     switch (knob) {
-    case UG4GB_TUNE_PDL: ctx->c.pdl = value != 0; return UG4GB_OK;
+    case UG4GB_TUNE_PDL:
+        if (value != 0 && value != 1) return UG4GB_ERR_INVALID;
+        ctx->c.pdl = value != 0;
+        return UG4GB_OK;
+    case UG4GB_TUNE_SWEEP_FUSION:
+        if (value < 0 || value > 3) return UG4GB_ERR_INVALID;
+        ctx->c.sweep_fusion = value;
+        return UG4GB_OK;
+    case UG4GB_TUNE_SWEEP_PLANES:
+        if (value < 2 || value > 128) return UG4GB_ERR_INVALID;
+        ctx->c.sweep_fusion_tz = value;
+        return UG4GB_OK;
     default: ctx->c.err = "ug4gb_set_tuning: unknown knob"; return UG4GB_ERR_INVALID;
     }
 }

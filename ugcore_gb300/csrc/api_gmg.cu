@@ -263,7 +263,6 @@ struct GmgT : GmgBase {
         copy_in(c, Ainv.p, inv.data(), sizeof(double) * inv.size());
         UG_CUDA(cudaStreamSynchronize(c.stream));
         nbase = n;
-        base_solve_prepare<V>(n);
     }
 
     // ------------------------------------------------------------ cycle --
@@ -300,6 +299,14 @@ struct GmgT : GmgBase {
         for (int k = 0; k < nu1; ++k) {
             V *out = (cur == L.dA.p) ? L.dB.p : L.dA.p;
             int mode = (k == 0) ? (first ? SC_SET_FROM_BASE : SC_ADD_FROM_BASE) : SC_ADD_FROM_BASE;
+            // two steps in one pass over the operator where the level allows it
+            if (k + 1 < nu1 && L.sweep2 &&
+                smooth_pair<V>(c, L.At, L.gp, cur, nullptr, L.dinv.p, L.sc.p, out, mode, SC_ADD_FROM_BASE, skip,
+                               nullptr, nullptr, 0, nullptr)) {
+                cur = out;
+                ++k;
+                continue;
+            }
             if (smoother == UG4GB_SMOOTHER_JACOBI) {
                 smooth_step<V, V, V>(c, L.At, cur, cur, L.dinv.p, L.sc.p, out, mode, skip, nullptr, nullptr, 0);
             } else {
@@ -332,6 +339,23 @@ struct GmgT : GmgBase {
         if (smoother == UG4GB_SMOOTHER_JACOBI) {
             for (int k = 0; k < nu2; ++k) {
                 const V *x = (k == 0) ? L.w.p : dbase;
+                // two steps in one pass where the level allows it
+                if (k + 1 < nu2 && L.sweep2) {
+                    bool need_out = (k + 1 < nu2 - 1) || (l != T && cycle > 1);
+                    V *out = need_out ? ((dbase == L.dA.p) ? L.dB.p : L.dA.p) : nullptr;
+                    bool last_top = (l == T && k + 1 == nu2 - 1);
+                    if (smooth_pair<V>(c, L.At, L.gp, x, k == 0 ? dbase : nullptr, L.dinv.p, L.sc.p, out,
+                                       SC_ADD_FROM_NEW, SC_ADD_FROM_NEW, skip, last_top ? r_rho : nullptr,
+                                       last_top ? red : nullptr, rho_kind, last_top ? z64.p : nullptr)) {
+                        if (last_top) {
+                            rho_done = (r_rho != nullptr);
+                            z_written = true;
+                        }
+                        if (out) dbase = out;
+                        ++k;
+                        continue;
+                    }
+                }
                 bool need_out = (k < nu2 - 1) || (l != T && cycle > 1);
                 V *out = need_out ? ((dbase == L.dA.p) ? L.dB.p : L.dA.p) : nullptr;
                 bool last_top = (l == T && k == nu2 - 1);
@@ -417,7 +441,10 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         }
         UG_CUDA(cudaStreamSynchronize(c.stream));
         G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
-        if (l > m->base) G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
+        if (l > m->base) {
+            G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
+            L.sweep2 = L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI && sweep2_supported<V>(c, L.At, L.gp);
+        }
     }
     G->setup_base(c);
     if (sizeof(V) != sizeof(double)) G->z64.alloc(g->lev[nl - 1].nv);

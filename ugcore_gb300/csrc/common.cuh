@@ -90,6 +90,11 @@ struct Ctx {
     bool profiling = false;
     bool allow_dia = true;      // operators with <= 27 offsets use the diagonal layout
     bool pdl = true;            // programmatic dependent launch on the solve path
+    // two Jacobi steps per pass on structured 3D FP32 levels (bit mask):
+    // 1 = on, 2 = every level size (else >= sweep_fusion_min_rows vertices)
+    int sweep_fusion = 0;
+    int sweep_fusion_min_rows = 1 << 18;
+    int sweep_fusion_tz = 16;   // z planes per block
     std::string prof_tag;       // set by the orchestration (level / phase)
     std::vector<ProfRec> prof;
     std::vector<cudaEvent_t> ev_pool;

@@ -116,7 +116,7 @@ struct DiaMV {
         for (int k = 0; k < S; ++k) {
             int j = i + off.o[k];
             j = j < 0 ? 0 : (j >= ncols ? ncols - 1 : j);
-            acc += (ACC)c.a[k] * (ACC)x[j];
+            acc = fma_rn((ACC)c.a[k], (ACC)x[j], acc);
         }
         return acc;
     }
@@ -128,7 +128,7 @@ struct DiaMV {
         for (int k = 0; k < S; ++k) {
             int j = i + off.o[k];
             j = j < 0 ? 0 : (j >= ncols ? ncols - 1 : j);
-            acc += (ACC)ld_stream(val + (size_t)k * ld + i) * (ACC)x[j];
+            acc = fma_rn((ACC)ld_stream(val + (size_t)k * ld + i), (ACC)x[j], acc);
         }
         return acc;
     }
@@ -155,7 +155,7 @@ struct DiaMV {
                 for (int e = 0; e < W; ++e) {
                     int jj = j + e;
                     jj = jj < 0 ? 0 : (jj >= ncols ? ncols - 1 : jj);
-                    acc[e] += a[k].v[e] * (V)x[jj];
+                    acc[e] = fma_rn(a[k].v[e], (V)x[jj], acc[e]);
                 }
             }
         }
@@ -232,10 +232,10 @@ __global__ void __launch_bounds__(NT) k_smooth(MV A, const XT *__restrict__ x, c
         const bool first = PF && (row == row0);
         V acc = first ? A.template dot_cached<V>(x, row, cache) : A.template dot<V>(x, row);
         V db = (V)dbase[row];
-        V dn = db - acc;
+        V s;
+        V dn = jacobi_row<V>(acc, db, first ? dinv0 : dinv[row], sc_mode,
+                             sc_mode == SC_SET_FROM_BASE ? (V)0 : sc[row], s);
         if (dout) dout[row] = dn;
-        V t = (first ? dinv0 : dinv[row]) * (sc_mode == SC_ADD_FROM_NEW ? dn : db);
-        V s = (sc_mode == SC_SET_FROM_BASE) ? t : sc[row] + t;
         sc[row] = s;
         if (RHO || z64) {
             const double s64 = f32_to_f64_t(s);   // one conversion per row, only where needed
@@ -283,11 +283,9 @@ __global__ void __launch_bounds__(NT, 4) k_smooth_dia(DiaMV<V, S> A, const V *__
             Pack<V, W> db = ld_pack<V, W>(dbase + r0), di = ld_pack<V, W>(dinv + r0), s, dn;
             if (sc_mode != SC_SET_FROM_BASE) s = ld_pack<V, W>(sc + r0);
 #pragma unroll
-            for (int e = 0; e < W; ++e) {
-                dn.v[e] = db.v[e] - acc[e];
-                V t = di.v[e] * (sc_mode == SC_ADD_FROM_NEW ? dn.v[e] : db.v[e]);
-                s.v[e] = (sc_mode == SC_SET_FROM_BASE) ? t : s.v[e] + t;
-            }
+            for (int e = 0; e < W; ++e)
+                dn.v[e] = jacobi_row<V>(acc[e], db.v[e], di.v[e], sc_mode,
+                                        sc_mode == SC_SET_FROM_BASE ? (V)0 : s.v[e], s.v[e]);
             if (dout) st_pack<V, W>(dout + r0, dn);
             st_pack<V, W>(sc + r0, s);
             if (RHO || z64) {
@@ -318,11 +316,10 @@ __global__ void __launch_bounds__(NT, 4) k_smooth_dia(DiaMV<V, S> A, const V *__
         } else {
             for (int row = r0; row < n; ++row) {
                 V acc = A.template dot<V>(x, row);
-                V db = dbase[row];
-                V dn = db - acc;
+                V s;
+                V dn = jacobi_row<V>(acc, dbase[row], dinv[row], sc_mode,
+                                     sc_mode == SC_SET_FROM_BASE ? (V)0 : sc[row], s);
                 if (dout) dout[row] = dn;
-                V t = dinv[row] * (sc_mode == SC_ADD_FROM_NEW ? dn : db);
-                V s = (sc_mode == SC_SET_FROM_BASE) ? t : sc[row] + t;
                 sc[row] = s;
                 if (RHO || z64) {
                     const double s64 = f32_to_f64_t(s);
@@ -476,17 +473,6 @@ void prolong_apply(Ctx &c, const OpMat<V> &P, const V *scc, V *sc, const V *dfac
 }
 
 // ------------------------------------------- grid-index transfers ---------
-__device__ __forceinline__ bool on_box_boundary(int i, int j, int k, int nx, int ny, int nz, int dim)
-{
-    return i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (dim == 3 && (k == 0 || k == nz - 1));
-}
-
-// StdTransfer weight of a parent along `nodd` odd directions: 1, 1/2, 1/4, 1/8
-template <class V>
-__device__ __forceinline__ V grid_weight(int nodd)
-{
-    return nodd == 0 ? (V)1 : (nodd == 1 ? (V)0.5 : (nodd == 2 ? (V)0.25 : (V)0.125));
-}
 
 // t = P scc for fine vertex f; sc += t; w = t * dfac (k_prolong on the assembled P)
 template <class V>
@@ -498,23 +484,9 @@ __global__ void __launch_bounds__(NT) k_prolong_grid(GridPair g, const V *__rest
     const int n = g.nx * g.ny * g.nz, stride = gridDim.x * NT;
     for (int f = blockIdx.x * NT + threadIdx.x; f < n; f += stride) {
         const int i = f % g.nx, j = (f / g.nx) % g.ny, k = f / (g.nx * g.ny);
-        const int p0 = i & 1, p1 = j & 1, p2 = k & 1, b0 = i >> 1, b1 = j >> 1, b2 = k >> 1;
-        const bool bnd = on_box_boundary(i, j, k, g.nx, g.ny, g.nz, g.dim);
-        V t = (V)0;
-        if (g.tet) {
-            const bool odd = (p0 | p1 | p2) != 0;
-            const V wt = odd ? (bnd ? (V)0 : (V)0.5) : (V)1;
-            t += wt * scc[b0 + g.cnx * (b1 + g.cny * b2)];
-            if (odd) t += wt * scc[(b0 + p0) + g.cnx * ((b1 + p1) + g.cny * (b2 + p2))];
-        } else {
-            const int np = 1 << (p0 + p1 + p2);
-            const V wt = bnd ? (np == 1 ? (V)1 : (V)0) : grid_weight<V>(p0 + p1 + p2);
-            for (int dk = 0; dk <= p2; ++dk)
-                for (int dj = 0; dj <= p1; ++dj)
-                    for (int di = 0; di <= p0; ++di) t += wt * scc[(b0 + di) + g.cnx * ((b1 + dj) + g.cny * (b2 + dk))];
-        }
-        sc[f] += t;
-        if (w) w[f] = t * dfac[f];
+        const V t = prolong_value<V>(g, scc, i, j, k);
+        sc[f] = add_rn(sc[f], t);
+        if (w) w[f] = mul_rn(t, dfac[f]);
     }
 }
 
@@ -574,56 +546,50 @@ template void prolong_grid<float>(Ctx &, const GridPair &, const float *, float 
 template void restrict_grid<double>(Ctx &, const GridPair &, const double *, double *, const int *);
 template void restrict_grid<float>(Ctx &, const GridPair &, const float *, float *, const int *);
 
-// dense base solve with the LU-factored inverse (one block, FP64)
-// Ainv is staged in shared memory before the wait when it fits (staged != 0)
+// dense base solve with the LU-factored inverse, FP64: one warp per row of
+// Ainv, eight rows per block.  Each lane's first entries of its row are read
+// before the launch wait (Ainv is set up once), the defect is staged in
+// shared memory, and the row sum is a fixed-order warp reduction.
+constexpr int kBaseRowsPerBlock = NT / 32;
+constexpr int kBasePre = 8;   // entries per lane read before the wait (rows up to 256 wide)
+
 template <class V>
-__global__ void k_base_solve(const double *__restrict__ Ainv, int n, const V *__restrict__ d, V *__restrict__ sc,
-                             const int *skip, int staged)
+__global__ void __launch_bounds__(NT) k_base_solve(const double *__restrict__ Ainv, int n, const V *__restrict__ d,
+                                                   V *__restrict__ sc, const int *skip)
 {
     extern __shared__ double dsh[];
-    double *ash = dsh + n;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * kBaseRowsPerBlock + warp;
+    const double *arow = Ainv + (size_t)(row < n ? row : 0) * n;
+    double a[kBasePre];
+#pragma unroll
+    for (int t = 0; t < kBasePre; ++t) {
+        const int j = lane + 32 * t;
+        a[t] = (row < n && j < n) ? __ldg(arow + j) : 0.0;
+    }
     pdl_trigger();
-    if (staged)
-        for (int q = threadIdx.x; q < n * n; q += blockDim.x) ash[q] = Ainv[q];
     pdl_wait();
     if (skip && *skip) return;
     for (int j = threadIdx.x; j < n; j += blockDim.x) dsh[j] = (double)d[j];
     __syncthreads();
-    const double *M = staged ? ash : Ainv;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double s = 0.0;
-        for (int j = 0; j < n; ++j) s += M[(size_t)i * n + j] * dsh[j];
-        sc[i] = (V)s;
+    if (row >= n) return;
+    double s = 0.0;
+#pragma unroll
+    for (int t = 0; t < kBasePre; ++t) {
+        const int j = lane + 32 * t;
+        if (j < n) s += a[t] * dsh[j];
     }
-}
-
-constexpr size_t kBaseStageMax = 160 * 1024;
-
-static size_t base_smem(int n, int &staged)
-{
-    const size_t full = ((size_t)n * n + n) * sizeof(double);
-    staged = full <= kBaseStageMax ? 1 : 0;
-    return staged ? full : (size_t)n * sizeof(double);
-}
-
-template <class V>
-void base_solve_prepare(int n)
-{
-    int staged = 0;
-    const size_t shm = base_smem(n, staged);
-    if (shm > 48 * 1024)
-        UG_CUDA(cudaFuncSetAttribute(k_base_solve<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    for (int j = lane + 32 * kBasePre; j < n; j += 32) s += __ldg(arow + j) * dsh[j];
+    s = warp_sum(s);
+    if (lane == 0) sc[row] = (V)s;
 }
 
 template <class V>
 void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip)
 {
-    int staged = 0;
-    const size_t shm = base_smem(n, staged);
-    UG_LAUNCH_PDL(c, k_base_solve<V>, 1, NT, shm, Ainv, n, d, sc, skip, staged);
+    UG_LAUNCH_PDL(c, k_base_solve<V>, div_up(n, kBaseRowsPerBlock), NT, (size_t)n * sizeof(double), Ainv, n, d, sc,
+                  skip);
 }
-template void base_solve_prepare<double>(int);
-template void base_solve_prepare<float>(int);
 
 // multicolour Gauss-Seidel: rows of one colour, t_i = relax (d_i - (A t)_i) / a_ii
 // (t_i is still 0 when its colour is processed)

@@ -25,6 +25,32 @@ struct KScal {
 
 enum ScMode { SC_SET_FROM_BASE = 0, SC_ADD_FROM_BASE = 1, SC_ADD_FROM_NEW = 2 };
 
+// Explicitly rounded arithmetic of the smoothing and transfer row updates.
+// Every kernel that applies a damped-Jacobi step (one step per launch, or two
+// fused) or the prolongation goes through these, so the compiler cannot
+// contract them differently in different kernels: the results of all
+// variants are bit-identical.
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+// One damped-Jacobi row update after the row's SpMV value acc = (At x)_i:
+// dn = db - acc; t = dinv * (dn or db); sc (=|+=) t.  Returns dn; sc is
+// updated in place (sc_in is only read when the mode adds).
+template <class V>
+__device__ __forceinline__ V jacobi_row(V acc, V db, V dinv, int mode, V sc_in, V &sc_out)
+{
+    const V dn = sub_rn(db, acc);
+    const V t = mul_rn(dinv, mode == SC_ADD_FROM_NEW ? dn : db);
+    sc_out = (mode == SC_SET_FROM_BASE) ? t : add_rn(sc_in, t);
+    return dn;
+}
+
 struct RedArgs {
     double *partials;
     unsigned int *counter;
@@ -42,6 +68,26 @@ template <class V, class XT, class DT>
 void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const V *dinv, V *sc, V *dout,
                  int sc_mode, const int *skip, const double *r_rho, RedArgs *red, int rho_kind,
                  double *z64 = nullptr);
+struct GridPair;
+// Set-up check (may synchronise): At is a 15- or 27-diagonal FP32 operator of
+// the structured level gp (nx, ny, nz) whose entries towards vertices outside
+// the level are all 0, so smooth_pair may run on it.
+template <class V>
+bool sweep2_supported(Ctx &c, const OpMat<V> &At, const GridPair &gp);
+// Two consecutive damped-Jacobi steps of a structured 3D FP32 level in one
+// pass over the operator (k_sweep2.cu):
+//   step A: d1 = dbA - At xA,  sc (=|+=) dinv*(dbA|d1)   (modeA)
+//   step B: d2 = d1 - At d1,   sc += dinv*(d1|d2)        (modeB)
+// dbA == nullptr: dbA = xA.  dout (nullable) receives d2; r_rho / z64 as in
+// smooth_step.  Returns false (and launches nothing) when the level does not
+// qualify (see Ctx::sweep_fusion; FP64 levels never do); the caller then
+// applies the steps one by one.  Results are bit-identical to two
+// smooth_step calls; only the summation order of the optional rho reduction
+// differs.
+template <class V>
+bool smooth_pair(Ctx &c, const OpMat<V> &At, const GridPair &gp, const V *xA, const V *dbA, const V *dinv, V *sc,
+                 V *dout, int modeA, int modeB, const int *skip, const double *r_rho, RedArgs *red, int rho_kind,
+                 double *z64);
 template <class V>
 void restrict_apply(Ctx &c, const OpMat<V> &R, const V *d, V *dc, const int *skip);
 template <class V>
@@ -55,15 +101,51 @@ struct GridPair {
     int cnx, cny, cnz;   // coarse level
     int dim, tet;        // tet: Kuhn split (two parents per edge midpoint)
 };
+__device__ __forceinline__ bool on_box_boundary(int i, int j, int k, int nx, int ny, int nz, int dim)
+{
+    return i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (dim == 3 && (k == 0 || k == nz - 1));
+}
+
+// StdTransfer weight of a parent along `nodd` odd directions: 1, 1/2, 1/4, 1/8
+template <class V>
+__device__ __forceinline__ V grid_weight(int nodd)
+{
+    return nodd == 0 ? (V)1 : (nodd == 1 ? (V)0.5 : (nodd == 2 ? (V)0.25 : (V)0.125));
+}
+
+// t = (P scc)_f for the fine vertex f = (i, j, k): parents in increasing
+// coarse index, as the rows of the assembled P (StdTransfer::
+// assemble_prolongation_p1, std_transfer_impl.h:47-168, with
+// DirichletBoundary::adjust_prolongation: a Dirichlet fine vertex keeps only
+// a coinciding coarse parent, weight 1).
+template <class V>
+__device__ __forceinline__ V prolong_value(const GridPair &g, const V *__restrict__ scc, int i, int j, int k)
+{
+    const int p0 = i & 1, p1 = j & 1, p2 = k & 1, b0 = i >> 1, b1 = j >> 1, b2 = k >> 1;
+    const bool bnd = on_box_boundary(i, j, k, g.nx, g.ny, g.nz, g.dim);
+    V t = (V)0;
+    if (g.tet) {
+        const bool odd = (p0 | p1 | p2) != 0;
+        const V wt = odd ? (bnd ? (V)0 : (V)0.5) : (V)1;
+        t = fma_rn(wt, scc[b0 + g.cnx * (b1 + g.cny * b2)], t);
+        if (odd) t = fma_rn(wt, scc[(b0 + p0) + g.cnx * ((b1 + p1) + g.cny * (b2 + p2))], t);
+    } else {
+        const int np = 1 << (p0 + p1 + p2);
+        const V wt = bnd ? (np == 1 ? (V)1 : (V)0) : grid_weight<V>(p0 + p1 + p2);
+        for (int dk = 0; dk <= p2; ++dk)
+            for (int dj = 0; dj <= p1; ++dj)
+                for (int di = 0; di <= p0; ++di)
+                    t = fma_rn(wt, scc[(b0 + di) + g.cnx * ((b1 + dj) + g.cny * (b2 + dk))], t);
+    }
+    return t;
+}
+
 template <class V>
 void prolong_grid(Ctx &c, const GridPair &g, const V *scc, V *sc, const V *dfac, V *w, const int *skip);
 template <class V>
 void restrict_grid(Ctx &c, const GridPair &g, const V *d, V *dc, const int *skip);
 template <class V>
 void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip);
-// once per base size, outside stream capture: allows the shared-memory copy of Ainv
-template <class V>
-void base_solve_prepare(int n);
 template <class V>
 void mcgs_colour(Ctx &c, const OpMat<V> &A, const int *rows, int nrows_c, const V *dinv_relax, const V *d, V *t,
                  const int *skip);
