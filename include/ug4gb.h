@@ -92,7 +92,7 @@ UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
 #define UG4GB_TUNE_PDL 1
 #define UG4GB_TUNE_SWEEP_FUSION 2
 /* UG4GB_TUNE_SWEEP_PLANES (2..128): z planes a block of the fused sweeps
-   marches through (default 16). */
+   marches through (default 8). */
 #define UG4GB_TUNE_SWEEP_PLANES 3
 UG4GB_API int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value);
 /* per-launch CUDA-event timing of every kernel until profile_end, which

@@ -184,7 +184,9 @@ def test_bitwise_reproducible(ctx, name, over):
 def test_sell_and_diagonal_layouts_agree(ctx, name, over):
     """the automatic diagonal layout and SELL-32 give the same solve (the
     full-size mixed cases run the 4-rows-per-thread FP32 smoother on the top
-    level)"""
+    level).  The two layouts map rows to threads differently, so the fused
+    (z, r) reduction sums in a different order: the iteration counts agree
+    within the +-1 bar of the parity contract."""
     import ugcore_gb300 as ug
     from ugcore_gb300 import problems
     cfg = problems.config(name, **over)
@@ -193,7 +195,8 @@ def test_sell_and_diagonal_layouts_agree(ctx, name, over):
     p1 = problems.Problem(ctx, cfg)
     p2 = problems.Problem(c2, cfg)
     s1, s2 = p1.solve(), p2.solve()
-    assert s1["steps"] == s2["steps"]
+    assert abs(s1["steps"] - s2["steps"]) <= 1
+    assert s1["defect"] / s1["initial_defect"] < 1e-10 and s2["defect"] / s2["initial_defect"] < 1e-10
     x1, x2 = p1.x.numpy(), p2.x.numpy()
     tol = 1e-13 if cfg["precision"] == "fp64" else 1e-7
     assert np.abs(x1 - x2).max() <= tol * np.abs(x2).max()

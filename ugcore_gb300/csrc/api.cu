@@ -84,7 +84,9 @@ int ug4gb_create(int device, ug4gb_ctx **out)
         c.red_partials.alloc((size_t)kRedMaxBlocks * kRedMaxValues);
         c.red_counter.alloc(64);
         c.red_result.alloc(8);
+        c.dev_err.alloc(1);
         UG_CUDA(cudaMemset(c.red_counter.p, 0, c.red_counter.bytes()));
+        UG_CUDA(cudaMemset(c.dev_err.p, 0, sizeof(int)));
         UG_CUDA(cudaMallocHost((void **)&c.host_pinned, 256));
     });
     if (rc != UG4GB_OK) {
@@ -127,6 +129,7 @@ static void ctx_free(ug4gb_ctx *ctx)
     ctx->c.red_partials.release();
     ctx->c.red_counter.release();
     ctx->c.red_result.release();
+    ctx->c.dev_err.release();
     if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
     delete ctx;
 }

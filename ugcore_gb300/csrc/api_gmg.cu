@@ -301,8 +301,8 @@ struct GmgT : GmgBase {
             int mode = (k == 0) ? (first ? SC_SET_FROM_BASE : SC_ADD_FROM_BASE) : SC_ADD_FROM_BASE;
             // two steps in one pass over the operator where the level allows it
             if (k + 1 < nu1 && L.sweep2 &&
-                smooth_pair<V>(c, L.At, L.gp, cur, nullptr, L.dinv.p, L.sc.p, out, mode, SC_ADD_FROM_BASE, skip,
-                               nullptr, nullptr, 0, nullptr)) {
+                smooth_pair<V>(c, L.sweep2.get(), L.gp, cur, nullptr, L.dinv.p, L.sc.p, out, mode, SC_ADD_FROM_BASE,
+                               skip, nullptr, nullptr, 0, nullptr)) {
                 cur = out;
                 ++k;
                 continue;
@@ -344,7 +344,7 @@ struct GmgT : GmgBase {
                     bool need_out = (k + 1 < nu2 - 1) || (l != T && cycle > 1);
                     V *out = need_out ? ((dbase == L.dA.p) ? L.dB.p : L.dA.p) : nullptr;
                     bool last_top = (l == T && k + 1 == nu2 - 1);
-                    if (smooth_pair<V>(c, L.At, L.gp, x, k == 0 ? dbase : nullptr, L.dinv.p, L.sc.p, out,
+                    if (smooth_pair<V>(c, L.sweep2.get(), L.gp, x, k == 0 ? dbase : nullptr, L.dinv.p, L.sc.p, out,
                                        SC_ADD_FROM_NEW, SC_ADD_FROM_NEW, skip, last_top ? r_rho : nullptr,
                                        last_top ? red : nullptr, rho_kind, last_top ? z64.p : nullptr)) {
                         if (last_top) {
@@ -443,7 +443,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
         if (l > m->base) {
             G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
-            L.sweep2 = L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI && sweep2_supported<V>(c, L.At, L.gp);
+            if (L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI) L.sweep2 = sweep2_prepare<V>(c, L.At, L.gp);
         }
     }
     G->setup_base(c);
@@ -567,6 +567,7 @@ int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
             const double *z = m->impl->apply(c, d->d, nullptr, nullptr, nullptr, 0, rd);
             copy_z<double>(c, m->n_top, z, cvec->d, nullptr);
             UG_CUDA(cudaStreamSynchronize(c.stream));
+            check_device_error(c);
             return;
         }
         if (!m->graph || m->graph_d != d->d || m->graph_c != cvec->d) {
@@ -593,6 +594,7 @@ int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
         UG_CUDA(cudaGraphLaunch(m->graph, c.stream));
         c.launches += m->graph_kernels;
         UG_CUDA(cudaStreamSynchronize(c.stream));
+        check_device_error(c);
     });
 }
 

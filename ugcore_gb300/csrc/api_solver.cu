@@ -218,6 +218,7 @@ void run(ug4gb_solver *s, double *x, double *r)
     int steps_before = s->kind == UG4GB_SOLVER_CG ? 1 : 0;
     UG_CUDA(cudaMemcpyAsync(&s->host_ks, s->ks.p, sizeof(KScal), cudaMemcpyDeviceToHost, c.stream));
     UG_CUDA(cudaStreamSynchronize(c.stream));
+    check_device_error(c);
     if (!c.profiling && s->iter_graph && s->host_ks.step > steps_before) {
         // the loop body ran once per CG step / per BiCGStab pair of half steps
         int64_t runs = s->kind == UG4GB_SOLVER_CG ? s->host_ks.step - steps_before : (s->host_ks.step + 1) / 2;

@@ -94,7 +94,7 @@ struct Ctx {
     // 1 = on, 2 = every level size (else >= sweep_fusion_min_rows vertices)
     int sweep_fusion = 0;
     int sweep_fusion_min_rows = 1 << 18;
-    int sweep_fusion_tz = 16;   // z planes per block
+    int sweep_fusion_tz = 8;    // z planes per block
     std::string prof_tag;       // set by the orchestration (level / phase)
     std::vector<ProfRec> prof;
     std::vector<cudaEvent_t> ev_pool;
@@ -102,6 +102,8 @@ struct Ctx {
     DevBuf<double> red_partials;        // kRedMaxBlocks * kRedMaxValues
     DevBuf<unsigned int> red_counter;   // one counter per reduction slot
     DevBuf<double> red_result;          // results of plain reductions
+    DevBuf<int> dev_err;                // set by a kernel whose bounded device-side wait ran out
+    bool dev_err_possible = false;      // a kernel that can set dev_err was launched or captured
     double *host_pinned = nullptr;      // small pinned readback area
 };
 
@@ -216,10 +218,16 @@ struct Offs {
 
 template <class T>
 struct Dia {
+    // the value array carries kGuard zero elements before diagonal 0 and
+    // after the last one, so aligned bulk copies of a grid line that start
+    // up to 4 elements early or end up to 64 elements late stay inside it
+    static constexpr int kGuard = 64;
     int nrows = 0, ncols = 0, S = 0;
     int ld = 0;       // stride between diagonals: nrows rounded up to 32 (128-byte aligned rows of values)
     Offs off{};
-    DevBuf<T> val;
+    DevBuf<T> val;    // kGuard + S * ld + kGuard elements
+    const T *vals() const { return val.p + kGuard; }
+    T *vals() { return val.p + kGuard; }
 };
 
 // An operator in its solve format: SELL-32 (general) or diagonal.
@@ -415,5 +423,8 @@ void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs,
 template <class T>
 void op_from_csr(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_scale, bool allow_dia);
 void fill_double(Ctx &c, double *p, size_t n, double v);
+// after a synchronisation of the stream: throws if a kernel reported that one
+// of its bounded waits ran out (and clears the flag)
+void check_device_error(Ctx &c);
 
 }  // namespace ug4gb

@@ -79,7 +79,7 @@ struct GLevel {
     Csr P, R;                    // P: this x coarse, R: coarse x this (FP64, exportable)
     OpMat<V> Ps, Rs;
     bool grid_transfer = false;  // apply P and R from grid indices (structured hierarchy)
-    bool sweep2 = false;         // At qualifies for two Jacobi steps per pass (smooth_pair)
+    std::shared_ptr<Sweep2Op> sweep2;   // At prepared for two Jacobi steps per pass (smooth_pair), or null
     GridPair gp{};
     DevBuf<V> sc, dA, dB, w, t;
     V *dcur = nullptr;

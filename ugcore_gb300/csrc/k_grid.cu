@@ -506,11 +506,11 @@ void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs,
     D.S = (int)offs.size();
     for (int k = 0; k < kMaxDiag; ++k) D.off.o[k] = k < D.S ? offs[k] : 0;
     D.ld = (A.nrows + 31) / 32 * 32;
-    D.val.alloc((size_t)D.S * D.ld);
-    // absent entries and the padding rows stay 0
+    D.val.alloc((size_t)D.S * D.ld + 2 * Dia<T>::kGuard);
+    // absent entries, the padding rows and the guards stay 0
     UG_CUDA(cudaMemsetAsync(D.val.p, 0, D.val.bytes(), c.stream));
     UG_LAUNCH(c, k_dia_fill<T>, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows, D.ld, D.off,
-              D.S, col_scale, D.val.p);
+              D.S, col_scale, D.vals());
 }
 
 // the diagonal kernels are instantiated for S = 9, 15, 27 (2D quads, Kuhn
@@ -565,6 +565,17 @@ void fill_double(Ctx &c, double *p, size_t n, double v)
 {
     if (n == 0) return;
     UG_LAUNCH(c, k_fill, div_up(n, 256), 256, 0, p, n, v);
+}
+
+void check_device_error(Ctx &c)
+{
+    if (!c.dev_err.p || !c.dev_err_possible) return;
+    int flag = 0;
+    UG_CUDA(cudaMemcpy(&flag, c.dev_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+        UG_CUDA(cudaMemset(c.dev_err.p, 0, sizeof(int)));
+        throw Error{UG4GB_ERR_CUDA, "a kernel's bounded wait for its own asynchronous copies ran out"};
+    }
 }
 
 }  // namespace ug4gb

@@ -172,9 +172,9 @@ void with_mv(const OpMat<V> &m, F &&f)
     }
     const Dia<V> &d = m.dia;
     switch (d.S) {
-    case 9: f(DiaMV<V, 9>{d.nrows, d.ncols, d.ld, d.val.p, d.off}); break;
-    case 15: f(DiaMV<V, 15>{d.nrows, d.ncols, d.ld, d.val.p, d.off}); break;
-    case 27: f(DiaMV<V, 27>{d.nrows, d.ncols, d.ld, d.val.p, d.off}); break;
+    case 9: f(DiaMV<V, 9>{d.nrows, d.ncols, d.ld, d.vals(), d.off}); break;
+    case 15: f(DiaMV<V, 15>{d.nrows, d.ncols, d.ld, d.vals(), d.off}); break;
+    case 27: f(DiaMV<V, 27>{d.nrows, d.ncols, d.ld, d.vals(), d.off}); break;
     default: throw Error{UG4GB_ERR_INVALID, "diagonal operator with unsupported width"};
     }
 }

@@ -4,6 +4,8 @@
 // wrappers dispatch to the kernel instantiated for that layout.
 #pragma once
 
+#include <memory>
+
 #include "common.cuh"
 
 namespace ug4gb {
@@ -69,23 +71,25 @@ void smooth_step(Ctx &c, const OpMat<V> &At, const XT *x, const DT *dbase, const
                  int sc_mode, const int *skip, const double *r_rho, RedArgs *red, int rho_kind,
                  double *z64 = nullptr);
 struct GridPair;
-// Set-up check (may synchronise): At is a 15- or 27-diagonal FP32 operator of
-// the structured level gp (nx, ny, nz) whose entries towards vertices outside
-// the level are all 0, so smooth_pair may run on it.
+// The operator of a structured 3D FP32 level prepared for smooth_pair: a copy
+// with 16-byte aligned grid lines and its TMA tensor descriptor (k_sweep2.cu).
+struct Sweep2Op;
+// Set-up (may synchronise): null unless At is a 15- or 27-diagonal FP32
+// operator of the structured level gp (nx, ny, nz) with the stencil of that
+// level's element type and no nonzero entry towards a vertex outside it.
 template <class V>
-bool sweep2_supported(Ctx &c, const OpMat<V> &At, const GridPair &gp);
+std::shared_ptr<Sweep2Op> sweep2_prepare(Ctx &c, const OpMat<V> &At, const GridPair &gp);
 // Two consecutive damped-Jacobi steps of a structured 3D FP32 level in one
 // pass over the operator (k_sweep2.cu):
 //   step A: d1 = dbA - At xA,  sc (=|+=) dinv*(dbA|d1)   (modeA)
 //   step B: d2 = d1 - At d1,   sc += dinv*(d1|d2)        (modeB)
 // dbA == nullptr: dbA = xA.  dout (nullable) receives d2; r_rho / z64 as in
-// smooth_step.  Returns false (and launches nothing) when the level does not
-// qualify (see Ctx::sweep_fusion; FP64 levels never do); the caller then
-// applies the steps one by one.  Results are bit-identical to two
-// smooth_step calls; only the summation order of the optional rho reduction
-// differs.
+// smooth_step.  Returns false (and launches nothing) when op is null or the
+// level does not qualify (see Ctx::sweep_fusion); the caller then applies the
+// steps one by one.  Results are bit-identical to two smooth_step calls; only
+// the summation order of the optional rho reduction differs.
 template <class V>
-bool smooth_pair(Ctx &c, const OpMat<V> &At, const GridPair &gp, const V *xA, const V *dbA, const V *dinv, V *sc,
+bool smooth_pair(Ctx &c, const Sweep2Op *op, const GridPair &gp, const V *xA, const V *dbA, const V *dinv, V *sc,
                  V *dout, int modeA, int modeB, const int *skip, const double *r_rho, RedArgs *red, int rho_kind,
                  double *z64);
 template <class V>

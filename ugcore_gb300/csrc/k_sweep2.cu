@@ -9,27 +9,31 @@
 // owns a 32 x TY column of the level's (x, y) plane and a chunk of its z
 // planes, and marches through the chunk one plane at a time:
 //   step A on plane p, for the block's vertices and a ring of one vertex:
-//       d1 = dA - At xA        (xA staged in a ring of 3 shared planes)
+//       d1 = dA - At xA        (xA staged in a ring of shared planes)
 //   step B on plane p - dir, for the block's vertices:
-//       d2 = d1 - At d1        (d1 kept in a second ring of 3 shared planes)
-// The block's operator rows are read from HBM once for both steps (kept in
-// registers between the steps for 15 diagonals, re-read from L2 for 27), and
-// the defect between the two steps never leaves the SM.  Consecutive z chunks
-// march in opposite directions, so the two chunks that both read a plane next
-// to their common boundary read it at about the same time (the second read
-// comes from L2).
+//       d2 = d1 - At d1        (d1 kept in a second ring of shared planes)
+// The block's operator tile of a plane (all diagonals, the block's lines and
+// the ring) arrives with ONE tiled TMA load into shared memory, issued one
+// plane ahead and completed on an mbarrier; the rows are read from HBM once
+// for both steps, and the defect between the steps never leaves the SM.
+// Consecutive z chunks march in opposite directions, so the two chunks that
+// both read a plane next to their common boundary read it at about the same
+// time (the second read comes from L2).
 //
-// In post-smoothing the structured prolongation (StdTransfer::prolongate,
-// std_transfer_impl.h:721) is folded into step A: the staged xA is
-// w = (P sc_c) * dfac, formed from the coarse correction while the plane is
-// staged, and the block's rows add P sc_c to sc before step A's increment.
+// TMA needs 16-byte multiples for the strides of the tensor it reads, so the
+// operator is kept a second time for this kernel with every grid line padded
+// to a multiple of 4 values: value (x, y, z) of diagonal k at
+// ((k*nz + z)*ny + y)*xpad + x.  The tensor map gives the hardware the level
+// extents, and it fills everything outside them with zeros.
 //
-// The level operator is the column-scaled At = A diag(dinv) in the
-// constant-offset layout: diagonal k couples vertex (x, y, z) with
-// (x+dx_k, y+dy_k, z+dz_k); an entry whose neighbour lies outside the level is
-// stored as 0 and multiplies a staged 0 here.  Each row update runs through
-// the explicitly rounded helpers of k_solve.cuh in the diagonal order of the
-// one-step kernels, so sc and the defects are bit-identical to theirs.
+// The level operator is the column-scaled At = A diag(dinv): diagonal k
+// couples vertex (x, y, z) with (x+dx_k, y+dy_k, z+dz_k); an entry whose
+// neighbour lies outside the level is 0 (checked at set-up).  Each row update
+// runs through the explicitly rounded helpers of k_solve.cuh in the diagonal
+// order of the one-step kernels, so sc and the defects are bit-identical to
+// theirs.
+#include <cuda.h>
+
 #include "k_solve.cuh"
 
 namespace ug4gb {
@@ -38,8 +42,6 @@ namespace {
 
 template <class V>
 struct Sweep2Args {
-    const V *__restrict__ val;   // At, constant-offset layout
-    int ld;                      // stride between diagonals
     int nx, ny, nz;              // level vertices per direction
     int tz, ntx, nty;            // z planes per block, blocks along x and y
     const V *__restrict__ xA;    // step A's x
@@ -53,6 +55,7 @@ struct Sweep2Args {
     RedArgs red;
     int rho_kind;
     double *__restrict__ z64;
+    int *err;                    // set when a bounded wait for the block's own copies runs out
 };
 
 // The stencils of the structured levels, in the order of the constant-offset
@@ -84,7 +87,8 @@ struct Stencil3<15> {
     __host__ __device__ static constexpr int dz(int k) { return k < 4 ? -1 : (k < 11 ? 0 : 1); }
 };
 
-// 4- or 8-byte asynchronous copy global -> shared; zero fill when !valid
+// ---- asynchronous copies ----------------------------------------------------
+// 4- or 8-byte copy global -> shared (cp.async); zero fill when !valid
 template <class T>
 __device__ __forceinline__ void cp_async(unsigned dst, const T *src, bool valid)
 {
@@ -99,53 +103,108 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
+// tiled TMA load of a 4D box at (c0, c1, c2, c3) into shared memory,
+// completion counted in bytes on an mbarrier
+__device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            unsigned bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for a phase of the block's own copies: gives up after about a
+// second, reports it through *err and lets the kernel run to its end
+constexpr unsigned kWaitTries = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int *err)
+{
+    for (unsigned t = 0; t < kWaitTries; ++t)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (err) atomicExch(err, 1);
+    return false;
+}
+
 __device__ __forceinline__ int ring4(int p) { return (p + 4) & 3; }
 
-// widening of a level-precision value to FP64 (identity for FP64)
-__device__ __forceinline__ double widen(double v) { return v; }
+// widening of an FP32 level value to FP64 (integer path, as the one-step kernels)
 __device__ __forceinline__ double widen(float v) { return f32_to_f64(v); }
 
 // shared-memory plan of one block
 template <class V, int S, int TY>
 struct Sweep2Smem {
     static constexpr int NTH = 32 * TY;
-    static constexpr int XW = 36, XH = TY + 4, XP = XW * XH;   // staged xA: block columns + 2 on each side
-    static constexpr int DW = 34, DH = TY + 2, DP = DW * DH;   // ring region: block columns + 1 on each side
-    static constexpr int NX = (XP + NTH - 1) / NTH;            // staged xA elements per thread
-    // byte offsets: FP64 r_rho first (8-byte alignment), then level-precision buffers
-    static constexpr size_t RR = 0;                                  // [2][NTH] double
-    static constexpr size_t M = RR + 2 * NTH * sizeof(double);       // [2][S][DP] operator tiles
-    static constexpr size_t X = M + 2 * S * DP * sizeof(V);          // [4][XP] staged xA planes
+    static constexpr int NL = TY + 2;                            // grid lines of step A (block + ring)
+    static constexpr int LW = 40;                                // values per line of the operator box: x0-4 .. x0+35
+    static constexpr int XW = 36, XH = TY + 4, XP = XW * XH;     // staged xA: block columns + 2 on each side
+    static constexpr int DW = 34, DH = TY + 2, DP = DW * DH;     // ring region: block columns + 1 on each side
+    static constexpr int NX = (XP + NTH - 1) / NTH;              // staged xA elements per thread
+    static constexpr int MT = S * NL * LW;                       // operator box of one plane (elements)
+    static constexpr size_t MTB = (MT * sizeof(V) + 127) / 128 * 128;
+    // byte offsets (TMA destinations 128-byte aligned)
+    static constexpr size_t BAR = 0;                                 // 2 mbarriers
+    static constexpr size_t M = 128;                                 // [2] operator boxes [S][NL][LW]
+    static constexpr size_t RR = M + 2 * MTB;                        // [2][NTH] double
+    static constexpr size_t X = RR + 2 * NTH * sizeof(double);       // [4][XP] staged xA planes
     static constexpr size_t D = X + 4 * XP * sizeof(V);              // [4][DP] d1 planes
     static constexpr size_t B = D + 4 * DP * sizeof(V);              // [2][DP] step A's defect (dbA != xA)
     static constexpr size_t SC = B + 2 * DP * sizeof(V);             // [2][NTH] sc of the block's rows
     static constexpr size_t DI = SC + 2 * NTH * sizeof(V);           // [2][NTH] dinv of the block's rows
-    static constexpr size_t BYTES = DI + 2 * NTH * sizeof(V);
+    static constexpr size_t BYTES = DI + 2 * NTH * sizeof(V) + 128;   // + slack to align the base to 128
 };
 
 // Software pipeline over the planes of the block's chunk.  Iteration p:
-//   wait for the copies of plane p (operator tile of the ring region, step
-//   A's defect, the block's sc and dinv) and of xA plane p+dir, issued one
-//   iteration earlier; issue the copies of plane p+dir and xA plane p+2dir;
-//   step A on plane p; step B on plane p-dir.
-// Every position outside the level is zero-filled by the copies (operator
-// entries and vectors alike), so step A gives d1 = 0 there without a branch.
-// Planes live in rings of 4 buffers: plane p in slot (p + 4) & 3.
+//   wait for the copies of plane p (issued one iteration earlier): the
+//   operator box (one TMA load on the mbarrier of its buffer) and step A's
+//   defect, the block's sc, dinv and r_rho, and xA plane p+dir (cp.async,
+//   zero-filled outside the level); issue the copies of plane p+dir and xA
+//   plane p+2dir; step A on plane p; step B on plane p-dir.
+// Planes live in rings of 4 buffers (plane p in slot (p + 4) & 3), operator
+// boxes in 2 (parity of p).  The box of plane p starts at (x0-4, y0-1, p, 0):
+// a 16-byte aligned x, the block's lines and the ring, all diagonals.
 template <class V, int S, int TY, bool RHO>
-__global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2) k_sweep2(const Sweep2Args<V> a)
+__global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2)
+    k_sweep2(const __grid_constant__ CUtensorMap tmap, const Sweep2Args<V> a)
 {
     using SM = Sweep2Smem<V, S, TY>;
     using ST = Stencil3<S>;
-    constexpr int NTH = SM::NTH, XW = SM::XW, XP = SM::XP, DW = SM::DW, DP = SM::DP, NX = SM::NX;
+    constexpr int NTH = SM::NTH, NL = SM::NL, LW = SM::LW, XW = SM::XW, XP = SM::XP, DW = SM::DW, DP = SM::DP;
+    constexpr int NX = SM::NX, MT = SM::MT;
+    constexpr int MTE = (int)(SM::MTB / sizeof(V));   // elements between the two operator buffers
     constexpr int NRING = 2 * DW + 2 * TY;
-    extern __shared__ __align__(16) unsigned char smem[];
-    double *RR = reinterpret_cast<double *>(smem + SM::RR);
-    V *M = reinterpret_cast<V *>(smem + SM::M);
-    V *X = reinterpret_cast<V *>(smem + SM::X);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // the plan starts at the first 128-byte boundary of the dynamic window
+    unsigned char *smem = smem_raw + ((128u - (smem_addr(smem_raw) & 127u)) & 127u);
+    const V *M = reinterpret_cast<const V *>(smem + SM::M);
+    const double *RR = reinterpret_cast<const double *>(smem + SM::RR);
+    const V *X = reinterpret_cast<const V *>(smem + SM::X);
     V *D = reinterpret_cast<V *>(smem + SM::D);
-    V *B = reinterpret_cast<V *>(smem + SM::B);
-    V *SC = reinterpret_cast<V *>(smem + SM::SC);
-    V *DI = reinterpret_cast<V *>(smem + SM::DI);
+    const V *B = reinterpret_cast<const V *>(smem + SM::B);
+    const V *SC = reinterpret_cast<const V *>(smem + SM::SC);
+    const V *DI = reinterpret_cast<const V *>(smem + SM::DI);
+    const unsigned s0 = smem_addr(smem);
+    const unsigned sBar = s0 + SM::BAR, sM = s0 + SM::M, sX = s0 + SM::X, sB = s0 + SM::B, sSC = s0 + SM::SC,
+                   sDI = s0 + SM::DI, sRR = s0 + SM::RR;
     PDL_ENTRY();
     if (a.skip && *a.skip) return;
 
@@ -158,7 +217,6 @@ __global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2) k_sweep2(const Sweep
     const int x0 = bx * 32, y0 = by * TY;
     const int z0 = bz * a.tz, z1 = min(z0 + a.tz, nz);
     const int dir = (bz & 1) ? -1 : 1;
-    const size_t ld = (size_t)a.ld;
     const bool sep_db = a.dbA != nullptr;
     const bool read_sc = a.modeA != SC_SET_FROM_BASE;
 
@@ -196,8 +254,13 @@ __global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2) k_sweep2(const Sweep
         xin[j] = e < XP && x >= 0 && x < nx && y >= 0 && y < ny;
         xgi[j] = xin[j] ? x + nx * y : 0;
     }
-    const unsigned sM = smem_addr(M), sX = smem_addr(X), sB = smem_addr(B), sSC = smem_addr(SC),
-                   sDI = smem_addr(DI), sRR = smem_addr(RR);
+
+    if (tid == 0) {
+        mbar_init(sBar, 1);
+        mbar_init(sBar + 8, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
 
     auto stage_x = [&](int pl) {
         const bool zin = pl >= 0 && pl < nz;
@@ -213,82 +276,89 @@ __global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2) k_sweep2(const Sweep
     auto issue = [&](int p) {
         const int mb = p & 1;
         const bool zin = p >= 0 && p < nz;
-        const int po = zin ? p * PS : 0;
-        const unsigned mdst = sM + (unsigned)(mb * S * DP * sizeof(V));
-        {
-            const bool in = zin && own;
-            const int i = po + ogi;
-            const V *src = a.val + i;
-#pragma unroll
-            for (int k = 0; k < S; ++k)
-                cp_async(mdst + (unsigned)((k * DP + opos) * sizeof(V)), src + k * ld, in);
-            if (sep_db) cp_async(sB + (unsigned)((mb * DP + opos) * sizeof(V)), a.dbA + i, in);
-            if (in && p >= z0 && p < z1) {
-                if (read_sc) cp_async(sSC + (unsigned)((mb * NTH + tid) * sizeof(V)), a.sc + i, true);
-                cp_async(sDI + (unsigned)((mb * NTH + tid) * sizeof(V)), a.dinv + i, true);
-            }
-            // r_rho of plane p - dir: used by step B one iteration after this copy
-            const int q = p - dir;
-            if (RHO && own && q >= z0 && q < z1)
-                cp_async(sRR + (unsigned)((mb * NTH + tid) * sizeof(double)), a.r_rho + (q * PS + ogi), true);
+        if (tid == 0) {
+            // the block's reads of this buffer (its previous use, ordered by the
+            // barrier before this call) precede the asynchronous copy into it
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive_expect_tx(sBar + 8 * mb, (unsigned)(MT * sizeof(V)));
+            tma_load_4d(sM + (unsigned)(mb * SM::MTB), &tmap, x0 - 4, y0 - 1, p, 0, sBar + 8 * mb);
         }
-        if (tid < NRING) {
-            const bool in = zin && ring_in;
-            const int i = po + rgi;
-            const V *src = a.val + i;
-#pragma unroll
-            for (int k = 0; k < S; ++k)
-                cp_async(mdst + (unsigned)((k * DP + rpos) * sizeof(V)), src + k * ld, in);
-            if (sep_db) cp_async(sB + (unsigned)((mb * DP + rpos) * sizeof(V)), a.dbA + i, in);
+        const bool in = zin && own;
+        const int i = (zin ? p * PS : 0) + ogi;
+        if (sep_db) cp_async(sB + (unsigned)((mb * DP + opos) * sizeof(V)), a.dbA + i, in);
+        if (in && p >= z0 && p < z1) {
+            if (read_sc) cp_async(sSC + (unsigned)((mb * NTH + tid) * sizeof(V)), a.sc + i, true);
+            cp_async(sDI + (unsigned)((mb * NTH + tid) * sizeof(V)), a.dinv + i, true);
         }
+        // r_rho of plane p - dir: used by step B one iteration after this copy
+        const int q = p - dir;
+        if (RHO && own && q >= z0 && q < z1)
+            cp_async(sRR + (unsigned)((mb * NTH + tid) * sizeof(double)), a.r_rho + (q * PS + ogi), true);
+        if (sep_db && tid < NRING)
+            cp_async(sB + (unsigned)((mb * DP + rpos) * sizeof(V)), a.dbA + ((zin ? p * PS : 0) + rgi), zin && ring_in);
         stage_x(p + dir);
         cp_async_commit();
     };
 
-    V acur[S];   // operator row of this thread's vertex on the plane step B works on next
+    V acur[S], anew[S];   // operator row of this thread's vertex: plane of step B / of step A
     V sc_cur = (V)0, di_cur = (V)0, sc_new = (V)0, di_new = (V)0;
     double rsum = 0.0;
+    unsigned phase = 0;   // bit b: parity of the next phase of operator buffer b
+    bool ok = true;
 
     const int pstart = dir > 0 ? z0 - 1 : z1, pend = dir > 0 ? z1 + 1 : z0 - 2;
     stage_x(pstart - dir);
     stage_x(pstart);
     issue(pstart);
     for (int p = pstart; p != pend; p += dir) {
+        const int mb = p & 1;
         cp_async_wait_all();
+        if (ok) ok = mbar_wait(sBar + 8 * mb, (phase >> mb) & 1u, a.err);
+        phase ^= 1u << mb;
         __syncthreads();
         if (p + dir != pend) issue(p + dir);
-        const int mb = p & 1;
-        const V *Mo = M + mb * S * DP + opos;
-        // ---- step A on plane p (block rows and ring; zero-filled outside)
+        const bool zin = p >= 0 && p < nz;
+        const V *Mo = M + mb * MTE + (ty + 1) * LW + tx + 4;
+        // ---- step A on plane p (block rows and ring)
         {
-            const V *xm = X + ring4(p - 1) * XP, *xc = X + ring4(p) * XP, *xp = X + ring4(p + 1) * XP;
-            const V *xom = xm + oxs, *xoc = xc + oxs, *xop = xp + oxs;
-            V acc = (V)0;
-#pragma unroll
-            for (int k = 0; k < S; ++k) {
-                const V *pl = ST::dz(k) < 0 ? xom : (ST::dz(k) > 0 ? xop : xoc);
-                acc = fma_rn(Mo[k * DP], pl[ST::dy(k) * XW + ST::dx(k)], acc);
-            }
-            const V db = sep_db ? B[mb * DP + opos] : xoc[0];
+            const V *xom = X + ring4(p - 1) * XP + oxs, *xoc = X + ring4(p) * XP + oxs,
+                    *xop = X + ring4(p + 1) * XP + oxs;
             V *d1 = D + ring4(p) * DP;
-            if (own && p >= z0 && p < z1) {
-                const V so = read_sc ? SC[mb * NTH + tid] : (V)0;
-                di_new = DI[mb * NTH + tid];
-                d1[opos] = jacobi_row<V>(acc, db, di_new, a.modeA, so, sc_new);
-            } else {
-                d1[opos] = sub_rn(db, acc);
-            }
-            if (tid < NRING) {
-                const V *Mr = M + mb * S * DP + rpos;
-                const V *xrm = xm + rxs, *xrc = xc + rxs, *xrp = xp + rxs;
-                V racc = (V)0;
+            V dn = (V)0;
+            if (zin && own) {
+                V acc = (V)0;
 #pragma unroll
                 for (int k = 0; k < S; ++k) {
-                    const V *pl = ST::dz(k) < 0 ? xrm : (ST::dz(k) > 0 ? xrp : xrc);
-                    racc = fma_rn(Mr[k * DP], pl[ST::dy(k) * XW + ST::dx(k)], racc);
+                    const V *pl = ST::dz(k) < 0 ? xom : (ST::dz(k) > 0 ? xop : xoc);
+                    anew[k] = Mo[k * NL * LW];
+                    acc = fma_rn(anew[k], pl[ST::dy(k) * XW + ST::dx(k)], acc);
                 }
-                const V rdb = sep_db ? B[mb * DP + rpos] : xrc[0];
-                d1[rpos] = sub_rn(rdb, racc);
+                const V db = sep_db ? B[mb * DP + opos] : xoc[0];
+                if (p >= z0 && p < z1) {
+                    const V so = read_sc ? SC[mb * NTH + tid] : (V)0;
+                    di_new = DI[mb * NTH + tid];
+                    dn = jacobi_row<V>(acc, db, di_new, a.modeA, so, sc_new);
+                } else {
+                    dn = sub_rn(db, acc);
+                }
+            }
+            d1[opos] = dn;
+            if (tid < NRING) {
+                V rdn = (V)0;
+                if (zin && ring_in) {
+                    const V *Mr = M + mb * MTE + rry * LW + rrx + 3;
+                    const V *xrm = X + ring4(p - 1) * XP + rxs, *xrc = X + ring4(p) * XP + rxs,
+                            *xrp = X + ring4(p + 1) * XP + rxs;
+                    V racc = (V)0;
+#pragma unroll
+                    for (int k = 0; k < S; ++k) {
+                        const V *pl = ST::dz(k) < 0 ? xrm : (ST::dz(k) > 0 ? xrp : xrc);
+                        racc = fma_rn(Mr[k * NL * LW], pl[ST::dy(k) * XW + ST::dx(k)], racc);
+                    }
+                    const V rdb = sep_db ? B[mb * DP + rpos] : xrc[0];
+                    rdn = sub_rn(rdb, racc);
+                }
+                d1[rpos] = rdn;
             }
         }
         __syncthreads();
@@ -304,19 +374,18 @@ __global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2) k_sweep2(const Sweep
                 acc = fma_rn(acur[k], pl[ST::dy(k) * DW + ST::dx(k)], acc);
             }
             V s;
-            const V dn = jacobi_row<V>(acc, dc[0], di_cur, a.modeB, sc_cur, s);
+            const V dnb = jacobi_row<V>(acc, dc[0], di_cur, a.modeB, sc_cur, s);
             const int i = q * PS + ogi;
             a.sc[i] = s;
-            if (a.dout) a.dout[i] = dn;
+            if (a.dout) a.dout[i] = dnb;
             if (RHO || a.z64) {
                 const double s64 = widen(s);
                 if (a.z64) a.z64[i] = s64;
                 if (RHO) rsum += s64 * RR[mb * NTH + tid];
             }
         }
-        // plane p's tile stays in place until the next iteration's wait
 #pragma unroll
-        for (int k = 0; k < S; ++k) acur[k] = Mo[k * DP];
+        for (int k = 0; k < S; ++k) acur[k] = anew[k];
         sc_cur = sc_new;
         di_cur = di_new;
     }
@@ -399,49 +468,131 @@ __global__ void k_count_wrapped(const V *__restrict__ val, int ld, int S, Stenci
     if (bad) atomicAdd(count, bad);
 }
 
-template <class V, int S, bool RHO>
-void launch_sweep2(Ctx &c, const Sweep2Args<V> &a, int blocks)
+// the padded operator copy: value (x, y, z) of diagonal k at ((k*nz + z)*ny + y)*xpad + x
+__global__ void k_pad_operator(const float *__restrict__ val, int ld, int S, int nx, int ny, int nz, int xpad,
+                               float *__restrict__ out)
 {
-    constexpr size_t bytes = Sweep2Smem<V, S, kTY>::BYTES;
-    UG_LAUNCH_PDL(c, (k_sweep2<V, S, kTY, RHO>), blocks, 32 * kTY, bytes, a);
+    const size_t n = (size_t)nx * ny * nz, total = n * S;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t / n);
+        const int i = (int)(t - (size_t)k * n);
+        const int x = i % nx, yz = i / nx;   // yz = y + ny*z
+        out[((size_t)k * nz * ny + yz) * xpad + x] = val[(size_t)k * ld + i];
+    }
 }
 
-template <class V, int S>
+template <int S, bool RHO>
+void launch_sweep2(Ctx &c, const CUtensorMap &map, const Sweep2Args<float> &a, int blocks)
+{
+    constexpr size_t bytes = Sweep2Smem<float, S, kTY>::BYTES;
+    UG_LAUNCH_PDL(c, (k_sweep2<float, S, kTY, RHO>), blocks, 32 * kTY, bytes, map, a);
+}
+
+template <int S>
 void sweep2_attributes()
 {
-    const int bytes = (int)Sweep2Smem<V, S, kTY>::BYTES;
-    UG_CUDA(cudaFuncSetAttribute(k_sweep2<V, S, kTY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    UG_CUDA(cudaFuncSetAttribute(k_sweep2<V, S, kTY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    const int bytes = (int)Sweep2Smem<float, S, kTY>::BYTES;
+    UG_CUDA(cudaFuncSetAttribute(k_sweep2<float, S, kTY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    UG_CUDA(cudaFuncSetAttribute(k_sweep2<float, S, kTY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                 const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_tiled()
+{
+    static EncodeTiled fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        UG_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        UG_REQUIRE(p && q == cudaDriverEntryPointSuccess, UG4GB_ERR_CUDA, "cuTensorMapEncodeTiled not available");
+        fn = reinterpret_cast<EncodeTiled>(p);
+    }
+    return fn;
 }
 
 }  // namespace
 
+struct Sweep2Op {
+    CUtensorMap map;        // 4D (x, y, z, diagonal) over pad, box 40 x (TY+2) x 1 x S
+    DevBuf<float> pad;      // the operator with 16-byte aligned grid lines
+    int S = 0, nx = 0, ny = 0, nz = 0;
+};
+
 template <class V>
-bool smooth_pair(Ctx &c, const OpMat<V> &At, const GridPair &gp, const V *xA, const V *dbA, const V *dinv, V *sc,
+std::shared_ptr<Sweep2Op> sweep2_prepare(Ctx &c, const OpMat<V> &At, const GridPair &gp)
+{
+    if constexpr (sizeof(V) != 4) {
+        return nullptr;   // FP64 steps are bound by the FP64 FMA rate, not by operator bytes
+    } else {
+        if (At.kind != 1 || gp.dim != 3) return nullptr;
+        const Dia<V> &D = At.dia;
+        if (D.S != 15 && D.S != 27) return nullptr;
+        if ((int64_t)gp.nx * gp.ny * gp.nz != D.nrows || D.nrows != D.ncols) return nullptr;
+        if (!stencil_matches(D.off.o, D.S, gp.nx, gp.ny)) return nullptr;
+        Stencil st{};
+        if (!decode_offsets(D.off.o, D.S, gp.nx, gp.ny, st.dx, st.dy, st.dz)) return nullptr;
+        DevBuf<unsigned int> cnt;
+        cnt.alloc(1);
+        UG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned int), c.stream));
+        UG_LAUNCH(c, k_count_wrapped<V>, row_grid(c, D.nrows), 256, 0, D.vals(), D.ld, D.S, st, gp.nx, gp.ny, gp.nz,
+                  cnt.p);
+        unsigned int bad = 0;
+        UG_CUDA(cudaMemcpyAsync(&bad, cnt.p, sizeof(bad), cudaMemcpyDeviceToHost, c.stream));
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        if (bad) return nullptr;
+
+        auto op = std::make_shared<Sweep2Op>();
+        op->S = D.S;
+        op->nx = gp.nx;
+        op->ny = gp.ny;
+        op->nz = gp.nz;
+        const int xpad = (gp.nx + 3) / 4 * 4;
+        const size_t total = (size_t)D.S * gp.nz * gp.ny * xpad;
+        op->pad.alloc(total);
+        UG_CUDA(cudaMemsetAsync(op->pad.p, 0, op->pad.bytes(), c.stream));
+        UG_LAUNCH(c, k_pad_operator, c.num_sms * 8, 256, 0, D.vals(), D.ld, D.S, gp.nx, gp.ny, gp.nz, xpad, op->pad.p);
+        const cuuint64_t dims[4] = {(cuuint64_t)gp.nx, (cuuint64_t)gp.ny, (cuuint64_t)gp.nz, (cuuint64_t)D.S};
+        const cuuint64_t strides[3] = {(cuuint64_t)xpad * 4, (cuuint64_t)xpad * gp.ny * 4,
+                                       (cuuint64_t)xpad * gp.ny * gp.nz * 4};
+        const cuuint32_t box[4] = {(cuuint32_t)Sweep2Smem<float, 15, kTY>::LW, (cuuint32_t)(kTY + 2), 1,
+                                   (cuuint32_t)D.S};
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        const CUresult r = encode_tiled()(&op->map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, op->pad.p, dims, strides, box,
+                                          estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        UG_REQUIRE(r == CUDA_SUCCESS, UG4GB_ERR_CUDA, "cuTensorMapEncodeTiled failed for the fused smoother");
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        // dynamic shared memory above 48 KB is opted into once, outside any capture
+        if (D.S == 15) sweep2_attributes<15>();
+        else sweep2_attributes<27>();
+        return op;
+    }
+}
+
+template <class V>
+bool smooth_pair(Ctx &c, const Sweep2Op *op, const GridPair &gp, const V *xA, const V *dbA, const V *dinv, V *sc,
                  V *dout, int modeA, int modeB, const int *skip, const double *r_rho, RedArgs *red, int rho_kind,
                  double *z64)
 {
     if constexpr (sizeof(V) != 4) {
-        return false;   // FP64 steps are bound by the FP64 FMA rate, not by operator bytes
+        return false;
     } else {
-        if (!(c.sweep_fusion & 1) || At.kind != 1 || gp.dim != 3) return false;
-        const Dia<V> &D = At.dia;
-        if (D.S != 15 && D.S != 27) return false;
-        const int nx = gp.nx, ny = gp.ny, nz = gp.nz;
-        if ((int64_t)nx * ny * nz != D.nrows || D.nrows != D.ncols) return false;
-        if (!(c.sweep_fusion & 2) && D.nrows < c.sweep_fusion_min_rows) return false;
+        if (!op || !(c.sweep_fusion & 1)) return false;
+        if (op->nx != gp.nx || op->ny != gp.ny || op->nz != gp.nz) return false;
+        const int64_t n = (int64_t)gp.nx * gp.ny * gp.nz;
+        if (!(c.sweep_fusion & 2) && n < c.sweep_fusion_min_rows) return false;
         if (modeB == SC_SET_FROM_BASE) return false;
-        Sweep2Args<V> a{};
-        if (!stencil_matches(D.off.o, D.S, nx, ny)) return false;
-        a.val = D.val.p;
-        a.ld = D.ld;
-        a.nx = nx;
-        a.ny = ny;
-        a.nz = nz;
+        Sweep2Args<float> a{};
+        a.nx = gp.nx;
+        a.ny = gp.ny;
+        a.nz = gp.nz;
         a.tz = c.sweep_fusion_tz > 0 ? c.sweep_fusion_tz : 16;
-        a.ntx = (int)div_up(nx, 32);
-        a.nty = (int)div_up(ny, kTY);
-        const int nzc = (int)div_up(nz, a.tz);
+        a.ntx = (int)div_up(gp.nx, 32);
+        a.nty = (int)div_up(gp.ny, kTY);
+        const int nzc = (int)div_up(gp.nz, a.tz);
         const int64_t blocks = (int64_t)a.ntx * a.nty * nzc;
         if (blocks > kRedMaxBlocks) return false;
         a.xA = xA;
@@ -456,53 +607,26 @@ bool smooth_pair(Ctx &c, const OpMat<V> &At, const GridPair &gp, const V *xA, co
         if (red) a.red = *red;
         a.rho_kind = rho_kind;
         a.z64 = z64;
+        a.err = c.dev_err.p;
+        c.dev_err_possible = true;
         const bool rho = r_rho != nullptr;
-        if (D.S == 15) {
-            if (rho) launch_sweep2<V, 15, true>(c, a, (int)blocks);
-            else launch_sweep2<V, 15, false>(c, a, (int)blocks);
+        if (op->S == 15) {
+            if (rho) launch_sweep2<15, true>(c, op->map, a, (int)blocks);
+            else launch_sweep2<15, false>(c, op->map, a, (int)blocks);
         } else {
-            if (rho) launch_sweep2<V, 27, true>(c, a, (int)blocks);
-            else launch_sweep2<V, 27, false>(c, a, (int)blocks);
+            if (rho) launch_sweep2<27, true>(c, op->map, a, (int)blocks);
+            else launch_sweep2<27, false>(c, op->map, a, (int)blocks);
         }
         return true;
     }
 }
 
-template <class V>
-bool sweep2_supported(Ctx &c, const OpMat<V> &At, const GridPair &gp)
-{
-    if constexpr (sizeof(V) != 4) {
-        return false;
-    } else {
-        if (At.kind != 1 || gp.dim != 3) return false;
-        const Dia<V> &D = At.dia;
-        if (D.S != 15 && D.S != 27) return false;
-        if ((int64_t)gp.nx * gp.ny * gp.nz != D.nrows || D.nrows != D.ncols) return false;
-        if (!stencil_matches(D.off.o, D.S, gp.nx, gp.ny)) return false;
-        Stencil st{};
-        if (!decode_offsets(D.off.o, D.S, gp.nx, gp.ny, st.dx, st.dy, st.dz)) return false;
-        DevBuf<unsigned int> cnt;
-        cnt.alloc(1);
-        UG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(unsigned int), c.stream));
-        UG_LAUNCH(c, k_count_wrapped<V>, row_grid(c, D.nrows), 256, 0, D.val.p, D.ld, D.S, st, gp.nx, gp.ny, gp.nz,
-                  cnt.p);
-        unsigned int bad = 0;
-        UG_CUDA(cudaMemcpyAsync(&bad, cnt.p, sizeof(bad), cudaMemcpyDeviceToHost, c.stream));
-        UG_CUDA(cudaStreamSynchronize(c.stream));
-        if (bad) return false;
-        // dynamic shared memory above 48 KB is opted into once, outside any capture
-        if (D.S == 15) sweep2_attributes<V, 15>();
-        else sweep2_attributes<V, 27>();
-        return true;
-    }
-}
-template bool sweep2_supported<float>(Ctx &, const OpMat<float> &, const GridPair &);
-template bool sweep2_supported<double>(Ctx &, const OpMat<double> &, const GridPair &);
-
-template bool smooth_pair<float>(Ctx &, const OpMat<float> &, const GridPair &, const float *, const float *,
+template std::shared_ptr<Sweep2Op> sweep2_prepare<float>(Ctx &, const OpMat<float> &, const GridPair &);
+template std::shared_ptr<Sweep2Op> sweep2_prepare<double>(Ctx &, const OpMat<double> &, const GridPair &);
+template bool smooth_pair<float>(Ctx &, const Sweep2Op *, const GridPair &, const float *, const float *,
                                  const float *, float *, float *, int, int, const int *, const double *, RedArgs *, int,
                                  double *);
-template bool smooth_pair<double>(Ctx &, const OpMat<double> &, const GridPair &, const double *, const double *,
+template bool smooth_pair<double>(Ctx &, const Sweep2Op *, const GridPair &, const double *, const double *,
                                   const double *, double *, double *, int, int, const int *, const double *,
                                   RedArgs *, int, double *);
 
