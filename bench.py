@@ -284,10 +284,11 @@ def run_ours(args, rank, world, local_rank):
                  "kernel_profile": profile_summary(prof_m)}
         del pm
 
-    target = adj = None
+    target = adj = conv = None
     if not args.no_extras:
         target = run_target(args, ctx, timed, world, hbm)
         adj = run_adjoint_grad(args, ctx, timed)
+        conv = run_convection_adjoint(args, ctx, timed, world, hbm)
 
     # ---- assembly throughput (top level, FP64 FV1 + CRS values + rhs)
     asm = None
@@ -329,6 +330,7 @@ def run_ours(args, rank, world, local_rank):
         "mixed": mixed,
         "variable_coefficient_tets": target,
         "adjoint_gradient": adj,
+        "convection_adjoint": conv,
         "assembly": asm,
         "clocks": clocks,
         "cpu_baseline": cpu,
@@ -395,6 +397,57 @@ def run_adjoint_grad(args, ctx, timed):
         out[prec + "_ms"] = (time.perf_counter() - t0) * 1e3 / args.steps
         out["dofs"], out["elements"] = prob.n, prob.num_elements
         del prob
+    return out
+
+
+def run_convection_adjoint(args, ctx, timed, world, hbm):
+    """3D convection-diffusion, 3^3 hexes refined 6 times (193^3 = 7,189,057
+    DoFs), D = 1e-2, v = curl of a 16-mode potential at cell Peclet 10, full
+    upwind: GMG-preconditioned BiCGStab to 1e-10 in FP64 and with the FP32
+    multigrid; then the adjoint of J = sum of u^2 over a seeded 10% vertex
+    subset: one transposed BiCGStab solve with the transposed multigrid plus
+    the source-gradient kernel (dJ/df per vertex).  Bytes per BiCGStab half
+    step are counted as one V-cycle plus one FP64 operator pass and six
+    vector passes."""
+    import numpy as np
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    out = {"workload": "3D convection-diffusion 193^3 hexes (7.19M DoFs), D=1e-2, cell Peclet 10, full upwind, "
+                       "GMG V(2,2) Jacobi(0.6)-BiCGStab to 1e-10; adjoint dJ/df for J = sum_S u^2"}
+    for prec in ("fp64", "mixed"):
+        p = problems.Problem(ctx, problems.config("c4", precision=prec))
+        for _ in range(min(args.warmup, 2)):
+            p.solve()
+        steps = max(2, args.steps // 3)
+        ms = max_over_ranks(timed(p.solve, steps), world)
+        st = p.solve()
+        sizes = level_sizes(p)
+        sv = 8 if prec == "fp64" else 4
+        gbs = iteration_bytes(sizes, sv) * st["steps"] / (ms * 1e-3) / 1e9
+        res = {"ms_per_solve": ms, "dofs_per_s": world * p.n / (ms * 1e-3), "bicgstab_half_steps": st["steps"],
+               "rel_residual": st["defect"] / st["initial_defect"], "solve_gbs": gbs,
+               "solve_frac_of_measured_hbm": gbs / hbm}
+        if prec == "mixed":
+            # adjoint: rhs = dJ/du on a seeded 10% subset, Dirichlet entries zero
+            u = p.x.numpy()
+            S = np.random.default_rng(p.cfg["seed"]).random(p.n) < 0.1
+            p.adjoint_solve(np.where(S, 2.0 * u, 0.0))      # builds A^T, the transposed multigrid, fills rhs
+            gf = ug.GPUVector(ctx, p.n)
+
+            def adjoint_step():
+                p.lam.set(0.0)
+                p.solverT.apply(p.lam, p.rhs)
+                p.disc.grad_source(p.lam, out=gf)
+            adjoint_step()
+            ms_a = max_over_ranks(timed(adjoint_step, steps), world)
+            sta = p.solverT.stats()
+            res["adjoint_ms"] = ms_a
+            res["adjoint_half_steps"] = sta["steps"]
+            res["adjoint_rel_residual"] = sta["defect"] / sta["initial_defect"]
+        out[prec] = res
+        out["dofs"], out["nnz"] = p.n, sizes[-1]["nnz"]
+        del p
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["ms_per_solve"] / out["mixed"]["ms_per_solve"]
     return out
 
 
