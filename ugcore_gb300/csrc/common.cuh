@@ -274,14 +274,20 @@ __device__ __forceinline__ int ld_stream(const int *p) { return __ldcs(p); }
 // kernels that also produce or consume the FP32 multigrid vectors.  Normal
 // numbers and zeros take the integer path (widening is exact; narrowing
 // rounds to nearest, ties to even, as cvt.rn.f32.f64); subnormal, out-of-
-// range, infinite and NaN inputs fall back to the hardware conversion.
+// range, infinite and NaN inputs fall back to the hardware conversion.  The
+// fallbacks are separate, non-inlined functions so that the compiler cannot
+// turn the rare branch into a select that runs the FP64-pipe conversion for
+// every value.
+static __device__ __noinline__ double f32_to_f64_hw(float f) { return (double)f; }
+static __device__ __noinline__ float f64_to_f32_hw(double d) { return (float)d; }
+
 __device__ __forceinline__ double f32_to_f64(float f)
 {
     const unsigned int u = __float_as_uint(f);
     const unsigned int e = (u >> 23) & 0xffu;
     const unsigned long long sgn = (unsigned long long)(u >> 31) << 63;
     if (e == 0u && (u & 0x7fffffu) == 0u) return __longlong_as_double((long long)sgn);
-    if (e == 0u || e == 0xffu) return (double)f;
+    if (__builtin_expect(e == 0u || e == 0xffu, 0)) return f32_to_f64_hw(f);
     const unsigned long long bits =
         sgn | ((unsigned long long)(e + (1023u - 127u)) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
     return __longlong_as_double((long long)bits);
@@ -295,7 +301,7 @@ __device__ __forceinline__ float f64_to_f32(double d)
     const unsigned long long m = b & 0xfffffffffffffULL;
     if (e == 0 && m == 0) return __uint_as_float(sgn);
     int fe = e - 1023 + 127;
-    if (fe <= 0 || fe >= 255) return (float)d;
+    if (__builtin_expect(fe <= 0 || fe >= 255, 0)) return f64_to_f32_hw(d);
     unsigned int mant = (unsigned int)(m >> 29);
     const unsigned long long rest = m & ((1ULL << 29) - 1), half = 1ULL << 28;
     if (rest > half || (rest == half && (mant & 1u))) {
@@ -303,7 +309,7 @@ __device__ __forceinline__ float f64_to_f32(double d)
         if (mant == (1u << 23)) {
             mant = 0u;
             fe += 1;
-            if (fe >= 255) return (float)d;
+            if (__builtin_expect(fe >= 255, 0)) return f64_to_f32_hw(d);
         }
     }
     return __uint_as_float(sgn | ((unsigned int)fe << 23) | mant);
