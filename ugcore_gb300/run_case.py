@@ -3,6 +3,12 @@ statistics as JSON, e.g. to profile one precision or layout in isolation:
 
     python -m ugcore_gb300.run_case --config c2 --precision mixed --solves 2
     python -m ugcore_gb300.run_case --config c1 --nref 5 --format sell
+    python -m ugcore_gb300.run_case --config c2 --precision mixed --direct --sweep-fusion 1
+
+--direct runs the solves with the library profiler on: every kernel is
+launched directly instead of being replayed from the solve's CUDA graph
+(profilers cannot attribute kernels inside graphs with conditional nodes),
+and the per-kernel CUDA-event totals are printed with the statistics.
 
 Configurations: c0 2D Poisson 129^2 quads, c1 3D Poisson 129^3 hexes,
 c2 3D lognormal diffusion on Kuhn tets (129^3 vertices), c3 2D log-K field
@@ -21,6 +27,9 @@ def main():
     ap.add_argument("--smoother", choices=["jacobi", "mcgs"], default=None)
     ap.add_argument("--format", choices=["auto", "sell"], default="auto")
     ap.add_argument("--solves", type=int, default=1)
+    ap.add_argument("--direct", action="store_true")
+    ap.add_argument("--sweep-fusion", type=int, default=None)
+    ap.add_argument("--sweep-planes", type=int, default=None)
     args = ap.parse_args()
 
     import ugcore_gb300 as ug
@@ -34,18 +43,25 @@ def main():
         over["smoother"] = args.smoother
     ctx = ug.Context(0)
     ctx.set_operator_format(args.format)
+    ctx.set_tuning(sweep_fusion=args.sweep_fusion, sweep_planes=args.sweep_planes)
     t0 = time.perf_counter()
     p = problems.Problem(ctx, problems.config(args.config, **over))
     ctx.synchronize()
     setup = time.perf_counter() - t0
     out = []
+    if args.direct:
+        ctx.profile_begin()
     for _ in range(args.solves):
         t0 = time.perf_counter()
         st = p.solve()
         ctx.synchronize()
         out.append({"ms": (time.perf_counter() - t0) * 1e3, "steps": st["steps"],
                     "rel_residual": st["defect"] / st["initial_defect"]})
-    print(json.dumps({"config": args.config, "dofs": p.n, "setup_s": setup, "solves": out}))
+    res = {"config": args.config, "dofs": p.n, "setup_s": setup, "solves": out}
+    if args.direct:
+        prof = ctx.profile_end()
+        res["kernels"] = {k: [v[0], round(v[1], 4)] for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
+    print(json.dumps(res))
 
 
 if __name__ == "__main__":
