@@ -26,6 +26,7 @@ class Params(C.Structure):
         ("solver", C.c_int), ("smoother", C.c_int), ("damp", C.c_double),
         ("nu1", C.c_int), ("nu2", C.c_int), ("cycle", C.c_int), ("base", C.c_int),
         ("maxit", C.c_int), ("rel_red", C.c_double), ("min_defect", C.c_double),
+        ("rap", C.c_int),
     ]
 
 
@@ -68,6 +69,9 @@ def lib():
         L.orc_prob_transfer_nnz.argtypes = [P, C.c_int, C.c_int]
         L.orc_prob_transfer_nnz.restype = C.c_int64
         L.orc_prob_transfer.argtypes = [P, C.c_int, C.c_int, ip, ip, dp]
+        L.orc_prob_gmg_level_nnz.argtypes = [P, C.c_int]
+        L.orc_prob_gmg_level_nnz.restype = C.c_int64
+        L.orc_prob_gmg_level.argtypes = [P, C.c_int, ip, ip, dp]
         L.orc_prob_apply_gmg.argtypes = [P, dp, dp]
         L.orc_prob_solve.argtypes = [P, dp, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                      C.POINTER(C.c_double), P, C.c_int]
@@ -86,10 +90,10 @@ def lib():
 def make_params(elem_type=ORC_QUAD, mx=2, my=2, mz=2, nref=6, seed=1, coef_kind=0, coef_modes=64,
                 coef_kmax=8.0, vel_kind=0, vel_modes=16, vel_kmax=2.0, diffusion=1.0, peclet=10.0,
                 solver=0, smoother=0, damp=0.6, nu1=2, nu2=2, cycle=1, base=0, maxit=200,
-                rel_red=1e-10, min_defect=1e-300):
+                rel_red=1e-10, min_defect=1e-300, rap=0):
     return Params(elem_type, mx, my, mz, nref, seed, coef_kind, coef_modes, coef_kmax, vel_kind,
                   vel_modes, vel_kmax, diffusion, peclet, solver, smoother, damp, nu1, nu2, cycle,
-                  base, maxit, rel_red, min_defect)
+                  base, maxit, rel_red, min_defect, rap)
 
 
 class Problem:
@@ -128,6 +132,19 @@ class Problem:
         ci = np.zeros(nnz, np.int32)
         va = np.zeros(nnz, np.float64)
         L.orc_prob_level_matrix(self.h, l, rp, ci, va)
+        return rp, ci, va
+
+    def gmg_level_matrix(self, l):
+        """the multigrid's operator of level l (R A P of the level above with rap)"""
+        L = lib()
+        n = self.nv(l)
+        nnz = L.orc_prob_gmg_level_nnz(self.h, l)
+        if nnz < 0:
+            raise RuntimeError("gmg init failed")
+        rp = np.zeros(n + 1, np.int32)
+        ci = np.zeros(nnz, np.int32)
+        va = np.zeros(nnz, np.float64)
+        L.orc_prob_gmg_level(self.h, l, rp, ci, va)
         return rp, ci, va
 
     def transfer(self, l, which):

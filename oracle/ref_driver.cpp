@@ -17,8 +17,13 @@
  * The multigrid cycle is the restated AssembledMultiGridCycle control flow
  * (mg_solver_impl.hpp:176-275,1687-2140) driving the reference components.
  *
+ * With rap = 1 the coarse level operators are Galerkin products computed by
+ * the reference's own ug::AddMultiplyOf(A_c, R, A_f, P)
+ * (lib_algebra/algebra_common/sparsematrix_util.h:167), top level down, as
+ * AssembledMultiGridCycle::init_rap_operator (mg_solver_impl.hpp:830-1012).
+ *
  * Usage: ref_driver <out.bin> elem mx my mz nref seed coef_kind solver vel_kind
- *                   [diffusion peclet smoother damp nu1 nu2 maxit]
+ *                   [diffusion peclet smoother damp nu1 nu2 maxit rap]
  * Output (little-endian binary): header ints, per-level CRS, rhs, solution,
  * defect history.
  */
@@ -164,6 +169,7 @@ int main(int argc, char **argv)
     double damp = argc > 14 ? atof(argv[14]) : 0.6;
     int nu1 = argc > 15 ? atoi(argv[15]) : 2, nu2 = argc > 16 ? atoi(argv[16]) : 2;
     int maxit = argc > 17 ? atoi(argv[17]) : 200;
+    int rap = argc > 18 ? atoi(argv[18]) : 0;
 
     orc_hier H;
     if (orc_hier_create(&H, elem, mx, my, mz, nref)) return 3;
@@ -239,9 +245,19 @@ int main(int argc, char **argv)
                 Rm(c, v) = 1.0;
             }
             Pm.defragment(); Rm.defragment();
-            G->S[l] = SmartPtr<ILinearIterator<Vec> >(new Jacobi<CPUAlgebra>(damp));
-            G->S[l]->init(G->A[l]);
         }
+    }
+    if (rap) {
+        for (int l = top; l > 0; --l) {
+            Mat &Ac = G->A[l - 1]->get_matrix();
+            Ac.resize_and_clear(H.lev[l - 1].nv, H.lev[l - 1].nv);
+            AddMultiplyOf(Ac, *G->Rp[l], G->A[l]->get_matrix(), *G->Pp[l]);
+            Ac.defragment();
+        }
+    }
+    for (int l = 1; l < nl; ++l) {
+        G->S[l] = SmartPtr<ILinearIterator<Vec> >(new Jacobi<CPUAlgebra>(damp));
+        G->S[l]->init(G->A[l]);
     }
     G->lu = SmartPtr<ILinearOperatorInverse<Vec> >(new LU<CPUAlgebra>);
     G->lu->init(G->A[0]);

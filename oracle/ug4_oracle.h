@@ -139,10 +139,21 @@ typedef struct {
     int *ncolor;
     double **sc, **sd, **st;
     orc_lu lu;
+    orc_crs *Arap;       /* rap: owned level operators (coarse levels), else NULL */
 } orc_gmg;
 
+/* M = R A P (Galerkin coarse operator), AddMultiplyOf(M, R, A, P) with M
+   empty (lib_algebra/algebra_common/sparsematrix_util.h:167-241): per row i
+   the products R_ik A_kl P_lj in the order k (R's row), l (A's row), j (P's
+   row), zero entries skipped, each product rounded before it is added;
+   every column reached is stored (sorted), also when its sum is 0. */
+int orc_rap(const orc_crs *R, const orc_crs *A, const orc_crs *P, orc_crs *M);
+/* rap != 0: the levels below the top are R A P of the level above
+   (AssembledMultiGridCycle::init_rap_operator, mg_solver_impl.hpp:830-1012,
+   for a fully refined hierarchy); levA[top] is used as given, the coarse
+   operators are owned by the multigrid (G->Arap). */
 int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, double damp,
-                 int nu1, int nu2, int cycle, int base);
+                 int nu1, int nu2, int cycle, int base, int rap);
 void orc_gmg_apply(orc_gmg *G, double *c, const double *d);
 void orc_gmg_free(orc_gmg *G);
 

@@ -35,6 +35,7 @@ typedef struct {
     int nu1, nu2, cycle, base;
     int maxit;
     double rel_red, min_defect;
+    int rap;            /* 1: Galerkin coarse operators R A P instead of re-assembly */
 } orc_params;
 
 typedef struct {
@@ -148,10 +149,23 @@ static int ensure_gmg(orc_prob *P)
 {
     if (P->gmg_ready) return 0;
     const orc_params *p = &P->p;
-    int rc = orc_gmg_init(&P->G, &P->H, P->A, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base);
+    int rc = orc_gmg_init(&P->G, &P->H, P->A, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap);
     if (rc) return rc;
     P->gmg_ready = 1;
     return 0;
+}
+
+/* the multigrid's operator of level l (re-assembled, or R A P with rap) */
+int64_t orc_prob_gmg_level_nnz(orc_prob *P, int l)
+{
+    if (ensure_gmg(P)) return -1;
+    return P->G.A[l].nnz;
+}
+
+void orc_prob_gmg_level(orc_prob *P, int l, int *rowptr, int *col, double *val)
+{
+    if (ensure_gmg(P)) return;
+    crs_out(&P->G.A[l], rowptr, col, val);
 }
 
 int64_t orc_prob_transfer_nnz(orc_prob *P, int l, int which)
@@ -220,7 +234,8 @@ int orc_prob_adjoint(orc_prob *P, const double *g, double *lam, int *steps, doub
         for (int l = 0; l < nl; ++l)
             if (transpose_dirichlet(&P->A[l], &P->H.lev[l], &P->AT[l])) return -1;
         const orc_params *p = &P->p;
-        int rc = orc_gmg_init(&P->GT, &P->H, P->AT, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base);
+        int rc = orc_gmg_init(&P->GT, &P->H, P->AT, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base,
+                              p->rap);
         if (rc) return rc;
         P->gmgT_ready = 1;
     }

@@ -72,6 +72,64 @@ int orc_restriction(const orc_level *F, const orc_level *C, const orc_crs *P, or
     return 0;
 }
 
+/* ----------------------------------------------------- Galerkin R A P -- */
+static int cmp_int(const void *a, const void *b)
+{
+    int x = *(const int *)a, y = *(const int *)b;
+    return (x > y) - (x < y);
+}
+
+int orc_rap(const orc_crs *R, const orc_crs *A, const orc_crs *P, orc_crs *M)
+{
+    memset(M, 0, sizeof(*M));
+    const int nr = R->n_rows, nc = P->n_cols;
+    M->n_rows = nr; M->n_cols = nc;
+    double *acc = (double *)calloc((size_t)nc, sizeof(double));
+    int *mark = (int *)malloc(sizeof(int) * (size_t)nc);
+    int *list = (int *)malloc(sizeof(int) * (size_t)nc);
+    M->rowptr = (int *)calloc((size_t)nr + 1, sizeof(int));
+    int64_t cap = 16 * (int64_t)nr + 16;
+    M->col = (int *)malloc(sizeof(int) * (size_t)cap);
+    M->val = (double *)malloc(sizeof(double) * (size_t)cap);
+    if (!acc || !mark || !list || !M->rowptr || !M->col || !M->val) return -1;
+    for (int j = 0; j < nc; ++j) mark[j] = -1;
+    int64_t nnz = 0;
+    for (int i = 0; i < nr; ++i) {
+        int nl = 0;
+        for (int a = R->rowptr[i]; a < R->rowptr[i + 1]; ++a) {
+            if (R->val[a] == 0.0) continue;
+            const int k = R->col[a];
+            for (int b = A->rowptr[k]; b < A->rowptr[k + 1]; ++b) {
+                if (A->val[b] == 0.0) continue;
+                const int l = A->col[b];
+                const double ab = R->val[a] * A->val[b];
+                for (int c = P->rowptr[l]; c < P->rowptr[l + 1]; ++c) {
+                    if (P->val[c] == 0.0) continue;
+                    const int j = P->col[c];
+                    if (mark[j] != i) { mark[j] = i; acc[j] = 0.0; list[nl++] = j; }
+                    acc[j] = acc[j] + ab * P->val[c];
+                }
+            }
+        }
+        qsort(list, (size_t)nl, sizeof(int), cmp_int);
+        if (nnz + nl > cap) {
+            while (nnz + nl > cap) cap *= 2;
+            M->col = (int *)realloc(M->col, sizeof(int) * (size_t)cap);
+            M->val = (double *)realloc(M->val, sizeof(double) * (size_t)cap);
+            if (!M->col || !M->val) return -1;
+        }
+        for (int t = 0; t < nl; ++t) {
+            M->col[nnz] = list[t];
+            M->val[nnz] = acc[list[t]];
+            ++nnz;
+        }
+        M->rowptr[i + 1] = (int)nnz;
+    }
+    M->nnz = nnz;
+    free(acc); free(mark); free(list);
+    return 0;
+}
+
 /* ------------------------------------------------------------------ LU -- */
 int orc_lu_init(orc_lu *F, const orc_crs *A)
 {
@@ -127,7 +185,7 @@ void orc_lu_free(orc_lu *F) { free(F->LU); free(F->piv); F->LU = NULL; F->piv = 
 static double *dvec(int n) { return (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
 
 int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, double damp,
-                 int nu1, int nu2, int cycle, int base)
+                 int nu1, int nu2, int cycle, int base, int rap)
 {
     memset(G, 0, sizeof(*G));
     G->nlev = H->nlev; G->base = base; G->cycle = cycle; G->nu1 = nu1; G->nu2 = nu2;
@@ -135,6 +193,19 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
     G->A = levA;
     G->P = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
     G->R = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
+    if (rap) {
+        /* transfers first, then the coarse operators from the top down */
+        const int top = G->nlev - 1;
+        G->Arap = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
+        G->Arap[top] = levA[top];
+        for (int l = top; l > base; --l) {
+            if (orc_prolongation(&H->lev[l], &H->lev[l - 1], &G->P[l])) return -1;
+            if (orc_restriction(&H->lev[l], &H->lev[l - 1], &G->P[l], &G->R[l])) return -1;
+            if (orc_rap(&G->R[l], &G->Arap[l], &G->P[l], &G->Arap[l - 1])) return -1;
+        }
+        levA = G->Arap;
+        G->A = levA;
+    }
     G->diaginv = (double **)calloc((size_t)G->nlev, sizeof(double *));
     G->color = (int **)calloc((size_t)G->nlev, sizeof(int *));
     G->ncolor = (int *)calloc((size_t)G->nlev, sizeof(int));
@@ -146,8 +217,8 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
         int n = L->nv;
         G->sc[l] = dvec(n); G->sd[l] = dvec(n); G->st[l] = dvec(n);
         if (l > base) {
-            if (orc_prolongation(L, &H->lev[l - 1], &G->P[l])) return -1;
-            if (orc_restriction(L, &H->lev[l - 1], &G->P[l], &G->R[l])) return -1;
+            if (!rap && orc_prolongation(L, &H->lev[l - 1], &G->P[l])) return -1;
+            if (!rap && orc_restriction(L, &H->lev[l - 1], &G->P[l], &G->R[l])) return -1;
             G->diaginv[l] = dvec(n);
             for (int i = 0; i < n; ++i) {
                 double m = levA[l].val[orc_crs_find(&levA[l], i, i)];
@@ -261,6 +332,11 @@ void orc_gmg_free(orc_gmg *G)
     }
     free(G->P); free(G->R); free(G->diaginv); free(G->color); free(G->ncolor);
     free(G->sc); free(G->sd); free(G->st);
+    if (G->Arap) {
+        /* the top entry is the caller's operator (shallow copy) */
+        for (int l = 0; l < G->nlev - 1; ++l) orc_crs_free(&G->Arap[l]);
+        free(G->Arap);
+    }
     orc_lu_free(&G->lu);
     memset(G, 0, sizeof(*G));
 }

@@ -6,8 +6,11 @@ the reference sources by oracle/build_ref.sh) on small seeded problems and
 stores, per case: every level's CRS, the top level's P and R, the rhs, the
 solution, the defect history and the iteration count.
 
+The *_rap cases build the coarse operators as Galerkin products with
+ugcore's own AddMultiplyOf (the multigrid's set_rap(true) path).
+
 Usage (needs the reference tree, i.e. this container):
-    sh oracle/build_ref.sh && python tests/golden/make_golden.py
+    sh oracle/build_ref.sh && python tests/golden/make_golden.py [case ...]
 """
 import os
 import subprocess
@@ -26,6 +29,13 @@ CASES = {
     "tet_4x4x4_r1_lognormal": (2, 4, 4, 4, 1, 1, 1, 0, 0, 1.0, 10.0),
     "hex_3x3x3_r1_convection": (1, 3, 3, 3, 1, 1, 3, 1, 1, 1e-2, 10.0),
 }
+# + (smoother, damp, nu1, nu2, maxit, rap)
+RAP = (0, 0.6, 2, 2, 200, 1)
+CASES.update({
+    "hex_2x2x2_r2_rap": CASES["hex_2x2x2_r2"] + RAP,
+    "tet_4x4x4_r1_lognormal_rap": CASES["tet_4x4x4_r1_lognormal"] + RAP,
+    "hex_3x3x3_r1_convection_rap": CASES["hex_3x3x3_r1_convection"] + RAP,
+})
 
 
 def read_ref(path):
@@ -57,7 +67,9 @@ def read_ref(path):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build oracle/_ref first: sh oracle/build_ref.sh")
-    for name, c in CASES.items():
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        c = CASES[name]
         out = "/tmp/_golden_%s.bin" % name
         args = [DRIVER, out] + [str(v) if not isinstance(v, float) else repr(v) for v in c]
         subprocess.check_call(args, stdout=subprocess.DEVNULL)

@@ -26,7 +26,7 @@ def oracle_params(orc, cfg):
         vel_modes=cfg["vel_modes"], vel_kmax=cfg["vel_kmax"], diffusion=cfg["diffusion"], peclet=cfg["peclet"],
         solver=0 if cfg["solver"] == "cg" else 1, smoother=0 if cfg["smoother"] == "jacobi" else 1,
         damp=cfg["damp"], nu1=cfg["nu1"], nu2=cfg["nu2"], cycle=cfg["cycle"], base=cfg["base"], maxit=cfg["maxit"],
-        rel_red=cfg["rel_red"], min_defect=cfg["min_defect"])
+        rel_red=cfg["rel_red"], min_defect=cfg["min_defect"], rap=int(cfg.get("rap", 0)))
 
 
 def assert_crs_equal(a, b, rtol=VAL_RTOL, what="matrix"):

@@ -67,25 +67,33 @@ def test_transpose_matches_ugcore_golden(oracle_lib, case):
 
 
 # ---- fixtures from ugcore's algebra (tests/golden/make_golden.py) ----------
-GOLDEN_CASES = ["quad_2x2_r4", "hex_2x2x2_r2", "tet_4x4x4_r1_lognormal", "hex_3x3x3_r1_convection"]
+GOLDEN_CASES = ["quad_2x2_r4", "hex_2x2x2_r2", "tet_4x4x4_r1_lognormal", "hex_3x3x3_r1_convection",
+                "hex_2x2x2_r2_rap", "tet_4x4x4_r1_lognormal_rap", "hex_3x3x3_r1_convection_rap"]
 
 
 def _golden_problem(orc, g):
-    e, mx, my, mz, nref, seed, ck, solver, vk, diff, pe = g["params"]
+    e, mx, my, mz, nref, seed, ck, solver, vk, diff, pe = g["params"][:11]
+    extra = {}
+    if len(g["params"]) > 11:   # smoother, damp, nu1, nu2, maxit, rap
+        sm, damp, nu1, nu2, maxit, rap = g["params"][11:17]
+        extra = dict(smoother=int(sm), damp=float(damp), nu1=int(nu1), nu2=int(nu2), maxit=int(maxit), rap=int(rap))
     p = orc.make_params(elem_type=int(e), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
-                        coef_kind=int(ck), solver=int(solver), vel_kind=int(vk), diffusion=diff, peclet=pe)
-    return orc.Problem(p)
+                        coef_kind=int(ck), solver=int(solver), vel_kind=int(vk), diffusion=diff, peclet=pe, **extra)
+    return orc.Problem(p), bool(extra.get("rap", 0))
 
 
 @pytest.mark.parametrize("name", GOLDEN_CASES)
 def test_oracle_reproduces_ugcore_algebra(oracle_lib, name):
+    """level operators (re-assembled, or Galerkin R A P computed by ugcore's
+    AddMultiplyOf in the *_rap cases), transfers, rhs, solution and defect
+    history bit for bit"""
     g = load_golden(name)
     assert g is not None, "missing fixture " + name
-    P = _golden_problem(oracle_lib, g)
+    P, rap = _golden_problem(oracle_lib, g)
     nl = int(g["nlev"])
     assert P.nlev == nl
     for l in range(nl):
-        got = P.matrix(l)
+        got = P.gmg_level_matrix(l) if rap else P.matrix(l)
         ref = (g["A%d_rowptr" % l], g["A%d_col" % l], g["A%d_val" % l])
         assert_crs_equal(got, ref, rtol=0.0, what="level %d operator" % l)
     assert_crs_equal(P.transfer(nl - 1, 0), (g["P_rowptr"], g["P_col"], g["P_val"]), rtol=0.0, what="P")
