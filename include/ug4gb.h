@@ -217,14 +217,26 @@ UG4GB_API int ug4gb_gmg_set_precision(ug4gb_gmg *m, int precision);
 /* transposed = 1 builds the cycle on A^T of every level (Dirichlet rows reset
    to identity): the preconditioner of the adjoint solve */
 UG4GB_API int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed);
+/* AssembledMultiGridCycle::set_rap (mg_solver.h:149; Lua gmg:set_rap(true),
+   multigrid_bridge.cpp:214): rap = 1 makes every coarse level operator the
+   Galerkin product R A P of the level above (init_rap_operator,
+   mg_solver_impl.hpp:830-1012, with AddMultiplyOf, sparsematrix_util.h:167)
+   instead of re-assembling it; default 0 */
+UG4GB_API int ug4gb_gmg_set_rap(ug4gb_gmg *m, int rap);
 /* AssembledMultiGridCycle::init (mg_solver_impl.hpp:380): copies the top
-   operator, re-assembles coarser levels, builds P/R, smoothers and the LU */
+   operator, re-assembles coarser levels (or forms R A P), builds P/R,
+   smoothers and the LU */
 UG4GB_API int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top);
 /* c = B d (AssembledMultiGridCycle::apply, mg_solver_impl.hpp:176) */
 UG4GB_API int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *c, const ug4gb_vector *d);
 /* transfer operators of fine level `level`: which = 0 P, 1 R */
 UG4GB_API int ug4gb_gmg_transfer_info(const ug4gb_gmg *m, int level, int which, int *num_rows, int *num_cols,
                             int64_t *nnz);
+/* the multigrid's FP64 operator of a level (base..top): re-assembled, or
+   R A P with set_rap (what AssembledMultiGridCycle writes as "LevelMatrix"
+   through write_debug, mg_solver_impl.hpp:898-902,966-970) */
+UG4GB_API int ug4gb_gmg_level_info(const ug4gb_gmg *m, int level, int *num_rows, int64_t *nnz);
+UG4GB_API int ug4gb_gmg_export_level(const ug4gb_gmg *m, int level, int *rowptr, int *col, double *val);
 UG4GB_API int ug4gb_gmg_export_transfer(const ug4gb_gmg *m, int level, int which, int *rowptr, int *col, double *val);
 UG4GB_API void ug4gb_gmg_destroy(ug4gb_gmg *m);
 

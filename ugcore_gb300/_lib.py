@@ -98,6 +98,9 @@ _SIGS = {
     "ug4gb_gmg_set_base_level": (I, [P, I]),
     "ug4gb_gmg_set_precision": (I, [P, I]),
     "ug4gb_gmg_set_transposed": (I, [P, I]),
+    "ug4gb_gmg_set_rap": (I, [P, I]),
+    "ug4gb_gmg_level_info": (I, [P, I, P, P]),
+    "ug4gb_gmg_export_level": (I, [P, I, P, P, P]),
     "ug4gb_gmg_init": (I, [P, P]),
     "ug4gb_gmg_apply": (I, [P, P, P]),
     "ug4gb_gmg_transfer_info": (I, [P, I, I, PI, PI, PI64]),

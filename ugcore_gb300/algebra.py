@@ -422,6 +422,10 @@ class GeometricMultiGrid:
         p = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, 0: 0, 1: 1}[prec]
         check(lib().ug4gb_gmg_set_precision(self.h, p), self.ctx.h)
 
+    def set_rap(self, flag=True):
+        """Galerkin coarse operators R A P instead of re-assembly (set_rap)"""
+        check(lib().ug4gb_gmg_set_rap(self.h, int(bool(flag))), self.ctx.h)
+
     def set_transposed(self, flag=True):
         check(lib().ug4gb_gmg_set_transposed(self.h, 1 if flag else 0), self.ctx.h)
 
@@ -440,6 +444,17 @@ class GeometricMultiGrid:
         ci = np.zeros(nnz.value, np.int32)
         va = np.zeros(nnz.value)
         check(lib().ug4gb_gmg_export_transfer(self.h, level, which, _ptr(rp), _ptr(ci), _ptr(va)), self.ctx.h)
+        return rp, ci, va
+
+    def level_matrix(self, level):
+        """(rowptr, col, val) of the multigrid's FP64 operator of `level`
+        (re-assembled, or R A P with set_rap)."""
+        r, nnz = C.c_int(), C.c_int64()
+        check(lib().ug4gb_gmg_level_info(self.h, level, C.byref(r), C.byref(nnz)), self.ctx.h)
+        rp = np.zeros(r.value + 1, np.int32)
+        ci = np.zeros(nnz.value, np.int32)
+        va = np.zeros(nnz.value)
+        check(lib().ug4gb_gmg_export_level(self.h, level, _ptr(rp), _ptr(ci), _ptr(va)), self.ctx.h)
         return rp, ci, va
 
 

@@ -174,6 +174,8 @@ struct GmgT : GmgBase {
     void *sc_top() override { return lev.back().sc.p; }
     const Csr &P(int l) const override { return lev[l].P; }
     const Csr &R(int l) const override { return lev[l].R; }
+    const Csr &levelA(int l) const override { return lev[l].A; }
+    int base_level() const override { return base; }
 
     void setup_level(Ctx &c, GLevel<V> &L, const Level &G, int l, double damp, bool is_base)
     {
@@ -420,30 +422,51 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
     G->lev.resize(nl);
     UG_REQUIRE(m->base >= 0 && m->base < nl, UG4GB_ERR_INVALID, "GMG: base level out of range");
     UG_REQUIRE(A_top->A.nrows == g->lev[nl - 1].nv, UG4GB_ERR_INVALID, "GMG: top operator size != top level");
-    for (int l = m->base; l < nl; ++l) {
+    auto transpose_level = [&](int l) {
         GLevel<V> &L = G->lev[l];
-        // level operator: copy of the surface operator on the top level,
-        // re-assembled on coarser levels (assemble_level_operator, :528-750)
-        if (l == nl - 1) {
-            csr_copy(c, A_top->A, L.A);
-        } else {
-            ug4gb_matrix tmp;
-            tmp.ctx = m->ctx;
-            disc_assemble(m->disc, l, &tmp, nullptr);
-            L.A = std::move(tmp.A);
+        Csr T;
+        csr_transpose(c, L.A, T, true);
+        UG_LAUNCH(c, k_dirichlet_identity, div_up(T.nrows, 256), 256, 0, g->lev[l].bnd.p, T.nrows, T.rowptr.p,
+                  T.col.p, T.val.p);
+        L.A = std::move(T);
+    };
+    if (!m->rap) {
+        for (int l = m->base; l < nl; ++l) {
+            GLevel<V> &L = G->lev[l];
+            // level operator: copy of the surface operator on the top level,
+            // re-assembled on coarser levels (assemble_level_operator, :528-750)
+            if (l == nl - 1) {
+                csr_copy(c, A_top->A, L.A);
+            } else {
+                ug4gb_matrix tmp;
+                tmp.ctx = m->ctx;
+                disc_assemble(m->disc, l, &tmp, nullptr);
+                L.A = std::move(tmp.A);
+            }
+            if (m->transposed) transpose_level(l);
+            UG_CUDA(cudaStreamSynchronize(c.stream));
+            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
+            if (l > m->base) {
+                G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
+                if (L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI)
+                    L.sweep2 = sweep2_prepare<V>(c, L.At, L.gp);
+            }
         }
-        if (m->transposed) {
-            Csr T;
-            csr_transpose(c, L.A, T, true);
-            UG_LAUNCH(c, k_dirichlet_identity, div_up(T.nrows, 256), 256, 0, g->lev[l].bnd.p, T.nrows, T.rowptr.p,
-                      T.col.p, T.val.p);
-            L.A = std::move(T);
+    } else {
+        // Galerkin coarse operators (init_rap_operator, :830-1012): the top
+        // level's operator, then from the top down the transfers of a level
+        // and R A P of it as the operator of the level below
+        csr_copy(c, A_top->A, G->lev[nl - 1].A);
+        if (m->transposed) transpose_level(nl - 1);
+        for (int l = nl - 1; l > m->base; --l) {
+            G->setup_transfers(c, G->lev[l], g->lev[l], g->lev[l - 1]);
+            csr_rap(c, G->lev[l].R, G->lev[l].A, G->lev[l].P, G->lev[l - 1].A);
         }
-        UG_CUDA(cudaStreamSynchronize(c.stream));
-        G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
-        if (l > m->base) {
-            G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
-            if (L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI) L.sweep2 = sweep2_prepare<V>(c, L.At, L.gp);
+        for (int l = m->base; l < nl; ++l) {
+            GLevel<V> &L = G->lev[l];
+            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
+            if (l > m->base && L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI)
+                L.sweep2 = sweep2_prepare<V>(c, L.At, L.gp);
         }
     }
     G->setup_base(c);
@@ -532,6 +555,13 @@ int ug4gb_gmg_set_precision(ug4gb_gmg *m, int precision)
     return UG4GB_OK;
 }
 
+int ug4gb_gmg_set_rap(ug4gb_gmg *m, int rap)
+{
+    if (!m) return UG4GB_ERR_INVALID;
+    m->rap = rap ? 1 : 0;
+    return UG4GB_OK;
+}
+
 int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed)
 {
     if (!m) return UG4GB_ERR_INVALID;
@@ -614,6 +644,27 @@ int ug4gb_gmg_export_transfer(const ug4gb_gmg *m, int level, int which, int *row
     return guarded(m->ctx, [&] {
         Ctx &c = m->ctx->c;
         const Csr &A = which ? m->impl->R(level) : m->impl->P(level);
+        if (rowptr) copy_out(c, rowptr, A.rowptr.p, sizeof(int) * (size_t)(A.nrows + 1));
+        if (col) copy_out(c, col, A.col.p, sizeof(int) * (size_t)A.nnz);
+        if (val) copy_out(c, val, A.val.p, sizeof(double) * (size_t)A.nnz);
+    });
+}
+
+int ug4gb_gmg_level_info(const ug4gb_gmg *m, int level, int *nrows, int64_t *nnz)
+{
+    if (!m || !m->impl || level < m->impl->base_level() || level > m->impl->top()) return UG4GB_ERR_INVALID;
+    const Csr &A = m->impl->levelA(level);
+    if (nrows) *nrows = A.nrows;
+    if (nnz) *nnz = A.nnz;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_export_level(const ug4gb_gmg *m, int level, int *rowptr, int *col, double *val)
+{
+    if (!m || !m->impl || level < m->impl->base_level() || level > m->impl->top()) return UG4GB_ERR_INVALID;
+    return guarded(m->ctx, [&] {
+        Ctx &c = m->ctx->c;
+        const Csr &A = m->impl->levelA(level);
         if (rowptr) copy_out(c, rowptr, A.rowptr.p, sizeof(int) * (size_t)(A.nrows + 1));
         if (col) copy_out(c, col, A.col.p, sizeof(int) * (size_t)A.nnz);
         if (val) copy_out(c, val, A.val.p, sizeof(double) * (size_t)A.nnz);

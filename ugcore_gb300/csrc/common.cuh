@@ -419,6 +419,10 @@ void exclusive_scan_int(Ctx &c, const int *in, int *out, int n, int64_t *total_o
 void csr_from_elements(Ctx &c, const Level &L, Csr &A);
 void csr_transpose(Ctx &c, const Csr &B, Csr &T, bool keep_zeros);
 void csr_copy(Ctx &c, const Csr &src, Csr &dst);
+// Galerkin product M = R A P (k_rap.cu), the product ugcore's AddMultiplyOf
+// forms for set_rap(true); at most kRapCap distinct columns per row of M
+constexpr int kRapCap = 64;
+void csr_rap(Ctx &c, const Csr &R, const Csr &A, const Csr &P, Csr &M);
 template <class T>
 void sell_from_csr(Ctx &c, const Csr &A, Sell<T> &S, const double *col_scale /* nullable */);
 // distinct column offsets (col - row) of A, sorted; false if more than max_s

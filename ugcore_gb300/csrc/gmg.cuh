@@ -102,6 +102,8 @@ struct GmgBase {
     virtual float *top_defect_buffer() = 0;
     virtual const Csr &P(int l) const = 0;
     virtual const Csr &R(int l) const = 0;
+    virtual const Csr &levelA(int l) const = 0;   // FP64 operator of level l (re-assembled or R A P)
+    virtual int base_level() const = 0;
 };
 
 }  // namespace ug4gb
@@ -120,6 +122,7 @@ struct ug4gb_gmg {
     int cycle = 1, nu1 = 2, nu2 = 2, base = 0;
     int precision = UG4GB_PREC_FP64;
     int transposed = 0;
+    int rap = 0;                 // coarse operators as Galerkin products R A P (set_rap)
     std::unique_ptr<ug4gb::GmgBase> impl;
     int n_top = 0;
     int gen = 0;                 // incremented by every init (invalidates captured graphs)

@@ -28,7 +28,7 @@ from .algebra import (BiCGStab, CG, DomainDiscretization, GaussSeidel, Geometric
 BASE = dict(elem="quad", mx=2, my=2, mz=1, nref=6, seed=1, coef="const", diffusion=1.0, coef_modes=64,
             coef_kmax=8.0, vel=None, vel_modes=16, vel_kmax=2.0, peclet=10.0, solver="cg", smoother="jacobi",
             damp=0.6, nu1=2, nu2=2, cycle=1, base=0, precision="fp64", maxit=200, rel_red=1e-10,
-            min_defect=1e-300)
+            min_defect=1e-300, rap=False)
 
 CONFIGS = {
     "c0": dict(elem="quad", mx=2, my=2, nref=6),
@@ -105,6 +105,7 @@ class Problem:
         g.set_base_level(c["base"])
         g.set_precision(c["precision"])
         g.set_transposed(transposed)
+        g.set_rap(c["rap"])
         return g
 
     def solve(self, raise_on_failure=True):
