@@ -284,11 +284,12 @@ def run_ours(args, rank, world, local_rank):
                  "kernel_profile": profile_summary(prof_m)}
         del pm
 
-    target = adj = conv = None
+    target = adj = conv = rap = None
     if not args.no_extras:
         target = run_target(args, ctx, timed, world, hbm)
         adj = run_adjoint_grad(args, ctx, timed)
         conv = run_convection_adjoint(args, ctx, timed, world, hbm)
+        rap = run_galerkin(args, ctx, timed, world)
 
     # ---- assembly throughput (top level, FP64 FV1 + CRS values + rhs)
     asm = None
@@ -331,6 +332,7 @@ def run_ours(args, rank, world, local_rank):
         "variable_coefficient_tets": target,
         "adjoint_gradient": adj,
         "convection_adjoint": conv,
+        "galerkin_coarse_operators": rap,
         "assembly": asm,
         "clocks": clocks,
         "cpu_baseline": cpu,
@@ -448,6 +450,33 @@ def run_convection_adjoint(args, ctx, timed, world, hbm):
         out["dofs"], out["nnz"] = p.n, sizes[-1]["nnz"]
         del p
     out["mixed_speedup_vs_fp64"] = out["fp64"]["ms_per_solve"] / out["mixed"]["ms_per_solve"]
+    return out
+
+
+def run_galerkin(args, ctx, timed, world):
+    """set_rap(true): coarse operators R A P (GPU sparse triple product)
+    against re-assembly, on the 129^3 hex Poisson (FP64) and lognormal tet
+    (mixed) problems: multigrid set-up time (host clock around init, which
+    ends with a synchronisation) and the solve."""
+    from ugcore_gb300 import problems
+    out = {}
+    for name, prec in (("c1", "fp64"), ("c2", "mixed")):
+        res = {}
+        for rap in (False, True):
+            p = problems.Problem(ctx, problems.config(name, precision=prec, rap=rap))
+            t0 = time.perf_counter()
+            p.gmg.init(p.A)
+            p.solver.init(p.A)
+            init_s = time.perf_counter() - t0
+            for _ in range(min(args.warmup, 2)):
+                p.solve()
+            ms = max_over_ranks(timed(p.solve, max(2, args.steps // 3)), world)
+            st = p.solve()
+            res["rap" if rap else "reassembly"] = {"gmg_init_s": init_s, "ms_per_solve": ms,
+                                                   "pcg_steps": st["steps"],
+                                                   "rel_residual": st["defect"] / st["initial_defect"]}
+            del p
+        out["%s_%s" % (name, prec)] = res
     return out
 
 
