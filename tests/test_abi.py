@@ -105,3 +105,36 @@ int main() {
         assert r.returncode == 0 and "ok 1" in r.stdout, r.stdout + r.stderr
     else:
         assert r.returncode == 2 and "error" in r.stdout
+
+
+def test_ugcore_glue_instantiates_reference_solvers(tmp_path):
+    """The ugcore-side GPU algebra (ugcore_gb300/adapters/ug4gb_algebra.h)
+    compiles against ugcore's own headers, and ugcore's CG and BiCGStab
+    templates instantiate with its vector type (where the ugcore tree is
+    present; four empty stand-ins replace headers that need Boost)."""
+    ref = os.environ.get("UG4_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "ugbase", "lib_algebra")):
+        pytest.skip("ugcore source tree not present")
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    shim = tmp_path / "shim"
+    for h in ("lib_disc/function_spaces/approximation_space.h", "lib_disc/common/function_group.h",
+              "boost/graph/adjacency_list.hpp", "boost/graph/graph_traits.hpp"):
+        (shim / h).parent.mkdir(parents=True, exist_ok=True)
+        (shim / h).write_text("")
+    src = tmp_path / "glue.cpp"
+    src.write_text(r'''
+#include "ug4gb_algebra.h"
+#include "lib_algebra/operator/interface/matrix_operator.h"
+#include "lib_algebra/operator/linear_solver/cg.h"
+#include "lib_algebra/operator/linear_solver/bicgstab.h"
+template class ug::CG<ug::GPUAlgebra::vector_type>;
+template class ug::BiCGStab<ug::GPUAlgebra::vector_type>;
+static_assert(ug::GPUAlgebra::blockSize == 1, "scalar algebra");
+int main() { return ug::GPUAlgebra::get_type().type() == ug::AlgebraType::GPU ? 0 : 1; }
+''')
+    r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-w", "-I" + str(shim), "-I" + os.path.join(ref, "ugbase"),
+                        "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "ugcore_gb300", "adapters"),
+                        str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
