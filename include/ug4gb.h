@@ -196,6 +196,27 @@ UG4GB_API int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matri
    of the adjoint (transposed) solve.  No ugcore counterpart (ugcore has
    SparseMatrix::set_as_transpose_of, sparsematrix_impl.h:149, and
    SetDirichletRow, sparsematrix_util.h:850, but no adjoint). */
+/* ---- time discretisation (ThetaTimeStep, lib_disc/time_disc/theta_time_step.h:165) ----
+   theta scheme over the FV1 discretisation with one previous time point:
+   (M + theta dt A) u_new = M u_old - (1 - theta) dt A u_old + dt f, where M is
+   the lumped FV1 mass (|SCV_i| on the diagonal) and f the discretisation's
+   source; assembled element by element as the instationary AssembleLinear /
+   AssembleJacobian (lib_disc/spatial_disc/elem_disc/elem_disc_assemble_util.h:
+   1032-1225, 439-560) with update_scaling's s_m = (1, -1), s_a = (theta dt,
+   (1 - theta) dt) (theta_time_step.h:230-246); Dirichlet rows as in the
+   stationary case. */
+typedef struct ug4gb_timedisc ug4gb_timedisc;
+UG4GB_API int ug4gb_timedisc_create(ug4gb_ctx *ctx, ug4gb_disc *d, ug4gb_timedisc **out);
+UG4GB_API int ug4gb_timedisc_set_theta(ug4gb_timedisc *td, double theta);   /* set_theta; default 1 */
+/* prepare_step(prevSol, dt): copies the previous (top-level) solution */
+UG4GB_API int ug4gb_timedisc_prepare_step(ug4gb_timedisc *td, const ug4gb_vector *u_old, double t_old, double dt);
+UG4GB_API int ug4gb_timedisc_future_time(const ug4gb_timedisc *td, double *t);
+/* assemble_linear(A, b) of the step (top level) */
+UG4GB_API int ug4gb_timedisc_assemble_linear(ug4gb_timedisc *td, int level, ug4gb_matrix *A, ug4gb_vector *b);
+/* assemble_jacobian(J) = M + theta dt A of any level */
+UG4GB_API int ug4gb_timedisc_assemble_jacobian(ug4gb_timedisc *td, int level, ug4gb_matrix *A);
+UG4GB_API void ug4gb_timedisc_destroy(ug4gb_timedisc *td);
+
 UG4GB_API int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A, ug4gb_matrix *AT);
 /* element coefficient K of a level (host or device out array, num_elements) */
 UG4GB_API int ug4gb_disc_export_coefficients(ug4gb_disc *d, int level, double *K);
@@ -223,6 +244,11 @@ UG4GB_API int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed);
    mg_solver_impl.hpp:830-1012, with AddMultiplyOf, sparsematrix_util.h:167)
    instead of re-assembling it; default 0 */
 UG4GB_API int ug4gb_gmg_set_rap(ug4gb_gmg *m, int rap);
+/* AssembledMultiGridCycle::set_discretization (mg_solver.h:126) with a time
+   discretisation: coarse levels are re-assembled as its jacobian M + theta dt A
+   of the prepared step (init() must follow prepare_step); NULL: the plain
+   stationary discretisation */
+UG4GB_API int ug4gb_gmg_set_time_disc(ug4gb_gmg *m, ug4gb_timedisc *td);
 /* AssembledMultiGridCycle::init (mg_solver_impl.hpp:380): copies the top
    operator, re-assembles coarser levels (or forms R A P), builds P/R,
    smoothers and the LU */

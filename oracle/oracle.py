@@ -69,6 +69,9 @@ def lib():
         L.orc_prob_transfer_nnz.argtypes = [P, C.c_int, C.c_int]
         L.orc_prob_transfer_nnz.restype = C.c_int64
         L.orc_prob_transfer.argtypes = [P, C.c_int, C.c_int, ip, ip, dp]
+        L.orc_prob_theta_system.argtypes = [P, C.c_double, C.c_double, dp, ip, ip, dp, dp]
+        L.orc_prob_theta_steps.argtypes = [P, C.c_double, C.c_double, C.c_int, dp, ip]
+        L.orc_prob_theta_jacobian.argtypes = [P, C.c_int, C.c_double, C.c_double, ip, ip, dp]
         L.orc_prob_gmg_level_nnz.argtypes = [P, C.c_int]
         L.orc_prob_gmg_level_nnz.restype = C.c_int64
         L.orc_prob_gmg_level.argtypes = [P, C.c_int, ip, ip, dp]
@@ -133,6 +136,33 @@ class Problem:
         va = np.zeros(nnz, np.float64)
         L.orc_prob_level_matrix(self.h, l, rp, ci, va)
         return rp, ci, va
+
+    def theta_system(self, theta, dt, u_old):
+        """top-level (M + theta dt A, rhs) of one theta step from u_old"""
+        rp, ci, va = self.matrix()
+        va = np.zeros_like(va)
+        b = np.zeros(self.nv())
+        rc = lib().orc_prob_theta_system(self.h, theta, dt, np.ascontiguousarray(u_old, np.float64), rp, ci, va, b)
+        if rc:
+            raise RuntimeError("theta assembly failed")
+        return (rp, ci, va), b
+
+    def theta_jacobian(self, l, theta, dt):
+        """level l's M + theta dt A (CRS pattern = the level's)"""
+        rp, ci, va = self.matrix(l)
+        va = np.zeros_like(va)
+        if lib().orc_prob_theta_jacobian(self.h, l, theta, dt, rp, ci, va):
+            raise RuntimeError("theta jacobian failed")
+        return rp, ci, va
+
+    def theta_steps(self, theta, dt, nsteps, u0):
+        """nsteps theta steps from u0; (u, iterations per step)"""
+        u = np.array(u0, dtype=np.float64, copy=True)
+        steps = np.zeros(nsteps, np.int32)
+        rc = lib().orc_prob_theta_steps(self.h, theta, dt, nsteps, u, steps)
+        if rc:
+            raise RuntimeError("theta steps failed %d" % rc)
+        return u, steps
 
     def gmg_level_matrix(self, l):
         """the multigrid's operator of level l (R A P of the level above with rap)"""

@@ -109,6 +109,12 @@ typedef struct {
     const double *f;         /* nv */
     int upwind;              /* 0 = none (no convection), 1 = full upwind */
     int dirichlet;           /* 1 = zero Dirichlet on the boundary */
+    /* instationary (ThetaTimeStep): element matrix sm0 M_e + sa0 A_e with the
+       lumped mass M_e = diag(|SCV_i|); rhs sa0 f_e - sm1 M_e u_old
+       - sa1 A_e u_old + sa1 f_e (elem_disc_assemble_util.h:1124-1205) */
+    int inst;
+    double sm0, sa0, sm1, sa1;
+    const double *u_old;     /* nv (top level), for the rhs */
 } orc_disc;
 
 int orc_assemble(const orc_level *L, const orc_disc *D, orc_crs *A, double *b);

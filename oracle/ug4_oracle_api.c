@@ -214,6 +214,91 @@ int orc_prob_solve(orc_prob *P, double *x, int *steps, double *d0, double *d1, d
     return rc;
 }
 
+/* ---- ThetaTimeStep ------------------------------------------------------ */
+/* the time-discrete operator of level l (M + theta dt A) and, with b, the
+   right-hand side of one step from u_old (top level) */
+static int theta_assemble(const orc_prob *P, int l, double theta, double dt, const double *u_old, orc_crs *A,
+                          double *b)
+{
+    const int top = P->H.nlev - 1;
+    orc_disc D;
+    memset(&D, 0, sizeof(D));
+    D.K = P->K[l];
+    D.upwind = P->has_vf ? 1 : 0;
+    D.vfield = P->has_vf ? &P->vf : NULL;
+    D.f = (l == top) ? P->f : NULL;
+    D.dirichlet = 1;
+    D.inst = 1;
+    D.sm0 = 1.0; D.sa0 = theta * dt; D.sm1 = -1.0; D.sa1 = (1.0 - theta) * dt;
+    D.u_old = u_old;
+    return orc_assemble(&P->H.lev[l], &D, A, b);
+}
+
+/* top-level time-discrete system of one step (CRS pattern = the level's) */
+int orc_prob_theta_system(const orc_prob *P, double theta, double dt, const double *u_old, int *rowptr, int *col,
+                          double *val, double *b)
+{
+    orc_crs A;
+    memset(&A, 0, sizeof(A));
+    if (theta_assemble(P, P->H.nlev - 1, theta, dt, u_old, &A, b)) return -1;
+    crs_out(&A, rowptr, col, val);
+    orc_crs_free(&A);
+    return 0;
+}
+
+/* the time-discrete operator M + theta dt A of level l (the jacobian the
+   coarse multigrid levels are assembled with) */
+int orc_prob_theta_jacobian(const orc_prob *P, int l, double theta, double dt, int *rowptr, int *col, double *val)
+{
+    orc_crs A;
+    memset(&A, 0, sizeof(A));
+    if (l < 0 || l >= P->H.nlev || theta_assemble(P, l, theta, dt, NULL, &A, NULL)) return -1;
+    crs_out(&A, rowptr, col, val);
+    orc_crs_free(&A);
+    return 0;
+}
+
+/* nsteps theta steps of constant size dt from u (in/out), as ugcore's
+   SolveLinearTimeProblem (scripts/util/time_step_util.lua:643-870): the
+   matrix and the multigrid (coarse levels: the time-discrete jacobians) are
+   set up once for the step size, every step assembles its right-hand side
+   from the previous solution and applies the solver with the previous
+   solution as the initial guess.  steps[s] = iterations of step s. */
+int orc_prob_theta_steps(orc_prob *P, double theta, double dt, int nsteps, double *u, int *steps)
+{
+    const int nl = P->H.nlev, top = nl - 1, nv = P->H.lev[top].nv;
+    orc_crs *At = (orc_crs *)calloc((size_t)nl, sizeof(orc_crs));
+    double *b = (double *)malloc(sizeof(double) * (size_t)nv);
+    double *u_old = (double *)malloc(sizeof(double) * (size_t)nv);
+    if (!At || !b || !u_old) return -1;
+    int rc = 0;
+    orc_gmg G;
+    memset(&G, 0, sizeof(G));
+    for (int l = 0; l < top; ++l)
+        if (theta_assemble(P, l, theta, dt, NULL, &At[l], NULL)) return -1;
+    for (int s = 0; s < nsteps && rc == 0; ++s) {
+        memcpy(u_old, u, sizeof(double) * (size_t)nv);
+        if (s == 0) {
+            if (theta_assemble(P, top, theta, dt, u_old, &At[top], b)) return -1;
+            const orc_params *p = &P->p;
+            if (orc_gmg_init(&G, &P->H, At, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap))
+                return -2;
+        } else {
+            orc_crs T;
+            memset(&T, 0, sizeof(T));
+            if (theta_assemble(P, top, theta, dt, u_old, &T, b)) return -1;
+            orc_crs_free(&T);
+        }
+        int st = 0;
+        rc = run_solver(&P->p, &At[top], &G, u, b, &st, NULL, NULL, NULL, 0);
+        if (steps) steps[s] = st;
+    }
+    orc_gmg_free(&G);
+    for (int l = 0; l < nl; ++l) orc_crs_free(&At[l]);
+    free(At); free(b); free(u_old);
+    return rc;
+}
+
 /* transposed operator with Dirichlet rows reset to identity */
 static int transpose_dirichlet(const orc_crs *A, const orc_level *L, orc_crs *T)
 {

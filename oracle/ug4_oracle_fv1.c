@@ -308,6 +308,35 @@ int orc_assemble(const orc_level *L, const orc_disc *D, orc_crs *A, double *b)
         double K = D->K ? D->K[e] : 1.0;
         element_matrix(L->elem_type, &G, dim, k, K, v, D->upwind, Aloc);
         const int *ev = L->elems + (size_t)e * k;
+        if (D->inst) {
+            /* rhs of the element first (it uses the stiffness A_e), then
+               locA = sm0 M_e + sa0 A_e; every scaled term rounded before it is added */
+            double rhs[8];
+            if (b) {
+                for (int i = 0; i < k; ++i) {
+                    const double fv = (D->f ? D->f[ev[i]] : 0.0) * G.vol[i];
+                    double r = 0.0;
+                    if (D->sa0 != 0.0) r = D->sa0 * fv;
+                    r = r + (-D->sm1) * (G.vol[i] * D->u_old[ev[i]]);
+                    if (D->sa1 != 0.0) {
+                        double au = 0.0;
+                        for (int j = 0; j < k; ++j) au = au + Aloc[i][j] * D->u_old[ev[j]];
+                        r = r + (-D->sa1) * au;
+                        r = r + D->sa1 * fv;
+                    }
+                    rhs[i] = r;
+                }
+            }
+            for (int i = 0; i < k; ++i)
+                for (int j = 0; j < k; ++j) {
+                    const double m = (i == j) ? D->sm0 * G.vol[i] : 0.0;
+                    const int s = orc_crs_find(A, ev[i], ev[j]);
+                    A->val[s] += m + D->sa0 * Aloc[i][j];
+                }
+            if (b)
+                for (int i = 0; i < k; ++i) b[ev[i]] += rhs[i];
+            continue;
+        }
         for (int i = 0; i < k; ++i)
             for (int j = 0; j < k; ++j) {
                 int s = orc_crs_find(A, ev[i], ev[j]);

@@ -232,3 +232,48 @@ def test_adjoint_oracle_matches_finite_differences(oracle_lib):
         d = rng.standard_normal(ne)
         fd = (J(m + h * d) - J(m - h * d)) / (2 * h)
         assert abs(fd - g @ d) <= 1e-6 * max(abs(fd), 1e-30) + 1e-12
+
+
+# ---- theta time stepping (ThetaTimeStep over the FV1 discretisation) ------
+def test_theta_mass_is_the_scv_volume(oracle_lib):
+    """(M + theta dt A) - theta dt A = lumped mass: the SCV volumes, which sum
+    to the volume of the unit square / cube on every interior row set"""
+    orc = oracle_lib
+    P = orc.Problem(orc.make_params(elem_type=orc.ORC_HEX, mx=2, my=2, mz=2, nref=2, seed=3))
+    rp, ci, va = P.matrix()
+    u0 = np.zeros(P.nv())
+    dt, theta = 0.25, 1.0
+    (rpt, cit, vat), _ = P.theta_system(theta, dt, u0)
+    assert np.array_equal(rp, rpt) and np.array_equal(ci, cit)
+    M = vat - theta * dt * va
+    diag = np.zeros(P.nv())
+    for i in range(P.nv()):
+        for a in range(rp[i], rp[i + 1]):
+            if ci[a] == i:
+                diag[i] = M[a]
+            else:
+                assert abs(M[a]) <= 1e-15
+    n = round(P.nv() ** (1 / 3))
+    interior = np.array([0 < i % n < n - 1 and 0 < (i // n) % n < n - 1 and 0 < i // (n * n) < n - 1
+                         for i in range(P.nv())])
+    h = 1.0 / (n - 1)
+    assert np.allclose(diag[interior], h ** 3, rtol=1e-12)
+
+
+def test_theta_steps_keep_the_stationary_solution(oracle_lib):
+    """from the stationary solution u* (A u* = f) every theta step returns u*"""
+    orc = oracle_lib
+    P = orc.Problem(orc.make_params(elem_type=orc.ORC_QUAD, mx=2, my=2, nref=4, seed=5, rel_red=1e-13, maxit=400))
+    us = P.solve()["x"]
+    for theta in (1.0, 0.5):
+        u, steps = P.theta_steps(theta, 0.05, 3, us)
+        assert np.abs(u - us).max() <= 1e-9 * np.abs(us).max()
+
+
+def test_implicit_euler_approaches_the_stationary_solution(oracle_lib):
+    orc = oracle_lib
+    P = orc.Problem(orc.make_params(elem_type=orc.ORC_QUAD, mx=2, my=2, nref=3, seed=5, rel_red=1e-12, maxit=400))
+    us = P.solve()["x"]
+    u, steps = P.theta_steps(1.0, 10.0, 6, np.zeros(P.nv()))
+    assert np.abs(u - us).max() <= 1e-6 * np.abs(us).max()
+    assert all(s > 0 for s in steps)

@@ -8,7 +8,8 @@ and there is no CPU fallback.
 """
 from ._lib import UG4GBError, exported_symbols, LIB_PATH  # noqa: F401
 from .algebra import (BiCGStab, CG, Context, DomainDiscretization, GaussSeidel, GeometricMultiGrid,  # noqa: F401
-                      GPUSparseMatrix, GPUVector, Jacobi, StdConvCheck, StructuredHierarchy)
+                      GPUSparseMatrix, GPUVector, Jacobi, StdConvCheck, StructuredHierarchy, ThetaTimeStep)
 
 __all__ = ["UG4GBError", "Context", "StructuredHierarchy", "GPUVector", "GPUSparseMatrix", "DomainDiscretization",
-           "GeometricMultiGrid", "Jacobi", "GaussSeidel", "StdConvCheck", "CG", "BiCGStab", "exported_symbols"]
+           "GeometricMultiGrid", "Jacobi", "GaussSeidel", "StdConvCheck", "CG", "BiCGStab", "ThetaTimeStep",
+           "exported_symbols"]

@@ -99,6 +99,14 @@ _SIGS = {
     "ug4gb_gmg_set_precision": (I, [P, I]),
     "ug4gb_gmg_set_transposed": (I, [P, I]),
     "ug4gb_gmg_set_rap": (I, [P, I]),
+    "ug4gb_gmg_set_time_disc": (I, [P, P]),
+    "ug4gb_timedisc_create": (I, [P, P, P]),
+    "ug4gb_timedisc_set_theta": (I, [P, D]),
+    "ug4gb_timedisc_prepare_step": (I, [P, P, D, D]),
+    "ug4gb_timedisc_future_time": (I, [P, P]),
+    "ug4gb_timedisc_assemble_linear": (I, [P, I, P, P]),
+    "ug4gb_timedisc_assemble_jacobian": (I, [P, I, P]),
+    "ug4gb_timedisc_destroy": (None, [P]),
     "ug4gb_gmg_level_info": (I, [P, I, P, P]),
     "ug4gb_gmg_export_level": (I, [P, I, P, P, P]),
     "ug4gb_gmg_init": (I, [P, P]),

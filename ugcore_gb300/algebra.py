@@ -371,6 +371,45 @@ class DomainDiscretization:
         return out
 
 
+class ThetaTimeStep:
+    """ThetaTimeStep(domainDisc) (theta_time_step.h:165): the theta scheme
+    (M + theta dt A) u_new = M u_old - (1 - theta) dt A u_old + dt f with the
+    lumped FV1 mass; theta = 1 implicit Euler, 0.5 Crank-Nicolson."""
+
+    def __init__(self, disc, theta=1.0):
+        self.ctx = disc.ctx
+        self.disc = disc
+        h = C.c_void_p()
+        check(lib().ug4gb_timedisc_create(self.ctx.h, disc.h, C.byref(h)), self.ctx.h)
+        self.h = h
+        self.set_theta(theta)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_timedisc_destroy(self.h)
+            self.h = None
+
+    def set_theta(self, theta):
+        check(lib().ug4gb_timedisc_set_theta(self.h, float(theta)), self.ctx.h)
+
+    def prepare_step(self, u_old, t_old, dt):
+        """previous solution (GPUVector of the top level), its time, the step size"""
+        check(lib().ug4gb_timedisc_prepare_step(self.h, u_old.h, float(t_old), float(dt)), self.ctx.h)
+
+    def future_time(self):
+        t = C.c_double()
+        check(lib().ug4gb_timedisc_future_time(self.h, C.byref(t)), self.ctx.h)
+        return t.value
+
+    def assemble_linear(self, A, b, level=None):
+        level = self.disc.hier.num_levels - 1 if level is None else level
+        check(lib().ug4gb_timedisc_assemble_linear(self.h, level, A.h, b.h), self.ctx.h)
+
+    def assemble_jacobian(self, A, level=None):
+        level = self.disc.hier.num_levels - 1 if level is None else level
+        check(lib().ug4gb_timedisc_assemble_jacobian(self.h, level, A.h), self.ctx.h)
+
+
 class Jacobi:
     """damped Jacobi smoother (jacobi.h); damp is the ugcore damping factor"""
 
@@ -421,6 +460,12 @@ class GeometricMultiGrid:
     def set_precision(self, prec):
         p = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, 0: 0, 1: 1}[prec]
         check(lib().ug4gb_gmg_set_precision(self.h, p), self.ctx.h)
+
+    def set_discretization(self, td):
+        """assemble the coarse levels with a ThetaTimeStep's jacobian (None: the
+        stationary discretisation); init() follows its prepare_step"""
+        check(lib().ug4gb_gmg_set_time_disc(self.h, td.h if td is not None else None), self.ctx.h)
+        self._td = td
 
     def set_rap(self, flag=True):
         """Galerkin coarse operators R A P instead of re-assembly (set_rap)"""

@@ -49,7 +49,7 @@ const double *disc_coefficients(ug4gb_disc *d, int level)
 }
 
 // assemble the FV1 operator of `level` into A (and the rhs into b if given)
-void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b)
+void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const TimeScale *ts)
 {
     Ctx &c = d->ctx->c;
     const Level &L = d->g->lev[level];
@@ -82,6 +82,16 @@ void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b)
     a.col = A->A.col.p;
     a.val = A->A.val.p;
     a.b = b;
+    if (ts) {
+        UG_REQUIRE(!b || (top && ts->u_old), UG4GB_ERR_INVALID,
+                   "time-discrete right-hand side: top level with a previous solution only");
+        a.inst = 1;
+        a.sm0 = ts->sm0;
+        a.sa0 = ts->sa0;
+        a.sm1 = ts->sm1;
+        a.sa1 = ts->sa1;
+        a.u_old = ts->u_old;
+    }
     launch_assemble(c, L, a);
     launch_dirichlet(c, L, A->A, b);
 }
@@ -223,7 +233,7 @@ int ug4gb_disc_assemble_linear(ug4gb_disc *d, int level, ug4gb_matrix *A, ug4gb_
         return UG4GB_ERR_INVALID;
     }
     return guarded(d->ctx, [&] {
-        disc_assemble(d, level, A, b->d);
+        disc_assemble(d, level, A, b->d, nullptr);
         UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
     });
 }
@@ -232,9 +242,96 @@ int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matrix *A)
 {
     if (!d || !A || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
     return guarded(d->ctx, [&] {
-        disc_assemble(d, level, A, nullptr);
+        disc_assemble(d, level, A, nullptr, nullptr);
         UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
     });
+}
+
+// ---- ThetaTimeStep ------------------------------------------------------
+int ug4gb_timedisc_create(ug4gb_ctx *ctx, ug4gb_disc *d, ug4gb_timedisc **out)
+{
+    if (!ctx || !d || !out) return UG4GB_ERR_INVALID;
+    ug4gb_timedisc *td = new ug4gb_timedisc;
+    td->ctx = ctx;
+    td->disc = d;
+    ug4gb_ctx_retain(ctx);
+    *out = td;
+    return UG4GB_OK;
+}
+
+int ug4gb_timedisc_set_theta(ug4gb_timedisc *td, double theta)
+{
+    if (!td || !(theta >= 0.0 && theta <= 1.0)) return UG4GB_ERR_INVALID;
+    td->theta = theta;
+    return UG4GB_OK;
+}
+
+int ug4gb_timedisc_prepare_step(ug4gb_timedisc *td, const ug4gb_vector *u_old, double t_old, double dt)
+{
+    if (!td || !u_old || !(dt > 0.0)) return UG4GB_ERR_INVALID;
+    const int nv = td->disc->g->lev.back().nv;
+    if (u_old->n != nv) {
+        td->ctx->c.err = "prepare_step: previous solution size != top level";
+        return UG4GB_ERR_INVALID;
+    }
+    return guarded(td->ctx, [&] {
+        Ctx &c = td->ctx->c;
+        td->u_old.alloc(nv);
+        UG_CUDA(cudaMemcpyAsync(td->u_old.p, u_old->d, sizeof(double) * (size_t)nv, cudaMemcpyDeviceToDevice,
+                                c.stream));
+        td->time = t_old;
+        td->dt = dt;
+        td->prepared = true;
+    });
+}
+
+int ug4gb_timedisc_future_time(const ug4gb_timedisc *td, double *t)
+{
+    if (!td || !t) return UG4GB_ERR_INVALID;
+    *t = td->time + td->dt;
+    return UG4GB_OK;
+}
+
+int ug4gb_timedisc_assemble_linear(ug4gb_timedisc *td, int level, ug4gb_matrix *A, ug4gb_vector *b)
+{
+    if (!td || !A || !b) return UG4GB_ERR_INVALID;
+    ug4gb_disc *d = td->disc;
+    if (level != (int)d->g->lev.size() - 1 || b->n != d->g->lev[level].nv) {
+        td->ctx->c.err = "time-discrete assemble_linear: top level, rhs of the level's size";
+        return UG4GB_ERR_INVALID;
+    }
+    if (!td->prepared) {
+        td->ctx->c.err = "time-discrete assemble_linear: prepare_step not called";
+        return UG4GB_ERR_STATE;
+    }
+    return guarded(td->ctx, [&] {
+        const TimeScale ts = td->scale();
+        disc_assemble(d, level, A, b->d, &ts);
+        UG_CUDA(cudaStreamSynchronize(td->ctx->c.stream));
+    });
+}
+
+int ug4gb_timedisc_assemble_jacobian(ug4gb_timedisc *td, int level, ug4gb_matrix *A)
+{
+    if (!td || !A || level < 0 || level >= (int)td->disc->g->lev.size()) return UG4GB_ERR_INVALID;
+    if (!td->prepared) {
+        td->ctx->c.err = "time-discrete assemble_jacobian: prepare_step not called";
+        return UG4GB_ERR_STATE;
+    }
+    return guarded(td->ctx, [&] {
+        const TimeScale ts = td->jacobian_scale();
+        disc_assemble(td->disc, level, A, nullptr, &ts);
+        UG_CUDA(cudaStreamSynchronize(td->ctx->c.stream));
+    });
+}
+
+void ug4gb_timedisc_destroy(ug4gb_timedisc *td)
+{
+    if (!td) return;
+    ug4gb_ctx *ctx = td->ctx;
+    cudaStreamSynchronize(ctx->c.stream);
+    delete td;
+    ug4gb_ctx_release(ctx);
 }
 
 int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A, ug4gb_matrix *AT)

@@ -21,7 +21,7 @@ using namespace ug4gb;
 
 namespace ug4gb {
 
-void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b);
+void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const TimeScale *ts);
 
 // ------------------------------------------------------------- helpers ---
 __global__ void k_diag_inv(const int *rowptr, const int *col, const double *val, int n, double damp, int smoother,
@@ -440,7 +440,12 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
             } else {
                 ug4gb_matrix tmp;
                 tmp.ctx = m->ctx;
-                disc_assemble(m->disc, l, &tmp, nullptr);
+                // with a time discretisation: the jacobian M + sa0 A of its
+                // current step (MultiStepTimeDiscretization::assemble_jacobian,
+                // theta_time_step_impl.h:123-140)
+                TimeScale ts{};
+                if (m->td) ts = m->td->jacobian_scale();
+                disc_assemble(m->disc, l, &tmp, nullptr, m->td ? &ts : nullptr);
                 L.A = std::move(tmp.A);
             }
             if (m->transposed) transpose_level(l);
@@ -559,6 +564,17 @@ int ug4gb_gmg_set_rap(ug4gb_gmg *m, int rap)
 {
     if (!m) return UG4GB_ERR_INVALID;
     m->rap = rap ? 1 : 0;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_time_disc(ug4gb_gmg *m, ug4gb_timedisc *td)
+{
+    if (!m) return UG4GB_ERR_INVALID;
+    if (td && td->disc != m->disc) {
+        m->ctx->c.err = "set_time_disc: the time discretisation belongs to another discretisation";
+        return UG4GB_ERR_INVALID;
+    }
+    m->td = td;
     return UG4GB_OK;
 }
 

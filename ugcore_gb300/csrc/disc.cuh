@@ -22,6 +22,18 @@ struct AsmArgs {
     double *val;
     double *b;                // rhs or null
     int cx, cy, cz;           // structured cell counts (set by launch_assemble)
+    // instationary assembly (ThetaTimeStep): element matrix sm0 M_e + sa0 A_e
+    // with the lumped FV1 mass M_e = diag(|SCV_i|); with b, the rhs of one
+    // previous time point: sa0 f_e - sm1 M_e u_old - sa1 A_e u_old + sa1 f_e
+    int inst = 0;
+    double sm0 = 0.0, sa0 = 1.0, sm1 = 0.0, sa1 = 0.0;
+    const double *u_old = nullptr;
+};
+
+// scalings of a time-discrete assembly (one previous time point)
+struct TimeScale {
+    double sm0, sa0, sm1, sa1;
+    const double *u_old;   // top-level previous solution (device), for the rhs
 };
 
 void launch_assemble(Ctx &c, const Level &L, const AsmArgs &a);

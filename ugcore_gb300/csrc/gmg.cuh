@@ -4,6 +4,7 @@
 #include <memory>
 
 #include "common.cuh"
+#include "disc.cuh"
 #include "k_solve.cuh"
 
 struct ug4gb_ctx {
@@ -114,6 +115,27 @@ struct ug4gb_disc {
     ug4gb::DiscImpl d;
 };
 
+// ThetaTimeStep (lib_disc/time_disc/theta_time_step.h:165-300): one previous
+// time point; scalings s_m = (1, -1), s_a = (theta dt, (1 - theta) dt)
+// (update_scaling, theta_time_step.h:230-246)
+struct ug4gb_timedisc {
+    ug4gb_ctx *ctx = nullptr;
+    ug4gb_disc *disc = nullptr;
+    double theta = 1.0;
+    double dt = 0.0;
+    double time = 0.0;           // time of the previous solution; future time = time + dt
+    bool prepared = false;
+    ug4gb::DevBuf<double> u_old;
+    ug4gb::TimeScale scale() const
+    {
+        return ug4gb::TimeScale{1.0, theta * dt, -1.0, (1.0 - theta) * dt, u_old.p};
+    }
+    ug4gb::TimeScale jacobian_scale() const
+    {
+        return ug4gb::TimeScale{1.0, theta * dt, 0.0, 0.0, nullptr};
+    }
+};
+
 struct ug4gb_gmg {
     ug4gb_ctx *ctx = nullptr;
     ug4gb_disc *disc = nullptr;
@@ -123,6 +145,7 @@ struct ug4gb_gmg {
     int precision = UG4GB_PREC_FP64;
     int transposed = 0;
     int rap = 0;                 // coarse operators as Galerkin products R A P (set_rap)
+    ug4gb_timedisc *td = nullptr;  // coarse levels assembled as this time discretisation's jacobian
     std::unique_ptr<ug4gb::GmgBase> impl;
     int n_top = 0;
     int gen = 0;                 // incremented by every init (invalidates captured graphs)

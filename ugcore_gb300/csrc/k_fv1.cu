@@ -68,7 +68,51 @@ __device__ __forceinline__ void assemble_element(const AsmArgs &a, int e)
     double Aloc[E::K][E::K];
     double vol[E::K];
     VelField vf{a.vmodes, a.vk, a.vc, a.vphase, a.vscale};
-    elem_matrix<T>(X, a.K[e], a.vmodes > 0 ? &vf : nullptr, Aloc, a.b ? vol : nullptr);
+    elem_matrix<T>(X, a.K[e], a.vmodes > 0 ? &vf : nullptr, Aloc, (a.b || a.inst) ? vol : nullptr);
+    if (a.inst) {
+        // instationary AssembleLinear / AssembleJacobian
+        // (lib_disc/spatial_disc/elem_disc/elem_disc_assemble_util.h:1124-1205, :520-535):
+        // locA = sm0 M_e + sa0 A_e, each scaled term rounded before the sum
+        double rhs[E::K];
+        if (a.b) {
+#pragma unroll
+            for (int i = 0; i < E::K; ++i) {
+                const double fi =
+                    a.f ? a.f[ev[i]] : (a.use_seed ? 2.0 * hash_uniform(a.f_seed, (uint64_t)ev[i]) - 1.0 : 0.0);
+                const double fv = __dmul_rn(fi, vol[i]);
+                double r = 0.0, au = 0.0;
+                if (a.sa0 != 0.0) r = __dmul_rn(a.sa0, fv);
+                // previous time point: -sm1 (M_e u_old), -sa1 (A_e u_old), +sa1 f_e
+                r = __dadd_rn(r, __dmul_rn(-a.sm1, __dmul_rn(vol[i], a.u_old[ev[i]])));
+                if (a.sa1 != 0.0) {
+#pragma unroll
+                    for (int j = 0; j < E::K; ++j) au = __dadd_rn(au, __dmul_rn(Aloc[i][j], a.u_old[ev[j]]));
+                    r = __dadd_rn(r, __dmul_rn(-a.sa1, au));
+                    r = __dadd_rn(r, __dmul_rn(a.sa1, fv));
+                }
+                rhs[i] = r;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < E::K; ++i)
+#pragma unroll
+            for (int j = 0; j < E::K; ++j) {
+                const double m = (i == j) ? __dmul_rn(a.sm0, vol[i]) : 0.0;
+                Aloc[i][j] = __dadd_rn(m, __dmul_rn(a.sa0, Aloc[i][j]));
+            }
+#pragma unroll
+        for (int i = 0; i < E::K; ++i)
+#pragma unroll
+            for (int j = 0; j < E::K; ++j) {
+                int s = find_slot(a.rowptr, a.col, ev[i], ev[j]);
+                if (s >= 0) a.val[s] = __dadd_rn(a.val[s], Aloc[i][j]);
+            }
+        if (a.b) {
+#pragma unroll
+            for (int i = 0; i < E::K; ++i) a.b[ev[i]] = __dadd_rn(a.b[ev[i]], rhs[i]);
+        }
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < E::K; ++i)
 #pragma unroll

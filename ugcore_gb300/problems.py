@@ -23,7 +23,7 @@ import numpy as np
 
 from . import fields
 from .algebra import (BiCGStab, CG, DomainDiscretization, GaussSeidel, GeometricMultiGrid, GPUSparseMatrix,
-                      GPUVector, Jacobi, StdConvCheck, StructuredHierarchy)
+                      GPUVector, Jacobi, StdConvCheck, StructuredHierarchy, ThetaTimeStep)
 
 BASE = dict(elem="quad", mx=2, my=2, mz=1, nref=6, seed=1, coef="const", diffusion=1.0, coef_modes=64,
             coef_kmax=8.0, vel=None, vel_modes=16, vel_kmax=2.0, peclet=10.0, solver="cg", smoother="jacobi",
@@ -115,6 +115,38 @@ class Problem:
         st = self.solver.stats()
         st["ok"] = ok
         return st
+
+    # ---- time stepping --------------------------------------------------
+    def theta_steps(self, theta, dt, nsteps, u0, t0=0.0):
+        """nsteps steps of the theta scheme du/dt + A u = f from u0, as
+        ugcore's SolveLinearTimeProblem (scripts/util/time_step_util.lua:
+        643-870) for a constant step: the step's matrix, the multigrid (coarse
+        levels: the time-discrete jacobians M + theta dt A) and the solver are
+        set up once; every step prepares the time discretisation with the
+        previous solution, assembles its right-hand side and applies the
+        solver from the previous solution.  Returns (u as numpy, iterations per
+        step)."""
+        c = self.cfg
+        td = ThetaTimeStep(self.disc, theta)
+        u = GPUVector(self.ctx, self.n).copy_from(u0)
+        A = GPUSparseMatrix(self.ctx)
+        b = GPUVector(self.ctx, self.n)
+        gmg = self._make_gmg(transposed=False)
+        gmg.set_discretization(td)
+        solver = (CG if c["solver"] == "cg" else BiCGStab)(self.ctx)
+        solver.set_preconditioner(gmg)
+        solver.set_convergence_check(StdConvCheck(c["maxit"], c["min_defect"], c["rel_red"]))
+        steps, t = [], t0
+        for s in range(nsteps):
+            td.prepare_step(u, t, dt)
+            td.assemble_linear(A, b)
+            if s == 0:
+                gmg.init(A)
+                solver.init(A)
+            solver.apply(u, b)
+            steps.append(solver.stats()["steps"])
+            t = td.future_time()
+        return u.numpy(), steps
 
     # ---- adjoint --------------------------------------------------------
     def adjoint_setup(self):
