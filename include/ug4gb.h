@@ -296,6 +296,46 @@ UG4GB_API void ug4gb_solver_destroy(ug4gb_solver *s);
 UG4GB_API int ug4gb_disc_grad_logk(ug4gb_disc *d, const ug4gb_vector *u, const ug4gb_vector *lambda, double *grad);
 UG4GB_API int ug4gb_disc_grad_source(ug4gb_disc *d, const ug4gb_vector *lambda, double *grad);
 
+/* ------------------------------------------------------- matrix files -- */
+/* MatrixMarket and ConnectionViewer files, byte-identical to ugcore's writers.
+   MatrixMarket write: SaveMatrixToMTX (lib_disc/function_spaces/
+   grid_function_util.h:761-778) / MatrixIOMtx::write_from (lib_algebra/common/
+   matrixio/matrix_io_mtx.h:243-275): the filename must end in ".mtx"; exact
+   symmetry / skew-symmetry detection, lower triangle only for those, zero
+   values skipped, entries column by column, values "%.13e"; comment NULL =
+   "%Generated with ug4.", "" = no comment line, a comment not starting with
+   '%' gets one prepended.  Read: MatrixIOMtx::read_into (matrix_io_mtx.h:
+   202-236): coordinate real/integer files; symmetric and skew-symmetric
+   entries are mirrored; a later assignment to a position replaces an earlier
+   one; stored zeros are kept.
+   ConnectionViewer: WriteMatrixToConnectionViewer / SaveMatrixForConnection
+   Viewer (grid_function_util.h:714-749, connection_viewer_output.h:114-140;
+   ".mat"), SaveVectorForConnectionViewer (connection_viewer_output.h:395-420;
+   ".vec"), LoadVector / ReadVector (grid_function_util.h:917-923,
+   connection_viewer_input.h:104-150).  Positions are the vertices of the
+   given grid level.
+   The ug4gb_io_* functions take host arrays (CRS with strictly increasing
+   columns per row) and need no context or GPU; a message goes to err (may be
+   NULL).  ug4gb_io_read_mtx_info gives the sizes to allocate for
+   ug4gb_io_read_mtx (rowptr: num_rows + 1, col / val: nnz). */
+UG4GB_API int ug4gb_io_write_mtx(int num_rows, int num_cols, const int *rowptr, const int *col, const double *val,
+                                 const char *filename, const char *comment, char *err, int err_capacity);
+UG4GB_API int ug4gb_io_read_mtx_info(const char *filename, int *num_rows, int *num_cols, int64_t *nnz, char *err,
+                                     int err_capacity);
+UG4GB_API int ug4gb_io_read_mtx(const char *filename, int *rowptr, int *col, double *val, char *err,
+                                int err_capacity);
+UG4GB_API int ug4gb_io_write_cv_matrix(int num_rows, const int *rowptr, const int *col, const double *val, int dim,
+                                       const double *positions, const char *filename, char *err, int err_capacity);
+UG4GB_API int ug4gb_io_write_cv_vector(int n, const double *values, int dim, const double *positions,
+                                       const char *filename, char *err, int err_capacity);
+UG4GB_API int ug4gb_io_read_cv_vector(const char *filename, int n, double *values, char *err, int err_capacity);
+/* the same for device matrices and vectors (copied through the host) */
+UG4GB_API int ug4gb_matrix_write_mtx(const ug4gb_matrix *A, const char *filename, const char *comment);
+UG4GB_API int ug4gb_matrix_read_mtx(ug4gb_matrix *A, const char *filename);
+UG4GB_API int ug4gb_matrix_write_cv(const ug4gb_matrix *A, const ug4gb_grid *g, int level, const char *filename);
+UG4GB_API int ug4gb_vector_write_cv(const ug4gb_vector *v, const ug4gb_grid *g, int level, const char *filename);
+UG4GB_API int ug4gb_vector_read_cv(ug4gb_vector *v, const char *filename);
+
 #ifdef __cplusplus
 }
 #endif

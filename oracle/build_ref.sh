@@ -35,6 +35,85 @@ uint32_t crc32(const char *s)
 }
 }
 EOC
+# ugcore's MatrixMarket reader uses boost::algorithm::split / is_any_of and
+# boost::lexical_cast; these stand-ins implement the behaviour it relies on
+mkdir -p "$OUT/shim/boost/algorithm"
+cat > "$OUT/shim/boost/algorithm/string.hpp" <<'EOC'
+#pragma once
+#include <string>
+namespace boost {
+namespace algorithm {
+enum token_compress_mode_type { token_compress_on, token_compress_off };
+struct any_of_pred {
+    std::string set;
+    bool operator()(char c) const { return set.find(c) != std::string::npos; }
+};
+/* tokens between separators; with token_compress_on a run of separators is one */
+template <class Seq>
+Seq &split(Seq &out, const std::string &in, any_of_pred p, token_compress_mode_type m = token_compress_off)
+{
+    out.clear();
+    std::string cur;
+    size_t i = 0;
+    for (;;) {
+        if (i == in.size()) { out.push_back(cur); break; }
+        if (p(in[i])) {
+            out.push_back(cur);
+            cur.clear();
+            ++i;
+            if (m == token_compress_on)
+                while (i < in.size() && p(in[i])) ++i;
+            continue;
+        }
+        cur += in[i++];
+    }
+    return out;
+}
+}
+inline algorithm::any_of_pred is_any_of(const char *s) { return algorithm::any_of_pred{s}; }
+using algorithm::split;
+using algorithm::token_compress_on;
+using algorithm::token_compress_off;
+}
+EOC
+cat > "$OUT/shim/boost/lexical_cast.hpp" <<'EOC'
+#pragma once
+#include <cerrno>
+#include <cmath>
+#include <cstdlib>
+#include <string>
+#include <type_traits>
+#include <typeinfo>
+namespace boost {
+struct bad_lexical_cast : std::bad_cast {};
+/* the whole string must convert (integers base 10, doubles as strtod); an
+   integer out of range and a double that overflows fail, an underflowing
+   double converts (as a stream extraction, which lexical_cast uses, does) */
+template <class T>
+T lexical_cast(const std::string &s)
+{
+    const char *b = s.c_str();
+    char *e = nullptr;
+    errno = 0;
+    T v;
+    bool range = false;
+    if (std::is_floating_point<T>::value) {
+        const double d = std::strtod(b, &e);
+        range = errno == ERANGE && (d == HUGE_VAL || d == -HUGE_VAL);
+        v = (T)d;
+    } else if (std::is_signed<T>::value) {
+        v = (T)std::strtoll(b, &e, 10);
+        range = errno == ERANGE;
+    } else {
+        if (s.find('-') != std::string::npos) throw bad_lexical_cast();
+        v = (T)std::strtoull(b, &e, 10);
+        range = errno == ERANGE;
+    }
+    if (s.empty() || e != b + s.size() || range) throw bad_lexical_cast();
+    return v;
+}
+}
+EOC
 CXX=${CXX:-g++}
 FLAGS="-std=c++17 -O3 -DNDEBUG -w -I$OUT/shim -I$REF/ugbase -I$HERE"
 SRCS="common/log.cpp common/debug_id.cpp common/assert.cpp common/error.cpp common/progress.cpp \
@@ -57,4 +136,18 @@ done
 $CXX $FLAGS "$HERE/ref_driver.cpp" $OBJS "$OUT/obj/crc32_stub.o" \
     "$OUT/obj/ug4_oracle_grid.o" "$OUT/obj/ug4_oracle_fv1.o" "$OUT/obj/ug4_oracle_solve.o" \
     "$OUT/obj/ug4_oracle_api.o" -o "$OUT/ref_driver" -lm
-echo "build_ref: built $OUT/ref_driver"
+# ugcore's matrix / vector file writers and readers (MatrixIOMtx, ConnectionViewer)
+IOSRCS="common/util/file_util.cpp common/util/os_dependent_impl/file_util_posix.cpp \
+common/util/os_dependent_impl/os_info_linux.cpp lib_algebra/common/matrixio/matrix_io.cpp \
+lib_algebra/common/matrixio/matrix_io_mtx.cpp lib_algebra/common/connection_viewer_output.cpp"
+IOOBJS=""
+for s in $IOSRCS; do
+    o="$OUT/obj/$(echo "$s" | tr '/' '_' | sed 's/\.cpp$/.o/')"
+    if [ ! -f "$o" ] || [ "$REF/ugbase/$s" -nt "$o" ]; then
+        $CXX $FLAGS -c "$REF/ugbase/$s" -o "$o" &
+    fi
+    IOOBJS="$IOOBJS $o"
+done
+wait
+$CXX $FLAGS "$HERE/ref_io.cpp" $IOOBJS $OBJS "$OUT/obj/crc32_stub.o" -o "$OUT/ref_io"
+echo "build_ref: built $OUT/ref_driver $OUT/ref_io"

@@ -126,6 +126,17 @@ _SIGS = {
     "ug4gb_solver_destroy": (None, [P]),
     "ug4gb_disc_grad_logk": (I, [P, P, P, P]),
     "ug4gb_disc_grad_source": (I, [P, P, P]),
+    "ug4gb_io_write_mtx": (I, [I, I, P, P, P, C.c_char_p, C.c_char_p, C.c_char_p, I]),
+    "ug4gb_io_read_mtx_info": (I, [C.c_char_p, PI, PI, PI64, C.c_char_p, I]),
+    "ug4gb_io_read_mtx": (I, [C.c_char_p, P, P, P, C.c_char_p, I]),
+    "ug4gb_io_write_cv_matrix": (I, [I, P, P, P, I, P, C.c_char_p, C.c_char_p, I]),
+    "ug4gb_io_write_cv_vector": (I, [I, P, I, P, C.c_char_p, C.c_char_p, I]),
+    "ug4gb_io_read_cv_vector": (I, [C.c_char_p, I, P, C.c_char_p, I]),
+    "ug4gb_matrix_write_mtx": (I, [P, C.c_char_p, C.c_char_p]),
+    "ug4gb_matrix_read_mtx": (I, [P, C.c_char_p]),
+    "ug4gb_matrix_write_cv": (I, [P, P, I, C.c_char_p]),
+    "ug4gb_vector_write_cv": (I, [P, P, I, C.c_char_p]),
+    "ug4gb_vector_read_cv": (I, [P, C.c_char_p]),
 }
 
 _lib = None
