@@ -192,6 +192,13 @@ UG4GB_API int ug4gb_disc_set_source_uniform(ug4gb_disc *d, uint64_t seed);
 UG4GB_API int ug4gb_disc_assemble_linear(ug4gb_disc *d, int level, ug4gb_matrix *A, ug4gb_vector *b);
 /* DomainDiscretizationBase::assemble_jacobian (domain_disc_impl.h:471) */
 UG4GB_API int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matrix *A);
+/* DomainDiscretizationBase::assemble_defect (domain_disc_impl.h:648):
+   d = A(u) u - f assembled element by element (add_def_A_elem + add_rhs_elem,
+   elem_disc_assemble_util.h:578-690), d = 0 at Dirichlet vertices
+   (DirichletBoundary::adjust_defect).  The source enters on the top level. */
+UG4GB_API int ug4gb_disc_assemble_defect(ug4gb_disc *d, int level, const ug4gb_vector *u, ug4gb_vector *dvec);
+/* DomainDiscretizationBase::adjust_solution: u = 0 at the Dirichlet vertices */
+UG4GB_API int ug4gb_disc_adjust_solution(ug4gb_disc *d, int level, ug4gb_vector *u);
 /* AT = A^T with the Dirichlet rows of `level` reset to identity: the operator
    of the adjoint (transposed) solve.  No ugcore counterpart (ugcore has
    SparseMatrix::set_as_transpose_of, sparsematrix_impl.h:149, and
@@ -215,6 +222,11 @@ UG4GB_API int ug4gb_timedisc_future_time(const ug4gb_timedisc *td, double *t);
 UG4GB_API int ug4gb_timedisc_assemble_linear(ug4gb_timedisc *td, int level, ug4gb_matrix *A, ug4gb_vector *b);
 /* assemble_jacobian(J) = M + theta dt A of any level */
 UG4GB_API int ug4gb_timedisc_assemble_jacobian(ug4gb_timedisc *td, int level, ug4gb_matrix *A);
+/* ThetaTimeStep::assemble_defect (theta_time_step_impl.h:200-240, instationary
+   AssembleDefect, elem_disc_assemble_util.h:713-860): the defect of u at the
+   future time with the stored previous solution, top level only */
+UG4GB_API int ug4gb_timedisc_assemble_defect(ug4gb_timedisc *td, int level, const ug4gb_vector *u,
+                                             ug4gb_vector *dvec);
 UG4GB_API void ug4gb_timedisc_destroy(ug4gb_timedisc *td);
 
 UG4GB_API int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A, ug4gb_matrix *AT);
@@ -286,6 +298,30 @@ UG4GB_API int ug4gb_solver_get_stats(const ug4gb_solver *s, int *steps, double *
 /* defect history: hist[0] = initial defect, hist[i] = defect after step i */
 UG4GB_API int ug4gb_solver_get_history(const ug4gb_solver *s, double *hist, int capacity);
 UG4GB_API void ug4gb_solver_destroy(ug4gb_solver *s);
+
+/* ------------------------------------------------------------- Newton -- */
+/* NewtonSolver (lib_disc/operator/non_linear_operator/newton_solver/newton.h:62,
+   newton_impl.h:171-340) without line search: the operator is the stationary
+   FV1 discretisation (init(nw, d, NULL)) or a prepared ThetaTimeStep
+   (init(nw, NULL, td)); every step assembles the jacobian, initialises the
+   linear solver and its multigrid with it, solves J c = d from c = 0, sets
+   u -= c and the Dirichlet values, and assembles the new defect.  Convergence
+   by StdConvCheck rules on |d|; UG4GB_ERR_NOT_CONVERGED when the step limit is
+   reached first, the linear solver's code when a linear solve fails. */
+typedef struct ug4gb_newton ug4gb_newton;
+UG4GB_API int ug4gb_newton_create(ug4gb_ctx *ctx, ug4gb_newton **out);
+UG4GB_API int ug4gb_newton_set_linear_solver(ug4gb_newton *nw, ug4gb_solver *s);
+UG4GB_API int ug4gb_newton_set_convergence_check(ug4gb_newton *nw, int max_steps, double min_defect,
+                                                 double reduction);
+UG4GB_API int ug4gb_newton_init(ug4gb_newton *nw, ug4gb_disc *d, ug4gb_timedisc *td);
+UG4GB_API int ug4gb_newton_prepare(ug4gb_newton *nw, ug4gb_vector *u);     /* Dirichlet values into u */
+UG4GB_API int ug4gb_newton_apply(ug4gb_newton *nw, ug4gb_vector *u);
+/* Newton steps, |d| at start and end, and the linear solver's steps per Newton step */
+UG4GB_API int ug4gb_newton_get_stats(const ug4gb_newton *nw, int *steps, double *initial_defect,
+                                     double *final_defect, int *lin_steps, int capacity);
+/* |d| after each Newton step (entry 0: start); returns the number available */
+UG4GB_API int ug4gb_newton_get_history(const ug4gb_newton *nw, double *defects, int capacity);
+UG4GB_API void ug4gb_newton_destroy(ug4gb_newton *nw);
 
 /* ------------------------------------------------------------ adjoint -- */
 /* No ugcore counterpart.  Gradients of J(u) with A(m) u = b(f), K = exp(m):

@@ -72,6 +72,9 @@ def lib():
         L.orc_prob_theta_system.argtypes = [P, C.c_double, C.c_double, dp, ip, ip, dp, dp]
         L.orc_prob_theta_steps.argtypes = [P, C.c_double, C.c_double, C.c_int, dp, ip]
         L.orc_prob_theta_jacobian.argtypes = [P, C.c_int, C.c_double, C.c_double, ip, ip, dp]
+        L.orc_prob_defect.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, dp]
+        L.orc_prob_newton.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, C.c_int, C.c_double, C.c_double,
+                                      ip, ip, dp]
         L.orc_prob_gmg_level_nnz.argtypes = [P, C.c_int]
         L.orc_prob_gmg_level_nnz.restype = C.c_int64
         L.orc_prob_gmg_level.argtypes = [P, C.c_int, ip, ip, dp]
@@ -146,6 +149,33 @@ class Problem:
         if rc:
             raise RuntimeError("theta assembly failed")
         return (rp, ci, va), b
+
+    def defect(self, u, theta=None, dt=0.0, u_old=None):
+        """top-level defect of u: stationary, or of one theta step from u_old"""
+        d = np.zeros(self.nv())
+        uo = None if u_old is None else np.ascontiguousarray(u_old, np.float64)
+        rc = lib().orc_prob_defect(self.h, -1.0 if theta is None else theta, dt,
+                                   None if uo is None else uo.ctypes.data_as(C.c_void_p),
+                                   np.ascontiguousarray(u, np.float64), d)
+        if rc:
+            raise RuntimeError("defect failed")
+        return d
+
+    def newton(self, u0, maxit=10, min_defect=1e-50, reduction=1e-10, theta=None, dt=0.0, u_old=None):
+        """NewtonSolver on the stationary operator or one theta step; returns
+        (u, rc, steps, linear steps per step, defects)"""
+        u = np.array(u0, dtype=np.float64, copy=True)
+        steps = np.zeros(1, np.int32)
+        ls = np.zeros(maxit + 1, np.int32)
+        defs = np.zeros(maxit + 1)
+        uo = None if u_old is None else np.ascontiguousarray(u_old, np.float64)
+        rc = lib().orc_prob_newton(self.h, -1.0 if theta is None else theta, dt,
+                                   None if uo is None else uo.ctypes.data_as(C.c_void_p), u, maxit, min_defect,
+                                   reduction, steps, ls, defs)
+        if rc < 0:
+            raise RuntimeError("Newton set-up failed %d" % rc)
+        n = int(steps[0])
+        return u, rc, n, ls[:n], defs[:n + 1]
 
     def theta_jacobian(self, l, theta, dt):
         """level l's M + theta dt A (CRS pattern = the level's)"""

@@ -118,6 +118,7 @@ typedef struct {
 } orc_disc;
 
 int orc_assemble(const orc_level *L, const orc_disc *D, orc_crs *A, double *b);
+int orc_assemble_defect(const orc_level *L, const orc_disc *D, const double *u, double *d);
 void orc_scv_volume_sum(const orc_level *L, double *vol);
 int orc_element_matrix(const orc_level *L, int e, double K, const orc_field *vf, int upwind,
                        double *Aloc, double *vol);
@@ -175,6 +176,11 @@ typedef struct {
 } orc_conv;
 
 int orc_cg(const orc_crs *A, orc_gmg *M, double *x, double *b, orc_conv *C);
+void orc_conv_start(orc_conv *C, double d);
+void orc_conv_update(orc_conv *C, double d);
+int orc_conv_ended(const orc_conv *C);
+int orc_conv_post(orc_conv *C);
+double orc_vnorm(int n, const double *a);
 int orc_bicgstab(const orc_crs *A, orc_gmg *M, double *x, double *b, orc_conv *C);
 
 /* full forward problem helper used by the tests */

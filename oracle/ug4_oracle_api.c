@@ -299,6 +299,95 @@ int orc_prob_theta_steps(orc_prob *P, double theta, double dt, int nsteps, doubl
     return rc;
 }
 
+/* ---- defect and Newton ----------------------------------------------- */
+static void prob_disc(const orc_prob *P, int l, orc_disc *D)
+{
+    memset(D, 0, sizeof(*D));
+    D->K = P->K[l];
+    D->upwind = P->has_vf ? 1 : 0;
+    D->vfield = P->has_vf ? &P->vf : NULL;
+    D->f = (l == P->H.nlev - 1) ? P->f : NULL;
+    D->dirichlet = 1;
+}
+
+/* top-level defect of u: stationary (theta < 0) or of one theta step from
+   u_old (ThetaTimeStep::assemble_defect, s_m = (1, -1),
+   s_a = (theta dt, (1 - theta) dt)) */
+int orc_prob_defect(const orc_prob *P, double theta, double dt, const double *u_old, const double *u, double *d)
+{
+    const int top = P->H.nlev - 1;
+    orc_disc D;
+    prob_disc(P, top, &D);
+    if (theta >= 0.0) {
+        if (!u_old) return -1;
+        D.inst = 1;
+        D.sm0 = 1.0; D.sa0 = theta * dt; D.sm1 = -1.0; D.sa1 = (1.0 - theta) * dt;
+        D.u_old = u_old;
+    }
+    return orc_assemble_defect(&P->H.lev[top], &D, u, d);
+}
+
+/* NewtonSolver::apply (newton_impl.h:171-340, no line search) with the
+   problem's GMG-preconditioned Krylov solver as the linear solver (its own
+   convergence parameters) on the stationary operator (theta < 0) or the
+   theta step from u_old.  u in/out.  Returns 0 if Newton converged, 1 if not,
+   2 if a linear solve failed, < 0 on set-up errors.  steps: Newton steps;
+   lin_steps[s], defects[s] (s <= maxit, defects[0] the start defect). */
+int orc_prob_newton(orc_prob *P, double theta, double dt, const double *u_old, double *u, int maxit,
+                    double min_defect, double reduction, int *steps, int *lin_steps, double *defects)
+{
+    const int nl = P->H.nlev, top = nl - 1, nv = P->H.lev[top].nv;
+    const orc_level *L = &P->H.lev[top];
+    double *d = (double *)malloc(sizeof(double) * (size_t)nv);
+    double *c = (double *)malloc(sizeof(double) * (size_t)nv);
+    double *rhs = (double *)malloc(sizeof(double) * (size_t)nv);
+    orc_crs *J = (orc_crs *)calloc((size_t)nl, sizeof(orc_crs));
+    if (!d || !c || !rhs || !J) return -1;
+    int rc = 0;
+    orc_conv NC;
+    memset(&NC, 0, sizeof(NC));
+    NC.maxit = maxit; NC.min_defect = min_defect; NC.rel_red = reduction;
+    for (int i = 0; i < nv; ++i) if (L->bnd[i]) u[i] = 0.0;          /* prepare */
+    if (orc_prob_defect(P, theta, dt, u_old, u, d)) return -1;
+    orc_conv_start(&NC, orc_vnorm(nv, d));
+    if (defects) defects[0] = NC.initial_defect;
+    while (!orc_conv_ended(&NC)) {
+        memset(c, 0, sizeof(double) * (size_t)nv);
+        /* jacobian of every level (the linear solver's multigrid is set up with it) */
+        for (int l = 0; l < nl; ++l) {
+            orc_crs_free(&J[l]);
+            orc_disc D;
+            prob_disc(P, l, &D);
+            D.f = NULL;
+            if (theta >= 0.0) {
+                D.inst = 1;
+                D.sm0 = 1.0; D.sa0 = theta * dt; D.sm1 = 0.0; D.sa1 = 0.0;
+            }
+            if (orc_assemble(&P->H.lev[l], &D, &J[l], NULL)) return -1;
+        }
+        orc_gmg G;
+        memset(&G, 0, sizeof(G));
+        const orc_params *p = &P->p;
+        if (orc_gmg_init(&G, &P->H, J, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap)) return -2;
+        memcpy(rhs, d, sizeof(double) * (size_t)nv);
+        int ls = 0;
+        const int lrc = run_solver(p, &J[top], &G, c, rhs, &ls, NULL, NULL, NULL, 0);
+        orc_gmg_free(&G);
+        if (lin_steps) lin_steps[NC.steps] = ls;
+        if (lrc) { rc = 2; break; }
+        for (int i = 0; i < nv; ++i) u[i] -= c[i];
+        for (int i = 0; i < nv; ++i) if (L->bnd[i]) u[i] = 0.0;      /* prepare */
+        if (orc_prob_defect(P, theta, dt, u_old, u, d)) return -1;
+        orc_conv_update(&NC, orc_vnorm(nv, d));
+        if (defects) defects[NC.steps] = NC.final_defect;
+    }
+    if (rc == 0) rc = orc_conv_post(&NC) ? 0 : 1;
+    if (steps) *steps = NC.steps;
+    for (int l = 0; l < nl; ++l) orc_crs_free(&J[l]);
+    free(J); free(d); free(c); free(rhs);
+    return rc;
+}
+
 /* transposed operator with Dirichlet rows reset to identity */
 static int transpose_dirichlet(const orc_crs *A, const orc_level *L, orc_crs *T)
 {

@@ -356,6 +356,69 @@ int orc_assemble(const orc_level *L, const orc_disc *D, orc_crs *A, double *b)
     return 0;
 }
 
+/* Defect d = A(u) u - f of the level (DomainDiscretization::assemble_defect,
+   lib_disc/spatial_disc/domain_disc_impl.h:648; StdGlobAssembler::
+   AssembleDefect, elem_disc_assemble_util.h:578-690): per element
+   locD = A_e u_e (add_def_A_elem, restated as the element operator applied to
+   the local solution), locD += (-1) rhs_e (add_rhs_elem, scale_append), added
+   to d in element order; Dirichlet vertices get d = 0
+   (DirichletBoundary::adjust_defect, lagrange_dirichlet_boundary_impl.h:
+   972-1033).  With D->inst the instationary AssembleDefect
+   (elem_disc_assemble_util.h:713-860) for the time points (u, u_old) with
+   s_m = (sm0, sm1), s_a = (sa0, sa1): per time point t,
+   locD += s_m[t] M_e u_t, then (s_a[t] != 0) locD += s_a[t] A_e u_t and
+   locD += (-s_a[t]) rhs_e; M_e = diag(|SCV_i|). */
+int orc_assemble_defect(const orc_level *L, const orc_disc *D, const double *u, double *d)
+{
+    const int k = L->k, dim = L->dim;
+    memset(d, 0, sizeof(double) * (size_t)L->nv);
+    double corner[24], vel[36];
+    orc_fv1geom G;
+    double Aloc[8][8];
+    for (int e = 0; e < L->ne; ++e) {
+        element_corners(L, e, corner);
+        orc_fv1_geometry(L->elem_type, corner, &G);
+        const double *v = NULL;
+        if (D->upwind) {
+            if (D->vel) v = D->vel + (size_t)e * G.nscvf * dim;
+            else if (D->vfield) {
+                for (int ip = 0; ip < G.nscvf; ++ip) orc_field_curl_eval(D->vfield, G.gip[ip], vel + ip * dim);
+                v = vel;
+            }
+        }
+        const double K = D->K ? D->K[e] : 1.0;
+        element_matrix(L->elem_type, &G, dim, k, K, v, D->upwind, Aloc);
+        const int *ev = L->elems + (size_t)e * k;
+        for (int i = 0; i < k; ++i) {
+            const double fv = (D->f ? D->f[ev[i]] : 0.0) * G.vol[i];
+            double au = 0.0;
+            for (int j = 0; j < k; ++j) au = au + Aloc[i][j] * u[ev[j]];
+            double r;
+            if (!D->inst) {
+                r = au + (-1.0) * fv;
+            } else {
+                r = 0.0 + D->sm0 * (G.vol[i] * u[ev[i]]);
+                if (D->sa0 != 0.0) {
+                    r = r + D->sa0 * au;
+                    r = r + (-D->sa0) * fv;
+                }
+                r = r + D->sm1 * (G.vol[i] * D->u_old[ev[i]]);
+                if (D->sa1 != 0.0) {
+                    double ao = 0.0;
+                    for (int j = 0; j < k; ++j) ao = ao + Aloc[i][j] * D->u_old[ev[j]];
+                    r = r + D->sa1 * ao;
+                    r = r + (-D->sa1) * fv;
+                }
+            }
+            d[ev[i]] += r;
+        }
+    }
+    if (D->dirichlet)
+        for (int v = 0; v < L->nv; ++v)
+            if (L->bnd[v]) d[v] = 0.0;
+    return 0;
+}
+
 /* sum over elements of the SCV volume of each vertex: d rhs_i / d f_i */
 void orc_scv_volume_sum(const orc_level *L, double *vol)
 {

@@ -385,6 +385,13 @@ static int conv_post(orc_conv *C)
     return C->converged;
 }
 
+/* StdConvCheck for callers outside this file (the Newton loop) */
+void orc_conv_start(orc_conv *C, double d) { conv_start(C, d); }
+void orc_conv_update(orc_conv *C, double d) { conv_update(C, d); }
+int orc_conv_ended(const orc_conv *C) { return conv_ended(C); }
+int orc_conv_post(orc_conv *C) { return conv_post(C); }
+double orc_vnorm(int n, const double *a) { return vnorm(n, a); }
+
 int orc_cg(const orc_crs *A, orc_gmg *M, double *x, double *b, orc_conv *C)
 {
     int n = A->n_rows;

@@ -7,9 +7,10 @@ CUDA library; importing works without a GPU, but creating a Context needs one
 and there is no CPU fallback.
 """
 from ._lib import UG4GBError, exported_symbols, LIB_PATH  # noqa: F401
-from .algebra import (BiCGStab, CG, Context, DomainDiscretization, GaussSeidel, GeometricMultiGrid,  # noqa: F401
-                      GPUSparseMatrix, GPUVector, Jacobi, StdConvCheck, StructuredHierarchy, ThetaTimeStep)
+from .algebra import (AssembledOperator, BiCGStab, CG, Context, DomainDiscretization, GaussSeidel,  # noqa: F401
+                      GeometricMultiGrid, GPUSparseMatrix, GPUVector, Jacobi, NewtonSolver, StdConvCheck,
+                      StructuredHierarchy, ThetaTimeStep)
 
 __all__ = ["UG4GBError", "Context", "StructuredHierarchy", "GPUVector", "GPUSparseMatrix", "DomainDiscretization",
            "GeometricMultiGrid", "Jacobi", "GaussSeidel", "StdConvCheck", "CG", "BiCGStab", "ThetaTimeStep",
-           "exported_symbols"]
+           "AssembledOperator", "NewtonSolver", "exported_symbols"]

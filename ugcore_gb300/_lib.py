@@ -106,7 +106,19 @@ _SIGS = {
     "ug4gb_timedisc_future_time": (I, [P, P]),
     "ug4gb_timedisc_assemble_linear": (I, [P, I, P, P]),
     "ug4gb_timedisc_assemble_jacobian": (I, [P, I, P]),
+    "ug4gb_timedisc_assemble_defect": (I, [P, I, P, P]),
     "ug4gb_timedisc_destroy": (None, [P]),
+    "ug4gb_disc_assemble_defect": (I, [P, I, P, P]),
+    "ug4gb_disc_adjust_solution": (I, [P, I, P]),
+    "ug4gb_newton_create": (I, [P, PP]),
+    "ug4gb_newton_set_linear_solver": (I, [P, P]),
+    "ug4gb_newton_set_convergence_check": (I, [P, I, D, D]),
+    "ug4gb_newton_init": (I, [P, P, P]),
+    "ug4gb_newton_prepare": (I, [P, P]),
+    "ug4gb_newton_apply": (I, [P, P]),
+    "ug4gb_newton_get_stats": (I, [P, PI, PD, PD, P, I]),
+    "ug4gb_newton_get_history": (I, [P, P, I]),
+    "ug4gb_newton_destroy": (None, [P]),
     "ug4gb_gmg_level_info": (I, [P, I, P, P]),
     "ug4gb_gmg_export_level": (I, [P, I, P, P, P]),
     "ug4gb_gmg_init": (I, [P, P]),

@@ -346,6 +346,16 @@ class DomainDiscretization:
         level = self.hier.top if level is None else level
         check(lib().ug4gb_disc_assemble_jacobian(self.h, level, A.h), self.ctx.h)
 
+    def assemble_defect(self, d, u, level=None):
+        """d = A(u) u - f element by element, 0 at Dirichlet vertices"""
+        level = self.hier.top if level is None else level
+        check(lib().ug4gb_disc_assemble_defect(self.h, level, u.h, d.h), self.ctx.h)
+
+    def adjust_solution(self, u, level=None):
+        """Dirichlet values (0) into u"""
+        level = self.hier.top if level is None else level
+        check(lib().ug4gb_disc_adjust_solution(self.h, level, u.h), self.ctx.h)
+
     def adjoint_operator(self, A, AT, level=None):
         """AT = A^T with Dirichlet rows reset to identity."""
         level = self.hier.top if level is None else level
@@ -408,6 +418,10 @@ class ThetaTimeStep:
     def assemble_jacobian(self, A, level=None):
         level = self.disc.hier.num_levels - 1 if level is None else level
         check(lib().ug4gb_timedisc_assemble_jacobian(self.h, level, A.h), self.ctx.h)
+
+    def assemble_defect(self, d, u):
+        """time-discrete defect of u at the future time (top level)"""
+        check(lib().ug4gb_timedisc_assemble_defect(self.h, self.disc.hier.num_levels - 1, u.h, d.h), self.ctx.h)
 
 
 class Jacobi:
@@ -564,6 +578,70 @@ class _Krylov:
         cap = self.conv.max_steps + 2
         buf = np.zeros(cap)
         n = lib().ug4gb_solver_get_history(self.h, _ptr(buf), cap)
+        return buf[:max(n, 0)]
+
+
+class AssembledOperator:
+    """AssembledOperator(domainDisc | timeDisc): the nonlinear operator N(u)
+    whose defect and jacobian the discretisation assembles"""
+
+    def __init__(self, disc):
+        self.disc = disc
+
+
+class NewtonSolver:
+    """NewtonSolver (newton.h:62) without line search: set_linear_solver,
+    set_convergence_check, init(AssembledOperator), prepare(u), apply(u)."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        h = C.c_void_p()
+        check(lib().ug4gb_newton_create(ctx.h, C.byref(h)), ctx.h)
+        self.h = h
+        self.conv = StdConvCheck(10, 1e-50, 1e-10)
+        check(lib().ug4gb_newton_set_convergence_check(self.h, 10, 1e-50, 1e-10), ctx.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_newton_destroy(self.h)
+            self.h = None
+
+    def set_linear_solver(self, solver):
+        self._lin = solver
+        check(lib().ug4gb_newton_set_linear_solver(self.h, solver.h), self.ctx.h)
+
+    def set_convergence_check(self, cc):
+        self.conv = cc
+        check(lib().ug4gb_newton_set_convergence_check(self.h, cc.max_steps, cc.min_defect, cc.rel_reduction),
+              self.ctx.h)
+
+    def init(self, op):
+        d = op.disc if isinstance(op, AssembledOperator) else op
+        self._op = d
+        if isinstance(d, ThetaTimeStep):
+            check(lib().ug4gb_newton_init(self.h, None, d.h), self.ctx.h)
+        else:
+            check(lib().ug4gb_newton_init(self.h, d.h, None), self.ctx.h)
+
+    def prepare(self, u):
+        check(lib().ug4gb_newton_prepare(self.h, u.h), self.ctx.h)
+
+    def apply(self, u, raise_on_failure=True):
+        rc = lib().ug4gb_newton_apply(self.h, u.h)
+        if rc != 0 and (raise_on_failure or rc != _lib.ERR_NOT_CONVERGED):
+            check(rc, self.ctx.h)
+        return rc == 0
+
+    def stats(self):
+        steps, d0, d1 = C.c_int(), C.c_double(), C.c_double()
+        ls = np.zeros(self.conv.max_steps + 1, np.int32)
+        check(lib().ug4gb_newton_get_stats(self.h, C.byref(steps), C.byref(d0), C.byref(d1), _ptr(ls), len(ls)))
+        return dict(steps=steps.value, initial_defect=d0.value, defect=d1.value,
+                    linear_steps=[int(x) for x in ls[:steps.value]])
+
+    def history(self):
+        buf = np.zeros(self.conv.max_steps + 2)
+        n = lib().ug4gb_newton_get_history(self.h, _ptr(buf), len(buf))
         return buf[:max(n, 0)]
 
 

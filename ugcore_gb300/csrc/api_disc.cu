@@ -96,6 +96,46 @@ void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const T
     launch_dirichlet(c, L, A->A, b);
 }
 
+// defect of u on `level` into dvec (stationary, or with ts the time-discrete
+// defect of one step from ts->u_old)
+void disc_defect(ug4gb_disc *d, int level, const double *u, double *dvec, const TimeScale *ts)
+{
+    Ctx &c = d->ctx->c;
+    const Level &L = d->g->lev[level];
+    const DiscImpl &D = d->d;
+    const bool top = (level == (int)d->g->lev.size() - 1);
+    UG_CUDA(cudaMemsetAsync(dvec, 0, sizeof(double) * (size_t)L.nv, c.stream));
+    AsmArgs a;
+    a.coords = L.coords.p;
+    a.elems = L.elems.p;
+    a.ne = L.ne;
+    a.K = disc_coefficients(d, level);
+    a.f = (top && D.f_kind == 1) ? D.f_top.p : nullptr;
+    a.f_seed = D.f_seed;
+    a.use_seed = (top && D.f_kind == 2) ? 1 : 0;
+    a.vmodes = D.upwind ? D.vmodes : 0;
+    a.vk = D.vk.p;
+    a.vc = D.vc.p;
+    a.vphase = D.vphase.p;
+    a.vscale = D.vscale;
+    a.rowptr = nullptr;
+    a.col = nullptr;
+    a.val = nullptr;
+    a.b = nullptr;
+    a.u = u;
+    a.d = dvec;
+    if (ts) {
+        UG_REQUIRE(top && ts->u_old, UG4GB_ERR_INVALID, "time-discrete defect: top level with a previous solution");
+        a.inst = 1;
+        a.sm0 = ts->sm0;
+        a.sa0 = ts->sa0;
+        a.sm1 = ts->sm1;
+        a.sa1 = ts->sa1;
+        a.u_old = ts->u_old;
+    }
+    launch_defect(c, L, a);
+}
+
 }  // namespace ug4gb
 
 template <class F>
@@ -247,6 +287,30 @@ int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matrix *A)
     });
 }
 
+int ug4gb_disc_assemble_defect(ug4gb_disc *d, int level, const ug4gb_vector *u, ug4gb_vector *dvec)
+{
+    if (!d || !u || !dvec || u == dvec || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
+    const int nv = d->g->lev[level].nv;
+    if (u->n != nv || dvec->n != nv) {
+        d->ctx->c.err = "assemble_defect: vector sizes != level vertices";
+        return UG4GB_ERR_INVALID;
+    }
+    return guarded(d->ctx, [&] {
+        disc_defect(d, level, u->d, dvec->d, nullptr);
+        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+    });
+}
+
+int ug4gb_disc_adjust_solution(ug4gb_disc *d, int level, ug4gb_vector *u)
+{
+    if (!d || !u || level < 0 || level >= (int)d->g->lev.size() || u->n != d->g->lev[level].nv)
+        return UG4GB_ERR_INVALID;
+    return guarded(d->ctx, [&] {
+        launch_dirichlet_values(d->ctx->c, d->g->lev[level], u->d);
+        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+    });
+}
+
 // ---- ThetaTimeStep ------------------------------------------------------
 int ug4gb_timedisc_create(ug4gb_ctx *ctx, ug4gb_disc *d, ug4gb_timedisc **out)
 {
@@ -321,6 +385,25 @@ int ug4gb_timedisc_assemble_jacobian(ug4gb_timedisc *td, int level, ug4gb_matrix
     return guarded(td->ctx, [&] {
         const TimeScale ts = td->jacobian_scale();
         disc_assemble(td->disc, level, A, nullptr, &ts);
+        UG_CUDA(cudaStreamSynchronize(td->ctx->c.stream));
+    });
+}
+
+int ug4gb_timedisc_assemble_defect(ug4gb_timedisc *td, int level, const ug4gb_vector *u, ug4gb_vector *dvec)
+{
+    if (!td || !u || !dvec || u == dvec) return UG4GB_ERR_INVALID;
+    ug4gb_disc *d = td->disc;
+    if (level != (int)d->g->lev.size() - 1 || u->n != d->g->lev[level].nv || dvec->n != u->n) {
+        td->ctx->c.err = "time-discrete assemble_defect: top level, vectors of the level's size";
+        return UG4GB_ERR_INVALID;
+    }
+    if (!td->prepared) {
+        td->ctx->c.err = "time-discrete assemble_defect: prepare_step not called";
+        return UG4GB_ERR_STATE;
+    }
+    return guarded(td->ctx, [&] {
+        const TimeScale ts = td->defect_scale();
+        disc_defect(d, level, u->d, dvec->d, &ts);
         UG_CUDA(cudaStreamSynchronize(td->ctx->c.stream));
     });
 }

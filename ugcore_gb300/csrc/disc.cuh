@@ -28,6 +28,9 @@ struct AsmArgs {
     int inst = 0;
     double sm0 = 0.0, sa0 = 1.0, sm1 = 0.0, sa1 = 0.0;
     const double *u_old = nullptr;
+    // defect assembly (launch_defect): d += per-element defect of u
+    const double *u = nullptr;
+    double *d = nullptr;
 };
 
 // scalings of a time-discrete assembly (one previous time point)
@@ -38,6 +41,11 @@ struct TimeScale {
 
 void launch_assemble(Ctx &c, const Level &L, const AsmArgs &a);
 void launch_dirichlet(Ctx &c, const Level &L, Csr &A, double *b);
+// d = defect of a.u on level L (a.d must be zero on entry; Dirichlet rows 0);
+// stationary, or instationary with a.inst and the scalings of AsmArgs
+void launch_defect(Ctx &c, const Level &L, const AsmArgs &a);
+// u = 0 at the Dirichlet vertices of L (DirichletBoundary::adjust_solution)
+void launch_dirichlet_values(Ctx &c, const Level &L, double *u);
 void launch_coef_fourier(Ctx &c, const Level &L, int nmodes, const double *k, const double *phase, double amp,
                          double factor, double *K);
 void coarsen_log(Ctx &c, const Level &F, const Level &Cl, const double *logf, double *logc);

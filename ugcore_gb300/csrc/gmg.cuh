@@ -134,6 +134,12 @@ struct ug4gb_timedisc {
     {
         return ug4gb::TimeScale{1.0, theta * dt, 0.0, 0.0, nullptr};
     }
+    // defect of the time points (u, u_old) with s_m = (1, -1),
+    // s_a = (theta dt, (1 - theta) dt) (theta_time_step_impl.h:200-240)
+    ug4gb::TimeScale defect_scale() const
+    {
+        return ug4gb::TimeScale{1.0, theta * dt, -1.0, (1.0 - theta) * dt, u_old.p};
+    }
 };
 
 struct ug4gb_gmg {

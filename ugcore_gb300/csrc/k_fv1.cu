@@ -173,6 +173,110 @@ void launch_dirichlet(Ctx &c, const Level &L, Csr &A, double *b)
     UG_LAUNCH(c, k_dirichlet_rows, div_up(L.nv, 256), 256, 0, L.bnd.p, L.nv, A.rowptr.p, A.col.p, A.val.p, b);
 }
 
+// ---------------------------------------------------------------- defect --
+// Element defect (StdGlobAssembler::AssembleDefect, lib_disc/spatial_disc/
+// elem_disc/elem_disc_assemble_util.h:578-690 stationary, 713-860
+// instationary).  add_def_A_elem is the element operator applied to the local
+// solution (the same sums the box method forms through the gradients at the
+// integration points); add_rhs_elem is f_i |SCV_i|, add_def_M_elem
+// |SCV_i| u_i.  Per element and corner i, with explicit rounding in the
+// reference's order:
+//   stationary:    r = (A_e u)_i + (-1) f_i |SCV_i|
+//   instationary:  r = 0 + sm0 |SCV_i| u_i [+ sa0 (A_e u)_i + (-sa0) f_i |SCV_i|]
+//                        + sm1 |SCV_i| uo_i [+ sa1 (A_e uo)_i + (-sa1) f_i |SCV_i|]
+// then d_i += r (cells of one parity colour per launch: no two threads share
+// a vertex).
+template <int T>
+__device__ __forceinline__ void defect_element(const AsmArgs &a, int e)
+{
+    using E = Elem<T>;
+    int ev[E::K];
+    double X[E::K][E::DIM];
+#pragma unroll
+    for (int i = 0; i < E::K; ++i) {
+        ev[i] = a.elems[(size_t)e * E::K + i];
+#pragma unroll
+        for (int d = 0; d < E::DIM; ++d) X[i][d] = a.coords[(size_t)ev[i] * E::DIM + d];
+    }
+    double Aloc[E::K][E::K];
+    double vol[E::K];
+    VelField vf{a.vmodes, a.vk, a.vc, a.vphase, a.vscale};
+    elem_matrix<T>(X, a.K[e], a.vmodes > 0 ? &vf : nullptr, Aloc, vol);
+    double uc[E::K];
+#pragma unroll
+    for (int j = 0; j < E::K; ++j) uc[j] = a.u[ev[j]];
+#pragma unroll
+    for (int i = 0; i < E::K; ++i) {
+        const double fi = a.f ? a.f[ev[i]] : (a.use_seed ? 2.0 * hash_uniform(a.f_seed, (uint64_t)ev[i]) - 1.0 : 0.0);
+        const double fv = __dmul_rn(fi, vol[i]);
+        double au = 0.0;
+#pragma unroll
+        for (int j = 0; j < E::K; ++j) au = __dadd_rn(au, __dmul_rn(Aloc[i][j], uc[j]));
+        double r;
+        if (!a.inst) {
+            r = __dadd_rn(au, __dmul_rn(-1.0, fv));
+        } else {
+            r = __dadd_rn(0.0, __dmul_rn(a.sm0, __dmul_rn(vol[i], uc[i])));
+            if (a.sa0 != 0.0) {
+                r = __dadd_rn(r, __dmul_rn(a.sa0, au));
+                r = __dadd_rn(r, __dmul_rn(-a.sa0, fv));
+            }
+            r = __dadd_rn(r, __dmul_rn(a.sm1, __dmul_rn(vol[i], a.u_old[ev[i]])));
+            if (a.sa1 != 0.0) {
+                double ao = 0.0;
+#pragma unroll
+                for (int j = 0; j < E::K; ++j) ao = __dadd_rn(ao, __dmul_rn(Aloc[i][j], a.u_old[ev[j]]));
+                r = __dadd_rn(r, __dmul_rn(a.sa1, ao));
+                r = __dadd_rn(r, __dmul_rn(-a.sa1, fv));
+            }
+        }
+        a.d[ev[i]] = __dadd_rn(a.d[ev[i]], r);
+    }
+}
+
+template <int T>
+__global__ void __launch_bounds__(128) k_defect(AsmArgs a, int colour)
+{
+    int cell;
+    if (!colour_cell(a, blockIdx.x * blockDim.x + threadIdx.x, colour, &cell)) return;
+    if (T == UG4GB_TET) {
+        for (int p = 0; p < 6; ++p) defect_element<T>(a, 6 * cell + p);
+    } else {
+        defect_element<T>(a, cell);
+    }
+}
+
+// Dirichlet vertices: defect 0 (DirichletBoundary::adjust_defect,
+// lagrange_dirichlet_boundary_impl.h:972-1033) or solution value 0
+// (adjust_solution); both set the boundary entries to zero here
+__global__ void k_zero_dirichlet(const unsigned char *bnd, int nv, double *x)
+{
+    int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < nv && bnd[v]) x[v] = 0.0;
+}
+
+void launch_defect(Ctx &c, const Level &L, const AsmArgs &a_in)
+{
+    AsmArgs a = a_in;
+    a.cx = L.nx - 1;
+    a.cy = L.ny - 1;
+    a.cz = (L.dim == 3) ? L.nz - 1 : 1;
+    const int ncol = (L.dim == 3) ? 8 : 4;
+    const int per = ((a.cx + 1) / 2) * ((a.cy + 1) / 2) * ((a.cz + 1) / 2);
+    unsigned g = div_up(per, 128);
+    for (int colour = 0; colour < ncol; ++colour) {
+        if (L.elem_type == UG4GB_QUAD) UG_LAUNCH(c, k_defect<UG4GB_QUAD>, g, 128, 0, a, colour);
+        else if (L.elem_type == UG4GB_HEX) UG_LAUNCH(c, k_defect<UG4GB_HEX>, g, 128, 0, a, colour);
+        else UG_LAUNCH(c, k_defect<UG4GB_TET>, g, 128, 0, a, colour);
+    }
+    UG_LAUNCH(c, k_zero_dirichlet, div_up(L.nv, 256), 256, 0, L.bnd.p, L.nv, a.d);
+}
+
+void launch_dirichlet_values(Ctx &c, const Level &L, double *u)
+{
+    UG_LAUNCH(c, k_zero_dirichlet, div_up(L.nv, 256), 256, 0, L.bnd.p, L.nv, u);
+}
+
 // ------------------------------------------------------ coefficients -----
 // K_e = exp(factor * amp * sum_m cos(k_m . c_e + phase_m)), c_e = centroid
 template <int T>
