@@ -44,6 +44,7 @@ extern "C" {
 #define UG4GB_QUAD 0                /* 2D quadrilaterals (ROID_QUADRILATERAL) */
 #define UG4GB_HEX 1                 /* 3D hexahedra (ROID_HEXAHEDRON) */
 #define UG4GB_TET 2                 /* 3D tetrahedra, 6 per hex, Kuhn split */
+#define UG4GB_TRI 3                 /* 2D triangles (ROID_TRIANGLE; unstructured grids) */
 
 /* smoothers, precisions, solvers */
 #define UG4GB_SMOOTHER_JACOBI 0     /* damped Jacobi (lib_algebra/operator/preconditioner/jacobi.h:90) */
@@ -117,6 +118,41 @@ UG4GB_API int ug4gb_grid_level_info(const ug4gb_grid *g, int level, int *num_ver
 UG4GB_API int ug4gb_grid_level_export(const ug4gb_grid *g, int level, double *coords, int *elems,
                             unsigned char *boundary);
 UG4GB_API void ug4gb_grid_destroy(ug4gb_grid *g);
+/* Unstructured hierarchies: a coarse grid refined nref times regularly
+   (GlobalMultiGridRefiner, lib_grid/refinement/global_multi_grid_refiner.h;
+   triangles and quadrilaterals -> 4, tetrahedra and hexahedra -> 8, the inner
+   octahedron of a tetrahedron cut along its shortest diagonal), built on the
+   host at set-up and uploaded.  Dirichlet vertices follow subset membership
+   through the refinement as in ugcore (objects created on an edge / face /
+   element belong to its subset).
+   ug4gb_grid_create_ugx reads a UGX file (lib_grid/file_io/file_io_ugx.cpp;
+   vertices, edges, triangles, quadrilaterals, tetrahedrons, hexahedrons and
+   the first subset_handler; one element type per grid): dirichlet_subsets is
+   a comma-separated list of subset names whose vertices, edges, faces and
+   volumes carry the zero Dirichlet condition (DirichletBoundary::add(0, "c",
+   "Name, ...")); NULL or "" = the topological boundary.
+   ug4gb_grid_create_unstructured takes the coarse grid as arrays: elements
+   with the reference corner order of elem_type, Dirichlet vertices (NULL:
+   none), Dirichlet edges (pairs) and faces (4 corners in cyclic order, -1 as
+   the 4th of a triangle); no Dirichlet arguments at all = the topological
+   boundary. */
+UG4GB_API int ug4gb_grid_create_ugx(ug4gb_ctx *ctx, const char *filename, int nref, const char *dirichlet_subsets,
+                                    ug4gb_grid **out);
+UG4GB_API int ug4gb_grid_create_unstructured(ug4gb_ctx *ctx, int elem_type, int num_vertices, const double *coords,
+                                             int num_elements, const int *elems,
+                                             const unsigned char *dirichlet_vertices, int num_dirichlet_edges,
+                                             const int *dirichlet_edges, int num_dirichlet_faces,
+                                             const int *dirichlet_faces, int nref, ug4gb_grid **out);
+/* 1 for a structured (box) hierarchy, 0 for an unstructured one */
+UG4GB_API int ug4gb_grid_is_structured(const ug4gb_grid *g);
+/* parents of the vertices of `level` >= 1 in level - 1: npar (nv) and par
+   (nv x 8, increasing, -1 padded) */
+UG4GB_API int ug4gb_grid_level_parents(const ug4gb_grid *g, int level, int *npar, int *par);
+/* host only, no context or GPU: level `level` of the hierarchy that
+   ug4gb_grid_create_ugx builds (sizes first with NULL arrays) */
+UG4GB_API int ug4gb_io_ugx_level(const char *filename, int nref, const char *dirichlet_subsets, int level,
+                                 int *elem_type, int *num_vertices, int *num_elements, double *coords, int *elems,
+                                 unsigned char *dirichlet, int *npar, int *par, char *err, int err_capacity);
 
 /* ------------------------------------------------------------- vectors -- */
 /* Replaces ug::Vector<double> (lib_algebra/cpu_algebra/vector.h:54). */

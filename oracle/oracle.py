@@ -13,7 +13,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
-ORC_QUAD, ORC_HEX, ORC_TET = 0, 1, 2
+ORC_QUAD, ORC_HEX, ORC_TET, ORC_TRI = 0, 1, 2, 3
 
 
 class Params(C.Structure):
@@ -72,6 +72,9 @@ def lib():
         L.orc_prob_theta_system.argtypes = [P, C.c_double, C.c_double, dp, ip, ip, dp, dp]
         L.orc_prob_theta_steps.argtypes = [P, C.c_double, C.c_double, C.c_int, dp, ip]
         L.orc_prob_theta_jacobian.argtypes = [P, C.c_int, C.c_double, C.c_double, ip, ip, dp]
+        L.orc_prob_create_ext.restype = P
+        L.orc_prob_create_ext.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_prob_defect.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, dp]
         L.orc_prob_newton.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, C.c_int, C.c_double, C.c_double,
                                       ip, ip, dp]
@@ -103,16 +106,32 @@ def make_params(elem_type=ORC_QUAD, mx=2, my=2, mz=2, nref=6, seed=1, coef_kind=
 
 
 class Problem:
-    """One assemble-and-solve problem held by the oracle."""
+    """One assemble-and-solve problem held by the oracle.  levels: optional
+    hierarchy [(coords, elems, bnd, npar, par), ...] coarse to fine (an
+    unstructured hierarchy exported by the library; npar/par None on level 0)
+    instead of the structured one the parameters describe."""
 
-    def __init__(self, params, m_top=None, f_top=None):
+    def __init__(self, params, m_top=None, f_top=None, levels=None):
         L = lib()
         self.params = params
         self._m = None if m_top is None else np.ascontiguousarray(m_top, dtype=np.float64)
         self._f = None if f_top is None else np.ascontiguousarray(f_top, dtype=np.float64)
-        self.h = L.orc_prob_create(C.byref(params),
-                                   None if self._m is None else self._m.ctypes.data,
-                                   None if self._f is None else self._f.ctypes.data)
+        if levels is not None:
+            self._lv = [tuple(None if a is None else np.ascontiguousarray(a) for a in lev) for lev in levels]
+            n = len(levels)
+            nv = (C.c_int * n)(*[len(lv[0]) for lv in self._lv])
+            ne = (C.c_int * n)(*[len(lv[1]) for lv in self._lv])
+            ptrs = []
+            for j in range(5):
+                arr = (C.c_void_p * n)(*[None if lv[j] is None else lv[j].ctypes.data for lv in self._lv])
+                ptrs.append(arr)
+            self._ptrs = ptrs
+            self.h = L.orc_prob_create_ext(C.byref(params), n, nv, ne, *ptrs,
+                                           None if self._f is None else self._f.ctypes.data)
+        else:
+            self.h = L.orc_prob_create(C.byref(params),
+                                       None if self._m is None else self._m.ctypes.data,
+                                       None if self._f is None else self._f.ctypes.data)
         if not self.h:
             raise RuntimeError("oracle problem setup failed")
         self.nlev = L.orc_prob_num_levels(self.h)

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-enum { ORC_QUAD = 0, ORC_HEX = 1, ORC_TET = 2 };
+enum { ORC_QUAD = 0, ORC_HEX = 1, ORC_TET = 2, ORC_TRI = 3 };
 
 typedef struct {
     int n_rows, n_cols;
@@ -76,6 +76,9 @@ void orc_field_free(orc_field *F);
 /* hierarchy */
 int orc_hier_create(orc_hier *H, int elem_type, int mx, int my, int mz, int nref);
 void orc_hier_free(orc_hier *H);
+int orc_hier_from_arrays(orc_hier *H, int elem_type, int nlev, const int *nv, const int *ne,
+                         const double *const *coords, const int *const *elems, const unsigned char *const *bnd,
+                         const int *const *npar, const int *const *par);
 void orc_level_centroids(const orc_level *L, double *c);
 
 /* CRS */

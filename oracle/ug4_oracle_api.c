@@ -72,12 +72,37 @@ static int assemble_all(orc_prob *P)
     return 0;
 }
 
+static orc_prob *prob_setup(orc_prob *P, const orc_params *p, const double *m_top, const double *f_top);
+
 orc_prob *orc_prob_create(const orc_params *p, const double *m_top, const double *f_top)
 {
     orc_prob *P = (orc_prob *)calloc(1, sizeof(orc_prob));
     if (!P) return NULL;
     P->p = *p;
     if (orc_hier_create(&P->H, p->elem_type, p->mx, p->my, p->mz, p->nref)) { free(P); return NULL; }
+    return prob_setup(P, p, m_top, f_top);
+}
+
+/* problem on a given hierarchy (unstructured grids): coefficient kinds 0, 1
+   and 3, no velocity field */
+orc_prob *orc_prob_create_ext(const orc_params *p, int nlev, const int *nv, const int *ne,
+                              const double *const *coords, const int *const *elems,
+                              const unsigned char *const *bnd, const int *const *npar, const int *const *par,
+                              const double *f_top)
+{
+    if (p->coef_kind == 2 || p->vel_kind != 0) return NULL;
+    orc_prob *P = (orc_prob *)calloc(1, sizeof(orc_prob));
+    if (!P) return NULL;
+    P->p = *p;
+    if (orc_hier_from_arrays(&P->H, p->elem_type, nlev, nv, ne, coords, elems, bnd, npar, par)) {
+        free(P);
+        return NULL;
+    }
+    return prob_setup(P, p, NULL, f_top);
+}
+
+static orc_prob *prob_setup(orc_prob *P, const orc_params *p, const double *m_top, const double *f_top)
+{
     int nl = P->H.nlev, top = nl - 1;
     P->K = (double **)calloc((size_t)nl, sizeof(double *));
     if (p->coef_kind == 3) {

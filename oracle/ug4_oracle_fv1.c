@@ -22,8 +22,8 @@
  *     shapes; JtInv per ip for multilinear elements, once for the tetrahedron
  *     (fv1_geom.cpp:406-446).
  * Reference-element tables (corner, edge, face numbering) are those of
- * lib_disc/reference_element/reference_element.cpp (quadrilateral :428,
- * tetrahedron :547, hexahedron :1327).
+ * lib_disc/reference_element/reference_element.cpp (triangle :320-420,
+ * quadrilateral :428, tetrahedron :547, hexahedron :1327).
  *
  * The element discretisation itself lives in the external ConvectionDiffusion
  * plugin (not part of ugcore).  It is restated here from the box-method
@@ -54,6 +54,12 @@ static const int hex_edge_face[12][2] = {{0,1},{0,2},{0,3},{0,4},{1,4},{2,1},{3,
 static const int hex_pt_edge[8][3] = {{3,0,4},{0,1,5},{1,2,6},{2,3,7},{4,8,11},{5,9,8},{6,10,9},{7,11,10}};
 static const int hex_pt_face[8][3] = {{0,4,1},{0,1,2},{0,2,3},{0,3,4},{1,4,5},{2,1,5},{3,2,5},{4,3,5}};
 
+/* triangle (reference_element.cpp, ReferenceTriangle): corners (0,0),(1,0),(0,1),
+   edges (0,1),(1,2),(2,0), edges at corner {2,0},{0,1},{1,2} */
+static const double tri_corner[3][2] = {{0,0},{1,0},{0,1}};
+static const int tri_edge[3][2] = {{0,1},{1,2},{2,0}};
+static const int tri_pt_edge[3][2] = {{2,0},{0,1},{1,2}};
+
 static const double tet_corner[4][3] = {{0,0,0},{1,0,0},{0,1,0},{0,0,1}};
 static const int tet_edge[6][2] = {{0,1},{1,2},{2,0},{0,3},{1,3},{2,3}};
 static const int tet_face[4][3] = {{0,2,1},{1,2,3},{0,3,2},{0,1,3}};
@@ -64,7 +70,11 @@ static const int tet_pt_face[4][3] = {{0,2,3},{0,3,1},{0,1,2},{3,2,1}};
 /* local gradients of the P1 Lagrange shapes at local position x */
 static void local_grads(int type, const double *x, double g[8][3])
 {
-    if (type == ORC_QUAD) {
+    if (type == ORC_TRI) {
+        g[0][0] = -1; g[0][1] = -1;
+        g[1][0] = 1;  g[1][1] = 0;
+        g[2][0] = 0;  g[2][1] = 1;
+    } else if (type == ORC_QUAD) {
         g[0][0] = -(1.0 - x[1]); g[0][1] = -(1.0 - x[0]);
         g[1][0] =  (1.0 - x[1]); g[1][1] = -x[0];
         g[2][0] =  x[1];         g[2][1] =  x[0];
@@ -162,18 +172,20 @@ static double hex_size(const double c[8][3])
 int orc_fv1_geometry(int type, const double *corner, orc_fv1geom *G)
 {
     memset(G, 0, sizeof(*G));
-    const int dim = (type == ORC_QUAD) ? 2 : 3;
-    const int k = (type == ORC_HEX) ? 8 : 4;
-    const int ne = (type == ORC_QUAD) ? 4 : (type == ORC_HEX ? 12 : 6);
+    const int dim = (type == ORC_QUAD || type == ORC_TRI) ? 2 : 3;
+    const int k = (type == ORC_HEX) ? 8 : (type == ORC_TRI ? 3 : 4);
+    const int ne = (type == ORC_QUAD) ? 4 : (type == ORC_HEX ? 12 : (type == ORC_TRI ? 3 : 6));
     const int nf = (type == ORC_HEX) ? 6 : (type == ORC_TET ? 4 : 0);
-    const int (*edge)[2] = (type == ORC_QUAD) ? quad_edge : (type == ORC_HEX ? hex_edge : tet_edge);
+    const int (*edge)[2] = (type == ORC_QUAD) ? quad_edge
+                           : (type == ORC_HEX ? hex_edge : (type == ORC_TRI ? tri_edge : tet_edge));
     G->nscv = k; G->nscvf = ne;
 
     /* loc/glob mids: [0] corners, [1] edges, [2] faces, [3] centre */
     double lc[8][3], gc[8][3], le[12][3], ge[12][3], lf[6][3], gf[6][3], lm[3], gm[3];
     for (int i = 0; i < k; ++i)
         for (int d = 0; d < dim; ++d) {
-            lc[i][d] = (type == ORC_QUAD) ? quad_corner[i][d] : (type == ORC_HEX ? hex_corner[i][d] : tet_corner[i][d]);
+            lc[i][d] = (type == ORC_QUAD) ? quad_corner[i][d]
+                       : (type == ORC_HEX ? hex_corner[i][d] : (type == ORC_TRI ? tri_corner[i][d] : tet_corner[i][d]));
             gc[i][d] = corner[i * dim + d];
         }
     for (int e = 0; e < ne; ++e) {
@@ -222,7 +234,8 @@ int orc_fv1_geometry(int type, const double *corner, orc_fv1geom *G)
     for (int i = 0; i < k; ++i) {
         if (dim == 2) {
             double q[4][3] = {{0}};
-            const double *p[4] = {gc[i], ge[quad_pt_edge[i][0]], gm, ge[quad_pt_edge[i][1]]};
+            const int (*pe)[2] = (type == ORC_TRI) ? tri_pt_edge : quad_pt_edge;
+            const double *p[4] = {gc[i], ge[pe[i][0]], gm, ge[pe[i][1]]};
             for (int j = 0; j < 4; ++j) { q[j][0] = p[j][0]; q[j][1] = p[j][1]; }
             G->vol[i] = quad_size2d(q);
         } else {
@@ -237,13 +250,14 @@ int orc_fv1_geometry(int type, const double *corner, orc_fv1geom *G)
 
     /* gradients */
     double Ji[3][3], lg[8][3];
-    if (type == ORC_TET) {
+    const int affine = (type == ORC_TET || type == ORC_TRI);
+    if (affine) {
         local_grads(type, lip[0], lg);
-        jt_inverse(3, 4, corner, lg, Ji);
+        jt_inverse(dim, k, corner, lg, Ji);
     }
     for (int e = 0; e < ne; ++e) {
         local_grads(type, lip[e], lg);
-        if (type != ORC_TET) jt_inverse(dim, k, corner, lg, Ji);
+        if (!affine) jt_inverse(dim, k, corner, lg, Ji);
         for (int sh = 0; sh < k; ++sh)
             for (int a = 0; a < dim; ++a) {
                 double s = 0.0;

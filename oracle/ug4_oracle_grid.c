@@ -262,6 +262,41 @@ void orc_hier_free(orc_hier *H)
     H->lev = NULL; H->nlev = 0;
 }
 
+/* hierarchy from given levels (an unstructured hierarchy exported by the
+   library under test): the arrays are copied; par is nv x 8 per level >= 1 */
+int orc_hier_from_arrays(orc_hier *H, int elem_type, int nlev, const int *nv, const int *ne,
+                         const double *const *coords, const int *const *elems, const unsigned char *const *bnd,
+                         const int *const *npar, const int *const *par)
+{
+    H->nlev = nlev;
+    H->lev = (orc_level *)calloc((size_t)nlev, sizeof(orc_level));
+    if (!H->lev) return -1;
+    for (int l = 0; l < nlev; ++l) {
+        orc_level *L = &H->lev[l];
+        L->elem_type = elem_type;
+        L->dim = (elem_type == ORC_QUAD || elem_type == ORC_TRI) ? 2 : 3;
+        L->k = (elem_type == ORC_HEX) ? 8 : (elem_type == ORC_TRI ? 3 : 4);
+        L->nx = L->ny = L->nz = 0;
+        L->nv = nv[l];
+        L->ne = ne[l];
+        L->coords = (double *)malloc(sizeof(double) * (size_t)L->nv * L->dim);
+        L->elems = (int *)malloc(sizeof(int) * (size_t)L->ne * L->k);
+        L->bnd = (unsigned char *)malloc((size_t)L->nv);
+        if (!L->coords || !L->elems || !L->bnd) return -1;
+        memcpy(L->coords, coords[l], sizeof(double) * (size_t)L->nv * L->dim);
+        memcpy(L->elems, elems[l], sizeof(int) * (size_t)L->ne * L->k);
+        memcpy(L->bnd, bnd[l], (size_t)L->nv);
+        if (l > 0) {
+            L->npar = (int *)malloc(sizeof(int) * (size_t)L->nv);
+            L->par = (int *)malloc(sizeof(int) * (size_t)L->nv * 8);
+            if (!L->npar || !L->par) return -1;
+            memcpy(L->npar, npar[l], sizeof(int) * (size_t)L->nv);
+            memcpy(L->par, par[l], sizeof(int) * (size_t)L->nv * 8);
+        }
+    }
+    return 0;
+}
+
 void orc_level_centroids(const orc_level *L, double *c)
 {
     for (int e = 0; e < L->ne; ++e) {

@@ -1,0 +1,164 @@
+"""Assembly and GMG solves on unstructured hierarchies (UGX coarse grids
+refined regularly) on the GPU, against the oracle run on the same levels
+(exported from the library: coordinates, elements, Dirichlet vertices,
+parents).
+
+Bars as for the structured grids: CRS pattern bit-exact, values 1e-13
+relative to the row's largest entry, right-hand side 1e-13, P and R
+bit-exact, FP64 GMG application 1e-12, iteration count +-1 and solution
+1e-8 (FP64), relative residual < 1e-10 in FP64 for mixed precision."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, assert_crs_equal
+
+pytestmark = pytest.mark.gpu
+
+GRIDS = os.path.join(GOLDEN, "grids")
+CASES = [
+    ("square_tris", "Dirichlet", 4, "const"),
+    ("square_quads", "Boundary", 4, "const"),
+    ("cube_tets", "Bottom", 3, "const"),
+    ("cube_tets", None, 3, "lognormal"),
+    ("cube_hexes", "Boundary", 3, "lognormal"),
+]
+
+
+def _setup(ctx, orc, name, dirichlet, nref, coef, precision="fp64", smoother="jacobi"):
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import fields
+    hier = ug.UnstructuredHierarchy.from_ugx(ctx, os.path.join(GRIDS, name + ".ugx"), nref, dirichlet)
+    assert not hier.structured
+    disc = ug.DomainDiscretization(hier)
+    seed = 3
+    if coef == "const":
+        disc.set_diffusion(1.0)
+    else:
+        disc.set_diffusion_field(fields.ScalarField(hier.dim, 64, 8.0, seed ^ fields.COEF_SEED_XOR), factor=2.0)
+    disc.set_source_uniform(seed)
+    A = ug.GPUSparseMatrix(ctx)
+    b = ug.GPUVector(ctx, hier.num_vertices())
+    disc.assemble_linear(A, b)
+    gmg = ug.GeometricMultiGrid(disc)
+    gmg.set_smoother(ug.Jacobi(0.6) if smoother == "jacobi" else ug.GaussSeidel(1.0))
+    gmg.set_num_presmooth(2)
+    gmg.set_num_postsmooth(2)
+    gmg.set_base_level(0)
+    gmg.set_precision(precision)
+    gmg.init(A)
+    levels = []
+    for l in range(hier.num_levels):
+        x, e, bnd = hier.export(l)
+        npar, par = hier.parents(l) if l > 0 else (None, None)
+        levels.append((x, e, bnd, npar, par))
+    et = {0: orc.ORC_QUAD, 1: orc.ORC_HEX, 2: orc.ORC_TET, 3: orc.ORC_TRI}[hier.elem_type]
+    params = orc.make_params(elem_type=et, seed=seed, coef_kind=0 if coef == "const" else 1, coef_modes=64,
+                             coef_kmax=8.0, solver=0, smoother=0, damp=0.6, nu1=2, nu2=2, cycle=1, base=0,
+                             maxit=200, rel_red=1e-10, min_defect=1e-300)
+    op = orc.Problem(params, levels=levels)
+    return hier, disc, A, b, gmg, op
+
+
+@pytest.mark.parametrize("name,dirichlet,nref,coef", CASES)
+def test_unstructured_assembly_and_transfers(ctx, oracle_lib, name, dirichlet, nref, coef):
+    hier, disc, A, b, gmg, op = _setup(ctx, oracle_lib, name, dirichlet, nref, coef)
+    assert_crs_equal(A.export_csr(), op.matrix(), what="top operator")
+    ob = op.rhs()
+    assert np.abs(b.numpy() - ob).max() <= 1e-13 * np.abs(ob).max()
+    for l in range(1, hier.num_levels):
+        assert_crs_equal(gmg.level_matrix(l - 1), op.matrix(l - 1), what="level %d operator" % (l - 1))
+        for which in (0, 1):
+            assert_crs_equal(gmg.transfer(l, which), op.transfer(l, which), rtol=0.0,
+                             what="%s level %d" % ("PR"[which], l))
+
+
+@pytest.mark.parametrize("name,dirichlet,nref,coef", CASES)
+def test_unstructured_gmg_and_solve(ctx, oracle_lib, name, dirichlet, nref, coef):
+    import ugcore_gb300 as ug
+    hier, disc, A, b, gmg, op = _setup(ctx, oracle_lib, name, dirichlet, nref, coef)
+    n = hier.num_vertices()
+    d = np.random.default_rng(0).standard_normal(n)
+    d[hier.export()[2].astype(bool)] = 0.0
+    c = ug.GPUVector(ctx, n)
+    gmg.apply(c, ug.GPUVector(ctx, n).copy_from(d))
+    ref = op.apply_gmg(d)
+    assert np.abs(c.numpy() - ref).max() <= 1e-12 * np.abs(ref).max()
+    solver = ug.CG(ctx)
+    solver.set_preconditioner(gmg)
+    solver.set_convergence_check(ug.StdConvCheck(200, 1e-300, 1e-10))
+    solver.init(A)
+    x = ug.GPUVector(ctx, n)
+    assert solver.apply(x, b)
+    st = solver.stats()
+    rs = op.solve()
+    assert abs(st["steps"] - rs["steps"]) <= 1, (st, rs["steps"])
+    assert np.abs(x.numpy() - rs["x"]).max() <= 1e-8 * np.abs(rs["x"]).max()
+
+
+@pytest.mark.parametrize("precision,smoother", [("mixed", "jacobi"), ("fp64", "mcgs")])
+def test_unstructured_variants_converge(ctx, oracle_lib, precision, smoother):
+    """mixed precision and the multicolour Gauss-Seidel (greedy vertex
+    colours) on the tetrahedral hierarchy: the FP64 residual reaches 1e-10"""
+    import ugcore_gb300 as ug
+    hier, disc, A, b, gmg, op = _setup(ctx, oracle_lib, "cube_tets", "Bottom", 3, "lognormal", precision, smoother)
+    solver = ug.CG(ctx)
+    solver.set_preconditioner(gmg)
+    solver.set_convergence_check(ug.StdConvCheck(200, 1e-300, 1e-10))
+    solver.init(A)
+    x = ug.GPUVector(ctx, hier.num_vertices())
+    assert solver.apply(x, b)
+    r = ug.GPUVector(ctx, hier.num_vertices())
+    A.axpy(r, 1.0, b, -1.0, x)
+    assert r.norm() / b.norm() < 1e-10
+    rs = op.solve()
+    assert np.abs(x.numpy() - rs["x"]).max() <= 1e-7 * np.abs(rs["x"]).max()
+
+
+def test_unstructured_matches_structured_on_the_same_mesh(ctx):
+    """the 2 x 2 quadrilateral unit square given as arrays and refined by the
+    unstructured builder solves the same discrete problem as the structured
+    hierarchy (vertices matched by coordinates)"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    cfg = problems.config("c0", nref=4, precision="fp64")
+    p = problems.Problem(ctx, cfg)
+    st = p.solve()
+    xs = p.x.numpy()
+    cs, _, _ = p.hier.export()
+    assert p.hier.structured
+    X0 = np.array([[x, y] for y in (0, .5, 1) for x in (0, .5, 1)])
+    quads = np.array([(0, 1, 4, 3), (1, 2, 5, 4), (3, 4, 7, 6), (4, 5, 8, 7)], np.int32)
+    hier = ug.UnstructuredHierarchy.from_arrays(ctx, "quad", X0, quads, num_refinements=4)
+    disc = ug.DomainDiscretization(hier)
+    disc.set_diffusion(1.0)
+    # vertices matched by coordinates; the structured problem's rhs carried over
+    cu, _, _ = hier.export()
+    key = lambda c: np.round(c * 1024).astype(np.int64) @ np.array([1, 4096])
+    pos = {k: i for i, k in enumerate(key(cs))}
+    perm = np.array([pos[k] for k in key(cu)])
+    bs = p.b.numpy()
+    A = ug.GPUSparseMatrix(ctx)
+    b = ug.GPUVector(ctx, hier.num_vertices())
+    disc.assemble_linear(A, b)
+    b.copy_from(bs[perm])
+    gmg = ug.GeometricMultiGrid(disc)
+    gmg.set_smoother(ug.Jacobi(0.6))
+    gmg.set_precision("fp64")
+    gmg.init(A)
+    solver = ug.CG(ctx)
+    solver.set_preconditioner(gmg)
+    solver.set_convergence_check(ug.StdConvCheck(200, 1e-300, 1e-10))
+    solver.init(A)
+    x = ug.GPUVector(ctx, hier.num_vertices())
+    assert solver.apply(x, b)
+    assert abs(solver.stats()["steps"] - st["steps"]) <= 1
+    assert np.abs(x.numpy() - xs[perm]).max() <= 1e-8 * np.abs(xs).max()
+    # and the operators agree entry by entry after the renumbering
+    rp, ci, va = A.export_csr()
+    import scipy.sparse as sp
+    Au = sp.csr_matrix((va, ci, rp)).toarray()
+    rps, cis, vas = p.A.export_csr()
+    As = sp.csr_matrix((vas, cis, rps)).toarray()
+    assert np.abs(Au - As[np.ix_(perm, perm)]).max() <= 1e-13 * np.abs(As).max()

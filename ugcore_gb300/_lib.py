@@ -11,7 +11,7 @@ LIB_PATH = os.path.join(HERE, "libug4gb.so")
 
 OK = 0
 ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_SINGULAR, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_STATE = -1, -2, -3, -4, -5, -6, -7
-QUAD, HEX, TET = 0, 1, 2
+QUAD, HEX, TET, TRI = 0, 1, 2, 3
 SMOOTHER_JACOBI, SMOOTHER_MCGS = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_CG, SOLVER_BICGSTAB = 0, 1
@@ -57,6 +57,11 @@ _SIGS = {
     "ug4gb_grid_level_info": (I, [P, I, PI, PI, PI, PI]),
     "ug4gb_grid_level_export": (I, [P, I, P, P, P]),
     "ug4gb_grid_destroy": (None, [P]),
+    "ug4gb_grid_create_ugx": (I, [P, C.c_char_p, I, C.c_char_p, PP]),
+    "ug4gb_grid_create_unstructured": (I, [P, I, I, P, I, P, P, I, P, I, P, I, PP]),
+    "ug4gb_grid_is_structured": (I, [P]),
+    "ug4gb_grid_level_parents": (I, [P, I, P, P]),
+    "ug4gb_io_ugx_level": (I, [C.c_char_p, I, C.c_char_p, I, PI, PI, PI, P, P, P, P, P, C.c_char_p, I]),
     "ug4gb_vector_create": (I, [P, I, PP]),
     "ug4gb_vector_wrap": (I, [P, P, I, PP]),
     "ug4gb_vector_size": (I, [P]),

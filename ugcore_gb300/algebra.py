@@ -29,7 +29,7 @@ from . import _lib
 from ._lib import check, lib
 
 _ELEM = {"quad": _lib.QUAD, "quadrilateral": _lib.QUAD, "hex": _lib.HEX, "hexahedron": _lib.HEX,
-         "tet": _lib.TET, "tetrahedron": _lib.TET}
+         "tet": _lib.TET, "tetrahedron": _lib.TET, "tri": _lib.TRI, "triangle": _lib.TRI}
 
 
 def _ptr(a):
@@ -106,19 +106,17 @@ class Context:
         return lib().ug4gb_stream(self.h)
 
 
-class StructuredHierarchy:
-    """Uniformly refined unit square/cube: levels 0..num_refinements."""
+class _Hierarchy:
+    """Multigrid hierarchy of a grid (levels 0 .. num_levels - 1)."""
 
-    def __init__(self, ctx, elem, mx, my, mz=1, num_refinements=0):
+    def _init(self, ctx, elem_type, h):
         self.ctx = ctx
-        self.elem_type = _ELEM[elem] if isinstance(elem, str) else int(elem)
-        h = C.c_void_p()
-        check(lib().ug4gb_grid_create_structured(ctx.h, self.elem_type, mx, my, mz, num_refinements, C.byref(h)),
-              ctx.h)
+        self.elem_type = int(elem_type)
         self.h = h
         self.num_levels = lib().ug4gb_grid_num_levels(h)
         self.top = self.num_levels - 1
-        self.dim = 2 if self.elem_type == _lib.QUAD else 3
+        self.dim = 2 if self.elem_type in (_lib.QUAD, _lib.TRI) else 3
+        self.structured = lib().ug4gb_grid_is_structured(h) == 1
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -145,6 +143,64 @@ class StructuredHierarchy:
         bnd = np.zeros(info["num_vertices"], np.uint8)
         check(lib().ug4gb_grid_level_export(self.h, level, _ptr(coords), _ptr(elems), _ptr(bnd)), self.ctx.h)
         return coords, elems, bnd
+
+    def parents(self, level=None):
+        """(npar, par): parents of the vertices of `level` >= 1 in level - 1"""
+        level = self.top if level is None else level
+        nv = self.num_vertices(level)
+        npar = np.zeros(nv, np.int32)
+        par = np.zeros((nv, 8), np.int32)
+        check(lib().ug4gb_grid_level_parents(self.h, level, _ptr(npar), _ptr(par)), self.ctx.h)
+        return npar, par
+
+
+class StructuredHierarchy(_Hierarchy):
+    """Uniformly refined unit square/cube: levels 0..num_refinements."""
+
+    def __init__(self, ctx, elem, mx, my, mz=1, num_refinements=0):
+        et = _ELEM[elem] if isinstance(elem, str) else int(elem)
+        h = C.c_void_p()
+        check(lib().ug4gb_grid_create_structured(ctx.h, et, mx, my, mz, num_refinements, C.byref(h)), ctx.h)
+        self._init(ctx, et, h)
+
+
+class UnstructuredHierarchy(_Hierarchy):
+    """Regular refinements of an unstructured coarse grid (a UGX file, as
+    util.refinement.CreateRegularHierarchy / GlobalMultiGridRefiner, or
+    arrays).  dirichlet: subset names (UGX) whose objects carry the zero
+    Dirichlet condition; None = the topological boundary."""
+
+    def __init__(self, ctx, elem_type, h):
+        self._init(ctx, elem_type, h)
+
+    @classmethod
+    def from_ugx(cls, ctx, filename, num_refinements=0, dirichlet=None):
+        names = None if dirichlet is None else (dirichlet if isinstance(dirichlet, str) else ",".join(dirichlet))
+        h = C.c_void_p()
+        check(lib().ug4gb_grid_create_ugx(ctx.h, filename.encode(), num_refinements,
+                                          None if names is None else names.encode(), C.byref(h)), ctx.h)
+        info = C.c_int()
+        k = C.c_int()
+        lib().ug4gb_grid_level_info(h, 0, None, None, C.byref(k), C.byref(info))
+        et = {(2, 3): _lib.TRI, (2, 4): _lib.QUAD, (3, 4): _lib.TET, (3, 8): _lib.HEX}[(info.value, k.value)]
+        return cls(ctx, et, h)
+
+    @classmethod
+    def from_arrays(cls, ctx, elem, coords, elems, dirichlet_vertices=None, dirichlet_edges=None,
+                    dirichlet_faces=None, num_refinements=0):
+        et = _ELEM[elem] if isinstance(elem, str) else int(elem)
+        x = np.ascontiguousarray(coords, np.float64)
+        el = np.ascontiguousarray(elems, np.int32)
+        dv = None if dirichlet_vertices is None else np.ascontiguousarray(dirichlet_vertices, np.uint8)
+        de = np.zeros((0, 2), np.int32) if dirichlet_edges is None else np.ascontiguousarray(dirichlet_edges, np.int32)
+        df = np.zeros((0, 4), np.int32) if dirichlet_faces is None else np.ascontiguousarray(dirichlet_faces, np.int32)
+        h = C.c_void_p()
+        check(lib().ug4gb_grid_create_unstructured(ctx.h, et, x.shape[0], _ptr(x), el.shape[0], _ptr(el),
+                                                   None if dv is None else _ptr(dv), de.shape[0],
+                                                   _ptr(de) if de.size else None, df.shape[0],
+                                                   _ptr(df) if df.size else None, num_refinements, C.byref(h)),
+              ctx.h)
+        return cls(ctx, et, h)
 
 
 class GPUVector:

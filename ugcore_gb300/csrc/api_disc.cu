@@ -30,6 +30,8 @@ const double *disc_coefficients(ug4gb_disc *d, int level)
         logk[nl - 1].alloc(lev[nl - 1].ne);
         UG_CUDA(cudaMemcpyAsync(logk[nl - 1].p, D.m_top.p, D.m_top.bytes(), cudaMemcpyDeviceToDevice, c.stream));
         for (int l = nl - 2; l >= 0; --l) {
+            UG_REQUIRE(lev[l].structured, UG4GB_ERR_INVALID,
+                       "per-element log coefficients need a structured hierarchy (children's mean)");
             logk[l].alloc(lev[l].ne);
             coarsen_log(c, lev[l + 1], lev[l], logk[l + 1].p, logk[l].p);
         }

@@ -200,7 +200,7 @@ struct GmgT : GmgBase {
         } else {
             op_from_csr<V>(c, L.A, L.At, nullptr, c.allow_dia);
             L.t.alloc(n);
-            int ncol = 1 << G.dim;
+            int ncol = G.ncolors;
             L.crow.resize(ncol);
             L.ncrow.assign(ncol, 0);
             DevBuf<int> cnt;
@@ -242,7 +242,7 @@ struct GmgT : GmgBase {
         op_from_csr<V>(c, F.R, F.Rs, nullptr, false);
         // the structured hierarchy's P and R need no stored matrix (AUTO
         // format); the assembled CSR stays for export and the SELL format
-        F.grid_transfer = c.allow_dia;
+        F.grid_transfer = c.allow_dia && Gf.structured && Gc.structured;
         F.gp = GridPair{Gf.nx, Gf.ny, Gf.nz, Gc.nx, Gc.ny, Gc.nz, Gf.dim, Gf.elem_type == UG4GB_TET ? 1 : 0};
         UG_CUDA(cudaStreamSynchronize(c.stream));
     }

@@ -247,12 +247,18 @@ struct OpMat {
 // ------------------------------------------------------------- grid level --
 struct Level {
     int elem_type = 0, dim = 2, k = 4;
-    int nx = 0, ny = 0, nz = 1, nv = 0, ne = 0;
+    int nx = 0, ny = 0, nz = 1, nv = 0, ne = 0;   // nx, ny, nz: structured levels only
+    bool structured = true;      // lexicographic box level (grid transfers, diagonal stencils)
     DevBuf<double> coords;
     DevBuf<int> elems;
     DevBuf<unsigned char> bnd;
     DevBuf<int> npar, par;       // parents in the next coarser level
-    DevBuf<int> color;           // parity colour of each vertex
+    DevBuf<int> color;           // vertex colour (parity on structured levels)
+    int ncolors = 0;             // vertex colours (multicolour Gauss-Seidel)
+    // unstructured levels: elements grouped by colour, no two elements of a
+    // colour sharing a vertex (the assembly's race-free scatter order)
+    std::vector<int> ecol_off;   // colour q: ecol[ecol_off[q] .. ecol_off[q+1])
+    DevBuf<int> ecol;
 };
 
 // ------------------------------------------------------ device utilities --

@@ -21,7 +21,9 @@ struct AsmArgs {
     const int *col;
     double *val;
     double *b;                // rhs or null
-    int cx, cy, cz;           // structured cell counts (set by launch_assemble)
+    int cx, cy, cz;           // structured cell counts (set by the coloured launch)
+    const int *elist = nullptr;  // unstructured: elements of the launched colour
+    int nlist = 0;
     // instationary assembly (ThetaTimeStep): element matrix sm0 M_e + sa0 A_e
     // with the lumped FV1 mass M_e = diag(|SCV_i|); with b, the rhs of one
     // previous time point: sa0 f_e - sm1 M_e u_old - sa1 A_e u_old + sa1 f_e

@@ -1,10 +1,10 @@
 // fv1_elem.cuh -- per-element FV1 geometry and element matrix (device code).
 //
 // Reference-element tables (lib_disc/reference_element/reference_element.cpp:
-// quadrilateral :428, tetrahedron :547, hexahedron :1327) are packed as 4-bit
-// nibbles in 64-bit literals so that, with every element loop unrolled, each
-// table lookup is a compile-time constant and the element matrix stays in
-// registers (a dynamic index would spill it to local memory).
+// triangle :320-420, quadrilateral :428, tetrahedron :547, hexahedron :1327)
+// are packed as 4-bit nibbles in 64-bit literals so that, with every element
+// loop unrolled, each table lookup is a compile-time constant and the element
+// matrix stays in registers (a dynamic index would spill it to local memory).
 #pragma once
 
 #include "common.cuh"
@@ -31,6 +31,25 @@ struct Elem<UG4GB_QUAD> {
     __host__ __device__ static constexpr double corner(int i, int d)
     {
         return (double)(((d == 0 ? 0x6 : 0xC) >> i) & 1);
+    }
+    __host__ __device__ static constexpr int face_n() { return 0; }
+    __host__ __device__ static constexpr int face(int, int) { return 0; }
+    __host__ __device__ static constexpr int edge_face(int, int) { return 0; }
+    __host__ __device__ static constexpr int pt_face(int, int) { return 0; }
+};
+
+// triangle: corners (0,0),(1,0),(0,1); edges (0,1),(1,2),(2,0)
+// (reference_element.cpp, ReferenceTriangle)
+template <>
+struct Elem<UG4GB_TRI> {
+    static constexpr int DIM = 2, K = 3, NSCVF = 3, NFACE = 0;
+    __host__ __device__ static constexpr int from(int e) { return nib(0x210ULL, e); }
+    __host__ __device__ static constexpr int to(int e) { return nib(0x021ULL, e); }
+    // edges at each corner [edge0, edge1]: {2,0},{0,1},{1,2}
+    __host__ __device__ static constexpr int pt_edge(int i, int q) { return nib(0x211002ULL, 2 * i + q); }
+    __host__ __device__ static constexpr double corner(int i, int d)
+    {
+        return (double)(((d == 0 ? 0x2 : 0x4) >> i) & 1);
     }
     __host__ __device__ static constexpr int face_n() { return 0; }
     __host__ __device__ static constexpr int face(int, int) { return 0; }
@@ -98,7 +117,10 @@ struct Elem<UG4GB_TET> {
 template <int T>
 __host__ __device__ __forceinline__ void local_grad(const double *xi, int sh, double *g)
 {
-    if constexpr (T == UG4GB_QUAD) {
+    if constexpr (T == UG4GB_TRI) {
+        g[0] = (sh == 0) ? -1.0 : (sh == 1 ? 1.0 : 0.0);
+        g[1] = (sh == 0) ? -1.0 : (sh == 2 ? 1.0 : 0.0);
+    } else if constexpr (T == UG4GB_QUAD) {
         double cx = Elem<T>::corner(sh, 0), cy = Elem<T>::corner(sh, 1);
         double fx = cx ? xi[0] : 1.0 - xi[0], fy = cy ? xi[1] : 1.0 - xi[1];
         g[0] = (cx ? 1.0 : -1.0) * fy;
@@ -305,7 +327,9 @@ __device__ __forceinline__ void elem_matrix(const double (&X)[Elem<T>::K][Elem<T
     double gm[3];
     elem_centre<T>(X, gm);
     double Ji[3][3];
-    if constexpr (T == UG4GB_TET) {
+    // simplices: affine map, one (J^T)^{-1} for the element
+    constexpr bool affine = (T == UG4GB_TET || T == UG4GB_TRI);
+    if constexpr (affine) {
         double xi[3] = {0.25, 0.25, 0.25};
         jt_inverse<T>(X, xi, Ji);
     }
@@ -338,7 +362,7 @@ __device__ __forceinline__ void elem_matrix(const double (&X)[Elem<T>::K][Elem<T
         }
         double xi[3];
         local_ip<T>(ip, xi);
-        if constexpr (T != UG4GB_TET) jt_inverse<T>(X, xi, Ji);
+        if constexpr (!affine) jt_inverse<T>(X, xi, Ji);
 #pragma unroll
         for (int sh = 0; sh < E::K; ++sh) {
             double lg[3];

@@ -1,7 +1,8 @@
 // k_fv1.cu -- FV1 (vertex-centred box) element assembly on the GPU, FP64.
 //
 // One thread per cell (a quad, a hex, or the 6 Kuhn tets of a hex), launched
-// once per parity colour.  The element geometry follows FV1Geometry_gen::
+// once per parity colour; on unstructured levels one thread per element,
+// launched once per element colour.  The element geometry follows FV1Geometry_gen::
 // update (lib_disc/spatial_disc/disc_util/fv1_geom.cpp:331-464): mid points
 // as corner averages, one SCVF per element edge with patch [edge mid, centre]
 // (2D) or [edge mid, side-0 centre, centre, side-1 centre] (3D), area normal
@@ -17,7 +18,9 @@
 // level CRS (slots found by binary search in the sorted row) colour by colour,
 // without atomics, so every run assembles the same bits.
 // Reference-element numbering: lib_disc/reference_element/reference_element.cpp
-// (quadrilateral :428, tetrahedron :547, hexahedron :1327).
+// (triangle :320-420, quadrilateral :428, tetrahedron :547, hexahedron :1327).
+#include <type_traits>
+
 #include "common.cuh"
 #include "fv1_elem.cuh"
 #include "disc.cuh"
@@ -51,6 +54,62 @@ __device__ __forceinline__ int colour_cell(const AsmArgs &a, int t, int colour, 
     const int t0 = t % n0, t1 = (t / n0) % n1, t2 = t / (n0 * n1);
     *cell = (2 * t0 + b0) + a.cx * ((2 * t1 + b1) + a.cy * (2 * t2 + b2));
     return 1;
+}
+
+// Calls f(e) for the elements of one colour handled by thread t: on a
+// structured level the element(s) of one parity cell (a tet cell holds 6
+// Kuhn tets), on an unstructured level one element of the colour's list
+// (element colours such that no two elements of a colour share a vertex).
+template <int T, class F>
+__device__ __forceinline__ void for_colour_elements(const AsmArgs &a, int colour, F &&f)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a.elist) {
+        if (t < a.nlist) f(a.elist[t]);
+        return;
+    }
+    int cell;
+    if (!colour_cell(a, t, colour, &cell)) return;
+    if (T == UG4GB_TET) {
+        for (int p = 0; p < 6; ++p) f(6 * cell + p);
+    } else {
+        f(cell);
+    }
+}
+
+// Launches kern(a, colour) once per colour of level L (parity cells of a
+// structured level, element lists of an unstructured one), 128 threads a block.
+template <class K>
+void launch_coloured(Ctx &c, const Level &L, AsmArgs a, K kern)
+{
+    if (L.structured) {
+        a.cx = L.nx - 1;
+        a.cy = L.ny - 1;
+        a.cz = (L.dim == 3) ? L.nz - 1 : 1;
+        a.elist = nullptr;
+        const int ncol = (L.dim == 3) ? 8 : 4;
+        const int per = ((a.cx + 1) / 2) * ((a.cy + 1) / 2) * ((a.cz + 1) / 2);
+        for (int colour = 0; colour < ncol; ++colour) kern(a, colour, div_up(per, 128));
+    } else {
+        for (int q = 0; q + 1 < (int)L.ecol_off.size(); ++q) {
+            a.elist = L.ecol.p + L.ecol_off[q];
+            a.nlist = L.ecol_off[q + 1] - L.ecol_off[q];
+            if (a.nlist > 0) kern(a, q, div_up(a.nlist, 128));
+        }
+    }
+}
+
+// Calls f(std::integral_constant<int, T>) for the element type of level L.
+template <class F>
+void dispatch_elem(int elem_type, F &&f)
+{
+    switch (elem_type) {
+        case UG4GB_QUAD: f(std::integral_constant<int, UG4GB_QUAD>()); break;
+        case UG4GB_HEX: f(std::integral_constant<int, UG4GB_HEX>()); break;
+        case UG4GB_TET: f(std::integral_constant<int, UG4GB_TET>()); break;
+        case UG4GB_TRI: f(std::integral_constant<int, UG4GB_TRI>()); break;
+        default: throw Error{UG4GB_ERR_INVALID, "unknown element type"};
+    }
 }
 
 template <int T>
@@ -132,13 +191,7 @@ __device__ __forceinline__ void assemble_element(const AsmArgs &a, int e)
 template <int T>
 __global__ void __launch_bounds__(128) k_assemble(AsmArgs a, int colour)
 {
-    int cell;
-    if (!colour_cell(a, blockIdx.x * blockDim.x + threadIdx.x, colour, &cell)) return;
-    if (T == UG4GB_TET) {
-        for (int p = 0; p < 6; ++p) assemble_element<T>(a, 6 * cell + p);
-    } else {
-        assemble_element<T>(a, cell);
-    }
+    for_colour_elements<T>(a, colour, [&](int e) { assemble_element<T>(a, e); });
 }
 
 // Dirichlet rows: values 0, diagonal 1, pattern kept, rhs 0
@@ -154,18 +207,12 @@ __global__ void k_dirichlet_rows(const unsigned char *bnd, int nv, const int *ro
 
 void launch_assemble(Ctx &c, const Level &L, const AsmArgs &a_in)
 {
-    AsmArgs a = a_in;
-    a.cx = L.nx - 1;
-    a.cy = L.ny - 1;
-    a.cz = (L.dim == 3) ? L.nz - 1 : 1;
-    const int ncol = (L.dim == 3) ? 8 : 4;
-    const int per = ((a.cx + 1) / 2) * ((a.cy + 1) / 2) * ((a.cz + 1) / 2);
-    unsigned g = div_up(per, 128);
-    for (int colour = 0; colour < ncol; ++colour) {
-        if (L.elem_type == UG4GB_QUAD) UG_LAUNCH(c, k_assemble<UG4GB_QUAD>, g, 128, 0, a, colour);
-        else if (L.elem_type == UG4GB_HEX) UG_LAUNCH(c, k_assemble<UG4GB_HEX>, g, 128, 0, a, colour);
-        else UG_LAUNCH(c, k_assemble<UG4GB_TET>, g, 128, 0, a, colour);
-    }
+    dispatch_elem(L.elem_type, [&](auto tag) {
+        constexpr int T = decltype(tag)::value;
+        launch_coloured(c, L, a_in, [&](const AsmArgs &a, int colour, int g) {
+            UG_LAUNCH(c, k_assemble<T>, g, 128, 0, a, colour);
+        });
+    });
 }
 
 void launch_dirichlet(Ctx &c, const Level &L, Csr &A, double *b)
@@ -237,13 +284,7 @@ __device__ __forceinline__ void defect_element(const AsmArgs &a, int e)
 template <int T>
 __global__ void __launch_bounds__(128) k_defect(AsmArgs a, int colour)
 {
-    int cell;
-    if (!colour_cell(a, blockIdx.x * blockDim.x + threadIdx.x, colour, &cell)) return;
-    if (T == UG4GB_TET) {
-        for (int p = 0; p < 6; ++p) defect_element<T>(a, 6 * cell + p);
-    } else {
-        defect_element<T>(a, cell);
-    }
+    for_colour_elements<T>(a, colour, [&](int e) { defect_element<T>(a, e); });
 }
 
 // Dirichlet vertices: defect 0 (DirichletBoundary::adjust_defect,
@@ -257,19 +298,13 @@ __global__ void k_zero_dirichlet(const unsigned char *bnd, int nv, double *x)
 
 void launch_defect(Ctx &c, const Level &L, const AsmArgs &a_in)
 {
-    AsmArgs a = a_in;
-    a.cx = L.nx - 1;
-    a.cy = L.ny - 1;
-    a.cz = (L.dim == 3) ? L.nz - 1 : 1;
-    const int ncol = (L.dim == 3) ? 8 : 4;
-    const int per = ((a.cx + 1) / 2) * ((a.cy + 1) / 2) * ((a.cz + 1) / 2);
-    unsigned g = div_up(per, 128);
-    for (int colour = 0; colour < ncol; ++colour) {
-        if (L.elem_type == UG4GB_QUAD) UG_LAUNCH(c, k_defect<UG4GB_QUAD>, g, 128, 0, a, colour);
-        else if (L.elem_type == UG4GB_HEX) UG_LAUNCH(c, k_defect<UG4GB_HEX>, g, 128, 0, a, colour);
-        else UG_LAUNCH(c, k_defect<UG4GB_TET>, g, 128, 0, a, colour);
-    }
-    UG_LAUNCH(c, k_zero_dirichlet, div_up(L.nv, 256), 256, 0, L.bnd.p, L.nv, a.d);
+    dispatch_elem(L.elem_type, [&](auto tag) {
+        constexpr int T = decltype(tag)::value;
+        launch_coloured(c, L, a_in, [&](const AsmArgs &a, int colour, int g) {
+            UG_LAUNCH(c, k_defect<T>, g, 128, 0, a, colour);
+        });
+    });
+    UG_LAUNCH(c, k_zero_dirichlet, div_up(L.nv, 256), 256, 0, L.bnd.p, L.nv, a_in.d);
 }
 
 void launch_dirichlet_values(Ctx &c, const Level &L, double *u)
@@ -311,12 +346,10 @@ void launch_coef_fourier(Ctx &c, const Level &L, int nmodes, const double *k, co
                          double factor, double *K)
 {
     unsigned g = div_up(L.ne, 256);
-    if (L.elem_type == UG4GB_QUAD)
-        UG_LAUNCH(c, k_coef_fourier<UG4GB_QUAD>, g, 256, 0, L.coords.p, L.elems.p, L.ne, nmodes, k, phase, amp, factor, K);
-    else if (L.elem_type == UG4GB_HEX)
-        UG_LAUNCH(c, k_coef_fourier<UG4GB_HEX>, g, 256, 0, L.coords.p, L.elems.p, L.ne, nmodes, k, phase, amp, factor, K);
-    else
-        UG_LAUNCH(c, k_coef_fourier<UG4GB_TET>, g, 256, 0, L.coords.p, L.elems.p, L.ne, nmodes, k, phase, amp, factor, K);
+    dispatch_elem(L.elem_type, [&](auto tag) {
+        constexpr int T = decltype(tag)::value;
+        UG_LAUNCH(c, k_coef_fourier<T>, g, 256, 0, L.coords.p, L.elems.p, L.ne, nmodes, k, phase, amp, factor, K);
+    });
 }
 
 // coarse log K = mean of the children's log K.  Gather: each coarse element
@@ -435,12 +468,10 @@ __global__ void __launch_bounds__(128) k_grad_logk(const double *coords, const i
 void launch_grad_logk(Ctx &c, const Level &L, const double *K, const double *u, const double *lam, double *g)
 {
     unsigned gr = div_up(L.ne, 128);
-    if (L.elem_type == UG4GB_QUAD)
-        UG_LAUNCH(c, k_grad_logk<UG4GB_QUAD>, gr, 128, 0, L.coords.p, L.elems.p, L.ne, L.bnd.p, K, u, lam, g);
-    else if (L.elem_type == UG4GB_HEX)
-        UG_LAUNCH(c, k_grad_logk<UG4GB_HEX>, gr, 128, 0, L.coords.p, L.elems.p, L.ne, L.bnd.p, K, u, lam, g);
-    else
-        UG_LAUNCH(c, k_grad_logk<UG4GB_TET>, gr, 128, 0, L.coords.p, L.elems.p, L.ne, L.bnd.p, K, u, lam, g);
+    dispatch_elem(L.elem_type, [&](auto tag) {
+        constexpr int T = decltype(tag)::value;
+        UG_LAUNCH(c, k_grad_logk<T>, gr, 128, 0, L.coords.p, L.elems.p, L.ne, L.bnd.p, K, u, lam, g);
+    });
 }
 
 // sum of SCV volumes per vertex (d rhs_i / d f_i)
@@ -448,11 +479,7 @@ template <int T>
 __global__ void k_scv_volumes(AsmArgs a, int colour, double *vol)
 {
     using E = Elem<T>;
-    int cell;
-    if (!colour_cell(a, blockIdx.x * blockDim.x + threadIdx.x, colour, &cell)) return;
-    const int per = (T == UG4GB_TET) ? 6 : 1;
-    for (int p = 0; p < per; ++p) {
-        const int e = per * cell + p;
+    for_colour_elements<T>(a, colour, [&](int e) {
         int ev[E::K];
         double X[E::K][E::DIM];
 #pragma unroll
@@ -465,7 +492,7 @@ __global__ void k_scv_volumes(AsmArgs a, int colour, double *vol)
         scv_volumes<T>(X, v);
 #pragma unroll
         for (int i = 0; i < E::K; ++i) vol[ev[i]] += v[i];
-    }
+    });
 }
 
 __global__ void k_grad_source(const double *vol, const unsigned char *bnd, const double *lam, int nv, double *g)
@@ -483,16 +510,12 @@ void launch_grad_source(Ctx &c, const Level &L, const double *lam, double *g)
     a.coords = L.coords.p;
     a.elems = L.elems.p;
     a.ne = L.ne;
-    a.cx = L.nx - 1;
-    a.cy = L.ny - 1;
-    a.cz = (L.dim == 3) ? L.nz - 1 : 1;
-    const int ncol = (L.dim == 3) ? 8 : 4;
-    unsigned gr = div_up(((a.cx + 1) / 2) * ((a.cy + 1) / 2) * ((a.cz + 1) / 2), 128);
-    for (int colour = 0; colour < ncol; ++colour) {
-        if (L.elem_type == UG4GB_QUAD) UG_LAUNCH(c, k_scv_volumes<UG4GB_QUAD>, gr, 128, 0, a, colour, vol.p);
-        else if (L.elem_type == UG4GB_HEX) UG_LAUNCH(c, k_scv_volumes<UG4GB_HEX>, gr, 128, 0, a, colour, vol.p);
-        else UG_LAUNCH(c, k_scv_volumes<UG4GB_TET>, gr, 128, 0, a, colour, vol.p);
-    }
+    dispatch_elem(L.elem_type, [&](auto tag) {
+        constexpr int T = decltype(tag)::value;
+        launch_coloured(c, L, a, [&](const AsmArgs &aa, int colour, int g) {
+            UG_LAUNCH(c, k_scv_volumes<T>, g, 128, 0, aa, colour, vol.p);
+        });
+    });
     UG_LAUNCH(c, k_grad_source, div_up(L.nv, 256), 256, 0, vol.p, L.bnd.p, lam, L.nv, g);
     UG_CUDA(cudaStreamSynchronize(c.stream));
 }

@@ -101,6 +101,8 @@ void gen_level(Ctx &c, Level &L, int elem_type, int cx, int cy, int cz, const Le
     L.elems.alloc((size_t)L.ne * L.k);
     L.bnd.alloc(L.nv);
     L.color.alloc(L.nv);
+    L.structured = true;
+    L.ncolors = 1 << L.dim;
     UG_LAUNCH(c, k_gen_vertices, div_up(L.nv, 256), 256, 0, L.nx, L.ny, L.nz, L.dim, L.coords.p, L.bnd.p,
               L.color.p);
     UG_LAUNCH(c, k_gen_elements, div_up(L.ne, 256), 256, 0, elem_type, L.nx, L.ny, L.nz, L.elems.p);
@@ -196,7 +198,7 @@ __global__ void k_fill_adjacency(const int *elems, int nek, int k, const int *vp
     adj[vptr[v] + pos] = t / k;
 }
 
-constexpr int kRowCand = 128;   // max candidate columns per row (96 for Kuhn tets)
+constexpr int kRowCand = 256;   // max candidate columns per row (96 for Kuhn tets, 64 corner-sharing tets)
 
 // One warp per row: gather corners of adjacent elements into shared memory,
 // keep first occurrences, rank them.  mode 0 counts, mode 1 writes columns.
@@ -269,7 +271,7 @@ void csr_from_elements(Ctx &c, const Level &L, Csr &A)
     exclusive_scan_int(c, rowlen.p, A.rowptr.p, nv + 1, &nnz);
     int ovf = 0;
     UG_CUDA(cudaMemcpy(&ovf, overflow.p, sizeof(int), cudaMemcpyDeviceToHost));
-    UG_REQUIRE(!ovf, UG4GB_ERR_INVALID, "csr_from_elements: a vertex couples to more than 128 corners");
+    UG_REQUIRE(!ovf, UG4GB_ERR_INVALID, "csr_from_elements: a vertex couples to more than 256 element corners");
     UG_REQUIRE(nnz < (int64_t)1 << 31, UG4GB_ERR_INVALID, "csr_from_elements: nnz exceeds int32 range");
     A.nnz = nnz;
     A.col.alloc(nnz);

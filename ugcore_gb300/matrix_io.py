@@ -113,3 +113,28 @@ def SaveVectorForConnectionViewer(hier, v, filename, level=None):
 def LoadVector(v, filename):
     check(lib().ug4gb_vector_read_cv(v.h, filename.encode()), v.ctx.h)
     return v
+
+
+# ---- UGX coarse grids (host only) -----------------------------------------
+def ugx_level(filename, num_refinements, level, dirichlet=None):
+    """Level `level` of the hierarchy ug4gb_grid_create_ugx builds, computed
+    on the host (no context, no GPU): dict with elem_type, coords, elems,
+    dirichlet (vertex flags), npar, par (level >= 1)."""
+    names = None if dirichlet is None else (dirichlet if isinstance(dirichlet, str) else ",".join(dirichlet))
+    nb = None if names is None else names.encode()
+    err = C.create_string_buffer(_ERRCAP)
+    et, nv, ne = C.c_int(), C.c_int(), C.c_int()
+    _raise(lib().ug4gb_io_ugx_level(filename.encode(), num_refinements, nb, level, C.byref(et), C.byref(nv),
+                                    C.byref(ne), None, None, None, None, None, err, _ERRCAP), err)
+    dim = 2 if et.value in (0, 3) else 3
+    k = {0: 4, 1: 8, 2: 4, 3: 3}[et.value]
+    coords = np.zeros((nv.value, dim))
+    elems = np.zeros((ne.value, k), np.int32)
+    bnd = np.zeros(nv.value, np.uint8)
+    npar = np.zeros(nv.value, np.int32)
+    par = np.zeros((nv.value, 8), np.int32)
+    _raise(lib().ug4gb_io_ugx_level(filename.encode(), num_refinements, nb, level, C.byref(et), C.byref(nv),
+                                    C.byref(ne), _p(coords), _p(elems), _p(bnd),
+                                    _p(npar) if level else None, _p(par) if level else None, err, _ERRCAP), err)
+    return dict(elem_type=et.value, coords=coords, elems=elems, dirichlet=bnd,
+                npar=npar if level else None, par=par if level else None)
