@@ -284,12 +284,13 @@ def run_ours(args, rank, world, local_rank):
                  "kernel_profile": profile_summary(prof_m)}
         del pm
 
-    target = adj = conv = rap = None
+    target = adj = conv = rap = unstr = None
     if not args.no_extras:
         target = run_target(args, ctx, timed, world, hbm)
         adj = run_adjoint_grad(args, ctx, timed)
         conv = run_convection_adjoint(args, ctx, timed, world, hbm)
         rap = run_galerkin(args, ctx, timed, world)
+        unstr = run_unstructured(args, ctx, timed, world, hbm)
 
     # ---- assembly throughput (top level, FP64 FV1 + CRS values + rhs)
     asm = None
@@ -333,6 +334,7 @@ def run_ours(args, rank, world, local_rank):
         "adjoint_gradient": adj,
         "convection_adjoint": conv,
         "galerkin_coarse_operators": rap,
+        "unstructured_tets": unstr,
         "assembly": asm,
         "clocks": clocks,
         "cpu_baseline": cpu,
@@ -477,6 +479,93 @@ def run_galerkin(args, ctx, timed, world):
                                                    "rel_residual": st["defect"] / st["initial_defect"]}
             del p
         out["%s_%s" % (name, prec)] = res
+    return out
+
+
+def sell_iteration_bytes(sizes, sv):
+    """algorithmic bytes of one PCG iteration on an unstructured hierarchy:
+    SELL-32 operators (values + 32-bit column indices per stored entry) and
+    stored P / R, otherwise as iteration_bytes"""
+    L = len(sizes) - 1
+    tot = 0
+    for l in range(1, L + 1):
+        s, c = sizes[l], sizes[l - 1]
+        M = s["nnz"] * (sv + 4)
+        tot += smooth_bytes(dict(s, nnz=0), sv, l == L) + 4 * M
+        tot += s["nR"] * (sv + 4) + s["N"] * sv + c["N"] * sv          # R d
+        tot += s["nP"] * (sv + 4) + c["N"] * sv + s["N"] * (4 * sv)    # sc += dfac * (P sc_c)
+    b = sizes[0]["N"]
+    tot += b * b * 8 + 2 * b * sv
+    top = sizes[L]
+    tot += top["nnz"] * 12 + top["N"] * (sv + 16 + 16) + top["N"] * 48
+    return tot
+
+
+def run_unstructured(args, ctx, timed, world, hbm):
+    """Unstructured tetrahedral hierarchy: the 12-tetrahedron unit-cube UGX
+    grid (tests/golden/grids/cube_tets.ugx) refined 7 times regularly
+    (25.2M tets, 4.26M DoFs), K = exp(2 g), Dirichlet subset "Bottom";
+    GMG V(2,2) Jacobi(0.6) on assembled P/R and SELL-32 operators, PCG to
+    1e-10, FP64 and mixed precision."""
+    import ctypes as C
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import _lib, fields
+    nref = 7
+    t0 = time.perf_counter()
+    hier = ug.UnstructuredHierarchy.from_ugx(ctx, os.path.join(ROOT, "tests", "golden", "grids", "cube_tets.ugx"),
+                                             nref, "Bottom")
+    grid_s = time.perf_counter() - t0
+    n = hier.num_vertices()
+    disc = ug.DomainDiscretization(hier)
+    disc.set_diffusion_field(fields.ScalarField(3, 64, 8.0, 1 ^ fields.COEF_SEED_XOR), factor=2.0)
+    disc.set_source_uniform(1)
+    A = ug.GPUSparseMatrix(ctx)
+    b = ug.GPUVector(ctx, n)
+    disc.assemble_linear(A, b)
+    ms_asm = timed(lambda: disc.assemble_linear(A, b), 3)
+    out = {"workload": "unstructured tets: 12-tet unit cube (UGX) refined 7x regularly, K=exp(2g), "
+                       "GMG V(2,2) Jacobi(0.6)-PCG to 1e-10, SELL-32 operators, stored P/R",
+           "dofs": n, "elements": hier.num_elements(), "hierarchy_setup_s": grid_s,
+           "assembly_ms": ms_asm, "assembly_dofs_per_s": n / (ms_asm * 1e-3)}
+    for prec in ("fp64", "mixed"):
+        gmg = ug.GeometricMultiGrid(disc)
+        gmg.set_smoother(ug.Jacobi(0.6))
+        gmg.set_precision(prec)
+        t0 = time.perf_counter()
+        gmg.init(A)
+        init_s = time.perf_counter() - t0
+        solver = ug.CG(ctx)
+        solver.set_preconditioner(gmg)
+        solver.set_convergence_check(ug.StdConvCheck(200, 1e-300, 1e-10))
+        solver.init(A)
+        x = ug.GPUVector(ctx, n)
+
+        def solve():
+            x.set(0.0)
+            solver.apply(x, b)
+        for _ in range(min(args.warmup, 3)):
+            solve()
+        ms = max_over_ranks(timed(solve, max(2, args.steps // 3)), world)
+        st = solver.stats()
+        sizes = []
+        for l in range(hier.num_levels):
+            r, nnz = C.c_int(), C.c_int64()
+            _lib.check(_lib.lib().ug4gb_gmg_level_info(gmg.h, l, C.byref(r), C.byref(nnz)))
+            nP = nR = 0
+            if l > 0:
+                rr, cc, z = C.c_int(), C.c_int(), C.c_int64()
+                _lib.check(_lib.lib().ug4gb_gmg_transfer_info(gmg.h, l, 0, C.byref(rr), C.byref(cc), C.byref(z)))
+                nP = z.value
+                _lib.check(_lib.lib().ug4gb_gmg_transfer_info(gmg.h, l, 1, C.byref(rr), C.byref(cc), C.byref(z)))
+                nR = z.value
+            sizes.append(dict(N=r.value, nnz=nnz.value, nP=nP, nR=nR))
+        gbs = sell_iteration_bytes(sizes, 8 if prec == "fp64" else 4) * st["steps"] / (ms * 1e-3) / 1e9
+        out[prec] = {"ms_per_solve": ms, "dofs_per_s": world * n / (ms * 1e-3), "pcg_steps": st["steps"],
+                     "rel_residual": st["defect"] / st["initial_defect"], "gmg_init_s": init_s,
+                     "solve_gbs": gbs, "solve_frac_of_measured_hbm": gbs / hbm}
+        out["nnz"] = sizes[-1]["nnz"]
+        del solver, gmg
+    out["mixed_speedup_vs_fp64"] = out["fp64"]["ms_per_solve"] / out["mixed"]["ms_per_solve"]
     return out
 
 
