@@ -5,6 +5,11 @@ statistics as JSON, e.g. to profile one precision or layout in isolation:
     python -m ugcore_gb300.run_case --config c1 --nref 5 --format sell
     python -m ugcore_gb300.run_case --config c2 --precision mixed --direct --sweep-fusion 1
 
+--ugx FILE runs an unstructured hierarchy instead (the UGX coarse grid refined
+--nref times, Dirichlet subsets --dirichlet, lognormal K, CG, Jacobi V(2,2)):
+
+    python -m ugcore_gb300.run_case --ugx tests/golden/grids/cube_tets.ugx --nref 7 --dirichlet Bottom
+
 --direct runs the solves with the library profiler on: every kernel is
 launched directly instead of being replayed from the solve's CUDA graph
 (profilers cannot attribute kernels inside graphs with conditional nodes),
@@ -19,6 +24,42 @@ import json
 import time
 
 
+class _UgxProblem:
+    """the solve of one unstructured hierarchy, with Problem's solve()"""
+
+    def __init__(self, ctx, args):
+        import ugcore_gb300 as ug
+        from ugcore_gb300 import fields
+        self.hier = ug.UnstructuredHierarchy.from_ugx(ctx, args.ugx, 3 if args.nref is None else args.nref,
+                                                      args.dirichlet)
+        self.n = self.hier.num_vertices()
+        self.disc = ug.DomainDiscretization(self.hier)
+        self.disc.set_diffusion_field(fields.ScalarField(self.hier.dim, 64, 8.0, 1 ^ fields.COEF_SEED_XOR),
+                                      factor=2.0)
+        self.disc.set_source_uniform(1)
+        self.A = ug.GPUSparseMatrix(ctx)
+        self.b = ug.GPUVector(ctx, self.n)
+        self.disc.assemble_linear(self.A, self.b)
+        self.gmg = ug.GeometricMultiGrid(self.disc)
+        self.gmg.set_smoother(ug.Jacobi(0.6) if args.smoother != "mcgs" else ug.GaussSeidel(1.0))
+        self.gmg.set_precision(args.precision or "fp64")
+        self.gmg.init(self.A)
+        self.solver = ug.CG(ctx)
+        self.solver.set_preconditioner(self.gmg)
+        self.solver.set_convergence_check(ug.StdConvCheck(200, 1e-300, 1e-10))
+        self.solver.init(self.A)
+        self.x = ug.GPUVector(ctx, self.n)
+
+    def solve(self):
+        self.x.set(0.0)
+        self.solver.apply(self.x, self.b)
+        return self.solver.stats()
+
+
+def ugx_problem(ctx, args):
+    return _UgxProblem(ctx, args)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c1")
@@ -30,6 +71,8 @@ def main():
     ap.add_argument("--direct", action="store_true")
     ap.add_argument("--sweep-fusion", type=int, default=None)
     ap.add_argument("--sweep-planes", type=int, default=None)
+    ap.add_argument("--ugx", default=None)
+    ap.add_argument("--dirichlet", default=None)
     args = ap.parse_args()
 
     import ugcore_gb300 as ug
@@ -45,7 +88,7 @@ def main():
     ctx.set_operator_format(args.format)
     ctx.set_tuning(sweep_fusion=args.sweep_fusion, sweep_planes=args.sweep_planes)
     t0 = time.perf_counter()
-    p = problems.Problem(ctx, problems.config(args.config, **over))
+    p = ugx_problem(ctx, args) if args.ugx else problems.Problem(ctx, problems.config(args.config, **over))
     ctx.synchronize()
     setup = time.perf_counter() - t0
     out = []
@@ -57,7 +100,7 @@ def main():
         ctx.synchronize()
         out.append({"ms": (time.perf_counter() - t0) * 1e3, "steps": st["steps"],
                     "rel_residual": st["defect"] / st["initial_defect"]})
-    res = {"config": args.config, "dofs": p.n, "setup_s": setup, "solves": out}
+    res = {"config": args.ugx or args.config, "dofs": p.n, "setup_s": setup, "solves": out}
     if args.direct:
         prof = ctx.profile_end()
         res["kernels"] = {k: [v[0], round(v[1], 4)] for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
