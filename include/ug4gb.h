@@ -49,6 +49,8 @@ extern "C" {
 /* smoothers, precisions, solvers */
 #define UG4GB_SMOOTHER_JACOBI 0     /* damped Jacobi (lib_algebra/operator/preconditioner/jacobi.h:90) */
 #define UG4GB_SMOOTHER_MCGS 1       /* multicolour Gauss-Seidel (opt-in; no ugcore counterpart) */
+#define UG4GB_SMOOTHER_MCSGS 2      /* symmetric multicolour Gauss-Seidel: forward colour sweep, then
+                                       backward (SymmetricGaussSeidel, gauss_seidel.h:350, in colour order) */
 #define UG4GB_PREC_FP64 0           /* whole preconditioner in FP64 */
 #define UG4GB_PREC_MIXED 1          /* FP32 smoother/transfers/SpMV, FP64 outer Krylov and base LU */
 #define UG4GB_SOLVER_CG 0           /* lib_algebra/operator/linear_solver/cg.h:59 */

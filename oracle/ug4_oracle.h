@@ -138,7 +138,7 @@ void orc_lu_apply(const orc_lu *F, double *x, const double *b);
 void orc_lu_free(orc_lu *F);
 
 /* GMG */
-enum { ORC_SMOOTH_JACOBI = 0, ORC_SMOOTH_MCGS = 1 };
+enum { ORC_SMOOTH_JACOBI = 0, ORC_SMOOTH_MCGS = 1, ORC_SMOOTH_MCSGS = 2 };
 typedef struct {
     int nlev, base, cycle, nu1, nu2, smoother;
     double damp;

@@ -256,6 +256,23 @@ static void mcgs_apply(const orc_crs *A, const int *color, int ncolor, double re
         }
 }
 
+/* backward multicolour sweep on c (SymmetricGaussSeidel, gauss_seidel.h:350,
+   in colour order): c_i += relax (d_i - (A c)_i) / a_ii, colours descending */
+static void mcgs_backward(const orc_crs *A, const int *color, int ncolor, double relax, double *c, const double *d)
+{
+    int n = A->n_rows;
+    for (int col = ncolor - 1; col >= 0; --col)
+        for (int i = 0; i < n; ++i) {
+            if (color[i] != col) continue;
+            double s = d[i], diag = 1.0;
+            for (int a = A->rowptr[i]; a < A->rowptr[i + 1]; ++a) {
+                if (A->col[a] == i) diag = A->val[a];
+                s -= A->val[a] * c[A->col[a]];
+            }
+            c[i] += relax * s / diag;
+        }
+}
+
 static void smooth(orc_gmg *G, int l, double *c, const double *d)
 {
     int n = G->A[l].n_rows;
@@ -264,6 +281,7 @@ static void smooth(orc_gmg *G, int l, double *c, const double *d)
         for (int i = 0; i < n; ++i) c[i] = di[i] * d[i];
     } else {
         mcgs_apply(&G->A[l], G->color[l], G->ncolor[l], G->damp, c, d);
+        if (G->smoother == ORC_SMOOTH_MCSGS) mcgs_backward(&G->A[l], G->color[l], G->ncolor[l], G->damp, c, d);
     }
 }
 

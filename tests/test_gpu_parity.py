@@ -129,10 +129,24 @@ def test_variable_coefficient_tets_full_size_against_fp64_oracle(ctx, oracle_lib
     assert abs(st["steps"] - ref["steps"]) <= 3
 
 
-def test_mcgs_smoother_matches_oracle(ctx, oracle_lib):
-    cfg, p = _problem(ctx, "c1", dict(nref=3, smoother="mcgs", damp=1.0))
-    st = p.solve()
+@pytest.mark.parametrize("name,smoother", [("c1", "mcgs"), ("c1", "mcsgs"), ("c0", "mcsgs"), ("c4", "mcsgs")])
+def test_mcgs_smoother_matches_oracle(ctx, oracle_lib, name, smoother):
+    """multicolour Gauss-Seidel and its symmetric variant (forward, then
+    backward colour sweep): GMG application 1e-12, solve iterations +-1"""
+    import ugcore_gb300 as ug
+    over = dict(nref=3 if name != "c0" else 5, smoother=smoother, damp=1.0, precision="fp64")
+    if name == "c4":
+        over["nref"] = 2
+    cfg, p = _problem(ctx, name, over)
     op = _oracle(oracle_lib, cfg, p)
+    d = np.random.default_rng(1).standard_normal(p.n)
+    _, _, bnd = p.hier.export()
+    d[bnd.astype(bool)] = 0.0
+    cv = ug.GPUVector(ctx, p.n)
+    p.gmg.apply(cv, ug.GPUVector(ctx, p.n).copy_from(d))
+    c_ref = op.apply_gmg(d)
+    assert np.abs(cv.numpy() - c_ref).max() <= 1e-12 * np.abs(c_ref).max()
+    st = p.solve()
     ref = op.solve()
     assert abs(st["steps"] - ref["steps"]) <= 1
     assert np.abs(p.x.numpy() - ref["x"]).max() <= 1e-8 * np.abs(ref["x"]).max()

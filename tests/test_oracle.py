@@ -215,6 +215,25 @@ def test_mcgs_oracle_converges(oracle_lib):
     assert s["converged"] and s["steps"] < 10
 
 
+def test_symmetric_mcgs_is_symmetric_and_converges(oracle_lib):
+    """the symmetric multicolour Gauss-Seidel smoother gives a symmetric
+    multigrid preconditioner on a symmetric operator (M d1 . d2 = d1 . M d2
+    away from the Dirichlet rows), as CG needs, and converges"""
+    o = oracle_lib
+    P = o.Problem(o.make_params(elem_type=o.ORC_QUAD, mx=2, my=2, nref=4, smoother=2, damp=1.0, nu1=2, nu2=2))
+    s = P.solve()
+    assert s["converged"] and s["steps"] < 12
+    rng = np.random.default_rng(0)
+    n = P.nv()
+    rp, ci, va = P.matrix()
+    bnd = np.array([va[rp[i]:rp[i + 1]][ci[rp[i]:rp[i + 1]] == i][0] == 1.0 and
+                    np.count_nonzero(va[rp[i]:rp[i + 1]]) == 1 for i in range(n)])
+    d1, d2 = rng.standard_normal(n), rng.standard_normal(n)
+    d1[bnd] = d2[bnd] = 0.0
+    a, b = P.apply_gmg(d1) @ d2, d1 @ P.apply_gmg(d2)
+    assert abs(a - b) <= 1e-12 * abs(a)
+
+
 def test_adjoint_oracle_matches_finite_differences(oracle_lib):
     o = oracle_lib
     rng = np.random.default_rng(1)

@@ -494,6 +494,14 @@ class GaussSeidel:
         self.kind, self.damp = _lib.SMOOTHER_MCGS, float(relax)
 
 
+class SymmetricGaussSeidel:
+    """symmetric multicolour Gauss-Seidel: forward, then backward colour sweep
+    (GPU variant of SymmetricGaussSeidel, gauss_seidel.h:350)"""
+
+    def __init__(self, relax=1.0):
+        self.kind, self.damp = _lib.SMOOTHER_MCSGS, float(relax)
+
+
 class GeometricMultiGrid:
     """AssembledMultiGridCycle: V/W cycle, re-assembled level operators,
     StdTransfer, LU base solver."""

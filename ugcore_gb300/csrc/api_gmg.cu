@@ -384,11 +384,16 @@ struct GmgT : GmgBase {
         L.dcur = const_cast<V *>(dbase);
     }
 
+    // t = B d: colours in increasing order from t = 0; the symmetric smoother
+    // then sweeps the colours in decreasing order
     void gs_sweep(Ctx &c, GLevel<V> &L, const V *dv, const int *skip)
     {
         UG_LAUNCH_PDL(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.t.p, skip);
         for (size_t q = 0; q < L.crow.size(); ++q)
             if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], L.dinv.p, dv, L.t.p, skip);
+        if (smoother == UG4GB_SMOOTHER_MCSGS)
+            for (size_t q = L.crow.size(); q-- > 0;)
+                if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], L.dinv.p, dv, L.t.p, skip);
     }
 
     const double *apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
@@ -519,7 +524,9 @@ int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out)
 
 int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp)
 {
-    if (!m || (kind != UG4GB_SMOOTHER_JACOBI && kind != UG4GB_SMOOTHER_MCGS) || !(damp > 0.0)) return UG4GB_ERR_INVALID;
+    if (!m || (kind != UG4GB_SMOOTHER_JACOBI && kind != UG4GB_SMOOTHER_MCGS && kind != UG4GB_SMOOTHER_MCSGS) ||
+        !(damp > 0.0))
+        return UG4GB_ERR_INVALID;
     m->smoother = kind;
     m->damp = damp;
     return UG4GB_OK;

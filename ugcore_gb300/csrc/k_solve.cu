@@ -657,7 +657,9 @@ __global__ void __launch_bounds__(NT) k_mcgs(MV A, const int *__restrict__ rows,
     for (int q = blockIdx.x * NT + threadIdx.x; q < nrows_c; q += stride) {
         int row = rows[q];
         V acc = A.template dot<V>(t, row);
-        t[row] = dr[row] * (d[row] - acc);
+        // t_i += w/a_ii (d_i - (A t)_i): the forward sweep starts from t = 0,
+        // the backward sweep of the symmetric smoother updates its result
+        t[row] = t[row] + dr[row] * (d[row] - acc);
     }
 }
 
