@@ -51,6 +51,8 @@ extern "C" {
 #define UG4GB_SMOOTHER_MCGS 1       /* multicolour Gauss-Seidel (opt-in; no ugcore counterpart) */
 #define UG4GB_SMOOTHER_MCSGS 2      /* symmetric multicolour Gauss-Seidel: forward colour sweep, then
                                        backward (SymmetricGaussSeidel, gauss_seidel.h:350, in colour order) */
+#define UG4GB_SMOOTHER_ILU 3        /* ILU(0) in multicolour order (ILU, ilu.h:109-290, of the colour-
+                                       permuted operator); damp scales the correction */
 #define UG4GB_PREC_FP64 0           /* whole preconditioner in FP64 */
 #define UG4GB_PREC_MIXED 1          /* FP32 smoother/transfers/SpMV, FP64 outer Krylov and base LU */
 #define UG4GB_SOLVER_CG 0           /* lib_algebra/operator/linear_solver/cg.h:59 */

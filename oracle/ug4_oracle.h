@@ -138,15 +138,17 @@ void orc_lu_apply(const orc_lu *F, double *x, const double *b);
 void orc_lu_free(orc_lu *F);
 
 /* GMG */
-enum { ORC_SMOOTH_JACOBI = 0, ORC_SMOOTH_MCGS = 1, ORC_SMOOTH_MCSGS = 2 };
+enum { ORC_SMOOTH_JACOBI = 0, ORC_SMOOTH_MCGS = 1, ORC_SMOOTH_MCSGS = 2, ORC_SMOOTH_ILU = 3 };
 typedef struct {
     int nlev, base, cycle, nu1, nu2, smoother;
     double damp;
     orc_crs *A;          /* per level */
     orc_crs *P, *R;      /* per level (index = fine level) */
     double **diaginv;
-    int **color;         /* multicolour GS: colour of each row */
+    int **color;         /* multicolour GS / ILU: colour of each row */
     int *ncolor;
+    orc_crs *ilu;        /* ILU: rows ordered by (colour, column), L and U values */
+    int **ilu_diag;      /* ILU: position of the diagonal in each row */
     double **sc, **sd, **st;
     orc_lu lu;
     orc_crs *Arap;       /* rap: owned level operators (coarse levels), else NULL */

@@ -184,6 +184,86 @@ void orc_lu_free(orc_lu *F) { free(F->LU); free(F->piv); F->LU = NULL; F->piv = 
 /* ----------------------------------------------------------------- GMG -- */
 static double *dvec(int n) { return (double *)calloc((size_t)(n > 0 ? n : 1), sizeof(double)); }
 
+/* ILU(0) in multicolour order (ILU, lib_algebra/operator/preconditioner/
+   ilu.h:109-210, of the colour-permuted operator): rows re-ordered by
+   (colour, column), IKJ elimination on A's pattern, colour by colour in
+   increasing order (rows of one colour are not coupled) */
+static long long ilu_key(const int *color, int n, int j) { return (long long)color[j] * n + j; }
+
+static int ilu_factor(const orc_crs *A, const int *color, int ncolor, orc_crs *F, int **diag_out)
+{
+    const int n = A->n_rows;
+    F->n_rows = F->n_cols = n;
+    F->nnz = A->nnz;
+    F->rowptr = (int *)malloc(sizeof(int) * (size_t)(n + 1));
+    F->col = (int *)malloc(sizeof(int) * (size_t)(A->nnz > 0 ? A->nnz : 1));
+    F->val = (double *)malloc(sizeof(double) * (size_t)(A->nnz > 0 ? A->nnz : 1));
+    int *dg = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    if (!F->rowptr || !F->col || !F->val || !dg) return -1;
+    memcpy(F->rowptr, A->rowptr, sizeof(int) * (size_t)(n + 1));
+    memcpy(F->col, A->col, sizeof(int) * (size_t)A->nnz);
+    memcpy(F->val, A->val, sizeof(double) * (size_t)A->nnz);
+    for (int r = 0; r < n; ++r) {
+        const int a0 = F->rowptr[r], a1 = F->rowptr[r + 1];
+        for (int a = a0 + 1; a < a1; ++a) {          /* insertion sort by key */
+            const int cc = F->col[a];
+            const double vv = F->val[a];
+            const long long kk = ilu_key(color, n, cc);
+            int b = a - 1;
+            while (b >= a0 && ilu_key(color, n, F->col[b]) > kk) {
+                F->col[b + 1] = F->col[b]; F->val[b + 1] = F->val[b]; --b;
+            }
+            F->col[b + 1] = cc; F->val[b + 1] = vv;
+        }
+        int lo = 0;
+        for (int a = a0; a < a1; ++a) lo += ilu_key(color, n, F->col[a]) < ilu_key(color, n, r);
+        dg[r] = a0 + lo;
+    }
+    for (int c = 0; c < ncolor; ++c)
+        for (int i = 0; i < n; ++i) {
+            if (color[i] != c) continue;
+            const int a1 = F->rowptr[i + 1];
+            for (int p = F->rowptr[i]; p < dg[i]; ++p) {
+                const int k = F->col[p];
+                const double ukk = F->val[dg[k]];
+                if (ukk == 0.0) return -2;
+                const double l = F->val[p] / ukk;
+                F->val[p] = l;
+                for (int s = p + 1; s < a1; ++s) {
+                    const long long js = ilu_key(color, n, F->col[s]);
+                    for (int q = dg[k] + 1; q < F->rowptr[k + 1]; ++q)
+                        if (ilu_key(color, n, F->col[q]) == js) { F->val[s] -= l * F->val[q]; break; }
+                }
+            }
+            if (F->val[dg[i]] == 0.0) return -2;
+        }
+    *diag_out = dg;
+    return 0;
+}
+
+/* c = damp (L U)^{-1} d: forward over the colours, then backward */
+static void ilu_apply(const orc_crs *F, const int *dg, const int *color, int ncolor, double damp, double *c,
+                      const double *d, double *y)
+{
+    const int n = F->n_rows;
+    for (int col = 0; col < ncolor; ++col)
+        for (int i = 0; i < n; ++i) {
+            if (color[i] != col) continue;
+            double s = d[i];
+            for (int a = F->rowptr[i]; a < dg[i]; ++a) s -= F->val[a] * y[F->col[a]];
+            y[i] = s;
+        }
+    for (int col = ncolor - 1; col >= 0; --col)
+        for (int i = 0; i < n; ++i) {
+            if (color[i] != col) continue;
+            double s = y[i];
+            for (int a = dg[i] + 1; a < F->rowptr[i + 1]; ++a) s -= F->val[a] * c[F->col[a]];
+            c[i] = s * (1.0 / F->val[dg[i]]);
+        }
+    if (damp != 1.0)
+        for (int i = 0; i < n; ++i) c[i] *= damp;
+}
+
 int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, double damp,
                  int nu1, int nu2, int cycle, int base, int rap)
 {
@@ -235,6 +315,12 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
                         G->color[l][i + L->nx * (j + L->ny * k)] = (i & 1) | ((j & 1) << 1) | ((k & 1) << 2);
         }
     }
+    if (G->smoother == ORC_SMOOTH_ILU) {
+        G->ilu = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
+        G->ilu_diag = (int **)calloc((size_t)G->nlev, sizeof(int *));
+        for (int l = base + 1; l < G->nlev; ++l)
+            if (ilu_factor(&levA[l], G->color[l], G->ncolor[l], &G->ilu[l], &G->ilu_diag[l])) return -3;
+    }
     if (orc_lu_init(&G->lu, &levA[base])) return -2;
     return 0;
 }
@@ -280,6 +366,12 @@ static void smooth(orc_gmg *G, int l, double *c, const double *d)
         const double *di = G->diaginv[l];
         for (int i = 0; i < n; ++i) c[i] = di[i] * d[i];
     } else {
+        if (G->smoother == ORC_SMOOTH_ILU) {
+            double *y = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+            ilu_apply(&G->ilu[l], G->ilu_diag[l], G->color[l], G->ncolor[l], G->damp, c, d, y);
+            free(y);
+            return;
+        }
         mcgs_apply(&G->A[l], G->color[l], G->ncolor[l], G->damp, c, d);
         if (G->smoother == ORC_SMOOTH_MCSGS) mcgs_backward(&G->A[l], G->color[l], G->ncolor[l], G->damp, c, d);
     }
@@ -347,6 +439,10 @@ void orc_gmg_free(orc_gmg *G)
         if (G->diaginv) free(G->diaginv[l]);
         if (G->color) free(G->color[l]);
         if (G->sc) { free(G->sc[l]); free(G->sd[l]); free(G->st[l]); }
+    }
+    if (G->ilu) {
+        for (int l = 0; l < G->nlev; ++l) { orc_crs_free(&G->ilu[l]); free(G->ilu_diag[l]); }
+        free(G->ilu); free(G->ilu_diag);
     }
     free(G->P); free(G->R); free(G->diaginv); free(G->color); free(G->ncolor);
     free(G->sc); free(G->sd); free(G->st);

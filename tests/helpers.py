@@ -24,7 +24,7 @@ def oracle_params(orc, cfg):
         elem_type=et, mx=cfg["mx"], my=cfg["my"], mz=cfg["mz"], nref=cfg["nref"], seed=cfg["seed"], coef_kind=ck,
         coef_modes=cfg["coef_modes"], coef_kmax=cfg["coef_kmax"], vel_kind=1 if cfg["vel"] else 0,
         vel_modes=cfg["vel_modes"], vel_kmax=cfg["vel_kmax"], diffusion=cfg["diffusion"], peclet=cfg["peclet"],
-        solver=0 if cfg["solver"] == "cg" else 1, smoother={"jacobi": 0, "mcgs": 1, "mcsgs": 2}[cfg["smoother"]],
+        solver=0 if cfg["solver"] == "cg" else 1, smoother={"jacobi": 0, "mcgs": 1, "mcsgs": 2, "ilu": 3}[cfg["smoother"]],
         damp=cfg["damp"], nu1=cfg["nu1"], nu2=cfg["nu2"], cycle=cfg["cycle"], base=cfg["base"], maxit=cfg["maxit"],
         rel_red=cfg["rel_red"], min_defect=cfg["min_defect"], rap=int(cfg.get("rap", 0)))
 

@@ -129,13 +129,15 @@ def test_variable_coefficient_tets_full_size_against_fp64_oracle(ctx, oracle_lib
     assert abs(st["steps"] - ref["steps"]) <= 3
 
 
-@pytest.mark.parametrize("name,smoother", [("c1", "mcgs"), ("c1", "mcsgs"), ("c0", "mcsgs"), ("c4", "mcsgs")])
+@pytest.mark.parametrize("name,smoother", [("c1", "mcgs"), ("c1", "mcsgs"), ("c0", "mcsgs"), ("c4", "mcsgs"),
+                                           ("c1", "ilu"), ("c0", "ilu"), ("c4", "ilu"), ("c2", "ilu")])
 def test_mcgs_smoother_matches_oracle(ctx, oracle_lib, name, smoother):
-    """multicolour Gauss-Seidel and its symmetric variant (forward, then
-    backward colour sweep): GMG application 1e-12, solve iterations +-1"""
+    """multicolour Gauss-Seidel, its symmetric variant (forward, then
+    backward colour sweep) and multicolour ILU(0): GMG application 1e-12,
+    solve iterations +-1"""
     import ugcore_gb300 as ug
     over = dict(nref=3 if name != "c0" else 5, smoother=smoother, damp=1.0, precision="fp64")
-    if name == "c4":
+    if name in ("c4", "c2"):
         over["nref"] = 2
     cfg, p = _problem(ctx, name, over)
     op = _oracle(oracle_lib, cfg, p)
@@ -266,3 +268,16 @@ def test_error_reporting(ctx):
     with pytest.raises(ug.UG4GBError) as ei:
         g.apply(c, p.b)
     assert ei.value.code == -7
+
+
+@pytest.mark.parametrize("smoother", ["mcsgs", "ilu"])
+def test_smoothers_in_mixed_precision(ctx, smoother):
+    """FP32 multigrid with the symmetric Gauss-Seidel / ILU smoother inside
+    FP64 CG: relative residual < 1e-10, solution within 1e-7 of FP64"""
+    cfg64, p64 = _problem(ctx, "c1", dict(nref=4, smoother=smoother, damp=1.0, precision="fp64"))
+    cfg32, p32 = _problem(ctx, "c1", dict(nref=4, smoother=smoother, damp=1.0, precision="mixed"))
+    s64, s32 = p64.solve(), p32.solve()
+    assert s32["converged"] and s32["defect"] / s32["initial_defect"] < 1e-10
+    assert abs(s32["steps"] - s64["steps"]) <= 2
+    x64 = p64.x.numpy()
+    assert np.abs(p32.x.numpy() - x64).max() <= 1e-7 * np.abs(x64).max()

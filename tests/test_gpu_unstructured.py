@@ -42,7 +42,8 @@ def _setup(ctx, orc, name, dirichlet, nref, coef, precision="fp64", smoother="ja
     b = ug.GPUVector(ctx, hier.num_vertices())
     disc.assemble_linear(A, b)
     gmg = ug.GeometricMultiGrid(disc)
-    gmg.set_smoother(ug.Jacobi(0.6) if smoother == "jacobi" else ug.GaussSeidel(1.0))
+    gmg.set_smoother({"jacobi": lambda: ug.Jacobi(0.6), "mcgs": lambda: ug.GaussSeidel(1.0),
+                      "mcsgs": lambda: ug.SymmetricGaussSeidel(1.0), "ilu": lambda: ug.ILU(1.0)}[smoother]())
     gmg.set_num_presmooth(2)
     gmg.set_num_postsmooth(2)
     gmg.set_base_level(0)
@@ -97,10 +98,12 @@ def test_unstructured_gmg_and_solve(ctx, oracle_lib, name, dirichlet, nref, coef
     assert np.abs(x.numpy() - rs["x"]).max() <= 1e-8 * np.abs(rs["x"]).max()
 
 
-@pytest.mark.parametrize("precision,smoother", [("mixed", "jacobi"), ("fp64", "mcgs")])
+@pytest.mark.parametrize("precision,smoother", [("mixed", "jacobi"), ("fp64", "mcgs"), ("fp64", "mcsgs"),
+                                               ("fp64", "ilu"), ("mixed", "ilu")])
 def test_unstructured_variants_converge(ctx, oracle_lib, precision, smoother):
-    """mixed precision and the multicolour Gauss-Seidel (greedy vertex
-    colours) on the tetrahedral hierarchy: the FP64 residual reaches 1e-10"""
+    """mixed precision, the multicolour Gauss-Seidel variants and ILU(0)
+    (greedy vertex colours) on the tetrahedral hierarchy: the FP64 residual
+    reaches 1e-10"""
     import ugcore_gb300 as ug
     hier, disc, A, b, gmg, op = _setup(ctx, oracle_lib, "cube_tets", "Bottom", 3, "lognormal", precision, smoother)
     solver = ug.CG(ctx)

@@ -215,6 +215,22 @@ def test_mcgs_oracle_converges(oracle_lib):
     assert s["converged"] and s["steps"] < 10
 
 
+def test_ilu_smoother_oracle(oracle_lib):
+    """multicolour ILU(0) smoother: the multigrid converges (Poisson CG) and
+    needs no more BiCGStab steps than damped Jacobi on convection-diffusion"""
+    o = oracle_lib
+    P = o.Problem(o.make_params(elem_type=o.ORC_HEX, mx=2, my=2, mz=2, nref=3, smoother=3, damp=1.0))
+    s = P.solve()
+    assert s["converged"] and s["steps"] < 12
+    C = o.Problem(o.make_params(elem_type=o.ORC_HEX, mx=3, my=3, mz=3, nref=2, smoother=3, damp=1.0, solver=1,
+                                vel_kind=1, diffusion=1e-2, coef_kind=3))
+    J = o.Problem(o.make_params(elem_type=o.ORC_HEX, mx=3, my=3, mz=3, nref=2, smoother=0, damp=0.6, solver=1,
+                                vel_kind=1, diffusion=1e-2, coef_kind=3))
+    sc, sj = C.solve(), J.solve()
+    assert sc["converged"] and sj["converged"]
+    assert sc["steps"] <= sj["steps"]
+
+
 def test_symmetric_mcgs_is_symmetric_and_converges(oracle_lib):
     """the symmetric multicolour Gauss-Seidel smoother gives a symmetric
     multigrid preconditioner on a symmetric operator (M d1 . d2 = d1 . M d2

@@ -12,7 +12,7 @@ LIB_PATH = os.path.join(HERE, "libug4gb.so")
 OK = 0
 ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_SINGULAR, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_STATE = -1, -2, -3, -4, -5, -6, -7
 QUAD, HEX, TET, TRI = 0, 1, 2, 3
-SMOOTHER_JACOBI, SMOOTHER_MCGS, SMOOTHER_MCSGS = 0, 1, 2
+SMOOTHER_JACOBI, SMOOTHER_MCGS, SMOOTHER_MCSGS, SMOOTHER_ILU = 0, 1, 2, 3
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_CG, SOLVER_BICGSTAB = 0, 1
 UPWIND_NONE, UPWIND_FULL = 0, 1

@@ -494,6 +494,14 @@ class GaussSeidel:
         self.kind, self.damp = _lib.SMOOTHER_MCGS, float(relax)
 
 
+class ILU:
+    """ILU(0) smoother in multicolour order (GPU variant of ILU, ilu.h);
+    damp scales the correction"""
+
+    def __init__(self, damp=1.0):
+        self.kind, self.damp = _lib.SMOOTHER_ILU, float(damp)
+
+
 class SymmetricGaussSeidel:
     """symmetric multicolour Gauss-Seidel: forward, then backward colour sweep
     (GPU variant of SymmetricGaussSeidel, gauss_seidel.h:350)"""

@@ -164,6 +164,7 @@ template <class V>
 struct GmgT : GmgBase {
     std::vector<GLevel<V>> lev;
     int base = 0, nu1 = 2, nu2 = 2, cycle = 1, smoother = 0;
+    double damp = 1.0;
     DevBuf<double> Ainv;
     DevBuf<double> z64;          // mixed precision: FP64 copy of the top correction
     int nbase = 0;
@@ -211,6 +212,10 @@ struct GmgT : GmgBase {
                 UG_LAUNCH(c, k_colour_rows, div_up(n, 256), 256, 0, G.color.p, n, q, L.crow[q].p, cnt.p);
                 UG_CUDA(cudaMemcpyAsync(&L.ncrow[q], cnt.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
                 UG_CUDA(cudaStreamSynchronize(c.stream));
+            }
+            if (smoother == UG4GB_SMOOTHER_ILU) {
+                ilu_setup<V>(c, L.A, G.color.p, L.crow, L.ncrow, L.ilu);
+                L.y.alloc(n);
             }
         }
         UG_CUDA(cudaStreamSynchronize(c.stream));
@@ -388,6 +393,10 @@ struct GmgT : GmgBase {
     // then sweeps the colours in decreasing order
     void gs_sweep(Ctx &c, GLevel<V> &L, const V *dv, const int *skip)
     {
+        if (smoother == UG4GB_SMOOTHER_ILU) {
+            ilu_apply<V>(c, L.ilu, L.crow, L.ncrow, dv, L.y.p, L.t.p, damp, skip);
+            return;
+        }
         UG_LAUNCH_PDL(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.t.p, skip);
         for (size_t q = 0; q < L.crow.size(); ++q)
             if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], L.dinv.p, dv, L.t.p, skip);
@@ -424,6 +433,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
     G->nu2 = m->nu2;
     G->cycle = m->cycle;
     G->smoother = m->smoother;
+    G->damp = m->damp;
     G->lev.resize(nl);
     UG_REQUIRE(m->base >= 0 && m->base < nl, UG4GB_ERR_INVALID, "GMG: base level out of range");
     UG_REQUIRE(A_top->A.nrows == g->lev[nl - 1].nv, UG4GB_ERR_INVALID, "GMG: top operator size != top level");
@@ -524,8 +534,7 @@ int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out)
 
 int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp)
 {
-    if (!m || (kind != UG4GB_SMOOTHER_JACOBI && kind != UG4GB_SMOOTHER_MCGS && kind != UG4GB_SMOOTHER_MCSGS) ||
-        !(damp > 0.0))
+    if (!m || kind < UG4GB_SMOOTHER_JACOBI || kind > UG4GB_SMOOTHER_ILU || !(damp > 0.0))
         return UG4GB_ERR_INVALID;
     m->smoother = kind;
     m->damp = damp;

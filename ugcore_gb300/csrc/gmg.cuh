@@ -84,8 +84,10 @@ struct GLevel {
     GridPair gp{};
     DevBuf<V> sc, dA, dB, w, t;
     V *dcur = nullptr;
-    std::vector<DevBuf<int>> crow;   // MCGS colour row lists
+    std::vector<DevBuf<int>> crow;   // MCGS / ILU colour row lists
     std::vector<int> ncrow;
+    IluFactors<V> ilu;               // ILU smoother factors
+    DevBuf<V> y;                     // ILU forward-substitution scratch
 };
 
 struct GmgBase {

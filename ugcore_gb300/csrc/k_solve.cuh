@@ -158,6 +158,24 @@ template <class V, class DT>
 void residual_update(Ctx &c, const OpMat<V> &A, const V *t, const DT *dbase, V *dout, V *sc, int sc_mode,
                      const int *skip);
 
+// ILU(0) in multicolour order (k_ilu.cu): level CRS rows re-ordered by
+// (colour, column), L multipliers before the diagonal, U from the diagonal on
+template <class V>
+struct IluFactors {
+    int n = 0;
+    DevBuf<int> rowptr, col, nlow;   // nlow[i]: position of the diagonal in row i
+    DevBuf<V> val, uinv;
+};
+// factorise the level operator A (FP64) with the vertex colours `color` and the
+// rows of each colour; throws UG4GB_ERR_SINGULAR on a zero pivot
+template <class V>
+void ilu_setup(Ctx &c, const Csr &A, const int *color, const std::vector<DevBuf<int>> &crow,
+               const std::vector<int> &ncrow, IluFactors<V> &F);
+// t = damp (L U)^{-1} d (y: scratch of the forward substitution)
+template <class V>
+void ilu_apply(Ctx &c, const IluFactors<V> &F, const std::vector<DevBuf<int>> &crow, const std::vector<int> &ncrow,
+               const V *d, V *y, V *t, double damp, const int *skip);
+
 // ---- Krylov kernels (FP64 outer vectors; z may be FP32 in mixed mode) ----
 // r -= A x, |r| starts the check; optionally r32 = (float) r
 void krylov_start(Ctx &c, const OpMat<double> &A, const double *x, double *r, RedArgs red, float *r32 = nullptr);

@@ -23,7 +23,8 @@ import numpy as np
 
 from . import fields
 from .algebra import (BiCGStab, CG, DomainDiscretization, GaussSeidel, GeometricMultiGrid, GPUSparseMatrix,
-                      GPUVector, Jacobi, StdConvCheck, StructuredHierarchy, SymmetricGaussSeidel, ThetaTimeStep)
+                      GPUVector, ILU, Jacobi, StdConvCheck, StructuredHierarchy, SymmetricGaussSeidel,
+                      ThetaTimeStep)
 
 BASE = dict(elem="quad", mx=2, my=2, mz=1, nref=6, seed=1, coef="const", diffusion=1.0, coef_modes=64,
             coef_kmax=8.0, vel=None, vel_modes=16, vel_kmax=2.0, peclet=10.0, solver="cg", smoother="jacobi",
@@ -98,7 +99,8 @@ class Problem:
     def _make_gmg(self, transposed):
         c = self.cfg
         g = GeometricMultiGrid(self.disc)
-        g.set_smoother({"jacobi": Jacobi, "mcgs": GaussSeidel, "mcsgs": SymmetricGaussSeidel}[c["smoother"]](c["damp"]))
+        g.set_smoother({"jacobi": Jacobi, "mcgs": GaussSeidel, "mcsgs": SymmetricGaussSeidel,
+                        "ilu": ILU}[c["smoother"]](c["damp"]))
         g.set_cycle_type(c["cycle"])
         g.set_num_presmooth(c["nu1"])
         g.set_num_postsmooth(c["nu2"])
