@@ -9,7 +9,7 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 # Tolerances stated by the benchmark spec for this path:
 #   CRS row pointers / column indices: bit-exact
 #   matrix values: 1e-13 relative in FP64 (relative to the largest |a_ij| of
-#     the row, so that entries that cancel to ~0 are judged against the row)
+#     the row, so that entries that cancel to ~0 are measured against the row)
 #   solution: 1e-10 relative residual, iteration count within +-1
 VAL_RTOL = 1e-13
 
