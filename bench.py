@@ -284,13 +284,14 @@ def run_ours(args, rank, world, local_rank):
                  "kernel_profile": profile_summary(prof_m)}
         del pm
 
-    target = adj = conv = rap = unstr = None
+    target = adj = conv = rap = unstr = smoothers = None
     if not args.no_extras:
         target = run_target(args, ctx, timed, world, hbm)
         adj = run_adjoint_grad(args, ctx, timed)
         conv = run_convection_adjoint(args, ctx, timed, world, hbm)
         rap = run_galerkin(args, ctx, timed, world)
         unstr = run_unstructured(args, ctx, timed, world, hbm)
+        smoothers = run_smoothers(args, ctx, timed, world)
 
     # ---- assembly throughput (top level, FP64 FV1 + CRS values + rhs)
     asm = None
@@ -335,6 +336,7 @@ def run_ours(args, rank, world, local_rank):
         "convection_adjoint": conv,
         "galerkin_coarse_operators": rap,
         "unstructured_tets": unstr,
+        "smoothers_convection": smoothers,
         "assembly": asm,
         "clocks": clocks,
         "cpu_baseline": cpu,
@@ -452,6 +454,26 @@ def run_convection_adjoint(args, ctx, timed, world, hbm):
         out["dofs"], out["nnz"] = p.n, sizes[-1]["nnz"]
         del p
     out["mixed_speedup_vs_fp64"] = out["fp64"]["ms_per_solve"] / out["mixed"]["ms_per_solve"]
+    return out
+
+
+def run_smoothers(args, ctx, timed, world):
+    """the smoothers on the 193^3 convection-diffusion problem (mixed
+    precision, BiCGStab to 1e-10): damped Jacobi, multicolour Gauss-Seidel,
+    its symmetric variant and multicolour ILU(0), time per solve and half
+    steps"""
+    from ugcore_gb300 import problems
+    out = {"workload": "3D convection-diffusion 193^3 hexes (7.19M DoFs), GMG V(2,2) mixed precision, "
+                       "BiCGStab to 1e-10, by smoother"}
+    for sm, damp in (("jacobi", 0.6), ("mcgs", 1.0), ("mcsgs", 1.0), ("ilu", 1.0)):
+        p = problems.Problem(ctx, problems.config("c4", precision="mixed", smoother=sm, damp=damp))
+        for _ in range(min(args.warmup, 2)):
+            p.solve()
+        ms = max_over_ranks(timed(p.solve, max(2, args.steps // 3)), world)
+        st = p.solve()
+        out[sm] = {"ms_per_solve": ms, "bicgstab_half_steps": st["steps"],
+                   "rel_residual": st["defect"] / st["initial_defect"]}
+        del p
     return out
 
 

@@ -95,11 +95,17 @@ __global__ void k_dirichlet_identity(const unsigned char *bnd, int n, const int 
     for (int a = rowptr[v]; a < rowptr[v + 1]; ++a) val[a] = (col[a] == v) ? 1.0 : 0.0;
 }
 
-__global__ void k_colour_rows(const int *color, int n, int c, int *rows, int *count)
+// rows of colour c in increasing order (stable compaction by a scan of the flags)
+__global__ void k_colour_flag(const int *color, int n, int c, int *flag)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || color[i] != c) return;
-    rows[atomicAdd(count, 1)] = i;
+    if (i < n) flag[i] = (color[i] == c) ? 1 : 0;
+}
+
+__global__ void k_colour_scatter(const int *color, int n, int c, const int *pos, int *rows)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && color[i] == c) rows[pos[i]] = i;
 }
 
 template <class V>
@@ -204,15 +210,19 @@ struct GmgT : GmgBase {
             int ncol = G.ncolors;
             L.crow.resize(ncol);
             L.ncrow.assign(ncol, 0);
-            DevBuf<int> cnt;
-            cnt.alloc(1);
+            DevBuf<int> flag, pos;
+            flag.alloc(n + 1);
+            pos.alloc(n + 1);
             for (int q = 0; q < ncol; ++q) {
                 L.crow[q].alloc(n);
-                UG_CUDA(cudaMemsetAsync(cnt.p, 0, sizeof(int), c.stream));
-                UG_LAUNCH(c, k_colour_rows, div_up(n, 256), 256, 0, G.color.p, n, q, L.crow[q].p, cnt.p);
-                UG_CUDA(cudaMemcpyAsync(&L.ncrow[q], cnt.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-                UG_CUDA(cudaStreamSynchronize(c.stream));
+                UG_CUDA(cudaMemsetAsync(flag.p + n, 0, sizeof(int), c.stream));
+                UG_LAUNCH(c, k_colour_flag, div_up(n, 256), 256, 0, G.color.p, n, q, flag.p);
+                int64_t cnt = 0;
+                exclusive_scan_int(c, flag.p, pos.p, n + 1, &cnt);
+                UG_LAUNCH(c, k_colour_scatter, div_up(n, 256), 256, 0, G.color.p, n, q, pos.p, L.crow[q].p);
+                L.ncrow[q] = (int)cnt;
             }
+            UG_CUDA(cudaStreamSynchronize(c.stream));
             if (smoother == UG4GB_SMOOTHER_ILU) {
                 ilu_setup<V>(c, L.A, G.color.p, L.crow, L.ncrow, L.ilu);
                 L.y.alloc(n);

@@ -41,7 +41,9 @@ class _UgxProblem:
         self.b = ug.GPUVector(ctx, self.n)
         self.disc.assemble_linear(self.A, self.b)
         self.gmg = ug.GeometricMultiGrid(self.disc)
-        self.gmg.set_smoother(ug.Jacobi(0.6) if args.smoother != "mcgs" else ug.GaussSeidel(1.0))
+        self.gmg.set_smoother({None: lambda: ug.Jacobi(0.6), "jacobi": lambda: ug.Jacobi(0.6),
+                               "mcgs": lambda: ug.GaussSeidel(1.0), "mcsgs": lambda: ug.SymmetricGaussSeidel(1.0),
+                               "ilu": lambda: ug.ILU(1.0)}[args.smoother]())
         self.gmg.set_precision(args.precision or "fp64")
         self.gmg.init(self.A)
         self.solver = ug.CG(ctx)
@@ -65,7 +67,7 @@ def main():
     ap.add_argument("--config", default="c1")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default=None)
     ap.add_argument("--nref", type=int, default=None)
-    ap.add_argument("--smoother", choices=["jacobi", "mcgs"], default=None)
+    ap.add_argument("--smoother", choices=["jacobi", "mcgs", "mcsgs", "ilu"], default=None)
     ap.add_argument("--format", choices=["auto", "sell"], default="auto")
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--direct", action="store_true")
@@ -84,6 +86,7 @@ def main():
         over["nref"] = args.nref
     if args.smoother:
         over["smoother"] = args.smoother
+        over["damp"] = 0.6 if args.smoother == "jacobi" else 1.0
     ctx = ug.Context(0)
     ctx.set_operator_format(args.format)
     ctx.set_tuning(sweep_fusion=args.sweep_fusion, sweep_planes=args.sweep_planes)
