@@ -165,3 +165,89 @@ def test_unstructured_matches_structured_on_the_same_mesh(ctx):
     rps, cis, vas = p.A.export_csr()
     As = sp.csr_matrix((vas, cis, rps)).toarray()
     assert np.abs(Au - As[np.ix_(perm, perm)]).max() <= 1e-13 * np.abs(As).max()
+
+
+def _levels(hier):
+    out = []
+    for l in range(hier.num_levels):
+        x, e, bnd = hier.export(l)
+        npar, par = hier.parents(l) if l > 0 else (None, None)
+        out.append((x, e, bnd, npar, par))
+    return out
+
+
+def _oracle_for(orc, hier, seed=3, **kw):
+    et = {0: orc.ORC_QUAD, 1: orc.ORC_HEX, 2: orc.ORC_TET, 3: orc.ORC_TRI}[hier.elem_type]
+    params = orc.make_params(elem_type=et, seed=seed, coef_kind=1, coef_modes=64, coef_kmax=8.0, solver=0,
+                             smoother=0, damp=0.6, nu1=2, nu2=2, cycle=1, base=0, maxit=200, rel_red=1e-10,
+                             min_defect=1e-300, **kw)
+    return orc.Problem(params, levels=_levels(hier))
+
+
+@pytest.mark.parametrize("name,dirichlet", [("cube_tets", "Bottom"), ("square_tris", "Dirichlet")])
+def test_unstructured_galerkin_coarse_operators(ctx, oracle_lib, name, dirichlet):
+    """set_rap on an unstructured hierarchy: R A P per level against the
+    oracle's restated AddMultiplyOf on the same levels, and the solve"""
+    import ugcore_gb300 as ug
+    hier, disc, A, b, _, _ = _setup(ctx, oracle_lib, name, dirichlet, 3, "lognormal")
+    gmg = ug.GeometricMultiGrid(disc)
+    gmg.set_smoother(ug.Jacobi(0.6))
+    gmg.set_precision("fp64")
+    gmg.set_rap(True)
+    gmg.init(A)
+    op = _oracle_for(oracle_lib, hier, rap=1)
+    for l in range(hier.num_levels):
+        assert_crs_equal(gmg.level_matrix(l), op.gmg_level_matrix(l), what="R A P level %d" % l)
+    solver = ug.CG(ctx)
+    solver.set_preconditioner(gmg)
+    solver.set_convergence_check(ug.StdConvCheck(200, 1e-300, 1e-10))
+    solver.init(A)
+    x = ug.GPUVector(ctx, hier.num_vertices())
+    assert solver.apply(x, b)
+    rs = op.solve()
+    assert abs(solver.stats()["steps"] - rs["steps"]) <= 1
+    assert np.abs(x.numpy() - rs["x"]).max() <= 1e-8 * np.abs(rs["x"]).max()
+
+
+def test_unstructured_adjoint_solve(ctx, oracle_lib):
+    """transposed operator (Dirichlet rows reset) and transposed multigrid on
+    the tetrahedral hierarchy against the oracle's adjoint solve"""
+    import ugcore_gb300 as ug
+    hier, disc, A, b, _, _ = _setup(ctx, oracle_lib, "cube_tets", "Bottom", 3, "lognormal")
+    AT = disc.adjoint_operator(A, ug.GPUSparseMatrix(ctx))
+    gmg = ug.GeometricMultiGrid(disc)
+    gmg.set_smoother(ug.Jacobi(0.6))
+    gmg.set_precision("fp64")
+    gmg.set_transposed(True)
+    gmg.init(AT)
+    solver = ug.CG(ctx)
+    solver.set_preconditioner(gmg)
+    solver.set_convergence_check(ug.StdConvCheck(200, 1e-300, 1e-10))
+    solver.init(AT)
+    n = hier.num_vertices()
+    g = np.random.default_rng(4).standard_normal(n)
+    bnd = hier.export()[2].astype(bool)
+    rhs = ug.GPUVector(ctx, n).copy_from(np.where(bnd, 0.0, g))
+    lam = ug.GPUVector(ctx, n)
+    assert solver.apply(lam, rhs)
+    ref = _oracle_for(oracle_lib, hier).adjoint(g)
+    assert abs(solver.stats()["steps"] - ref["steps"]) <= 1
+    assert np.abs(lam.numpy() - ref["lam"]).max() <= 1e-8 * np.abs(ref["lam"]).max()
+
+
+@pytest.mark.parametrize("theta", [1.0, 0.5])
+def test_unstructured_theta_step(ctx, oracle_lib, theta):
+    """time-discrete system of one theta step on the triangle hierarchy"""
+    import ugcore_gb300 as ug
+    hier, disc, A, b, _, _ = _setup(ctx, oracle_lib, "square_tris", "Dirichlet", 3, "lognormal")
+    n = hier.num_vertices()
+    u_old = np.random.default_rng(2).standard_normal(n)
+    u_old[hier.export()[2].astype(bool)] = 0.0
+    td = ug.ThetaTimeStep(disc, theta)
+    td.prepare_step(ug.GPUVector(ctx, n).copy_from(u_old), 0.0, 0.01)
+    At = ug.GPUSparseMatrix(ctx)
+    bt = ug.GPUVector(ctx, n)
+    td.assemble_linear(At, bt)
+    (rp, ci, va), ob = _oracle_for(oracle_lib, hier).theta_system(theta, 0.01, u_old)
+    assert_crs_equal(At.export_csr(), (rp, ci, va), what="M + theta dt A")
+    assert np.abs(bt.numpy() - ob).max() <= 1e-13 * np.abs(ob).max()
