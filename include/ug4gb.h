@@ -174,6 +174,11 @@ UG4GB_API int ug4gb_vector_dot(const ug4gb_vector *a, const ug4gb_vector *b, dou
 UG4GB_API int ug4gb_vector_scale_add(ug4gb_vector *dest, double alpha, const ug4gb_vector *a, double beta,
                            const ug4gb_vector *b);
 UG4GB_API void ug4gb_vector_destroy(ug4gb_vector *v);
+/* Vector::maxnorm (vector_impl.h) and entry access from the host (indices and
+   values in host arrays; out-of-range indices are an error) */
+UG4GB_API int ug4gb_vector_maxnorm(const ug4gb_vector *v, double *out);
+UG4GB_API int ug4gb_vector_get_values(const ug4gb_vector *v, int n, const int *idx, double *vals);
+UG4GB_API int ug4gb_vector_set_values(ug4gb_vector *v, int n, const int *idx, const double *vals);
 /* (a, b) of two FP64 device arrays of the current device, for callers that
    may not allocate device memory (no context needed; nothing is allocated,
    not even on first use).  Has no counterpart in the reference.  The result
@@ -205,6 +210,23 @@ UG4GB_API int ug4gb_matrix_axpy_transposed(const ug4gb_matrix *A, ug4gb_vector *
    (sparsematrix_impl.h:149,186) */
 UG4GB_API int ug4gb_matrix_set_as_transpose_of(ug4gb_matrix *T, const ug4gb_matrix *B, int keep_zeros);
 UG4GB_API void ug4gb_matrix_destroy(ug4gb_matrix *A);
+/* the rest of the SparseMatrix interface ugcore's templates use (set-up and
+   glue, not the solve path): resize_and_clear (sparsematrix_impl.h:91; empty
+   rows), clear_retain_structure (:142; values 0), set_as_copy_of (:472;
+   this = scale * B), scale (:487), apply_ignore_zero_rows (:270-288; dest =
+   beta A w on rows with stored entries, others kept), row access (get_row:
+   returns the row length, copies up to capacity entries to host arrays) and
+   the scatter-add of element contributions into the existing pattern
+   (add_entries; host arrays; an entry outside the pattern is an error) */
+UG4GB_API int ug4gb_matrix_resize_and_clear(ug4gb_matrix *A, int num_rows, int num_cols);
+UG4GB_API int ug4gb_matrix_clear_retain_structure(ug4gb_matrix *A);
+UG4GB_API int ug4gb_matrix_set_as_copy_of(ug4gb_matrix *A, const ug4gb_matrix *B, double scale);
+UG4GB_API int ug4gb_matrix_scale(ug4gb_matrix *A, double alpha);
+UG4GB_API int ug4gb_matrix_apply_ignore_zero_rows(const ug4gb_matrix *A, ug4gb_vector *dest, double beta,
+                                                  const ug4gb_vector *w);
+UG4GB_API int ug4gb_matrix_get_row(const ug4gb_matrix *A, int row, int *cols, double *vals, int capacity);
+UG4GB_API int ug4gb_matrix_add_entries(ug4gb_matrix *A, int n, const int *rows, const int *cols,
+                                       const double *vals);
 
 /* ------------------------------------------------------ discretisation -- */
 /* Replaces DomainDiscretization (lib_disc/spatial_disc/domain_disc.h) with one

@@ -109,9 +109,10 @@ int main() {
 
 def test_ugcore_glue_instantiates_reference_solvers(tmp_path):
     """The ugcore-side GPU algebra (ugcore_gb300/adapters/ug4gb_algebra.h)
-    compiles against ugcore's own headers, and ugcore's CG and BiCGStab
-    templates instantiate with its vector type (where the ugcore tree is
-    present; four empty stand-ins replace headers that need Boost)."""
+    compiles against ugcore's own headers, and ugcore's CG, BiCGStab,
+    LinearSolver and MatrixOperator templates instantiate with its types
+    (where the ugcore tree is present; four empty stand-ins replace headers
+    that need Boost)."""
     ref = os.environ.get("UG4_REFERENCE", "/root/reference")
     if not os.path.isdir(os.path.join(ref, "ugbase", "lib_algebra")):
         pytest.skip("ugcore source tree not present")
@@ -129,9 +130,24 @@ def test_ugcore_glue_instantiates_reference_solvers(tmp_path):
 #include "lib_algebra/operator/interface/matrix_operator.h"
 #include "lib_algebra/operator/linear_solver/cg.h"
 #include "lib_algebra/operator/linear_solver/bicgstab.h"
+#include "lib_algebra/operator/linear_solver/linear_solver.h"
 template class ug::CG<ug::GPUAlgebra::vector_type>;
 template class ug::BiCGStab<ug::GPUAlgebra::vector_type>;
+template class ug::LinearSolver<ug::GPUAlgebra::vector_type>;
+template class ug::MatrixOperator<ug::GPUAlgebra::matrix_type, ug::GPUAlgebra::vector_type>;
 static_assert(ug::GPUAlgebra::blockSize == 1, "scalar algebra");
+// the rest of the matrix / vector interface the algebra templates call
+void use(ug::UG4GBSparseMatrix &A, const ug::UG4GBSparseMatrix &B, ug::UG4GBVector &v, const ug::UG4GBVector &w)
+{
+    A.resize_and_clear(4, 4);
+    A.set_as_copy_of(B, 2.0);
+    A.scale(0.5);
+    A.clear_retain_structure();
+    A.apply_ignore_zero_rows(v, 1.0, w);
+    double a = A(0, 1) + v.maxnorm() + w[2];
+    v.set_value(0, a);
+    A.add_entries({0}, {0}, {1.0});
+}
 int main() { return ug::GPUAlgebra::get_type().type() == ug::AlgebraType::GPU ? 0 : 1; }
 ''')
     r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-w", "-I" + str(shim), "-I" + os.path.join(ref, "ugbase"),

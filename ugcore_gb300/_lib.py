@@ -143,6 +143,16 @@ _SIGS = {
     "ug4gb_solver_destroy": (None, [P]),
     "ug4gb_disc_grad_logk": (I, [P, P, P, P]),
     "ug4gb_disc_grad_source": (I, [P, P, P]),
+    "ug4gb_matrix_resize_and_clear": (I, [P, I, I]),
+    "ug4gb_matrix_clear_retain_structure": (I, [P]),
+    "ug4gb_matrix_set_as_copy_of": (I, [P, P, D]),
+    "ug4gb_matrix_scale": (I, [P, D]),
+    "ug4gb_matrix_apply_ignore_zero_rows": (I, [P, P, D, P]),
+    "ug4gb_matrix_get_row": (I, [P, I, P, P, I]),
+    "ug4gb_matrix_add_entries": (I, [P, I, P, P, P]),
+    "ug4gb_vector_maxnorm": (I, [P, PD]),
+    "ug4gb_vector_get_values": (I, [P, I, P, P]),
+    "ug4gb_vector_set_values": (I, [P, I, P, P]),
     "ug4gb_io_write_mtx": (I, [I, I, P, P, P, C.c_char_p, C.c_char_p, C.c_char_p, I]),
     "ug4gb_io_read_mtx_info": (I, [C.c_char_p, PI, PI, PI64, C.c_char_p, I]),
     "ug4gb_io_read_mtx": (I, [C.c_char_p, P, P, P, C.c_char_p, I]),

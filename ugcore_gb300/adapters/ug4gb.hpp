@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstdint>
+#include <algorithm>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -123,6 +124,19 @@ public:
     {
         check(ug4gb_vector_scale_add(get(), a, x.get(), b, y.get()), ctx_, "vector scale_add");
     }
+    double maxnorm() const
+    {
+        double r = 0.0;
+        check(ug4gb_vector_maxnorm(get(), &r), ctx_, "vector maxnorm");
+        return r;
+    }
+    double get_value(int i) const
+    {
+        double v = 0.0;
+        check(ug4gb_vector_get_values(get(), 1, &i, &v), ctx_, "vector get");
+        return v;
+    }
+    void set_value(int i, double v) { check(ug4gb_vector_set_values(get(), 1, &i, &v), ctx_, "vector set value"); }
 
 private:
     ug4gb_ctx *ctx_;
@@ -161,6 +175,34 @@ public:
     void set_as_transpose_of(const Matrix &B, bool keep_zeros = true)
     {
         check(ug4gb_matrix_set_as_transpose_of(get(), B.get(), keep_zeros ? 1 : 0), ctx_, "transpose");
+    }
+    void resize_and_clear(int rows, int cols)
+    {
+        check(ug4gb_matrix_resize_and_clear(get(), rows, cols), ctx_, "resize_and_clear");
+    }
+    void clear_retain_structure() { check(ug4gb_matrix_clear_retain_structure(get()), ctx_, "clear values"); }
+    void set_as_copy_of(const Matrix &B, double scale = 1.0)
+    {
+        check(ug4gb_matrix_set_as_copy_of(get(), B.get(), scale), ctx_, "set_as_copy_of");
+    }
+    void scale(double a) { check(ug4gb_matrix_scale(get(), a), ctx_, "matrix scale"); }
+    void apply_ignore_zero_rows(Vector &dest, double beta, const Vector &w) const
+    {
+        check(ug4gb_matrix_apply_ignore_zero_rows(get(), dest.get(), beta, w.get()), ctx_, "apply_ignore_zero_rows");
+    }
+    // row r copied to the host
+    void row(int r, std::vector<int> &cols, std::vector<double> &vals) const
+    {
+        const int n = ug4gb_matrix_get_row(get(), r, nullptr, nullptr, 0);
+        if (n < 0) check(n, ctx_, "matrix row");
+        cols.resize(n);
+        vals.resize(n);
+        if (n > 0) check(std::min(0, ug4gb_matrix_get_row(get(), r, cols.data(), vals.data(), n)), ctx_, "matrix row");
+    }
+    void add_entries(const std::vector<int> &rows, const std::vector<int> &cols, const std::vector<double> &vals)
+    {
+        check(ug4gb_matrix_add_entries(get(), (int)rows.size(), rows.data(), cols.data(), vals.data()), ctx_,
+              "add_entries");
     }
 
 private:

@@ -95,12 +95,24 @@ public:
         ug4gb_glue::guarded([&] { r = m_v->dot(*o.m_v); }, "UG4GBVector::dotprod");
         return r;
     }
-    /// entries read through a host copy (for set-up and output code, not for solver loops)
+    /// max |v_i| (Vector::maxnorm)
+    double maxnorm() const
+    {
+        double r = 0;
+        ug4gb_glue::guarded([&] { r = m_v->maxnorm(); }, "UG4GBVector::maxnorm");
+        return r;
+    }
+    /// one entry read from the device (set-up and output code, not solver loops)
     double operator[](size_t i) const
     {
-        std::vector<double> h(size());
-        ug4gb_glue::guarded([&] { m_v->copy_to(h.data()); }, "UG4GBVector::operator[]");
-        return h[i];
+        double r = 0;
+        ug4gb_glue::guarded([&] { r = m_v->get_value((int)i); }, "UG4GBVector::operator[]");
+        return r;
+    }
+    /// one entry written on the device
+    void set_value(size_t i, double v)
+    {
+        ug4gb_glue::guarded([&] { m_v->set_value((int)i, v); }, "UG4GBVector::set_value");
     }
     void copy_from_host(const double *src)
     {
@@ -149,6 +161,49 @@ public:
     size_t num_rows() const { return (size_t)info().r; }
     size_t num_cols() const { return (size_t)info().c; }
     size_t total_num_connections() const { return (size_t)info().nnz; }
+
+    /// SparseMatrix::resize_and_clear (sparsematrix_impl.h:91): empty rows
+    void resize_and_clear(size_t rows, size_t cols)
+    {
+        ug4gb_glue::guarded([&] { m_A->resize_and_clear((int)rows, (int)cols); }, "resize_and_clear");
+    }
+    /// SparseMatrix::clear_retain_structure (:142): values 0, pattern kept
+    void clear_retain_structure()
+    {
+        ug4gb_glue::guarded([&] { m_A->clear_retain_structure(); }, "clear_retain_structure");
+    }
+    /// SparseMatrix::set_as_copy_of (:472): this = scale * B
+    void set_as_copy_of(const UG4GBSparseMatrix &B, double scale = 1.0)
+    {
+        ug4gb_glue::guarded([&] { m_A->set_as_copy_of(*B.m_A, scale); }, "set_as_copy_of");
+    }
+    /// SparseMatrix::scale (:487)
+    bool scale(double d)
+    {
+        ug4gb_glue::guarded([&] { m_A->scale(d); }, "scale");
+        return true;
+    }
+    /// SparseMatrix::apply_ignore_zero_rows (:270-288): dest = beta A w on rows with stored entries
+    void apply_ignore_zero_rows(UG4GBVector &dest, const double &beta1, const UG4GBVector &w1) const
+    {
+        ug4gb_glue::guarded([&] { m_A->apply_ignore_zero_rows(dest.impl(), beta1, w1.impl()); },
+                            "apply_ignore_zero_rows");
+    }
+    /// A(r, c) read from the device (0 if not stored; set-up code, not solver loops)
+    double operator()(size_t r, size_t c) const
+    {
+        std::vector<int> ci;
+        std::vector<double> va;
+        ug4gb_glue::guarded([&] { m_A->row((int)r, ci, va); }, "SparseMatrix::operator()");
+        for (size_t a = 0; a < ci.size(); ++a)
+            if (ci[a] == (int)c) return va[a];
+        return 0.0;
+    }
+    /// element contributions added into the existing pattern (AddLocalMatrixToGlobal)
+    void add_entries(const std::vector<int> &rows, const std::vector<int> &cols, const std::vector<double> &vals)
+    {
+        ug4gb_glue::guarded([&] { m_A->add_entries(rows, cols, vals); }, "add_entries");
+    }
 
     /// CRS from host arrays (sorted columns per row, as SparseMatrix::defragment leaves them)
     void set_csr(int rows, int cols, const std::vector<int> &rowptr, const std::vector<int> &col,

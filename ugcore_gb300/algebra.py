@@ -255,6 +255,22 @@ class GPUVector:
         check(lib().ug4gb_vector_norm(self.h, C.byref(out)), self.ctx.h)
         return out.value
 
+    def maxnorm(self):
+        out = C.c_double()
+        check(lib().ug4gb_vector_maxnorm(self.h, C.byref(out)), self.ctx.h)
+        return out.value
+
+    def get_values(self, idx):
+        i = np.ascontiguousarray(idx, np.int32)
+        out = np.zeros(len(i))
+        check(lib().ug4gb_vector_get_values(self.h, len(i), _ptr(i), _ptr(out)), self.ctx.h)
+        return out
+
+    def set_values(self, idx, vals):
+        i = np.ascontiguousarray(idx, np.int32)
+        v = np.ascontiguousarray(vals, np.float64)
+        check(lib().ug4gb_vector_set_values(self.h, len(i), _ptr(i), _ptr(v)), self.ctx.h)
+
     def dot(self, other):
         out = C.c_double()
         check(lib().ug4gb_vector_dot(self.h, other.h, C.byref(out)), self.ctx.h)
@@ -337,6 +353,40 @@ class GPUSparseMatrix:
     def matmul_minus(self, res, x):
         """res -= A x"""
         self.axpy(res, 1.0, res, -1.0, x)
+
+    def resize_and_clear(self, num_rows, num_cols):
+        check(lib().ug4gb_matrix_resize_and_clear(self.h, num_rows, num_cols), self.ctx.h)
+        return self
+
+    def clear_retain_structure(self):
+        check(lib().ug4gb_matrix_clear_retain_structure(self.h), self.ctx.h)
+        return self
+
+    def set_as_copy_of(self, B, scale=1.0):
+        check(lib().ug4gb_matrix_set_as_copy_of(self.h, B.h, float(scale)), self.ctx.h)
+        return self
+
+    def scale(self, alpha):
+        check(lib().ug4gb_matrix_scale(self.h, float(alpha)), self.ctx.h)
+        return self
+
+    def apply_ignore_zero_rows(self, dest, beta, w):
+        check(lib().ug4gb_matrix_apply_ignore_zero_rows(self.h, dest.h, float(beta), w.h), self.ctx.h)
+
+    def row(self, r):
+        """(columns, values) of row r, copied to the host"""
+        n = lib().ug4gb_matrix_get_row(self.h, r, None, None, 0)
+        check(min(n, 0), self.ctx.h)
+        ci, va = np.zeros(n, np.int32), np.zeros(n)
+        lib().ug4gb_matrix_get_row(self.h, r, _ptr(ci) if n else None, _ptr(va) if n else None, n)
+        return ci, va
+
+    def add_entries(self, rows, cols, vals):
+        """A(r, c) += v for entries of the existing pattern"""
+        r = np.ascontiguousarray(rows, np.int32)
+        c = np.ascontiguousarray(cols, np.int32)
+        v = np.ascontiguousarray(vals, np.float64)
+        check(lib().ug4gb_matrix_add_entries(self.h, len(r), _ptr(r), _ptr(c), _ptr(v)), self.ctx.h)
 
     def set_as_transpose_of(self, B, keep_zeros=True):
         check(lib().ug4gb_matrix_set_as_transpose_of(self.h, B.h, 1 if keep_zeros else 0), self.ctx.h)

@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libug4gb.so")
 
 SOURCES = ["k_grid.cu", "k_fv1.cu", "k_solve.cu", "k_sweep2.cu", "k_rap.cu", "api.cu", "api_disc.cu", "api_gmg.cu", "api_solver.cu",
            "api_noalloc.cu", "api_io.cu", "api_newton.cu",
-           "grid_unstructured.cu", "k_ilu.cu"]
+           "grid_unstructured.cu", "k_ilu.cu", "api_algebra.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", "-I" + os.path.join(ROOT, "include")]
