@@ -109,10 +109,11 @@ int main() {
 
 def test_ugcore_glue_instantiates_reference_solvers(tmp_path):
     """The ugcore-side GPU algebra (ugcore_gb300/adapters/ug4gb_algebra.h)
-    compiles against ugcore's own headers, and ugcore's CG, BiCGStab,
-    LinearSolver and MatrixOperator templates instantiate with its types
-    (where the ugcore tree is present; four empty stand-ins replace headers
-    that need Boost)."""
+    compiles against ugcore's own headers, ugcore's CG, BiCGStab,
+    LinearSolver and MatrixOperator templates instantiate with its types, and
+    ugcore's CG takes the library's multigrid (ug4gb_preconditioner.h) as its
+    ILinearIterator preconditioner (where the ugcore tree is present; four
+    empty stand-ins replace headers that need Boost)."""
     ref = os.environ.get("UG4_REFERENCE", "/root/reference")
     if not os.path.isdir(os.path.join(ref, "ugbase", "lib_algebra")):
         pytest.skip("ugcore source tree not present")
@@ -127,6 +128,7 @@ def test_ugcore_glue_instantiates_reference_solvers(tmp_path):
     src = tmp_path / "glue.cpp"
     src.write_text(r'''
 #include "ug4gb_algebra.h"
+#include "ug4gb_preconditioner.h"
 #include "lib_algebra/operator/interface/matrix_operator.h"
 #include "lib_algebra/operator/linear_solver/cg.h"
 #include "lib_algebra/operator/linear_solver/bicgstab.h"
@@ -147,6 +149,18 @@ void use(ug::UG4GBSparseMatrix &A, const ug::UG4GBSparseMatrix &B, ug::UG4GBVect
     double a = A(0, 1) + v.maxnorm() + w[2];
     v.set_value(0, a);
     A.add_entries({0}, {0}, {1.0});
+}
+// ugcore's CG with the library's multigrid as its preconditioner
+bool solve(ug4gb_disc *disc, SmartPtr<ug::MatrixOperator<ug::UG4GBSparseMatrix, ug::UG4GBVector> > A,
+           ug::UG4GBVector &u, ug::UG4GBVector &b)
+{
+    SmartPtr<ug::UG4GBGeometricMultiGrid> gmg = make_sp(new ug::UG4GBGeometricMultiGrid(disc));
+    gmg->set_smoother(UG4GB_SMOOTHER_JACOBI, 0.6);
+    gmg->set_precision("mixed");
+    ug::CG<ug::UG4GBVector> cg;
+    cg.set_preconditioner(gmg);
+    cg.init(A);
+    return cg.apply(u, b);
 }
 int main() { return ug::GPUAlgebra::get_type().type() == ug::AlgebraType::GPU ? 0 : 1; }
 ''')
