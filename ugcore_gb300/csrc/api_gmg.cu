@@ -11,6 +11,7 @@
 // after the base solve is dead (m_LocalFullRefLevel == top level) except on
 // the top level, where it only feeds the returned correction's defect and
 // is skipped here because apply() returns the correction alone.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 
@@ -207,7 +208,34 @@ struct GmgT : GmgBase {
         } else {
             op_from_csr<V>(c, L.A, L.At, nullptr, c.allow_dia);
             L.t.alloc(n);
+            // colours with no coupling inside a colour: parity on structured
+            // levels (valid for their stencils and for R A P of them); on
+            // unstructured levels a greedy colouring of this operator's graph,
+            // which a Galerkin operator may widen beyond the grid's elements
+            const int *colour = G.color.p;
             int ncol = G.ncolors;
+            if (!G.structured) {
+                std::vector<int> rp(n + 1), ci((size_t)L.A.nnz), vc(n, -1), seen;
+                copy_out(c, rp.data(), L.A.rowptr.p, sizeof(int) * (size_t)(n + 1));
+                copy_out(c, ci.data(), L.A.col.p, sizeof(int) * (size_t)L.A.nnz);
+                ncol = 0;
+                for (int i = 0; i < n; ++i) {
+                    seen.clear();
+                    for (int a = rp[i]; a < rp[i + 1]; ++a)
+                        if (ci[a] != i && vc[ci[a]] >= 0) seen.push_back(vc[ci[a]]);
+                    std::sort(seen.begin(), seen.end());
+                    int q = 0;
+                    for (int x : seen) {
+                        if (x == q) ++q;
+                        else if (x > q) break;
+                    }
+                    vc[i] = q;
+                    ncol = std::max(ncol, q + 1);
+                }
+                L.vcolor.alloc(n > 0 ? n : 1);
+                copy_in(c, L.vcolor.p, vc.data(), sizeof(int) * (size_t)n);
+                colour = L.vcolor.p;
+            }
             L.crow.resize(ncol);
             L.ncrow.assign(ncol, 0);
             DevBuf<int> flag, pos;
@@ -216,15 +244,15 @@ struct GmgT : GmgBase {
             for (int q = 0; q < ncol; ++q) {
                 L.crow[q].alloc(n);
                 UG_CUDA(cudaMemsetAsync(flag.p + n, 0, sizeof(int), c.stream));
-                UG_LAUNCH(c, k_colour_flag, div_up(n, 256), 256, 0, G.color.p, n, q, flag.p);
+                UG_LAUNCH(c, k_colour_flag, div_up(n, 256), 256, 0, colour, n, q, flag.p);
                 int64_t cnt = 0;
                 exclusive_scan_int(c, flag.p, pos.p, n + 1, &cnt);
-                UG_LAUNCH(c, k_colour_scatter, div_up(n, 256), 256, 0, G.color.p, n, q, pos.p, L.crow[q].p);
+                UG_LAUNCH(c, k_colour_scatter, div_up(n, 256), 256, 0, colour, n, q, pos.p, L.crow[q].p);
                 L.ncrow[q] = (int)cnt;
             }
             UG_CUDA(cudaStreamSynchronize(c.stream));
             if (smoother == UG4GB_SMOOTHER_ILU) {
-                ilu_setup<V>(c, L.A, G.color.p, L.crow, L.ncrow, L.ilu);
+                ilu_setup<V>(c, L.A, colour, L.crow, L.ncrow, L.ilu);
                 L.y.alloc(n);
             }
         }

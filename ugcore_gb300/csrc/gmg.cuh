@@ -86,6 +86,7 @@ struct GLevel {
     V *dcur = nullptr;
     std::vector<DevBuf<int>> crow;   // MCGS / ILU colour row lists
     std::vector<int> ncrow;
+    DevBuf<int> vcolor;              // unstructured levels: colours of the operator's own graph
     IluFactors<V> ilu;               // ILU smoother factors
     DevBuf<V> y;                     // ILU forward-substitution scratch
 };
