@@ -74,7 +74,7 @@ def lib():
         L.orc_prob_theta_jacobian.argtypes = [P, C.c_int, C.c_double, C.c_double, ip, ip, dp]
         L.orc_prob_create_ext.restype = P
         L.orc_prob_create_ext.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
-                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_prob_defect.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, dp]
         L.orc_prob_newton.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, C.c_int, C.c_double, C.c_double,
                                       ip, ip, dp]
@@ -127,6 +127,7 @@ class Problem:
                 ptrs.append(arr)
             self._ptrs = ptrs
             self.h = L.orc_prob_create_ext(C.byref(params), n, nv, ne, *ptrs,
+                                           None if self._m is None else self._m.ctypes.data,
                                            None if self._f is None else self._f.ctypes.data)
         else:
             self.h = L.orc_prob_create(C.byref(params),

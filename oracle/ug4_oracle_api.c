@@ -83,14 +83,14 @@ orc_prob *orc_prob_create(const orc_params *p, const double *m_top, const double
     return prob_setup(P, p, m_top, f_top);
 }
 
-/* problem on a given hierarchy (unstructured grids): coefficient kinds 0, 1
-   and 3, no velocity field */
+/* problem on a given hierarchy (unstructured grids): no velocity field;
+   coefficient kind 2 takes m_top (coarse m = mean of the children) */
 orc_prob *orc_prob_create_ext(const orc_params *p, int nlev, const int *nv, const int *ne,
                               const double *const *coords, const int *const *elems,
                               const unsigned char *const *bnd, const int *const *npar, const int *const *par,
-                              const double *f_top)
+                              const double *m_top, const double *f_top)
 {
-    if (p->coef_kind == 2 || p->vel_kind != 0) return NULL;
+    if ((p->coef_kind == 2 && !m_top) || p->vel_kind != 0) return NULL;
     orc_prob *P = (orc_prob *)calloc(1, sizeof(orc_prob));
     if (!P) return NULL;
     P->p = *p;
@@ -98,7 +98,7 @@ orc_prob *orc_prob_create_ext(const orc_params *p, int nlev, const int *nv, cons
         free(P);
         return NULL;
     }
-    return prob_setup(P, p, NULL, f_top);
+    return prob_setup(P, p, m_top, f_top);
 }
 
 static orc_prob *prob_setup(orc_prob *P, const orc_params *p, const double *m_top, const double *f_top)

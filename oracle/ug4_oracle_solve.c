@@ -594,6 +594,18 @@ static void coarsen_logk(const orc_level *F, const orc_level *C, const double *l
 {
     int *cnt = (int *)calloc((size_t)C->ne, sizeof(int));
     memset(logc, 0, sizeof(double) * (size_t)C->ne);
+    if (F->nx == 0) {
+        /* unstructured hierarchy: the children of coarse element ce are the
+           fine elements ce*nchild .. ce*nchild + nchild - 1 */
+        const int nchild = (F->dim == 2) ? 4 : 8;
+        for (int e = 0; e < F->ne; ++e) {
+            logc[e / nchild] += logf[e];
+            cnt[e / nchild]++;
+        }
+        for (int e = 0; e < C->ne; ++e) logc[e] /= (double)(cnt[e] ? cnt[e] : 1);
+        free(cnt);
+        return;
+    }
     int cx = C->nx - 1, cy = C->ny - 1;
     int fx = F->nx - 1, fy = F->ny - 1;
     for (int e = 0; e < F->ne; ++e) {

@@ -277,3 +277,66 @@ def test_unstructured_galerkin_with_colour_smoothers(ctx, oracle_lib, smoother):
     assert np.array_equal(xs[0], xs[1])
     rs = _oracle_for(oracle_lib, hier).solve()
     assert np.abs(xs[0] - rs["x"]).max() <= 1e-8 * np.abs(rs["x"]).max()
+
+
+def test_unstructured_log_coefficients_and_adjoint_gradient(ctx, oracle_lib):
+    """per-element K = exp(m) on the tetrahedral hierarchy (coarse m = mean of
+    the element's children): every level's operator against the oracle, and
+    dJ/dm of J = 0.5 |u|^2 (transposed solve + element gradient) against the
+    oracle's adjoint and central finite differences (h = 1e-5, 1e-6 relative)"""
+    import ugcore_gb300 as ug
+    hier = ug.UnstructuredHierarchy.from_ugx(ctx, os.path.join(GRIDS, "cube_tets.ugx"), 3, "Bottom")
+    ne, n = hier.num_elements(), hier.num_vertices()
+    m = 0.5 * np.random.default_rng(8).standard_normal(ne)
+    disc = ug.DomainDiscretization(hier)
+    disc.set_log_diffusion(m)
+    disc.set_source_uniform(5)
+    A = ug.GPUSparseMatrix(ctx)
+    b = ug.GPUVector(ctx, n)
+    disc.assemble_linear(A, b)
+    params = oracle_lib.make_params(elem_type=oracle_lib.ORC_TET, seed=5, coef_kind=2, solver=0, smoother=0,
+                                    damp=0.6, maxit=400, rel_red=1e-13, min_defect=1e-300)
+    op = oracle_lib.Problem(params, m_top=m, levels=_levels(hier))
+    assert_crs_equal(A.export_csr(), op.matrix(), what="top operator")
+    for l in range(hier.num_levels):
+        Al = ug.GPUSparseMatrix(ctx)
+        disc.assemble_jacobian(Al, l)
+        assert_crs_equal(Al.export_csr(), op.matrix(l), what="level %d operator" % l)
+
+    def solve(Amat, rhs, transposed=False):
+        gmg = ug.GeometricMultiGrid(disc)
+        gmg.set_smoother(ug.Jacobi(0.6))
+        gmg.set_precision("fp64")
+        gmg.set_transposed(transposed)
+        gmg.init(Amat)
+        s = ug.CG(ctx)
+        s.set_preconditioner(gmg)
+        s.set_convergence_check(ug.StdConvCheck(400, 1e-300, 1e-13))
+        s.init(Amat)
+        x = ug.GPUVector(ctx, n)
+        assert s.apply(x, rhs)
+        return x
+
+    u = solve(A, b)
+    AT = disc.adjoint_operator(A, ug.GPUSparseMatrix(ctx))
+    bnd = hier.export()[2].astype(bool)
+    g = np.where(bnd, 0.0, u.numpy())
+    lam = solve(AT, ug.GPUVector(ctx, n).copy_from(g), transposed=True)
+    grad = disc.grad_logk(u, lam)
+    ref = op.grad_logk(op.solve()["x"], op.adjoint(g)["lam"])
+    assert np.abs(grad - ref).max() <= 1e-9 * np.abs(ref).max()
+
+    def J(mm):
+        disc.set_log_diffusion(mm)
+        Am = ug.GPUSparseMatrix(ctx)
+        bm = ug.GPUVector(ctx, n)
+        disc.assemble_linear(Am, bm)
+        x = solve(Am, bm).numpy()
+        return 0.5 * float(x @ x)
+
+    rng = np.random.default_rng(9)
+    h = 1e-5
+    for _ in range(3):
+        d = rng.standard_normal(ne)
+        fd = (J(m + h * d) - J(m - h * d)) / (2 * h)
+        assert abs(grad @ d - fd) <= 1e-6 * abs(fd), (grad @ d, fd)

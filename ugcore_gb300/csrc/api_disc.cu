@@ -30,10 +30,9 @@ const double *disc_coefficients(ug4gb_disc *d, int level)
         logk[nl - 1].alloc(lev[nl - 1].ne);
         UG_CUDA(cudaMemcpyAsync(logk[nl - 1].p, D.m_top.p, D.m_top.bytes(), cudaMemcpyDeviceToDevice, c.stream));
         for (int l = nl - 2; l >= 0; --l) {
-            UG_REQUIRE(lev[l].structured, UG4GB_ERR_INVALID,
-                       "per-element log coefficients need a structured hierarchy (children's mean)");
             logk[l].alloc(lev[l].ne);
-            coarsen_log(c, lev[l + 1], lev[l], logk[l + 1].p, logk[l].p);
+            if (lev[l].structured) coarsen_log(c, lev[l + 1], lev[l], logk[l + 1].p, logk[l].p);
+            else coarsen_log_children(c, lev[l + 1], lev[l], logk[l + 1].p, logk[l].p);
         }
         for (int l = 0; l < nl; ++l) {
             D.Klev[l].alloc(lev[l].ne);

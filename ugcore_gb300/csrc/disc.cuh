@@ -51,6 +51,8 @@ void launch_dirichlet_values(Ctx &c, const Level &L, double *u);
 void launch_coef_fourier(Ctx &c, const Level &L, int nmodes, const double *k, const double *phase, double amp,
                          double factor, double *K);
 void coarsen_log(Ctx &c, const Level &F, const Level &Cl, const double *logf, double *logc);
+// unstructured levels: coarse log K = mean of the element's children
+void coarsen_log_children(Ctx &c, const Level &F, const Level &Cl, const double *logf, double *logc);
 void exp_elements(Ctx &c, const double *m, int n, double *K);
 void launch_grad_logk(Ctx &c, const Level &L, const double *K, const double *u, const double *lam, double *g);
 void launch_grad_source(Ctx &c, const Level &L, const double *lam, double *g);

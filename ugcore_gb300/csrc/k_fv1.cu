@@ -428,6 +428,24 @@ void coarsen_log(Ctx &c, const Level &F, const Level &Cl, const double *logf, do
               Cl.ny, Cl.ne, logf, logc);
 }
 
+// unstructured levels: the children of coarse element e are the fine
+// elements e*nchild .. e*nchild + nchild - 1 (regular refinement order)
+__global__ void k_coarsen_children(const double *logf, int nchild, int cne, double *logc)
+{
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= cne) return;
+    double s = 0.0;
+    for (int q = 0; q < nchild; ++q) s += logf[(size_t)e * nchild + q];
+    logc[e] = s / (double)nchild;
+}
+
+void coarsen_log_children(Ctx &c, const Level &F, const Level &Cl, const double *logf, double *logc)
+{
+    UG_REQUIRE((int64_t)Cl.ne * (F.dim == 2 ? 4 : 8) == F.ne, UG4GB_ERR_INVALID,
+               "coarse log coefficients: the fine level is not a regular refinement of the coarse one");
+    UG_LAUNCH(c, k_coarsen_children, div_up(Cl.ne, 256), 256, 0, logf, F.dim == 2 ? 4 : 8, Cl.ne, logc);
+}
+
 void exp_elements(Ctx &c, const double *m, int n, double *K)
 {
     UG_LAUNCH(c, k_exp, div_up(n, 256), 256, 0, m, n, K);
