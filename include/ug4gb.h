@@ -304,7 +304,7 @@ UG4GB_API void ug4gb_disc_destroy(ug4gb_disc *d);
    level 0; Jacobi damping 0.6 as in the configured scripts. */
 UG4GB_API int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out);
 UG4GB_API int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp);            /* set_smoother */
-UG4GB_API int ug4gb_gmg_set_cycle_type(ug4gb_gmg *m, int cycle);                      /* 1 = V, 2 = W */
+UG4GB_API int ug4gb_gmg_set_cycle_type(ug4gb_gmg *m, int cycle);  /* 1 = V, 2 = W, up to 4; -1 = F (mg_solver.h:339-341) */
 UG4GB_API int ug4gb_gmg_set_num_presmooth(ug4gb_gmg *m, int n);
 UG4GB_API int ug4gb_gmg_set_num_postsmooth(ug4gb_gmg *m, int n);
 UG4GB_API int ug4gb_gmg_set_base_level(ug4gb_gmg *m, int level);

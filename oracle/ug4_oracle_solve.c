@@ -411,13 +411,17 @@ static void prolongation_and_postsmooth(orc_gmg *G, int l)
     if (l >= G->nlev - 1) orc_crs_matmul_minus(&G->A[l], G->sd[l], G->st[l]);
 }
 
-static void lmgc(orc_gmg *G, int l)
+/* AssembledMultiGridCycle::lmgc (mg_solver_impl.hpp:2091-2134): cycle type
+   gamma >= 1 (V = 1, W = 2) visits the coarser level gamma times; the
+   F-cycle (-1) visits it once as an F-cycle, then once as a V-cycle */
+static void lmgc(orc_gmg *G, int l, int ctype)
 {
     int top = G->nlev - 1;
     if (l == G->base) { base_solve(G, top); return; }
     presmooth_and_restriction(G, l);
     if (l - 1 == G->base) base_solve(G, l - 1);
-    else for (int i = 0; i < G->cycle; ++i) lmgc(G, l - 1);
+    else if (ctype == -1) { lmgc(G, l - 1, -1); lmgc(G, l - 1, 1); }
+    else for (int i = 0; i < ctype; ++i) lmgc(G, l - 1, ctype);
     prolongation_and_postsmooth(G, l);
 }
 
@@ -427,7 +431,7 @@ void orc_gmg_apply(orc_gmg *G, double *c, const double *d)
     memcpy(G->sd[top], d, sizeof(double) * (size_t)n);
     memset(c, 0, sizeof(double) * (size_t)n);
     memset(G->sc[top], 0, sizeof(double) * (size_t)n);
-    lmgc(G, top);
+    lmgc(G, top, G->cycle);
     for (int i = 0; i < n; ++i) c[i] += G->sc[top][i];
 }
 

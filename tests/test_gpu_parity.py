@@ -281,3 +281,24 @@ def test_smoothers_in_mixed_precision(ctx, smoother):
     assert abs(s32["steps"] - s64["steps"]) <= 2
     x64 = p64.x.numpy()
     assert np.abs(p32.x.numpy() - x64).max() <= 1e-7 * np.abs(x64).max()
+
+
+@pytest.mark.parametrize("name,cycle,over", [("c1", 2, dict(nref=3)), ("c1", -1, dict(nref=3)),
+                                             ("c2", -1, dict(nref=2, solver="bicgstab")), ("c0", 3, dict(nref=5)),
+                                             ("c4", -1, dict(nref=2))])
+def test_cycle_types_match_oracle(ctx, oracle_lib, name, cycle, over):
+    """W-, F- (-1: the coarser level once as F, then once as V) and gamma = 3
+    cycles (AssembledMultiGridCycle::lmgc, mg_solver_impl.hpp:2091-2134):
+    GMG application 1e-12, solve iterations +-1.  The F-cycle is not a
+    symmetric preconditioner, so its lognormal case runs BiCGStab"""
+    import ugcore_gb300 as ug
+    cfg, p = _problem(ctx, name, dict(over, cycle=cycle, precision="fp64"))
+    op = _oracle(oracle_lib, cfg, p)
+    d = np.random.default_rng(2).standard_normal(p.n)
+    d[p.hier.export()[2].astype(bool)] = 0.0
+    cv = ug.GPUVector(ctx, p.n)
+    p.gmg.apply(cv, ug.GPUVector(ctx, p.n).copy_from(d))
+    ref = op.apply_gmg(d)
+    assert np.abs(cv.numpy() - ref).max() <= 1e-12 * np.abs(ref).max()
+    st, rs = p.solve(), op.solve()
+    assert abs(st["steps"] - rs["steps"]) <= 1

@@ -581,7 +581,8 @@ class GeometricMultiGrid:
         check(lib().ug4gb_gmg_set_smoother(self.h, sm.kind, sm.damp), self.ctx.h)
 
     def set_cycle_type(self, cycle):
-        c = {"V": 1, "W": 2, 1: 1, 2: 2}[cycle]
+        """"V" (1), "W" (2), gamma up to 4, or "F" (-1), as set_cycle_type"""
+        c = {"V": 1, "W": 2, "F": -1}[cycle] if isinstance(cycle, str) else int(cycle)
         check(lib().ug4gb_gmg_set_cycle_type(self.h, c), self.ctx.h)
 
     def set_num_presmooth(self, n):

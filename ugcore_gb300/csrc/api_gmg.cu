@@ -316,7 +316,11 @@ struct GmgT : GmgBase {
     // last top-level kernel writes the correction back in FP64 (z64): every
     // float<->double conversion happens once per row, never per nonzero
     // (conversions issue on GB300's slow FP64 pipe).
-    void lmgc(Ctx &c, int l, const double *dtop, bool first, const int *skip, const double *r_rho, RedArgs *red,
+    // ctype: this visit's cycle type (gamma >= 1, or -1 for the F-cycle:
+    // the coarser level once as an F-cycle, then once as a V-cycle;
+    // AssembledMultiGridCycle::lmgc, mg_solver_impl.hpp:2091-2134)
+    void lmgc(Ctx &c, int l, int ctype, const double *dtop, bool first, const int *skip, const double *r_rho,
+              RedArgs *red,
               int rho_kind, bool &rho_done)
     {
         const int T = top();
@@ -370,9 +374,11 @@ struct GmgT : GmgBase {
             c.prof_tag = "L" + std::to_string(l - 1);
             base_solve<V>(c, Ainv.p, nbase, C.dA.p, C.sc.p, skip);
         } else {
-            for (int i = 0; i < cycle; ++i) {
+            const int visits = (ctype == -1) ? 2 : ctype;
+            for (int i = 0; i < visits; ++i) {
                 bool rd = false;
-                lmgc(c, l - 1, nullptr, i == 0, skip, nullptr, nullptr, 0, rd);
+                const int sub = (ctype == -1) ? (i == 0 ? -1 : 1) : ctype;
+                lmgc(c, l - 1, sub, nullptr, i == 0, skip, nullptr, nullptr, 0, rd);
             }
         }
         c.prof_tag = "L" + std::to_string(l);
@@ -386,7 +392,7 @@ struct GmgT : GmgBase {
                 const V *x = (k == 0) ? L.w.p : dbase;
                 // two steps in one pass where the level allows it
                 if (k + 1 < nu2 && L.sweep2) {
-                    bool need_out = (k + 1 < nu2 - 1) || (l != T && cycle > 1);
+                    bool need_out = (k + 1 < nu2 - 1) || (l != T && cycle != 1);
                     V *out = need_out ? ((dbase == L.dA.p) ? L.dB.p : L.dA.p) : nullptr;
                     bool last_top = (l == T && k + 1 == nu2 - 1);
                     if (smooth_pair<V>(c, L.sweep2.get(), L.gp, x, k == 0 ? dbase : nullptr, L.dinv.p, L.sc.p, out,
@@ -401,7 +407,9 @@ struct GmgT : GmgBase {
                         continue;
                     }
                 }
-                bool need_out = (k < nu2 - 1) || (l != T && cycle > 1);
+                // a level below the top is visited again (W, gamma > 2, F cycles):
+                // its last defect is the next visit's start
+                bool need_out = (k < nu2 - 1) || (l != T && cycle != 1);
                 V *out = need_out ? ((dbase == L.dA.p) ? L.dB.p : L.dA.p) : nullptr;
                 bool last_top = (l == T && k == nu2 - 1);
                 smooth_step<V, V, V>(c, L.At, x, dbase, L.dinv.p, L.sc.p, out, SC_ADD_FROM_NEW, skip,
@@ -448,7 +456,7 @@ struct GmgT : GmgBase {
     {
         rho_done = false;
         top_converted = top_ready && sizeof(V) == 4;
-        lmgc(c, top(), dtop, true, skip, r_rho, red, rho_kind, rho_done);
+        lmgc(c, top(), cycle, dtop, true, skip, r_rho, red, rho_kind, rho_done);
         return z64.p ? z64.p : (const double *)lev.back().sc.p;
     }
     float *top_defect_buffer() override
@@ -581,7 +589,7 @@ int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp)
 
 int ug4gb_gmg_set_cycle_type(ug4gb_gmg *m, int cycle)
 {
-    if (!m || (cycle != 1 && cycle != 2)) return UG4GB_ERR_INVALID;
+    if (!m || !(cycle == -1 || (cycle >= 1 && cycle <= 4))) return UG4GB_ERR_INVALID;
     m->cycle = cycle;
     return UG4GB_OK;
 }
