@@ -24,6 +24,7 @@
  *   ref_io read-mtx   in.mtx out.csr
  *   ref_io write-mat  A.csr pos.bin out.mat
  *   ref_io write-vec  v.bin pos.bin out.vec
+ *   ref_io write-vec-diff  v.bin w.bin pos.bin out.vec   (WriteVector with compareVec: v - w)
  *   ref_io read-vec   in.vec n out.bin
  */
 #include <cstdint>
@@ -130,12 +131,24 @@ static int write_mat(const Mat &A, const std::vector<char> &pb, const char *out)
 }
 
 template <int dim>
-static int write_vec(const Vec &v, const std::vector<char> &pb, const char *out)
+static int write_vec(const Vec &v, const std::vector<char> &pb, const char *out, const Vec *cmp = NULL)
 {
     std::vector<MathVector<dim> > pos;
     if (!load_positions<dim>(pb, pos)) return 3;
-    ConnectionViewer::WriteVector(std::string(out), v, &pos[0], dim);
+    ConnectionViewer::WriteVector(std::string(out), v, &pos[0], dim, cmp);
     return 0;
+}
+
+static bool load_vec(const char *path, Vec &v)
+{
+    std::vector<char> vb;
+    if (!read_file(path, vb)) return false;
+    int32_t n;
+    memcpy(&n, &vb[0], 4);
+    v.resize(n);
+    const double *x = (const double *)&vb[4];
+    for (int i = 0; i < n; ++i) v[i] = x[i];
+    return true;
 }
 
 int main(int argc, char **argv)
@@ -188,6 +201,17 @@ int main(int argc, char **argv)
                 case 1: return write_vec<1>(v, pb, argv[4]);
                 case 2: return write_vec<2>(v, pb, argv[4]);
                 case 3: return write_vec<3>(v, pb, argv[4]);
+            }
+            return 3;
+        }
+        if (cmd == "write-vec-diff" && argc >= 6) {
+            Vec v, w;
+            std::vector<char> pb;
+            if (!load_vec(argv[2], v) || !load_vec(argv[3], w) || !read_file(argv[4], pb)) return 3;
+            switch (pos_dim(pb)) {
+                case 1: return write_vec<1>(v, pb, argv[5], &w);
+                case 2: return write_vec<2>(v, pb, argv[5], &w);
+                case 3: return write_vec<3>(v, pb, argv[5], &w);
             }
             return 3;
         }

@@ -203,6 +203,14 @@ def main():
             run("read-vec", vec, str(n), back)
             store["vec%dd" % d] = v
             store["vec%dd_read" % d] = np.frombuffer(open(back, "rb").read()[4:], np.float64).copy()
+            # WriteVector with a compare vector (SaveVectorDiffForConnectionViewer): v - w
+            w = rng.standard_normal(n)
+            wb = os.path.join(tmp, "w%d.bin" % d)
+            with open(wb, "wb") as f:
+                f.write(struct.pack("<i", n))
+                f.write(w.tobytes())
+            run("write-vec-diff", vb, wb, os.path.join(tmp, "pos%d.bin" % d), os.path.join(OUT, "vec%dd_diff.vec" % d))
+            store["vec%dd_cmp" % d] = w
     np.savez(os.path.join(OUT, "cases.npz"), **store)
     print("wrote", sorted(os.listdir(OUT)))
 

@@ -72,6 +72,10 @@ def test_connection_viewer_files_on_grid_positions(ctx, tmp_path, cases, name, e
     assert open(vout, "rb").read() == _golden("vec%dd.vec" % d)
     w = matrix_io.LoadVector(ug.GPUVector(ctx, hier.num_vertices()), os.path.join(IO, "vec%dd.vec" % d))
     assert np.array_equal(_bits(w.numpy()), _bits(cases["vec%dd_read" % d]))
+    cmp = ug.GPUVector(ctx, hier.num_vertices()).copy_from(cases["vec%dd_cmp" % d])
+    dout = str(tmp_path / "d.vec")
+    matrix_io.SaveVectorDiffForConnectionViewer(hier, v, cmp, dout)
+    assert open(dout, "rb").read() == _golden("vec%dd_diff.vec" % d)
 
 
 def test_assembled_operator_round_trip(ctx, tmp_path):

@@ -83,6 +83,14 @@ def test_connection_viewer_vector_matches_ugcore(tmp_path, cases, mio, dim):
     assert np.array_equal(_bits(back), _bits(cases["vec%dd_read" % dim]))
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_connection_viewer_vector_difference_matches_ugcore(tmp_path, cases, mio, dim):
+    """WriteVector with a compare vector writes v - w (SaveVectorDiffForConnectionViewer)"""
+    out = str(tmp_path / "d.vec")
+    mio.write_cv_vector(out, cases["vec%dd" % dim] - cases["vec%dd_cmp" % dim], cases["pos%d" % dim])
+    assert open(out, "rb").read() == _golden("vec%dd_diff.vec" % dim)
+
+
 def test_round_trip_of_a_large_random_matrix(tmp_path, mio):
     """general matrix with 200k entries: write, read back, same CRS up to the
     13 significant digits the format keeps; zero values are dropped"""

@@ -110,6 +110,15 @@ def SaveVectorForConnectionViewer(hier, v, filename, level=None):
     check(lib().ug4gb_vector_write_cv(v.h, hier.h, level, filename.encode()), v.ctx.h)
 
 
+def SaveVectorDiffForConnectionViewer(hier, a, b, filename, level=None):
+    """a - b as a .vec file (output_bridge.cpp:226-232; WriteVector with a
+    compare vector, connection_viewer_output.h:413-418)"""
+    from .algebra import GPUVector
+    d = GPUVector(a.ctx, len(a))
+    d.scale_add(1.0, a, -1.0, b)
+    SaveVectorForConnectionViewer(hier, d, filename, level)
+
+
 def LoadVector(v, filename):
     check(lib().ug4gb_vector_read_cv(v.h, filename.encode()), v.ctx.h)
     return v
