@@ -31,9 +31,12 @@
 // Without subsets, the topological boundary (facets of one element) is the
 // Dirichlet boundary.
 //
-// The hierarchy is built on the host once (set-up) and uploaded; element and
-// vertex colourings (greedy, in index order) give the assembly its race-free
-// scatter order and the multicolour Gauss-Seidel its colours.
+// refine() below is the host statement of these rules (it also serves the
+// host-only ug4gb_io_ugx_level); the hierarchies the solvers use are refined
+// on the device by grid_refine_device.cu with the same numbering and the same
+// (explicitly rounded) arithmetic.  Element and vertex colourings (greedy, in
+// index order) give the assembly its race-free scatter order and the
+// multicolour Gauss-Seidel its colours.
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -44,6 +47,7 @@
 #include <vector>
 
 #include "gmg.cuh"
+#include "grid_refine.cuh"
 
 namespace ug4gb {
 
@@ -853,20 +857,66 @@ HostLevel ugx_level0(const char *path, const char *dirichlet)
 
 }  // namespace
 
-// hierarchy of `nref` refinements of level 0 on the device
-void build_unstructured(Ctx &c, HostLevel L0, int nref, std::vector<Level> &lev);
+namespace {
 
+// the Dirichlet objects of a host level, for the device refinement
+void upload_dirichlet(Ctx &c, const HostLevel &H, DevDir &D)
+{
+    std::vector<u64> e(H.dir_edges.size());
+    for (size_t i = 0; i < e.size(); ++i)
+        e[i] = ((u64)(unsigned)H.dir_edges[i][0] << 32) | (u64)(unsigned)H.dir_edges[i][1];
+    std::vector<int4> f(H.dir_faces.size());
+    for (size_t i = 0; i < f.size(); ++i)
+        f[i] = make_int4(H.dir_faces[i][0], H.dir_faces[i][1], H.dir_faces[i][2], H.dir_faces[i][3]);
+    D.n_edges = (int)e.size();
+    D.n_faces = (int)f.size();
+    D.edges.alloc(std::max<size_t>(e.size(), 1));
+    D.faces.alloc(std::max<size_t>(f.size(), 1));
+    D.edir.alloc(std::max<size_t>(H.edir.size(), 1));
+    copy_in(c, D.edges.p, e.data(), sizeof(u64) * e.size());
+    copy_in(c, D.faces.p, f.data(), sizeof(int4) * f.size());
+    copy_in(c, D.edir.p, H.edir.data(), H.edir.size());
+}
+
+// element and vertex colourings of a level refined on the device
+void colour_level(Ctx &c, Level &L)
+{
+    HostLevel H;
+    H.elem_type = L.elem_type;
+    H.dim = L.dim;
+    H.k = L.k;
+    H.nv = L.nv;
+    H.ne = L.ne;
+    H.elems.resize((size_t)L.ne * L.k);
+    copy_out(c, H.elems.data(), L.elems.p, sizeof(int) * H.elems.size());
+    std::vector<int> list;
+    colour_elements(H, L.ecol_off, list);
+    L.ecol.alloc(std::max<size_t>(list.size(), 1));
+    copy_in(c, L.ecol.p, list.data(), sizeof(int) * list.size());
+    std::vector<int> vcol;
+    L.ncolors = colour_vertices(H, vcol);
+    L.color.alloc(H.nv);
+    copy_in(c, L.color.p, vcol.data(), sizeof(int) * vcol.size());
+    UG_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+}  // namespace
+
+// Hierarchy of `nref` refinements of level 0: level 0 is uploaded, every
+// finer level is refined on the device from the one below it (the same
+// numbering and arithmetic as refine() above); only the greedy colourings,
+// sequential in index order, run on the host.
 void build_unstructured(Ctx &c, HostLevel L0, int nref, std::vector<Level> &lev)
 {
     lev.clear();
     lev.resize(nref + 1);
-    HostLevel cur = std::move(L0);
-    for (int l = 0; l <= nref; ++l) {
-        upload(c, cur, lev[l]);
-        if (l == nref) break;
-        HostLevel next;
-        refine(cur, next);
-        cur = std::move(next);
+    upload(c, L0, lev[0]);
+    std::vector<DevDir> dir(nref + 1);
+    upload_dirichlet(c, L0, dir[0]);
+    for (int l = 1; l <= nref; ++l) {
+        refine_device(c, lev[l - 1], dir[l - 1], lev[l], dir[l]);
+        colour_level(c, lev[l]);
+        dir[l - 1] = DevDir();
     }
 }
 
