@@ -383,6 +383,20 @@ UG4GB_API int ug4gb_newton_get_stats(const ug4gb_newton *nw, int *steps, double 
                                      double *final_defect, int *lin_steps, int capacity);
 /* |d| after each Newton step (entry 0: start); returns the number available */
 UG4GB_API int ug4gb_newton_get_history(const ug4gb_newton *nw, double *defects, int capacity);
+/* StandardLineSearch (lib_disc/operator/non_linear_operator/line_search.h:
+   115-400; the constructor's defaults 10, 1.0, 0.5, 0.25, false, false,
+   1e10) for every Newton step: set_maximum_steps, set_lambda_start,
+   set_reduce_factor, set_suff_descent_factor, set_accept_best, set_check_all,
+   set_maximum_defect.  A failed search ends apply with
+   UG4GB_ERR_NOT_CONVERGED, as NewtonSolver::apply returns false. */
+UG4GB_API int ug4gb_newton_set_line_search(ug4gb_newton *nw, int max_steps, double lambda_start,
+                                          double lambda_reduce, double suff_descent_factor, int accept_best,
+                                          int check_all, double max_defect);
+UG4GB_API int ug4gb_newton_clear_line_search(ug4gb_newton *nw);
+/* per Newton step of the last apply: line-search tries evaluated and the
+   lambda of the accepted solution; returns the number of steps recorded */
+UG4GB_API int ug4gb_newton_get_line_search_history(const ug4gb_newton *nw, int *tries, double *lambdas,
+                                                  int capacity);
 UG4GB_API void ug4gb_newton_destroy(ug4gb_newton *nw);
 
 /* ------------------------------------------------------------ adjoint -- */

@@ -16,6 +16,13 @@ _LIB = None
 ORC_QUAD, ORC_HEX, ORC_TET, ORC_TRI = 0, 1, 2, 3
 
 
+class LineSearch(C.Structure):
+    """StandardLineSearch parameters (orc_line_search)"""
+    _fields_ = [("max_steps", C.c_int), ("lambda_start", C.c_double), ("lambda_reduce", C.c_double),
+                ("alpha", C.c_double), ("max_defect", C.c_double), ("accept_best", C.c_int),
+                ("check_all", C.c_int)]
+
+
 class Params(C.Structure):
     _fields_ = [
         ("elem_type", C.c_int), ("mx", C.c_int), ("my", C.c_int), ("mz", C.c_int), ("nref", C.c_int),
@@ -78,6 +85,8 @@ def lib():
         L.orc_prob_defect.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, dp]
         L.orc_prob_newton.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, C.c_int, C.c_double, C.c_double,
                                       ip, ip, dp]
+        L.orc_prob_newton_ls.argtypes = [P, C.c_double, C.c_double, C.c_void_p, dp, C.c_int, C.c_double,
+                                         C.c_double, C.c_void_p, ip, ip, dp, ip, dp]
         L.orc_prob_gmg_level_nnz.argtypes = [P, C.c_int]
         L.orc_prob_gmg_level_nnz.restype = C.c_int64
         L.orc_prob_gmg_level.argtypes = [P, C.c_int, ip, ip, dp]
@@ -181,21 +190,38 @@ class Problem:
             raise RuntimeError("defect failed")
         return d
 
-    def newton(self, u0, maxit=10, min_defect=1e-50, reduction=1e-10, theta=None, dt=0.0, u_old=None):
-        """NewtonSolver on the stationary operator or one theta step; returns
-        (u, rc, steps, linear steps per step, defects)"""
+    def newton(self, u0, maxit=10, min_defect=1e-50, reduction=1e-10, theta=None, dt=0.0, u_old=None,
+               line_search=None):
+        """NewtonSolver on the stationary operator or one theta step, with
+        line_search = dict(max_steps, lambda_start, lambda_reduce, alpha,
+        max_defect, accept_best, check_all) or None; returns (u, rc, steps,
+        linear steps per step, defects), plus (tries, lambdas) per step with a
+        line search"""
         u = np.array(u0, dtype=np.float64, copy=True)
         steps = np.zeros(1, np.int32)
         ls = np.zeros(maxit + 1, np.int32)
         defs = np.zeros(maxit + 1)
+        tries = np.zeros(maxit + 1, np.int32)
+        lams = np.zeros(maxit + 1)
         uo = None if u_old is None else np.ascontiguousarray(u_old, np.float64)
-        rc = lib().orc_prob_newton(self.h, -1.0 if theta is None else theta, dt,
-                                   None if uo is None else uo.ctypes.data_as(C.c_void_p), u, maxit, min_defect,
-                                   reduction, steps, ls, defs)
+        ptr = None
+        if line_search is not None:
+            p = dict(max_steps=10, lambda_start=1.0, lambda_reduce=0.5, alpha=0.25, max_defect=1e10,
+                     accept_best=0, check_all=0)
+            p.update(line_search)
+            lsp = LineSearch(int(p["max_steps"]), p["lambda_start"], p["lambda_reduce"], p["alpha"],
+                             p["max_defect"], int(p["accept_best"]), int(p["check_all"]))
+            ptr = C.cast(C.pointer(lsp), C.c_void_p)
+        rc = lib().orc_prob_newton_ls(self.h, -1.0 if theta is None else theta, dt,
+                                      None if uo is None else uo.ctypes.data_as(C.c_void_p), u, maxit, min_defect,
+                                      reduction, ptr, steps, ls, defs, tries, lams)
         if rc < 0:
             raise RuntimeError("Newton set-up failed %d" % rc)
         n = int(steps[0])
-        return u, rc, n, ls[:n], defs[:n + 1]
+        if line_search is None:
+            return u, rc, n, ls[:n], defs[:n + 1]
+        nt = n + (1 if rc == 3 else 0)
+        return u, rc, n, ls[:n], defs[:n + 1], (tries[:nt].tolist(), lams[:nt].tolist())
 
     def theta_jacobian(self, l, theta, dt):
         """level l's M + theta dt A (CRS pattern = the level's)"""

@@ -352,22 +352,80 @@ int orc_prob_defect(const orc_prob *P, double theta, double dt, const double *u_
     return orc_assemble_defect(&P->H.lev[top], &D, u, d);
 }
 
-/* NewtonSolver::apply (newton_impl.h:171-340, no line search) with the
-   problem's GMG-preconditioned Krylov solver as the linear solver (its own
-   convergence parameters) on the stationary operator (theta < 0) or the
-   theta step from u_old.  u in/out.  Returns 0 if Newton converged, 1 if not,
-   2 if a linear solve failed, < 0 on set-up errors.  steps: Newton steps;
-   lin_steps[s], defects[s] (s <= maxit, defects[0] the start defect). */
-int orc_prob_newton(orc_prob *P, double theta, double dt, const double *u_old, double *u, int maxit,
-                    double min_defect, double reduction, int *steps, int *lin_steps, double *defects)
+/* parameters of StandardLineSearch (its setters) */
+typedef struct {
+    int max_steps;              /* <= 64 */
+    double lambda_start, lambda_reduce, alpha, max_defect;
+    int accept_best, check_all;
+} orc_line_search;
+
+/* StandardLineSearch::search (lib_disc/operator/non_linear_operator/
+   line_search.h:186-400) along the correction c from s = u with the start
+   defect norm norm_old: tries u = u - lambda c (lambda = start, start*reduce,
+   ...), accepting the first with |N(u)| / norm_old <= 1 - alpha |lambda|
+   (all max_steps tries with check_all); after max_steps tries, with
+   accept_best, u = s - start reduce^best c for the first smallest ratio,
+   failing when its defect exceeds max_defect; without accept_best it fails.
+   d = N(u) on return.  Returns 0, or 3 when the search failed. */
+static int line_search(orc_prob *P, double theta, double dt, const double *u_old, const orc_level *L,
+                       const orc_line_search *LS, double *u, const double *c, double *d, double *s, double norm_old,
+                       double *norm, int *tries, double *lambda_out)
+{
+    const int nv = L->nv;
+    double lambda = LS->lambda_start, nrm = 0.0;
+    double rho[64];
+    memcpy(s, u, sizeof(double) * (size_t)nv);
+    for (int k = 1; k <= LS->max_steps; ++k) {
+        for (int i = 0; i < nv; ++i) u[i] = 1.0 * u[i] + (-lambda) * c[i];
+        for (int i = 0; i < nv; ++i) if (L->bnd[i]) u[i] = 0.0;      /* prepare */
+        if (orc_prob_defect(P, theta, dt, u_old, u, d)) return -1;
+        nrm = orc_vnorm(nv, d);
+        *tries = k;
+        *lambda_out = lambda;
+        rho[k - 1] = nrm / norm_old;
+        if (rho[k - 1] <= 1.0 - LS->alpha * fabs(lambda) && !LS->check_all) break;
+        lambda *= LS->lambda_reduce;
+        if (k == LS->max_steps) {
+            if (!LS->accept_best) return 3;
+            int best = 0;
+            for (int i = 1; i < k; ++i)
+                if (rho[best] > rho[i]) best = i;
+            const double lb = LS->lambda_start * pow(LS->lambda_reduce, (double)best);
+            *lambda_out = lb;
+            for (int i = 0; i < nv; ++i) u[i] = 1.0 * s[i] + (-lb) * c[i];
+            for (int i = 0; i < nv; ++i) if (L->bnd[i]) u[i] = 0.0;
+            if (orc_prob_defect(P, theta, dt, u_old, u, d)) return -1;
+            nrm = orc_vnorm(nv, d);
+            if (nrm > LS->max_defect) return 3;
+            break;
+        }
+        memcpy(u, s, sizeof(double) * (size_t)nv);
+    }
+    *norm = nrm;
+    return 0;
+}
+
+/* NewtonSolver::apply (newton_impl.h:171-340) with the problem's
+   GMG-preconditioned Krylov solver as the linear solver (its own convergence
+   parameters) on the stationary operator (theta < 0) or the theta step from
+   u_old, without (LS NULL) or with StandardLineSearch.  u in/out.  Returns 0
+   if Newton converged, 1 if not, 2 if a linear solve failed, 3 if a line
+   search failed, < 0 on set-up errors.  steps: Newton steps; lin_steps[s],
+   defects[s] (s <= maxit, defects[0] the start defect); ls_tries[s],
+   ls_lambda[s] per step with a line search. */
+int orc_prob_newton_ls(orc_prob *P, double theta, double dt, const double *u_old, double *u, int maxit,
+                       double min_defect, double reduction, const orc_line_search *LS, int *steps, int *lin_steps,
+                       double *defects, int *ls_tries, double *ls_lambda)
 {
     const int nl = P->H.nlev, top = nl - 1, nv = P->H.lev[top].nv;
     const orc_level *L = &P->H.lev[top];
     double *d = (double *)malloc(sizeof(double) * (size_t)nv);
     double *c = (double *)malloc(sizeof(double) * (size_t)nv);
     double *rhs = (double *)malloc(sizeof(double) * (size_t)nv);
+    double *s = (double *)malloc(sizeof(double) * (size_t)nv);
     orc_crs *J = (orc_crs *)calloc((size_t)nl, sizeof(orc_crs));
-    if (!d || !c || !rhs || !J) return -1;
+    if (!d || !c || !rhs || !s || !J) return -1;
+    if (LS && (LS->max_steps < 1 || LS->max_steps > 64)) return -1;
     int rc = 0;
     orc_conv NC;
     memset(&NC, 0, sizeof(NC));
@@ -400,17 +458,36 @@ int orc_prob_newton(orc_prob *P, double theta, double dt, const double *u_old, d
         orc_gmg_free(&G);
         if (lin_steps) lin_steps[NC.steps] = ls;
         if (lrc) { rc = 2; break; }
-        for (int i = 0; i < nv; ++i) u[i] -= c[i];
-        for (int i = 0; i < nv; ++i) if (L->bnd[i]) u[i] = 0.0;      /* prepare */
-        if (orc_prob_defect(P, theta, dt, u_old, u, d)) return -1;
-        orc_conv_update(&NC, orc_vnorm(nv, d));
+        double nd = 0.0;
+        if (LS) {
+            int tr = 0;
+            double lam = 0.0;
+            const int src = line_search(P, theta, dt, u_old, L, LS, u, c, d, s, NC.final_defect, &nd, &tr, &lam);
+            if (ls_tries) ls_tries[NC.steps] = tr;
+            if (ls_lambda) ls_lambda[NC.steps] = lam;
+            if (src < 0) return -1;
+            if (src) { rc = 3; break; }
+        } else {
+            for (int i = 0; i < nv; ++i) u[i] -= c[i];
+            for (int i = 0; i < nv; ++i) if (L->bnd[i]) u[i] = 0.0;      /* prepare */
+            if (orc_prob_defect(P, theta, dt, u_old, u, d)) return -1;
+            nd = orc_vnorm(nv, d);
+        }
+        orc_conv_update(&NC, nd);
         if (defects) defects[NC.steps] = NC.final_defect;
     }
     if (rc == 0) rc = orc_conv_post(&NC) ? 0 : 1;
     if (steps) *steps = NC.steps;
     for (int l = 0; l < nl; ++l) orc_crs_free(&J[l]);
-    free(J); free(d); free(c); free(rhs);
+    free(J); free(d); free(c); free(rhs); free(s);
     return rc;
+}
+
+int orc_prob_newton(orc_prob *P, double theta, double dt, const double *u_old, double *u, int maxit,
+                    double min_defect, double reduction, int *steps, int *lin_steps, double *defects)
+{
+    return orc_prob_newton_ls(P, theta, dt, u_old, u, maxit, min_defect, reduction, NULL, steps, lin_steps, defects,
+                              NULL, NULL);
 }
 
 /* transposed operator with Dirichlet rows reset to identity */

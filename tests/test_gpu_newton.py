@@ -179,3 +179,94 @@ def test_newton_not_converged_is_reported(ctx):
     assert nw.stats()["steps"] == 1
     with pytest.raises(ug.UG4GBError):
         nw.apply(u)
+
+
+LS_CASES = [
+    (dict(lambda_start=2.0), "rejects the overshooting lambda = 2, accepts lambda = 1"),
+    (dict(lambda_start=2.0, max_steps=3, accept_best=1, check_all=1), "evaluates all three tries, takes the best"),
+    (dict(lambda_start=1.0, lambda_reduce=0.25, alpha=0.6), "sufficient descent 0.6"),
+]
+
+
+@pytest.mark.parametrize("ls", [c[0] for c in LS_CASES])
+@pytest.mark.parametrize("name,over", [("c1", dict(nref=3, precision="fp64")), ("c4", dict(nref=2, precision="fp64")),
+                                       ("c1", dict(nref=3, precision="mixed"))])
+def test_newton_line_search_matches_oracle(ctx, oracle_lib, name, over, ls):
+    """Newton with StandardLineSearch (inexact linear solves to 1e-8, so
+    several Newton steps): the same tries and accepted lambdas per step as the
+    oracle, and the same solution"""
+    import ugcore_gb300 as ug
+    cfg, p, op = _setup(ctx, oracle_lib, name, over)
+    cfg = dict(cfg, rel_red=1e-8)
+    op = oracle_lib.Problem(oracle_params(oracle_lib, cfg), m_top=getattr(p, "m_top", None))
+    u0 = _random(p, 6)
+    nw, _ = _newton(ctx, p, cfg)
+    s = ug.StandardLineSearch(ls.get("max_steps", 10), ls["lambda_start"], ls.get("lambda_reduce", 0.5),
+                              bool(ls.get("accept_best", 0)), bool(ls.get("check_all", 0)))
+    s.set_suff_descent_factor(ls.get("alpha", 0.25))
+    nw.set_line_search(s)
+    nw.init(ug.AssembledOperator(p.disc))
+    u = ug.GPUVector(ctx, p.n).copy_from(u0)
+    assert nw.apply(u)
+    ref = op.newton(u0, maxit=6, reduction=1e-12, line_search=ls)
+    _compare(nw, u.numpy(), ref[:5])
+    tries, lams = nw.line_search_history()
+    assert tries == ref[5][0] and lams == ref[5][1], (tries, lams, ref[5])
+
+
+def test_newton_line_search_on_a_theta_step(ctx, oracle_lib):
+    import ugcore_gb300 as ug
+    cfg, p, op = _setup(ctx, oracle_lib, "c1", dict(nref=3, precision="fp64"))
+    cfg = dict(cfg, rel_red=1e-8)
+    op = oracle_lib.Problem(oracle_params(oracle_lib, cfg), m_top=getattr(p, "m_top", None))
+    dt, theta = 0.02, 0.5
+    u_old = _random(p, 7)
+    td = ug.ThetaTimeStep(p.disc, theta)
+    td.prepare_step(ug.GPUVector(ctx, p.n).copy_from(u_old), 0.0, dt)
+    nw, gmg = _newton(ctx, p, cfg)
+    gmg.set_discretization(td)
+    nw.set_line_search(ug.StandardLineSearch(lambda_start=2.0))
+    nw.init(ug.AssembledOperator(td))
+    u = ug.GPUVector(ctx, p.n).copy_from(u_old)
+    assert nw.apply(u)
+    ref = op.newton(u_old, maxit=6, reduction=1e-12, theta=theta, dt=dt, u_old=u_old,
+                    line_search=dict(lambda_start=2.0))
+    _compare(nw, u.numpy(), ref[:5])
+    assert nw.line_search_history() == (ref[5][0], ref[5][1])
+
+
+def test_newton_line_search_failures(ctx, oracle_lib):
+    """without accept_best a search whose tries all fail ends Newton
+    (NewtonSolver::apply returns false); with accept_best the best try is
+    taken, and max_defect caps it"""
+    import ugcore_gb300 as ug
+    cfg, p, op = _setup(ctx, oracle_lib, "c1", dict(nref=3, precision="fp64"))
+    u0 = _random(p, 6)
+    nw, _ = _newton(ctx, p, cfg)
+    nw.init(ug.AssembledOperator(p.disc))
+    nw.set_line_search(ug.StandardLineSearch(max_steps=1, lambda_start=2.0))
+    u = ug.GPUVector(ctx, p.n).copy_from(u0)
+    assert nw.apply(u, raise_on_failure=False) is False
+    assert nw.line_search_history() == ([1], [2.0])
+    assert nw.stats()["steps"] == 0
+    with pytest.raises(ug.UG4GBError, match="line search"):
+        nw.apply(ug.GPUVector(ctx, p.n).copy_from(u0))
+    ls = ug.StandardLineSearch(max_steps=1, lambda_start=2.0, accept_best=True)
+    nw.set_line_search(ls)
+    nw.set_convergence_check(ug.StdConvCheck(2, 1e-50, 1e-12))
+    u = ug.GPUVector(ctx, p.n).copy_from(u0)
+    assert nw.apply(u, raise_on_failure=False) is False
+    ref = op.newton(u0, maxit=2, reduction=1e-12, line_search=dict(max_steps=1, lambda_start=2.0, accept_best=1))
+    assert ref[1] == 1 and nw.line_search_history() == ref[5] == ([1, 1], [2.0, 2.0])
+    h = nw.history()
+    assert np.allclose(h, ref[4], rtol=1e-6)
+    ls.set_maximum_defect(0.5 * h[0])
+    nw.set_line_search(ls)
+    with pytest.raises(ug.UG4GBError, match="defect-limit"):
+        nw.apply(ug.GPUVector(ctx, p.n).copy_from(u0))
+    nw.set_line_search(None)
+    nw.set_convergence_check(ug.StdConvCheck(6, 1e-50, 1e-12))
+    assert nw.apply(ug.GPUVector(ctx, p.n).copy_from(u0))
+    assert nw.line_search_history() == ([], [])
+    with pytest.raises(ug.UG4GBError):
+        nw.set_line_search(ug.StandardLineSearch(max_steps=0))

@@ -312,3 +312,35 @@ def test_implicit_euler_approaches_the_stationary_solution(oracle_lib):
     u, steps = P.theta_steps(1.0, 10.0, 6, np.zeros(P.nv()))
     assert np.abs(u - us).max() <= 1e-6 * np.abs(us).max()
     assert all(s > 0 for s in steps)
+
+
+def test_newton_line_search_paths(oracle_lib):
+    """StandardLineSearch in the oracle's Newton (linear operator, accurate
+    linear solves, so the full step lambda = 1 takes the defect to ~1e-10 and
+    lambda = 2 leaves |d| unchanged): the default search is Newton without one;
+    lambda_start = 2 is rejected (rho ~ 1 > 1 - 0.25 * 2) and lambda = 1
+    accepted; check_all + accept_best evaluates every try and takes the best;
+    accept_best after one rejected try takes it; without accept_best the search
+    (and Newton) fails; max_defect caps the accepted defect."""
+    orc = oracle_lib
+    P = orc.Problem(orc.make_params(elem_type=orc.ORC_QUAD, mx=2, my=2, nref=3, seed=5, rel_red=1e-12, maxit=400))
+    u0 = np.zeros(P.nv())
+    ref = P.newton(u0, maxit=4, reduction=1e-9)
+    assert ref[1] == 0 and ref[2] == 1
+    r = P.newton(u0, maxit=4, reduction=1e-9, line_search={})
+    assert r[1] == 0 and r[5] == ([1], [1.0])
+    assert np.array_equal(r[0], ref[0]) and np.array_equal(r[4], ref[4])
+    r = P.newton(u0, maxit=4, reduction=1e-9, line_search=dict(lambda_start=2.0))
+    assert r[1] == 0 and r[5] == ([2], [1.0])
+    assert np.abs(r[0] - ref[0]).max() <= 1e-14 * np.abs(ref[0]).max()
+    r = P.newton(u0, maxit=4, reduction=1e-9,
+                 line_search=dict(lambda_start=2.0, max_steps=3, accept_best=1, check_all=1))
+    assert r[1] == 0 and r[5] == ([3], [1.0])
+    r = P.newton(u0, maxit=2, reduction=1e-9, line_search=dict(lambda_start=2.0, max_steps=1, accept_best=1))
+    assert r[1] == 1 and r[2] == 2 and r[5] == ([1, 1], [2.0, 2.0])
+    assert all(abs(x / r[4][0] - 1.0) < 1e-6 for x in r[4])
+    r = P.newton(u0, maxit=4, reduction=1e-9, line_search=dict(lambda_start=2.0, max_steps=1))
+    assert r[1] == 3 and r[2] == 0 and r[5] == ([1], [2.0])
+    r = P.newton(u0, maxit=4, reduction=1e-9,
+                 line_search=dict(lambda_start=2.0, max_steps=1, accept_best=1, max_defect=0.5 * ref[4][0]))
+    assert r[1] == 3 and r[5] == ([1], [2.0])

@@ -712,9 +712,45 @@ class AssembledOperator:
         self.disc = disc
 
 
+class StandardLineSearch:
+    """StandardLineSearch (line_search.h:115-400): the constructor's defaults
+    and its setters; handed to NewtonSolver.set_line_search."""
+
+    def __init__(self, max_steps=10, lambda_start=1.0, lambda_reduce=0.5, accept_best=False, check_all=False):
+        self.max_steps = int(max_steps)
+        self.lambda_start = float(lambda_start)
+        self.lambda_reduce = float(lambda_reduce)
+        self.suff_descent_factor = 0.25
+        self.accept_best = bool(accept_best)
+        self.check_all = bool(check_all)
+        self.max_defect = 1e10
+
+    def set_maximum_steps(self, steps):
+        self.max_steps = int(steps)
+
+    def set_lambda_start(self, start):
+        self.lambda_start = float(start)
+
+    def set_reduce_factor(self, factor):
+        self.lambda_reduce = float(factor)
+
+    def set_suff_descent_factor(self, factor):
+        self.suff_descent_factor = float(factor)
+
+    def set_accept_best(self, b):
+        self.accept_best = bool(b)
+
+    def set_check_all(self, b):
+        self.check_all = bool(b)
+
+    def set_maximum_defect(self, d):
+        self.max_defect = float(d)
+
+
 class NewtonSolver:
-    """NewtonSolver (newton.h:62) without line search: set_linear_solver,
-    set_convergence_check, init(AssembledOperator), prepare(u), apply(u)."""
+    """NewtonSolver (newton.h:62): set_linear_solver, set_convergence_check,
+    set_line_search (StandardLineSearch or None), init(AssembledOperator),
+    prepare(u), apply(u)."""
 
     def __init__(self, ctx):
         self.ctx = ctx
@@ -737,6 +773,22 @@ class NewtonSolver:
         self.conv = cc
         check(lib().ug4gb_newton_set_convergence_check(self.h, cc.max_steps, cc.min_defect, cc.rel_reduction),
               self.ctx.h)
+
+    def set_line_search(self, ls):
+        if ls is None:
+            check(lib().ug4gb_newton_clear_line_search(self.h), self.ctx.h)
+            return
+        check(lib().ug4gb_newton_set_line_search(self.h, ls.max_steps, ls.lambda_start, ls.lambda_reduce,
+                                                 ls.suff_descent_factor, int(ls.accept_best), int(ls.check_all),
+                                                 ls.max_defect), self.ctx.h)
+
+    def line_search_history(self):
+        """per Newton step of the last apply: (tries evaluated, accepted lambda)"""
+        cap = self.conv.max_steps + 1
+        tries = np.zeros(cap, np.int32)
+        lam = np.zeros(cap)
+        n = lib().ug4gb_newton_get_line_search_history(self.h, _ptr(tries), _ptr(lam), cap)
+        return tries[:max(n, 0)].tolist(), lam[:max(n, 0)].tolist()
 
     def init(self, op):
         d = op.disc if isinstance(op, AssembledOperator) else op

@@ -1,8 +1,8 @@
 // api_newton.cu -- NewtonSolver over the FV1 operator (host orchestration).
 //
 // Follows NewtonSolver::apply (lib_disc/operator/non_linear_operator/
-// newton_solver/newton_impl.h:171-340) without line search, Jacobian reuse
-// or update hooks:
+// newton_solver/newton_impl.h:171-340) without Jacobian reuse or update
+// hooks, optionally with StandardLineSearch:
 //   prepare(u)          Dirichlet values into u (AssembledOperator::prepare ->
 //                       DirichletBoundary::adjust_solution)
 //   d = N(u)            assemble_defect (stationary or time-discrete)
@@ -11,7 +11,17 @@
 //                       linear solver (and its multigrid) init(J);
 //                       apply(c, d) -- a failed linear solve ends Newton;
 //                       u -= c;  prepare(u);  d = N(u);  update(|d|)
+//                       (or the line search below in place of the update)
 //   post()
+// StandardLineSearch::search (line_search.h:186-400), from the defect norm
+// |d_old| of the step's start and s = u:
+//   for k = 1 .. max_steps:  u = u - lambda c;  prepare(u);  d = N(u);
+//       rho_k = |d| / |d_old|;  accepted (and done, unless check_all) when
+//       rho_k <= 1 - alpha |lambda|;  lambda *= reduce;
+//       at k = max_steps: without accept_best the search (and Newton) fails;
+//       else u = s - lambda_start reduce^best c for the first smallest rho,
+//       d = N(u), failing when |d| > max_defect;
+//       u = s before the next try.
 // with StdConvCheck's rules (convergence_check_impl.h:130-172): ended when the
 // defect is not a number, step >= max steps, defect < minimum defect or
 // defect / initial defect < reduction; converged by the last two.
@@ -42,6 +52,14 @@ struct ug4gb_newton {
     double d0 = 0.0, dcur = 0.0;
     std::vector<int> lin_steps;
     std::vector<double> defects;
+    // StandardLineSearch (off until set)
+    bool ls_on = false;
+    int ls_max = 10;
+    double ls_start = 1.0, ls_reduce = 0.5, ls_alpha = 0.25, ls_max_defect = 1e10;
+    bool ls_accept_best = false, ls_check_all = false;
+    ug4gb_vector *s = nullptr;
+    std::vector<int> ls_tries;          // per Newton step: tries evaluated
+    std::vector<double> ls_lambda;      // per Newton step: the lambda of the accepted u
 };
 
 namespace {
@@ -108,6 +126,53 @@ bool valid(double v)
     return v >= 2.2250738585072014e-308 && v <= 1.7976931348623157e308 && v == v;
 }
 
+// StandardLineSearch::search; u = s - lambda c with d = N(u) on return,
+// *norm = |d|.  Throws when the search fails.
+void line_search(ug4gb_newton *nw, ug4gb_vector *u, double norm_old, double *norm)
+{
+    ug4gb_ctx *ctx = nw->ctx;
+    check(ctx, ug4gb_vector_scale_add(nw->s, 1.0, u, 0.0, u));
+    double lambda = nw->ls_start, nrm = 0.0, accepted = nw->ls_start;
+    std::vector<double> rho;
+    int tries = 0;
+    for (int k = 1; k <= nw->ls_max; ++k) {
+        check(ctx, ug4gb_vector_scale_add(u, 1.0, u, -lambda, nw->c));
+        prepare(nw, u);
+        defect(nw, u);
+        check(ctx, ug4gb_vector_norm(nw->d, &nrm));
+        tries = k;
+        accepted = lambda;
+        rho.push_back(nrm / norm_old);
+        if (rho.back() <= 1.0 - nw->ls_alpha * std::fabs(lambda) && !nw->ls_check_all) break;
+        lambda *= nw->ls_reduce;
+        if (k == nw->ls_max) {
+            if (!nw->ls_accept_best) {
+                nw->ls_tries.push_back(tries);
+                nw->ls_lambda.push_back(accepted);
+                throw Error{UG4GB_ERR_NOT_CONVERGED, "NewtonSolver::apply: line search did not converge"};
+            }
+            size_t best = 0;
+            for (size_t i = 1; i < rho.size(); ++i)
+                if (rho[best] > rho[i]) best = i;
+            accepted = nw->ls_start * std::pow(nw->ls_reduce, (double)best);
+            check(ctx, ug4gb_vector_scale_add(u, 1.0, nw->s, -accepted, nw->c));
+            prepare(nw, u);
+            defect(nw, u);
+            check(ctx, ug4gb_vector_norm(nw->d, &nrm));
+            if (nrm > nw->ls_max_defect) {
+                nw->ls_tries.push_back(tries);
+                nw->ls_lambda.push_back(accepted);
+                throw Error{UG4GB_ERR_NOT_CONVERGED, "StandardLineSearch::search: maximum defect-limit is reached"};
+            }
+            break;
+        }
+        check(ctx, ug4gb_vector_scale_add(u, 1.0, nw->s, 0.0, nw->s));
+    }
+    nw->ls_tries.push_back(tries);
+    nw->ls_lambda.push_back(accepted);
+    *norm = nrm;
+}
+
 bool ended(const ug4gb_newton *nw)
 {
     if (!valid(nw->dcur)) return true;
@@ -147,6 +212,43 @@ int ug4gb_newton_set_convergence_check(ug4gb_newton *nw, int max_steps, double m
     return UG4GB_OK;
 }
 
+int ug4gb_newton_set_line_search(ug4gb_newton *nw, int max_steps, double lambda_start, double lambda_reduce,
+                                 double suff_descent_factor, int accept_best, int check_all, double max_defect)
+{
+    if (!nw) return UG4GB_ERR_INVALID;
+    if (max_steps < 1 || !(lambda_reduce > 0.0) || !std::isfinite(lambda_start) || !std::isfinite(max_defect)) {
+        nw->ctx->c.err = "StandardLineSearch: max_steps >= 1, lambda_reduce > 0, finite lambda_start and max_defect";
+        return UG4GB_ERR_INVALID;
+    }
+    nw->ls_on = true;
+    nw->ls_max = max_steps;
+    nw->ls_start = lambda_start;
+    nw->ls_reduce = lambda_reduce;
+    nw->ls_alpha = suff_descent_factor;
+    nw->ls_accept_best = accept_best != 0;
+    nw->ls_check_all = check_all != 0;
+    nw->ls_max_defect = max_defect;
+    return UG4GB_OK;
+}
+
+int ug4gb_newton_clear_line_search(ug4gb_newton *nw)
+{
+    if (!nw) return UG4GB_ERR_INVALID;
+    nw->ls_on = false;
+    return UG4GB_OK;
+}
+
+int ug4gb_newton_get_line_search_history(const ug4gb_newton *nw, int *tries, double *lambdas, int capacity)
+{
+    if (!nw || capacity < 0) return UG4GB_ERR_INVALID;
+    const int n = (int)nw->ls_tries.size();
+    for (int i = 0; i < capacity && i < n; ++i) {
+        if (tries) tries[i] = nw->ls_tries[i];
+        if (lambdas) lambdas[i] = nw->ls_lambda[i];
+    }
+    return n;
+}
+
 int ug4gb_newton_init(ug4gb_newton *nw, ug4gb_disc *d, ug4gb_timedisc *td)
 {
     if (!nw || (!d) == (!td)) return UG4GB_ERR_INVALID;
@@ -182,12 +284,16 @@ int ug4gb_newton_apply(ug4gb_newton *nw, ug4gb_vector *u)
         if (!nw->d || nw->d->n != nv) {
             ug4gb_vector_destroy(nw->d);
             ug4gb_vector_destroy(nw->c);
-            nw->d = nw->c = nullptr;
+            ug4gb_vector_destroy(nw->s);
+            nw->d = nw->c = nw->s = nullptr;
             check(ctx, ug4gb_vector_create(ctx, nv, &nw->d));
             check(ctx, ug4gb_vector_create(ctx, nv, &nw->c));
+            check(ctx, ug4gb_vector_create(ctx, nv, &nw->s));
         }
         nw->lin_steps.clear();
         nw->defects.clear();
+        nw->ls_tries.clear();
+        nw->ls_lambda.clear();
         prepare(nw, u);
         defect(nw, u);
         check(ctx, ug4gb_vector_norm(nw->d, &nw->d0));
@@ -206,11 +312,15 @@ int ug4gb_newton_apply(ug4gb_newton *nw, ug4gb_vector *u)
             if (lrc != UG4GB_OK) {
                 throw Error{lrc, std::string("NewtonSolver::apply: linear solver failed: ") + ctx->c.err};
             }
-            check(ctx, ug4gb_vector_scale_add(u, 1.0, u, -1.0, nw->c));
-            prepare(nw, u);
-            defect(nw, u);
             double nd = 0.0;
-            check(ctx, ug4gb_vector_norm(nw->d, &nd));
+            if (nw->ls_on) {
+                line_search(nw, u, nw->dcur, &nd);
+            } else {
+                check(ctx, ug4gb_vector_scale_add(u, 1.0, u, -1.0, nw->c));
+                prepare(nw, u);
+                defect(nw, u);
+                check(ctx, ug4gb_vector_norm(nw->d, &nd));
+            }
             nw->dcur = nd;
             nw->steps++;
             nw->defects.push_back(nd);
@@ -252,6 +362,7 @@ void ug4gb_newton_destroy(ug4gb_newton *nw)
     ug4gb_matrix_destroy(nw->J);
     ug4gb_vector_destroy(nw->d);
     ug4gb_vector_destroy(nw->c);
+    ug4gb_vector_destroy(nw->s);
     delete nw;
     ug4gb_ctx_release(ctx);
 }
