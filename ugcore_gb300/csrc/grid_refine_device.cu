@@ -522,7 +522,8 @@ int sort_unique_keys(Ctx &c, DevBuf<u64> &keys, int n, DevBuf<u64> &out)
     UG_CUDA(cudaStreamSynchronize(c.stream));
     if (m > 0) {
         u64 last = 0;
-        UG_CUDA(cudaMemcpy(&last, out.p + m - 1, sizeof(u64), cudaMemcpyDeviceToHost));
+        UG_CUDA(cudaMemcpyAsync(&last, out.p + m - 1, sizeof(u64), cudaMemcpyDeviceToHost, c.stream));
+        UG_CUDA(cudaStreamSynchronize(c.stream));
         if (last == kNoKey) --m;
     }
     return m;
@@ -551,6 +552,7 @@ void sort_pairs128(Ctx &c, DevBuf<u64> &hi, DevBuf<u64> &lo, DevBuf<int> &idx, i
     UG_LAUNCH(c, k_gather_pairs, grid1(n), 256, 0, hi.p, lo.p, idx.p, n, h2.p, k2.p);
     UG_CUDA(cudaMemcpyAsync(hi.p, h2.p, sizeof(u64) * (size_t)n, cudaMemcpyDeviceToDevice, c.stream));
     UG_CUDA(cudaMemcpyAsync(lo.p, k2.p, sizeof(u64) * (size_t)n, cudaMemcpyDeviceToDevice, c.stream));
+    UG_CUDA(cudaStreamSynchronize(c.stream));   // before the temporaries are freed
 }
 
 // indices of the first entry of each run of equal (hi, lo); returns the count
@@ -621,6 +623,7 @@ void refine_device(Ctx &c, const Level &C, const DevDir &Cd, Level &F, DevDir &F
         FH.alloc(nqf > 0 ? nqf : 1);
         FL.alloc(nqf > 0 ? nqf : 1);
         UG_LAUNCH(c, k_gather_pairs, grid1(nqf), 256, 0, hi.p, lo.p, sel.p, nqf, FH.p, FL.p);
+        UG_CUDA(cudaStreamSynchronize(c.stream));   // before the temporaries are freed
     } else if (t == UG4GB_QUAD) {
         nqf = ne;
     }
@@ -719,6 +722,7 @@ void refine_device(Ctx &c, const Level &C, const DevDir &Cd, Level &F, DevDir &F
         Fd.n_faces = first_of_runs(c, hi, lo, idx, n, sel);
         Fd.faces.alloc(Fd.n_faces > 0 ? Fd.n_faces : 1);
         UG_LAUNCH(c, k_gather_faces, grid1(Fd.n_faces), 256, 0, faces.p, sel.p, Fd.n_faces, Fd.faces.p);
+        UG_CUDA(cudaStreamSynchronize(c.stream));   // before the temporaries are freed
     } else {
         Fd.n_faces = 0;
         Fd.faces.alloc(1);
