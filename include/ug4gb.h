@@ -392,6 +392,12 @@ UG4GB_API int ug4gb_newton_get_history(const ug4gb_newton *nw, double *defects, 
 UG4GB_API int ug4gb_newton_set_line_search(ug4gb_newton *nw, int max_steps, double lambda_start,
                                           double lambda_reduce, double suff_descent_factor, int accept_best,
                                           int check_all, double max_defect);
+/* NewtonSolver::set_reassemble_J_freq (newton.h:156, newton_impl.h:246): the
+   jacobian is assembled in Newton steps 0, freq, 2 freq, ... (0: every step);
+   the linear solver and its multigrid are initialised every step, as there */
+UG4GB_API int ug4gb_newton_set_reassemble_J_freq(ug4gb_newton *nw, int freq);
+/* jacobian assemblies of the last apply */
+UG4GB_API int ug4gb_newton_num_jacobian_assemblies(const ug4gb_newton *nw);
 UG4GB_API int ug4gb_newton_clear_line_search(ug4gb_newton *nw);
 /* per Newton step of the last apply: line-search tries evaluated and the
    lambda of the accepted solution; returns the number of steps recorded */

@@ -270,3 +270,33 @@ def test_newton_line_search_failures(ctx, oracle_lib):
     assert nw.line_search_history() == ([], [])
     with pytest.raises(ug.UG4GBError):
         nw.set_line_search(ug.StandardLineSearch(max_steps=0))
+
+
+@pytest.mark.parametrize("freq,expected", [(0, None), (1, None), (2, "half"), (100, 1)])
+def test_newton_reassemble_jacobian_frequency(ctx, oracle_lib, freq, expected):
+    """set_reassemble_J_freq: the jacobian is assembled in steps 0, k, 2k, ...
+    only; the FV1 operator is linear, so the reused jacobian is the same
+    matrix and the iterates are bit-identical to reassembling every step"""
+    import ugcore_gb300 as ug
+    cfg, p, op = _setup(ctx, oracle_lib, "c1", dict(nref=3, precision="fp64"))
+    cfg = dict(cfg, rel_red=1e-6)
+    u0 = _random(p, 6)
+    res = []
+    for f in (0, freq):
+        nw, _ = _newton(ctx, p, cfg)
+        nw.set_reassemble_J_freq(f)
+        nw.init(ug.AssembledOperator(p.disc))
+        u = ug.GPUVector(ctx, p.n).copy_from(u0)
+        assert nw.apply(u)
+        res.append((u.numpy(), nw.history(), nw.stats()["steps"], nw.num_jacobian_assemblies()))
+    (u_a, h_a, s_a, n_a), (u_b, h_b, s_b, n_b) = res
+    assert s_a >= 2 and s_a == s_b and n_a == s_a
+    assert np.array_equal(u_a.view(np.int64), u_b.view(np.int64)) and np.array_equal(h_a, h_b)
+    if expected is None:
+        assert n_b == s_b
+    elif expected == "half":
+        assert n_b == (s_b + 1) // 2
+    else:
+        assert n_b == 1
+    with pytest.raises(ug.UG4GBError):
+        nw.set_reassemble_J_freq(-1)

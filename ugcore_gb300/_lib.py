@@ -125,6 +125,8 @@ _SIGS = {
     "ug4gb_newton_get_history": (I, [P, P, I]),
     "ug4gb_newton_set_line_search": (I, [P, I, D, D, D, I, I, D]),
     "ug4gb_newton_clear_line_search": (I, [P]),
+    "ug4gb_newton_set_reassemble_J_freq": (I, [P, I]),
+    "ug4gb_newton_num_jacobian_assemblies": (I, [P]),
     "ug4gb_newton_get_line_search_history": (I, [P, P, P, I]),
     "ug4gb_newton_destroy": (None, [P]),
     "ug4gb_gmg_level_info": (I, [P, I, P, P]),

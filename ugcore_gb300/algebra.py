@@ -782,6 +782,13 @@ class NewtonSolver:
                                                  ls.suff_descent_factor, int(ls.accept_best), int(ls.check_all),
                                                  ls.max_defect), self.ctx.h)
 
+    def set_reassemble_J_freq(self, freq):
+        """assemble the jacobian only in steps 0, freq, 2 freq, ... (0: every step)"""
+        check(lib().ug4gb_newton_set_reassemble_J_freq(self.h, int(freq)), self.ctx.h)
+
+    def num_jacobian_assemblies(self):
+        return lib().ug4gb_newton_num_jacobian_assemblies(self.h)
+
     def line_search_history(self):
         """per Newton step of the last apply: (tries evaluated, accepted lambda)"""
         cap = self.conv.max_steps + 1

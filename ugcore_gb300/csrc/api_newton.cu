@@ -7,7 +7,8 @@
 //                       DirichletBoundary::adjust_solution)
 //   d = N(u)            assemble_defect (stationary or time-discrete)
 //   start(|d|)
-//   while not ended:    c = 0;  J = N'(u) (assemble_jacobian);
+//   while not ended:    c = 0;  J = N'(u) (assemble_jacobian; with
+//                       set_reassemble_J_freq(k > 0) only in steps 0, k, 2k, ...);
 //                       linear solver (and its multigrid) init(J);
 //                       apply(c, d) -- a failed linear solve ends Newton;
 //                       u -= c;  prepare(u);  d = N(u);  update(|d|)
@@ -49,6 +50,8 @@ struct ug4gb_newton {
     ug4gb_matrix *J = nullptr;
     ug4gb_vector *d = nullptr, *c = nullptr;
     int steps = 0;
+    int j_freq = 0;                    // set_reassemble_J_freq (0: every step)
+    int j_count = 0;                   // jacobian assemblies in the last apply
     double d0 = 0.0, dcur = 0.0;
     std::vector<int> lin_steps;
     std::vector<double> defects;
@@ -231,6 +234,18 @@ int ug4gb_newton_set_line_search(ug4gb_newton *nw, int max_steps, double lambda_
     return UG4GB_OK;
 }
 
+int ug4gb_newton_set_reassemble_J_freq(ug4gb_newton *nw, int freq)
+{
+    if (!nw || freq < 0) return UG4GB_ERR_INVALID;
+    nw->j_freq = freq;
+    return UG4GB_OK;
+}
+
+int ug4gb_newton_num_jacobian_assemblies(const ug4gb_newton *nw)
+{
+    return nw ? nw->j_count : UG4GB_ERR_INVALID;
+}
+
 int ug4gb_newton_clear_line_search(ug4gb_newton *nw)
 {
     if (!nw) return UG4GB_ERR_INVALID;
@@ -294,6 +309,7 @@ int ug4gb_newton_apply(ug4gb_newton *nw, ug4gb_vector *u)
         nw->defects.clear();
         nw->ls_tries.clear();
         nw->ls_lambda.clear();
+        nw->j_count = 0;
         prepare(nw, u);
         defect(nw, u);
         check(ctx, ug4gb_vector_norm(nw->d, &nw->d0));
@@ -302,7 +318,10 @@ int ug4gb_newton_apply(ug4gb_newton *nw, ug4gb_vector *u)
         nw->defects.push_back(nw->d0);
         while (!ended(nw)) {
             check(ctx, ug4gb_vector_set(nw->c, 0.0));
-            jacobian(nw);
+            if (nw->j_freq == 0 || nw->steps % nw->j_freq == 0) {
+                jacobian(nw);
+                nw->j_count++;
+            }
             if (nw->lin->pre) check(ctx, ug4gb_gmg_init(nw->lin->pre, nw->J));
             check(ctx, ug4gb_solver_init(nw->lin, nw->J));
             const int lrc = ug4gb_solver_apply(nw->lin, nw->c, nw->d);
