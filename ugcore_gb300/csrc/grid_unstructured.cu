@@ -34,9 +34,9 @@
 // refine() below is the host statement of these rules (it also serves the
 // host-only ug4gb_io_ugx_level); the hierarchies the solvers use are refined
 // on the device by grid_refine_device.cu with the same numbering and the same
-// (explicitly rounded) arithmetic.  Element and vertex colourings (greedy, in
-// index order) give the assembly its race-free scatter order and the
-// multicolour Gauss-Seidel its colours.
+// (explicitly rounded) arithmetic.  A greedy element colouring (in index
+// order) gives the assembly its race-free scatter order; the colour-ordered
+// smoothers colour each level's operator graph themselves.
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -497,8 +497,7 @@ void refine(const HostLevel &C, HostLevel &F)
     dedupe(F);
 }
 
-// greedy colourings in index order: elements (no shared vertex within a
-// colour) and vertices (no shared element within a colour)
+// greedy colouring in index order: elements, no shared vertex within a colour
 void colour_elements(const HostLevel &L, std::vector<int> &off, std::vector<int> &list)
 {
     const int W = 8;   // 512 colours at most
@@ -526,37 +525,6 @@ void colour_elements(const HostLevel &L, std::vector<int> &off, std::vector<int>
     for (int e = 0; e < L.ne; ++e) list[cur[col[e]]++] = e;
 }
 
-int colour_vertices(const HostLevel &L, std::vector<int> &col)
-{
-    // vertex -> elements
-    std::vector<int> voff((size_t)L.nv + 1, 0), vel((size_t)L.ne * L.k);
-    for (int a = 0; a < L.ne * L.k; ++a) ++voff[L.elems[a] + 1];
-    for (int v = 0; v < L.nv; ++v) voff[v + 1] += voff[v];
-    std::vector<int> cur(voff.begin(), voff.end() - 1);
-    for (int e = 0; e < L.ne; ++e)
-        for (int i = 0; i < L.k; ++i) vel[cur[L.elems[(size_t)e * L.k + i]]++] = e;
-    col.assign(L.nv, -1);
-    int ncol = 0;
-    std::vector<int> seen;
-    for (int v = 0; v < L.nv; ++v) {
-        seen.clear();
-        for (int a = voff[v]; a < voff[v + 1]; ++a) {
-            const int *ev = &L.elems[(size_t)vel[a] * L.k];
-            for (int i = 0; i < L.k; ++i)
-                if (ev[i] != v && col[ev[i]] >= 0) seen.push_back(col[ev[i]]);
-        }
-        std::sort(seen.begin(), seen.end());
-        int c = 0;
-        for (int s : seen) {
-            if (s == c) ++c;
-            else if (s > c) break;
-        }
-        col[v] = c;
-        ncol = std::max(ncol, c + 1);
-    }
-    return ncol;
-}
-
 void upload(Ctx &c, const HostLevel &H, Level &L)
 {
     L.elem_type = H.elem_type;
@@ -582,10 +550,6 @@ void upload(Ctx &c, const HostLevel &H, Level &L)
     colour_elements(H, L.ecol_off, list);
     L.ecol.alloc(std::max<size_t>(list.size(), 1));
     copy_in(c, L.ecol.p, list.data(), sizeof(int) * list.size());
-    std::vector<int> vcol;
-    L.ncolors = colour_vertices(H, vcol);
-    L.color.alloc(H.nv);
-    copy_in(c, L.color.p, vcol.data(), sizeof(int) * vcol.size());
     UG_CUDA(cudaStreamSynchronize(c.stream));
 }
 
@@ -878,7 +842,7 @@ void upload_dirichlet(Ctx &c, const HostLevel &H, DevDir &D)
     copy_in(c, D.edir.p, H.edir.data(), H.edir.size());
 }
 
-// element and vertex colourings of a level refined on the device
+// element colouring of a level refined on the device
 void colour_level(Ctx &c, Level &L)
 {
     HostLevel H;
@@ -893,10 +857,6 @@ void colour_level(Ctx &c, Level &L)
     colour_elements(H, L.ecol_off, list);
     L.ecol.alloc(std::max<size_t>(list.size(), 1));
     copy_in(c, L.ecol.p, list.data(), sizeof(int) * list.size());
-    std::vector<int> vcol;
-    L.ncolors = colour_vertices(H, vcol);
-    L.color.alloc(H.nv);
-    copy_in(c, L.color.p, vcol.data(), sizeof(int) * vcol.size());
     UG_CUDA(cudaStreamSynchronize(c.stream));
 }
 
@@ -904,8 +864,8 @@ void colour_level(Ctx &c, Level &L)
 
 // Hierarchy of `nref` refinements of level 0: level 0 is uploaded, every
 // finer level is refined on the device from the one below it (the same
-// numbering and arithmetic as refine() above); only the greedy colourings,
-// sequential in index order, run on the host.
+// numbering and arithmetic as refine() above); only the greedy element colouring,
+// sequential in index order, runs on the host.
 void build_unstructured(Ctx &c, HostLevel L0, int nref, std::vector<Level> &lev)
 {
     lev.clear();
