@@ -141,3 +141,25 @@ def test_c4_mixed_adjoint_full_size(ctx):
     assert ast["converged"], ast
     gf = p.disc.grad_source(p.lam)
     assert np.isfinite(gf).all() and np.abs(gf).max() > 0
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_repeated_gradients_reuse_the_adjoint_set_up(ctx, precision):
+    """a gradient after an operator update re-initialises the kept transposed
+    multigrid and solver: bit-identical to a fresh problem's gradient"""
+    import torch
+    from ugcore_gb300 import adjoint
+
+    def grad(prob, m, f):
+        mm = m.clone().requires_grad_(True)
+        u = adjoint.fv1_solve(mm, f, prob)
+        (0.5 * (u ** 2).sum()).backward()
+        return mm.grad.cpu().numpy()
+
+    cfg, prob, m_true, f = _c3(ctx, 4, precision, 1e-10)
+    g1 = grad(prob, m_true * 0.7, f)
+    g2 = grad(prob, m_true * 1.3, f)
+    _, fresh, _, _ = _c3(ctx, 4, precision, 1e-10)
+    g2_fresh = grad(fresh, m_true * 1.3, f)
+    assert not np.array_equal(g1, g2)
+    assert np.array_equal(g2.view(np.int64), g2_fresh.view(np.int64))

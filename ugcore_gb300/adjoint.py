@@ -37,7 +37,7 @@ class DifferentiableProblem(problems.Problem):
         self.disc.assemble_linear(self.A, self.b)
         self.gmg.init(self.A)
         self.solver.init(self.A)
-        self.AT = None
+        self.invalidate_adjoint()
 
     def solve_into(self, out):
         """solve and copy u into the CUDA tensor out"""

@@ -466,14 +466,19 @@ struct GmgT : GmgBase {
     }
 };
 
+// reuse: the multigrid of the previous init with the same hierarchy and
+// structural settings (ug4gb_gmg_init checks): its level buffers and its
+// transfers P, R (which depend on the grid only) are kept; the operators,
+// smoother data and base factorisation are rebuilt.
 template <class V>
-static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
+static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reuse = nullptr)
 {
     Ctx &c = m->ctx->c;
     const ug4gb_grid *g = m->disc->g;
     int nl = (int)g->lev.size();
-    auto *G = new GmgT<V>;
+    auto *G = reuse ? reuse : new GmgT<V>;
     std::unique_ptr<GmgT<V>> guard(G);
+    const bool keep_transfers = reuse != nullptr;
     G->base = m->base;
     G->nu1 = m->nu1;
     G->nu2 = m->nu2;
@@ -513,7 +518,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
             UG_CUDA(cudaStreamSynchronize(c.stream));
             G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
             if (l > m->base) {
-                G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
+                if (!keep_transfers) G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
                 if (L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI)
                     L.sweep2 = sweep2_prepare<V>(c, L.At, L.gp);
             }
@@ -525,7 +530,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         csr_copy(c, A_top->A, G->lev[nl - 1].A);
         if (m->transposed) transpose_level(nl - 1);
         for (int l = nl - 1; l > m->base; --l) {
-            G->setup_transfers(c, G->lev[l], g->lev[l], g->lev[l - 1]);
+            if (!keep_transfers) G->setup_transfers(c, G->lev[l], g->lev[l], g->lev[l - 1]);
             csr_rap(c, G->lev[l].R, G->lev[l].A, G->lev[l].P, G->lev[l - 1].A);
         }
         for (int l = m->base; l < nl; ++l) {
@@ -652,10 +657,20 @@ int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
     if (!m || !A_top) return UG4GB_ERR_INVALID;
     return guarded(m->ctx, [&] {
         drop_graph(m);
-        m->impl.reset();
         m->gen++;
-        if (m->precision == UG4GB_PREC_FP64) m->impl.reset(build_gmg<double>(m, A_top));
-        else m->impl.reset(build_gmg<float>(m, A_top));
+        // a re-init with the same hierarchy and structure (typically a new
+        // operator every Newton, time or optimisation step) keeps the level
+        // buffers and the transfers
+        const GmgKey key{m->disc->g, (int)m->disc->g->lev.size(), m->base, m->smoother, m->damp, m->rap,
+                         m->transposed, m->precision, m->ctx->c.allow_dia ? 1 : 0};
+        GmgBase *old = (m->impl && m->built == key) ? m->impl.release() : nullptr;
+        m->impl.reset();
+        m->built = GmgKey{};
+        if (m->precision == UG4GB_PREC_FP64)
+            m->impl.reset(build_gmg<double>(m, A_top, static_cast<GmgT<double> *>(old)));
+        else
+            m->impl.reset(build_gmg<float>(m, A_top, static_cast<GmgT<float> *>(old)));
+        m->built = key;
         m->n_top = A_top->A.nrows;
     });
 }

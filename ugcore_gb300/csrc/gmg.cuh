@@ -145,6 +145,20 @@ struct ug4gb_timedisc {
     }
 };
 
+// what a multigrid's structure depends on: a re-init with the same key may
+// keep the previous level buffers and transfers
+struct GmgKey {
+    const ug4gb_grid *g = nullptr;
+    int nl = 0, base = 0, smoother = 0;
+    double damp = 0.0;
+    int rap = 0, transposed = 0, precision = 0, allow_dia = 0;
+    bool operator==(const GmgKey &o) const
+    {
+        return g && g == o.g && nl == o.nl && base == o.base && smoother == o.smoother && damp == o.damp &&
+               rap == o.rap && transposed == o.transposed && precision == o.precision && allow_dia == o.allow_dia;
+    }
+};
+
 struct ug4gb_gmg {
     ug4gb_ctx *ctx = nullptr;
     ug4gb_disc *disc = nullptr;
@@ -156,6 +170,7 @@ struct ug4gb_gmg {
     int rap = 0;                 // coarse operators as Galerkin products R A P (set_rap)
     ug4gb_timedisc *td = nullptr;  // coarse levels assembled as this time discretisation's jacobian
     std::unique_ptr<ug4gb::GmgBase> impl;
+    GmgKey built;                // the structure impl was built for
     int n_top = 0;
     int gen = 0;                 // incremented by every init (invalidates captured graphs)
     // standalone apply graph

@@ -152,17 +152,27 @@ class Problem:
 
     # ---- adjoint --------------------------------------------------------
     def adjoint_setup(self):
-        if getattr(self, "AT", None) is None:
+        """A^T, the transposed multigrid and its solver for the current
+        operator; the objects are kept across operator updates and only
+        re-initialised (invalidate_adjoint)."""
+        if getattr(self, "_adj_ready", False):
+            return
+        if getattr(self, "gmgT", None) is None:
             self.AT = GPUSparseMatrix(self.ctx)
-            self.disc.adjoint_operator(self.A, self.AT)
             self.gmgT = self._make_gmg(transposed=True)
-            self.gmgT.init(self.A)
             self.solverT = (CG if self.cfg["solver"] == "cg" else BiCGStab)(self.ctx)
             self.solverT.set_preconditioner(self.gmgT)
             self.solverT.set_convergence_check(StdConvCheck(self.cfg["maxit"], self.cfg["min_defect"],
                                                             self.cfg["rel_red"]))
-            self.solverT.init(self.AT)
             self.lam = GPUVector(self.ctx, self.n)
+        self.disc.adjoint_operator(self.A, self.AT)
+        self.gmgT.init(self.A)
+        self.solverT.init(self.AT)
+        self._adj_ready = True
+
+    def invalidate_adjoint(self):
+        """the operator changed: the next adjoint solve re-initialises"""
+        self._adj_ready = False
 
     def adjoint_solve(self, g):
         """lambda = A^{-T} g (g = dJ/du, Dirichlet entries ignored)."""
