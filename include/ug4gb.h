@@ -180,14 +180,17 @@ UG4GB_API int ug4gb_vector_maxnorm(const ug4gb_vector *v, double *out);
 UG4GB_API int ug4gb_vector_get_values(const ug4gb_vector *v, int n, const int *idx, double *vals);
 UG4GB_API int ug4gb_vector_set_values(ug4gb_vector *v, int n, const int *idx, const double *vals);
 /* (a, b) of two FP64 device arrays of the current device, for callers that
-   may not allocate device memory (no context needed; nothing is allocated,
-   not even on first use).  Has no counterpart in the reference.  The result
-   goes to *result, a device pointer, in stream order on `stream`; nothing is
-   synchronised.  Reduction scratch is one static array of the library per
-   device, so n <= UG4GB_DOT_NOALLOC_MAX_N (else UG4GB_ERR_INVALID), and calls
-   that overlap in time on one device race on it: order them on one stream.
-   The first call on a device sets the scratch up; make it before any stream
-   capture.  On failure a message goes to err (may be NULL). */
+   may not allocate device memory (no context needed).  Has no counterpart in
+   the reference.  The library allocates nothing for it, ever; but the first
+   call in a CUDA context can make the CUDA runtime load the library's device
+   code (with the 64 KiB static scratch) onto the device, so a caller with a
+   strict no-allocation phase makes one warm-up call (n = 1) before that phase
+   and before any stream capture.  The scratch exists once per CUDA context
+   (its address is looked up once per context).  The result goes to *result,
+   a device pointer, in stream order on `stream`; nothing is synchronised.
+   n <= UG4GB_DOT_NOALLOC_MAX_N (else UG4GB_ERR_INVALID), and calls that
+   overlap in time on one device race on the shared scratch: order them on
+   one stream.  On failure a message goes to err (may be NULL). */
 #define UG4GB_DOT_NOALLOC_MAX_N 67108864
 UG4GB_API int ug4gb_vector_dot_noalloc(const double *a, const double *b, int64_t n, double *result, void *stream,
                                        char *err, int err_capacity);

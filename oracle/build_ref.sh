@@ -2,12 +2,18 @@
 # Builds oracle/_ref/ref_driver: ugcore's own algebra classes compiled from
 # the reference sources where they lie (nothing is copied into this repo),
 # driven by ref_driver.cpp and the oracle's restated hierarchy/assembly.
-# Needs the reference tree (default /root/reference); prints a note and exits
-# 0 without building when it is absent (e.g. on a machine without it).
+# Needs the reference tree (UG4_REFERENCE, else /root/reference); prints a
+# note and exits 0 without building when it is absent (e.g. on a machine
+# without it).  "build_ref.sh --where" only prints the tree's location (empty
+# when absent): the one place tests and the build entry learn where it is.
 set -e
 REF=${UG4_REFERENCE:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
+if [ "$1" = "--where" ]; then
+    if [ -d "$REF/ugbase/lib_algebra" ]; then echo "$REF"; fi
+    exit 0
+fi
 if [ ! -d "$REF/ugbase/lib_algebra" ]; then
     echo "build_ref: reference tree not found at $REF; skipping"
     exit 0

@@ -44,6 +44,16 @@ def assert_crs_equal(a, b, rtol=VAL_RTOL, what="matrix"):
         what, int(bad.sum()), rtol, float((err / np.maximum(scale, 1e-300)).max()))
 
 
+def reference_tree():
+    """location of the ugcore source tree, or None where it is absent (asked
+    of oracle/build_ref.sh, the recipe that compiles it)"""
+    import subprocess
+    r = subprocess.run(["sh", os.path.join(os.path.dirname(GOLDEN), "..", "oracle", "build_ref.sh"), "--where"],
+                       capture_output=True, text=True)
+    where = r.stdout.strip()
+    return where if r.returncode == 0 and where else None
+
+
 def load_golden(name):
     path = os.path.join(GOLDEN, name + ".npz")
     return dict(np.load(path)) if os.path.exists(path) else None

@@ -114,8 +114,9 @@ def test_ugcore_glue_instantiates_reference_solvers(tmp_path):
     ugcore's CG takes the library's multigrid (ug4gb_preconditioner.h) as its
     ILinearIterator preconditioner (where the ugcore tree is present; four
     empty stand-ins replace headers that need Boost)."""
-    ref = os.environ.get("UG4_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "ugbase", "lib_algebra")):
+    from helpers import reference_tree
+    ref = reference_tree()
+    if ref is None:
         pytest.skip("ugcore source tree not present")
     cxx = shutil.which("g++")
     if not cxx:

@@ -1,9 +1,14 @@
 """ug4gb_vector_dot_noalloc, the dot product that allocates no device memory,
 called through the C ABI and checked against ug4gb_vector_dot.
 
+Callers that cannot allocate (an application whose allocator owns the GPU's
+memory, or a phase where cudaMalloc/cudaFree must not run) use it; besides
+the values, the tests check that a warmed call leaves the device's free
+memory unchanged and that the largest n the static scratch allows works.
+
 The two entry points sum the same products in a different order, so they
 are compared within 1e-12 * sum_i |a_i b_i| (rounding of an FP64 sum of up to
-a few million terms).  Two calls in a row must give bit-identical results:
+67 million terms, summed in blocks of 8192).  Two calls in a row must give bit-identical results:
 the static scratch has to be left clean by the first call.  This file runs
 last so that it also sees the library after every other test has used it.
 """
@@ -91,3 +96,35 @@ def test_noalloc_dot_edge_cases(ctx):
     assert rc == _lib.OK, msg
     torch.cuda.synchronize()
     assert res.item() == 16.0
+
+
+def test_noalloc_dot_at_the_scratch_limit_allocates_nothing(ctx):
+    """n = UG4GB_DOT_NOALLOC_MAX_N (every partial slot of the scratch in use,
+    two vectors of 512 MiB): matches ug4gb_vector_dot, two calls in a row are
+    bit-identical, and the device's free memory is the same before and after
+    the (warmed) calls"""
+    import torch
+    from ugcore_gb300 import _lib
+    L = _lib.lib()
+    n = MAX_N
+    g = torch.Generator(device="cuda").manual_seed(99)
+    a = torch.rand(n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    b = torch.rand(n, dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    res = torch.full((2,), float("nan"), dtype=torch.float64, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    rc, msg = _noalloc(L, a, b, 1, res[0:1], stream)            # warm-up call (module load, look-up)
+    assert rc == _lib.OK, msg
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    rc0, msg0 = _noalloc(L, a, b, n, res[0:1], stream)
+    rc1, msg1 = _noalloc(L, a, b, n, res[1:2], stream)
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert rc0 == _lib.OK, msg0
+    assert rc1 == _lib.OK, msg1
+    assert free1 == free0, (free0, free1)
+    r = res.cpu().numpy()
+    assert r[0] == r[1]
+    ref = _reference_dot(L, ctx, a, b)
+    scale = float((a * b).abs().sum())
+    assert abs(r[0] - ref) <= TOL * scale, (r[0], ref)

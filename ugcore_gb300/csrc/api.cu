@@ -1,4 +1,5 @@
 // api.cu -- C ABI: context, grid hierarchy, vectors, matrices.
+#include <atomic>
 #include <cstring>
 
 #include "gmg.cuh"
@@ -221,6 +222,12 @@ int ug4gb_profile_end(ug4gb_ctx *ctx, char *buf, int cap)
 }
 
 // ------------------------------------------------------------------ grid --
+uint64_t ug4gb_next_grid_uid()
+{
+    static std::atomic<uint64_t> next{1};
+    return next.fetch_add(1, std::memory_order_relaxed);
+}
+
 int ug4gb_grid_create_structured(ug4gb_ctx *ctx, int elem_type, int mx, int my, int mz, int nref, ug4gb_grid **out)
 {
     if (!ctx || !out) return UG4GB_ERR_INVALID;
@@ -417,7 +424,7 @@ int ug4gb_matrix_set_csr(ug4gb_matrix *m, int nrows, int ncols, int64_t nnz, con
         copy_in(c, m->A.val.p, val, sizeof(double) * (size_t)nnz);
         UG_CUDA(cudaStreamSynchronize(c.stream));
         m->op_valid = false;
-        m->pattern_grid = nullptr;
+        m->pattern_grid = 0;
         m->pattern_level = -1;
     });
 }
@@ -474,7 +481,7 @@ int ug4gb_matrix_set_as_transpose_of(ug4gb_matrix *T, const ug4gb_matrix *B, int
         csr_transpose(T->ctx->c, B->A, T->A, keep_zeros != 0);
         UG_CUDA(cudaStreamSynchronize(T->ctx->c.stream));
         T->op_valid = false;
-        T->pattern_grid = nullptr;
+        T->pattern_grid = 0;
         T->pattern_level = -1;
     });
 }

@@ -144,7 +144,7 @@ int ug4gb_matrix_resize_and_clear(ug4gb_matrix *A, int num_rows, int num_cols)
         UG_CUDA(cudaMemsetAsync(A->A.rowptr.p, 0, sizeof(int) * (size_t)(num_rows + 1), c.stream));
         UG_CUDA(cudaStreamSynchronize(c.stream));
         A->op_valid = false;
-        A->pattern_grid = nullptr;
+        A->pattern_grid = 0;
         A->pattern_level = -1;
     });
 }

@@ -55,9 +55,9 @@ void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const T
     Ctx &c = d->ctx->c;
     const Level &L = d->g->lev[level];
     const double *K = disc_coefficients(d, level);
-    if (A->pattern_grid != (const void *)d->g || A->pattern_level != level) {
+    if (A->pattern_grid != d->g->uid || A->pattern_level != level) {
         csr_from_elements(c, L, A->A);
-        A->pattern_grid = d->g;
+        A->pattern_grid = d->g->uid;
         A->pattern_level = level;
     } else {
         UG_CUDA(cudaMemsetAsync(A->A.val.p, 0, sizeof(double) * (size_t)A->A.nnz, c.stream));
@@ -428,7 +428,7 @@ int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A,
         launch_dirichlet(c, d->g->lev[level], AT->A, nullptr);
         UG_CUDA(cudaStreamSynchronize(c.stream));
         AT->op_valid = false;
-        AT->pattern_grid = nullptr;
+        AT->pattern_grid = 0;
         AT->pattern_level = -1;
     });
 }

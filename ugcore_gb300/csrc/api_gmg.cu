@@ -661,7 +661,7 @@ int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         // a re-init with the same hierarchy and structure (typically a new
         // operator every Newton, time or optimisation step) keeps the level
         // buffers and the transfers
-        const GmgKey key{m->disc->g, (int)m->disc->g->lev.size(), m->base, m->smoother, m->damp, m->rap,
+        const GmgKey key{m->disc->g->uid, (int)m->disc->g->lev.size(), m->base, m->smoother, m->damp, m->rap,
                          m->transposed, m->precision, m->ctx->c.allow_dia ? 1 : 0};
         GmgBase *old = (m->impl && m->built == key) ? m->impl.release() : nullptr;
         m->impl.reset();

@@ -15,13 +15,21 @@
 // limited to kChunk * kMaxBlocks = 67,108,864 elements; larger n is rejected
 // with UG4GB_ERR_INVALID before anything is launched.
 //
-// Set-up: the first call on each device (with that device current) looks up
-// the device address of the scratch with cudaGetSymbolAddress and clears the
-// block counter on the caller's stream.  That first call can make the CUDA
-// runtime load this library's kernels onto the device, so it should come
-// before the caller begins any stream capture.
+// Set-up: the first call in each CUDA context (normally the primary context
+// of a device, with that device current) looks up the device address of the
+// scratch with cudaGetSymbolAddress.  The address is cached per context, by
+// the context's process-unique id (cuCtxGetId), so a context created after
+// cudaDeviceReset or by cuCtxCreate gets its own look-up.  That first call
+// can make the CUDA runtime load this library's kernels onto the device
+// (the runtime, not this library, then places the code and the 64 KiB array
+// in device memory), so a caller with a strict no-allocation phase makes one
+// call (n = 1 is enough) before it, and before any stream capture.
 //
-// Concurrency: all calls on one device share the one scratch array.  Calls
+// Every call clears the block counter on the caller's stream before its
+// launch (a memset, no allocation), so a call cut short by an earlier error
+// cannot leave a count behind that corrupts the next result.
+//
+// Concurrency: all calls in one context share the one scratch array.  Calls
 // that overlap in time on that device (two streams, or two host threads
 // without ordering between them) race on it and give wrong results; order
 // them on one stream or synchronise between them.
@@ -30,6 +38,7 @@
 // adds the partials in block order, so the value depends only on n and the
 // data, not on the GPU or on timing.  It is a different summation order than
 // ug4gb_vector_dot's grid-stride reduction, so the two agree to rounding.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdarg>
@@ -46,15 +55,14 @@ constexpr int kChunk = 8192;          // elements per block (32 per thread)
 constexpr int kMaxBlocks = 8192;      // partial slots in the scratch
 constexpr int64_t kMaxN = (int64_t)kChunk * kMaxBlocks;
 static_assert(kMaxN == UG4GB_DOT_NOALLOC_MAX_N, "header limit out of date");
-constexpr int kMaxDevices = 64;
 
 struct DotScratch {
     double partial[kMaxBlocks];
     unsigned int counter;             // blocks finished; must read 0 when a call starts
 };
 
-// zero-initialised when the module is loaded; the set-up clears the counter
-// again, and the last block of every call resets it to 0
+// zero-initialised when the module is loaded; every call clears the counter
+// on its stream before the launch, and the last block resets it to 0
 static __device__ __align__(256) DotScratch g_dot_scratch;
 
 __device__ __forceinline__ double warp_sum64(double v)
@@ -102,7 +110,41 @@ __global__ void __launch_bounds__(kThreads) k_dot_static(const double *__restric
 }
 
 std::mutex g_setup_mutex;
-DotScratch *g_scratch[kMaxDevices] = {};
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    DotScratch *p;
+};
+constexpr int kMaxContexts = 64;
+ScratchEntry g_scratch[kMaxContexts] = {};
+int g_num_scratch = 0;
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+// process-unique id of the current context (0 if unavailable)
+unsigned long long current_context_id()
+{
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static bool looked_up = false;
+    if (!looked_up) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (CtxGetCurrentFn)p;
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (CtxGetIdFn)p;
+        (void)cudaGetLastError();
+        looked_up = true;
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 int fail(char *err, int cap, int code, const char *fmt, ...)
 {
@@ -146,8 +188,6 @@ extern "C" int ug4gb_vector_dot_noalloc(const double *a, const double *b, int64_
     if (e != cudaSuccess)
         return fail(err, err_capacity, UG4GB_ERR_CUDA, "ug4gb_vector_dot_noalloc: cudaGetDevice: %s",
                     cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices)
-        return fail(err, err_capacity, UG4GB_ERR_INVALID, "ug4gb_vector_dot_noalloc: device %d not supported", dev);
     if (!on_device(result, dev) || (n > 0 && (!on_device(a, dev) || !on_device(b, dev))))
         return fail(err, err_capacity, UG4GB_ERR_INVALID,
                     "ug4gb_vector_dot_noalloc: a, b and result must be device memory of the current device %d", dev);
@@ -155,20 +195,21 @@ extern "C" int ug4gb_vector_dot_noalloc(const double *a, const double *b, int64_
     DotScratch *s = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch[dev]) {
+        unsigned long long id = current_context_id();
+        for (int i = 0; i < g_num_scratch && id; ++i)
+            if (g_scratch[i].ctx_id == id) s = g_scratch[i].p;
+        if (!s) {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_dot_scratch);
             if (e != cudaSuccess)
                 return fail(err, err_capacity, UG4GB_ERR_CUDA, "ug4gb_vector_dot_noalloc: cudaGetSymbolAddress: %s",
                             cudaGetErrorString(e));
             s = (DotScratch *)p;
-            e = cudaMemsetAsync(&s->counter, 0, sizeof(unsigned int), st);
-            if (e != cudaSuccess)
-                return fail(err, err_capacity, UG4GB_ERR_CUDA, "ug4gb_vector_dot_noalloc: clearing the counter: %s",
-                            cudaGetErrorString(e));
-            g_scratch[dev] = s;
+            // the look-up made the device's primary context current if no
+            // context was; a context without an id is looked up every call
+            if (!id) id = current_context_id();
+            if (id && g_num_scratch < kMaxContexts) g_scratch[g_num_scratch++] = ScratchEntry{id, s};
         }
-        s = g_scratch[dev];
     }
     if (n == 0) {
         e = cudaMemsetAsync(result, 0, sizeof(double), st);
@@ -176,6 +217,10 @@ extern "C" int ug4gb_vector_dot_noalloc(const double *a, const double *b, int64_
             return fail(err, err_capacity, UG4GB_ERR_CUDA, "ug4gb_vector_dot_noalloc: %s", cudaGetErrorString(e));
         return UG4GB_OK;
     }
+    e = cudaMemsetAsync(&s->counter, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess)
+        return fail(err, err_capacity, UG4GB_ERR_CUDA, "ug4gb_vector_dot_noalloc: clearing the counter: %s",
+                    cudaGetErrorString(e));
     const unsigned int blocks = (unsigned int)((n + kChunk - 1) / kChunk);
     void *args[] = {(void *)&a, (void *)&b, (void *)&n, (void *)&result, (void *)&s};
     e = cudaLaunchKernel((const void *)k_dot_static, dim3(blocks), dim3(kThreads), args, 0, st);

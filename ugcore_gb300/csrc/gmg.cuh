@@ -20,9 +20,13 @@ void ug4gb_ctx_retain(ug4gb_ctx *ctx);
 void ug4gb_ctx_release(ug4gb_ctx *ctx);
 }
 
+// process-wide unique id of a grid (never reused, unlike an address after free)
+extern "C" uint64_t ug4gb_next_grid_uid();
+
 struct ug4gb_grid {
     ug4gb_ctx *ctx = nullptr;
     int elem_type = 0;
+    uint64_t uid = ug4gb_next_grid_uid();
     std::vector<ug4gb::Level> lev;
 };
 
@@ -38,7 +42,7 @@ struct ug4gb_matrix {
     ug4gb::Csr A;
     ug4gb::OpMat<double> op;              // solve format of A (SELL-32 or diagonal)
     bool op_valid = false;
-    const void *pattern_grid = nullptr;   // grid/level whose element pattern A holds
+    uint64_t pattern_grid = 0;            // uid of the grid (and the level) whose element pattern A holds
     int pattern_level = -1;
     void ensure_op()
     {
@@ -148,7 +152,7 @@ struct ug4gb_timedisc {
 // what a multigrid's structure depends on: a re-init with the same key may
 // keep the previous level buffers and transfers
 struct GmgKey {
-    const ug4gb_grid *g = nullptr;
+    uint64_t g = 0;                       // grid uid
     int nl = 0, base = 0, smoother = 0;
     double damp = 0.0;
     int rap = 0, transposed = 0, precision = 0, allow_dia = 0;
