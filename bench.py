@@ -194,6 +194,9 @@ def run_ours(args, rank, world, local_rank):
     import ugcore_gb300 as ug
     from ugcore_gb300 import problems
 
+    jobs = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        jobs = OracleJobs(["c1"] + ([] if args.no_extras else ["c2", "c3grad"]))
     torch.cuda.set_device(local_rank)
     ctx = ug.Context(local_rank)
     stream = torch.cuda.ExternalStream(ctx.stream)
@@ -276,17 +279,19 @@ def run_ours(args, rank, world, local_rank):
         prof_m = ctx.profile_end()
         stm = pm.solve()
         xm, x64 = pm.x.numpy(), p.x.numpy()
+        xo = jobs.solution("c1") if jobs else None
         mixed = {"value": world * n / (ms_m * 1e-3), "ms_per_step": ms_m, "steps_pcg": stm["steps"],
                  "speedup_vs_fp64": ms_max / ms_m,
                  "rel_residual": stm["defect"] / stm["initial_defect"],
                  "max_rel_diff_vs_fp64_solution": float(abs(xm - x64).max() / abs(x64).max()),
+                 "max_rel_err_vs_fp64_oracle": None if xo is None else float(abs(xm - xo).max() / abs(xo).max()),
                  "hbm_gbs_solve": iteration_bytes(sizes, 4) * stm["steps"] / (ms_m * 1e-3) / 1e9,
                  "kernel_profile": profile_summary(prof_m)}
         del pm
 
     target = adj = conv = rap = unstr = smoothers = None
     if not args.no_extras:
-        target = run_target(args, ctx, timed, world, hbm)
+        target = run_target(args, ctx, timed, world, hbm, jobs)
         adj = run_adjoint_grad(args, ctx, timed)
         conv = run_convection_adjoint(args, ctx, timed, world, hbm)
         rap = run_galerkin(args, ctx, timed, world)
@@ -303,9 +308,18 @@ def run_ours(args, rank, world, local_rank):
         asm = {"ms": ms_a, "dofs_per_s": n / (ms_a * 1e-3),
                "gbs": assembly_bytes(p, sizes[top]) / (ms_a * 1e-3) / 1e9, "setup_s_all_levels": setup_s}
 
-    cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline_sample()
+    cpu = cpu_c2 = cpu_c3 = None
+    if jobs:
+        cpu = cpu_baseline_from(jobs, "c1", "c1")
+        if not args.no_extras:
+            cpu_c2 = cpu_baseline_from(jobs, "c2", "c2 (FP64)")
+            r = jobs.results().get("c3grad", {})
+            cpu_c3 = r if "error" in r or not r else {
+                "value": r["ms"], "unit": "ms per gradient", "cores": 1, "kind": "port",
+                "sample": "best of 3 full gradients dJ/dm of the 257^2 problem (%d DoFs, %d elements): "
+                          "assembly and multigrid set-up, forward CG, transposed set-up and CG, element "
+                          "gradient" % (r["n"], r["elements"])}
+        jobs.close()
 
     if rank != 0:
         return None
@@ -341,10 +355,47 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
+    if not args.no_extras:
+        line["north_star"] = north_star_summary(mixed, target, adj, conv, asm, cpu, cpu_c2, cpu_c3)
     return line
 
 
-def run_target(args, ctx, timed, world, hbm):
+def _r(x, nd=4):
+    return None if x is None else float("%.*g" % (nd, x))
+
+
+def north_star_summary(mixed, target, adj, conv, asm, cpu_c1, cpu_c2, cpu_c3):
+    """the numbers the target of this path is stated in, in one compact
+    object at the end of the line: the 3D variable-coefficient problem with
+    the FP32 multigrid (time, HBM fraction of the whole solve, speed-up over
+    FP64, error against the FP64 oracle), the adjoint-gradient times, the
+    mixed-precision error of every configuration, and the CPU baselines"""
+    tf, tm = target["fp64"], target["mixed"]
+    out = {
+        "c2_mixed_ms": _r(tm["ms_per_step"]), "c2_fp64_ms": _r(tf["ms_per_step"]),
+        "c2_mixed_speedup_vs_fp64": _r(target["mixed_speedup_vs_fp64"]),
+        "c2_mixed_solve_hbm_frac": _r(tm["solve_frac_of_measured_hbm"]),
+        "c2_mixed_pcg_steps": tm["pcg_steps"], "c2_fp64_pcg_steps": tf["pcg_steps"],
+        "c2_mixed_max_rel_err_vs_fp64_oracle": _r(target.get("max_rel_err_mixed_vs_fp64_oracle")),
+        "c1_mixed_ms": _r(mixed["ms_per_step"]), "c1_mixed_speedup_vs_fp64": _r(mixed["speedup_vs_fp64"]),
+        "c1_mixed_max_rel_err_vs_fp64_oracle": _r(mixed.get("max_rel_err_vs_fp64_oracle")),
+        "c3_grad_ms_fp64": _r(adj["fp64_ms"]), "c3_grad_ms_mixed": _r(adj["mixed_ms"]),
+        "c4_mixed_ms": _r(conv["mixed"]["ms_per_solve"]), "c4_fp64_ms": _r(conv["fp64"]["ms_per_solve"]),
+        "c4_mixed_adjoint_ms": _r(conv["mixed"].get("adjoint_ms")),
+        "c4_mixed_max_rel_diff_vs_gpu_fp64": _r(conv.get("max_rel_diff_mixed_vs_fp64")),
+        "c1_assembly_ms": _r(asm["ms"]) if asm else None,
+        "cpu_1core_c1_fp64_dofs_per_s": _r(cpu_c1.get("value")) if cpu_c1 else None,
+        "cpu_1core_c2_fp64_dofs_per_s": _r(cpu_c2.get("value")) if cpu_c2 else None,
+        "cpu_1core_c3_grad_ms": _r(cpu_c3.get("value")) if cpu_c3 else None,
+    }
+    if cpu_c2 and cpu_c2.get("value"):
+        out["c2_mixed_vs_cpu_1core"] = _r(tm["dofs_per_s"] / cpu_c2["value"])
+    if cpu_c3 and cpu_c3.get("value"):
+        out["c3_grad_fp64_vs_cpu_1core"] = _r(cpu_c3["value"] / adj["fp64_ms"])
+    return out
+
+
+def run_target(args, ctx, timed, world, hbm, jobs=None):
     """3D variable-coefficient diffusion on Kuhn tetrahedra (4^3 hexes x 6 tets,
     refined 5 times, K = exp(2 g), g a 64-mode Gaussian field): FP64 GMG-PCG
     against FP32-GMG-in-FP64-CG, both to 1e-10."""
@@ -370,6 +421,10 @@ def run_target(args, ctx, timed, world, hbm):
     out.update(res)
     out["mixed_speedup_vs_fp64"] = res["fp64"]["ms_per_step"] / res["mixed"]["ms_per_step"]
     out["max_rel_diff_mixed_vs_fp64"] = float(abs(xs["mixed"] - xs["fp64"]).max() / abs(xs["fp64"]).max())
+    xo = jobs.solution("c2") if jobs else None
+    if xo is not None:
+        out["max_rel_err_mixed_vs_fp64_oracle"] = float(abs(xs["mixed"] - xo).max() / abs(xo).max())
+        out["max_rel_err_fp64_vs_fp64_oracle"] = float(abs(xs["fp64"] - xo).max() / abs(xo).max())
     return out
 
 
@@ -420,6 +475,7 @@ def run_convection_adjoint(args, ctx, timed, world, hbm):
     from ugcore_gb300 import problems
     out = {"workload": "3D convection-diffusion 193^3 hexes (7.19M DoFs), D=1e-2, cell Peclet 10, full upwind, "
                        "GMG V(2,2) Jacobi(0.6)-BiCGStab to 1e-10; adjoint dJ/df for J = sum_S u^2"}
+    xs = {}
     for prec in ("fp64", "mixed"):
         p = problems.Problem(ctx, problems.config("c4", precision=prec))
         for _ in range(min(args.warmup, 2)):
@@ -452,8 +508,12 @@ def run_convection_adjoint(args, ctx, timed, world, hbm):
             res["adjoint_rel_residual"] = sta["defect"] / sta["initial_defect"]
         out[prec] = res
         out["dofs"], out["nnz"] = p.n, sizes[-1]["nnz"]
+        xs[prec] = p.x.numpy()
         del p
     out["mixed_speedup_vs_fp64"] = out["fp64"]["ms_per_solve"] / out["mixed"]["ms_per_solve"]
+    # the GPU FP64 solution of this problem matches the FP64 oracle to 1e-8
+    # (tests/test_gpu_full_size.py); the oracle itself needs minutes here
+    out["max_rel_diff_mixed_vs_fp64"] = float(abs(xs["mixed"] - xs["fp64"]).max() / abs(xs["fp64"]).max())
     return out
 
 
@@ -591,19 +651,113 @@ def run_unstructured(args, ctx, timed, world, hbm):
     return out
 
 
-def cpu_baseline_sample():
-    """oracle port (restated ugcore algebra, 1 core) on the same workload:
-    one full c1 solve after assembling all levels."""
+def _oracle_params(name):
+    """oracle parameters of a benchmark configuration (FP64, as ugcore runs it)"""
     from oracle import oracle as orc
-    orc.build()
-    t0 = time.perf_counter()
-    P = orc.Problem(orc.make_params(elem_type=orc.ORC_HEX, mx=2, my=2, mz=2, nref=6, seed=1))
-    t1 = time.perf_counter()
-    s = P.solve()
-    t2 = time.perf_counter()
-    return {"value": P.nv() / (t2 - t1), "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "one full c1 solve (%d DoFs, %d PCG steps, %.1f s) after %.1f s of assembly/setup; "
-                      "single thread like ugcore's hot path" % (P.nv(), s["steps"], t2 - t1, t1 - t0)}
+    from ugcore_gb300 import problems
+    c = problems.config(name, precision="fp64")
+    et = {"quad": orc.ORC_QUAD, "hex": orc.ORC_HEX, "tet": orc.ORC_TET}[c["elem"]]
+    ck = {"const": 0 if c["diffusion"] == 1.0 else 3, "lognormal": 1, "logk": 2}[c["coef"]]
+    return orc.make_params(elem_type=et, mx=c["mx"], my=c["my"], mz=c["mz"], nref=c["nref"], seed=c["seed"],
+                           coef_kind=ck, coef_modes=c["coef_modes"], coef_kmax=c["coef_kmax"],
+                           vel_kind=1 if c["vel"] else 0, vel_modes=c["vel_modes"], vel_kmax=c["vel_kmax"],
+                           diffusion=c["diffusion"], peclet=c["peclet"], solver=0 if c["solver"] == "cg" else 1,
+                           damp=c["damp"], nu1=c["nu1"], nu2=c["nu2"], maxit=c["maxit"], rel_red=c["rel_red"])
+
+
+def _oracle_job(name, out_dir, q):
+    """CPU baseline legs (run in a spawned process, one core each): the
+    oracle port of the reference path on a benchmark configuration.
+    "c1"/"c2": assembly + multigrid set-up, then one full FP64 solve (timed;
+    the solution is kept to state the mixed-precision error against it).
+    "c3grad": one full adjoint gradient dJ/dm of the 257^2 inverse problem
+    as the GPU leg computes it (f = 1, J = 0.5 |u|^2): set-up, forward solve,
+    transposed set-up and solve, element gradient."""
+    import numpy as np
+    from oracle import oracle as orc
+    from ugcore_gb300 import fields, problems
+    try:
+        if name in ("c1", "c2"):
+            t0 = time.perf_counter()
+            P = orc.Problem(_oracle_params(name))
+            t1 = time.perf_counter()
+            s = P.solve()
+            t2 = time.perf_counter()
+            path = os.path.join(out_dir, name + ".npy")
+            np.save(path, s["x"])
+            q.put((name, {"setup_s": t1 - t0, "solve_s": t2 - t1, "steps": s["steps"], "n": P.nv(), "x": path}))
+        elif name == "c3grad":
+            c = problems.config("c3", precision="fp64")
+            par = _oracle_params("c3")
+            par.coef_kind = 0
+            coords, elems, _ = orc.Problem(par).level_geometry()
+            m = fields.ScalarField(2, c["coef_modes"], c["coef_kmax"], c["seed"] ^ fields.COEF_SEED_XOR)(
+                coords[elems].mean(axis=1))
+            f = np.ones(len(coords))
+            times = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                P = orc.Problem(_oracle_params("c3"), m_top=m, f_top=f)
+                u = P.solve()["x"]
+                lam = P.adjoint(u)["lam"]
+                P.grad_logk(u, lam)
+                times.append(time.perf_counter() - t0)
+                del P
+            q.put((name, {"ms": 1e3 * min(times), "n": len(coords), "elements": len(elems)}))
+    except Exception as ex:  # reported, never fatal for the GPU legs
+        q.put((name, {"error": repr(ex)}))
+
+
+class OracleJobs:
+    """the CPU baseline legs, started in spawned processes before the GPU
+    work so that they run beside it (a forked child of a CUDA process is not
+    safe; spawn is)"""
+
+    def __init__(self, names):
+        import multiprocessing as mp
+        from oracle import oracle as orc
+        orc.build()
+        self.dir = tempfile.mkdtemp(prefix="ug4gb_bench_")
+        ctx = mp.get_context("spawn")
+        self.q = ctx.Queue()
+        self.procs = [ctx.Process(target=_oracle_job, args=(nm, self.dir, self.q)) for nm in names]
+        for pr in self.procs:
+            pr.start()
+        self.res = {}
+
+    def results(self, timeout=600.0):
+        t_end = time.time() + timeout
+        while len(self.res) < len(self.procs) and time.time() < t_end:
+            try:
+                name, r = self.q.get(timeout=max(0.1, t_end - time.time()))
+                self.res[name] = r
+            except Exception:
+                break
+        for pr in self.procs:
+            pr.join(timeout=1.0)
+        return self.res
+
+    def solution(self, name):
+        import numpy as np
+        r = self.results().get(name, {})
+        return np.load(r["x"]) if "x" in r else None
+
+    def close(self):
+        import shutil
+        for pr in self.procs:
+            if pr.is_alive():
+                pr.terminate()
+        shutil.rmtree(self.dir, ignore_errors=True)
+
+
+def cpu_baseline_from(jobs, name, label):
+    """cpu_baseline object of one oracle solve leg"""
+    r = jobs.results().get(name)
+    if not r or "error" in r:
+        return {"error": (r or {}).get("error", "not finished")}
+    return {"value": r["n"] / r["solve_s"], "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "one full %s solve (%d DoFs, %d steps, %.2f s) after %.1f s of assembly/set-up; "
+                      "single thread like ugcore's hot path" % (label, r["n"], r["steps"], r["solve_s"], r["setup_s"])}
 
 
 # ------------------------------------------------------ reference arm -----
@@ -634,7 +788,7 @@ def run_reference(args, rank, world):
     from oracle import oracle as orc
     orc.build()
     nw = int(os.environ.get("UG4GB_REFERENCE_WORKERS", "0")) or (os.cpu_count() or 1)
-    warm = min(args.warmup, 1)
+    warm = args.warmup
     ctx = mp.get_context("spawn")
     barrier = ctx.Barrier(nw)
     out = ctx.Queue()
@@ -652,7 +806,7 @@ def run_reference(args, rank, world):
             "warmup": warm, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded splitmix64 source, structured grid)",
             "impl": "reference",
-            "config": {"workload": WORKLOAD, "dofs": n, "pcg_steps": res[0][2], "replicas": nw},
+            "config": {"workload": WORKLOAD, "dofs": n, "pcg_steps": res[0][2]},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nw, "kind": "port",
                              "sample": "%d concurrent replicas (one process per host core) of the full c1 solve; "
                                        "each step = one solve per replica" % nw},

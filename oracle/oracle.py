@@ -264,6 +264,19 @@ class Problem:
         L.orc_prob_transfer(self.h, l, which, rp, ci, va)
         return rp, ci, va
 
+    def level_geometry(self, l=None):
+        """(coords nv x dim, elems ne x k, Dirichlet flags nv) of level l"""
+        l = self.top if l is None else l
+        L = lib()
+        n, ne = self.nv(l), self.ne(l)
+        dim = 2 if self.params.elem_type in (ORC_QUAD, ORC_TRI) else 3
+        k = 8 if self.params.elem_type == ORC_HEX else (3 if self.params.elem_type == ORC_TRI else 4)
+        coords = np.zeros(n * dim)
+        elems = np.zeros(ne * k, np.int32)
+        bnd = np.zeros(n, np.uint8)
+        L.orc_prob_level_elems(self.h, l, elems.ctypes.data, coords.ctypes.data, bnd.ctypes.data)
+        return coords.reshape(n, dim), elems.reshape(ne, k), bnd
+
     def coef(self, l=None):
         l = self.top if l is None else l
         K = np.zeros(self.ne(l))

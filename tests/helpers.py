@@ -44,6 +44,15 @@ def assert_crs_equal(a, b, rtol=VAL_RTOL, what="matrix"):
         what, int(bad.sum()), rtol, float((err / np.maximum(scale, 1e-300)).max()))
 
 
+def rel_residual(p, x):
+    """|b - A x| / |b| of a problems.Problem for a host solution x"""
+    import ugcore_gb300 as ug
+    r = ug.GPUVector(p.ctx, p.n)
+    xv = ug.GPUVector(p.ctx, p.n).copy_from(x)
+    p.A.axpy(r, 1.0, p.b, -1.0, xv)
+    return r.norm() / p.b.norm()
+
+
 def reference_tree():
     """location of the ugcore source tree, or None where it is absent (asked
     of oracle/build_ref.sh, the recipe that compiles it)"""

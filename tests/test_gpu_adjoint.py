@@ -126,23 +126,6 @@ def test_c4_source_gradient(ctx, oracle_lib):
     _fd_check(Jf, gf, f0, 5, 1e-6, 5, 1e-6, normwise=True)
 
 
-def test_c4_mixed_adjoint_full_size(ctx):
-    """193^3 convection-diffusion, FP32 GMG inside FP64 BiCGStab: forward and
-    transposed solves reach 1e-10 and the source gradient is finite."""
-    from ugcore_gb300 import problems
-    cfg = problems.config("c4")
-    p = problems.Problem(ctx, cfg)
-    assert p.n == 193 ** 3
-    st = p.solve()
-    assert st["converged"], st
-    u = p.x.numpy()
-    S = np.random.default_rng(cfg["seed"]).random(p.n) < 0.1
-    ast = p.adjoint_solve(np.where(S, 2.0 * u, 0.0))
-    assert ast["converged"], ast
-    gf = p.disc.grad_source(p.lam)
-    assert np.isfinite(gf).all() and np.abs(gf).max() > 0
-
-
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_repeated_gradients_reuse_the_adjoint_set_up(ctx, precision):
     """a gradient after an operator update re-initialises the kept transposed
