@@ -156,4 +156,94 @@ for s in $IOSRCS; do
 done
 wait
 $CXX $FLAGS "$HERE/ref_io.cpp" $IOOBJS $OBJS "$OUT/obj/crc32_stub.o" -o "$OUT/ref_io"
-echo "build_ref: built $OUT/ref_driver $OUT/ref_io"
+# ugcore's FV1 element geometry and full-upwind convection shapes
+# (FV1Geometry, ConvectionShapesFullUpwind) with the reference-element,
+# reference-mapping and Lagrange shape-function code they use.  Their headers
+# use a few boost::mpl metafunctions; this stand-in implements that subset
+# (type lists, int_, fold with max, transform_view, for_each, range_c).
+SHIM2="$OUT/shim_fv1"
+mkdir -p "$SHIM2/boost/mpl"
+cat > "$SHIM2/boost/mpl/mpl_standin.hpp" <<'EOC'
+#pragma once
+#include <type_traits>
+namespace boost { namespace mpl {
+template <int N> struct int_ { static const int value = N; typedef int_ type; typedef int value_type; };
+template <typename... T> struct list { typedef list type; };
+struct _1 {}; struct _2 {}; struct _ {};
+template <typename A, typename B> struct max { typedef max type; };
+template <typename A, typename B> struct pair { typedef A first; typedef B second; };
+template <bool C, typename A, typename B> struct if_c { typedef typename std::conditional<C, A, B>::type type; };
+template <typename T, T lo, T hi> struct range_c { typedef range_c type; };
+template <typename Seq, typename F> struct transform_view;
+template <typename... T, typename F> struct transform_view<list<T...>, F> {
+    typedef list<typename F::template apply<T>::type...> type; };
+/* fold is only used as the maximum of int_ values */
+template <typename Seq, typename Init, typename Op> struct fold;
+template <typename Init, typename Op> struct fold<list<>, Init, Op> { typedef Init type; };
+template <typename H, typename... T, typename Init> struct fold<list<H, T...>, Init, max<_1, _2> > {
+    typedef typename fold<list<T...>, int_<(H::value > Init::value ? H::value : Init::value)>, max<_1, _2> >::type type; };
+template <typename... T, typename F, typename Init, typename Op> struct fold<transform_view<list<T...>, F>, Init, Op> {
+    typedef typename fold<typename transform_view<list<T...>, F>::type, Init, Op>::type type; };
+template <typename Seq> struct empty;
+template <typename... T> struct empty<list<T...> > { static const bool value = sizeof...(T) == 0; typedef empty type; };
+template <typename Seq> struct front;
+template <typename H, typename... T> struct front<list<H, T...> > { typedef H type; };
+template <typename Seq> struct pop_front;
+template <typename H, typename... T> struct pop_front<list<H, T...> > { typedef list<T...> type; };
+namespace standin {
+template <typename Seq> struct each;
+template <> struct each<list<> > { template <typename F> static void run(F &) {} };
+/* the functors ugcore passes use only the argument's type: no object of it
+   is constructed (grid element classes would need lib_grid) */
+template <typename H, typename... T> struct each<list<H, T...> > {
+    template <typename F> static void run(F &f) {
+        alignas(H) unsigned char buf[sizeof(H)];
+        f(*reinterpret_cast<H *>(buf));
+        each<list<T...> >::run(f); } };
+template <typename T, T i, T hi, bool done = (i >= hi)> struct each_range {
+    template <typename F> static void run(F &f) { int_<i> x; f(x); each_range<T, i + 1, hi>::run(f); } };
+template <typename T, T i, T hi> struct each_range<T, i, hi, true> { template <typename F> static void run(F &) {} };
+template <typename T, T lo, T hi> struct each<range_c<T, lo, hi> > {
+    template <typename F> static void run(F &f) { each_range<T, lo, hi>::run(f); } };
+}
+template <typename Seq, typename F> void for_each(F f) { standin::each<typename Seq::type>::run(f); }
+}}
+EOC
+for h in transform_view fold min_max for_each list range_c; do
+    echo '#include "mpl_standin.hpp"' > "$SHIM2/boost/mpl/$h.hpp"
+done
+# link stand-ins for lib_grid functions that the geometry's boundary-face code
+# names; with no subset handler (as the driver calls it) they are never run
+cat > "$OUT/lib_grid_standin.cpp" <<'EOC'
+#include <stdexcept>
+#include <vector>
+namespace ug {
+class Grid; class Edge; class Face; class Volume; class Vertex;
+#define UG_STANDIN(T, E) \
+    void T(std::vector<E *> &, Grid &, Edge *, bool) { throw std::logic_error(#T); } \
+    void T(std::vector<E *> &, Grid &, Face *, bool) { throw std::logic_error(#T); } \
+    void T(std::vector<E *> &, Grid &, Vertex *, bool) { throw std::logic_error(#T); } \
+    void T(std::vector<E *> &, Grid &, Volume *, bool) { throw std::logic_error(#T); }
+UG_STANDIN(CollectEdgesSorted, Edge)
+UG_STANDIN(CollectFacesSorted, Face)
+UG_STANDIN(CollectVertices, Vertex)
+class ISubsetHandler { public: bool elements_are_supported(unsigned int) const; Grid *grid() const; };
+bool ISubsetHandler::elements_are_supported(unsigned int) const { throw std::logic_error("subset handler"); }
+Grid *ISubsetHandler::grid() const { throw std::logic_error("subset handler"); }
+}
+EOC
+GFLAGS="-std=c++17 -O3 -DNDEBUG -w -I$OUT/shim -I$SHIM2 -I$REF/ugbase"
+GSRCS="lib_disc/spatial_disc/disc_util/fv1_geom.cpp lib_disc/local_finite_element/lagrange/lagrange.cpp lib_disc/local_finite_element/lagrange/lagrange_local_dof.cpp lib_disc/local_finite_element/lagrange/lagrangep1.cpp lib_disc/local_finite_element/local_dof_set.cpp lib_disc/local_finite_element/local_finite_element_id.cpp lib_disc/local_finite_element/local_finite_element_provider.cpp lib_disc/local_finite_element/mini/mini.cpp lib_disc/reference_element/reference_element.cpp lib_disc/reference_element/reference_mapping_provider.cpp common/math/misc/math_util.cpp common/math/math_vector_matrix/math_vector.cpp common/math/misc/eigenvalues.cpp common/math/misc/lineintersect_utils.cpp"
+GOBJS=""
+for s in $GSRCS; do
+    o="$OUT/obj/g_$(echo "$s" | tr '/' '_' | sed 's/\.cpp$/.o/')"
+    if [ ! -f "$o" ] || [ "$REF/ugbase/$s" -nt "$o" ]; then
+        $CXX $GFLAGS -c "$REF/ugbase/$s" -o "$o" &
+    fi
+    GOBJS="$GOBJS $o"
+done
+wait
+$CXX $GFLAGS -c "$OUT/lib_grid_standin.cpp" -o "$OUT/obj/lib_grid_standin.o"
+$CXX $GFLAGS "$HERE/ref_fv1geom.cpp" $GOBJS "$OUT/obj/lib_grid_standin.o" $OBJS "$OUT/obj/crc32_stub.o" \
+    -o "$OUT/ref_fv1geom"
+echo "build_ref: built $OUT/ref_driver $OUT/ref_io $OUT/ref_fv1geom"

@@ -100,7 +100,7 @@ def lib():
         L.orc_prob_free.argtypes = [P]
         L.orc_transpose_nnz.argtypes = [C.c_int, C.c_int, ip, ip, dp, C.c_int]
         L.orc_transpose_nnz.restype = C.c_int64
-        L.orc_geometry.argtypes = [C.c_int, dp, dp, dp, dp, ip, ip]
+        L.orc_geometry.argtypes = [C.c_int, dp, dp, dp, dp, ip, ip, dp]
         _LIB = L
     return _LIB
 
@@ -337,15 +337,18 @@ def transpose_nnz(rowptr, col, val, n_cols, keep_zeros):
 
 
 def geometry(elem_type, corners):
-    dim = 2 if elem_type == ORC_QUAD else 3
-    k = 8 if elem_type == ORC_HEX else 4
-    nf = {ORC_QUAD: 4, ORC_HEX: 12, ORC_TET: 6}[elem_type]
+    """FV1 geometry of one element: SCVF area normals, integration points,
+    shape gradients at them, from/to corners, and the SCV volumes"""
+    dim = 2 if elem_type in (ORC_QUAD, ORC_TRI) else 3
+    k = {ORC_QUAD: 4, ORC_HEX: 8, ORC_TET: 4, ORC_TRI: 3}[elem_type]
+    nf = {ORC_QUAD: 4, ORC_HEX: 12, ORC_TET: 6, ORC_TRI: 3}[elem_type]
     corners = np.ascontiguousarray(corners, np.float64).reshape(-1)
     normals = np.zeros(nf * dim)
+    ips = np.zeros(nf * dim)
     vols = np.zeros(k)
     grads = np.zeros(nf * k * dim)
     fr = np.zeros(nf, np.int32)
     to = np.zeros(nf, np.int32)
-    lib().orc_geometry(elem_type, corners, normals, vols, grads, fr, to)
+    lib().orc_geometry(elem_type, corners, normals, vols, grads, fr, to, ips)
     return dict(normals=normals.reshape(nf, dim), vols=vols, grads=grads.reshape(nf, k, dim),
-                frm=fr, to=to)
+                frm=fr, to=to, ips=ips.reshape(nf, dim))

@@ -584,14 +584,16 @@ int orc_field_params(int kind, int dim, int nmodes, double kmax, uint64_t seed, 
 
 /* FV1 geometry of one element (for geometry unit tests) */
 int orc_geometry(int elem_type, const double *corner, double *normals, double *vols, double *grads,
-                 int *from, int *to)
+                 int *from, int *to, double *ips)
 {
     orc_fv1geom G;
     orc_fv1_geometry(elem_type, corner, &G);
-    int dim = (elem_type == ORC_QUAD) ? 2 : 3;
+    int dim = (elem_type == ORC_QUAD || elem_type == ORC_TRI) ? 2 : 3;
     for (int i = 0; i < G.nscvf; ++i) {
         from[i] = G.from[i]; to[i] = G.to[i];
         for (int d = 0; d < dim; ++d) normals[i * dim + d] = G.normal[i][d];
+        if (ips)
+            for (int d = 0; d < dim; ++d) ips[i * dim + d] = G.gip[i][d];
         for (int s = 0; s < G.nscv; ++s)
             for (int d = 0; d < dim; ++d) grads[(i * G.nscv + s) * dim + d] = G.grad[i][s][d];
     }
