@@ -349,6 +349,14 @@ UG4GB_API int ug4gb_solver_create(ug4gb_ctx *ctx, int kind, ug4gb_solver **out);
 UG4GB_API int ug4gb_solver_set_preconditioner(ug4gb_solver *s, ug4gb_gmg *m);
 UG4GB_API int ug4gb_solver_set_convergence_check(ug4gb_solver *s, int max_steps, double min_defect,
                                        double rel_reduction);
+/* BiCGStab::set_restart (lib_algebra/operator/linear_solver/bicgstab.h:387):
+   restart (r0 = r, p = v = 0) whenever the convergence check's step count,
+   which counts half steps, is a multiple of num_restarts; 0 = off (default).
+   BiCGStab::set_min_orthogonality (bicgstab.h:390): restart in the next
+   iteration when |(r, r0)| <= min_ortho |r| |r0| (default 0).  Both are
+   UG4GB_ERR_INVALID for a CG solver. */
+UG4GB_API int ug4gb_solver_set_restart(ug4gb_solver *s, int num_restarts);
+UG4GB_API int ug4gb_solver_set_min_orthogonality(ug4gb_solver *s, double min_ortho);
 /* ILinearOperatorInverse::init (preconditioned_linear_operator_inverse.h:123) */
 UG4GB_API int ug4gb_solver_init(ug4gb_solver *s, const ug4gb_matrix *A);
 /* apply_return_defect (cg.h:103, bicgstab.h:112): x is the start iterate and

@@ -156,7 +156,7 @@ int main(int argc, char **argv)
 {
     if (argc < 11) {
         fprintf(stderr, "usage: ref_driver out.bin elem mx my mz nref seed coef_kind solver vel_kind "
-                        "[diffusion peclet smoother damp nu1 nu2 maxit]\n");
+                        "[diffusion peclet smoother damp nu1 nu2 maxit rap bicg_restart bicg_min_ortho]\n");
         return 2;
     }
     const char *out = argv[1];
@@ -170,6 +170,8 @@ int main(int argc, char **argv)
     int nu1 = argc > 15 ? atoi(argv[15]) : 2, nu2 = argc > 16 ? atoi(argv[16]) : 2;
     int maxit = argc > 17 ? atoi(argv[17]) : 200;
     int rap = argc > 18 ? atoi(argv[18]) : 0;
+    int bicg_restart = argc > 19 ? atoi(argv[19]) : 0;
+    double bicg_min_ortho = argc > 20 ? atof(argv[20]) : 0.0;
 
     orc_hier H;
     if (orc_hier_create(&H, elem, mx, my, mz, nref)) return 3;
@@ -278,6 +280,8 @@ int main(int argc, char **argv)
         ok = cg.apply_return_defect(x, rhs);
     } else {
         BiCGStab<Vec> bi;
+        bi.set_restart(bicg_restart);
+        bi.set_min_orthogonality(bicg_min_ortho);
         bi.set_preconditioner(spG);
         bi.set_convergence_check(conv);
         bi.init(G->A[top]);

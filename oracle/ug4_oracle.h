@@ -178,6 +178,8 @@ typedef struct {
     double *history;     /* optional, capacity hist_cap */
     int hist_cap;
     int converged;
+    int restart;         /* BiCGStab: restart when step % restart == 0 (0: off) */
+    double min_ortho;    /* BiCGStab: restart when |(r,r0)| <= min_ortho |r| |r0| */
 } orc_conv;
 
 int orc_cg(const orc_crs *A, orc_gmg *M, double *x, double *b, orc_conv *C);

@@ -36,6 +36,8 @@ typedef struct {
     int maxit;
     double rel_red, min_defect;
     int rap;            /* 1: Galerkin coarse operators R A P instead of re-assembly */
+    int bicg_restart;   /* BiCGStab::set_restart (0: off) */
+    double bicg_min_ortho; /* BiCGStab::set_min_orthogonality */
 } orc_params;
 
 typedef struct {
@@ -219,6 +221,7 @@ static int run_solver(const orc_params *p, const orc_crs *A, orc_gmg *G, double 
     memset(&C, 0, sizeof(C));
     C.maxit = p->maxit; C.min_defect = p->min_defect; C.rel_red = p->rel_red;
     C.history = hist; C.hist_cap = hist_cap;
+    C.restart = p->bicg_restart; C.min_ortho = p->bicg_min_ortho;
     int ok = (p->solver == 0) ? orc_cg(A, G, x, rhs, &C) : orc_bicgstab(A, G, x, rhs, &C);
     if (steps) *steps = C.steps;
     if (d0) *d0 = C.initial_defect;

@@ -550,6 +550,8 @@ int orc_bicgstab(const orc_crs *A, orc_gmg *M, double *x, double *b, orc_conv *C
     double rho = 1, alpha = 1, omega = 1, norm_r0 = 0.0;
     int bRestart = 1, ok = 1;
     while (!conv_ended(C)) {
+        /* restart by period (bicgstab.h:161-170; the check counts half steps) */
+        if (C->restart > 0 && C->steps % C->restart == 0) bRestart = 1;
         if (bRestart) {
             memcpy(r0, r, sizeof(double) * (size_t)n);
             memset(p, 0, sizeof(double) * (size_t)n); alpha = 0.0;
@@ -561,7 +563,8 @@ int orc_bicgstab(const orc_crs *A, orc_gmg *M, double *x, double *b, orc_conv *C
         const double rhoOld = rho;
         rho = vdot(n, r0, r);
         const double norm_r = C->final_defect;
-        if (fabs(rho) / (norm_r * norm_r0) <= 0.0) bRestart = 1;
+        /* restart in the next iteration when the orthogonality is lost (:206-215) */
+        if (fabs(rho) / (norm_r * norm_r0) <= C->min_ortho) bRestart = 1;
         if (rhoOld == 0.0) { ok = 0; break; }
         const double beta = (rho / rhoOld) * (alpha / omega);
         for (int i = 0; i < n; ++i) p[i] = 1.0 * r[i] + beta * p[i] + (-beta * omega) * v[i];

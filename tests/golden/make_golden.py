@@ -36,6 +36,14 @@ CASES.update({
     "tet_4x4x4_r1_lognormal_rap": CASES["tet_4x4x4_r1_lognormal"] + RAP,
     "hex_3x3x3_r1_convection_rap": CASES["hex_3x3x3_r1_convection"] + RAP,
 })
+# + (bicg_restart, bicg_min_ortho): BiCGStab::set_restart / set_min_orthogonality
+NORAP = (0, 0.6, 2, 2, 200, 0)
+CONV2 = (1, 3, 3, 3, 2, 1, 3, 1, 1, 1e-2, 10.0)
+CASES.update({
+    "hex_3x3x3_r2_convection_restart2": CONV2 + NORAP + (2, 0.0),
+    "hex_3x3x3_r2_convection_minortho": CONV2 + NORAP + (0, 0.1),
+    "hex_3x3x3_r2_convection_restart4_minortho": CONV2 + NORAP + (4, 0.3),
+})
 
 
 def read_ref(path):

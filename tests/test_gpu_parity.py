@@ -158,6 +158,27 @@ def test_gpu_against_ugcore_algebra_golden(ctx, name):
     assert np.abs(x - g["x"]).max() <= 1e-8 * np.abs(g["x"]).max()
 
 
+@pytest.mark.parametrize("name", ["hex_3x3x3_r2_convection_restart2", "hex_3x3x3_r2_convection_minortho",
+                                  "hex_3x3x3_r2_convection_restart4_minortho"])
+def test_bicgstab_restarts_against_ugcore_golden(ctx, name):
+    """BiCGStab::set_restart / set_min_orthogonality: fixtures written by
+    ugcore's own BiCGStab (with the oracle's multigrid); steps +-1, defect
+    history 1e-6, solution 1e-8"""
+    from ugcore_gb300 import problems
+    g = load_golden(name)
+    par = g["params"]
+    cfg = problems.config("c4", nref=int(par[4]), precision="fp64", bicg_restart=int(par[17]),
+                          bicg_min_ortho=float(par[18]))
+    p = problems.Problem(ctx, cfg)
+    st = p.solve()
+    assert abs(st["steps"] - int(g["steps"])) <= 1, (st["steps"], int(g["steps"]))
+    x = p.x.numpy()
+    assert np.abs(x - g["x"]).max() <= 1e-8 * np.abs(g["x"]).max()
+    h = p.solver.history()
+    n = min(len(h), len(g["hist"]))
+    assert np.allclose(h[:n], g["hist"][:n], rtol=1e-6, atol=0)
+
+
 @pytest.mark.parametrize("name,over", [("c2", dict(nref=2)), ("c4", dict(nref=2)), ("c3", dict(nref=4))])
 def test_bitwise_reproducible(ctx, name, over):
     """assembly (coloured, no atomics), reductions and the solve give the same

@@ -68,7 +68,9 @@ def test_transpose_matches_ugcore_golden(oracle_lib, case):
 
 # ---- fixtures from ugcore's algebra (tests/golden/make_golden.py) ----------
 GOLDEN_CASES = ["quad_2x2_r4", "hex_2x2x2_r2", "tet_4x4x4_r1_lognormal", "hex_3x3x3_r1_convection",
-                "hex_2x2x2_r2_rap", "tet_4x4x4_r1_lognormal_rap", "hex_3x3x3_r1_convection_rap"]
+                "hex_2x2x2_r2_rap", "tet_4x4x4_r1_lognormal_rap", "hex_3x3x3_r1_convection_rap",
+                "hex_3x3x3_r2_convection_restart2", "hex_3x3x3_r2_convection_minortho",
+                "hex_3x3x3_r2_convection_restart4_minortho"]
 
 
 def _golden_problem(orc, g):
@@ -77,6 +79,8 @@ def _golden_problem(orc, g):
     if len(g["params"]) > 11:   # smoother, damp, nu1, nu2, maxit, rap
         sm, damp, nu1, nu2, maxit, rap = g["params"][11:17]
         extra = dict(smoother=int(sm), damp=float(damp), nu1=int(nu1), nu2=int(nu2), maxit=int(maxit), rap=int(rap))
+    if len(g["params"]) > 17:   # BiCGStab restart period, minimal orthogonality
+        extra.update(bicg_restart=int(g["params"][17]), bicg_min_ortho=float(g["params"][18]))
     p = orc.make_params(elem_type=int(e), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
                         coef_kind=int(ck), solver=int(solver), vel_kind=int(vk), diffusion=diff, peclet=pe, **extra)
     return orc.Problem(p), bool(extra.get("rap", 0))

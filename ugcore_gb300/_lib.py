@@ -140,6 +140,8 @@ _SIGS = {
     "ug4gb_solver_set_preconditioner": (I, [P, P]),
     "ug4gb_solver_set_convergence_check": (I, [P, I, D, D]),
     "ug4gb_solver_init": (I, [P, P]),
+    "ug4gb_solver_set_restart": (I, [P, I]),
+    "ug4gb_solver_set_min_orthogonality": (I, [P, D]),
     "ug4gb_solver_apply_return_defect": (I, [P, P, P]),
     "ug4gb_solver_apply": (I, [P, P, P]),
     "ug4gb_solver_solve_host": (I, [P, P, P]),

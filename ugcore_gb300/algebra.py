@@ -833,3 +833,12 @@ class CG(_Krylov):
 
 class BiCGStab(_Krylov):
     KIND = _lib.SOLVER_BICGSTAB
+
+    def set_restart(self, num_restarts):
+        """restart every num_restarts steps of the convergence check (which
+        counts half steps); 0 = never (bicgstab.h:387)"""
+        check(lib().ug4gb_solver_set_restart(self.h, int(num_restarts)), self.ctx.h)
+
+    def set_min_orthogonality(self, min_ortho):
+        """restart when |(r, r0)| <= min_ortho |r| |r0| (bicgstab.h:390)"""
+        check(lib().ug4gb_solver_set_min_orthogonality(self.h, float(min_ortho)), self.ctx.h)

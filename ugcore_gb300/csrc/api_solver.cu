@@ -176,6 +176,8 @@ void run(ug4gb_solver *s, double *x, double *r)
     h.maxit = s->maxit;
     h.min_def = s->min_def;
     h.rel_red = s->rel_red;
+    h.num_restarts = s->num_restarts;
+    h.min_ortho = s->min_ortho;
     h.hist_cap = s->maxit + 2;
     s->hist.alloc(h.hist_cap);
     h.hist = s->hist.p;
@@ -275,6 +277,20 @@ int ug4gb_solver_set_convergence_check(ug4gb_solver *s, int maxit, double min_de
     s->maxit = maxit;
     s->min_def = min_def;
     s->rel_red = rel_red;
+    return UG4GB_OK;
+}
+
+int ug4gb_solver_set_restart(ug4gb_solver *s, int num_restarts)
+{
+    if (!s || num_restarts < 0 || s->kind != UG4GB_SOLVER_BICGSTAB) return UG4GB_ERR_INVALID;
+    s->num_restarts = num_restarts;
+    return UG4GB_OK;
+}
+
+int ug4gb_solver_set_min_orthogonality(ug4gb_solver *s, double min_ortho)
+{
+    if (!s || !(min_ortho >= 0.0) || s->kind != UG4GB_SOLVER_BICGSTAB) return UG4GB_ERR_INVALID;
+    s->min_ortho = min_ortho;
     return UG4GB_OK;
 }
 

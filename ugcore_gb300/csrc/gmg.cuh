@@ -190,6 +190,8 @@ struct ug4gb_solver {
     ug4gb_gmg *pre = nullptr;
     int maxit = 100;
     double min_def = 1e-300, rel_red = 1e-10;
+    int num_restarts = 0;        // BiCGStab: restart every num_restarts half steps (0: off)
+    double min_ortho = 0.0;      // BiCGStab: restart when (r, r0) <= min_ortho |r| |r0|
     const ug4gb_matrix *A = nullptr;
     int n = 0;
     ug4gb::DevBuf<double> r, p, q, r0, v, s, t, zcopy;

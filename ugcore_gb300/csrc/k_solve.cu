@@ -919,12 +919,20 @@ template void copy_z<double>(Ctx &, int, const double *, double *, const int *);
 template void copy_z<float>(Ctx &, int, const float *, double *, const int *);
 
 // ------------------------------------------------------------ BiCGStab ---
-// (BiCGStab::apply_return_defect, bicgstab.h:158-390; restarts off, minOrtho 0)
+// (BiCGStab::apply_return_defect, bicgstab.h:158-390).  A restart at the top
+// of an iteration comes from the previous iteration's orthogonality test
+// (ks->restart) or from the fixed restart period (step % num_restarts == 0,
+// bicgstab.h:161-170; the check counts half steps).
+__device__ __forceinline__ bool bicg_restarting(const KScal *ks)
+{
+    return ks->restart || (ks->num_restarts > 0 && ks->step % ks->num_restarts == 0);
+}
+
 __global__ void k_bicg_restart(int n, const double *__restrict__ r, double *__restrict__ r0, double *__restrict__ p,
                                double *__restrict__ v, KScal *ks)
 {
     PDL_ENTRY();
-    if (ks->done || !ks->restart) return;
+    if (ks->done || !bicg_restarting(ks)) return;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         r0[i] = r[i];
@@ -949,7 +957,7 @@ __global__ void __launch_bounds__(NT) k_bicg_rho(int n, const double *__restrict
     for (int i = blockIdx.x * NT + threadIdx.x; i < n; i += stride) sum += r0[i] * r[i];
     double v[1] = {sum};
     grid_reduce<NT, 1>(v, red.partials, red.counter, [&](const double(&tot)[1]) {
-        if (ks->restart) {
+        if (bicg_restarting(ks)) {
             ks->alpha = 0.0;
             ks->omega = 1.0;
             ks->rho = 1.0;
@@ -959,7 +967,9 @@ __global__ void __launch_bounds__(NT) k_bicg_rho(int n, const double *__restrict
         const double rho_old = ks->rho;
         ks->rho_old = rho_old;
         ks->rho = tot[0];
-        if (fabs(tot[0]) / (ks->dcur * ks->norm_r0) <= 0.0) ks->restart = 1;
+        // restart in the next iteration when (r, r0) <= minOrtho |r| |r0|
+        // (bicgstab.h:206-215)
+        if (fabs(tot[0]) / (ks->dcur * ks->norm_r0) <= ks->min_ortho) ks->restart = 1;
         if (rho_old == 0.0) {
             ks->fail = 1;
             ks->done = 1;

@@ -21,6 +21,8 @@ struct KScal {
     double d0, dcur;
     double rho, rho_old, alpha, beta, lambda;   // CG
     double omega, norm_r0;                      // BiCGStab
+    int num_restarts;                           // BiCGStab::set_restart (0: off)
+    double min_ortho;                           // BiCGStab::set_min_orthogonality
     double dot_out[2];                          // plain reductions
     double *hist;                               // hist_cap entries
 };

@@ -29,7 +29,7 @@ from .algebra import (BiCGStab, CG, DomainDiscretization, GaussSeidel, Geometric
 BASE = dict(elem="quad", mx=2, my=2, mz=1, nref=6, seed=1, coef="const", diffusion=1.0, coef_modes=64,
             coef_kmax=8.0, vel=None, vel_modes=16, vel_kmax=2.0, peclet=10.0, solver="cg", smoother="jacobi",
             damp=0.6, nu1=2, nu2=2, cycle=1, base=0, precision="fp64", maxit=200, rel_red=1e-10,
-            min_defect=1e-300, rap=False)
+            min_defect=1e-300, rap=False, bicg_restart=0, bicg_min_ortho=0.0)
 
 CONFIGS = {
     "c0": dict(elem="quad", mx=2, my=2, nref=6),
@@ -89,12 +89,20 @@ class Problem:
         self.disc.assemble_linear(self.A, self.b)
         self.gmg = self._make_gmg(transposed=False)
         self.gmg.init(self.A)
-        self.solver = (CG if c["solver"] == "cg" else BiCGStab)(ctx)
+        self.solver = self._make_solver()
         self.solver.set_preconditioner(self.gmg)
         self.solver.set_convergence_check(StdConvCheck(c["maxit"], c["min_defect"], c["rel_red"]))
         self.solver.init(self.A)
         self.x = GPUVector(ctx, self.n)
         self.rhs = GPUVector(ctx, self.n)
+
+    def _make_solver(self):
+        c = self.cfg
+        s = (CG if c["solver"] == "cg" else BiCGStab)(self.ctx)
+        if c["solver"] != "cg":
+            s.set_restart(c.get("bicg_restart", 0))
+            s.set_min_orthogonality(c.get("bicg_min_ortho", 0.0))
+        return s
 
     def _make_gmg(self, transposed):
         c = self.cfg
@@ -135,7 +143,7 @@ class Problem:
         b = GPUVector(self.ctx, self.n)
         gmg = self._make_gmg(transposed=False)
         gmg.set_discretization(td)
-        solver = (CG if c["solver"] == "cg" else BiCGStab)(self.ctx)
+        solver = self._make_solver()
         solver.set_preconditioner(gmg)
         solver.set_convergence_check(StdConvCheck(c["maxit"], c["min_defect"], c["rel_red"]))
         steps, t = [], t0
@@ -160,7 +168,7 @@ class Problem:
         if getattr(self, "gmgT", None) is None:
             self.AT = GPUSparseMatrix(self.ctx)
             self.gmgT = self._make_gmg(transposed=True)
-            self.solverT = (CG if self.cfg["solver"] == "cg" else BiCGStab)(self.ctx)
+            self.solverT = self._make_solver()
             self.solverT.set_preconditioner(self.gmgT)
             self.solverT.set_convergence_check(StdConvCheck(self.cfg["maxit"], self.cfg["min_defect"],
                                                             self.cfg["rel_red"]))
