@@ -312,6 +312,14 @@ UG4GB_API int ug4gb_gmg_set_num_presmooth(ug4gb_gmg *m, int n);
 UG4GB_API int ug4gb_gmg_set_num_postsmooth(ug4gb_gmg *m, int n);
 UG4GB_API int ug4gb_gmg_set_base_level(ug4gb_gmg *m, int level);
 UG4GB_API int ug4gb_gmg_set_precision(ug4gb_gmg *m, int precision);
+/* StdTransfer::set_prolongation_damping / set_restriction_damping
+   (lib_disc/operator/linear_operator/std_transfer.h:92,95; Lua
+   transfer:set_prolongation_damping(d), gmg:set_transfer(transfer)): the
+   applied prolongation is d_p P c and the applied restriction d_r R d
+   (std_transfer_impl.h:740,792); the assembled P and R (export_transfer) are
+   not damped, as in ugcore.  Default 1; applies at the next init. */
+UG4GB_API int ug4gb_gmg_set_prolongation_damping(ug4gb_gmg *m, double damp);
+UG4GB_API int ug4gb_gmg_set_restriction_damping(ug4gb_gmg *m, double damp);
 /* transposed = 1 builds the cycle on A^T of every level (Dirichlet rows reset
    to identity): the preconditioner of the adjoint solve */
 UG4GB_API int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed);

@@ -57,6 +57,7 @@ class RefGMG : public ILinearIterator<Vec>
 {
 public:
     int nlev, base, cycle, nu1, nu2;
+    double damp_res = 1.0, damp_prol = 1.0;   // StdTransfer::set_restriction/prolongation_damping
     std::vector<SmartPtr<MatOp> > A;
     std::vector<SmartPtr<Mat> > Pp, Rp;
     std::vector<SmartPtr<ILinearIterator<Vec> > > S;
@@ -83,11 +84,11 @@ public:
         }
         sc[l - 1].set(0.0);
         if (nu1 > 0) sc[l] += st[l];
-        Rp[l]->apply_ignore_zero_rows(sd[l - 1], 1.0, sd[l]);
+        Rp[l]->apply_ignore_zero_rows(sd[l - 1], damp_res, sd[l]);
     }
     void prolongation_and_postsmooth(int l)
     {
-        Pp[l]->axpy(st[l], 0.0, st[l], 1.0, sc[l - 1]);
+        Pp[l]->axpy(st[l], 0.0, st[l], damp_prol, sc[l - 1]);
         sc[l] += st[l];
         for (int nu = 0; nu < nu2; ++nu) {
             A[l]->apply_sub(sd[l], st[l]);
@@ -156,7 +157,7 @@ int main(int argc, char **argv)
 {
     if (argc < 11) {
         fprintf(stderr, "usage: ref_driver out.bin elem mx my mz nref seed coef_kind solver vel_kind "
-                        "[diffusion peclet smoother damp nu1 nu2 maxit rap bicg_restart bicg_min_ortho]\n");
+                        "[diffusion peclet smoother damp nu1 nu2 maxit rap bicg_restart bicg_min_ortho damp_prol damp_res]\n");
         return 2;
     }
     const char *out = argv[1];
@@ -172,6 +173,7 @@ int main(int argc, char **argv)
     int rap = argc > 18 ? atoi(argv[18]) : 0;
     int bicg_restart = argc > 19 ? atoi(argv[19]) : 0;
     double bicg_min_ortho = argc > 20 ? atof(argv[20]) : 0.0;
+    double damp_prol = argc > 21 ? atof(argv[21]) : 1.0, damp_res = argc > 22 ? atof(argv[22]) : 1.0;
 
     orc_hier H;
     if (orc_hier_create(&H, elem, mx, my, mz, nref)) return 3;
@@ -202,6 +204,7 @@ int main(int argc, char **argv)
     RefGMG *G = new RefGMG;
     SmartPtr<ILinearIterator<Vec> > spG(G);
     G->nlev = nl; G->base = 0; G->cycle = 1; G->nu1 = nu1; G->nu2 = nu2;
+    G->damp_prol = damp_prol; G->damp_res = damp_res;
     G->A.resize(nl); G->Pp.resize(nl); G->Rp.resize(nl); G->S.resize(nl);
     G->sc.resize(nl); G->sd.resize(nl); G->st.resize(nl);
     Vec b;

@@ -152,6 +152,7 @@ typedef struct {
     double **sc, **sd, **st;
     orc_lu lu;
     orc_crs *Arap;       /* rap: owned level operators (coarse levels), else NULL */
+    double damp_prol, damp_res; /* StdTransfer prolongation / restriction damping (1 after init) */
 } orc_gmg;
 
 /* M = R A P (Galerkin coarse operator), AddMultiplyOf(M, R, A, P) with M

@@ -38,6 +38,7 @@ typedef struct {
     int rap;            /* 1: Galerkin coarse operators R A P instead of re-assembly */
     int bicg_restart;   /* BiCGStab::set_restart (0: off) */
     double bicg_min_ortho; /* BiCGStab::set_min_orthogonality */
+    double damp_prol, damp_res; /* StdTransfer damping (both 1 = none) */
 } orc_params;
 
 typedef struct {
@@ -172,11 +173,21 @@ void orc_prob_source(const orc_prob *P, double *f)
     memcpy(f, P->f, sizeof(double) * (size_t)P->H.lev[P->H.nlev - 1].nv);
 }
 
+/* orc_gmg_init with the problem's smoother, cycle and transfer damping */
+static int gmg_init_p(orc_gmg *G, const orc_prob *P, orc_crs *levA)
+{
+    const orc_params *p = &P->p;
+    int rc = orc_gmg_init(G, &P->H, levA, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap);
+    if (rc) return rc;
+    G->damp_prol = p->damp_prol > 0.0 ? p->damp_prol : 1.0;
+    G->damp_res = p->damp_res > 0.0 ? p->damp_res : 1.0;
+    return 0;
+}
+
 static int ensure_gmg(orc_prob *P)
 {
     if (P->gmg_ready) return 0;
-    const orc_params *p = &P->p;
-    int rc = orc_gmg_init(&P->G, &P->H, P->A, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap);
+    int rc = gmg_init_p(&P->G, P, P->A);
     if (rc) return rc;
     P->gmg_ready = 1;
     return 0;
@@ -308,9 +319,7 @@ int orc_prob_theta_steps(orc_prob *P, double theta, double dt, int nsteps, doubl
         memcpy(u_old, u, sizeof(double) * (size_t)nv);
         if (s == 0) {
             if (theta_assemble(P, top, theta, dt, u_old, &At[top], b)) return -1;
-            const orc_params *p = &P->p;
-            if (orc_gmg_init(&G, &P->H, At, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap))
-                return -2;
+            if (gmg_init_p(&G, P, At)) return -2;
         } else {
             orc_crs T;
             memset(&T, 0, sizeof(T));
@@ -454,7 +463,7 @@ int orc_prob_newton_ls(orc_prob *P, double theta, double dt, const double *u_old
         orc_gmg G;
         memset(&G, 0, sizeof(G));
         const orc_params *p = &P->p;
-        if (orc_gmg_init(&G, &P->H, J, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap)) return -2;
+        if (gmg_init_p(&G, P, J)) return -2;
         memcpy(rhs, d, sizeof(double) * (size_t)nv);
         int ls = 0;
         const int lrc = run_solver(p, &J[top], &G, c, rhs, &ls, NULL, NULL, NULL, 0);
@@ -512,9 +521,7 @@ int orc_prob_adjoint(orc_prob *P, const double *g, double *lam, int *steps, doub
         P->AT = (orc_crs *)calloc((size_t)nl, sizeof(orc_crs));
         for (int l = 0; l < nl; ++l)
             if (transpose_dirichlet(&P->A[l], &P->H.lev[l], &P->AT[l])) return -1;
-        const orc_params *p = &P->p;
-        int rc = orc_gmg_init(&P->GT, &P->H, P->AT, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base,
-                              p->rap);
+        int rc = gmg_init_p(&P->GT, P, P->AT);
         if (rc) return rc;
         P->gmgT_ready = 1;
     }

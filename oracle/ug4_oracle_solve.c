@@ -270,6 +270,7 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
     memset(G, 0, sizeof(*G));
     G->nlev = H->nlev; G->base = base; G->cycle = cycle; G->nu1 = nu1; G->nu2 = nu2;
     G->smoother = smoother; G->damp = damp;
+    G->damp_prol = 1.0; G->damp_res = 1.0;
     G->A = levA;
     G->P = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
     G->R = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
@@ -395,13 +396,17 @@ static void presmooth_and_restriction(orc_gmg *G, int l)
     }
     memset(G->sc[l - 1], 0, sizeof(double) * (size_t)nc);
     if (G->nu1 > 0) vadd(n, G->sc[l], G->st[l]);
-    orc_crs_apply_ignore_zero_rows(&G->R[l], G->sd[l - 1], 1.0, G->sd[l]);
+    /* StdTransfer::do_restrict (std_transfer_impl.h:776-806): R applied
+       with the restriction damping as its factor */
+    orc_crs_apply_ignore_zero_rows(&G->R[l], G->sd[l - 1], G->damp_res, G->sd[l]);
 }
 
 static void prolongation_and_postsmooth(orc_gmg *G, int l)
 {
     int n = G->A[l].n_rows;
-    orc_crs_axpy(&G->P[l], G->st[l], 0.0, G->st[l], 1.0, G->sc[l - 1]);
+    /* StdTransfer::prolongate (std_transfer_impl.h:721-772): P.axpy with the
+       prolongation damping as its factor */
+    orc_crs_axpy(&G->P[l], G->st[l], 0.0, G->st[l], G->damp_prol, G->sc[l - 1]);
     vadd(n, G->sc[l], G->st[l]);
     for (int nu = 0; nu < G->nu2; ++nu) {
         orc_crs_matmul_minus(&G->A[l], G->sd[l], G->st[l]);

@@ -44,6 +44,11 @@ CASES.update({
     "hex_3x3x3_r2_convection_minortho": CONV2 + NORAP + (0, 0.1),
     "hex_3x3x3_r2_convection_restart4_minortho": CONV2 + NORAP + (4, 0.3),
 })
+# + (damp_prol, damp_res): StdTransfer::set_prolongation_damping / set_restriction_damping
+CASES.update({
+    "hex_2x2x2_r2_damped": CASES["hex_2x2x2_r2"] + NORAP + (0, 0.0, 0.8, 1.25),
+    "tet_4x4x4_r1_lognormal_damped": CASES["tet_4x4x4_r1_lognormal"] + NORAP + (0, 0.0, 1.3, 0.7),
+})
 
 
 def read_ref(path):

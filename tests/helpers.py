@@ -27,7 +27,8 @@ def oracle_params(orc, cfg):
         solver=0 if cfg["solver"] == "cg" else 1, smoother={"jacobi": 0, "mcgs": 1, "mcsgs": 2, "ilu": 3}[cfg["smoother"]],
         damp=cfg["damp"], nu1=cfg["nu1"], nu2=cfg["nu2"], cycle=cfg["cycle"], base=cfg["base"], maxit=cfg["maxit"],
         rel_red=cfg["rel_red"], min_defect=cfg["min_defect"], rap=int(cfg.get("rap", 0)),
-        bicg_restart=int(cfg.get("bicg_restart", 0)), bicg_min_ortho=float(cfg.get("bicg_min_ortho", 0.0)))
+        bicg_restart=int(cfg.get("bicg_restart", 0)), bicg_min_ortho=float(cfg.get("bicg_min_ortho", 0.0)),
+        damp_prol=float(cfg.get("damp_prol", 1.0)), damp_res=float(cfg.get("damp_res", 1.0)))
 
 
 def assert_crs_equal(a, b, rtol=VAL_RTOL, what="matrix"):

@@ -179,6 +179,37 @@ def test_bicgstab_restarts_against_ugcore_golden(ctx, name):
     assert np.allclose(h[:n], g["hist"][:n], rtol=1e-6, atol=0)
 
 
+@pytest.mark.parametrize("name,golden", [("c1", "hex_2x2x2_r2_damped"), ("c2", "tet_4x4x4_r1_lognormal_damped")])
+def test_transfer_damping_against_ugcore_golden(ctx, oracle_lib, name, golden):
+    """StdTransfer::set_prolongation_damping / set_restriction_damping:
+    against fixtures from ugcore's SparseMatrix axpy / apply_ignore_zero_rows
+    with the damping factors (steps +-1, solution 1e-8), and the damped
+    multigrid application against the oracle's to 1e-12; the exported P and R
+    stay undamped"""
+    import ugcore_gb300 as ug
+    g = load_golden(golden)
+    par = g["params"]
+    cfg = dict(nref=int(par[4]), precision="fp64", damp_prol=float(par[19]), damp_res=float(par[20]))
+    cfg, p = _problem(ctx, name, cfg)
+    st = p.solve()
+    assert abs(st["steps"] - int(g["steps"])) <= 1, (st["steps"], int(g["steps"]))
+    assert np.abs(p.x.numpy() - g["x"]).max() <= 1e-8 * np.abs(g["x"]).max()
+    top = p.hier.num_levels - 1
+    assert_crs_equal(p.gmg.transfer(top, 0), (g["P_rowptr"], g["P_col"], g["P_val"]), rtol=0.0, what="P")
+    op = _oracle(oracle_lib, cfg, p)
+    d = np.random.default_rng(4).standard_normal(p.n)
+    d[p.hier.export()[2].astype(bool)] = 0.0
+    cv = ug.GPUVector(ctx, p.n)
+    p.gmg.apply(cv, ug.GPUVector(ctx, p.n).copy_from(d))
+    ref = op.apply_gmg(d)
+    assert np.abs(cv.numpy() - ref).max() <= 1e-12 * np.abs(ref).max()
+    # the FP32 multigrid with the same damping: converged, close to FP64
+    _, pm = _problem(ctx, name, dict(cfg, precision="mixed"))
+    sm = pm.solve()
+    assert sm["converged"] and abs(sm["steps"] - st["steps"]) <= 2
+    assert np.abs(pm.x.numpy() - p.x.numpy()).max() <= 1e-7 * np.abs(p.x.numpy()).max()
+
+
 @pytest.mark.parametrize("name,over", [("c2", dict(nref=2)), ("c4", dict(nref=2)), ("c3", dict(nref=4))])
 def test_bitwise_reproducible(ctx, name, over):
     """assembly (coloured, no atomics), reductions and the solve give the same

@@ -70,7 +70,8 @@ def test_transpose_matches_ugcore_golden(oracle_lib, case):
 GOLDEN_CASES = ["quad_2x2_r4", "hex_2x2x2_r2", "tet_4x4x4_r1_lognormal", "hex_3x3x3_r1_convection",
                 "hex_2x2x2_r2_rap", "tet_4x4x4_r1_lognormal_rap", "hex_3x3x3_r1_convection_rap",
                 "hex_3x3x3_r2_convection_restart2", "hex_3x3x3_r2_convection_minortho",
-                "hex_3x3x3_r2_convection_restart4_minortho"]
+                "hex_3x3x3_r2_convection_restart4_minortho", "hex_2x2x2_r2_damped",
+                "tet_4x4x4_r1_lognormal_damped"]
 
 
 def _golden_problem(orc, g):
@@ -81,6 +82,8 @@ def _golden_problem(orc, g):
         extra = dict(smoother=int(sm), damp=float(damp), nu1=int(nu1), nu2=int(nu2), maxit=int(maxit), rap=int(rap))
     if len(g["params"]) > 17:   # BiCGStab restart period, minimal orthogonality
         extra.update(bicg_restart=int(g["params"][17]), bicg_min_ortho=float(g["params"][18]))
+    if len(g["params"]) > 19:   # transfer damping (prolongation, restriction)
+        extra.update(damp_prol=float(g["params"][19]), damp_res=float(g["params"][20]))
     p = orc.make_params(elem_type=int(e), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
                         coef_kind=int(ck), solver=int(solver), vel_kind=int(vk), diffusion=diff, peclet=pe, **extra)
     return orc.Problem(p), bool(extra.get("rap", 0))

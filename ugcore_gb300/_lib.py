@@ -104,6 +104,8 @@ _SIGS = {
     "ug4gb_gmg_set_precision": (I, [P, I]),
     "ug4gb_gmg_set_transposed": (I, [P, I]),
     "ug4gb_gmg_set_rap": (I, [P, I]),
+    "ug4gb_gmg_set_prolongation_damping": (I, [P, D]),
+    "ug4gb_gmg_set_restriction_damping": (I, [P, D]),
     "ug4gb_gmg_set_time_disc": (I, [P, P]),
     "ug4gb_timedisc_create": (I, [P, P, P]),
     "ug4gb_timedisc_set_theta": (I, [P, D]),

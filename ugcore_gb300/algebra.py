@@ -560,6 +560,30 @@ class SymmetricGaussSeidel:
         self.kind, self.damp = _lib.SMOOTHER_MCSGS, float(relax)
 
 
+class StdTransfer:
+    """StdTransfer (lib_disc/operator/linear_operator/std_transfer.h:57): P1
+    prolongation / restriction between the levels of the hierarchy.  The
+    damping factors scale the applied transfers (not the assembled
+    matrices).  enable_p1_lagrange_optimization selects ugcore's assembly
+    shortcut for P1 elements under regular refinement; the hierarchies here
+    are always regularly refined, where both assembly paths give the same P,
+    so the flag is kept but changes nothing."""
+
+    def __init__(self):
+        self.prolongation_damping = 1.0
+        self.restriction_damping = 1.0
+        self.p1_lagrange_optimization = True
+
+    def set_prolongation_damping(self, damp):
+        self.prolongation_damping = float(damp)
+
+    def set_restriction_damping(self, damp):
+        self.restriction_damping = float(damp)
+
+    def enable_p1_lagrange_optimization(self, enable=True):
+        self.p1_lagrange_optimization = bool(enable)
+
+
 class GeometricMultiGrid:
     """AssembledMultiGridCycle: V/W cycle, re-assembled level operators,
     StdTransfer, LU base solver."""
@@ -610,6 +634,13 @@ class GeometricMultiGrid:
 
     def set_transposed(self, flag=True):
         check(lib().ug4gb_gmg_set_transposed(self.h, 1 if flag else 0), self.ctx.h)
+
+    def set_transfer(self, transfer):
+        """AssembledMultiGridCycle::set_transfer (mg_solver.h:146) with a
+        StdTransfer: its prolongation and restriction damping"""
+        self.transfer_op = transfer
+        check(lib().ug4gb_gmg_set_prolongation_damping(self.h, float(transfer.prolongation_damping)), self.ctx.h)
+        check(lib().ug4gb_gmg_set_restriction_damping(self.h, float(transfer.restriction_damping)), self.ctx.h)
 
     def init(self, A):
         check(lib().ug4gb_gmg_init(self.h, A.h), self.ctx.h)

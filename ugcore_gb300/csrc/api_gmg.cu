@@ -44,6 +44,12 @@ __global__ void k_diag_inv(const int *rowptr, const int *col, const double *val,
     }
 }
 
+__global__ void k_scale_vals(double *val, int64_t nnz, double s)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nnz) val[i] *= s;
+}
+
 template <class V>
 __global__ void k_to_v(const double *in, V *out, int n)
 {
@@ -260,7 +266,23 @@ struct GmgT : GmgBase {
         (void)l;
     }
 
-    void setup_transfers(Ctx &c, GLevel<V> &F, const Level &Gf, const Level &Gc)
+    // solve-format copy of a transfer matrix scaled by a damping factor (the
+    // assembled P and R, which export returns, stay undamped as in ugcore)
+    void damped_op(Ctx &c, const Csr &T, double damp, OpMat<V> &out)
+    {
+        if (damp == 1.0) {
+            op_from_csr<V>(c, T, out, nullptr, false);
+            return;
+        }
+        Csr S;
+        csr_copy(c, T, S);
+        if (S.nnz > 0)
+            UG_LAUNCH(c, k_scale_vals, (unsigned)div_up(S.nnz, (int64_t)256), 256, 0, S.val.p, S.nnz, damp);
+        op_from_csr<V>(c, S, out, nullptr, false);
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+    }
+
+    void setup_transfers(Ctx &c, GLevel<V> &F, const Level &Gf, const Level &Gc, double dprol, double dres)
     {
         Csr &P = F.P;
         P.nrows = Gf.nv;
@@ -281,12 +303,13 @@ struct GmgT : GmgBase {
         csr_transpose(c, P, F.R, true);
         UG_LAUNCH(c, k_adjust_R, div_up(Gf.nv, 256), 256, 0, Gf.npar.p, Gf.par.p, Gf.bnd.p, Gf.nv, F.R.rowptr.p,
                   F.R.col.p, F.R.val.p);
-        op_from_csr<V>(c, F.P, F.Ps, nullptr, false);
-        op_from_csr<V>(c, F.R, F.Rs, nullptr, false);
+        damped_op(c, F.P, dprol, F.Ps);
+        damped_op(c, F.R, dres, F.Rs);
         // the structured hierarchy's P and R need no stored matrix (AUTO
         // format); the assembled CSR stays for export and the SELL format
         F.grid_transfer = c.allow_dia && Gf.structured && Gc.structured;
-        F.gp = GridPair{Gf.nx, Gf.ny, Gf.nz, Gc.nx, Gc.ny, Gc.nz, Gf.dim, Gf.elem_type == UG4GB_TET ? 1 : 0};
+        F.gp = GridPair{Gf.nx, Gf.ny, Gf.nz, Gc.nx, Gc.ny, Gc.nz, Gf.dim, Gf.elem_type == UG4GB_TET ? 1 : 0,
+                        dprol, dres};
         UG_CUDA(cudaStreamSynchronize(c.stream));
     }
 
@@ -518,7 +541,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
             UG_CUDA(cudaStreamSynchronize(c.stream));
             G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
             if (l > m->base) {
-                if (!keep_transfers) G->setup_transfers(c, L, g->lev[l], g->lev[l - 1]);
+                if (!keep_transfers) G->setup_transfers(c, L, g->lev[l], g->lev[l - 1], m->damp_prol, m->damp_res);
                 if (L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI)
                     L.sweep2 = sweep2_prepare<V>(c, L.At, L.gp);
             }
@@ -530,7 +553,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
         csr_copy(c, A_top->A, G->lev[nl - 1].A);
         if (m->transposed) transpose_level(nl - 1);
         for (int l = nl - 1; l > m->base; --l) {
-            if (!keep_transfers) G->setup_transfers(c, G->lev[l], g->lev[l], g->lev[l - 1]);
+            if (!keep_transfers) G->setup_transfers(c, G->lev[l], g->lev[l], g->lev[l - 1], m->damp_prol, m->damp_res);
             csr_rap(c, G->lev[l].R, G->lev[l].A, G->lev[l].P, G->lev[l - 1].A);
         }
         for (int l = m->base; l < nl; ++l) {
@@ -645,6 +668,20 @@ int ug4gb_gmg_set_time_disc(ug4gb_gmg *m, ug4gb_timedisc *td)
     return UG4GB_OK;
 }
 
+int ug4gb_gmg_set_prolongation_damping(ug4gb_gmg *m, double damp)
+{
+    if (!m || !(damp > 0.0) || !std::isfinite(damp)) return UG4GB_ERR_INVALID;
+    m->damp_prol = damp;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_restriction_damping(ug4gb_gmg *m, double damp)
+{
+    if (!m || !(damp > 0.0) || !std::isfinite(damp)) return UG4GB_ERR_INVALID;
+    m->damp_res = damp;
+    return UG4GB_OK;
+}
+
 int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed)
 {
     if (!m) return UG4GB_ERR_INVALID;
@@ -662,7 +699,7 @@ int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         // operator every Newton, time or optimisation step) keeps the level
         // buffers and the transfers
         const GmgKey key{m->disc->g->uid, (int)m->disc->g->lev.size(), m->base, m->smoother, m->damp, m->rap,
-                         m->transposed, m->precision, m->ctx->c.allow_dia ? 1 : 0};
+                         m->transposed, m->precision, m->ctx->c.allow_dia ? 1 : 0, m->damp_prol, m->damp_res};
         GmgBase *old = (m->impl && m->built == key) ? m->impl.release() : nullptr;
         m->impl.reset();
         m->built = GmgKey{};

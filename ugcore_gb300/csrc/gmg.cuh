@@ -156,10 +156,12 @@ struct GmgKey {
     int nl = 0, base = 0, smoother = 0;
     double damp = 0.0;
     int rap = 0, transposed = 0, precision = 0, allow_dia = 0;
+    double damp_prol = 1.0, damp_res = 1.0;
     bool operator==(const GmgKey &o) const
     {
         return g && g == o.g && nl == o.nl && base == o.base && smoother == o.smoother && damp == o.damp &&
-               rap == o.rap && transposed == o.transposed && precision == o.precision && allow_dia == o.allow_dia;
+               rap == o.rap && transposed == o.transposed && precision == o.precision && allow_dia == o.allow_dia &&
+               damp_prol == o.damp_prol && damp_res == o.damp_res;
     }
 };
 
@@ -172,6 +174,8 @@ struct ug4gb_gmg {
     int precision = UG4GB_PREC_FP64;
     int transposed = 0;
     int rap = 0;                 // coarse operators as Galerkin products R A P (set_rap)
+    double damp_prol = 1.0;      // StdTransfer prolongation / restriction damping
+    double damp_res = 1.0;
     ug4gb_timedisc *td = nullptr;  // coarse levels assembled as this time discretisation's jacobian
     std::unique_ptr<ug4gb::GmgBase> impl;
     GmgKey built;                // the structure impl was built for

@@ -492,7 +492,8 @@ __device__ __forceinline__ void prolong_row(const GridPair &g, const V *__restri
                                             const V *__restrict__ dfac, V *__restrict__ w, int i, int j, int k)
 {
     const int f = i + g.nx * (j + g.ny * k);
-    const V t = prolong_value<V>(g, scc, i, j, k);
+    V t = prolong_value<V>(g, scc, i, j, k);
+    if (g.dprol != 1.0) t = mul_rn(t, (V)g.dprol);
     sc[f] = add_rn(sc[f], t);
     if (w) w[f] = mul_rn(t, dfac[f]);
 }
@@ -506,7 +507,8 @@ __device__ __forceinline__ void restrict_row(const GridPair &g, const V *__restr
     const int c = I + g.cnx * (J + g.cny * K);
     const int fv = 2 * I + g.nx * (2 * J + g.ny * 2 * K);
     if (on_box_boundary(I, J, K, g.cnx, g.cny, g.cnz, g.dim)) {
-        dc[c] = (V)0 + (V)1 * d[fv];
+        const V v = (V)0 + (V)1 * d[fv];
+        dc[c] = (g.dres != 1.0) ? mul_rn(v, (V)g.dres) : v;
         return;
     }
     const int kr = (g.dim == 3) ? 1 : 0;
@@ -525,7 +527,7 @@ __device__ __forceinline__ void restrict_row(const GridPair &g, const V *__restr
                 }
                 acc += wt * d[fv + di + g.nx * (dj + g.ny * dk)];
             }
-    dc[c] = acc;
+    dc[c] = (g.dres != 1.0) ? mul_rn(acc, (V)g.dres) : acc;
 }
 
 template <class V, bool TILED>

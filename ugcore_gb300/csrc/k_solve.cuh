@@ -106,6 +106,9 @@ struct GridPair {
     int nx, ny, nz;      // fine level vertices per direction (nz = 1 in 2D)
     int cnx, cny, cnz;   // coarse level
     int dim, tet;        // tet: Kuhn split (two parents per edge midpoint)
+    // StdTransfer::set_prolongation_damping / set_restriction_damping: factors
+    // of the applied transfers (std_transfer_impl.h:740,792), 1 = none
+    double dprol = 1.0, dres = 1.0;
 };
 __device__ __forceinline__ bool on_box_boundary(int i, int j, int k, int nx, int ny, int nz, int dim)
 {

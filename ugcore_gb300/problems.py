@@ -23,13 +23,13 @@ import numpy as np
 
 from . import fields
 from .algebra import (BiCGStab, CG, DomainDiscretization, GaussSeidel, GeometricMultiGrid, GPUSparseMatrix,
-                      GPUVector, ILU, Jacobi, StdConvCheck, StructuredHierarchy, SymmetricGaussSeidel,
+                      GPUVector, ILU, Jacobi, StdConvCheck, StdTransfer, StructuredHierarchy, SymmetricGaussSeidel,
                       ThetaTimeStep)
 
 BASE = dict(elem="quad", mx=2, my=2, mz=1, nref=6, seed=1, coef="const", diffusion=1.0, coef_modes=64,
             coef_kmax=8.0, vel=None, vel_modes=16, vel_kmax=2.0, peclet=10.0, solver="cg", smoother="jacobi",
             damp=0.6, nu1=2, nu2=2, cycle=1, base=0, precision="fp64", maxit=200, rel_red=1e-10,
-            min_defect=1e-300, rap=False, bicg_restart=0, bicg_min_ortho=0.0)
+            min_defect=1e-300, rap=False, bicg_restart=0, bicg_min_ortho=0.0, damp_prol=1.0, damp_res=1.0)
 
 CONFIGS = {
     "c0": dict(elem="quad", mx=2, my=2, nref=6),
@@ -116,6 +116,11 @@ class Problem:
         g.set_precision(c["precision"])
         g.set_transposed(transposed)
         g.set_rap(c["rap"])
+        if c.get("damp_prol", 1.0) != 1.0 or c.get("damp_res", 1.0) != 1.0:
+            t = StdTransfer()
+            t.set_prolongation_damping(c.get("damp_prol", 1.0))
+            t.set_restriction_damping(c.get("damp_res", 1.0))
+            g.set_transfer(t)
         return g
 
     def solve(self, raise_on_failure=True):
