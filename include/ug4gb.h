@@ -99,6 +99,12 @@ UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
 /* UG4GB_TUNE_SWEEP_PLANES (2..128): z planes a block of the fused sweeps
    marches through (default 8). */
 #define UG4GB_TUNE_SWEEP_PLANES 3
+/* UG4GB_TUNE_ROW_ASSEMBLY (0 or 1): stationary assembly of structured levels
+   row by row from the per-class element geometry (default 1), or with the
+   element kernel used for unstructured levels (0).  Both give the same
+   values to rounding (the cells of a structured level are congruent up to
+   the rounding of their corner coordinates); each is bit-reproducible. */
+#define UG4GB_TUNE_ROW_ASSEMBLY 4
 UG4GB_API int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value);
 /* per-launch CUDA-event timing of every kernel until profile_end, which
    writes "tag|kernel<TAB>launches<TAB>total_ms" lines into buf.  While it is

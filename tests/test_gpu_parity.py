@@ -210,6 +210,32 @@ def test_transfer_damping_against_ugcore_golden(ctx, oracle_lib, name, golden):
     assert np.abs(pm.x.numpy() - p.x.numpy()).max() <= 1e-7 * np.abs(p.x.numpy()).max()
 
 
+@pytest.mark.parametrize("name,over", [("c0", dict(nref=5)), ("c1", dict(nref=3)), ("c2", dict(nref=3)),
+                                       ("c3", dict(nref=4)), ("c4", dict(nref=3))])
+def test_row_assembly_matches_element_assembly(ctx, name, over):
+    """structured levels: the row-wise assembly (per-class geometry, every
+    value written once) and the element kernel give the same operator and
+    rhs to 1e-13 of the row maximum on every level; the row-wise result is
+    bit-reproducible"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    cfg = problems.config(name, **over)
+    c2 = ug.Context(0)
+    c2.set_tuning(row_assembly=False)
+    p1 = problems.Problem(ctx, cfg)
+    p2 = problems.Problem(c2, cfg)
+    for l in range(p1.hier.num_levels):
+        A1, A2 = ug.GPUSparseMatrix(ctx), ug.GPUSparseMatrix(c2)
+        p1.disc.assemble_jacobian(A1, l)
+        p2.disc.assemble_jacobian(A2, l)
+        assert_crs_equal(A1.export_csr(), A2.export_csr(), what="level %d" % l)
+        A3 = ug.GPUSparseMatrix(ctx)
+        p1.disc.assemble_jacobian(A3, l)
+        assert np.array_equal(A1.export_csr()[2], A3.export_csr()[2])
+    b1, b2 = p1.b.numpy(), p2.b.numpy()
+    assert np.abs(b1 - b2).max() <= 1e-13 * np.abs(b2).max()
+
+
 @pytest.mark.parametrize("name,over", [("c2", dict(nref=2)), ("c4", dict(nref=2)), ("c3", dict(nref=4))])
 def test_bitwise_reproducible(ctx, name, over):
     """assembly (coloured, no atomics), reductions and the solve give the same

@@ -75,12 +75,18 @@ class Context:
         """'auto' (diagonal layout for structured operators) or 'sell'."""
         check(lib().ug4gb_set_operator_format(self.h, {"auto": 0, "sell": 1}[fmt]), self.h)
 
-    def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None):
-        """performance switches that leave results bit-identical:
+    def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None, row_assembly=None):
+        """performance switches:
         pdl: programmatic dependent launch of the solve kernels;
         sweep_fusion: bit mask (1 on, 2 every level size) of the
         two-Jacobi-steps-per-pass smoother of structured 3D FP32 levels;
-        sweep_planes: z planes per block of that smoother."""
+        sweep_planes: z planes per block of that smoother (these three leave
+        results bit-identical);
+        row_assembly: stationary assembly of structured levels row by row
+        from the per-class element geometry (default) or element by element
+        (same values to rounding)."""
+        if row_assembly is not None:
+            check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_ROW_ASSEMBLY, int(bool(row_assembly))), self.h)
         if pdl is not None:
             check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_PDL, int(bool(pdl))), self.h)
         if sweep_fusion is not None:

@@ -55,16 +55,14 @@ void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const T
     Ctx &c = d->ctx->c;
     const Level &L = d->g->lev[level];
     const double *K = disc_coefficients(d, level);
-    if (A->pattern_grid != d->g->uid || A->pattern_level != level) {
+    const bool fresh = (A->pattern_grid != d->g->uid || A->pattern_level != level);
+    if (fresh) {
         csr_from_elements(c, L, A->A);
         A->pattern_grid = d->g->uid;
         A->pattern_level = level;
-    } else {
-        UG_CUDA(cudaMemsetAsync(A->A.val.p, 0, sizeof(double) * (size_t)A->A.nnz, c.stream));
     }
     A->op_valid = false;
-    if (b) UG_CUDA(cudaMemsetAsync(b, 0, sizeof(double) * (size_t)L.nv, c.stream));
-    const DiscImpl &D = d->d;
+    DiscImpl &D = d->d;
     bool top = (level == (int)d->g->lev.size() - 1);
     AsmArgs a;
     a.coords = L.coords.p;
@@ -93,6 +91,13 @@ void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const T
         a.sa1 = ts->sa1;
         a.u_old = ts->u_old;
     }
+    // structured levels, stationary: row by row, every value written once
+    if (c.row_assembly) {
+        if (D.rows.size() < d->g->lev.size()) D.rows.resize(d->g->lev.size());
+        if (launch_assemble_rows(c, L, a, D.rows[level])) return;
+    }
+    if (!fresh) UG_CUDA(cudaMemsetAsync(A->A.val.p, 0, sizeof(double) * (size_t)A->A.nnz, c.stream));
+    if (b) UG_CUDA(cudaMemsetAsync(b, 0, sizeof(double) * (size_t)L.nv, c.stream));
     launch_assemble(c, L, a);
     launch_dirichlet(c, L, A->A, b);
 }

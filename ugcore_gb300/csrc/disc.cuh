@@ -2,6 +2,8 @@
 // kernels (k_fv1.cu) used by the host orchestration.
 #pragma once
 
+#include <vector>
+
 #include "common.cuh"
 
 namespace ug4gb {
@@ -42,6 +44,17 @@ struct TimeScale {
 };
 
 void launch_assemble(Ctx &c, const Level &L, const AsmArgs &a);
+// class geometry of a structured level, kept for the row-wise assembly
+struct RowAsmCache {
+    bool ready = false, usable = false;
+    std::vector<double> A, vol;         // unit-coefficient element matrices, SCV volumes per class
+    DevBuf<double> normal, ipoff;       // SCVF area normals / ips relative to the cell origin per class
+    DevBuf<double> flux;                // per element and SCVF: v(ip).n (convection)
+};
+// stationary assembly of a structured level row by row (k_fv1_rows.cu):
+// every value of A and b written once, Dirichlet rows included; returns
+// false, launching nothing, where it does not apply
+bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a, RowAsmCache &cache);
 void launch_dirichlet(Ctx &c, const Level &L, Csr &A, double *b);
 // d = defect of a.u on level L (a.d must be zero on entry; Dirichlet rows 0);
 // stationary, or instationary with a.inst and the scalings of AsmArgs

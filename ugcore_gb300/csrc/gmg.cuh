@@ -73,6 +73,7 @@ struct DiscImpl {
     DevBuf<double> f_top;
     int f_kind = 0;                        // 0 none, 1 array, 2 seeded uniform
     uint64_t f_seed = 0;
+    std::vector<RowAsmCache> rows;         // per level: class geometry of the row-wise assembly
 };
 
 template <class V>

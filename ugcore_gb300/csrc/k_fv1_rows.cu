@@ -1,0 +1,454 @@
+// k_fv1_rows.cu -- FV1 assembly of a structured level row by row.
+//
+// On a structured level every cell is the same box (spacing hx, hy, hz), so
+// the FV1 geometry of an element depends only on its class: the hexahedron
+// or quadrilateral of a cell, or one of the 6 Kuhn tetrahedra of a cell.  The
+// element matrix of unit coefficient A1_c, the SCV volumes vol_c, the SCVF
+// area normals and the integration-point offsets from the cell origin are
+// computed once per class (k_class_data, with the same device code as the
+// element kernel of k_fv1.cu) and passed to the row kernel as a kernel
+// parameter, so that every table lookup is a constant-bank operand.  The
+// element matrix of an element e of class c is then K_e A1_c (the box-method
+// stencil F_sh = -(K grad phi_sh).n is linear in K).
+//
+// One thread per interior row gathers the contributions of the elements
+// around its vertex (8 cells in 3D, 4 in 2D; for Kuhn cells the tets that
+// contain the vertex) in increasing cell order, the order in which the
+// element-wise reference adds them, and writes every value of the row and
+// its right-hand side once: no read-modify-write of the matrix, no colour
+// passes, no atomics.  Convection (full upwind, ConvectionShapesFullUpwind,
+// conv_shape.h:277-345) enters through the SCVF fluxes v(ip).n of each
+// element, computed once per element and SCVF by k_scvf_flux.
+// Rows on the box boundary (Dirichlet rows) get the identity row and a zero
+// right-hand side (SetDirichletRow, sparsematrix_util.h:850-862); a boundary
+// row without the Dirichlet flag is assembled by the general path.
+//
+// The element kernel of k_fv1.cu stays the path of unstructured levels and of
+// the time-discrete assembly.  Values agree with it (and with the oracle,
+// which computes every element's geometry from its own corner coordinates)
+// to rounding: the cells of a structured level are congruent up to the
+// rounding of their corner coordinates i / (n - 1).
+#include <cstring>
+#include <type_traits>
+
+#include "common.cuh"
+#include "disc.cuh"
+#include "fv1_elem.cuh"
+
+namespace ug4gb {
+
+namespace {
+
+// ------------------------------------------------------ class geometry ----
+// Corner bits (x | y << 1 | z << 2) of the cell for corner q of element class
+// p, as k_gen_elements (k_grid.cu) numbers them.
+template <int T>
+__host__ __device__ constexpr int class_corner_bits(int p, int q)
+{
+    if constexpr (T == UG4GB_QUAD) {
+        // (0,0),(1,0),(1,1),(0,1)
+        return q == 0 ? 0 : (q == 1 ? 1 : (q == 2 ? 3 : 2));
+    } else if constexpr (T == UG4GB_HEX) {
+        // bottom (0,0,0),(1,0,0),(1,1,0),(0,1,0), then the top
+        return (q & 4) | (q == 0 || q == 4 ? 0 : (q == 1 || q == 5 ? 1 : (q == 2 || q == 6 ? 3 : 2)));
+    } else {
+        // Kuhn tet p: v0, v0 + e_a, v0 + e_a + e_b, v0 + (1,1,1) with
+        // (a, b) = (0,1),(0,2),(1,0),(1,2),(2,0),(2,1); corners 1 and 2
+        // swapped for p = 1, 2, 5 (positive orientation)
+        const int a = (p < 2) ? 0 : (p < 4 ? 1 : 2);
+        const int b = (p == 0) ? 1 : (p == 1 ? 2 : (p == 2 ? 0 : (p == 3 ? 2 : (p == 4 ? 0 : 1))));
+        const int one = 1 << a, two = one | (1 << b);
+        const bool odd = (p == 1 || p == 2 || p == 5);
+        return q == 0 ? 0 : (q == 3 ? 7 : ((q == 1) != odd ? one : two));
+    }
+}
+
+template <int T>
+struct ClassTraits {
+    using E = Elem<T>;
+    static constexpr int NC = (T == UG4GB_TET) ? 6 : 1;   // element classes per cell
+    static constexpr int K = E::K, NF = E::NSCVF, DIM = E::DIM;
+    static constexpr int NCELL = (DIM == 3) ? 8 : 4;       // cells around a vertex
+};
+
+// per-class data passed by value to the row kernel
+template <int T>
+struct ClassData {
+    double A[ClassTraits<T>::NC][ClassTraits<T>::K][ClassTraits<T>::K];   // unit-coefficient element matrix
+    double vol[ClassTraits<T>::NC][ClassTraits<T>::K];                    // SCV volumes
+};
+
+// one thread per class: geometry of the classes of cell 0 from its actual
+// corner coordinates (X), element matrix with K = 1 and no convection, SCV
+// volumes, SCVF normals and integration points relative to the cell origin
+template <int T>
+__global__ void k_class_data(const double *coords, const int *elems, double *A, double *vol, double *normal,
+                             double *ipoff, int *corner_ok)
+{
+    using E = Elem<T>;
+    using CT = ClassTraits<T>;
+    const int p = threadIdx.x;
+    if (p >= CT::NC) return;
+    double X[E::K][E::DIM];
+    const int *ev = elems + (size_t)p * E::K;   // cell 0: elements 0 .. NC-1
+    int ok = 1;
+#pragma unroll
+    for (int q = 0; q < E::K; ++q) {
+        const int bits = class_corner_bits<T>(p, q);
+#pragma unroll
+        for (int d = 0; d < E::DIM; ++d) {
+            X[q][d] = coords[(size_t)ev[q] * E::DIM + d];
+            // the corner must sit where the class table says (cell 0 at the origin)
+            const bool upper = (bits >> d) & 1;
+            if ((X[q][d] > 0.0) != upper) ok = 0;
+        }
+    }
+    double Aloc[E::K][E::K], v[E::K];
+    elem_matrix<T>(X, 1.0, nullptr, Aloc, v);
+#pragma unroll
+    for (int i = 0; i < E::K; ++i) {
+        vol[p * E::K + i] = v[i];
+#pragma unroll
+        for (int j = 0; j < E::K; ++j) A[(p * E::K + i) * E::K + j] = Aloc[i][j];
+    }
+    // SCVF normals and integration points (as elem_matrix forms them)
+    double gm[3];
+    elem_centre<T>(X, gm);
+#pragma unroll
+    for (int ip = 0; ip < E::NSCVF; ++ip) {
+        double n[3] = {0, 0, 0}, gip[3] = {0, 0, 0}, em[3];
+        edge_mid<T>(X, ip, em);
+        if constexpr (E::DIM == 2) {
+            n[0] = gm[1] - em[1];
+            n[1] = -(gm[0] - em[0]);
+            gip[0] = (em[0] + gm[0]) * 0.5;
+            gip[1] = (em[1] + gm[1]) * 0.5;
+        } else {
+            double f0[3], f1[3], a[3], b[3];
+            face_mid<T>(X, E::edge_face(ip, 0), f0);
+            face_mid<T>(X, E::edge_face(ip, 1), f1);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                a[d] = gm[d] - em[d];
+                b[d] = f1[d] - f0[d];
+                gip[d] = (em[d] + f0[d] + gm[d] + f1[d]) * 0.25;
+            }
+            n[0] = 0.5 * (a[1] * b[2] - a[2] * b[1]);
+            n[1] = 0.5 * (a[2] * b[0] - a[0] * b[2]);
+            n[2] = 0.5 * (a[0] * b[1] - a[1] * b[0]);
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            normal[(p * E::NSCVF + ip) * 3 + d] = n[d];
+            ipoff[(p * E::NSCVF + ip) * 3 + d] = gip[d];
+        }
+    }
+    // corner ordering of the classes as k_gen_elements builds them
+    if (!ok) atomicExch(corner_ok, 0);
+}
+
+// ----------------------------------------------------------- SCVF flux ----
+// flux[e * NF + f] = v(ip).n of SCVF f of element e, the ip placed at the
+// cell origin plus the class's offset (VelField::eval, as the element kernel)
+template <int T>
+__global__ void __launch_bounds__(128) k_scvf_flux(int cx, int cy, int ncell, double hx, double hy, double hz,
+                                                   const double *__restrict__ normal, const double *__restrict__ ipoff,
+                                                   VelField vf, double *__restrict__ flux)
+{
+    using CT = ClassTraits<T>;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ncell * CT::NC) return;
+    const int cell = t / CT::NC, p = t % CT::NC;
+    const int i = cell % cx, j = (cell / cx) % cy, k = cell / (cx * cy);
+    const double o[3] = {i * hx, j * hy, k * hz};
+#pragma unroll 1
+    for (int f = 0; f < CT::NF; ++f) {
+        double x[3], v[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) x[d] = o[d] + __ldg(ipoff + (p * CT::NF + f) * 3 + d);
+        vf.eval(x, v);
+        double fl = 0.0;
+#pragma unroll
+        for (int d = 0; d < CT::DIM; ++d) fl += __ldg(normal + (p * CT::NF + f) * 3 + d) * v[d];
+        flux[(size_t)t * CT::NF + f] = fl;
+    }
+}
+
+// ------------------------------------------------------------- stencil ----
+// Offsets of the stencil of an interior row, in the order of the sorted
+// columns (increasing dz, then dy, then dx).  Quadrilaterals 9, hexahedra
+// 27, Kuhn tetrahedra 15 (0 and the +-offsets with components of one sign).
+template <int T>
+struct Stencil {
+    static constexpr int DIM = Elem<T>::DIM;
+    static constexpr int N = (T == UG4GB_QUAD) ? 9 : (T == UG4GB_HEX ? 27 : 15);
+    __host__ __device__ static constexpr bool member(int dx, int dy, int dz)
+    {
+        if (DIM == 2 && dz != 0) return false;
+        if (T != UG4GB_TET) return true;
+        const bool pos = dx > 0 || dy > 0 || dz > 0, neg = dx < 0 || dy < 0 || dz < 0;
+        return !(pos && neg);
+    }
+    // position of offset (dx, dy, dz) among the members
+    __host__ __device__ static constexpr int slot(int dx, int dy, int dz)
+    {
+        int s = 0;
+        for (int z = -1; z <= 1; ++z)
+            for (int y = -1; y <= 1; ++y)
+                for (int x = -1; x <= 1; ++x) {
+                    if (z == dz && y == dy && x == dx) return s;
+                    if (member(x, y, z)) ++s;
+                }
+        return -1;
+    }
+};
+
+// Contributions of the elements around vertex (i, j, k) to its row: calls
+// add(slot, value) for every element entry in increasing cell order (and
+// class order inside a cell), and rhs(vol) for the SCV volumes.
+template <int T, class FA, class FV>
+__device__ __forceinline__ void gather_row(const ClassData<T> &cd, const AsmArgs &a, int i, int j, int k,
+                                           const double *__restrict__ flux, FA &&add, FV &&rhs)
+{
+    using CT = ClassTraits<T>;
+    using E = Elem<T>;
+    using S = Stencil<T>;
+#pragma unroll
+    for (int cz = (CT::DIM == 3 ? -1 : 0); cz <= 0; ++cz)
+#pragma unroll
+        for (int cy = -1; cy <= 0; ++cy)
+#pragma unroll
+            for (int cxo = -1; cxo <= 0; ++cxo) {
+                // the vertex is corner (-cxo, -cy, -cz) of this cell
+                const int lb = (-cxo) | ((-cy) << 1) | ((-cz) << 2);
+                const int cell = (i + cxo) + a.cx * ((j + cy) + a.cy * (k + cz));
+#pragma unroll
+                for (int p = 0; p < CT::NC; ++p) {
+                    // local index of the vertex in class p (or none)
+                    int li = -1;
+#pragma unroll
+                    for (int q = 0; q < E::K; ++q)
+                        if (class_corner_bits<T>(p, q) == lb) li = q;
+                    if (li < 0) continue;
+                    const int e = cell * CT::NC + p;
+                    const double Ke = __ldg(a.K + e);
+#pragma unroll
+                    for (int q = 0; q < E::K; ++q) {
+                        const int bq = class_corner_bits<T>(p, q);
+                        const int s = S::slot(cxo + (bq & 1), cy + ((bq >> 1) & 1), cz + ((bq >> 2) & 1));
+                        add(s, Ke * cd.A[p][li][q]);
+                    }
+                    if (flux) {
+                        // full upwind: row li of SCVF f (from -> to, flux fl)
+#pragma unroll
+                        for (int f = 0; f < E::NSCVF; ++f) {
+                            const int fr = E::from(f), to = E::to(f);
+                            if (fr != li && to != li) continue;
+                            const double fl = flux[(size_t)e * E::NSCVF + f];
+                            const int bf = class_corner_bits<T>(p, fr), bt = class_corner_bits<T>(p, to);
+                            const int sf = S::slot(cxo + (bf & 1), cy + ((bf >> 1) & 1), cz + ((bf >> 2) & 1));
+                            const int st = S::slot(cxo + (bt & 1), cy + ((bt >> 1) & 1), cz + ((bt >> 2) & 1));
+                            if (fr == li) {
+                                // A[from][up] += flux
+                                if (fl >= 0.0) add(sf, fl);
+                                else add(st, fl);
+                            } else {
+                                // A[to][up] -= flux
+                                if (fl >= 0.0) add(sf, -fl);
+                                else add(st, -fl);
+                            }
+                        }
+                    }
+                    rhs(cd.vol[p][li]);
+                }
+            }
+}
+
+__device__ __forceinline__ double source_at(const AsmArgs &a, int r)
+{
+    return a.f ? a.f[r] : (a.use_seed ? 2.0 * hash_uniform(a.f_seed, (uint64_t)r) - 1.0 : 0.0);
+}
+
+// every interior row must hold exactly the stencil's entries (the pattern of
+// csr_from_elements); ok is cleared otherwise (checked once per level)
+template <int T>
+__global__ void k_check_row_lengths(int cx, int cy, int cz, const int *__restrict__ rowptr, int *ok)
+{
+    using S = Stencil<T>;
+    const int nix = cx - 1, niy = cy - 1, niz = (S::DIM == 3) ? cz - 1 : 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nix * niy * niz) return;
+    const int i = 1 + t % nix, j = 1 + (t / nix) % niy, k = (S::DIM == 3) ? 1 + t / (nix * niy) : 0;
+    const int r = i + (cx + 1) * (j + (cy + 1) * k);
+    if (rowptr[r + 1] - rowptr[r] != S::N) atomicExch(ok, 0);
+}
+
+// interior rows: one thread per row, every value written once
+template <int T>
+__global__ void __launch_bounds__(128) k_assemble_rows(AsmArgs a, ClassData<T> cd, const double *__restrict__ flux)
+{
+    using S = Stencil<T>;
+    const int nix = a.cx - 1, niy = a.cy - 1, niz = (S::DIM == 3) ? a.cz - 1 : 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nix * niy * niz) return;
+    const int i = 1 + t % nix, j = 1 + (t / nix) % niy, k = (S::DIM == 3) ? 1 + t / (nix * niy) : 0;
+    const int nx = a.cx + 1, ny = a.cy + 1;
+    const int r = i + nx * (j + ny * k);
+    double acc[S::N];
+#pragma unroll
+    for (int s = 0; s < S::N; ++s) acc[s] = 0.0;
+    double vsum = 0.0;
+    const double fr = a.b ? source_at(a, r) : 0.0;
+    gather_row<T>(cd, a, i, j, k, flux, [&](int s, double v) { acc[s] += v; },
+                  [&](double vol) { vsum += fr * vol; });
+    double *row = a.val + __ldg(a.rowptr + r);
+#pragma unroll
+    for (int s = 0; s < S::N; ++s) row[s] = acc[s];
+    if (a.b) a.b[r] = vsum;
+}
+
+// rows on the box boundary: the identity row and b = 0 at Dirichlet
+// vertices; otherwise the elements that exist, entries found by search
+template <int T>
+__global__ void __launch_bounds__(128) k_assemble_boundary_rows(AsmArgs a, ClassData<T> cd,
+                                                                const double *__restrict__ flux,
+                                                                const unsigned char *__restrict__ bnd)
+{
+    using CT = ClassTraits<T>;
+    using E = Elem<T>;
+    const int nx = a.cx + 1, ny = a.cy + 1, nz = (CT::DIM == 3) ? a.cz + 1 : 1;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nx * ny * nz) return;
+    const int i = r % nx, j = (r / nx) % ny, k = r / (nx * ny);
+    const bool onb = i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (CT::DIM == 3 && (k == 0 || k == nz - 1));
+    if (!onb) return;
+    const int r0 = a.rowptr[r], r1 = a.rowptr[r + 1];
+    if (bnd[r]) {
+        for (int q = r0; q < r1; ++q) a.val[q] = (a.col[q] == r) ? 1.0 : 0.0;
+        if (a.b) a.b[r] = 0.0;
+        return;
+    }
+    for (int q = r0; q < r1; ++q) a.val[q] = 0.0;
+    double vsum = 0.0;
+    const double fr = a.b ? source_at(a, r) : 0.0;
+    for (int cz = (CT::DIM == 3 ? -1 : 0); cz <= 0; ++cz)
+        for (int cy = -1; cy <= 0; ++cy)
+            for (int cxo = -1; cxo <= 0; ++cxo) {
+                if (i + cxo < 0 || i + cxo >= a.cx || j + cy < 0 || j + cy >= a.cy ||
+                    (CT::DIM == 3 && (k + cz < 0 || k + cz >= a.cz)))
+                    continue;
+                const int lb = (-cxo) | ((-cy) << 1) | ((-cz) << 2);
+                const int cell = (i + cxo) + a.cx * ((j + cy) + a.cy * (k + cz));
+                for (int p = 0; p < CT::NC; ++p) {
+                    int li = -1;
+                    for (int q = 0; q < E::K; ++q)
+                        if (class_corner_bits<T>(p, q) == lb) li = q;
+                    if (li < 0) continue;
+                    const int e = cell * CT::NC + p;
+                    auto col_of = [&](int q) {
+                        const int bq = class_corner_bits<T>(p, q);
+                        return (i + cxo + (bq & 1)) + nx * ((j + cy + ((bq >> 1) & 1)) + ny * (k + cz + ((bq >> 2) & 1)));
+                    };
+                    auto slot = [&](int c) {
+                        int lo = r0, hi = r1 - 1;
+                        while (lo <= hi) {
+                            const int mid = (lo + hi) >> 1;
+                            if (a.col[mid] == c) return mid;
+                            if (a.col[mid] < c) lo = mid + 1; else hi = mid - 1;
+                        }
+                        return -1;
+                    };
+                    for (int q = 0; q < E::K; ++q) {
+                        const int s = slot(col_of(q));
+                        if (s >= 0) a.val[s] += a.K[e] * cd.A[p][li][q];
+                    }
+                    if (flux) {
+                        for (int f = 0; f < E::NSCVF; ++f) {
+                            const int fr2 = E::from(f), to = E::to(f);
+                            if (fr2 != li && to != li) continue;
+                            const double fl = flux[(size_t)e * E::NSCVF + f];
+                            const int up = (fl >= 0.0) ? fr2 : to;
+                            const int s = slot(col_of(up));
+                            if (s >= 0) a.val[s] += (fr2 == li) ? fl : -fl;
+                        }
+                    }
+                    vsum += fr * cd.vol[p][li];
+                }
+            }
+    if (a.b) a.b[r] = vsum;
+}
+
+}  // namespace
+
+// Assembles level L row by row when it is a structured level and the
+// assembly is stationary; returns false (nothing launched) otherwise.
+bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCache &cache)
+{
+    if (!L.structured || a_in.inst || L.nx < 3 || L.ny < 3 || (L.dim == 3 && L.nz < 3)) return false;
+    bool done = false;
+    auto run = [&](auto tag) {
+        constexpr int T = decltype(tag)::value;
+        using CT = ClassTraits<T>;
+        using E = Elem<T>;
+        const int cx = L.nx - 1, cy = L.ny - 1, cz = (L.dim == 3) ? L.nz - 1 : 1;
+        const int nint = (cx - 1) * (cy - 1) * ((L.dim == 3) ? cz - 1 : 1);
+        if (!cache.ready) {
+            DevBuf<double> A, vol, nrm, ipo;
+            DevBuf<int> ok;
+            A.alloc(CT::NC * E::K * E::K);
+            vol.alloc(CT::NC * E::K);
+            nrm.alloc(CT::NC * E::NSCVF * 3);
+            ipo.alloc(CT::NC * E::NSCVF * 3);
+            ok.alloc(1);
+            const int one = 1;
+            copy_in(c, ok.p, &one, sizeof(int));
+            UG_LAUNCH(c, k_class_data<T>, 1, 32, 0, L.coords.p, L.elems.p, A.p, vol.p, nrm.p, ipo.p, ok.p);
+            UG_LAUNCH(c, k_check_row_lengths<T>, div_up(nint, 256), 256, 0, cx, cy, cz, a_in.rowptr, ok.p);
+            cache.A.resize(CT::NC * E::K * E::K);
+            cache.vol.resize(CT::NC * E::K);
+            copy_out(c, cache.A.data(), A.p, sizeof(double) * cache.A.size());
+            copy_out(c, cache.vol.data(), vol.p, sizeof(double) * cache.vol.size());
+            int okh = 0;
+            copy_out(c, &okh, ok.p, sizeof(int));
+            cache.normal = std::move(nrm);
+            cache.ipoff = std::move(ipo);
+            cache.usable = (okh == 1);
+            cache.ready = true;
+        }
+        if (!cache.usable) return;
+        ClassData<T> cd;
+        std::memcpy(&cd.A[0][0][0], cache.A.data(), sizeof(cd.A));
+        std::memcpy(&cd.vol[0][0], cache.vol.data(), sizeof(cd.vol));
+        AsmArgs a = a_in;
+        a.cx = cx;
+        a.cy = cy;
+        a.cz = cz;
+        const double *flux = nullptr;
+        if (a.vmodes > 0) {
+            if constexpr (E::DIM == 3) {
+                const int ncell = a.cx * a.cy * a.cz;
+                const size_t nf = (size_t)ncell * CT::NC * E::NSCVF;
+                if (cache.flux.n < nf) cache.flux.alloc(nf);
+                VelField vf{a.vmodes, a.vk, a.vc, a.vphase, a.vscale};
+                UG_LAUNCH(c, k_scvf_flux<T>, div_up(ncell * CT::NC, 128), 128, 0, a.cx, a.cy, ncell,
+                          1.0 / (double)a.cx, 1.0 / (double)a.cy, 1.0 / (double)a.cz, cache.normal.p,
+                          cache.ipoff.p, vf, cache.flux.p);
+                flux = cache.flux.p;
+            } else {
+                return;   // no 2D velocity field
+            }
+        }
+        UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux);
+        UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(L.nv, 128), 128, 0, a, cd, flux, L.bnd.p);
+        done = true;
+    };
+    switch (L.elem_type) {
+        case UG4GB_QUAD: run(std::integral_constant<int, UG4GB_QUAD>()); break;
+        case UG4GB_HEX: run(std::integral_constant<int, UG4GB_HEX>()); break;
+        case UG4GB_TET: run(std::integral_constant<int, UG4GB_TET>()); break;
+        default: break;
+    }
+    return done;
+}
+
+}  // namespace ug4gb
