@@ -429,6 +429,7 @@ int ug4gb_matrix_set_csr(ug4gb_matrix *m, int nrows, int ncols, int64_t nnz, con
         UG_CUDA(cudaStreamSynchronize(c.stream));
         m->op_valid = false;
         m->pattern_grid = 0;
+        m->derived_key = 0;
         m->pattern_level = -1;
     });
 }
@@ -486,6 +487,7 @@ int ug4gb_matrix_set_as_transpose_of(ug4gb_matrix *T, const ug4gb_matrix *B, int
         UG_CUDA(cudaStreamSynchronize(T->ctx->c.stream));
         T->op_valid = false;
         T->pattern_grid = 0;
+        T->derived_key = 0;
         T->pattern_level = -1;
     });
 }

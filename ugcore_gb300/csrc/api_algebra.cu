@@ -145,6 +145,7 @@ int ug4gb_matrix_resize_and_clear(ug4gb_matrix *A, int num_rows, int num_cols)
         UG_CUDA(cudaStreamSynchronize(c.stream));
         A->op_valid = false;
         A->pattern_grid = 0;
+        A->derived_key = 0;
         A->pattern_level = -1;
     });
 }
@@ -184,6 +185,7 @@ int ug4gb_matrix_set_as_copy_of(ug4gb_matrix *A, const ug4gb_matrix *B, double s
         A->op_valid = false;
         A->pattern_grid = B->pattern_grid;
         A->pattern_level = B->pattern_level;
+        A->derived_key = B->derived_key;
     });
 }
 

@@ -429,12 +429,21 @@ int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A,
     if (A->A.nrows != d->g->lev[level].nv) return UG4GB_ERR_INVALID;
     return guarded(d->ctx, [&] {
         Ctx &c = d->ctx->c;
-        csr_transpose(c, A->A, AT->A, true);
+        // the transposition of a level's element pattern is computed once;
+        // later operators of the same pattern only move their values
+        const uint64_t src = A->pattern_key();
+        const uint64_t key = src ? (src | (1ULL << 63)) : 0;
+        if (key && AT->tperm_key == src && AT->derived_key == key && AT->A.nnz == A->A.nnz) {
+            transpose_values(c, A->A, AT->A, AT->tperm);
+        } else {
+            transpose_perm(c, A->A, AT->A, AT->tperm);
+            AT->tperm_key = src;
+        }
         launch_dirichlet(c, d->g->lev[level], AT->A, nullptr);
-        UG_CUDA(cudaStreamSynchronize(c.stream));
         AT->op_valid = false;
         AT->pattern_grid = 0;
         AT->pattern_level = -1;
+        AT->derived_key = key;
     });
 }
 

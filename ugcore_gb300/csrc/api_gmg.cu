@@ -191,7 +191,30 @@ struct GmgT : GmgBase {
     const Csr &levelA(int l) const override { return lev[l].A; }
     int base_level() const override { return base; }
 
-    void setup_level(Ctx &c, GLevel<V> &L, const Level &G, int l, double damp, bool is_base)
+    uint64_t signature() const override
+    {
+        uint64_t h = 1469598103934665603ULL;
+        auto mix = [&](const void *p) {
+            h ^= (uint64_t)(uintptr_t)p;
+            h *= 1099511628211ULL;
+        };
+        for (const GLevel<V> &L : lev) {
+            mix(L.At.dia.val.p); mix(L.At.sell.val.p); mix(L.At.sell.col.p); mix(L.At.sell.sptr.p);
+            mix(L.At.sell.swidth.p); mix(L.dinv.p); mix(L.dfac.p); mix(L.sc.p); mix(L.dA.p); mix(L.dB.p);
+            mix(L.w.p); mix(L.t.p); mix(L.y.p); mix(L.Ps.dia.val.p); mix(L.Ps.sell.val.p); mix(L.Rs.dia.val.p);
+            mix(L.Rs.sell.val.p); mix(L.sweep2.get()); mix(L.vcolor.p);
+            for (const DevBuf<int> &q : L.crow) mix(q.p);
+            mix(L.ilu.val.p); mix(L.ilu.col.p); mix(L.ilu.rowptr.p); mix(L.ilu.nlow.p); mix(L.ilu.uinv.p);
+            h ^= (uint64_t)L.n;
+        }
+        mix(Ainv.p);
+        mix(z64.p);
+        return h;
+    }
+
+    // reuse: the same structure as the previous set-up of this level (its
+    // pattern, layout, colours): only values are refreshed, in place
+    void setup_level(Ctx &c, GLevel<V> &L, const Level &G, int l, double damp, bool is_base, bool reuse)
     {
         int n = L.A.nrows;
         L.n = n;
@@ -199,28 +222,30 @@ struct GmgT : GmgBase {
         L.dA.alloc(n);
         L.dB.alloc(n);
         if (is_base) return;
+        if (!reuse) L.At_lay.known = false;
         L.w.alloc(n);
-        DevBuf<double> dinv64, dfac64;
-        dinv64.alloc(n);
-        dfac64.alloc(n);
+        L.dinv64.alloc(n);
+        L.dfac64.alloc(n);
         UG_LAUNCH(c, k_diag_inv, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp, smoother,
-                  dinv64.p, dfac64.p);
+                  L.dinv64.p, L.dfac64.p);
         L.dinv.alloc(n);
         L.dfac.alloc(n);
-        UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, dinv64.p, L.dinv.p, n);
-        UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, dfac64.p, L.dfac.p, n);
+        UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, L.dinv64.p, L.dinv.p, n);
+        UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, L.dfac64.p, L.dfac.p, n);
         if (smoother == UG4GB_SMOOTHER_JACOBI) {
-            op_from_csr<V>(c, L.A, L.At, dinv64.p, c.allow_dia);
+            op_from_csr_cached<V>(c, L.A, L.At, L.dinv64.p, c.allow_dia, L.At_lay);
         } else {
-            op_from_csr<V>(c, L.A, L.At, nullptr, c.allow_dia);
+            op_from_csr_cached<V>(c, L.A, L.At, nullptr, c.allow_dia, L.At_lay);
             L.t.alloc(n);
             // colours with no coupling inside a colour: parity on structured
             // levels (valid for their stencils and for R A P of them); on
             // unstructured levels a greedy colouring of this operator's graph,
             // which a Galerkin operator may widen beyond the grid's elements
-            const int *colour = G.color.p;
+            const int *colour = G.structured ? G.color.p : L.vcolor.p;
             int ncol = G.ncolors;
-            if (!G.structured) {
+            // a re-init on the same structure keeps the colours and row lists
+            const bool have_colours = reuse && !L.crow.empty();
+            if (!G.structured && !have_colours) {
                 std::vector<int> rp(n + 1), ci((size_t)L.A.nnz), vc(n, -1), seen;
                 copy_out(c, rp.data(), L.A.rowptr.p, sizeof(int) * (size_t)(n + 1));
                 copy_out(c, ci.data(), L.A.col.p, sizeof(int) * (size_t)L.A.nnz);
@@ -242,6 +267,7 @@ struct GmgT : GmgBase {
                 copy_in(c, L.vcolor.p, vc.data(), sizeof(int) * (size_t)n);
                 colour = L.vcolor.p;
             }
+            if (!have_colours) {
             L.crow.resize(ncol);
             L.ncrow.assign(ncol, 0);
             DevBuf<int> flag, pos;
@@ -257,12 +283,12 @@ struct GmgT : GmgBase {
                 L.ncrow[q] = (int)cnt;
             }
             UG_CUDA(cudaStreamSynchronize(c.stream));
+            }
             if (smoother == UG4GB_SMOOTHER_ILU) {
                 ilu_setup<V>(c, L.A, colour, L.crow, L.ncrow, L.ilu);
                 L.y.alloc(n);
             }
         }
-        UG_CUDA(cudaStreamSynchronize(c.stream));
         (void)l;
     }
 
@@ -511,35 +537,48 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
     G->lev.resize(nl);
     UG_REQUIRE(m->base >= 0 && m->base < nl, UG4GB_ERR_INVALID, "GMG: base level out of range");
     UG_REQUIRE(A_top->A.nrows == g->lev[nl - 1].nv, UG4GB_ERR_INVALID, "GMG: top operator size != top level");
-    auto transpose_level = [&](int l) {
+    // transposed multigrid: A of the level = (Aasm)^T with Dirichlet rows
+    // reset to identity; the transposition permutation is kept for re-inits
+    auto transpose_level = [&](int l, const Csr &src, bool same_pattern) {
         GLevel<V> &L = G->lev[l];
-        Csr T;
-        csr_transpose(c, L.A, T, true);
-        UG_LAUNCH(c, k_dirichlet_identity, div_up(T.nrows, 256), 256, 0, g->lev[l].bnd.p, T.nrows, T.rowptr.p,
-                  T.col.p, T.val.p);
-        L.A = std::move(T);
+        if (same_pattern && L.tperm.p && L.A.nnz == src.nnz) {
+            transpose_values(c, src, L.A, L.tperm);
+        } else {
+            transpose_perm(c, src, L.A, L.tperm);
+        }
+        UG_LAUNCH(c, k_dirichlet_identity, div_up(L.A.nrows, 256), 256, 0, g->lev[l].bnd.p, L.A.nrows, L.A.rowptr.p,
+                  L.A.col.p, L.A.val.p);
     };
     if (!m->rap) {
         for (int l = m->base; l < nl; ++l) {
             GLevel<V> &L = G->lev[l];
+            const bool same = keep_transfers && L.asm_ok;
+            Csr &dst = m->transposed ? L.Aasm : L.A;
             // level operator: copy of the surface operator on the top level,
             // re-assembled on coarser levels (assemble_level_operator, :528-750)
             if (l == nl - 1) {
-                csr_copy(c, A_top->A, L.A);
+                csr_copy(c, A_top->A, dst);
             } else {
+                // re-assembled into the level's kept storage: the element
+                // pattern is built once per multigrid
                 ug4gb_matrix tmp;
                 tmp.ctx = m->ctx;
+                tmp.A = std::move(dst);
+                if (same) {
+                    tmp.pattern_grid = g->uid;
+                    tmp.pattern_level = l;
+                }
                 // with a time discretisation: the jacobian M + sa0 A of its
                 // current step (MultiStepTimeDiscretization::assemble_jacobian,
                 // theta_time_step_impl.h:123-140)
                 TimeScale ts{};
                 if (m->td) ts = m->td->jacobian_scale();
                 disc_assemble(m->disc, l, &tmp, nullptr, m->td ? &ts : nullptr);
-                L.A = std::move(tmp.A);
+                dst = std::move(tmp.A);
             }
-            if (m->transposed) transpose_level(l);
-            UG_CUDA(cudaStreamSynchronize(c.stream));
-            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
+            if (m->transposed) transpose_level(l, L.Aasm, same);
+            L.asm_ok = true;
+            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base, same);
             if (l > m->base) {
                 if (!keep_transfers) G->setup_transfers(c, L, g->lev[l], g->lev[l - 1], m->damp_prol, m->damp_res);
                 if (L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI)
@@ -550,15 +589,19 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
         // Galerkin coarse operators (init_rap_operator, :830-1012): the top
         // level's operator, then from the top down the transfers of a level
         // and R A P of it as the operator of the level below
-        csr_copy(c, A_top->A, G->lev[nl - 1].A);
-        if (m->transposed) transpose_level(nl - 1);
+        if (m->transposed) {
+            csr_copy(c, A_top->A, G->lev[nl - 1].Aasm);
+            transpose_level(nl - 1, G->lev[nl - 1].Aasm, false);
+        } else {
+            csr_copy(c, A_top->A, G->lev[nl - 1].A);
+        }
         for (int l = nl - 1; l > m->base; --l) {
             if (!keep_transfers) G->setup_transfers(c, G->lev[l], g->lev[l], g->lev[l - 1], m->damp_prol, m->damp_res);
             csr_rap(c, G->lev[l].R, G->lev[l].A, G->lev[l].P, G->lev[l - 1].A);
         }
         for (int l = m->base; l < nl; ++l) {
             GLevel<V> &L = G->lev[l];
-            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base);
+            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base, false);
             if (l > m->base && L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI)
                 L.sweep2 = sweep2_prepare<V>(c, L.At, L.gp);
         }
@@ -692,15 +735,18 @@ int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed)
 int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
 {
     if (!m || !A_top) return UG4GB_ERR_INVALID;
-    return guarded(m->ctx, [&] {
-        drop_graph(m);
-        m->gen++;
+    // what the cycle's launch sequence depends on besides the buffers
+    const uint64_t settings = ((uint64_t)(m->cycle + 8) << 40) ^ ((uint64_t)m->nu1 << 20) ^ (uint64_t)m->nu2;
+    bool keep_graphs = false;
+    const int rc = guarded(m->ctx, [&] {
         // a re-init with the same hierarchy and structure (typically a new
         // operator every Newton, time or optimisation step) keeps the level
-        // buffers and the transfers
+        // buffers and the transfers and refreshes the values in place
         const GmgKey key{m->disc->g->uid, (int)m->disc->g->lev.size(), m->base, m->smoother, m->damp, m->rap,
                          m->transposed, m->precision, m->ctx->c.allow_dia ? 1 : 0, m->damp_prol, m->damp_res};
-        GmgBase *old = (m->impl && m->built == key) ? m->impl.release() : nullptr;
+        const bool reuse = m->impl && m->built == key;
+        const uint64_t before = reuse ? (m->impl->signature() ^ m->built_settings) : 0;
+        GmgBase *old = reuse ? m->impl.release() : nullptr;
         m->impl.reset();
         m->built = GmgKey{};
         if (m->precision == UG4GB_PREC_FP64)
@@ -708,8 +754,17 @@ int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         else
             m->impl.reset(build_gmg<float>(m, A_top, static_cast<GmgT<float> *>(old)));
         m->built = key;
+        m->built_settings = settings;
         m->n_top = A_top->A.nrows;
+        // the same device buffers and launch sequence: the captured graphs
+        // (this multigrid's and its solvers') replay the refreshed values
+        keep_graphs = reuse && before == (m->impl->signature() ^ settings);
     });
+    if (!keep_graphs) {
+        drop_graph(m);
+        m->gen++;
+    }
+    return rc;
 }
 
 int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)

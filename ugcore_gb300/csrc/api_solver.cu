@@ -31,6 +31,25 @@ static int guarded(ug4gb_ctx *ctx, F &&f)
     }
 }
 
+// the device buffers of an operator's solve format
+static uint64_t op_signature(const OpMat<double> &M)
+{
+    uint64_t h = 1469598103934665603ULL;
+    auto mix = [&](uint64_t v) {
+        h ^= v;
+        h *= 1099511628211ULL;
+    };
+    mix((uint64_t)M.kind);
+    mix((uint64_t)M.nrows);
+    mix((uint64_t)(uintptr_t)M.dia.val.p);
+    mix((uint64_t)M.dia.S);
+    mix((uint64_t)(uintptr_t)M.sell.val.p);
+    mix((uint64_t)(uintptr_t)M.sell.col.p);
+    mix((uint64_t)(uintptr_t)M.sell.sptr.p);
+    mix((uint64_t)(uintptr_t)M.sell.swidth.p);
+    return h;
+}
+
 static void drop_graph(ug4gb_solver *s)
 {
     if (s->iter_graph) cudaGraphExecDestroy(s->iter_graph);
@@ -298,10 +317,15 @@ int ug4gb_solver_init(ug4gb_solver *s, const ug4gb_matrix *A)
 {
     if (!s || !A || A->A.nrows != A->A.ncols) return UG4GB_ERR_INVALID;
     return guarded(s->ctx, [&] {
-        drop_graph(s);
         ug4gb_matrix *Am = const_cast<ug4gb_matrix *>(A);
         Am->ensure_op();
+        // the same operator refreshed in place (same buffers, same layout) and
+        // the same vectors: the captured iteration graph stays valid
+        const uint64_t sig = op_signature(A->op);
+        const bool same = (s->A == A && s->n == A->A.nrows && s->op_sig == sig);
+        if (!same) drop_graph(s);
         s->A = A;
+        s->op_sig = sig;
         s->n = A->A.nrows;
         size_t n = s->n > 0 ? s->n : 1;
         s->p.alloc(n);
@@ -313,7 +337,6 @@ int ug4gb_solver_init(ug4gb_solver *s, const ug4gb_matrix *A)
             s->s.alloc(n);
             s->t.alloc(n);
         }
-        UG_CUDA(cudaStreamSynchronize(s->ctx->c.stream));
     });
 }
 

@@ -439,6 +439,25 @@ void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs,
 // solve format: diagonal when A is square with <= 27 offsets and allow_dia, else SELL-32
 template <class T>
 void op_from_csr(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_scale, bool allow_dia);
+// The layout an operator's solve format was built with (diagonal offsets or
+// SELL-32 slices).  While the caller knows the CRS pattern is unchanged (the
+// same level, re-assembled), op_from_csr_cached refills the values of the
+// existing buffers in place: no host round trip, no allocation, the same
+// device pointers (captured CUDA graphs stay valid).
+struct OpLayout {
+    bool known = false;
+    int kind = 0;                 // 0 SELL-32, 1 diagonal
+    int nrows = 0;
+    int64_t nnz = 0;
+    std::vector<int> offs;        // diagonal offsets (padded)
+};
+template <class T>
+void op_from_csr_cached(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_scale, bool allow_dia, OpLayout &lay);
+// T = A^T (structural zeros kept) and perm[k] = position in A of the entry
+// that lands at position k of T; transpose_values refills T's values from
+// A's through perm (the same pattern)
+void transpose_perm(Ctx &c, const Csr &A, Csr &T, DevBuf<int> &perm);
+void transpose_values(Ctx &c, const Csr &A, Csr &T, const DevBuf<int> &perm);
 void fill_double(Ctx &c, double *p, size_t n, double v);
 // after a synchronisation of the stream: throws if a kernel reported that one
 // of its bounded waits ran out (and clears the flag)

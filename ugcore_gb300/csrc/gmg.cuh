@@ -44,10 +44,28 @@ struct ug4gb_matrix {
     bool op_valid = false;
     uint64_t pattern_grid = 0;            // uid of the grid (and the level) whose element pattern A holds
     int pattern_level = -1;
+    // the transposed element pattern of a level (the adjoint operator), else 0
+    uint64_t derived_key = 0;
+    // layout of op, valid while the pattern has the key op_key (0: unknown)
+    ug4gb::OpLayout op_layout;
+    uint64_t op_key = 0;
+    // transposition permutation of the adjoint operator and its source key
+    ug4gb::DevBuf<int> tperm;
+    uint64_t tperm_key = 0;
+    // identity of the current pattern: the element pattern of (grid, level),
+    // or the transposed one; 0 = any other (set from arrays, products, ...)
+    uint64_t pattern_key() const
+    {
+        if (pattern_grid) return (pattern_grid << 6) + (uint64_t)(pattern_level + 1);
+        return derived_key;
+    }
     void ensure_op()
     {
         if (!op_valid) {
-            ug4gb::op_from_csr<double>(ctx->c, A, op, nullptr, ctx->c.allow_dia);
+            const uint64_t key = pattern_key();
+            if (!key || key != op_key) op_layout.known = false;
+            ug4gb::op_from_csr_cached<double>(ctx->c, A, op, nullptr, ctx->c.allow_dia, op_layout);
+            op_key = key;
             op_valid = true;
         }
     }
@@ -94,6 +112,12 @@ struct GLevel {
     DevBuf<int> vcolor;              // unstructured levels: colours of the operator's own graph
     IluFactors<V> ilu;               // ILU smoother factors
     DevBuf<V> y;                     // ILU forward-substitution scratch
+    // kept for a re-init on the same structure (values refreshed in place)
+    OpLayout At_lay;                 // layout of At
+    bool asm_ok = false;             // A (or Aasm) holds this level's element pattern
+    Csr Aasm;                        // transposed multigrid: the level operator before transposition
+    DevBuf<int> tperm;               // its transposition permutation
+    DevBuf<double> dinv64, dfac64;   // FP64 Jacobi factors
 };
 
 struct GmgBase {
@@ -113,6 +137,9 @@ struct GmgBase {
     virtual const Csr &R(int l) const = 0;
     virtual const Csr &levelA(int l) const = 0;   // FP64 operator of level l (re-assembled or R A P)
     virtual int base_level() const = 0;
+    // the device buffers the cycle's kernels use: equal signatures before and
+    // after a re-init mean the captured graphs stay valid
+    virtual uint64_t signature() const = 0;
 };
 
 }  // namespace ug4gb
@@ -180,6 +207,7 @@ struct ug4gb_gmg {
     ug4gb_timedisc *td = nullptr;  // coarse levels assembled as this time discretisation's jacobian
     std::unique_ptr<ug4gb::GmgBase> impl;
     GmgKey built;                // the structure impl was built for
+    uint64_t built_settings = 0; // cycle type and smoothing steps impl's graphs were captured with
     int n_top = 0;
     int gen = 0;                 // incremented by every init (invalidates captured graphs)
     // standalone apply graph
@@ -198,6 +226,7 @@ struct ug4gb_solver {
     int num_restarts = 0;        // BiCGStab: restart every num_restarts half steps (0: off)
     double min_ortho = 0.0;      // BiCGStab: restart when (r, r0) <= min_ortho |r| |r0|
     const ug4gb_matrix *A = nullptr;
+    uint64_t op_sig = 0;         // device buffers of A's solve format at init
     int n = 0;
     ug4gb::DevBuf<double> r, p, q, r0, v, s, t, zcopy;
     ug4gb::DevBuf<ug4gb::KScal> ks;

@@ -552,6 +552,83 @@ void op_from_csr(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_scale, boo
     }
 }
 
+template <class T>
+void op_from_csr_cached(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_scale, bool allow_dia, OpLayout &lay)
+{
+    if (lay.known && lay.nrows == A.nrows && lay.nnz == A.nnz && (lay.kind == 0 || allow_dia)) {
+        if (lay.kind == 1) {
+            dia_from_csr<T>(c, A, M.dia, lay.offs, col_scale);
+        } else {
+            UG_LAUNCH(c, k_sell_fill<T>, div_up((size_t)M.sell.nslices * kSliceH, 256), 256, 0, A.rowptr.p, A.col.p,
+                      A.val.p, A.nrows, M.sell.sptr.p, M.sell.swidth.p, col_scale, M.sell.col.p, M.sell.val.p);
+        }
+        return;
+    }
+    op_from_csr<T>(c, A, M, col_scale, allow_dia);
+    lay.known = true;
+    lay.kind = M.kind;
+    lay.nrows = A.nrows;
+    lay.nnz = A.nnz;
+    lay.offs.assign(M.dia.off.o, M.dia.off.o + (M.kind == 1 ? M.dia.S : 0));
+}
+
+template void op_from_csr_cached<double>(Ctx &, const Csr &, OpMat<double> &, const double *, bool, OpLayout &);
+template void op_from_csr_cached<float>(Ctx &, const Csr &, OpMat<float> &, const double *, bool, OpLayout &);
+
+__global__ void k_iota_val(double *v, int64_t n)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (double)i;
+}
+
+// perm from the transposed index values; then the real values through it
+__global__ void k_perm_gather(int64_t n, const double *tidx, int *perm, const double *aval, double *tval)
+{
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int a = (int)tidx[k];
+    perm[k] = a;
+    tval[k] = aval[a];
+}
+
+__global__ void k_gather_perm(int64_t n, const int *perm, const double *aval, double *tval)
+{
+    int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) tval[k] = aval[perm[k]];
+}
+
+void transpose_perm(Ctx &c, const Csr &A, Csr &T, DevBuf<int> &perm)
+{
+    UG_REQUIRE(A.nnz < ((int64_t)1 << 31), UG4GB_ERR_INVALID, "transpose_perm: nnz exceeds int32 range");
+    Csr B;
+    B.nrows = A.nrows;
+    B.ncols = A.ncols;
+    B.nnz = A.nnz;
+    B.rowptr.alloc(A.nrows + 1);
+    B.col.alloc(A.nnz > 0 ? A.nnz : 1);
+    B.val.alloc(A.nnz > 0 ? A.nnz : 1);
+    UG_CUDA(cudaMemcpyAsync(B.rowptr.p, A.rowptr.p, sizeof(int) * (size_t)(A.nrows + 1), cudaMemcpyDeviceToDevice,
+                            c.stream));
+    if (A.nnz) {
+        UG_CUDA(cudaMemcpyAsync(B.col.p, A.col.p, sizeof(int) * (size_t)A.nnz, cudaMemcpyDeviceToDevice, c.stream));
+        UG_LAUNCH(c, k_iota_val, div_up(A.nnz, (int64_t)256), 256, 0, B.val.p, A.nnz);
+    }
+    csr_transpose(c, B, T, true);
+    perm.alloc(T.nnz > 0 ? T.nnz : 1);
+    if (T.nnz) {
+        DevBuf<double> tidx;
+        tidx.alloc(T.nnz);
+        UG_CUDA(cudaMemcpyAsync(tidx.p, T.val.p, sizeof(double) * (size_t)T.nnz, cudaMemcpyDeviceToDevice, c.stream));
+        UG_LAUNCH(c, k_perm_gather, div_up(T.nnz, (int64_t)256), 256, 0, T.nnz, tidx.p, perm.p, A.val.p, T.val.p);
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+    }
+}
+
+void transpose_values(Ctx &c, const Csr &A, Csr &T, const DevBuf<int> &perm)
+{
+    if (T.nnz) UG_LAUNCH(c, k_gather_perm, div_up(T.nnz, (int64_t)256), 256, 0, T.nnz, perm.p, A.val.p, T.val.p);
+}
+
 template void dia_from_csr<double>(Ctx &, const Csr &, Dia<double> &, const std::vector<int> &, const double *);
 template void dia_from_csr<float>(Ctx &, const Csr &, Dia<float> &, const std::vector<int> &, const double *);
 template void op_from_csr<double>(Ctx &, const Csr &, OpMat<double> &, const double *, bool);
