@@ -19,8 +19,20 @@ from . import problems
 from .algebra import GPUVector
 
 
+def _library_waits_for_torch(ctx):
+    """the library's stream waits (on the device, through an event) for the
+    work queued so far on torch's current stream"""
+    torch.cuda.ExternalStream(ctx.stream).wait_stream(torch.cuda.current_stream())
+
+
+def _torch_waits_for_library(ctx):
+    torch.cuda.current_stream().wait_stream(torch.cuda.ExternalStream(ctx.stream))
+
+
 class DifferentiableProblem(problems.Problem):
-    """A Problem whose coefficient and source come from torch tensors."""
+    """A Problem whose coefficient and source come from torch tensors.  The
+    solution lives in a torch tensor the library writes directly; the two
+    streams are ordered by events, not by host synchronisation."""
 
     def __init__(self, ctx, cfg, m=None, f=None):
         cfg = dict(cfg)
@@ -28,24 +40,29 @@ class DifferentiableProblem(problems.Problem):
         super().__init__(ctx, cfg, m_top=None if m is None else m.detach().cpu().numpy(),
                          f_top=None if f is None else f.detach().cpu().numpy())
         self.num_elements = self.hier.num_elements()
+        self._x_t = torch.zeros(self.n, dtype=torch.float64, device="cuda")
+        self.x = GPUVector(self.ctx, wrap=self._x_t)
+        self._inputs = None
 
     def update(self, m, f):
-        """re-assemble for new (m, f) (CUDA float64 tensors) and re-initialise."""
-        torch.cuda.synchronize()
-        self.disc.set_log_diffusion(m.detach().contiguous())
-        self.disc.set_source(f.detach().contiguous())
+        """re-assemble for new (m, f) (CUDA float64 tensors) and re-initialise
+        (on an unchanged hierarchy the multigrid and the solvers refresh their
+        values in place and keep their captured graphs)."""
+        _library_waits_for_torch(self.ctx)
+        # kept alive until the library has read them (the uploads synchronise)
+        self._inputs = (m.detach().contiguous(), f.detach().contiguous())
+        self.disc.set_log_diffusion(self._inputs[0])
+        self.disc.set_source(self._inputs[1])
         self.disc.assemble_linear(self.A, self.b)
         self.gmg.init(self.A)
         self.solver.init(self.A)
         self.invalidate_adjoint()
 
-    def solve_into(self, out):
-        """solve and copy u into the CUDA tensor out"""
+    def solve_u(self):
+        """solve; returns u as a new CUDA tensor (a copy on torch's stream)"""
         self.solve()
-        v = GPUVector(self.ctx, wrap=out)
-        v.scale_add(1.0, self.x, 0.0, self.x)
-        self.ctx.synchronize()
-        return out
+        _torch_waits_for_library(self.ctx)
+        return self._x_t.clone()
 
     def backward(self, u_tensor, grad_u):
         self.adjoint_setup()
@@ -55,16 +72,16 @@ class DifferentiableProblem(problems.Problem):
         # rhs = dJ/du without its Dirichlet entries
         rhs_t = (grad_u.detach() * self._interior).contiguous()
         u_t = u_tensor.detach().contiguous()
-        torch.cuda.synchronize()
+        gm = torch.empty(self.num_elements, dtype=torch.float64, device=u_tensor.device)
+        gf = torch.empty(self.n, dtype=torch.float64, device=u_tensor.device)
+        _library_waits_for_torch(self.ctx)
         rhs = GPUVector(self.ctx, wrap=rhs_t)
         u = GPUVector(self.ctx, wrap=u_t)
         self.lam.set(0.0)
         self.solverT.apply(self.lam, rhs)
-        gm = torch.empty(self.num_elements, dtype=torch.float64, device=u_tensor.device)
-        gf = torch.empty(self.n, dtype=torch.float64, device=u_tensor.device)
         self.disc.grad_logk(u, self.lam, out=gm)
         self.disc.grad_source(self.lam, out=gf)
-        self.ctx.synchronize()
+        _torch_waits_for_library(self.ctx)
         self.last_adjoint_stats = self.solverT.stats()
         return gm, gf
 
@@ -75,8 +92,7 @@ class FV1Solve(torch.autograd.Function):
     @staticmethod
     def forward(ctx, m, f, problem):
         problem.update(m, f)
-        u = torch.empty(problem.n, dtype=torch.float64, device=m.device)
-        problem.solve_into(u)
+        u = problem.solve_u()
         ctx.problem = problem
         ctx.save_for_backward(u)
         return u
