@@ -237,6 +237,30 @@ UG4GB_API int ug4gb_matrix_get_row(const ug4gb_matrix *A, int row, int *cols, do
 UG4GB_API int ug4gb_matrix_add_entries(ug4gb_matrix *A, int n, const int *rows, const int *cols,
                                        const double *vals);
 
+/* ----------------------------------------------------- DoF permutation -- */
+/* No ugcore counterpart (ugcore has one numbering).  The engine numbers the
+   vertices of a level its own way (lexicographic on structured levels, the
+   refinement order on unstructured ones); ugcore numbers DoFs in lib_grid's
+   element-list order (DoFDistribution::reinit, lib_disc/dof_manager/
+   dof_distribution.cpp:1339-1440).  A ug4gb_perm moves vectors and operators
+   between the two numberings: perm[i] = engine index of external DoF i (a
+   bijection of 0..n-1; host or device array). */
+typedef struct ug4gb_perm ug4gb_perm;
+UG4GB_API int ug4gb_perm_create(ug4gb_ctx *ctx, int n, const int *engine_of_external, ug4gb_perm **out);
+/* the permutation that matches external DoF positions (n x dim doubles, host
+   or device; the vertex positions of ugcore's DoFs) to the vertices of
+   `level` of g, each within distance tol of exactly one unused vertex */
+UG4GB_API int ug4gb_perm_from_positions(ug4gb_ctx *ctx, const ug4gb_grid *g, int level, int n,
+                                        const double *positions, double tol, ug4gb_perm **out);
+/* to_external = 1: dst[i] = src[perm[i]] (engine -> external); 0: the inverse */
+UG4GB_API int ug4gb_perm_vector(const ug4gb_perm *p, int to_external, const ug4gb_vector *src, ug4gb_vector *dst);
+/* to_external = 1: B(i, j) = A(perm[i], perm[j]) (columns sorted per row);
+   0: the inverse.  The pattern of B and the value map are built once per
+   pattern of A (an assembled level operator); later calls after a
+   re-assembly of the same pattern only gather the values. */
+UG4GB_API int ug4gb_perm_matrix(ug4gb_perm *p, int to_external, const ug4gb_matrix *A, ug4gb_matrix *B);
+UG4GB_API void ug4gb_perm_destroy(ug4gb_perm *p);
+
 /* ------------------------------------------------------ discretisation -- */
 /* Replaces DomainDiscretization (lib_disc/spatial_disc/domain_disc.h) with one
    FV1 convection-diffusion IElemDisc (elem_disc_interface.h:797; the

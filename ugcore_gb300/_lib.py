@@ -144,6 +144,11 @@ _SIGS = {
     "ug4gb_solver_set_convergence_check": (I, [P, I, D, D]),
     "ug4gb_solver_init": (I, [P, P]),
     "ug4gb_solver_set_restart": (I, [P, I]),
+    "ug4gb_perm_create": (I, [P, I, P, C.POINTER(P)]),
+    "ug4gb_perm_from_positions": (I, [P, P, I, I, P, D, C.POINTER(P)]),
+    "ug4gb_perm_vector": (I, [P, I, P, P]),
+    "ug4gb_perm_matrix": (I, [P, I, P, P]),
+    "ug4gb_perm_destroy": (None, [P]),
     "ug4gb_solver_set_min_orthogonality": (I, [P, D]),
     "ug4gb_solver_apply_return_defect": (I, [P, P, P]),
     "ug4gb_solver_apply": (I, [P, P, P]),

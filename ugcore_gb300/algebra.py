@@ -566,6 +566,38 @@ class SymmetricGaussSeidel:
         self.kind, self.damp = _lib.SMOOTHER_MCSGS, float(relax)
 
 
+class DofPermutation:
+    """DoF permutation between the engine's vertex numbering of a level and
+    an external numbering (ugcore's DoFDistribution): perm[i] = engine index
+    of external DoF i.  No ugcore counterpart."""
+
+    def __init__(self, ctx, perm=None, hier=None, level=None, positions=None, tol=1e-9):
+        self.ctx = ctx
+        h = C.c_void_p()
+        if perm is not None:
+            self._perm = np.ascontiguousarray(perm, np.int32)
+            check(lib().ug4gb_perm_create(ctx.h, len(self._perm), _ptr(self._perm), C.byref(h)), ctx.h)
+        else:
+            level = hier.top if level is None else level
+            x = np.ascontiguousarray(positions, np.float64)
+            check(lib().ug4gb_perm_from_positions(ctx.h, hier.h, level, x.shape[0], _ptr(x), float(tol),
+                                                  C.byref(h)), ctx.h)
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ug4gb_perm_destroy(self.h)
+            self.h = None
+
+    def vector(self, src, dst, to_external=True):
+        check(lib().ug4gb_perm_vector(self.h, int(bool(to_external)), src.h, dst.h), self.ctx.h)
+        return dst
+
+    def matrix(self, A, B, to_external=True):
+        check(lib().ug4gb_perm_matrix(self.h, int(bool(to_external)), A.h, B.h), self.ctx.h)
+        return B
+
+
 class StdTransfer:
     """StdTransfer (lib_disc/operator/linear_operator/std_transfer.h:57): P1
     prolongation / restriction between the levels of the hierarchy.  The
