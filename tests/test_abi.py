@@ -169,3 +169,54 @@ int main() { return ug::GPUAlgebra::get_type().type() == ug::AlgebraType::GPU ? 
                         "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "ugcore_gb300", "adapters"),
                         str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
+
+
+BOOST_STANDIN_HEADERS = [
+    "boost/mpl/at.hpp", "boost/mpl/empty.hpp", "boost/mpl/fold.hpp", "boost/mpl/for_each.hpp", "boost/mpl/front.hpp",
+    "boost/mpl/if.hpp", "boost/mpl/list.hpp", "boost/mpl/map.hpp", "boost/mpl/min_max.hpp", "boost/mpl/pop_front.hpp",
+    "boost/mpl/size.hpp", "boost/mpl/transform_view.hpp", "boost/optional.hpp", "boost/serialization/access.hpp",
+    "boost/serialization/export.hpp", "boost/serialization/level.hpp", "boost/serialization/nvp.hpp",
+    "boost/serialization/version.hpp"]
+
+
+@pytest.mark.parametrize("negative", [False, True])
+def test_ugcore_bridge_compiles_against_ugcore_headers(tmp_path, negative):
+    """The ugcore-side bridge -- UG4GBDomainDiscretization as ugcore's
+    IDomainDiscretization<GPUAlgebra> (ug4gb_domain_disc.h), the multigrid on
+    it (ug4gb_preconditioner.h) and the registration RegisterUG4GB /
+    InitUGPlugin_UG4GB (ug4gb_bridge.cpp) -- compiles against ugcore's own
+    lib_disc, lib_grid, registry and bridge headers for 2D and 3D domains
+    (both instantiated), with the Boost headers they name replaced by the
+    stand-in tests/standins/boost/ug_boost_standin.hpp (Boost is absent).
+    The negative case plants a wrong call in a copy of the adapter to show
+    that the instantiated code is checked."""
+    from helpers import reference_tree
+    ref = reference_tree()
+    if ref is None:
+        pytest.skip("ugcore source tree not present")
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    shim = tmp_path / "shim"
+    for h in BOOST_STANDIN_HEADERS:
+        (shim / h).parent.mkdir(parents=True, exist_ok=True)
+        (shim / h).write_text('#include "boost/ug_boost_standin.hpp"\n')
+    src_dir = os.path.join(ROOT, "ugcore_gb300", "adapters")
+    if negative:
+        work = tmp_path / "adapters"
+        shutil.copytree(src_dir, work)
+        dd = work / "ug4gb_domain_disc.h"
+        txt = dd.read_text()
+        bad = txt.replace("ug4gb_disc_adjust_solution(m_disc, m_top, m_u->get())",
+                          "ug4gb_disc_adjust_solution(m_disc, m_top, m_u->get(), 1)")
+        assert bad != txt
+        dd.write_text(bad)
+        src_dir = str(work)
+    r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-w", "-DUG_DIM_2", "-DUG_DIM_3", "-I" + str(shim),
+                        "-I" + os.path.join(ROOT, "tests", "standins"), "-I" + os.path.join(ref, "ugbase"),
+                        "-I" + os.path.join(ROOT, "include"), "-I" + src_dir,
+                        os.path.join(src_dir, "ug4gb_bridge.cpp")], capture_output=True, text=True)
+    if negative:
+        assert r.returncode != 0 and "ug4gb_disc_adjust_solution" in r.stderr
+    else:
+        assert r.returncode == 0, r.stderr[-4000:]

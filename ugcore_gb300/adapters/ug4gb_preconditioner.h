@@ -14,6 +14,7 @@
 // Needs ugcore's lib_algebra headers on the include path, like ug4gb_algebra.h.
 #pragma once
 
+#include <memory>
 #include <string>
 
 #include "lib_algebra/operator/interface/linear_iterator.h"
@@ -32,7 +33,17 @@ public:
 
     /// disc: the library discretisation of the grid hierarchy the levels come from
     explicit UG4GBGeometricMultiGrid(ug4gb_disc *disc) : m_disc(disc) { create(); }
-    UG4GBGeometricMultiGrid(const UG4GBGeometricMultiGrid &o) : base_type(o), m_disc(o.m_disc), m_cfg(o.m_cfg)
+    /// the multigrid of a UG4GBDomainDiscretization (ug4gb_domain_disc.h):
+    /// operators and vectors come in ugcore's DoF numbering and cross to the
+    /// engine's through the discretisation's DoF permutation
+    template <class TDomainDisc>
+    explicit UG4GBGeometricMultiGrid(SmartPtr<TDomainDisc> domainDisc)
+        : m_keep(domainDisc), m_disc(domainDisc->engine_disc()), m_perm(domainDisc->engine_perm())
+    {
+        create();
+    }
+    UG4GBGeometricMultiGrid(const UG4GBGeometricMultiGrid &o)
+        : base_type(o), m_keep(o.m_keep), m_disc(o.m_disc), m_perm(o.m_perm), m_cfg(o.m_cfg)
     {
         create();
     }
@@ -56,6 +67,18 @@ public:
         configure();
     }
     void set_rap(bool rap) { m_cfg.rap = rap; configure(); }
+    /// AssembledMultiGridCycle::set_transfer with a StdTransfer's damping
+    /// (std_transfer.h:92,95)
+    void set_transfer_damping(double prolongation, double restriction)
+    {
+        ug4gb_glue::guarded(
+            [&] {
+                ug4gb_ctx *ctx = ug4gb_glue::context().get();
+                ug4gb::check(ug4gb_gmg_set_prolongation_damping(m_gmg, prolongation), ctx, "prolongation damping");
+                ug4gb::check(ug4gb_gmg_set_restriction_damping(m_gmg, restriction), ctx, "restriction damping");
+            },
+            "GPU GeometricMultiGrid::set_transfer");
+    }
     /// coarse levels assembled as a time discretisation's jacobian (null: stationary)
     void set_discretization(ug4gb_timedisc *td)
     {
@@ -74,7 +97,22 @@ public:
         if (op.invalid()) UG_THROW("GPU GeometricMultiGrid: the operator is not an assembled GPU matrix");
         m_A = &op->get_matrix();
         ug4gb_glue::guarded(
-            [&] { ug4gb::check(ug4gb_gmg_init(m_gmg, m_A->impl().get()), ug4gb_glue::context().get(), "gmg init"); },
+            [&] {
+                ug4gb_ctx *ctx = ug4gb_glue::context().get();
+                const ug4gb_matrix *A = m_A->impl().get();
+                if (m_perm) {
+                    // the top operator in the engine's numbering
+                    if (!m_Aeng) m_Aeng.reset(new ug4gb::Matrix(ctx));
+                    ug4gb::check(ug4gb_perm_matrix(m_perm, 0, A, m_Aeng->get()), ctx, "permute operator");
+                    A = m_Aeng->get();
+                    const int n = (int)m_A->num_rows();
+                    if (!m_deng || m_deng->size() != n) {
+                        m_deng.reset(new ug4gb::Vector(ctx, n));
+                        m_ceng.reset(new ug4gb::Vector(ctx, n));
+                    }
+                }
+                ug4gb::check(ug4gb_gmg_init(m_gmg, A), ctx, "gmg init");
+            },
             "GPU GeometricMultiGrid::init");
         return true;
     }
@@ -84,8 +122,14 @@ public:
     {
         ug4gb_glue::guarded(
             [&] {
-                ug4gb::check(ug4gb_gmg_apply(m_gmg, c.impl().get(), d.impl().get()), ug4gb_glue::context().get(),
-                             "gmg apply");
+                ug4gb_ctx *ctx = ug4gb_glue::context().get();
+                if (m_perm) {
+                    ug4gb::check(ug4gb_perm_vector(m_perm, 0, d.impl().get(), m_deng->get()), ctx, "permute d");
+                    ug4gb::check(ug4gb_gmg_apply(m_gmg, m_ceng->get(), m_deng->get()), ctx, "gmg apply");
+                    ug4gb::check(ug4gb_perm_vector(m_perm, 1, m_ceng->get(), c.impl().get()), ctx, "permute c");
+                } else {
+                    ug4gb::check(ug4gb_gmg_apply(m_gmg, c.impl().get(), d.impl().get()), ctx, "gmg apply");
+                }
             },
             "GPU GeometricMultiGrid::apply");
         return true;
@@ -140,10 +184,14 @@ private:
             "GPU GeometricMultiGrid configuration");
     }
 
+    SmartPtr<void> m_keep;               // the domain discretisation that owns m_disc / m_perm, or null
     ug4gb_disc *m_disc = nullptr;
+    ug4gb_perm *m_perm = nullptr;
     ug4gb_gmg *m_gmg = nullptr;
     Config m_cfg;
     const matrix_type *m_A = nullptr;
+    std::shared_ptr<ug4gb::Matrix> m_Aeng;   // the top operator in the engine's numbering
+    std::shared_ptr<ug4gb::Vector> m_deng, m_ceng;
 };
 
 }  // namespace ug
