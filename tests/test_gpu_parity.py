@@ -350,7 +350,11 @@ def test_cycle_types_match_oracle(ctx, oracle_lib, name, cycle, over):
     """W-, F- (-1: the coarser level once as F, then once as V) and gamma = 3
     cycles (AssembledMultiGridCycle::lmgc, mg_solver_impl.hpp:2091-2134):
     GMG application 1e-12, solve iterations +-1.  The F-cycle is not a
-    symmetric preconditioner, so its lognormal case runs BiCGStab"""
+    symmetric preconditioner, so its lognormal case runs BiCGStab, whose step
+    count on this problem moves under rounding-level changes of the
+    operator: the oracle alone needs 57 to 60 half steps when K is perturbed
+    by 1e-16..1e-15 relative (wavenumbers scaled by 1 + k 1e-16, |k| <= 12);
+    that case is held to 10% and to the solution (1e-8)"""
     import ugcore_gb300 as ug
     cfg, p = _problem(ctx, name, dict(over, cycle=cycle, precision="fp64"))
     op = _oracle(oracle_lib, cfg, p)
@@ -361,4 +365,8 @@ def test_cycle_types_match_oracle(ctx, oracle_lib, name, cycle, over):
     ref = op.apply_gmg(d)
     assert np.abs(cv.numpy() - ref).max() <= 1e-12 * np.abs(ref).max()
     st, rs = p.solve(), op.solve()
-    assert abs(st["steps"] - rs["steps"]) <= 1
+    if cfg["solver"] == "bicgstab" and cfg["coef"] == "lognormal":
+        assert abs(st["steps"] - rs["steps"]) <= max(1, 0.1 * rs["steps"]), (st["steps"], rs["steps"])
+        assert np.abs(p.x.numpy() - rs["x"]).max() <= 1e-8 * np.abs(rs["x"]).max()
+    else:
+        assert abs(st["steps"] - rs["steps"]) <= 1
