@@ -324,6 +324,9 @@ UG4GB_API int ug4gb_timedisc_assemble_defect(ug4gb_timedisc *td, int level, cons
                                              ug4gb_vector *dvec);
 UG4GB_API void ug4gb_timedisc_destroy(ug4gb_timedisc *td);
 
+/* AT may be A itself: the values are transposed in place (the level
+   operators' patterns are symmetric; UG4GB_ERR_INVALID otherwise), which
+   keeps the adjoint solve within the forward solve's memory */
 UG4GB_API int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A, ug4gb_matrix *AT);
 /* element coefficient K of a level (host or device out array, num_elements) */
 UG4GB_API int ug4gb_disc_export_coefficients(ug4gb_disc *d, int level, double *K);
@@ -351,7 +354,10 @@ UG4GB_API int ug4gb_gmg_set_precision(ug4gb_gmg *m, int precision);
 UG4GB_API int ug4gb_gmg_set_prolongation_damping(ug4gb_gmg *m, double damp);
 UG4GB_API int ug4gb_gmg_set_restriction_damping(ug4gb_gmg *m, double damp);
 /* transposed = 1 builds the cycle on A^T of every level (Dirichlet rows reset
-   to identity): the preconditioner of the adjoint solve */
+   to identity): the preconditioner of the adjoint solve.  The level operators
+   are transposed in place, so one multigrid may alternate between the
+   forward and the transposed cycle (set_transposed, then init) on the same
+   buffers: re-assembly instead of a second stored hierarchy */
 UG4GB_API int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed);
 /* AssembledMultiGridCycle::set_rap (mg_solver.h:149; Lua gmg:set_rap(true),
    multigrid_bridge.cpp:214): rap = 1 makes every coarse level operator the

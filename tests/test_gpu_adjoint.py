@@ -146,3 +146,67 @@ def test_repeated_gradients_reuse_the_adjoint_set_up(ctx, precision):
     g2_fresh = grad(fresh, m_true * 1.3, f)
     assert not np.array_equal(g1, g2)
     assert np.array_equal(g2.view(np.int64), g2_fresh.view(np.int64))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_recomputed_adjoint_equals_stored(ctx, precision):
+    """adjoint_memory "recompute" (the forward operator and multigrid
+    transposed in place for the adjoint, re-assembled for the next forward
+    solve) gives the gradients of the stored transposed hierarchy to 1e-12,
+    also after alternating forward and adjoint solves"""
+    import torch
+    from ugcore_gb300 import adjoint, problems
+
+    def grads(mode):
+        cfg = problems.config("c3", nref=5, precision=precision, adjoint_memory=mode)
+        prob = adjoint.DifferentiableProblem(ctx, cfg)
+        m0 = torch.tensor(prob.m_top, device="cuda")
+        f = torch.ones(prob.n, dtype=torch.float64, device="cuda")
+        out = []
+        for s in (0.7, 1.3, 0.7):
+            mm = (m0 * s).clone().requires_grad_(True)
+            u = adjoint.fv1_solve(mm, f, prob)
+            (0.5 * (u ** 2).sum()).backward()
+            out.append(mm.grad.cpu().numpy())
+        return out
+
+    gs, gr = grads("store"), grads("recompute")
+    for a, b in zip(gs, gr):
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+    assert np.array_equal(gr[0], gr[2])
+
+
+def test_recomputed_adjoint_memory_c4_full_size(ctx):
+    """193^3 convection-diffusion with the FP32 multigrid: the adjoint solve
+    with adjoint_memory "recompute" holds no more than 1.15x the forward
+    solve's device memory (the stored transposed hierarchy needs a second
+    one), and its source gradient equals the stored variant's to 1e-12"""
+    import torch
+    from ugcore_gb300 import problems
+
+    def run(mode):
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        p = problems.Problem(ctx, problems.config("c4", adjoint_memory=mode))
+        st = p.solve()
+        assert st["converged"]
+        ctx.synchronize()
+        fwd = free0 - torch.cuda.mem_get_info()[0]
+        u = p.x.numpy()
+        S = np.random.default_rng(p.cfg["seed"]).random(p.n) < 0.1
+        ast = p.adjoint_solve(np.where(S, 2.0 * u, 0.0))
+        assert ast["converged"]
+        g = p.disc.grad_source(p.lam)
+        ctx.synchronize()
+        both = free0 - torch.cuda.mem_get_info()[0]
+        del p
+        ctx.synchronize()
+        return fwd, both, g
+
+    f_r, b_r, g_r = run("recompute")
+    f_s, b_s, g_s = run("store")
+    print("c4 device memory: forward %.2f GB; with the adjoint: recompute %.2f GB, store %.2f GB"
+          % (f_r / 1e9, b_r / 1e9, b_s / 1e9))
+    assert b_r <= 1.15 * f_r, (b_r, f_r)
+    assert b_s > 1.15 * f_s
+    assert np.abs(g_r - g_s).max() <= 1e-12 * np.abs(g_s).max()

@@ -54,8 +54,10 @@ class DifferentiableProblem(problems.Problem):
         self.disc.set_log_diffusion(self._inputs[0])
         self.disc.set_source(self._inputs[1])
         self.disc.assemble_linear(self.A, self.b)
+        self.gmg.set_transposed(False)
         self.gmg.init(self.A)
         self.solver.init(self.A)
+        self._fwd_valid = True
         self.invalidate_adjoint()
 
     def solve_u(self):

@@ -425,8 +425,25 @@ void ug4gb_timedisc_destroy(ug4gb_timedisc *td)
 
 int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A, ug4gb_matrix *AT)
 {
-    if (!d || !A || !AT || A == AT || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
+    if (!d || !A || !AT || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
     if (A->A.nrows != d->g->lev[level].nv) return UG4GB_ERR_INVALID;
+    if (A == AT) {
+        // in place: the pattern is symmetric (checked once per pattern), the
+        // values of each pair (i, j), (j, i) are swapped; no extra memory
+        return guarded(d->ctx, [&] {
+            Ctx &c = d->ctx->c;
+            ug4gb_matrix *M = AT;
+            const uint64_t key = M->pattern_key();
+            if (!key || M->sym_key != key) {
+                UG_REQUIRE(csr_pattern_symmetric(c, M->A), UG4GB_ERR_INVALID,
+                           "adjoint operator in place: the operator's pattern is not symmetric");
+                M->sym_key = key;
+            }
+            csr_transpose_symmetric_inplace(c, M->A);
+            launch_dirichlet(c, d->g->lev[level], M->A, nullptr);
+            M->op_valid = false;
+        });
+    }
     return guarded(d->ctx, [&] {
         Ctx &c = d->ctx->c;
         // the transposition of a level's element pattern is computed once;

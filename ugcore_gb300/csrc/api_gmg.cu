@@ -180,6 +180,7 @@ struct GmgT : GmgBase {
     double damp = 1.0;
     DevBuf<double> Ainv;
     DevBuf<double> z64;          // mixed precision: FP64 copy of the top correction
+    uint64_t top_key = 0;        // pattern key of the top operator of the last set-up
     int nbase = 0;
     bool top_converted = false;  // this apply: the FP32 top defect is already in dA of the top level
 
@@ -537,14 +538,20 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
     G->lev.resize(nl);
     UG_REQUIRE(m->base >= 0 && m->base < nl, UG4GB_ERR_INVALID, "GMG: base level out of range");
     UG_REQUIRE(A_top->A.nrows == g->lev[nl - 1].nv, UG4GB_ERR_INVALID, "GMG: top operator size != top level");
-    // transposed multigrid: A of the level = (Aasm)^T with Dirichlet rows
-    // reset to identity; the transposition permutation is kept for re-inits
-    auto transpose_level = [&](int l, const Csr &src, bool same_pattern) {
+    // transposed multigrid: A of the level = A^T with Dirichlet rows reset to
+    // identity.  The level patterns (element cliques, and R A P of them) are
+    // symmetric, so A^T has A's pattern and its values are swapped pairwise
+    // in place (no second copy of the level); a non-symmetric pattern (a
+    // user's top operator) is transposed explicitly
+    auto transpose_level = [&](int l, bool same_pattern) {
         GLevel<V> &L = G->lev[l];
-        if (same_pattern && L.tperm.p && L.A.nnz == src.nnz) {
-            transpose_values(c, src, L.A, L.tperm);
+        if (!same_pattern || L.sym < 0) L.sym = csr_pattern_symmetric(c, L.A) ? 1 : 0;
+        if (L.sym == 1) {
+            csr_transpose_symmetric_inplace(c, L.A);
         } else {
-            transpose_perm(c, src, L.A, L.tperm);
+            Csr T;
+            csr_transpose(c, L.A, T, true);
+            L.A = std::move(T);
         }
         UG_LAUNCH(c, k_dirichlet_identity, div_up(L.A.nrows, 256), 256, 0, g->lev[l].bnd.p, L.A.nrows, L.A.rowptr.p,
                   L.A.col.p, L.A.val.p);
@@ -552,8 +559,11 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
     if (!m->rap) {
         for (int l = m->base; l < nl; ++l) {
             GLevel<V> &L = G->lev[l];
-            const bool same = keep_transfers && L.asm_ok;
-            Csr &dst = m->transposed ? L.Aasm : L.A;
+            // the level's pattern is the one of the previous set-up (the top
+            // level: the same assembled operator pattern as then)
+            const bool same = keep_transfers && L.asm_ok &&
+                              (l != nl - 1 || (A_top->pattern_key() && A_top->pattern_key() == G->top_key));
+            Csr &dst = L.A;
             // level operator: copy of the surface operator on the top level,
             // re-assembled on coarser levels (assemble_level_operator, :528-750)
             if (l == nl - 1) {
@@ -576,7 +586,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
                 disc_assemble(m->disc, l, &tmp, nullptr, m->td ? &ts : nullptr);
                 dst = std::move(tmp.A);
             }
-            if (m->transposed) transpose_level(l, L.Aasm, same);
+            if (m->transposed) transpose_level(l, same);
             L.asm_ok = true;
             G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base, same);
             if (l > m->base) {
@@ -589,12 +599,8 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
         // Galerkin coarse operators (init_rap_operator, :830-1012): the top
         // level's operator, then from the top down the transfers of a level
         // and R A P of it as the operator of the level below
-        if (m->transposed) {
-            csr_copy(c, A_top->A, G->lev[nl - 1].Aasm);
-            transpose_level(nl - 1, G->lev[nl - 1].Aasm, false);
-        } else {
-            csr_copy(c, A_top->A, G->lev[nl - 1].A);
-        }
+        csr_copy(c, A_top->A, G->lev[nl - 1].A);
+        if (m->transposed) transpose_level(nl - 1, false);
         for (int l = nl - 1; l > m->base; --l) {
             if (!keep_transfers) G->setup_transfers(c, G->lev[l], g->lev[l], g->lev[l - 1], m->damp_prol, m->damp_res);
             csr_rap(c, G->lev[l].R, G->lev[l].A, G->lev[l].P, G->lev[l - 1].A);
@@ -608,6 +614,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
     }
     G->setup_base(c);
     if (sizeof(V) != sizeof(double)) G->z64.alloc(g->lev[nl - 1].nv);
+    G->top_key = A_top->pattern_key();
     return guard.release();
 }
 
@@ -742,8 +749,10 @@ int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         // a re-init with the same hierarchy and structure (typically a new
         // operator every Newton, time or optimisation step) keeps the level
         // buffers and the transfers and refreshes the values in place
+        // (the transposition is applied to the values in place: a flip between
+        // the forward and the transposed cycle keeps the structure)
         const GmgKey key{m->disc->g->uid, (int)m->disc->g->lev.size(), m->base, m->smoother, m->damp, m->rap,
-                         m->transposed, m->precision, m->ctx->c.allow_dia ? 1 : 0, m->damp_prol, m->damp_res};
+                         0, m->precision, m->ctx->c.allow_dia ? 1 : 0, m->damp_prol, m->damp_res};
         const bool reuse = m->impl && m->built == key;
         const uint64_t before = reuse ? (m->impl->signature() ^ m->built_settings) : 0;
         GmgBase *old = reuse ? m->impl.release() : nullptr;

@@ -458,6 +458,13 @@ void op_from_csr_cached(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_sca
 // A's through perm (the same pattern)
 void transpose_perm(Ctx &c, const Csr &A, Csr &T, DevBuf<int> &perm);
 void transpose_values(Ctx &c, const Csr &A, Csr &T, const DevBuf<int> &perm);
+// the same row pointers and column indices (one host round trip)
+bool csr_same_pattern(Ctx &c, const Csr &A, const Csr &B);
+// the pattern holds (j, i) for every (i, j) (one host round trip)
+bool csr_pattern_symmetric(Ctx &c, const Csr &A);
+// A = A^T in place for a symmetric pattern: every pair (i, j), (j, i) of
+// values swapped; no extra memory
+void csr_transpose_symmetric_inplace(Ctx &c, Csr &A);
 void fill_double(Ctx &c, double *p, size_t n, double v);
 // after a synchronisation of the stream: throws if a kernel reported that one
 // of its bounded waits ran out (and clears the flag)

@@ -52,6 +52,8 @@ struct ug4gb_matrix {
     // transposition permutation of the adjoint operator and its source key
     ug4gb::DevBuf<int> tperm;
     uint64_t tperm_key = 0;
+    // pattern key for which the pattern was found symmetric (in-place adjoint)
+    uint64_t sym_key = 0;
     // identity of the current pattern: the element pattern of (grid, level),
     // or the transposed one; 0 = any other (set from arrays, products, ...)
     uint64_t pattern_key() const
@@ -114,9 +116,8 @@ struct GLevel {
     DevBuf<V> y;                     // ILU forward-substitution scratch
     // kept for a re-init on the same structure (values refreshed in place)
     OpLayout At_lay;                 // layout of At
-    bool asm_ok = false;             // A (or Aasm) holds this level's element pattern
-    Csr Aasm;                        // transposed multigrid: the level operator before transposition
-    DevBuf<int> tperm;               // its transposition permutation
+    bool asm_ok = false;             // A holds this level's pattern (re-assembled in place)
+    int sym = -1;                    // A's pattern is symmetric (1), not (0), unknown (-1)
     DevBuf<double> dinv64, dfac64;   // FP64 Jacobi factors
 };
 

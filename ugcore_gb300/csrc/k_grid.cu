@@ -624,6 +624,88 @@ void transpose_perm(Ctx &c, const Csr &A, Csr &T, DevBuf<int> &perm)
     }
 }
 
+__global__ void k_diff_int(int64_t n, const int *a, const int *b, int *flag)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && a[i] != b[i]) *flag = 1;
+}
+
+bool csr_same_pattern(Ctx &c, const Csr &A, const Csr &B)
+{
+    if (A.nrows != B.nrows || A.ncols != B.ncols || A.nnz != B.nnz) return false;
+    DevBuf<int> flag;
+    flag.alloc(1);
+    UG_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), c.stream));
+    UG_LAUNCH(c, k_diff_int, div_up((int64_t)A.nrows + 1, (int64_t)256), 256, 0, (int64_t)A.nrows + 1, A.rowptr.p,
+              B.rowptr.p, flag.p);
+    if (A.nnz) UG_LAUNCH(c, k_diff_int, div_up(A.nnz, (int64_t)256), 256, 0, A.nnz, A.col.p, B.col.p, flag.p);
+    int h = 0;
+    UG_CUDA(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    UG_CUDA(cudaStreamSynchronize(c.stream));
+    return h == 0;
+}
+
+// position of column c in row r (columns sorted), or -1
+__device__ __forceinline__ int row_find(const int *__restrict__ rowptr, const int *__restrict__ col, int r, int c)
+{
+    int lo = rowptr[r], hi = rowptr[r + 1] - 1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int cm = col[mid];
+        if (cm == c) return mid;
+        if (cm < c) lo = mid + 1; else hi = mid - 1;
+    }
+    return -1;
+}
+
+__global__ void k_check_symmetric(const int *rowptr, const int *col, int n, int *bad)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int a = rowptr[i]; a < rowptr[i + 1]; ++a) {
+        const int j = col[a];
+        if (j != i && (j < 0 || j >= n || row_find(rowptr, col, j, i) < 0)) {
+            atomicExch(bad, 1);
+            return;
+        }
+    }
+}
+
+// entry (i, j) swapped with (j, i), each pair by the row with the smaller index
+__global__ void k_transpose_symmetric(const int *rowptr, const int *col, double *val, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int a = rowptr[i]; a < rowptr[i + 1]; ++a) {
+        const int j = col[a];
+        if (j <= i) continue;
+        const int b = row_find(rowptr, col, j, i);
+        if (b < 0) continue;
+        const double t = val[a];
+        val[a] = val[b];
+        val[b] = t;
+    }
+}
+
+bool csr_pattern_symmetric(Ctx &c, const Csr &A)
+{
+    if (A.nrows != A.ncols) return false;
+    if (A.nrows == 0) return true;
+    DevBuf<int> bad;
+    bad.alloc(1);
+    UG_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), c.stream));
+    UG_LAUNCH(c, k_check_symmetric, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.nrows, bad.p);
+    int h = 0;
+    UG_CUDA(cudaMemcpyAsync(&h, bad.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    UG_CUDA(cudaStreamSynchronize(c.stream));
+    return h == 0;
+}
+
+void csr_transpose_symmetric_inplace(Ctx &c, Csr &A)
+{
+    if (A.nrows) UG_LAUNCH(c, k_transpose_symmetric, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows);
+}
+
 void transpose_values(Ctx &c, const Csr &A, Csr &T, const DevBuf<int> &perm)
 {
     if (T.nnz) UG_LAUNCH(c, k_gather_perm, div_up(T.nnz, (int64_t)256), 256, 0, T.nnz, perm.p, A.val.p, T.val.p);

@@ -29,7 +29,8 @@ from .algebra import (BiCGStab, CG, DomainDiscretization, GaussSeidel, Geometric
 BASE = dict(elem="quad", mx=2, my=2, mz=1, nref=6, seed=1, coef="const", diffusion=1.0, coef_modes=64,
             coef_kmax=8.0, vel=None, vel_modes=16, vel_kmax=2.0, peclet=10.0, solver="cg", smoother="jacobi",
             damp=0.6, nu1=2, nu2=2, cycle=1, base=0, precision="fp64", maxit=200, rel_red=1e-10,
-            min_defect=1e-300, rap=False, bicg_restart=0, bicg_min_ortho=0.0, damp_prol=1.0, damp_res=1.0)
+            min_defect=1e-300, rap=False, bicg_restart=0, bicg_min_ortho=0.0, damp_prol=1.0, damp_res=1.0,
+            adjoint_memory="store")
 
 CONFIGS = {
     "c0": dict(elem="quad", mx=2, my=2, nref=6),
@@ -123,8 +124,21 @@ class Problem:
             g.set_transfer(t)
         return g
 
+    def forward_ready(self):
+        """the operator, multigrid and solver hold the forward problem again
+        after an adjoint solve that reused them (adjoint_memory
+        "recompute"): re-assembly and a value refresh of the multigrid"""
+        if getattr(self, "_fwd_valid", True):
+            return
+        self.disc.assemble_linear(self.A, self.b)
+        self.gmg.set_transposed(False)
+        self.gmg.init(self.A)
+        self.solver.init(self.A)
+        self._fwd_valid = True
+
     def solve(self, raise_on_failure=True):
         """x = A^{-1} b from x0 = 0; b is kept."""
+        self.forward_ready()
         self.x.set(0.0)
         ok = self.solver.apply(self.x, self.b, raise_on_failure=raise_on_failure)
         st = self.solver.stats()
@@ -167,8 +181,28 @@ class Problem:
     def adjoint_setup(self):
         """A^T, the transposed multigrid and its solver for the current
         operator; the objects are kept across operator updates and only
-        re-initialised (invalidate_adjoint)."""
+        re-initialised (invalidate_adjoint).
+
+        adjoint_memory "store" (default): a second operator, multigrid and
+        solver hold the transposed problem beside the forward one.
+        "recompute": the forward operator and multigrid are transposed in
+        place (level by level, through the transposition permutation of their
+        symmetric patterns) and serve the adjoint solve; the next forward
+        solve re-assembles them.  The adjoint then needs no memory beyond the
+        forward solve's (the levels are recomputed instead of stored)."""
         if getattr(self, "_adj_ready", False):
+            return
+        if self.cfg.get("adjoint_memory", "store") == "recompute":
+            if getattr(self, "lam", None) is None:
+                self.lam = GPUVector(self.ctx, self.n)
+            self.forward_ready()
+            self.disc.adjoint_operator(self.A, self.A)
+            self.gmg.set_transposed(True)
+            self.gmg.init(self.A)
+            self.solver.init(self.A)
+            self.AT, self.gmgT, self.solverT = self.A, self.gmg, self.solver
+            self._fwd_valid = False
+            self._adj_ready = True
             return
         if getattr(self, "gmgT", None) is None:
             self.AT = GPUSparseMatrix(self.ctx)
