@@ -5,6 +5,12 @@ statistics as JSON, e.g. to profile one precision or layout in isolation:
     python -m ugcore_gb300.run_case --config c1 --nref 5 --format sell
     python -m ugcore_gb300.run_case --config c2 --precision mixed --direct --sweep-fusion 1
 
+--assemblies N re-assembles the top-level operator and rhs N times after
+the set-up and reports the time per assembly (--row-assembly 0 selects the
+element kernel instead of the row-wise one on structured levels):
+
+    python -m ugcore_gb300.run_case --config c1 --solves 0 --assemblies 3
+
 --ugx FILE runs an unstructured hierarchy instead (the UGX coarse grid refined
 --nref times, Dirichlet subsets --dirichlet, lognormal K, CG, Jacobi V(2,2)):
 
@@ -75,6 +81,8 @@ def main():
     ap.add_argument("--sweep-planes", type=int, default=None)
     ap.add_argument("--ugx", default=None)
     ap.add_argument("--dirichlet", default=None)
+    ap.add_argument("--assemblies", type=int, default=0)
+    ap.add_argument("--row-assembly", type=int, default=None)
     args = ap.parse_args()
 
     import ugcore_gb300 as ug
@@ -89,7 +97,8 @@ def main():
         over["damp"] = 0.6 if args.smoother == "jacobi" else 1.0
     ctx = ug.Context(0)
     ctx.set_operator_format(args.format)
-    ctx.set_tuning(sweep_fusion=args.sweep_fusion, sweep_planes=args.sweep_planes)
+    ctx.set_tuning(sweep_fusion=args.sweep_fusion, sweep_planes=args.sweep_planes,
+                   row_assembly=None if args.row_assembly is None else bool(args.row_assembly))
     t0 = time.perf_counter()
     p = ugx_problem(ctx, args) if args.ugx else problems.Problem(ctx, problems.config(args.config, **over))
     ctx.synchronize()
@@ -104,6 +113,13 @@ def main():
         out.append({"ms": (time.perf_counter() - t0) * 1e3, "steps": st["steps"],
                     "rel_residual": st["defect"] / st["initial_defect"]})
     res = {"config": args.ugx or args.config, "dofs": p.n, "setup_s": setup, "solves": out}
+    if args.assemblies:
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.assemblies):
+            p.disc.assemble_linear(p.A, p.b)
+        ctx.synchronize()
+        res["assembly_ms"] = (time.perf_counter() - t0) * 1e3 / args.assemblies
     if args.direct:
         prof = ctx.profile_end()
         res["kernels"] = {k: [v[0], round(v[1], 4)] for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
