@@ -105,6 +105,14 @@ UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
    values to rounding (the cells of a structured level are congruent up to
    the rounding of their corner coordinates); each is bit-reproducible. */
 #define UG4GB_TUNE_ROW_ASSEMBLY 4
+/* UG4GB_TUNE_SWEEP_WAIT_TEST (bytes, multiple of 16, 0..4096; default 0):
+   failure test of the fused sweeps only.  Block 0 of the next fused sweep
+   launched after the call (one launch) announces this many bytes more than
+   its first operator copy delivers, so its bounded wait runs out (half a
+   second): the block issues no further copies and leaves, the solve returns
+   UG4GB_ERR_CUDA ("a kernel's bounded wait ... ran out") and the context
+   stays usable.  Never set outside such a test. */
+#define UG4GB_TUNE_SWEEP_WAIT_TEST 5
 UG4GB_API int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value);
 /* per-launch CUDA-event timing of every kernel until profile_end, which
    writes "tag|kernel<TAB>launches<TAB>total_ms" lines into buf.  While it is

@@ -131,3 +131,29 @@ def test_wrapped_entries_keep_the_one_step_kernels():
         if mask:
             assert any("k_sweep2" in k for k in prof)
     assert np.array_equal(out[0], out[1])
+
+
+def test_bounded_wait_gives_up_and_the_context_recovers():
+    """failure detection without a fault: with the test-only setting
+    UG4GB_TUNE_SWEEP_WAIT_TEST block 0 of the next fused sweep announces bytes
+    that no copy delivers, so its bounded wait runs out (half a second); the
+    block issues no further copies, still joins the grid reduction, and the
+    solve reports UG4GB_ERR_CUDA.  The context stays usable: a solve on it
+    afterwards (setting off, fresh multigrid) is bit-identical to a solve on
+    a fresh context, so the error flag and the reduction counters were left
+    clean."""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import _lib
+    c = _ctx(ALL_LEVELS)
+    c.set_tuning(sweep_wait_test=64)
+    p = _problem(c, "c1", dict(nref=3), "mixed")
+    with pytest.raises(ug.UG4GBError) as ei:
+        p.solve()
+    assert ei.value.code == _lib.ERR_CUDA and "bounded wait" in str(ei.value)
+    c.set_tuning(sweep_wait_test=0)
+    q = _problem(c, "c1", dict(nref=3), "mixed")
+    s1 = q.solve()
+    r = _problem(_ctx(ALL_LEVELS), "c1", dict(nref=3), "mixed")
+    s2 = r.solve()
+    assert s1["converged"] and s1["steps"] == s2["steps"]
+    assert np.array_equal(q.x.numpy(), r.x.numpy())

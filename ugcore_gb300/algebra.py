@@ -75,7 +75,7 @@ class Context:
         """'auto' (diagonal layout for structured operators) or 'sell'."""
         check(lib().ug4gb_set_operator_format(self.h, {"auto": 0, "sell": 1}[fmt]), self.h)
 
-    def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None, row_assembly=None):
+    def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None, row_assembly=None, sweep_wait_test=None):
         """performance switches:
         pdl: programmatic dependent launch of the solve kernels;
         sweep_fusion: bit mask (1 on, 2 every level size) of the
@@ -85,6 +85,9 @@ class Context:
         row_assembly: stationary assembly of structured levels row by row
         from the per-class element geometry (default) or element by element
         (same values to rounding)."""
+        if sweep_wait_test is not None:
+            # failure test of the fused sweeps' bounded waits only
+            check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_SWEEP_WAIT_TEST, int(sweep_wait_test)), self.h)
         if row_assembly is not None:
             check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_ROW_ASSEMBLY, int(bool(row_assembly))), self.h)
         if pdl is not None:

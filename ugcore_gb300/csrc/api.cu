@@ -170,6 +170,10 @@ int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value)
         if (value < 2 || value > 128) return UG4GB_ERR_INVALID;
         ctx->c.sweep_fusion_tz = value;
         return UG4GB_OK;
+    case UG4GB_TUNE_SWEEP_WAIT_TEST:
+        if (value < 0 || value > 4096 || value % 16) return UG4GB_ERR_INVALID;
+        ctx->c.sweep_wait_test = value;
+        return UG4GB_OK;
     case UG4GB_TUNE_ROW_ASSEMBLY:
         if (value != 0 && value != 1) return UG4GB_ERR_INVALID;
         ctx->c.row_assembly = value != 0;

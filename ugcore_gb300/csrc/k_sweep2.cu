@@ -56,6 +56,10 @@ struct Sweep2Args {
     int rho_kind;
     double *__restrict__ z64;
     int *err;                    // set when a bounded wait for the block's own copies runs out
+    // failure test only (0 in every solve): extra bytes block 0 announces for
+    // its first operator plane, which no copy delivers, so that its bounded
+    // wait runs out (the give-up path exercised without a fault)
+    unsigned test_extra_tx;
 };
 
 // The stencils of the structured levels, in the order of the constant-offset
@@ -136,11 +140,22 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
 }
 // bounded wait for a phase of the block's own copies: gives up after about a
 // second, reports it through *err and lets the kernel run to its end
-constexpr unsigned kWaitTries = 1u << 22;
+// bounded by time, whatever try_wait's own suspension is: 0.5 s (a copy
+// that has not landed by then is reported, never waited for indefinitely)
+constexpr unsigned long long kWaitNs = 500000000ULL;
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int *err)
 {
-    for (unsigned t = 0; t < kWaitTries; ++t)
+    const unsigned long long t0 = global_ns();
+    for (unsigned t = 0;; ++t) {
         if (mbar_try_wait(bar, parity)) return true;
+        if ((t & 63u) == 63u && global_ns() - t0 > kWaitNs) break;
+    }
     if (err) atomicExch(err, 1);
     return false;
 }
@@ -262,6 +277,7 @@ __global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2)
     }
     __syncthreads();
 
+    const int pstart = dir > 0 ? z0 - 1 : z1, pend = dir > 0 ? z1 + 1 : z0 - 2;
     auto stage_x = [&](int pl) {
         const bool zin = pl >= 0 && pl < nz;
         const int po = zin ? pl * PS : 0;
@@ -280,7 +296,8 @@ __global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2)
             // the block's reads of this buffer (its previous use, ordered by the
             // barrier before this call) precede the asynchronous copy into it
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive_expect_tx(sBar + 8 * mb, (unsigned)(MT * sizeof(V)));
+            const bool test = a.test_extra_tx && p == pstart && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
+            mbar_arrive_expect_tx(sBar + 8 * mb, (unsigned)(MT * sizeof(V)) + (test ? a.test_extra_tx : 0u));
             tma_load_4d(sM + (unsigned)(mb * SM::MTB), &tmap, x0 - 4, y0 - 1, p, 0, sBar + 8 * mb);
         }
         const bool in = zin && own;
@@ -306,16 +323,23 @@ __global__ void __launch_bounds__(32 * TY, S <= 15 ? 3 : 2)
     unsigned phase = 0;   // bit b: parity of the next phase of operator buffer b
     bool ok = true;
 
-    const int pstart = dir > 0 ? z0 - 1 : z1, pend = dir > 0 ? z1 + 1 : z0 - 2;
     stage_x(pstart - dir);
     stage_x(pstart);
     issue(pstart);
     for (int p = pstart; p != pend; p += dir) {
         const int mb = p & 1;
         cp_async_wait_all();
-        if (ok) ok = mbar_wait(sBar + 8 * mb, (phase >> mb) & 1u, a.err);
+        const unsigned par = (phase >> mb) & 1u;
+        if (ok) ok = mbar_wait(sBar + 8 * mb, par, a.err);
         phase ^= 1u << mb;
-        __syncthreads();
+        // the block gives up together when a wait ran out: no further copies
+        // are issued, the copy of this plane gets one more bounded wait, and
+        // the block still joins the grid reduction below (its result is
+        // discarded: the host reports the error after the solve)
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) (void)mbar_wait(sBar + 8 * mb, par, nullptr);
+            break;
+        }
         if (p + dir != pend) issue(p + dir);
         const bool zin = p >= 0 && p < nz;
         const V *Mo = M + mb * MTE + (ty + 1) * LW + tx + 4;
@@ -608,6 +632,9 @@ bool smooth_pair(Ctx &c, const Sweep2Op *op, const GridPair &gp, const V *xA, co
         a.rho_kind = rho_kind;
         a.z64 = z64;
         a.err = c.dev_err.p;
+        // the failure test applies to one launch only
+        a.test_extra_tx = (unsigned)c.sweep_wait_test;
+        c.sweep_wait_test = 0;
         c.dev_err_possible = true;
         const bool rho = r_rho != nullptr;
         if (op->S == 15) {
