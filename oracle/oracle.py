@@ -54,7 +54,9 @@ def build():
 def lib():
     global _LIB
     if _LIB is None:
-        path = os.path.join(_HERE, "liboracle.so")
+        # UG4GB_ORACLE_LIB: another build of the same sources (the sanitizer
+        # build of tests/test_sanitizers.py)
+        path = os.environ.get("UG4GB_ORACLE_LIB") or os.path.join(_HERE, "liboracle.so")
         if not os.path.exists(path):
             build()
         L = C.CDLL(path)

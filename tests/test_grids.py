@@ -136,3 +136,34 @@ def test_oracle_solves_on_the_hierarchy(mio, oracle_lib, name, dirichlet):
     A = sp.csr_matrix((va, ci, rp))
     r = A @ rs["x"] - op.rhs()
     assert np.linalg.norm(r) < 1e-9 * np.linalg.norm(op.rhs())
+
+
+MALFORMED_UGX = [
+    "",
+    "<grid>",
+    '<grid><vertices coords="3">0 0 0 1 0</vertices><tetrahedrons>0 1 2 3</tetrahedrons></grid>',
+    '<grid><vertices coords="2">0 0 1 0 0 1</vertices><triangles>0 1 7</triangles></grid>',
+    '<grid><vertices coords="2">0 0 1 0 0 1</vertices><triangles>0 1</triangles></grid>',
+    '<grid><vertices coords="2">0 0 1 0 0 1</vertices><triangles>0 1 -3</triangles></grid>',
+    '<grid><vertices coords="9">0 0 0</vertices></grid>',
+    '<grid><vertices coords="2">0 0 1 0 0 1</vertices><triangles>0 1 2</triangles>'
+    '<subset_handler name="defSH"><subset name="A"><vertices>0 5</vertices></subset></subset_handler></grid>',
+    '<grid><vertices coords="2">0 0 1 0 0 1</vertices><triangles>0 1 2</triangles>'
+    '<subset_handler name="defSH"><subset name="A"><edges>9</edges></subset></subset_handler></grid>',
+    '<grid><vertices coords="2">a b c d e f</vertices><triangles>0 1 2</triangles></grid>',
+]
+
+
+@pytest.mark.parametrize("k", range(len(MALFORMED_UGX)))
+def test_malformed_ugx_files_are_rejected(mio, tmp_path, k):
+    """malformed UGX grids: an error with a message or a consistent level,
+    never a crash (also run under the sanitizers, test_sanitizers.py)"""
+    from ugcore_gb300 import UG4GBError
+    f = tmp_path / ("g%d.ugx" % k)
+    f.write_text(MALFORMED_UGX[k])
+    try:
+        L = mio.ugx_level(str(f), 1, 1, "A" if "subset" in MALFORMED_UGX[k] else None)
+    except UG4GBError as e:
+        assert str(e)
+        return
+    assert L["elems"].min() >= 0 and L["elems"].max() < len(L["coords"])

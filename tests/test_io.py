@@ -139,3 +139,51 @@ def test_errors_are_reported(tmp_path, mio):
         mio.write_cv_matrix(str(tmp_path / "m.mtx"), rp, ci, va, np.zeros((1, 2)))
     with pytest.raises(UG4GBError, match="entries"):
         mio.read_cv_vector(os.path.join(IO, "vec2d.vec"), 7)
+
+
+MALFORMED_MTX = [
+    "",                                                                   # empty file
+    "%%MatrixMarket matrix coordinate real general\n",                   # no size line
+    "%%MatrixMarket matrix coordinate real general\n3\n",                # short size line
+    "%%MatrixMarket matrix coordinate real general\n-2 2 1\n1 1 1.0\n",  # negative size
+    "%%MatrixMarket matrix coordinate real general\n2 2 5\n1 1 1.0\n",   # fewer entries than announced
+    "%%MatrixMarket matrix coordinate real general\n2 2 1\n0 1 1.0\n",   # index 0
+    "%%MatrixMarket matrix coordinate real general\n2 2 1\n1 x 1.0\n",   # non-numeric index
+    "%%MatrixMarket matrix coordinate real general\n2 2 1\n1 1 nanx\n",  # bad value
+    "%%MatrixMarket matrix coordinate real general\n99999999999 2 1\n1 1 1.0\n",   # size beyond int
+    "%%MatrixMarket matrix coordinate complex general\n2 2 1\n1 1 1.0 0.0\n",     # complex
+    "%%MatrixMarket matrix coordinate real general\n2 2 1\n" + "1 " * 5000 + "\n",  # a very long line
+    "%%MatrixMarket matrix coordinate real symmetric\n2 3 1\n1 1 1.0\n",  # non-square symmetric
+]
+
+
+@pytest.mark.parametrize("k", range(len(MALFORMED_MTX)))
+def test_malformed_mtx_files_are_rejected_or_read_safely(tmp_path, mio, k):
+    """malformed MatrixMarket files: an error with a message, or (for what
+    the format allows) a consistent matrix; never a crash (this test also runs
+    under AddressSanitizer/UndefinedBehaviorSanitizer in test_sanitizers.py)"""
+    from ugcore_gb300 import UG4GBError
+    f = tmp_path / ("m%d.mtx" % k)
+    f.write_text(MALFORMED_MTX[k])
+    try:
+        rp, ci, va, nc = mio.read_mtx(str(f))
+    except UG4GBError as e:
+        assert str(e)
+        return
+    assert rp[0] == 0 and np.all(np.diff(rp) >= 0) and len(ci) == rp[-1] == len(va)
+    assert len(ci) == 0 or (ci.min() >= 0 and ci.max() < nc)
+
+
+MALFORMED_VEC = ["", "1\n", "2\n0 0 1.0\n", "1\n0 0\n", "3\n0 0 1.0\n0 1 2.0\n", "1\nx y z\n"]
+
+
+@pytest.mark.parametrize("k", range(len(MALFORMED_VEC)))
+def test_malformed_cv_vectors_are_rejected_or_read_safely(tmp_path, mio, k):
+    from ugcore_gb300 import UG4GBError
+    f = tmp_path / ("v%d.vec" % k)
+    f.write_text(MALFORMED_VEC[k])
+    try:
+        v = mio.read_cv_vector(str(f), 2)
+        assert len(v) == 2
+    except UG4GBError as e:
+        assert str(e)

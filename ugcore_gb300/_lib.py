@@ -7,7 +7,9 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libug4gb.so")
+# UG4GB_LIB_PATH: another build of the same sources (the sanitizer build
+# tests/test_sanitizers.py loads); the default is the in-tree library
+LIB_PATH = os.environ.get("UG4GB_LIB_PATH") or os.path.join(HERE, "libug4gb.so")
 
 OK = 0
 ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_SINGULAR, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_STATE = -1, -2, -3, -4, -5, -6, -7

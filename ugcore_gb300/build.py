@@ -92,5 +92,39 @@ def build(verbose=False, extra_flags=()):
     return LIB
 
 
+def build_sanitized(out_dir):
+    """The library with AddressSanitizer and UndefinedBehaviorSanitizer in its
+    host code (the file parsers, the C-ABI argument checks, the hierarchy
+    set-up), for tests that load it with the sanitizer runtime preloaded;
+    device code is compiled as usual.  Returns the path of the .so."""
+    nvcc = _nvcc()
+    os.makedirs(out_dir, exist_ok=True)
+    # one option per -Xcompiler: nvcc splits its argument at commas
+    san = ["-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined", "-Xcompiler",
+           "-fno-omit-frame-pointer", "-Xcompiler", "-fno-sanitize-recover=undefined", "-g"]
+    flags = [f for f in NVCC_FLAGS if f != "-O3"] + ["-O1"]
+    lib = os.path.join(out_dir, "libug4gb_asan.so")
+    hdrs = _headers()
+    objs, jobs = [], []
+    for src in SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(out_dir, src.replace(".cu", ".o"))
+        objs.append(o)
+        if _newer(o, [s] + hdrs):
+            jobs.append([nvcc] + ARCH + flags + san + ["-c", s, "-o", o])
+    if jobs:
+        with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
+            for r in ex.map(lambda cmd: subprocess.run(cmd, capture_output=True, text=True), jobs):
+                if r.returncode:
+                    raise RuntimeError("nvcc failed (sanitized build): " + r.stderr[-2000:])
+    if jobs or _newer(lib, objs):
+        r = subprocess.run([nvcc] + ARCH + ["-shared", "-o", lib] + objs +
+                           ["-lcudart", "-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined"],
+                           capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError("link failed (sanitized build): " + r.stderr[-2000:])
+    return lib
+
+
 if __name__ == "__main__":
     print(build(verbose="-v" in sys.argv))
