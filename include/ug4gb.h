@@ -99,11 +99,14 @@ UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
 /* UG4GB_TUNE_SWEEP_PLANES (2..128): z planes a block of the fused sweeps
    marches through (default 8). */
 #define UG4GB_TUNE_SWEEP_PLANES 3
-/* UG4GB_TUNE_ROW_ASSEMBLY (0 or 1): stationary assembly of structured levels
-   row by row from the per-class element geometry (default 1), or with the
-   element kernel used for unstructured levels (0).  Both give the same
-   values to rounding (the cells of a structured level are congruent up to
-   the rounding of their corner coordinates); each is bit-reproducible. */
+/* UG4GB_TUNE_ROW_ASSEMBLY (0, 1 or 2): stationary assembly of structured
+   levels row by row from the per-class element geometry (1), in addition
+   with a constant coefficient and no convection from the one interior
+   stencil, computed once and written to every interior row (2, default;
+   the same values as 1), or with the element kernel used for unstructured
+   levels (0).  All give the same values to rounding (the cells of a
+   structured level are congruent up to the rounding of their corner
+   coordinates); each is bit-reproducible. */
 #define UG4GB_TUNE_ROW_ASSEMBLY 4
 /* UG4GB_TUNE_SWEEP_WAIT_TEST (bytes, multiple of 16, 0..4096; default 0):
    failure test of the fused sweeps only.  Block 0 of the next fused sweep

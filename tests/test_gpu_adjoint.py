@@ -176,6 +176,28 @@ def test_recomputed_adjoint_equals_stored(ctx, precision):
     assert np.array_equal(gr[0], gr[2])
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_recomputed_adjoint_nonsymmetric(ctx, precision):
+    """convection-diffusion (a non-symmetric operator): the adjoint solution
+    of adjoint_memory "recompute" equals the stored variant's, in the same
+    number of steps, before and after a forward solve in between"""
+    from ugcore_gb300 import problems
+
+    def lam(mode):
+        p = problems.Problem(ctx, problems.config("c4", nref=3, precision=precision, adjoint_memory=mode))
+        out = []
+        for _ in range(2):
+            p.solve()
+            u = p.x.numpy()
+            st = p.adjoint_solve(np.where(np.arange(p.n) % 7 == 0, u, 0.0))
+            out.append((p.lam.numpy(), st["steps"]))
+        return out
+
+    for (a, sa), (b, sb) in zip(lam("store"), lam("recompute")):
+        assert sa == sb
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max()
+
+
 def test_recomputed_adjoint_memory_c4_full_size(ctx):
     """193^3 convection-diffusion with the FP32 multigrid: the adjoint solve
     with adjoint_memory "recompute" holds no more than 1.15x the forward

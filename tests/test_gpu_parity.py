@@ -236,6 +236,30 @@ def test_row_assembly_matches_element_assembly(ctx, name, over):
     assert np.abs(b1 - b2).max() <= 1e-13 * np.abs(b2).max()
 
 
+@pytest.mark.parametrize("name,over", [("c0", dict(nref=4)), ("c1", dict(nref=3)),
+                                       ("c1", dict(nref=2, elem="tet")), ("c3", dict(nref=3, coef="const"))])
+def test_uniform_stencil_assembly_matches_rows(ctx, name, over):
+    """one coefficient and no convection: the interior stencil gathered once
+    and written to every interior row gives the bits of the row-wise kernel,
+    operator and rhs, on every level"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    cfg = problems.config(name, **over)
+    assert cfg["coef"] == "const" and cfg.get("vel", "none") in (None, "none")
+    c2 = ug.Context(0)
+    c2.set_tuning(row_assembly=1)
+    p1 = problems.Problem(ctx, cfg)
+    p2 = problems.Problem(c2, cfg)
+    for l in range(p1.hier.num_levels):
+        A1, A2 = ug.GPUSparseMatrix(ctx), ug.GPUSparseMatrix(c2)
+        p1.disc.assemble_jacobian(A1, l)
+        p2.disc.assemble_jacobian(A2, l)
+        e1, e2 = A1.export_csr(), A2.export_csr()
+        assert np.array_equal(e1[0], e2[0]) and np.array_equal(e1[1], e2[1])
+        assert np.array_equal(e1[2].view(np.int64), e2[2].view(np.int64)), "level %d" % l
+    assert np.array_equal(p1.b.numpy().view(np.int64), p2.b.numpy().view(np.int64))
+
+
 @pytest.mark.parametrize("name,over", [("c2", dict(nref=2)), ("c4", dict(nref=2)), ("c3", dict(nref=4))])
 def test_bitwise_reproducible(ctx, name, over):
     """assembly (coloured, no atomics), reductions and the solve give the same

@@ -83,13 +83,15 @@ class Context:
         sweep_planes: z planes per block of that smoother (these three leave
         results bit-identical);
         row_assembly: stationary assembly of structured levels row by row
-        from the per-class element geometry (default) or element by element
-        (same values to rounding)."""
+        from the per-class element geometry (True or 1), in addition from
+        the one interior stencil when the coefficient is constant and there
+        is no convection (2, the default), or element by element (False or
+        0); the same values to rounding."""
         if sweep_wait_test is not None:
             # failure test of the fused sweeps' bounded waits only
             check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_SWEEP_WAIT_TEST, int(sweep_wait_test)), self.h)
         if row_assembly is not None:
-            check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_ROW_ASSEMBLY, int(bool(row_assembly))), self.h)
+            check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_ROW_ASSEMBLY, int(row_assembly)), self.h)
         if pdl is not None:
             check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_PDL, int(bool(pdl))), self.h)
         if sweep_fusion is not None:

@@ -175,8 +175,8 @@ int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value)
         ctx->c.sweep_wait_test = value;
         return UG4GB_OK;
     case UG4GB_TUNE_ROW_ASSEMBLY:
-        if (value != 0 && value != 1) return UG4GB_ERR_INVALID;
-        ctx->c.row_assembly = value != 0;
+        if (value < 0 || value > 2) return UG4GB_ERR_INVALID;
+        ctx->c.row_assembly = value;
         return UG4GB_OK;
     default: ctx->c.err = "ug4gb_set_tuning: unknown knob"; return UG4GB_ERR_INVALID;
     }

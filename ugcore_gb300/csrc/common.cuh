@@ -90,7 +90,9 @@ struct Ctx {
     bool profiling = false;
     bool allow_dia = true;      // operators with <= 27 offsets use the diagonal layout
     bool pdl = true;            // programmatic dependent launch on the solve path
-    bool row_assembly = true;   // structured levels: stationary assembly row by row
+    // structured levels: stationary assembly row by row (1), and with one
+    // coefficient for all elements from the one interior stencil (2)
+    int row_assembly = 2;
     // two Jacobi steps per pass on structured 3D FP32 levels (bit mask):
     // 1 = on, 2 = every level size (else >= sweep_fusion_min_rows vertices)
     int sweep_fusion = 0;

@@ -307,6 +307,51 @@ __global__ void __launch_bounds__(128) k_assemble_rows(AsmArgs a, ClassData<T> c
     if (a.b) a.b[r] = vsum;
 }
 
+// interior rows with one coefficient K for all elements and no convection:
+// every interior row holds the same stencil.  One block per line of interior
+// rows (fixed j, k), whose values are contiguous in the CRS; thread 0
+// gathers the stencil of the interior row (1, 1, 1) with the arithmetic of
+// k_assemble_rows (so the values are the same), then the block writes the
+// line with consecutive threads on consecutive values.  b as in
+// k_assemble_rows, from the same sequence of SCV volumes.
+template <int T>
+__global__ void __launch_bounds__(128) k_assemble_rows_uniform(AsmArgs a, ClassData<T> cd)
+{
+    using S = Stencil<T>;
+    constexpr int MAXV = 8 * ClassTraits<T>::NC;
+    __shared__ double st[S::N];
+    __shared__ double vols[MAXV];
+    __shared__ int nvol;
+    const int nix = a.cx - 1, niy = a.cy - 1;
+    const int j = 1 + (int)(blockIdx.x % (unsigned)niy), k = (S::DIM == 3) ? 1 + (int)(blockIdx.x / (unsigned)niy) : 0;
+    if (threadIdx.x == 0) {
+        double acc[S::N];
+#pragma unroll
+        for (int s = 0; s < S::N; ++s) acc[s] = 0.0;
+        int m = 0;
+        gather_row<T>(cd, a, 1, 1, (S::DIM == 3) ? 1 : 0, nullptr, [&](int s, double v) { acc[s] += v; },
+                      [&](double vol) { if (m < MAXV) vols[m++] = vol; });
+#pragma unroll
+        for (int s = 0; s < S::N; ++s) st[s] = acc[s];
+        nvol = m;
+    }
+    __syncthreads();
+    const int nx = a.cx + 1, ny = a.cy + 1;
+    const int r0 = 1 + nx * (j + ny * k);
+    double *line = a.val + __ldg(a.rowptr + r0);
+    const int len = S::N * nix;
+    for (int q = threadIdx.x; q < len; q += blockDim.x) line[q] = st[q % S::N];
+    if (a.b) {
+        for (int i = threadIdx.x; i < nix; i += blockDim.x) {
+            const int r = r0 + i;
+            const double fr = source_at(a, r);
+            double vsum = 0.0;
+            for (int m = 0; m < nvol; ++m) vsum += fr * vols[m];
+            a.b[r] = vsum;
+        }
+    }
+}
+
 // rows on the box boundary: the identity row and b = 0 at Dirichlet
 // vertices; otherwise the elements that exist, entries found by search
 template <int T>
@@ -438,7 +483,12 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
                 return;   // no 2D velocity field
             }
         }
-        UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux);
+        if (a.k_uniform && !flux) {
+            const int nlines = (cy - 1) * ((L.dim == 3) ? cz - 1 : 1);
+            UG_LAUNCH(c, k_assemble_rows_uniform<T>, nlines, 128, 0, a, cd);
+        } else {
+            UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux);
+        }
         UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(L.nv, 128), 128, 0, a, cd, flux, L.bnd.p);
         done = true;
     };

@@ -135,6 +135,8 @@ class Problem:
         self.gmg.init(self.A)
         self.solver.init(self.A)
         self._fwd_valid = True
+        # the operator no longer holds the transposed problem
+        self._adj_ready = False
 
     def solve(self, raise_on_failure=True):
         """x = A^{-1} b from x0 = 0; b is kept."""
@@ -196,9 +198,12 @@ class Problem:
             if getattr(self, "lam", None) is None:
                 self.lam = GPUVector(self.ctx, self.n)
             self.forward_ready()
-            self.disc.adjoint_operator(self.A, self.A)
+            # the transposed multigrid is built from the forward operator
+            # (it transposes its own copy of the top level), then the
+            # operator itself is transposed for the solver
             self.gmg.set_transposed(True)
             self.gmg.init(self.A)
+            self.disc.adjoint_operator(self.A, self.A)
             self.solver.init(self.A)
             self.AT, self.gmgT, self.solverT = self.A, self.gmg, self.solver
             self._fwd_valid = False

@@ -7,7 +7,8 @@ statistics as JSON, e.g. to profile one precision or layout in isolation:
 
 --assemblies N re-assembles the top-level operator and rhs N times after
 the set-up and reports the time per assembly (--row-assembly 0 selects the
-element kernel instead of the row-wise one on structured levels):
+element kernel instead of the row-wise one on structured levels, 1 the
+row-wise kernel also with a constant coefficient, 2 the default):
 
     python -m ugcore_gb300.run_case --config c1 --solves 0 --assemblies 3
 
@@ -98,7 +99,7 @@ def main():
     ctx = ug.Context(0)
     ctx.set_operator_format(args.format)
     ctx.set_tuning(sweep_fusion=args.sweep_fusion, sweep_planes=args.sweep_planes,
-                   row_assembly=None if args.row_assembly is None else bool(args.row_assembly))
+                   row_assembly=args.row_assembly)
     t0 = time.perf_counter()
     p = ugx_problem(ctx, args) if args.ugx else problems.Problem(ctx, problems.config(args.config, **over))
     ctx.synchronize()
