@@ -157,10 +157,13 @@ def iteration_bytes(sizes, sv):
 
 
 def assembly_bytes(p, sz):
+    """bytes a top-level assembly must move: the operator's values and the
+    rhs written once (8 nnz + 8 N) and, unless one coefficient serves every
+    element, the element coefficients read once (8 E); on structured levels
+    the geometry is per element class (a few KB) and the pattern is known"""
     N, E = sz["N"], p.hier.num_elements()
-    k = 8 if p.cfg["elem"] == "hex" else 4
-    dim = p.hier.dim
-    return 8 * dim * N + 4 * k * E + 8 * E + sz["nnz"] * 12 + 4 * (N + 1) + 8 * N
+    coef = 0 if p.cfg["coef"] == "const" else 8 * E
+    return 8 * sz["nnz"] + 8 * N + coef
 
 
 def profile_summary(prof, top=14):
