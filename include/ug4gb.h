@@ -53,6 +53,8 @@ extern "C" {
                                        backward (SymmetricGaussSeidel, gauss_seidel.h:350, in colour order) */
 #define UG4GB_SMOOTHER_ILU 3        /* ILU(0) in multicolour order (ILU, ilu.h:109-290, of the colour-
                                        permuted operator); damp scales the correction */
+#define UG4GB_SMOOTHER_MCBGS 4      /* backward multicolour Gauss-Seidel: colours in decreasing order
+                                       (BackwardGaussSeidel, gauss_seidel.h:316, in colour order) */
 #define UG4GB_PREC_FP64 0           /* whole preconditioner in FP64 */
 #define UG4GB_PREC_MIXED 1          /* FP32 smoother/transfers/SpMV, FP64 outer Krylov and base LU */
 #define UG4GB_SOLVER_CG 0           /* lib_algebra/operator/linear_solver/cg.h:59 */
@@ -88,12 +90,15 @@ UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
 /* performance switches that leave every result bit-identical.
    UG4GB_TUNE_PDL (0 or 1): programmatic dependent launch of the solve-path
    kernels, each kernel scheduled while its predecessor still runs (default 1).
-   UG4GB_TUNE_SWEEP_FUSION (bit mask, 0..3): two consecutive damped-Jacobi
+   UG4GB_TUNE_SWEEP_FUSION (bit mask, 0..7): two consecutive damped-Jacobi
    steps of a structured 3D FP32 level in one pass over its operator.  Bit 1:
    on; bit 2: levels of every size (else only levels of at least 2^18
-   vertices).  Default 0.  Smoothed corrections and defects are
-   bit-identical; inside a Krylov solve only the summation order of the
-   fused (z, r) product changes.  Applies to multigrids set up after the call. */
+   vertices); bit 4: automatic, on for 27-point (hexahedral) levels of at
+   least 4,194,304 vertices, where it is faster.  Default 4.  Smoothed
+   corrections and defects are bit-identical; inside a Krylov solve only the
+   summation order of the fused (z, r) product changes.  Applies to
+   multigrids set up after the call (the fused levels keep a line-padded
+   copy of their operator). */
 #define UG4GB_TUNE_PDL 1
 #define UG4GB_TUNE_SWEEP_FUSION 2
 /* UG4GB_TUNE_SWEEP_PLANES (2..128): z planes a block of the fused sweeps
@@ -351,6 +356,15 @@ UG4GB_API void ug4gb_disc_destroy(ug4gb_disc *d);
    level 0; Jacobi damping 0.6 as in the configured scripts. */
 UG4GB_API int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out);
 UG4GB_API int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp);            /* set_smoother */
+/* set_presmoother / set_postsmoother (mg_solver.h:179-183): different pre-
+   and post-smoothers.  damp is the Jacobi damping, the Gauss-Seidel SOR
+   relaxation (set_sor_relax, gauss_seidel.h:96) or the ILU correction
+   factor.  Any two of the Gauss-Seidel kinds and ILU combine, each with its
+   own factor; the Jacobi smoother works on the column-scaled level operator
+   and combines only with itself at the same damping (ug4gb_gmg_init returns
+   UG4GB_ERR_INVALID otherwise). */
+UG4GB_API int ug4gb_gmg_set_presmoother(ug4gb_gmg *m, int kind, double damp);
+UG4GB_API int ug4gb_gmg_set_postsmoother(ug4gb_gmg *m, int kind, double damp);
 UG4GB_API int ug4gb_gmg_set_cycle_type(ug4gb_gmg *m, int cycle);  /* 1 = V, 2 = W, up to 4; -1 = F (mg_solver.h:339-341) */
 UG4GB_API int ug4gb_gmg_set_num_presmooth(ug4gb_gmg *m, int n);
 UG4GB_API int ug4gb_gmg_set_num_postsmooth(ug4gb_gmg *m, int n);

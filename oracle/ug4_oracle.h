@@ -138,10 +138,17 @@ void orc_lu_apply(const orc_lu *F, double *x, const double *b);
 void orc_lu_free(orc_lu *F);
 
 /* GMG */
-enum { ORC_SMOOTH_JACOBI = 0, ORC_SMOOTH_MCGS = 1, ORC_SMOOTH_MCSGS = 2, ORC_SMOOTH_ILU = 3 };
+/* MCBGS: backward Gauss-Seidel (BackwardGaussSeidel, gauss_seidel.h:316),
+   colours in decreasing order */
+enum { ORC_SMOOTH_JACOBI = 0, ORC_SMOOTH_MCGS = 1, ORC_SMOOTH_MCSGS = 2, ORC_SMOOTH_ILU = 3, ORC_SMOOTH_MCBGS = 4 };
 typedef struct {
     int nlev, base, cycle, nu1, nu2, smoother;
     double damp;
+    /* post-smoother (set_postsmoother, mg_solver.h:179-183); the same as
+       the pre-smoother after orc_gmg_init */
+    int smoother2;
+    double damp2;
+    double **diaginv2;   /* Jacobi post-smoother with its own damping, else NULL */
     orc_crs *A;          /* per level */
     orc_crs *P, *R;      /* per level (index = fine level) */
     double **diaginv;
@@ -167,6 +174,8 @@ int orc_rap(const orc_crs *R, const orc_crs *A, const orc_crs *P, orc_crs *M);
    operators are owned by the multigrid (G->Arap). */
 int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, double damp,
                  int nu1, int nu2, int cycle, int base, int rap);
+/* a post-smoother other than the pre-smoother (after orc_gmg_init) */
+int orc_gmg_set_postsmoother(orc_gmg *G, int smoother, double damp);
 void orc_gmg_apply(orc_gmg *G, double *c, const double *d);
 void orc_gmg_free(orc_gmg *G);
 

@@ -39,6 +39,8 @@ typedef struct {
     int bicg_restart;   /* BiCGStab::set_restart (0: off) */
     double bicg_min_ortho; /* BiCGStab::set_min_orthogonality */
     double damp_prol, damp_res; /* StdTransfer damping (both 1 = none) */
+    int post_smoother;  /* set_postsmoother: -1 = the pre-smoother */
+    double post_damp;
 } orc_params;
 
 typedef struct {
@@ -179,6 +181,10 @@ static int gmg_init_p(orc_gmg *G, const orc_prob *P, orc_crs *levA)
     const orc_params *p = &P->p;
     int rc = orc_gmg_init(G, &P->H, levA, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap);
     if (rc) return rc;
+    if (p->post_smoother >= 0) {
+        rc = orc_gmg_set_postsmoother(G, p->post_smoother, p->post_damp);
+        if (rc) return rc;
+    }
     G->damp_prol = p->damp_prol > 0.0 ? p->damp_prol : 1.0;
     G->damp_res = p->damp_res > 0.0 ? p->damp_res : 1.0;
     return 0;

@@ -270,6 +270,7 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
     memset(G, 0, sizeof(*G));
     G->nlev = H->nlev; G->base = base; G->cycle = cycle; G->nu1 = nu1; G->nu2 = nu2;
     G->smoother = smoother; G->damp = damp;
+    G->smoother2 = smoother; G->damp2 = damp;
     G->damp_prol = 1.0; G->damp_res = 1.0;
     G->A = levA;
     G->P = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
@@ -326,6 +327,32 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
     return 0;
 }
 
+int orc_gmg_set_postsmoother(orc_gmg *G, int smoother, double damp)
+{
+    G->smoother2 = smoother;
+    G->damp2 = damp;
+    if (smoother == ORC_SMOOTH_JACOBI) {
+        if (!G->diaginv2) G->diaginv2 = (double **)calloc((size_t)G->nlev, sizeof(double *));
+        for (int l = G->base + 1; l < G->nlev; ++l) {
+            int n = G->A[l].n_rows;
+            free(G->diaginv2[l]);
+            G->diaginv2[l] = dvec(n);
+            for (int i = 0; i < n; ++i) {
+                double m = G->A[l].val[orc_crs_find(&G->A[l], i, i)];
+                m *= 1. / damp;
+                G->diaginv2[l][i] = 1. / m;
+            }
+        }
+    }
+    if (smoother == ORC_SMOOTH_ILU && !G->ilu) {
+        G->ilu = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
+        G->ilu_diag = (int **)calloc((size_t)G->nlev, sizeof(int *));
+        for (int l = G->base + 1; l < G->nlev; ++l)
+            if (ilu_factor(&G->A[l], G->color[l], G->ncolor[l], &G->ilu[l], &G->ilu_diag[l])) return -3;
+    }
+    return 0;
+}
+
 /* multicolour Gauss-Seidel sweep from zero: c = B d */
 static void mcgs_apply(const orc_crs *A, const int *color, int ncolor, double relax, double *c, const double *d)
 {
@@ -360,21 +387,30 @@ static void mcgs_backward(const orc_crs *A, const int *color, int ncolor, double
         }
 }
 
-static void smooth(orc_gmg *G, int l, double *c, const double *d)
+/* one smoothing step c = B d from zero: the pre-smoother (post = 0) or the
+   post-smoother (post = 1) */
+static void smooth(orc_gmg *G, int l, double *c, const double *d, int post)
 {
     int n = G->A[l].n_rows;
-    if (G->smoother == ORC_SMOOTH_JACOBI) {
-        const double *di = G->diaginv[l];
+    const int kind = post ? G->smoother2 : G->smoother;
+    const double damp = post ? G->damp2 : G->damp;
+    if (kind == ORC_SMOOTH_JACOBI) {
+        const double *di = (post && G->diaginv2) ? G->diaginv2[l] : G->diaginv[l];
         for (int i = 0; i < n; ++i) c[i] = di[i] * d[i];
     } else {
-        if (G->smoother == ORC_SMOOTH_ILU) {
+        if (kind == ORC_SMOOTH_ILU) {
             double *y = (double *)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
-            ilu_apply(&G->ilu[l], G->ilu_diag[l], G->color[l], G->ncolor[l], G->damp, c, d, y);
+            ilu_apply(&G->ilu[l], G->ilu_diag[l], G->color[l], G->ncolor[l], damp, c, d, y);
             free(y);
             return;
         }
-        mcgs_apply(&G->A[l], G->color[l], G->ncolor[l], G->damp, c, d);
-        if (G->smoother == ORC_SMOOTH_MCSGS) mcgs_backward(&G->A[l], G->color[l], G->ncolor[l], G->damp, c, d);
+        if (kind == ORC_SMOOTH_MCBGS) {
+            memset(c, 0, sizeof(double) * (size_t)n);
+            mcgs_backward(&G->A[l], G->color[l], G->ncolor[l], damp, c, d);
+            return;
+        }
+        mcgs_apply(&G->A[l], G->color[l], G->ncolor[l], damp, c, d);
+        if (kind == ORC_SMOOTH_MCSGS) mcgs_backward(&G->A[l], G->color[l], G->ncolor[l], damp, c, d);
     }
 }
 
@@ -390,7 +426,7 @@ static void presmooth_and_restriction(orc_gmg *G, int l)
 {
     int n = G->A[l].n_rows, nc = G->A[l - 1].n_rows;
     for (int nu = 0; nu < G->nu1; ++nu) {
-        smooth(G, l, G->st[l], G->sd[l]);
+        smooth(G, l, G->st[l], G->sd[l], 0);
         orc_crs_matmul_minus(&G->A[l], G->sd[l], G->st[l]);
         if (nu < G->nu1 - 1) vadd(n, G->sc[l], G->st[l]);
     }
@@ -410,7 +446,7 @@ static void prolongation_and_postsmooth(orc_gmg *G, int l)
     vadd(n, G->sc[l], G->st[l]);
     for (int nu = 0; nu < G->nu2; ++nu) {
         orc_crs_matmul_minus(&G->A[l], G->sd[l], G->st[l]);
-        smooth(G, l, G->st[l], G->sd[l]);
+        smooth(G, l, G->st[l], G->sd[l], 1);
         vadd(n, G->sc[l], G->st[l]);
     }
     if (l >= G->nlev - 1) orc_crs_matmul_minus(&G->A[l], G->sd[l], G->st[l]);
@@ -446,6 +482,7 @@ void orc_gmg_free(orc_gmg *G)
         if (G->P) orc_crs_free(&G->P[l]);
         if (G->R) orc_crs_free(&G->R[l]);
         if (G->diaginv) free(G->diaginv[l]);
+        if (G->diaginv2) free(G->diaginv2[l]);
         if (G->color) free(G->color[l]);
         if (G->sc) { free(G->sc[l]); free(G->sd[l]); free(G->st[l]); }
     }
@@ -453,6 +490,7 @@ void orc_gmg_free(orc_gmg *G)
         for (int l = 0; l < G->nlev; ++l) { orc_crs_free(&G->ilu[l]); free(G->ilu_diag[l]); }
         free(G->ilu); free(G->ilu_diag);
     }
+    free(G->diaginv2);
     free(G->P); free(G->R); free(G->diaginv); free(G->color); free(G->ncolor);
     free(G->sc); free(G->sd); free(G->st);
     if (G->Arap) {

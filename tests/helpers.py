@@ -14,6 +14,9 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 VAL_RTOL = 1e-13
 
 
+SMOOTHERS = {"jacobi": 0, "mcgs": 1, "mcsgs": 2, "ilu": 3, "mcbgs": 4}
+
+
 def oracle_params(orc, cfg):
     et = {"quad": orc.ORC_QUAD, "hex": orc.ORC_HEX, "tet": orc.ORC_TET}[cfg["elem"]]
     if cfg["coef"] == "const":
@@ -24,11 +27,13 @@ def oracle_params(orc, cfg):
         elem_type=et, mx=cfg["mx"], my=cfg["my"], mz=cfg["mz"], nref=cfg["nref"], seed=cfg["seed"], coef_kind=ck,
         coef_modes=cfg["coef_modes"], coef_kmax=cfg["coef_kmax"], vel_kind=1 if cfg["vel"] else 0,
         vel_modes=cfg["vel_modes"], vel_kmax=cfg["vel_kmax"], diffusion=cfg["diffusion"], peclet=cfg["peclet"],
-        solver=0 if cfg["solver"] == "cg" else 1, smoother={"jacobi": 0, "mcgs": 1, "mcsgs": 2, "ilu": 3}[cfg["smoother"]],
+        solver=0 if cfg["solver"] == "cg" else 1, smoother=SMOOTHERS[cfg["smoother"]],
         damp=cfg["damp"], nu1=cfg["nu1"], nu2=cfg["nu2"], cycle=cfg["cycle"], base=cfg["base"], maxit=cfg["maxit"],
         rel_red=cfg["rel_red"], min_defect=cfg["min_defect"], rap=int(cfg.get("rap", 0)),
         bicg_restart=int(cfg.get("bicg_restart", 0)), bicg_min_ortho=float(cfg.get("bicg_min_ortho", 0.0)),
-        damp_prol=float(cfg.get("damp_prol", 1.0)), damp_res=float(cfg.get("damp_res", 1.0)))
+        damp_prol=float(cfg.get("damp_prol", 1.0)), damp_res=float(cfg.get("damp_res", 1.0)),
+        post_smoother=SMOOTHERS[cfg["post_smoother"]] if cfg.get("post_smoother") else -1,
+        post_damp=float(cfg.get("post_damp", 1.0)))
 
 
 def assert_crs_equal(a, b, rtol=VAL_RTOL, what="matrix"):

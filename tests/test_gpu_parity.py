@@ -136,6 +136,75 @@ def test_mcgs_smoother_matches_oracle(ctx, oracle_lib, name, smoother):
     assert np.abs(p.x.numpy() - ref["x"]).max() <= 1e-8 * np.abs(ref["x"]).max()
 
 
+@pytest.mark.parametrize("name,pre,post", [("c1", ("mcgs", 1.0), ("mcbgs", 1.0)), ("c0", ("mcgs", 1.2), ("mcbgs", 0.8)),
+                                           ("c4", ("mcbgs", 1.0), ("ilu", 0.9)), ("c1", ("ilu", 1.0), ("mcsgs", 1.1)),
+                                           ("c2", ("mcsgs", 0.9), ("mcgs", 1.0))])
+def test_separate_pre_and_post_smoothers_match_oracle(ctx, oracle_lib, name, pre, post):
+    """set_presmoother / set_postsmoother (mg_solver.h:179-183): forward
+    Gauss-Seidel before and backward Gauss-Seidel after the coarse
+    correction, ILU with a Gauss-Seidel kind, each with its own SOR
+    relaxation / ILU factor; GMG application 1e-12 against the oracle, solve
+    iterations +-1"""
+    import ugcore_gb300 as ug
+    over = dict(nref=3 if name != "c0" else 5, smoother=pre[0], damp=pre[1], post_smoother=post[0],
+                post_damp=post[1], precision="fp64")
+    if name in ("c4", "c2"):
+        over["nref"] = 2
+    cfg, p = _problem(ctx, name, over)
+    op = _oracle(oracle_lib, cfg, p)
+    d = np.random.default_rng(2).standard_normal(p.n)
+    _, _, bnd = p.hier.export()
+    d[bnd.astype(bool)] = 0.0
+    cv = ug.GPUVector(ctx, p.n)
+    p.gmg.apply(cv, ug.GPUVector(ctx, p.n).copy_from(d))
+    c_ref = op.apply_gmg(d)
+    assert np.abs(cv.numpy() - c_ref).max() <= 1e-12 * np.abs(c_ref).max()
+    st = p.solve()
+    ref = op.solve()
+    assert abs(st["steps"] - ref["steps"]) <= 1
+    assert np.abs(p.x.numpy() - ref["x"]).max() <= 1e-8 * np.abs(ref["x"]).max()
+
+
+@pytest.mark.parametrize("name,over", [("c1", dict(nref=3)), ("c1", dict(nref=3, row_assembly=0)),
+                                       ("c2", dict(nref=2)), ("c0", dict(nref=4))])
+def test_seeded_source_equals_explicit_source(ctx, name, over):
+    """the seeded source f_i = 2 u(seed, i) - 1 (splitmix64 hash, its 53-bit
+    integer scaled by 2^-53 in integer arithmetic on the device) gives the
+    bits of the same source passed as an array (computed here with Python's
+    own conversion), on the row-wise and on the element assembly"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import fields, problems
+    over = dict(over)
+    mode = over.pop("row_assembly", None)
+    cfg = problems.config(name, **over)
+    c = ctx
+    if mode is not None:
+        c = ug.Context(0)
+        c.set_tuning(row_assembly=mode)
+    p = problems.Problem(c, cfg)
+    b_seed = p.b.numpy()
+    p.disc.set_source(fields.source_uniform(cfg["seed"], p.n))
+    A2, b2 = ug.GPUSparseMatrix(c), ug.GPUVector(c, p.n)
+    p.disc.assemble_linear(A2, b2)
+    assert np.array_equal(b_seed.view(np.int64), b2.numpy().view(np.int64))
+
+
+def test_jacobi_combines_only_with_itself(ctx):
+    """a Jacobi pre-smoother with a Gauss-Seidel post-smoother, or two Jacobi
+    dampings, are refused at init with a message (the Jacobi smoother works
+    on the column-scaled level operator)"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    p = problems.Problem(ctx, problems.config("c0", nref=3))
+    for post in (ug.GaussSeidel(1.0), ug.Jacobi(0.5)):
+        g = ug.GeometricMultiGrid(p.disc)
+        g.set_smoother(ug.Jacobi(0.6))
+        g.set_postsmoother(post)
+        with pytest.raises(ug.UG4GBError) as e:
+            g.init(p.A)
+        assert "Jacobi" in str(e.value)
+
+
 @pytest.mark.parametrize("name", ["quad_2x2_r4", "hex_2x2x2_r2", "tet_4x4x4_r1_lognormal", "hex_3x3x3_r1_convection"])
 def test_gpu_against_ugcore_algebra_golden(ctx, name):
     """fixtures written by ugcore's own SparseMatrix/Jacobi/LU/CG/BiCGStab"""

@@ -351,3 +351,23 @@ def test_newton_line_search_paths(oracle_lib):
     r = P.newton(u0, maxit=4, reduction=1e-9,
                  line_search=dict(lambda_start=2.0, max_steps=1, accept_best=1, max_defect=0.5 * ref[4][0]))
     assert r[1] == 3 and r[5] == ([1], [2.0])
+
+
+def test_backward_and_separate_smoothers_in_the_oracle(oracle_lib):
+    """the oracle's post-smoother of its own: a post-smoother equal to the
+    pre-smoother changes nothing; forward Gauss-Seidel before and backward
+    after the coarse correction converges with CG like the symmetric
+    smoother (+-2 steps); the backward sweep alone differs from the forward
+    one"""
+    o = oracle_lib
+    base = dict(elem_type=o.ORC_HEX, mx=2, my=2, mz=2, nref=3, seed=3, smoother=1, damp=1.0)
+    same = o.Problem(o.make_params(**base, post_smoother=1, post_damp=1.0)).solve()
+    ref = o.Problem(o.make_params(**base)).solve()
+    assert same["steps"] == ref["steps"] and np.array_equal(same["x"], ref["x"])
+    st = o.Problem(o.make_params(**base, post_smoother=4, post_damp=1.0)).solve()
+    sgs = o.Problem(o.make_params(**dict(base, smoother=2))).solve()
+    assert st["converged"] and abs(st["steps"] - sgs["steps"]) <= 2
+    P1 = o.Problem(o.make_params(**base))
+    P4 = o.Problem(o.make_params(**dict(base, smoother=4)))
+    d = np.random.default_rng(0).standard_normal(P1.nv())
+    assert not np.array_equal(P1.apply_gmg(d), P4.apply_gmg(d))

@@ -55,6 +55,8 @@ struct Functionality {
                 .template add_constructor<void (*)(SmartPtr<UG4GBDomainDiscretization<TDomain> >)>(
                     "DomainDiscretization")
                 .add_method("set_smoother", &T::set_smoother, "", "Kind#Damping")
+                .add_method("set_presmoother", &T::set_presmoother, "", "Kind#Damping")
+                .add_method("set_postsmoother", &T::set_postsmoother, "", "Kind#Damping")
                 .add_method("set_cycle_type", &T::set_cycle_type, "", "Cycle Type")
                 .add_method("set_num_presmooth", &T::set_num_presmooth, "", "Number PreSmooth Steps")
                 .add_method("set_num_postsmooth", &T::set_num_postsmooth, "", "Number PostSmooth Steps")

@@ -52,8 +52,23 @@ public:
     /// multicolour Gauss-Seidel / symmetric Gauss-Seidel / ILU variants
     void set_smoother(int kind, double damp)
     {
+        m_cfg.smoother = m_cfg.smoother2 = kind;
+        m_cfg.damp = m_cfg.damp2 = damp;
+        configure();
+    }
+    /// set_presmoother / set_postsmoother (mg_solver.h:179-183): damp is the
+    /// Jacobi damping, the SOR relaxation of the Gauss-Seidel kinds
+    /// (including UG4GB_SMOOTHER_MCBGS, backward) or the ILU factor
+    void set_presmoother(int kind, double damp)
+    {
         m_cfg.smoother = kind;
         m_cfg.damp = damp;
+        configure();
+    }
+    void set_postsmoother(int kind, double damp)
+    {
+        m_cfg.smoother2 = kind;
+        m_cfg.damp2 = damp;
         configure();
     }
     void set_cycle_type(int c) { m_cfg.cycle = c; configure(); }
@@ -153,8 +168,8 @@ public:
 
 private:
     struct Config {
-        int smoother = UG4GB_SMOOTHER_JACOBI;
-        double damp = 0.6;
+        int smoother = UG4GB_SMOOTHER_JACOBI, smoother2 = UG4GB_SMOOTHER_JACOBI;
+        double damp = 0.6, damp2 = 0.6;
         int cycle = 1, nu1 = 2, nu2 = 2, base = 0;
         int precision = UG4GB_PREC_FP64;
         bool rap = false;
@@ -173,7 +188,8 @@ private:
         ug4gb_glue::guarded(
             [&] {
                 ug4gb_ctx *ctx = ug4gb_glue::context().get();
-                ug4gb::check(ug4gb_gmg_set_smoother(m_gmg, m_cfg.smoother, m_cfg.damp), ctx, "smoother");
+                ug4gb::check(ug4gb_gmg_set_presmoother(m_gmg, m_cfg.smoother, m_cfg.damp), ctx, "presmoother");
+                ug4gb::check(ug4gb_gmg_set_postsmoother(m_gmg, m_cfg.smoother2, m_cfg.damp2), ctx, "postsmoother");
                 ug4gb::check(ug4gb_gmg_set_cycle_type(m_gmg, m_cfg.cycle), ctx, "cycle");
                 ug4gb::check(ug4gb_gmg_set_num_presmooth(m_gmg, m_cfg.nu1), ctx, "presmooth");
                 ug4gb::check(ug4gb_gmg_set_num_postsmooth(m_gmg, m_cfg.nu2), ctx, "postsmooth");

@@ -78,7 +78,8 @@ class Context:
     def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None, row_assembly=None, sweep_wait_test=None):
         """performance switches:
         pdl: programmatic dependent launch of the solve kernels;
-        sweep_fusion: bit mask (1 on, 2 every level size) of the
+        sweep_fusion: bit mask (1 on, 2 every level size, 4 automatic: the
+        default, on for hexahedral levels of at least 4M vertices) of the
         two-Jacobi-steps-per-pass smoother of structured 3D FP32 levels;
         sweep_planes: z planes per block of that smoother (these three leave
         results bit-identical);
@@ -548,11 +549,26 @@ class Jacobi:
         self.kind, self.damp = _lib.SMOOTHER_JACOBI, float(damp)
 
 
-class GaussSeidel:
+class _SorRelax:
+    def set_sor_relax(self, relax):
+        """GaussSeidelBase::set_sor_relax (gauss_seidel.h:96)"""
+        self.damp = float(relax)
+        return self
+
+
+class GaussSeidel(_SorRelax):
     """multicolour Gauss-Seidel smoother (opt-in GPU variant of gauss_seidel.h)"""
 
     def __init__(self, relax=1.0):
         self.kind, self.damp = _lib.SMOOTHER_MCGS, float(relax)
+
+
+class BackwardGaussSeidel(_SorRelax):
+    """backward multicolour Gauss-Seidel: colours in decreasing order (GPU
+    variant of BackwardGaussSeidel, gauss_seidel.h:316)"""
+
+    def __init__(self, relax=1.0):
+        self.kind, self.damp = _lib.SMOOTHER_MCBGS, float(relax)
 
 
 class ILU:
@@ -563,7 +579,7 @@ class ILU:
         self.kind, self.damp = _lib.SMOOTHER_ILU, float(damp)
 
 
-class SymmetricGaussSeidel:
+class SymmetricGaussSeidel(_SorRelax):
     """symmetric multicolour Gauss-Seidel: forward, then backward colour sweep
     (GPU variant of SymmetricGaussSeidel, gauss_seidel.h:350)"""
 
@@ -646,6 +662,15 @@ class GeometricMultiGrid:
 
     def set_smoother(self, sm):
         check(lib().ug4gb_gmg_set_smoother(self.h, sm.kind, sm.damp), self.ctx.h)
+
+    def set_presmoother(self, sm):
+        """set_presmoother (mg_solver.h:179-183); Gauss-Seidel kinds and ILU
+        combine freely with a different post-smoother, Jacobi only with the
+        same Jacobi"""
+        check(lib().ug4gb_gmg_set_presmoother(self.h, sm.kind, sm.damp), self.ctx.h)
+
+    def set_postsmoother(self, sm):
+        check(lib().ug4gb_gmg_set_postsmoother(self.h, sm.kind, sm.damp), self.ctx.h)
 
     def set_cycle_type(self, cycle):
         """"V" (1), "W" (2), gamma up to 4, or "F" (-1), as set_cycle_type"""

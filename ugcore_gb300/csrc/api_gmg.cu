@@ -176,8 +176,8 @@ static void dense_lu_inverse(int n, std::vector<double> &M, std::vector<double> 
 template <class V>
 struct GmgT : GmgBase {
     std::vector<GLevel<V>> lev;
-    int base = 0, nu1 = 2, nu2 = 2, cycle = 1, smoother = 0;
-    double damp = 1.0;
+    int base = 0, nu1 = 2, nu2 = 2, cycle = 1, smoother = 0, smoother2 = 0;
+    double damp = 1.0, damp2 = 1.0;
     DevBuf<double> Ainv;
     DevBuf<double> z64;          // mixed precision: FP64 copy of the top correction
     uint64_t top_key = 0;        // pattern key of the top operator of the last set-up
@@ -202,7 +202,7 @@ struct GmgT : GmgBase {
         for (const GLevel<V> &L : lev) {
             mix(L.At.dia.val.p); mix(L.At.sell.val.p); mix(L.At.sell.col.p); mix(L.At.sell.sptr.p);
             mix(L.At.sell.swidth.p); mix(L.dinv.p); mix(L.dfac.p); mix(L.sc.p); mix(L.dA.p); mix(L.dB.p);
-            mix(L.w.p); mix(L.t.p); mix(L.y.p); mix(L.Ps.dia.val.p); mix(L.Ps.sell.val.p); mix(L.Rs.dia.val.p);
+            mix(L.w.p); mix(L.t.p); mix(L.y.p); mix(L.dinv2.p); mix(L.Ps.dia.val.p); mix(L.Ps.sell.val.p); mix(L.Rs.dia.val.p);
             mix(L.Rs.sell.val.p); mix(L.sweep2.get()); mix(L.vcolor.p);
             for (const DevBuf<int> &q : L.crow) mix(q.p);
             mix(L.ilu.val.p); mix(L.ilu.col.p); mix(L.ilu.rowptr.p); mix(L.ilu.nlow.p); mix(L.ilu.uinv.p);
@@ -233,6 +233,14 @@ struct GmgT : GmgBase {
         L.dfac.alloc(n);
         UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, L.dinv64.p, L.dinv.p, n);
         UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, L.dfac64.p, L.dfac.p, n);
+        // a Gauss-Seidel post-smoother with its own relaxation
+        if (smoother2 != UG4GB_SMOOTHER_JACOBI && smoother2 != UG4GB_SMOOTHER_ILU && damp2 != damp) {
+            L.dinv2_64.alloc(n);
+            L.dinv2.alloc(n);
+            UG_LAUNCH(c, k_diag_inv, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp2, smoother2,
+                      L.dinv2_64.p, L.dfac64.p);
+            UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, L.dinv2_64.p, L.dinv2.p, n);
+        }
         if (smoother == UG4GB_SMOOTHER_JACOBI) {
             op_from_csr_cached<V>(c, L.A, L.At, L.dinv64.p, c.allow_dia, L.At_lay);
         } else {
@@ -285,7 +293,7 @@ struct GmgT : GmgBase {
             }
             UG_CUDA(cudaStreamSynchronize(c.stream));
             }
-            if (smoother == UG4GB_SMOOTHER_ILU) {
+            if (smoother == UG4GB_SMOOTHER_ILU || smoother2 == UG4GB_SMOOTHER_ILU) {
                 ilu_setup<V>(c, L.A, colour, L.crow, L.ncrow, L.ilu);
                 L.y.alloc(n);
             }
@@ -409,7 +417,7 @@ struct GmgT : GmgBase {
             if (smoother == UG4GB_SMOOTHER_JACOBI) {
                 smooth_step<V, V, V>(c, L.At, cur, cur, L.dinv.p, L.sc.p, out, mode, skip, nullptr, nullptr, 0);
             } else {
-                gs_sweep(c, L, cur, skip);
+                gs_sweep(c, L, cur, skip, smoother, L.dinv.p, damp);
                 residual_update<V, V>(c, L.At, L.t.p, cur, out, L.sc.p, mode == SC_SET_FROM_BASE ? 1 : 0, skip);
             }
             cur = out;
@@ -437,7 +445,7 @@ struct GmgT : GmgBase {
         else prolong_apply<V>(c, L.Ps, C.sc.p, L.sc.p, L.dfac.p, nu2 > 0 ? L.w.p : (V *)nullptr, skip);
         const V *dbase = dpre;
         bool z_written = false;
-        if (smoother == UG4GB_SMOOTHER_JACOBI) {
+        if (smoother2 == UG4GB_SMOOTHER_JACOBI) {
             for (int k = 0; k < nu2; ++k) {
                 const V *x = (k == 0) ? L.w.p : dbase;
                 // two steps in one pass where the level allows it
@@ -476,7 +484,7 @@ struct GmgT : GmgBase {
                 const V *tprev = (k == 0) ? L.w.p : L.t.p;
                 V *out = (dbase == L.dA.p) ? L.dB.p : L.dA.p;
                 residual_update<V, V>(c, L.At, tprev, dbase, out, L.sc.p, k == 0 ? 2 : 0, skip);
-                gs_sweep(c, L, out, skip);
+                gs_sweep(c, L, out, skip, smoother2, L.dinv2.p ? L.dinv2.p : L.dinv.p, damp2);
                 dbase = out;
             }
             if (nu2 > 0) UG_LAUNCH_PDL(c, k_vadd<V>, div_up(L.n, 256), 256, 0, L.n, L.sc.p, L.t.p, skip);
@@ -485,20 +493,23 @@ struct GmgT : GmgBase {
         L.dcur = const_cast<V *>(dbase);
     }
 
-    // t = B d: colours in increasing order from t = 0; the symmetric smoother
-    // then sweeps the colours in decreasing order
-    void gs_sweep(Ctx &c, GLevel<V> &L, const V *dv, const int *skip)
+    // t = B d of smoother `kind` (dinv = relax/a_ii; ILU: damp scales the
+    // correction): colours in increasing order from t = 0; the symmetric
+    // smoother then sweeps the colours in decreasing order, the backward one
+    // only in decreasing order
+    void gs_sweep(Ctx &c, GLevel<V> &L, const V *dv, const int *skip, int kind, const V *dinv, double dmp)
     {
-        if (smoother == UG4GB_SMOOTHER_ILU) {
-            ilu_apply<V>(c, L.ilu, L.crow, L.ncrow, dv, L.y.p, L.t.p, damp, skip);
+        if (kind == UG4GB_SMOOTHER_ILU) {
+            ilu_apply<V>(c, L.ilu, L.crow, L.ncrow, dv, L.y.p, L.t.p, dmp, skip);
             return;
         }
         UG_LAUNCH_PDL(c, k_zero<V>, div_up(L.n, 256), 256, 0, L.n, L.t.p, skip);
-        for (size_t q = 0; q < L.crow.size(); ++q)
-            if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], L.dinv.p, dv, L.t.p, skip);
-        if (smoother == UG4GB_SMOOTHER_MCSGS)
+        if (kind != UG4GB_SMOOTHER_MCBGS)
+            for (size_t q = 0; q < L.crow.size(); ++q)
+                if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], dinv, dv, L.t.p, skip);
+        if (kind == UG4GB_SMOOTHER_MCSGS || kind == UG4GB_SMOOTHER_MCBGS)
             for (size_t q = L.crow.size(); q-- > 0;)
-                if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], L.dinv.p, dv, L.t.p, skip);
+                if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], dinv, dv, L.t.p, skip);
     }
 
     const double *apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
@@ -535,6 +546,13 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
     G->cycle = m->cycle;
     G->smoother = m->smoother;
     G->damp = m->damp;
+    G->smoother2 = m->smoother2;
+    G->damp2 = m->damp2;
+    UG_REQUIRE((m->smoother == UG4GB_SMOOTHER_JACOBI) == (m->smoother2 == UG4GB_SMOOTHER_JACOBI) &&
+                   (m->smoother != UG4GB_SMOOTHER_JACOBI || m->damp == m->damp2),
+               UG4GB_ERR_INVALID,
+               "GMG: a Jacobi smoother combines only with the same Jacobi smoother (it works on the column-scaled "
+               "level operator); pre- and post-smoothers of the Gauss-Seidel kinds and ILU combine freely");
     G->lev.resize(nl);
     UG_REQUIRE(m->base >= 0 && m->base < nl, UG4GB_ERR_INVALID, "GMG: base level out of range");
     UG_REQUIRE(A_top->A.nrows == g->lev[nl - 1].nv, UG4GB_ERR_INVALID, "GMG: top operator size != top level");
@@ -656,12 +674,32 @@ int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out)
     return UG4GB_OK;
 }
 
+static bool smoother_ok(int kind, double damp)
+{
+    return kind >= UG4GB_SMOOTHER_JACOBI && kind <= UG4GB_SMOOTHER_MCBGS && damp > 0.0 && std::isfinite(damp);
+}
+
 int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp)
 {
-    if (!m || kind < UG4GB_SMOOTHER_JACOBI || kind > UG4GB_SMOOTHER_ILU || !(damp > 0.0))
-        return UG4GB_ERR_INVALID;
+    if (!m || !smoother_ok(kind, damp)) return UG4GB_ERR_INVALID;
+    m->smoother = m->smoother2 = kind;
+    m->damp = m->damp2 = damp;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_presmoother(ug4gb_gmg *m, int kind, double damp)
+{
+    if (!m || !smoother_ok(kind, damp)) return UG4GB_ERR_INVALID;
     m->smoother = kind;
     m->damp = damp;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_postsmoother(ug4gb_gmg *m, int kind, double damp)
+{
+    if (!m || !smoother_ok(kind, damp)) return UG4GB_ERR_INVALID;
+    m->smoother2 = kind;
+    m->damp2 = damp;
     return UG4GB_OK;
 }
 
@@ -752,7 +790,8 @@ int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         // (the transposition is applied to the values in place: a flip between
         // the forward and the transposed cycle keeps the structure)
         const GmgKey key{m->disc->g->uid, (int)m->disc->g->lev.size(), m->base, m->smoother, m->damp, m->rap,
-                         0, m->precision, m->ctx->c.allow_dia ? 1 : 0, m->damp_prol, m->damp_res};
+                         0, m->precision, m->ctx->c.allow_dia ? 1 : 0, m->damp_prol, m->damp_res, m->smoother2,
+                         m->damp2};
         const bool reuse = m->impl && m->built == key;
         const uint64_t before = reuse ? (m->impl->signature() ^ m->built_settings) : 0;
         GmgBase *old = reuse ? m->impl.release() : nullptr;

@@ -102,6 +102,7 @@ struct GLevel {
     Csr A;                       // FP64 level operator
     OpMat<V> At;                 // Jacobi: A * diag(dinv); MCGS: A
     DevBuf<V> dinv, dfac;        // Jacobi: dinv = 1/(a_ii/damp), dfac = a_ii/damp; MCGS: relax/a_ii, 1
+    DevBuf<V> dinv2;             // Gauss-Seidel post-smoother with its own relaxation: relax2/a_ii
     Csr P, R;                    // P: this x coarse, R: coarse x this (FP64, exportable)
     OpMat<V> Ps, Rs;
     bool grid_transfer = false;  // apply P and R from grid indices (structured hierarchy)
@@ -119,6 +120,7 @@ struct GLevel {
     bool asm_ok = false;             // A holds this level's pattern (re-assembled in place)
     int sym = -1;                    // A's pattern is symmetric (1), not (0), unknown (-1)
     DevBuf<double> dinv64, dfac64;   // FP64 Jacobi factors
+    DevBuf<double> dinv2_64;
 };
 
 struct GmgBase {
@@ -186,19 +188,23 @@ struct GmgKey {
     double damp = 0.0;
     int rap = 0, transposed = 0, precision = 0, allow_dia = 0;
     double damp_prol = 1.0, damp_res = 1.0;
+    int smoother2 = 0;
+    double damp2 = 0.0;
     bool operator==(const GmgKey &o) const
     {
         return g && g == o.g && nl == o.nl && base == o.base && smoother == o.smoother && damp == o.damp &&
                rap == o.rap && transposed == o.transposed && precision == o.precision && allow_dia == o.allow_dia &&
-               damp_prol == o.damp_prol && damp_res == o.damp_res;
+               damp_prol == o.damp_prol && damp_res == o.damp_res && smoother2 == o.smoother2 && damp2 == o.damp2;
     }
 };
 
 struct ug4gb_gmg {
     ug4gb_ctx *ctx = nullptr;
     ug4gb_disc *disc = nullptr;
-    int smoother = UG4GB_SMOOTHER_JACOBI;
+    int smoother = UG4GB_SMOOTHER_JACOBI;   // pre-smoother
     double damp = 0.6;
+    int smoother2 = UG4GB_SMOOTHER_JACOBI;  // post-smoother
+    double damp2 = 0.6;
     int cycle = 1, nu1 = 2, nu2 = 2, base = 0;
     int precision = UG4GB_PREC_FP64;
     int transposed = 0;

@@ -318,38 +318,35 @@ template <int T>
 __global__ void __launch_bounds__(128) k_assemble_rows_uniform(AsmArgs a, ClassData<T> cd)
 {
     using S = Stencil<T>;
-    constexpr int MAXV = 8 * ClassTraits<T>::NC;
     __shared__ double st[S::N];
-    __shared__ double vols[MAXV];
-    __shared__ int nvol;
     const int nix = a.cx - 1, niy = a.cy - 1;
     const int j = 1 + (int)(blockIdx.x % (unsigned)niy), k = (S::DIM == 3) ? 1 + (int)(blockIdx.x / (unsigned)niy) : 0;
+    const int kk = (S::DIM == 3) ? 1 : 0;
     if (threadIdx.x == 0) {
         double acc[S::N];
 #pragma unroll
         for (int s = 0; s < S::N; ++s) acc[s] = 0.0;
-        int m = 0;
-        gather_row<T>(cd, a, 1, 1, (S::DIM == 3) ? 1 : 0, nullptr, [&](int s, double v) { acc[s] += v; },
-                      [&](double vol) { if (m < MAXV) vols[m++] = vol; });
+        gather_row<T>(cd, a, 1, 1, kk, nullptr, [&](int s, double v) { acc[s] += v; }, [](double) {});
 #pragma unroll
         for (int s = 0; s < S::N; ++s) st[s] = acc[s];
-        nvol = m;
     }
-    __syncthreads();
+    // b while thread 0 gathers the stencil: the SCV volumes in the order of
+    // gather_row come from the kernel parameters (its value callback is empty)
     const int nx = a.cx + 1, ny = a.cy + 1;
     const int r0 = 1 + nx * (j + ny * k);
-    double *line = a.val + __ldg(a.rowptr + r0);
-    const int len = S::N * nix;
-    for (int q = threadIdx.x; q < len; q += blockDim.x) line[q] = st[q % S::N];
     if (a.b) {
         for (int i = threadIdx.x; i < nix; i += blockDim.x) {
             const int r = r0 + i;
             const double fr = source_at(a, r);
             double vsum = 0.0;
-            for (int m = 0; m < nvol; ++m) vsum += fr * vols[m];
+            gather_row<T>(cd, a, 1, 1, kk, nullptr, [](int, double) {}, [&](double vol) { vsum += fr * vol; });
             a.b[r] = vsum;
         }
     }
+    __syncthreads();
+    double *line = a.val + __ldg(a.rowptr + r0);
+    const int len = S::N * nix;
+    for (int q = threadIdx.x; q < len; q += blockDim.x) line[q] = st[q % S::N];
 }
 
 // rows on the box boundary: the identity row and b = 0 at Dirichlet

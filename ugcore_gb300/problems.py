@@ -22,7 +22,8 @@ import copy
 import numpy as np
 
 from . import fields
-from .algebra import (BiCGStab, CG, DomainDiscretization, GaussSeidel, GeometricMultiGrid, GPUSparseMatrix,
+from .algebra import (BackwardGaussSeidel, BiCGStab, CG, DomainDiscretization, GaussSeidel, GeometricMultiGrid,
+                      GPUSparseMatrix,
                       GPUVector, ILU, Jacobi, StdConvCheck, StdTransfer, StructuredHierarchy, SymmetricGaussSeidel,
                       ThetaTimeStep)
 
@@ -108,8 +109,12 @@ class Problem:
     def _make_gmg(self, transposed):
         c = self.cfg
         g = GeometricMultiGrid(self.disc)
-        g.set_smoother({"jacobi": Jacobi, "mcgs": GaussSeidel, "mcsgs": SymmetricGaussSeidel,
-                        "ilu": ILU}[c["smoother"]](c["damp"]))
+        kinds = {"jacobi": Jacobi, "mcgs": GaussSeidel, "mcsgs": SymmetricGaussSeidel, "ilu": ILU,
+                 "mcbgs": BackwardGaussSeidel}
+        g.set_smoother(kinds[c["smoother"]](c["damp"]))
+        if c.get("post_smoother"):
+            # a post-smoother of its own (set_postsmoother)
+            g.set_postsmoother(kinds[c["post_smoother"]](c.get("post_damp", 1.0)))
         g.set_cycle_type(c["cycle"])
         g.set_num_presmooth(c["nu1"])
         g.set_num_postsmooth(c["nu2"])
