@@ -128,6 +128,17 @@ UG4GB_API int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value);
    (Stands in for ugcore's PROFILE_BEGIN/END probes, common/profiler/profiler.h.) */
 UG4GB_API int ug4gb_profile_begin(ug4gb_ctx *ctx);
 UG4GB_API int ug4gb_profile_end(ug4gb_ctx *ctx, char *buf, int capacity);
+/* Guarded (debug) builds only (compiled with UG4GB_GUARDED): every device
+   buffer lies between two 4 KB guard zones, and zones and buffer start out
+   as 0xFF bytes (NaN in every floating-point type, -1 in the integers), so
+   a kernel that writes outside a buffer changes a zone and one that uses
+   memory nobody wrote produces NaN.  Synchronises the device, checks the
+   zones of every live buffer (freed buffers are checked when freed) and
+   writes one line per damaged zone into buf; returns the number of damaged
+   zones seen so far (0: none), or UG4GB_ERR_STATE in a normal build.  Stands
+   in for the bounds checks of ugcore's debug builds (UG_ASSERT in
+   lib_algebra) on the device.  No context needed. */
+UG4GB_API int ug4gb_debug_guard_check(char *buf, int capacity);
 
 /* ------------------------------------------------------ grid hierarchy -- */
 /* Replaces MultiGrid + GlobalMultiGridRefiner::perform_refinement

@@ -13,6 +13,19 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "slow: full-size configurations")
 
 
+def pytest_sessionfinish(session, exitstatus):
+    """UG4GB_GUARD_REPORT (set by tests/test_gpu_guarded.py for its child
+    run against the guarded library): write the guard-zone check there"""
+    path = os.environ.get("UG4GB_GUARD_REPORT")
+    if not path:
+        return
+    import json
+    from ugcore_gb300 import _lib
+    n, text = _lib.debug_guard_check()
+    with open(path, "w") as fh:
+        json.dump({"library": _lib.LIB_PATH, "damaged": n, "report": text, "exitstatus": int(exitstatus)}, fh)
+
+
 @pytest.fixture(scope="session")
 def oracle_lib():
     from oracle import oracle as orc

@@ -56,6 +56,7 @@ _SIGS = {
     "ug4gb_set_tuning": (I, [P, I, I]),
     "ug4gb_profile_begin": (I, [P]),
     "ug4gb_profile_end": (I, [P, C.c_char_p, I]),
+    "ug4gb_debug_guard_check": (I, [C.c_char_p, I]),
     "ug4gb_grid_create_structured": (I, [P, I, I, I, I, I, PP]),
     "ug4gb_grid_num_levels": (I, [P]),
     "ug4gb_grid_level_info": (I, [P, I, PI, PI, PI, PI]),
@@ -215,3 +216,13 @@ def check(rc, ctx=None):
         msg = lib().ug4gb_last_error(ctx).decode() if ctx else ""
         raise UG4GBError(rc, msg)
     return rc
+
+
+def debug_guard_check():
+    """(damaged zones, report) of a guarded build (ug4gb_debug_guard_check);
+    (None, "") for a normal build"""
+    buf = C.create_string_buffer(1 << 16)
+    n = lib().ug4gb_debug_guard_check(buf, len(buf))
+    if n == ERR_STATE:
+        return None, ""
+    return n, buf.value.decode()

@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libug4gb.so")
 
 SOURCES = ["k_grid.cu", "k_fv1.cu", "k_fv1_rows.cu", "k_solve.cu", "k_sweep2.cu", "k_rap.cu", "api.cu", "api_disc.cu", "api_gmg.cu", "api_solver.cu",
            "api_noalloc.cu", "api_perm.cu", "api_io.cu", "api_newton.cu",
-           "grid_unstructured.cu", "grid_refine_device.cu", "k_ilu.cu", "api_algebra.cu"]
+           "grid_unstructured.cu", "grid_refine_device.cu", "k_ilu.cu", "api_algebra.cu", "guard.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden",
@@ -92,18 +92,19 @@ def build(verbose=False, extra_flags=()):
     return LIB
 
 
-def build_sanitized(out_dir):
-    """The library with AddressSanitizer and UndefinedBehaviorSanitizer in its
-    host code (the file parsers, the C-ABI argument checks, the hierarchy
-    set-up), for tests that load it with the sanitizer runtime preloaded;
-    device code is compiled as usual.  Returns the path of the .so."""
+def build_guarded(out_dir):
+    """The library with guard zones around every device buffer and poisoned
+    contents (UG4GB_GUARDED, csrc/guard.cu), for the tests that run the GPU
+    paths against it and then call ug4gb_debug_guard_check.  Returns the path
+    of the .so."""
+    return _build_variant(out_dir, "libug4gb_guarded.so", ["-DUG4GB_GUARDED"], [])
+
+
+def _build_variant(out_dir, name, flags_extra, link_extra, drop_o3=False):
     nvcc = _nvcc()
     os.makedirs(out_dir, exist_ok=True)
-    # one option per -Xcompiler: nvcc splits its argument at commas
-    san = ["-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined", "-Xcompiler",
-           "-fno-omit-frame-pointer", "-Xcompiler", "-fno-sanitize-recover=undefined", "-g"]
-    flags = [f for f in NVCC_FLAGS if f != "-O3"] + ["-O1"]
-    lib = os.path.join(out_dir, "libug4gb_asan.so")
+    flags = [f for f in NVCC_FLAGS if not (drop_o3 and f == "-O3")] + (["-O1"] if drop_o3 else [])
+    lib = os.path.join(out_dir, name)
     hdrs = _headers()
     objs, jobs = [], []
     for src in SOURCES:
@@ -111,19 +112,30 @@ def build_sanitized(out_dir):
         o = os.path.join(out_dir, src.replace(".cu", ".o"))
         objs.append(o)
         if _newer(o, [s] + hdrs):
-            jobs.append([nvcc] + ARCH + flags + san + ["-c", s, "-o", o])
+            jobs.append([nvcc] + ARCH + flags + flags_extra + ["-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             for r in ex.map(lambda cmd: subprocess.run(cmd, capture_output=True, text=True), jobs):
                 if r.returncode:
-                    raise RuntimeError("nvcc failed (sanitized build): " + r.stderr[-2000:])
+                    raise RuntimeError("nvcc failed (%s): %s" % (name, r.stderr[-2000:]))
     if jobs or _newer(lib, objs):
-        r = subprocess.run([nvcc] + ARCH + ["-shared", "-o", lib] + objs +
-                           ["-lcudart", "-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined"],
+        r = subprocess.run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart"] + link_extra,
                            capture_output=True, text=True)
         if r.returncode:
-            raise RuntimeError("link failed (sanitized build): " + r.stderr[-2000:])
+            raise RuntimeError("link failed (%s): %s" % (name, r.stderr[-2000:]))
     return lib
+
+
+def build_sanitized(out_dir):
+    """The library with AddressSanitizer and UndefinedBehaviorSanitizer in its
+    host code (the file parsers, the C-ABI argument checks, the hierarchy
+    set-up), for tests that load it with the sanitizer runtime preloaded;
+    device code is compiled as usual.  Returns the path of the .so."""
+    # one option per -Xcompiler: nvcc splits its argument at commas
+    san = ["-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined", "-Xcompiler",
+           "-fno-omit-frame-pointer", "-Xcompiler", "-fno-sanitize-recover=undefined", "-g"]
+    return _build_variant(out_dir, "libug4gb_asan.so", san,
+                          ["-Xcompiler", "-fsanitize=address", "-Xcompiler", "-fsanitize=undefined"], drop_o3=True)
 
 
 if __name__ == "__main__":

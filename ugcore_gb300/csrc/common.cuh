@@ -43,6 +43,13 @@ struct Error {
         if (!(cond)) throw ::ug4gb::Error{(code), std::string(text)};                             \
     } while (0)
 
+#ifdef UG4GB_GUARDED
+// guarded build: buffers between guard zones (ug4gb_debug_guard_check)
+constexpr size_t kGuardBytes = 4096;
+void guard_register(char *base, void *user, size_t user_bytes);
+char *guard_release(void *user) noexcept;
+#endif
+
 // Owning device buffer (move-only).
 template <class T>
 struct DevBuf {
@@ -63,12 +70,23 @@ struct DevBuf {
         if (count == n && p) return;
         release();
         if (count == 0) return;
+#ifdef UG4GB_GUARDED
+        char *base = nullptr;
+        UG_CUDA(cudaMalloc((void **)&base, count * sizeof(T) + 2 * kGuardBytes));
+        p = (T *)(base + kGuardBytes);
+        guard_register(base, p, count * sizeof(T));
+#else
         UG_CUDA(cudaMalloc((void **)&p, count * sizeof(T)));
+#endif
         n = count;
     }
     void release()
     {
+#ifdef UG4GB_GUARDED
+        if (p) cudaFree(guard_release(p));
+#else
         if (p) cudaFree(p);
+#endif
         p = nullptr;
         n = 0;
     }
