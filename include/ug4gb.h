@@ -374,6 +374,16 @@ UG4GB_API int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp);      
    own factor; the Jacobi smoother works on the column-scaled level operator
    and combines only with itself at the same damping (ug4gb_gmg_init returns
    UG4GB_ERR_INVALID otherwise). */
+/* set_base_solver (mg_solver.h:136): UG4GB_BASE_LU (default), the dense
+   partially pivoted LU of the base level (at most 4096 unknowns), or
+   UG4GB_BASE_SMOOTHER: `steps` steps of the pre-smoother on the base level
+   from a zero correction, c += B d, d -= A (B d) -- ugcore's LinearSolver
+   with the pre-smoother as its preconditioner and StdConvCheck(steps, 0, 0)
+   with unsuccessful ends suppressed (convergence_check.h:191) -- for base
+   levels too large for the dense LU.  steps 1..1000. */
+#define UG4GB_BASE_LU 0
+#define UG4GB_BASE_SMOOTHER 1
+UG4GB_API int ug4gb_gmg_set_base_solver(ug4gb_gmg *m, int kind, int steps);
 UG4GB_API int ug4gb_gmg_set_presmoother(ug4gb_gmg *m, int kind, double damp);
 UG4GB_API int ug4gb_gmg_set_postsmoother(ug4gb_gmg *m, int kind, double damp);
 UG4GB_API int ug4gb_gmg_set_cycle_type(ug4gb_gmg *m, int cycle);  /* 1 = V, 2 = W, up to 4; -1 = F (mg_solver.h:339-341) */

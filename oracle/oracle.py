@@ -35,7 +35,7 @@ class Params(C.Structure):
         ("maxit", C.c_int), ("rel_red", C.c_double), ("min_defect", C.c_double),
         ("rap", C.c_int), ("bicg_restart", C.c_int), ("bicg_min_ortho", C.c_double),
         ("damp_prol", C.c_double), ("damp_res", C.c_double),
-        ("post_smoother", C.c_int), ("post_damp", C.c_double),
+        ("post_smoother", C.c_int), ("post_damp", C.c_double), ("base_steps", C.c_int),
     ]
 
 
@@ -113,11 +113,11 @@ def make_params(elem_type=ORC_QUAD, mx=2, my=2, mz=2, nref=6, seed=1, coef_kind=
                 coef_kmax=8.0, vel_kind=0, vel_modes=16, vel_kmax=2.0, diffusion=1.0, peclet=10.0,
                 solver=0, smoother=0, damp=0.6, nu1=2, nu2=2, cycle=1, base=0, maxit=200,
                 rel_red=1e-10, min_defect=1e-300, rap=0, bicg_restart=0, bicg_min_ortho=0.0, damp_prol=1.0,
-                damp_res=1.0, post_smoother=-1, post_damp=1.0):
+                damp_res=1.0, post_smoother=-1, post_damp=1.0, base_steps=0):
     return Params(elem_type, mx, my, mz, nref, seed, coef_kind, coef_modes, coef_kmax, vel_kind,
                   vel_modes, vel_kmax, diffusion, peclet, solver, smoother, damp, nu1, nu2, cycle,
                   base, maxit, rel_red, min_defect, rap, bicg_restart, bicg_min_ortho, damp_prol, damp_res,
-                  post_smoother, post_damp)
+                  post_smoother, post_damp, base_steps)
 
 
 class Problem:

@@ -149,6 +149,10 @@ typedef struct {
     int smoother2;
     double damp2;
     double **diaginv2;   /* Jacobi post-smoother with its own damping, else NULL */
+    /* base solver (set_base_solver, mg_solver.h:136): 0 = dense LU, 1 =
+       base_steps steps of the pre-smoother from zero (LinearSolver with
+       StdConvCheck(base_steps, 0, 0), unsuccessful ends suppressed) */
+    int base_kind, base_steps;
     orc_crs *A;          /* per level */
     orc_crs *P, *R;      /* per level (index = fine level) */
     double **diaginv;
@@ -176,6 +180,10 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
                  int nu1, int nu2, int cycle, int base, int rap);
 /* a post-smoother other than the pre-smoother (after orc_gmg_init) */
 int orc_gmg_set_postsmoother(orc_gmg *G, int smoother, double damp);
+/* base_steps > 0: the base solver is base_steps steps of the pre-smoother
+   (base_kind 1) instead of the dense LU */
+int orc_gmg_init_ex(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, double damp,
+                    int nu1, int nu2, int cycle, int base, int rap, int base_steps);
 void orc_gmg_apply(orc_gmg *G, double *c, const double *d);
 void orc_gmg_free(orc_gmg *G);
 

@@ -41,6 +41,7 @@ typedef struct {
     double damp_prol, damp_res; /* StdTransfer damping (both 1 = none) */
     int post_smoother;  /* set_postsmoother: -1 = the pre-smoother */
     double post_damp;
+    int base_steps;     /* set_base_solver: 0 = dense LU, k > 0 = k pre-smoother steps */
 } orc_params;
 
 typedef struct {
@@ -179,7 +180,8 @@ void orc_prob_source(const orc_prob *P, double *f)
 static int gmg_init_p(orc_gmg *G, const orc_prob *P, orc_crs *levA)
 {
     const orc_params *p = &P->p;
-    int rc = orc_gmg_init(G, &P->H, levA, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap);
+    int rc = orc_gmg_init_ex(G, &P->H, levA, p->smoother, p->damp, p->nu1, p->nu2, p->cycle, p->base, p->rap,
+                             p->base_steps);
     if (rc) return rc;
     if (p->post_smoother >= 0) {
         rc = orc_gmg_set_postsmoother(G, p->post_smoother, p->post_damp);

@@ -267,7 +267,15 @@ static void ilu_apply(const orc_crs *F, const int *dg, const int *color, int nco
 int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, double damp,
                  int nu1, int nu2, int cycle, int base, int rap)
 {
+    return orc_gmg_init_ex(G, H, levA, smoother, damp, nu1, nu2, cycle, base, rap, 0);
+}
+
+int orc_gmg_init_ex(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, double damp,
+                    int nu1, int nu2, int cycle, int base, int rap, int base_steps)
+{
     memset(G, 0, sizeof(*G));
+    G->base_kind = base_steps > 0 ? 1 : 0;
+    G->base_steps = base_steps;
     G->nlev = H->nlev; G->base = base; G->cycle = cycle; G->nu1 = nu1; G->nu2 = nu2;
     G->smoother = smoother; G->damp = damp;
     G->smoother2 = smoother; G->damp2 = damp;
@@ -298,9 +306,13 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
         const orc_level *L = &H->lev[l];
         int n = L->nv;
         G->sc[l] = dvec(n); G->sd[l] = dvec(n); G->st[l] = dvec(n);
-        if (l > base) {
-            if (!rap && orc_prolongation(L, &H->lev[l - 1], &G->P[l])) return -1;
-            if (!rap && orc_restriction(L, &H->lev[l - 1], &G->P[l], &G->R[l])) return -1;
+        if (l > base && !rap) {
+            if (orc_prolongation(L, &H->lev[l - 1], &G->P[l])) return -1;
+            if (orc_restriction(L, &H->lev[l - 1], &G->P[l], &G->R[l])) return -1;
+        }
+        /* smoother data on every level above the base, and on the base level
+           when it smooths instead of the LU */
+        if (l > base || G->base_kind == 1) {
             G->diaginv[l] = dvec(n);
             for (int i = 0; i < n; ++i) {
                 double m = levA[l].val[orc_crs_find(&levA[l], i, i)];
@@ -320,10 +332,10 @@ int orc_gmg_init(orc_gmg *G, const orc_hier *H, orc_crs *levA, int smoother, dou
     if (G->smoother == ORC_SMOOTH_ILU) {
         G->ilu = (orc_crs *)calloc((size_t)G->nlev, sizeof(orc_crs));
         G->ilu_diag = (int **)calloc((size_t)G->nlev, sizeof(int *));
-        for (int l = base + 1; l < G->nlev; ++l)
+        for (int l = base + 1 - G->base_kind; l < G->nlev; ++l)
             if (ilu_factor(&levA[l], G->color[l], G->ncolor[l], &G->ilu[l], &G->ilu_diag[l])) return -3;
     }
-    if (orc_lu_init(&G->lu, &levA[base])) return -2;
+    if (G->base_kind == 0 && orc_lu_init(&G->lu, &levA[base])) return -2;
     return 0;
 }
 
@@ -414,9 +426,27 @@ static void smooth(orc_gmg *G, int l, double *c, const double *d, int post)
     }
 }
 
+static void vadd(int n, double *a, const double *b);
+
 static void base_solve(orc_gmg *G, int l)
 {
-    orc_lu_apply(&G->lu, G->sc[l], G->sd[l]);
+    if (G->base_kind == 1) {
+        /* LinearSolver::apply_return_defect (linear_solver.h) on a copy of
+           the defect: c = B d, x += c, d -= A c, base_steps times */
+        int n = G->A[l].n_rows;
+        double *d = dvec(n), *c = dvec(n);
+        memcpy(d, G->sd[l], sizeof(double) * (size_t)n);
+        memset(G->sc[l], 0, sizeof(double) * (size_t)n);
+        for (int k = 0; k < G->base_steps; ++k) {
+            smooth(G, l, c, d, 0);
+            vadd(n, G->sc[l], c);
+            orc_crs_matmul_minus(&G->A[l], d, c);
+        }
+        free(d);
+        free(c);
+    } else {
+        orc_lu_apply(&G->lu, G->sc[l], G->sd[l]);
+    }
     if (l >= G->nlev - 1) orc_crs_matmul_minus(&G->A[l], G->sd[l], G->sc[l]);
 }
 

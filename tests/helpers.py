@@ -33,7 +33,8 @@ def oracle_params(orc, cfg):
         bicg_restart=int(cfg.get("bicg_restart", 0)), bicg_min_ortho=float(cfg.get("bicg_min_ortho", 0.0)),
         damp_prol=float(cfg.get("damp_prol", 1.0)), damp_res=float(cfg.get("damp_res", 1.0)),
         post_smoother=SMOOTHERS[cfg["post_smoother"]] if cfg.get("post_smoother") else -1,
-        post_damp=float(cfg.get("post_damp", 1.0)))
+        post_damp=float(cfg.get("post_damp", 1.0)),
+        base_steps=int(cfg.get("base_steps", 0)) if cfg.get("base_solver", "lu") == "smoother" else 0)
 
 
 def assert_crs_equal(a, b, rtol=VAL_RTOL, what="matrix"):

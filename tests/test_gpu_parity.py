@@ -189,6 +189,55 @@ def test_seeded_source_equals_explicit_source(ctx, name, over):
     assert np.array_equal(b_seed.view(np.int64), b2.numpy().view(np.int64))
 
 
+@pytest.mark.parametrize("name,over", [
+    ("c1", dict(nref=3, base=1, base_steps=20)),
+    ("c0", dict(nref=5, base=2, smoother="mcsgs", damp=1.0, base_steps=8)),
+    ("c2", dict(nref=2, base=1, precision="fp64", base_steps=10)),
+    ("c1", dict(nref=4, base=3, base_steps=30)),          # 17^3 = 4913 base unknowns: beyond the dense LU
+    ("c0", dict(nref=3, base=3, base_steps=5)),           # top = base: the cycle is the base iteration
+    ("c4", dict(nref=2, base=1, precision="fp64", smoother="ilu", damp=1.0, base_steps=6)),
+])
+def test_smoothing_base_solver_matches_oracle(ctx, oracle_lib, name, over):
+    """set_base_solver with a fixed number of pre-smoother steps (ugcore's
+    LinearSolver with StdConvCheck(k, 0, 0), unsuccessful end suppressed):
+    GMG application 1e-12 against the oracle, solve iterations +-1, also on
+    a base level beyond the dense LU's 4096 unknowns and with top = base"""
+    import ugcore_gb300 as ug
+    cfg, p = _problem(ctx, name, dict(over, base_solver="smoother"))
+    op = _oracle(oracle_lib, cfg, p)
+    d = np.random.default_rng(5).standard_normal(p.n)
+    _, _, bnd = p.hier.export()
+    d[bnd.astype(bool)] = 0.0
+    cv = ug.GPUVector(ctx, p.n)
+    p.gmg.apply(cv, ug.GPUVector(ctx, p.n).copy_from(d))
+    c_ref = op.apply_gmg(d)
+    assert np.abs(cv.numpy() - c_ref).max() <= 1e-12 * np.abs(c_ref).max()
+    if cfg["base"] < cfg["nref"]:
+        st = p.solve()
+        ref = op.solve()
+        assert abs(st["steps"] - ref["steps"]) <= 1
+        assert np.abs(p.x.numpy() - ref["x"]).max() <= 1e-8 * np.abs(ref["x"]).max()
+
+
+def test_smoothing_base_solver_mixed_precision(ctx, oracle_lib):
+    """the base iteration in the FP32 multigrid: the FP64 solve converges to
+    the FP64 oracle's solution"""
+    cfg, p = _problem(ctx, "c1", dict(nref=4, base=3, base_solver="smoother", base_steps=30, precision="mixed"))
+    st = p.solve()
+    ref = _oracle(oracle_lib, dict(cfg, precision="fp64"), p).solve()
+    assert st["converged"] and abs(st["steps"] - ref["steps"]) <= 2
+    assert np.abs(p.x.numpy() - ref["x"]).max() <= 1e-7 * np.abs(ref["x"]).max()
+
+
+def test_dense_lu_base_limit_is_reported(ctx):
+    """the dense LU refuses a base level above 4096 unknowns with a message"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    with pytest.raises(ug.UG4GBError) as e:
+        problems.Problem(ctx, problems.config("c1", nref=4, base=3))
+    assert "4096" in str(e.value)
+
+
 def test_jacobi_combines_only_with_itself(ctx):
     """a Jacobi pre-smoother with a Gauss-Seidel post-smoother, or two Jacobi
     dampings, are refused at init with a message (the Jacobi smoother works

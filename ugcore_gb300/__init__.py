@@ -10,9 +10,9 @@ from ._lib import UG4GBError, exported_symbols, LIB_PATH  # noqa: F401
 from .algebra import (AssembledOperator, BiCGStab, CG, Context, DomainDiscretization, GaussSeidel,  # noqa: F401
                       GeometricMultiGrid, GPUSparseMatrix, GPUVector, Jacobi, NewtonSolver, StandardLineSearch, StdConvCheck,
                       StructuredHierarchy, SymmetricGaussSeidel, ThetaTimeStep, UnstructuredHierarchy, ILU, StdTransfer, DofPermutation,
-                      BackwardGaussSeidel)
+                      BackwardGaussSeidel, LU, BaseSmoothing)
 
 __all__ = ["UG4GBError", "Context", "StructuredHierarchy", "GPUVector", "GPUSparseMatrix", "DomainDiscretization",
            "GeometricMultiGrid", "Jacobi", "GaussSeidel", "StdConvCheck", "CG", "BiCGStab", "ThetaTimeStep",
-           "AssembledOperator", "NewtonSolver", "StandardLineSearch", "UnstructuredHierarchy", "SymmetricGaussSeidel", "BackwardGaussSeidel", "ILU", "StdTransfer", "DofPermutation",
+           "AssembledOperator", "NewtonSolver", "StandardLineSearch", "UnstructuredHierarchy", "SymmetricGaussSeidel", "BackwardGaussSeidel", "LU", "BaseSmoothing", "ILU", "StdTransfer", "DofPermutation",
            "exported_symbols"]

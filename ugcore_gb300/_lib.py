@@ -15,6 +15,7 @@ OK = 0
 ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_SINGULAR, ERR_NOT_CONVERGED, ERR_BREAKDOWN, ERR_STATE = -1, -2, -3, -4, -5, -6, -7
 QUAD, HEX, TET, TRI = 0, 1, 2, 3
 SMOOTHER_JACOBI, SMOOTHER_MCGS, SMOOTHER_MCSGS, SMOOTHER_ILU, SMOOTHER_MCBGS = 0, 1, 2, 3, 4
+BASE_LU, BASE_SMOOTHER = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 SOLVER_CG, SOLVER_BICGSTAB = 0, 1
 UPWIND_NONE, UPWIND_FULL = 0, 1
@@ -103,6 +104,7 @@ _SIGS = {
     "ug4gb_gmg_create": (I, [P, P, PP]),
     "ug4gb_gmg_set_smoother": (I, [P, I, D]),
     "ug4gb_gmg_set_presmoother": (I, [P, I, D]),
+    "ug4gb_gmg_set_base_solver": (I, [P, I, I]),
     "ug4gb_gmg_set_postsmoother": (I, [P, I, D]),
     "ug4gb_gmg_set_cycle_type": (I, [P, I]),
     "ug4gb_gmg_set_num_presmooth": (I, [P, I]),

@@ -14,8 +14,11 @@ disc_bridges/multigrid_bridge.cpp, domain_disc_bridge.cpp):
     AssembledLinearOperator / matrix      GPUSparseMatrix
     GeometricMultiGrid(approxSpace)       GeometricMultiGrid(disc)
     Jacobi(0.6) / GaussSeidel()           Jacobi(0.6) / GaussSeidel() (multicolour)
-    StdTransfer                           built in (P1 prolongation, R = P^T)
-    LU                                    built in (dense base solver)
+    BackwardGaussSeidel / SGS / ILU       BackwardGaussSeidel() / SymmetricGaussSeidel() / ILU()
+    gmg:set_presmoother / postsmoother    GeometricMultiGrid.set_presmoother / set_postsmoother
+    StdTransfer                           StdTransfer (P1 prolongation, R = P^T, dampings)
+    LU (base solver)                      LU() (dense, the default)
+    LinearSolver + ConvCheck(k, 0, 0)     BaseSmoothing(k) (k pre-smoother steps)
     CG() / BiCGStab()                     CG() / BiCGStab()
     ConvCheck(maxit, minDef, red)         StdConvCheck(maxit, minDef, red)
 
@@ -571,6 +574,22 @@ class BackwardGaussSeidel(_SorRelax):
         self.kind, self.damp = _lib.SMOOTHER_MCBGS, float(relax)
 
 
+class LU:
+    """dense partially pivoted LU as the multigrid's base solver (lu.h:50;
+    the default, base levels of at most 4096 unknowns)"""
+    kind, steps = _lib.BASE_LU, 0
+
+
+class BaseSmoothing:
+    """the base solver as `steps` steps of the multigrid's pre-smoother from
+    a zero correction: ugcore's LinearSolver with that smoother and
+    StdConvCheck(steps, 0, 0) whose unsuccessful end is suppressed
+    (convergence_check.h:191); for base levels too large for the dense LU"""
+
+    def __init__(self, steps=10):
+        self.kind, self.steps = _lib.BASE_SMOOTHER, int(steps)
+
+
 class ILU:
     """ILU(0) smoother in multicolour order (GPU variant of ILU, ilu.h);
     damp scales the correction"""
@@ -685,6 +704,10 @@ class GeometricMultiGrid:
 
     def set_base_level(self, level):
         check(lib().ug4gb_gmg_set_base_level(self.h, level), self.ctx.h)
+
+    def set_base_solver(self, solver):
+        """set_base_solver (mg_solver.h:136): LU() or BaseSmoothing(steps)"""
+        check(lib().ug4gb_gmg_set_base_solver(self.h, solver.kind, solver.steps), self.ctx.h)
 
     def set_precision(self, prec):
         p = {"fp64": _lib.PREC_FP64, "mixed": _lib.PREC_MIXED, 0: 0, 1: 1}[prec]

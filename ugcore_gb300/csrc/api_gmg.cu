@@ -177,6 +177,7 @@ template <class V>
 struct GmgT : GmgBase {
     std::vector<GLevel<V>> lev;
     int base = 0, nu1 = 2, nu2 = 2, cycle = 1, smoother = 0, smoother2 = 0;
+    int base_kind = UG4GB_BASE_LU, base_steps = 0;
     double damp = 1.0, damp2 = 1.0;
     DevBuf<double> Ainv;
     DevBuf<double> z64;          // mixed precision: FP64 copy of the top correction
@@ -350,6 +351,7 @@ struct GmgT : GmgBase {
 
     void setup_base(Ctx &c)
     {
+        if (base_kind != UG4GB_BASE_LU) return;   // the base level smooths (setup_level)
         const Csr &A = lev[base].A;
         int n = A.nrows;
         UG_REQUIRE(n <= 4096, UG4GB_ERR_INVALID, "GMG base level larger than 4096 unknowns (dense LU limit)");
@@ -395,7 +397,7 @@ struct GmgT : GmgBase {
         }
         if (l == base) {
             // top == base: a single-level "cycle" is the base solve
-            base_solve<V>(c, Ainv.p, nbase, top_in, L.sc.p, skip);
+            base_correct(c, L, top_in, skip);
             if (z64.p) copy_z<V>(c, L.n, L.sc.p, z64.p, skip);
             return;
         }
@@ -430,7 +432,7 @@ struct GmgT : GmgBase {
         // ---- coarse correction
         if (l - 1 == base) {
             c.prof_tag = "L" + std::to_string(l - 1);
-            base_solve<V>(c, Ainv.p, nbase, C.dA.p, C.sc.p, skip);
+            base_correct(c, C, C.dA.p, skip);
         } else {
             const int visits = (ctype == -1) ? 2 : ctype;
             for (int i = 0; i < visits; ++i) {
@@ -493,6 +495,29 @@ struct GmgT : GmgBase {
         L.dcur = const_cast<V *>(dbase);
     }
 
+    // sc = base solver applied to the base level defect d: the dense LU, or
+    // base_steps steps of the pre-smoother from sc = 0 (c += B d, d -= A B d;
+    // the defect buffers of the level take the updated defects)
+    void base_correct(Ctx &c, GLevel<V> &L, const V *d, const int *skip)
+    {
+        if (base_kind == UG4GB_BASE_LU) {
+            base_solve<V>(c, Ainv.p, nbase, d, L.sc.p, skip);
+            return;
+        }
+        const V *cur = d;
+        for (int k = 0; k < base_steps; ++k) {
+            V *out = (cur == L.dA.p) ? L.dB.p : L.dA.p;
+            const int mode = (k == 0) ? SC_SET_FROM_BASE : SC_ADD_FROM_BASE;
+            if (smoother == UG4GB_SMOOTHER_JACOBI) {
+                smooth_step<V, V, V>(c, L.At, cur, cur, L.dinv.p, L.sc.p, out, mode, skip, nullptr, nullptr, 0);
+            } else {
+                gs_sweep(c, L, cur, skip, smoother, L.dinv.p, damp);
+                residual_update<V, V>(c, L.At, L.t.p, cur, out, L.sc.p, mode == SC_SET_FROM_BASE ? 1 : 0, skip);
+            }
+            cur = out;
+        }
+    }
+
     // t = B d of smoother `kind` (dinv = relax/a_ii; ILU: damp scales the
     // correction): colours in increasing order from t = 0; the symmetric
     // smoother then sweeps the colours in decreasing order, the backward one
@@ -548,6 +573,8 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
     G->damp = m->damp;
     G->smoother2 = m->smoother2;
     G->damp2 = m->damp2;
+    G->base_kind = m->base_kind;
+    G->base_steps = m->base_steps;
     UG_REQUIRE((m->smoother == UG4GB_SMOOTHER_JACOBI) == (m->smoother2 == UG4GB_SMOOTHER_JACOBI) &&
                    (m->smoother != UG4GB_SMOOTHER_JACOBI || m->damp == m->damp2),
                UG4GB_ERR_INVALID,
@@ -606,7 +633,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
             }
             if (m->transposed) transpose_level(l, same);
             L.asm_ok = true;
-            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base, same);
+            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base && m->base_kind == UG4GB_BASE_LU, same);
             if (l > m->base) {
                 if (!keep_transfers) G->setup_transfers(c, L, g->lev[l], g->lev[l - 1], m->damp_prol, m->damp_res);
                 if (L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI)
@@ -625,7 +652,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
         }
         for (int l = m->base; l < nl; ++l) {
             GLevel<V> &L = G->lev[l];
-            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base, false);
+            G->setup_level(c, L, g->lev[l], l, m->damp, l == m->base && m->base_kind == UG4GB_BASE_LU, false);
             if (l > m->base && L.grid_transfer && m->smoother == UG4GB_SMOOTHER_JACOBI)
                 L.sweep2 = sweep2_prepare<V>(c, L.At, L.gp);
         }
@@ -684,6 +711,15 @@ int ug4gb_gmg_set_smoother(ug4gb_gmg *m, int kind, double damp)
     if (!m || !smoother_ok(kind, damp)) return UG4GB_ERR_INVALID;
     m->smoother = m->smoother2 = kind;
     m->damp = m->damp2 = damp;
+    return UG4GB_OK;
+}
+
+int ug4gb_gmg_set_base_solver(ug4gb_gmg *m, int kind, int steps)
+{
+    if (!m || (kind != UG4GB_BASE_LU && kind != UG4GB_BASE_SMOOTHER)) return UG4GB_ERR_INVALID;
+    if (kind == UG4GB_BASE_SMOOTHER && (steps < 1 || steps > 1000)) return UG4GB_ERR_INVALID;
+    m->base_kind = kind;
+    m->base_steps = kind == UG4GB_BASE_SMOOTHER ? steps : 0;
     return UG4GB_OK;
 }
 
@@ -791,7 +827,7 @@ int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
         // the forward and the transposed cycle keeps the structure)
         const GmgKey key{m->disc->g->uid, (int)m->disc->g->lev.size(), m->base, m->smoother, m->damp, m->rap,
                          0, m->precision, m->ctx->c.allow_dia ? 1 : 0, m->damp_prol, m->damp_res, m->smoother2,
-                         m->damp2};
+                         m->damp2, m->base_kind, m->base_steps};
         const bool reuse = m->impl && m->built == key;
         const uint64_t before = reuse ? (m->impl->signature() ^ m->built_settings) : 0;
         GmgBase *old = reuse ? m->impl.release() : nullptr;

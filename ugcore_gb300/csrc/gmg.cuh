@@ -190,11 +190,13 @@ struct GmgKey {
     double damp_prol = 1.0, damp_res = 1.0;
     int smoother2 = 0;
     double damp2 = 0.0;
+    int base_kind = 0, base_steps = 0;
     bool operator==(const GmgKey &o) const
     {
         return g && g == o.g && nl == o.nl && base == o.base && smoother == o.smoother && damp == o.damp &&
                rap == o.rap && transposed == o.transposed && precision == o.precision && allow_dia == o.allow_dia &&
-               damp_prol == o.damp_prol && damp_res == o.damp_res && smoother2 == o.smoother2 && damp2 == o.damp2;
+               damp_prol == o.damp_prol && damp_res == o.damp_res && smoother2 == o.smoother2 && damp2 == o.damp2 &&
+               base_kind == o.base_kind && base_steps == o.base_steps;
     }
 };
 
@@ -206,6 +208,7 @@ struct ug4gb_gmg {
     int smoother2 = UG4GB_SMOOTHER_JACOBI;  // post-smoother
     double damp2 = 0.6;
     int cycle = 1, nu1 = 2, nu2 = 2, base = 0;
+    int base_kind = UG4GB_BASE_LU, base_steps = 10;   // base solver (set_base_solver)
     int precision = UG4GB_PREC_FP64;
     int transposed = 0;
     int rap = 0;                 // coarse operators as Galerkin products R A P (set_rap)

@@ -22,7 +22,7 @@ import copy
 import numpy as np
 
 from . import fields
-from .algebra import (BackwardGaussSeidel, BiCGStab, CG, DomainDiscretization, GaussSeidel, GeometricMultiGrid,
+from .algebra import (BackwardGaussSeidel, BaseSmoothing, BiCGStab, CG, DomainDiscretization, GaussSeidel, GeometricMultiGrid,
                       GPUSparseMatrix,
                       GPUVector, ILU, Jacobi, StdConvCheck, StdTransfer, StructuredHierarchy, SymmetricGaussSeidel,
                       ThetaTimeStep)
@@ -119,6 +119,8 @@ class Problem:
         g.set_num_presmooth(c["nu1"])
         g.set_num_postsmooth(c["nu2"])
         g.set_base_level(c["base"])
+        if c.get("base_solver", "lu") == "smoother":
+            g.set_base_solver(BaseSmoothing(c.get("base_steps", 10)))
         g.set_precision(c["precision"])
         g.set_transposed(transposed)
         g.set_rap(c["rap"])
