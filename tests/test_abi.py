@@ -171,6 +171,90 @@ int main() { return ug::GPUAlgebra::get_type().type() == ug::AlgebraType::GPU ? 
     assert r.returncode == 0, r.stderr[-4000:]
 
 
+def test_ugcore_cg_drives_the_library_at_run_time(tmp_path):
+    """An executable from ugcore's own CG, StdConvCheck and MatrixOperator
+    (headers of the reference tree) over the GPU algebra and multigrid,
+    linked with ugcore's common/ objects (built by oracle/build_ref.sh from
+    the reference sources) and libug4gb.so: it assembles the 17^3 hex
+    Poisson problem through the C ABI and solves it with ugcore's CG and the
+    library's multigrid.  Where a GPU is present it must converge; without
+    one it must stop at the first device call with ugcore's error type
+    (UGError, exit 2) and the library's message."""
+    from helpers import reference_tree
+    from ugcore_gb300 import build
+    ref = reference_tree()
+    if ref is None:
+        pytest.skip("ugcore source tree not present")
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("no C++ compiler")
+    r = subprocess.run(["sh", os.path.join(ROOT, "oracle", "build_ref.sh")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    obj = os.path.join(ROOT, "oracle", "_ref", "obj")
+    objs = [os.path.join(obj, o) for o in ("common_log.o", "common_debug_id.o", "common_assert.o", "common_error.o",
+                                           "common_progress.o", "common_util_string_util.o",
+                                           "common_util_ostream_buffer_splitter.o", "crc32_stub.o")]
+    for o in objs:
+        assert os.path.exists(o), o
+    lib = build.build()
+    src = tmp_path / "run.cpp"
+    src.write_text(r'''
+#include <cstdio>
+#include "ug4gb_algebra.h"
+#include "ug4gb_preconditioner.h"
+#include "lib_algebra/operator/interface/matrix_operator.h"
+#include "lib_algebra/operator/linear_solver/cg.h"
+#include "lib_algebra/operator/convergence_check.h"
+using namespace ug;
+typedef MatrixOperator<UG4GBSparseMatrix, UG4GBVector> Op;
+int main()
+{
+    try {
+        SmartPtr<Op> A = make_sp(new Op);                       // first device call: the engine context
+        ug4gb_ctx *ctx = ug4gb_glue::context().get();
+        ug4gb_grid *g = nullptr;
+        ug4gb_disc *d = nullptr;
+        ug4gb::check(ug4gb_grid_create_structured(ctx, UG4GB_HEX, 2, 2, 2, 3, &g), ctx, "grid");
+        ug4gb::check(ug4gb_disc_create(ctx, g, &d), ctx, "disc");
+        ug4gb::check(ug4gb_disc_set_diffusion_constant(d, 1.0), ctx, "diffusion");
+        ug4gb::check(ug4gb_disc_set_source_uniform(d, 1), ctx, "source");
+        const int top = ug4gb_grid_num_levels(g) - 1;
+        int n = 0;
+        ug4gb::check(ug4gb_grid_level_info(g, top, &n, nullptr, nullptr, nullptr), ctx, "level");
+        UG4GBVector u(n), b(n);
+        ug4gb::check(ug4gb_disc_assemble_linear(d, top, A->impl().get(), b.impl().get()), ctx, "assemble");
+        SmartPtr<UG4GBGeometricMultiGrid> gmg = make_sp(new UG4GBGeometricMultiGrid(d));
+        gmg->set_smoother(UG4GB_SMOOTHER_JACOBI, 0.6);
+        CG<UG4GBVector> cg;                                      // ugcore's own CG (cg.h)
+        cg.set_preconditioner(gmg);
+        cg.set_convergence_check(make_sp(new StdConvCheck<UG4GBVector>(100, 1e-50, 1e-10, false)));
+        cg.init(A);
+        u.set(0.0);
+        const bool ok = cg.apply(u, b);
+        std::printf("ok %d steps %d\n", ok ? 1 : 0, cg.step());
+        return ok ? 0 : 1;
+    } catch (const UGError &e) {
+        std::printf("error: %s\n", e.get_msg().c_str());
+        return 2;
+    }
+}
+''')
+    shim = os.path.join(ROOT, "oracle", "_ref", "shim")
+    exe = tmp_path / "run"
+    r = subprocess.run([cxx, "-std=c++17", "-O1", "-w", "-I" + shim, "-I" + os.path.join(ref, "ugbase"),
+                        "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "ugcore_gb300", "adapters"),
+                        str(src)] + objs + [lib, "-Wl,-rpath," + os.path.dirname(lib), "-o", str(exe)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-4000:]
+    import torch
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    if torch.cuda.is_available():
+        assert r.returncode == 0 and "ok 1" in r.stdout, r.stdout + r.stderr
+    else:
+        assert r.returncode == 2 and r.stdout.startswith("error:") and "UG4GBSparseMatrix" in r.stdout, \
+            r.stdout + r.stderr
+
+
 BOOST_STANDIN_HEADERS = [
     "boost/mpl/at.hpp", "boost/mpl/empty.hpp", "boost/mpl/fold.hpp", "boost/mpl/for_each.hpp", "boost/mpl/front.hpp",
     "boost/mpl/if.hpp", "boost/mpl/list.hpp", "boost/mpl/map.hpp", "boost/mpl/min_max.hpp", "boost/mpl/pop_front.hpp",
