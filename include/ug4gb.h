@@ -90,11 +90,11 @@ UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
 /* performance switches that leave every result bit-identical.
    UG4GB_TUNE_PDL (0 or 1): programmatic dependent launch of the solve-path
    kernels, each kernel scheduled while its predecessor still runs (default 1).
-   UG4GB_TUNE_SWEEP_FUSION (bit mask, 0..7): two consecutive damped-Jacobi
+   UG4GB_TUNE_SWEEP_FUSION (bit mask, 0..3): two consecutive damped-Jacobi
    steps of a structured 3D FP32 level in one pass over its operator.  Bit 1:
    on; bit 2: levels of every size (else only levels of at least 2^18
-   vertices); bit 4: automatic, on for 27-point (hexahedral) levels of at
-   least 4,194,304 vertices, where it is faster.  Default 4.  Smoothed
+   vertices).  Default 0: inside the solve's CUDA graph the one-step kernels
+   overlap through programmatic dependent launch and are as fast.  Smoothed
    corrections and defects are bit-identical; inside a Krylov solve only the
    summation order of the fused (z, r) product changes.  Applies to
    multigrids set up after the call (the fused levels keep a line-padded

@@ -28,7 +28,7 @@ FILES = ["tests/test_gpu_parity.py", "tests/test_gpu_algebra_ops.py", "tests/tes
          "tests/test_gpu_sweep_fusion.py", "tests/test_gpu_time_step.py", "tests/test_gpu_unstructured.py",
          "tests/test_gpu_adjoint.py"]
 # full-size cases (193^3 and 129^3 problems) are left to the normal build
-SKIP = "not full_size and not automatic_fusion"
+SKIP = "not full_size"
 
 
 def test_gpu_paths_keep_their_buffers(tmp_path):

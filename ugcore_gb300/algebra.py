@@ -81,8 +81,7 @@ class Context:
     def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None, row_assembly=None, sweep_wait_test=None):
         """performance switches:
         pdl: programmatic dependent launch of the solve kernels;
-        sweep_fusion: bit mask (1 on, 2 every level size, 4 automatic: the
-        default, on for hexahedral levels of at least 4M vertices) of the
+        sweep_fusion: bit mask (1 on, 2 every level size) of the
         two-Jacobi-steps-per-pass smoother of structured 3D FP32 levels;
         sweep_planes: z planes per block of that smoother (these three leave
         results bit-identical);

@@ -163,7 +163,7 @@ int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value)
         ctx->c.pdl = value != 0;
         return UG4GB_OK;
     case UG4GB_TUNE_SWEEP_FUSION:
-        if (value < 0 || value > 7) return UG4GB_ERR_INVALID;
+        if (value < 0 || value > 3) return UG4GB_ERR_INVALID;
         ctx->c.sweep_fusion = value;
         return UG4GB_OK;
     case UG4GB_TUNE_SWEEP_PLANES:

@@ -113,13 +113,9 @@ struct Ctx {
     // coefficient for all elements from the one interior stencil (2)
     int row_assembly = 2;
     // two Jacobi steps per pass on structured 3D FP32 levels (bit mask):
-    // 1 = on, 2 = every level size (else >= sweep_fusion_min_rows vertices),
-    // 4 = automatic: 27-point levels of >= sweep_fusion_auto_rows vertices,
-    // where the pass over the operator saves more than the shared-memory
-    // traffic costs (193^3 hexahedra: 226 against 278 us per pair)
-    int sweep_fusion = 4;
+    // 1 = on, 2 = every level size (else >= sweep_fusion_min_rows vertices)
+    int sweep_fusion = 0;
     int sweep_fusion_min_rows = 1 << 18;
-    int sweep_fusion_auto_rows = 4 << 20;
     int sweep_fusion_tz = 8;    // z planes per block
     int sweep_wait_test = 0;    // failure test only: bytes no copy delivers (fused sweeps' bounded waits run out)
     std::string prof_tag;       // set by the orchestration (level / phase)

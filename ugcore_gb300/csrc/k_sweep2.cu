@@ -539,12 +539,11 @@ EncodeTiled encode_tiled()
 
 }  // namespace
 
-// the fused pairs run on a level of S diagonals and n vertices (the bit
-// mask Ctx::sweep_fusion)
-static bool sweep2_wanted(const Ctx &c, int S, int64_t n)
+// the fused pairs run on a level of n vertices (the bit mask
+// Ctx::sweep_fusion)
+static bool sweep2_wanted(const Ctx &c, int64_t n)
 {
-    if (c.sweep_fusion & 1) return (c.sweep_fusion & 2) || n >= c.sweep_fusion_min_rows;
-    return (c.sweep_fusion & 4) && S == 27 && n >= c.sweep_fusion_auto_rows;
+    return (c.sweep_fusion & 1) && ((c.sweep_fusion & 2) || n >= c.sweep_fusion_min_rows);
 }
 
 struct Sweep2Op {
@@ -563,7 +562,7 @@ std::shared_ptr<Sweep2Op> sweep2_prepare(Ctx &c, const OpMat<V> &At, const GridP
         const Dia<V> &D = At.dia;
         if (D.S != 15 && D.S != 27) return nullptr;
         // no padded copy for a level the pairs will not run on
-        if (!sweep2_wanted(c, D.S, (int64_t)gp.nx * gp.ny * gp.nz)) return nullptr;
+        if (!sweep2_wanted(c, (int64_t)gp.nx * gp.ny * gp.nz)) return nullptr;
         if ((int64_t)gp.nx * gp.ny * gp.nz != D.nrows || D.nrows != D.ncols) return nullptr;
         if (!stencil_matches(D.off.o, D.S, gp.nx, gp.ny)) return nullptr;
         Stencil st{};
@@ -617,7 +616,7 @@ bool smooth_pair(Ctx &c, const Sweep2Op *op, const GridPair &gp, const V *xA, co
         if (!op) return false;
         if (op->nx != gp.nx || op->ny != gp.ny || op->nz != gp.nz) return false;
         const int64_t n = (int64_t)gp.nx * gp.ny * gp.nz;
-        if (!sweep2_wanted(c, op->S, n)) return false;
+        if (!sweep2_wanted(c, n)) return false;
         if (modeB == SC_SET_FROM_BASE) return false;
         Sweep2Args<float> a{};
         a.nx = gp.nx;
