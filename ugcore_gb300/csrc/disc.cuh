@@ -51,6 +51,9 @@ struct RowAsmCache {
     std::vector<double> A, vol;         // unit-coefficient element matrices, SCV volumes per class
     DevBuf<double> normal, ipoff;       // SCVF area normals / ips relative to the cell origin per class
     DevBuf<double> flux;                // per element and SCVF: v(ip).n (convection)
+    double volsum = 0.0;                // sum of an interior vertex's SCV volumes (gather order)
+    DevBuf<int> brows;                  // the rows on the box boundary
+    int nbrows = 0;
 };
 // stationary assembly of a structured level row by row (k_fv1_rows.cu):
 // every value of A and b written once, Dirichlet rows included; returns

@@ -16,7 +16,10 @@
 // contain the vertex) in increasing cell order, the order in which the
 // element-wise reference adds them, and writes every value of the row and
 // its right-hand side once: no read-modify-write of the matrix, no colour
-// passes, no atomics.  Convection (full upwind, ConvectionShapesFullUpwind,
+// passes, no atomics.  The right-hand side of an interior row is
+// f_i * sum_e |SCV_i^e|, the volumes summed once per level in the gather
+// order (the element-wise reference adds the products f_i |SCV_i^e|; the two
+// agree to rounding).  Convection (full upwind, ConvectionShapesFullUpwind,
 // conv_shape.h:277-345) enters through the SCVF fluxes v(ip).n of each
 // element, computed once per element and SCVF by k_scvf_flux.
 // Rows on the box boundary (Dirichlet rows) get the identity row and a zero
@@ -283,9 +286,20 @@ __global__ void k_check_row_lengths(int cx, int cy, int cz, const int *__restric
     if (rowptr[r + 1] - rowptr[r] != S::N) atomicExch(ok, 0);
 }
 
+// the sum of an interior vertex's SCV volumes in the order of gather_row
+template <int T>
+__global__ void k_row_volsum(AsmArgs a, ClassData<T> cd, double *out)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    gather_row<T>(cd, a, 1, 1, (Stencil<T>::DIM == 3) ? 1 : 0, nullptr, [](int, double) {}, [&](double v) { s += v; });
+    out[0] = s;
+}
+
 // interior rows: one thread per row, every value written once
 template <int T>
-__global__ void __launch_bounds__(128) k_assemble_rows(AsmArgs a, ClassData<T> cd, const double *__restrict__ flux)
+__global__ void __launch_bounds__(128) k_assemble_rows(AsmArgs a, ClassData<T> cd, const double *__restrict__ flux,
+                                                       double volsum)
 {
     using S = Stencil<T>;
     const int nix = a.cx - 1, niy = a.cy - 1, niz = (S::DIM == 3) ? a.cz - 1 : 1;
@@ -297,14 +311,11 @@ __global__ void __launch_bounds__(128) k_assemble_rows(AsmArgs a, ClassData<T> c
     double acc[S::N];
 #pragma unroll
     for (int s = 0; s < S::N; ++s) acc[s] = 0.0;
-    double vsum = 0.0;
-    const double fr = a.b ? source_at(a, r) : 0.0;
-    gather_row<T>(cd, a, i, j, k, flux, [&](int s, double v) { acc[s] += v; },
-                  [&](double vol) { vsum += fr * vol; });
+    gather_row<T>(cd, a, i, j, k, flux, [&](int s, double v) { acc[s] += v; }, [](double) {});
     double *row = a.val + __ldg(a.rowptr + r);
 #pragma unroll
     for (int s = 0; s < S::N; ++s) row[s] = acc[s];
-    if (a.b) a.b[r] = vsum;
+    if (a.b) a.b[r] = source_at(a, r) * volsum;
 }
 
 // interior rows with one coefficient K for all elements and no convection:
@@ -315,7 +326,7 @@ __global__ void __launch_bounds__(128) k_assemble_rows(AsmArgs a, ClassData<T> c
 // line with consecutive threads on consecutive values.  b as in
 // k_assemble_rows, from the same sequence of SCV volumes.
 template <int T>
-__global__ void __launch_bounds__(128) k_assemble_rows_uniform(AsmArgs a, ClassData<T> cd)
+__global__ void __launch_bounds__(128) k_assemble_rows_uniform(AsmArgs a, ClassData<T> cd, double volsum)
 {
     using S = Stencil<T>;
     __shared__ double st[S::N];
@@ -330,19 +341,11 @@ __global__ void __launch_bounds__(128) k_assemble_rows_uniform(AsmArgs a, ClassD
 #pragma unroll
         for (int s = 0; s < S::N; ++s) st[s] = acc[s];
     }
-    // b while thread 0 gathers the stencil: the SCV volumes in the order of
-    // gather_row come from the kernel parameters (its value callback is empty)
+    // b while thread 0 gathers the stencil
     const int nx = a.cx + 1, ny = a.cy + 1;
     const int r0 = 1 + nx * (j + ny * k);
-    if (a.b) {
-        for (int i = threadIdx.x; i < nix; i += blockDim.x) {
-            const int r = r0 + i;
-            const double fr = source_at(a, r);
-            double vsum = 0.0;
-            gather_row<T>(cd, a, 1, 1, kk, nullptr, [](int, double) {}, [&](double vol) { vsum += fr * vol; });
-            a.b[r] = vsum;
-        }
-    }
+    if (a.b)
+        for (int i = threadIdx.x; i < nix; i += blockDim.x) a.b[r0 + i] = source_at(a, r0 + i) * volsum;
     __syncthreads();
     double *line = a.val + __ldg(a.rowptr + r0);
     const int len = S::N * nix;
@@ -354,16 +357,16 @@ __global__ void __launch_bounds__(128) k_assemble_rows_uniform(AsmArgs a, ClassD
 template <int T>
 __global__ void __launch_bounds__(128) k_assemble_boundary_rows(AsmArgs a, ClassData<T> cd,
                                                                 const double *__restrict__ flux,
-                                                                const unsigned char *__restrict__ bnd)
+                                                                const unsigned char *__restrict__ bnd,
+                                                                const int *__restrict__ brows, int nbrows)
 {
     using CT = ClassTraits<T>;
     using E = Elem<T>;
-    const int nx = a.cx + 1, ny = a.cy + 1, nz = (CT::DIM == 3) ? a.cz + 1 : 1;
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= nx * ny * nz) return;
+    const int nx = a.cx + 1, ny = a.cy + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nbrows) return;
+    const int r = brows[t];
     const int i = r % nx, j = (r / nx) % ny, k = r / (nx * ny);
-    const bool onb = i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (CT::DIM == 3 && (k == 0 || k == nz - 1));
-    if (!onb) return;
     const int r0 = a.rowptr[r], r1 = a.rowptr[r + 1];
     if (bnd[r]) {
         for (int q = r0; q < r1; ++q) a.val[q] = (a.col[q] == r) ? 1.0 : 0.0;
@@ -465,6 +468,25 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
         a.cx = cx;
         a.cy = cy;
         a.cz = cz;
+        if (cache.nbrows == 0) {
+            // once per level: the interior rows' SCV volume sum and the list of
+            // the rows on the box boundary
+            DevBuf<double> vs;
+            vs.alloc(1);
+            UG_LAUNCH(c, k_row_volsum<T>, 1, 32, 0, a, cd, vs.p);
+            copy_out(c, &cache.volsum, vs.p, sizeof(double));
+            const int nx = L.nx, ny = L.ny, nz = (L.dim == 3) ? L.nz : 1;
+            std::vector<int> rows;
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i)
+                        if (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (L.dim == 3 && (k == 0 || k == nz - 1)))
+                            rows.push_back(i + nx * (j + ny * k));
+            cache.brows.alloc(rows.size());
+            copy_in(c, cache.brows.p, rows.data(), sizeof(int) * rows.size());
+            UG_CUDA(cudaStreamSynchronize(c.stream));
+            cache.nbrows = (int)rows.size();
+        }
         const double *flux = nullptr;
         if (a.vmodes > 0) {
             if constexpr (E::DIM == 3) {
@@ -482,11 +504,12 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
         }
         if (a.k_uniform && !flux) {
             const int nlines = (cy - 1) * ((L.dim == 3) ? cz - 1 : 1);
-            UG_LAUNCH(c, k_assemble_rows_uniform<T>, nlines, 128, 0, a, cd);
+            UG_LAUNCH(c, k_assemble_rows_uniform<T>, nlines, 128, 0, a, cd, cache.volsum);
         } else {
-            UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux);
+            UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux, cache.volsum);
         }
-        UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(L.nv, 128), 128, 0, a, cd, flux, L.bnd.p);
+        UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 128), 128, 0, a, cd, flux, L.bnd.p,
+                  cache.brows.p, cache.nbrows);
         done = true;
     };
     switch (L.elem_type) {
