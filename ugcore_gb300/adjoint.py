@@ -8,10 +8,12 @@ transposed system A^T lambda = dJ/du with the same multigrid built on the
 transposed level operators (Dirichlet rows reset to identity) and forms
     dJ/dm_e = -K_e * sum_{i not Dirichlet} lambda_i (A1_e u_e)_i
     dJ/df_i = lambda_i * |SCV_i|
-with element-local kernels.  Level checkpointing: the forward pass keeps only
-u (one vector) for the backward pass; the multigrid hierarchy of the adjoint
-is rebuilt from the stored operators instead of keeping per-level forward
-states, so the memory cost of the backward pass is one extra hierarchy.
+with element-local kernels.  The forward pass keeps only u (one vector) for
+the backward pass.  The transposed multigrid either sits beside the forward
+one (adjoint_memory "store": one extra hierarchy of device memory) or is the
+forward multigrid transposed in place, level by level, and re-assembled for
+the next forward pass (adjoint_memory "recompute": no memory beyond the
+forward solve's).
 """
 import torch
 

@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(128) k_assemble_rows_uniform(AsmArgs a, ClassD
 // rows on the box boundary: the identity row and b = 0 at Dirichlet
 // vertices; otherwise the elements that exist, entries found by search
 template <int T>
-__global__ void __launch_bounds__(128) k_assemble_boundary_rows(AsmArgs a, ClassData<T> cd,
+__global__ void __launch_bounds__(256) k_assemble_boundary_rows(AsmArgs a, ClassData<T> cd,
                                                                 const double *__restrict__ flux,
                                                                 const unsigned char *__restrict__ bnd,
                                                                 const int *__restrict__ brows, int nbrows)
@@ -363,16 +363,20 @@ __global__ void __launch_bounds__(128) k_assemble_boundary_rows(AsmArgs a, Class
     using CT = ClassTraits<T>;
     using E = Elem<T>;
     const int nx = a.cx + 1, ny = a.cy + 1;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    // one warp per row: the lanes write a Dirichlet row's entries side by
+    // side; lane 0 assembles a row without the Dirichlet flag
+    const int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (t >= nbrows) return;
     const int r = brows[t];
     const int i = r % nx, j = (r / nx) % ny, k = r / (nx * ny);
     const int r0 = a.rowptr[r], r1 = a.rowptr[r + 1];
     if (bnd[r]) {
-        for (int q = r0; q < r1; ++q) a.val[q] = (a.col[q] == r) ? 1.0 : 0.0;
-        if (a.b) a.b[r] = 0.0;
+        for (int q = r0 + lane; q < r1; q += 32) a.val[q] = (a.col[q] == r) ? 1.0 : 0.0;
+        if (a.b && lane == 0) a.b[r] = 0.0;
         return;
     }
+    if (lane != 0) return;
     for (int q = r0; q < r1; ++q) a.val[q] = 0.0;
     double vsum = 0.0;
     const double fr = a.b ? source_at(a, r) : 0.0;
@@ -508,7 +512,7 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
         } else {
             UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux, cache.volsum);
         }
-        UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 128), 128, 0, a, cd, flux, L.bnd.p,
+        UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 8), 256, 0, a, cd, flux, L.bnd.p,
                   cache.brows.p, cache.nbrows);
         done = true;
     };
