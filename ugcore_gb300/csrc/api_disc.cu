@@ -78,6 +78,7 @@ void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const T
     a.vc = D.vc.p;
     a.vphase = D.vphase.p;
     a.vscale = D.vscale;
+    a.vel_version = D.vel_version;
     a.rowptr = A->A.rowptr.p;
     a.col = A->A.col.p;
     a.val = A->A.val.p;
@@ -125,6 +126,7 @@ void disc_defect(ug4gb_disc *d, int level, const double *u, double *dvec, const 
     a.vc = D.vc.p;
     a.vphase = D.vphase.p;
     a.vscale = D.vscale;
+    a.vel_version = D.vel_version;
     a.rowptr = nullptr;
     a.col = nullptr;
     a.val = nullptr;
@@ -242,6 +244,7 @@ int ug4gb_disc_set_velocity_fourier_curl(ug4gb_disc *d, int nmodes, const double
         copy_in(d->ctx->c, D.vphase.p, phase, sizeof(double) * (size_t)nmodes);
         UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
         D.vscale = scale;
+        D.vel_version++;
     });
 }
 

@@ -19,6 +19,7 @@ struct AsmArgs {
     int vmodes;               // velocity field (3D curl form), 0 = none
     const double *vk, *vc, *vphase;
     double vscale;
+    uint64_t vel_version = 0;  // changes with the velocity field (cached fluxes)
     const int *rowptr;        // level CRS to scatter into
     const int *col;
     double *val;
@@ -51,6 +52,7 @@ struct RowAsmCache {
     std::vector<double> A, vol;         // unit-coefficient element matrices, SCV volumes per class
     DevBuf<double> normal, ipoff;       // SCVF area normals / ips relative to the cell origin per class
     DevBuf<double> flux;                // per element and SCVF: v(ip).n (convection)
+    uint64_t flux_version = 0;          // velocity field version flux holds (0: none)
     double volsum = 0.0;                // sum of an interior vertex's SCV volumes (gather order)
     DevBuf<int> brows;                  // the rows on the box boundary
     int nbrows = 0;

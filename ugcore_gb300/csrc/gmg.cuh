@@ -87,6 +87,7 @@ struct DiscImpl {
     std::vector<DevBuf<double>> Klev;      // cache per level
     std::vector<bool> Kvalid;
     int vmodes = 0;
+    uint64_t vel_version = 0;              // counts velocity field changes
     DevBuf<double> vk, vc, vphase;
     double vscale = 1.0;
     int upwind = 0;

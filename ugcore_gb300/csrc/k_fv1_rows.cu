@@ -318,65 +318,19 @@ __global__ void __launch_bounds__(128) k_assemble_rows(AsmArgs a, ClassData<T> c
     if (a.b) a.b[r] = source_at(a, r) * volsum;
 }
 
-// interior rows with one coefficient K for all elements and no convection:
-// every interior row holds the same stencil.  One block per line of interior
-// rows (fixed j, k), whose values are contiguous in the CRS; thread 0
-// gathers the stencil of the interior row (1, 1, 1) with the arithmetic of
-// k_assemble_rows (so the values are the same), then the block writes the
-// line with consecutive threads on consecutive values.  b as in
-// k_assemble_rows, from the same sequence of SCV volumes.
-template <int T>
-__global__ void __launch_bounds__(128) k_assemble_rows_uniform(AsmArgs a, ClassData<T> cd, double volsum)
-{
-    using S = Stencil<T>;
-    __shared__ double st[S::N];
-    const int nix = a.cx - 1, niy = a.cy - 1;
-    const int j = 1 + (int)(blockIdx.x % (unsigned)niy), k = (S::DIM == 3) ? 1 + (int)(blockIdx.x / (unsigned)niy) : 0;
-    const int kk = (S::DIM == 3) ? 1 : 0;
-    if (threadIdx.x == 0) {
-        double acc[S::N];
-#pragma unroll
-        for (int s = 0; s < S::N; ++s) acc[s] = 0.0;
-        gather_row<T>(cd, a, 1, 1, kk, nullptr, [&](int s, double v) { acc[s] += v; }, [](double) {});
-#pragma unroll
-        for (int s = 0; s < S::N; ++s) st[s] = acc[s];
-    }
-    // b while thread 0 gathers the stencil
-    const int nx = a.cx + 1, ny = a.cy + 1;
-    const int r0 = 1 + nx * (j + ny * k);
-    if (a.b)
-        for (int i = threadIdx.x; i < nix; i += blockDim.x) a.b[r0 + i] = source_at(a, r0 + i) * volsum;
-    __syncthreads();
-    double *line = a.val + __ldg(a.rowptr + r0);
-    const int len = S::N * nix;
-    for (int q = threadIdx.x; q < len; q += blockDim.x) line[q] = st[q % S::N];
-}
 
 // rows on the box boundary: the identity row and b = 0 at Dirichlet
 // vertices; otherwise the elements that exist, entries found by search
+// a boundary row without the Dirichlet flag: the elements that exist, entries
+// found by binary search in the row (rare; kept out of line)
 template <int T>
-__global__ void __launch_bounds__(256) k_assemble_boundary_rows(AsmArgs a, ClassData<T> cd,
-                                                                const double *__restrict__ flux,
-                                                                const unsigned char *__restrict__ bnd,
-                                                                const int *__restrict__ brows, int nbrows)
+__device__ __noinline__ void boundary_row_general(const AsmArgs &a, const ClassData<T> &cd,
+                                                  const double *__restrict__ flux, int r, int r0, int r1)
 {
     using CT = ClassTraits<T>;
     using E = Elem<T>;
     const int nx = a.cx + 1, ny = a.cy + 1;
-    // one warp per row: the lanes write a Dirichlet row's entries side by
-    // side; lane 0 assembles a row without the Dirichlet flag
-    const int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    const int lane = threadIdx.x & 31;
-    if (t >= nbrows) return;
-    const int r = brows[t];
     const int i = r % nx, j = (r / nx) % ny, k = r / (nx * ny);
-    const int r0 = a.rowptr[r], r1 = a.rowptr[r + 1];
-    if (bnd[r]) {
-        for (int q = r0 + lane; q < r1; q += 32) a.val[q] = (a.col[q] == r) ? 1.0 : 0.0;
-        if (a.b && lane == 0) a.b[r] = 0.0;
-        return;
-    }
-    if (lane != 0) return;
     for (int q = r0; q < r1; ++q) a.val[q] = 0.0;
     double vsum = 0.0;
     const double fr = a.b ? source_at(a, r) : 0.0;
@@ -425,6 +379,80 @@ __global__ void __launch_bounds__(256) k_assemble_boundary_rows(AsmArgs a, Class
                 }
             }
     if (a.b) a.b[r] = vsum;
+}
+
+// one boundary row by the lanes of a warp: a Dirichlet row is the identity
+// row with b = 0, any other row is assembled by lane 0
+template <int T>
+__device__ __forceinline__ void boundary_row(const AsmArgs &a, const ClassData<T> &cd, const double *__restrict__ flux,
+                                             const unsigned char *__restrict__ bnd, int r, int lane)
+{
+    const int r0 = a.rowptr[r], r1 = a.rowptr[r + 1];
+    if (bnd[r]) {
+        for (int q = r0 + lane; q < r1; q += 32) a.val[q] = (a.col[q] == r) ? 1.0 : 0.0;
+        if (a.b && lane == 0) a.b[r] = 0.0;
+        return;
+    }
+    if (lane == 0) boundary_row_general<T>(a, cd, flux, r, r0, r1);
+}
+
+// the rows of a list (the box surface), one warp per row
+template <int T>
+__global__ void __launch_bounds__(256) k_assemble_boundary_rows(AsmArgs a, ClassData<T> cd,
+                                                                const double *__restrict__ flux,
+                                                                const unsigned char *__restrict__ bnd,
+                                                                const int *__restrict__ brows, int nbrows)
+{
+    const int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (t >= nbrows) return;
+    boundary_row<T>(a, cd, flux, bnd, brows[t], threadIdx.x & 31);
+}
+
+// One coefficient K for all elements and no convection: every interior row
+// holds the same stencil.  One block per grid line (fixed j, k) of the
+// level, whose rows (and values) are contiguous in the CRS.  On a line
+// inside the box, thread 0 gathers the stencil of the interior row (1, 1, 1)
+// with the arithmetic of k_assemble_rows (so the values are the same) while
+// the other threads write the right-hand side and warps 0 and 1 the line's
+// two end rows on the boundary; then the block writes the interior values
+// with consecutive threads on consecutive values.  A line on the box surface
+// consists of boundary rows, one warp per row.  The memory a block writes is
+// one contiguous range, also for the boundary rows.
+template <int T>
+__global__ void __launch_bounds__(128) k_assemble_lines_uniform(AsmArgs a, ClassData<T> cd, double volsum,
+                                                                const unsigned char *__restrict__ bnd)
+{
+    using S = Stencil<T>;
+    __shared__ double st[S::N];
+    const int nx = a.cx + 1, ny = a.cy + 1, nz = (S::DIM == 3) ? a.cz + 1 : 1;
+    const int j = (int)(blockIdx.x % (unsigned)ny), k = (int)(blockIdx.x / (unsigned)ny);
+    const int rl = nx * (j + ny * k);   // row of (0, j, k)
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    if (j == 0 || j == ny - 1 || (S::DIM == 3 && (k == 0 || k == nz - 1))) {
+        for (int i = warp; i < nx; i += nwarps) boundary_row<T>(a, cd, nullptr, bnd, rl + i, lane);
+        return;
+    }
+    const int nix = a.cx - 1;
+    if (threadIdx.x == 0) {
+        double acc[S::N];
+#pragma unroll
+        for (int s = 0; s < S::N; ++s) acc[s] = 0.0;
+        gather_row<T>(cd, a, 1, 1, (S::DIM == 3) ? 1 : 0, nullptr, [&](int s, double v) { acc[s] += v; },
+                      [](double) {});
+#pragma unroll
+        for (int s = 0; s < S::N; ++s) st[s] = acc[s];
+    } else if (warp == 1) {
+        boundary_row<T>(a, cd, nullptr, bnd, rl, lane);
+    } else if (warp == 2) {
+        boundary_row<T>(a, cd, nullptr, bnd, rl + nx - 1, lane);
+    }
+    const int r0 = rl + 1;
+    if (a.b)
+        for (int i = threadIdx.x; i < nix; i += blockDim.x) a.b[r0 + i] = source_at(a, r0 + i) * volsum;
+    __syncthreads();
+    double *line = a.val + __ldg(a.rowptr + r0);
+    const int len = S::N * nix;
+    for (int q = threadIdx.x; q < len; q += blockDim.x) line[q] = st[q % S::N];
 }
 
 }  // namespace
@@ -496,24 +524,30 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
             if constexpr (E::DIM == 3) {
                 const int ncell = a.cx * a.cy * a.cz;
                 const size_t nf = (size_t)ncell * CT::NC * E::NSCVF;
-                if (cache.flux.n < nf) cache.flux.alloc(nf);
-                VelField vf{a.vmodes, a.vk, a.vc, a.vphase, a.vscale};
-                UG_LAUNCH(c, k_scvf_flux<T>, div_up(ncell * CT::NC, 128), 128, 0, a.cx, a.cy, ncell,
-                          1.0 / (double)a.cx, 1.0 / (double)a.cy, 1.0 / (double)a.cz, cache.normal.p,
-                          cache.ipoff.p, vf, cache.flux.p);
+                // the fluxes depend on the velocity field and the geometry
+                // only: computed again when the field changed
+                if (cache.flux.n < nf || cache.flux_version != a.vel_version) {
+                    if (cache.flux.n < nf) cache.flux.alloc(nf);
+                    VelField vf{a.vmodes, a.vk, a.vc, a.vphase, a.vscale};
+                    UG_LAUNCH(c, k_scvf_flux<T>, div_up(ncell * CT::NC, 128), 128, 0, a.cx, a.cy, ncell,
+                              1.0 / (double)a.cx, 1.0 / (double)a.cy, 1.0 / (double)a.cz, cache.normal.p,
+                              cache.ipoff.p, vf, cache.flux.p);
+                    cache.flux_version = a.vel_version;
+                }
                 flux = cache.flux.p;
             } else {
                 return;   // no 2D velocity field
             }
         }
         if (a.k_uniform && !flux) {
-            const int nlines = (cy - 1) * ((L.dim == 3) ? cz - 1 : 1);
-            UG_LAUNCH(c, k_assemble_rows_uniform<T>, nlines, 128, 0, a, cd, cache.volsum);
+            // every grid line, the boundary rows with it
+            const int nlines = L.ny * ((L.dim == 3) ? L.nz : 1);
+            UG_LAUNCH(c, k_assemble_lines_uniform<T>, nlines, 128, 0, a, cd, cache.volsum, L.bnd.p);
         } else {
             UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux, cache.volsum);
+            UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 8), 256, 0, a, cd, flux, L.bnd.p,
+                      cache.brows.p, cache.nbrows);
         }
-        UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 8), 256, 0, a, cd, flux, L.bnd.p,
-                  cache.brows.p, cache.nbrows);
         done = true;
     };
     switch (L.elem_type) {
