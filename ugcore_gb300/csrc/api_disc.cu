@@ -277,6 +277,7 @@ int ug4gb_disc_set_source_uniform(ug4gb_disc *d, uint64_t seed)
 
 int ug4gb_disc_assemble_linear(ug4gb_disc *d, int level, ug4gb_matrix *A, ug4gb_vector *b)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:disc_assemble_linear");
     if (!d || !A || !b || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
     if (b->n != d->g->lev[level].nv) {
         d->ctx->c.err = "assemble_linear: rhs size mismatch";
@@ -290,6 +291,7 @@ int ug4gb_disc_assemble_linear(ug4gb_disc *d, int level, ug4gb_matrix *A, ug4gb_
 
 int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matrix *A)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:disc_assemble_jacobian");
     if (!d || !A || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
     return guarded(d->ctx, [&] {
         disc_assemble(d, level, A, nullptr, nullptr);
@@ -299,6 +301,7 @@ int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matrix *A)
 
 int ug4gb_disc_assemble_defect(ug4gb_disc *d, int level, const ug4gb_vector *u, ug4gb_vector *dvec)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:disc_assemble_defect");
     if (!d || !u || !dvec || u == dvec || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
     const int nv = d->g->lev[level].nv;
     if (u->n != nv || dvec->n != nv) {
@@ -368,6 +371,7 @@ int ug4gb_timedisc_future_time(const ug4gb_timedisc *td, double *t)
 
 int ug4gb_timedisc_assemble_linear(ug4gb_timedisc *td, int level, ug4gb_matrix *A, ug4gb_vector *b)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:timedisc_assemble_linear");
     if (!td || !A || !b) return UG4GB_ERR_INVALID;
     ug4gb_disc *d = td->disc;
     if (level != (int)d->g->lev.size() - 1 || b->n != d->g->lev[level].nv) {
@@ -387,6 +391,7 @@ int ug4gb_timedisc_assemble_linear(ug4gb_timedisc *td, int level, ug4gb_matrix *
 
 int ug4gb_timedisc_assemble_jacobian(ug4gb_timedisc *td, int level, ug4gb_matrix *A)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:timedisc_assemble_jacobian");
     if (!td || !A || level < 0 || level >= (int)td->disc->g->lev.size()) return UG4GB_ERR_INVALID;
     if (!td->prepared) {
         td->ctx->c.err = "time-discrete assemble_jacobian: prepare_step not called";
@@ -401,6 +406,7 @@ int ug4gb_timedisc_assemble_jacobian(ug4gb_timedisc *td, int level, ug4gb_matrix
 
 int ug4gb_timedisc_assemble_defect(ug4gb_timedisc *td, int level, const ug4gb_vector *u, ug4gb_vector *dvec)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:timedisc_assemble_defect");
     if (!td || !u || !dvec || u == dvec) return UG4GB_ERR_INVALID;
     ug4gb_disc *d = td->disc;
     if (level != (int)d->g->lev.size() - 1 || u->n != d->g->lev[level].nv || dvec->n != u->n) {
@@ -429,6 +435,7 @@ void ug4gb_timedisc_destroy(ug4gb_timedisc *td)
 
 int ug4gb_disc_adjoint_operator(ug4gb_disc *d, int level, const ug4gb_matrix *A, ug4gb_matrix *AT)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:disc_adjoint_operator");
     if (!d || !A || !AT || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
     if (A->A.nrows != d->g->lev[level].nv) return UG4GB_ERR_INVALID;
     if (A == AT) {
@@ -488,6 +495,7 @@ void ug4gb_disc_destroy(ug4gb_disc *d)
 
 int ug4gb_disc_grad_logk(ug4gb_disc *d, const ug4gb_vector *u, const ug4gb_vector *lam, double *grad)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:disc_grad_logk");
     if (!d || !u || !lam || !grad) return UG4GB_ERR_INVALID;
     const Level &L = d->g->lev.back();
     if (u->n != L.nv || lam->n != L.nv) return UG4GB_ERR_INVALID;
@@ -508,6 +516,7 @@ int ug4gb_disc_grad_logk(ug4gb_disc *d, const ug4gb_vector *u, const ug4gb_vecto
 
 int ug4gb_disc_grad_source(ug4gb_disc *d, const ug4gb_vector *lam, double *grad)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:disc_grad_source");
     if (!d || !lam || !grad) return UG4GB_ERR_INVALID;
     const Level &L = d->g->lev.back();
     if (lam->n != L.nv) return UG4GB_ERR_INVALID;

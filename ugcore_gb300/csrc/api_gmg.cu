@@ -815,6 +815,7 @@ int ug4gb_gmg_set_transposed(ug4gb_gmg *m, int transposed)
 
 int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:gmg_init");
     if (!m || !A_top) return UG4GB_ERR_INVALID;
     // what the cycle's launch sequence depends on besides the buffers
     const uint64_t settings = ((uint64_t)(m->cycle + 8) << 40) ^ ((uint64_t)m->nu1 << 20) ^ (uint64_t)m->nu2;
@@ -853,6 +854,7 @@ int ug4gb_gmg_init(ug4gb_gmg *m, const ug4gb_matrix *A_top)
 
 int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:gmg_apply");
     if (!m || !cvec || !d) return UG4GB_ERR_INVALID;
     if (!m->impl) {
         m->ctx->c.err = "ug4gb_gmg_apply: init() not called";

@@ -284,6 +284,7 @@ int ug4gb_newton_prepare(ug4gb_newton *nw, ug4gb_vector *u)
 
 int ug4gb_newton_apply(ug4gb_newton *nw, ug4gb_vector *u)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:newton_apply");
     if (!nw || !u) return UG4GB_ERR_INVALID;
     if (!nw->lin || (!nw->disc && !nw->td)) {
         if (nw) nw->ctx->c.err = "NewtonSolver::apply: linear solver or operator not set";

@@ -315,6 +315,7 @@ int ug4gb_solver_set_min_orthogonality(ug4gb_solver *s, double min_ortho)
 
 int ug4gb_solver_init(ug4gb_solver *s, const ug4gb_matrix *A)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:solver_init");
     if (!s || !A || A->A.nrows != A->A.ncols) return UG4GB_ERR_INVALID;
     return guarded(s->ctx, [&] {
         ug4gb_matrix *Am = const_cast<ug4gb_matrix *>(A);
@@ -342,12 +343,14 @@ int ug4gb_solver_init(ug4gb_solver *s, const ug4gb_matrix *A)
 
 int ug4gb_solver_apply_return_defect(ug4gb_solver *s, ug4gb_vector *x, ug4gb_vector *b)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:solver_apply_return_defect");
     if (!s || !x || !b || x->n != s->n || b->n != s->n) return UG4GB_ERR_INVALID;
     return guarded(s->ctx, [&] { run(s, x->d, b->d); });
 }
 
 int ug4gb_solver_apply(ug4gb_solver *s, ug4gb_vector *x, const ug4gb_vector *b)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:solver_apply");
     if (!s || !x || !b || x->n != s->n || b->n != s->n) return UG4GB_ERR_INVALID;
     return guarded(s->ctx, [&] {
         UG_CUDA(cudaMemcpyAsync(s->r.p, b->d, sizeof(double) * (size_t)s->n, cudaMemcpyDeviceToDevice,
@@ -358,6 +361,7 @@ int ug4gb_solver_apply(ug4gb_solver *s, ug4gb_vector *x, const ug4gb_vector *b)
 
 int ug4gb_solver_solve_host(ug4gb_solver *s, const double *b_host, double *x_host)
 {
+    ug4gb::NvtxRange nvtx_("ug4gb:solver_solve_host");
     if (!s || !b_host || !x_host) return UG4GB_ERR_INVALID;
     return guarded(s->ctx, [&] {
         Ctx &c = s->ctx->c;

@@ -21,6 +21,8 @@
 #include <utility>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/ug4gb.h"
 
 namespace ug4gb {
@@ -49,6 +51,16 @@ constexpr size_t kGuardBytes = 4096;
 void guard_register(char *base, void *user, size_t user_bytes);
 char *guard_release(void *user) noexcept;
 #endif
+
+// NVTX range around a library call ("ug4gb:<call>"), visible to profilers
+// that record NVTX (ncu --nvtx, Nsight Systems); it costs nothing while no
+// such tool is attached.  Stands in for ugcore's PROFILE_FUNC regions.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Owning device buffer (move-only).
 template <class T>

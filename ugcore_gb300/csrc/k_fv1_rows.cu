@@ -150,13 +150,41 @@ __global__ void k_class_data(const double *coords, const int *elems, double *A, 
     if (!ok) atomicExch(corner_ok, 0);
 }
 
-// ----------------------------------------------------------- SCVF flux ----
-// flux[e * NF + f] = v(ip).n of SCVF f of element e, the ip placed at the
-// cell origin plus the class's offset (VelField::eval, as the element kernel)
+// SCVF fluxes v(ip).n of the convection velocity v = curl of the random
+// vector potential (VelField: v = scale sum_m -sin(phase_m + k_m.x) c_m) at
+// the integration points x = o + d of every element: cell origin o plus the
+// class's offset d.  The phase splits, sin(a + b) = sin a cos b + cos a sin b
+// with a = phase_m + k_m.o per cell and mode and b = k_m.d per class, SCVF
+// and mode, so one sine and cosine per cell and mode serve all SCVFs of the
+// cell (GB300 evaluates FP64 sines on its slow FP64 pipe).  Table per class,
+// SCVF and mode: cos b, sin b and w = c_m.n (the SCVF's area normal n).
+template <int T>
+__global__ void k_flux_table(int nmodes, const double *__restrict__ kv, const double *__restrict__ cv,
+                             const double *__restrict__ normal, const double *__restrict__ ipoff,
+                             double *__restrict__ tab)
+{
+    using CT = ClassTraits<T>;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= CT::NC * CT::NF * nmodes) return;
+    const int m = t % nmodes, pf = t / nmodes;
+    double b = 0.0, w = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        b += kv[3 * m + d] * ipoff[pf * 3 + d];
+        w += cv[3 * m + d] * normal[pf * 3 + d];
+    }
+    double sb, cb;
+    sincos(b, &sb, &cb);
+    tab[3 * t] = cb;
+    tab[3 * t + 1] = sb;
+    tab[3 * t + 2] = w;
+}
+
 template <int T>
 __global__ void __launch_bounds__(128) k_scvf_flux(int cx, int cy, int ncell, double hx, double hy, double hz,
-                                                   const double *__restrict__ normal, const double *__restrict__ ipoff,
-                                                   VelField vf, double *__restrict__ flux)
+                                                   int nmodes, const double *__restrict__ kv,
+                                                   const double *__restrict__ phase, double scale,
+                                                   const double *__restrict__ tab, double *__restrict__ flux)
 {
     using CT = ClassTraits<T>;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -164,17 +192,23 @@ __global__ void __launch_bounds__(128) k_scvf_flux(int cx, int cy, int ncell, do
     const int cell = t / CT::NC, p = t % CT::NC;
     const int i = cell % cx, j = (cell / cx) % cy, k = cell / (cx * cy);
     const double o[3] = {i * hx, j * hy, k * hz};
-#pragma unroll 1
-    for (int f = 0; f < CT::NF; ++f) {
-        double x[3], v[3];
+    double acc[CT::NF];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) x[d] = o[d] + __ldg(ipoff + (p * CT::NF + f) * 3 + d);
-        vf.eval(x, v);
-        double fl = 0.0;
+    for (int f = 0; f < CT::NF; ++f) acc[f] = 0.0;
+    for (int m = 0; m < nmodes; ++m) {
+        const double a = __ldg(phase + m) + __ldg(kv + 3 * m) * o[0] + __ldg(kv + 3 * m + 1) * o[1] +
+                         __ldg(kv + 3 * m + 2) * o[2];
+        double sa, ca;
+        sincos(a, &sa, &ca);
 #pragma unroll
-        for (int d = 0; d < CT::DIM; ++d) fl += __ldg(normal + (p * CT::NF + f) * 3 + d) * v[d];
-        flux[(size_t)t * CT::NF + f] = fl;
+        for (int f = 0; f < CT::NF; ++f) {
+            const double *e = tab + 3 * ((p * CT::NF + f) * nmodes + m);
+            const double s = sa * __ldg(e) + ca * __ldg(e + 1);
+            acc[f] -= s * __ldg(e + 2);
+        }
     }
+#pragma unroll
+    for (int f = 0; f < CT::NF; ++f) flux[(size_t)t * CT::NF + f] = scale * acc[f];
 }
 
 // ------------------------------------------------------------- stencil ----
@@ -528,10 +562,16 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
                 // only: computed again when the field changed
                 if (cache.flux.n < nf || cache.flux_version != a.vel_version) {
                     if (cache.flux.n < nf) cache.flux.alloc(nf);
-                    VelField vf{a.vmodes, a.vk, a.vc, a.vphase, a.vscale};
+                    const int ntab = CT::NC * CT::NF * a.vmodes;
+                    DevBuf<double> tab;
+                    tab.alloc(3 * (size_t)ntab);
+                    UG_LAUNCH(c, k_flux_table<T>, div_up(ntab, 128), 128, 0, a.vmodes, a.vk, a.vc, cache.normal.p,
+                              cache.ipoff.p, tab.p);
                     UG_LAUNCH(c, k_scvf_flux<T>, div_up(ncell * CT::NC, 128), 128, 0, a.cx, a.cy, ncell,
-                              1.0 / (double)a.cx, 1.0 / (double)a.cy, 1.0 / (double)a.cz, cache.normal.p,
-                              cache.ipoff.p, vf, cache.flux.p);
+                              1.0 / (double)a.cx, 1.0 / (double)a.cy, 1.0 / (double)a.cz, a.vmodes, a.vk, a.vphase,
+                              a.vscale, tab.p, cache.flux.p);
+                    // the table is freed on return: its kernel must have read it
+                    UG_CUDA(cudaStreamSynchronize(c.stream));
                     cache.flux_version = a.vel_version;
                 }
                 flux = cache.flux.p;
