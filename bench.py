@@ -15,8 +15,11 @@ are measured as extra fields.
 Under torchrun with N > 1 every rank solves its own replica on its own GPU
 ("replicas only": the path has no data exchange at one GPU per problem);
 value = N * DoFs / max-over-ranks time per step.  --impl reference times the
-CPU oracle port of the reference algebra (oracle/, single-threaded like
-ugcore's hot path) on the same workload, rank 0 only.
+CPU oracle port of the reference algebra (oracle/; serial like ugcore's hot
+path) on the same workload, one independent replica per host core, rank 0
+only.  The `roofline` object gives the top-level FP64 smoother's fraction of
+the measured HBM copy bandwidth and, in `roofline.fp64`, of the FP64 rate
+measured with cuBLAS DGEMM, the bound that holds for it on GB300.
 """
 import argparse
 import json
@@ -49,6 +52,28 @@ def peaks():
         return p["hbm_gbs"], "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def fp64_peak_tflops():
+    """FP64 throughput measured here: cuBLAS DGEMM 4096^3 (torch.matmul,
+    best of 3, CUDA events) -- the denominator of the FP64-pipe fraction of
+    the FP64 kernels, which GB300's FP64 rate bounds before HBM"""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
 class ClockSampler:
@@ -260,6 +285,7 @@ def run_ours(args, rank, world, local_rank):
     iters = st["steps"]
     top = len(sizes) - 1
     hbm, peak_kind = peaks()
+    fp64_peak = fp64_peak_tflops()
     smooth = [(k, v) for k, v in prof.items() if k.startswith("L%d|" % top) and "k_smooth" in k]
     s_cnt = sum(v[0] for _, v in smooth)
     s_ms = sum(v[1] for _, v in smooth)
@@ -343,7 +369,11 @@ def run_ours(args, rank, world, local_rank):
                      "peak_kind": peak_kind, "traffic": NCU_TRAFFIC_TOP_SMOOTH,
                      "limiter": "FP64 FMA pipe (%.0f%% busy in ncu): 27 FP64 FMAs per row" % (100 * NCU_FP64_PIPE_TOP_SMOOTH),
                      "bytes_per_launch": s_bytes / max(s_cnt, 1), "avg_launch_ms": s_ms / max(s_cnt, 1),
-                     "share_of_solve": s_ms / total_prof_ms if total_prof_ms else None},
+                     "share_of_solve": s_ms / total_prof_ms if total_prof_ms else None,
+                     # the bound that holds: 28 FP64 FMAs per row (27 diagonals + the Jacobi update)
+                     "fp64": {"achieved_tflops": 56.0 * n / (s_ms / max(s_cnt, 1) * 1e-3) / 1e12,
+                              "peak_tflops": fp64_peak, "peak_kind": "measured (cuBLAS DGEMM 4096^3)",
+                              "frac": 56.0 * n / (s_ms / max(s_cnt, 1) * 1e-3) / 1e12 / fp64_peak}},
         "solve_roofline": {"achieved": solve_gbs, "peak": hbm, "unit": "GB/s", "frac": solve_gbs / hbm,
                            "bytes_per_iteration": it_bytes},
         "kernel_profile": profile_summary(prof),

@@ -70,6 +70,7 @@ void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const T
     a.ne = L.ne;
     a.K = K;
     a.k_uniform = (D.coef_kind == COEF_CONST && c.row_assembly == 2) ? 1 : 0;
+    a.k_value = D.K_const;
     a.f = (top && D.f_kind == 1) ? D.f_top.p : nullptr;
     a.f_seed = D.f_seed;
     a.use_seed = (top && D.f_kind == 2) ? 1 : 0;

@@ -31,7 +31,8 @@ struct AsmArgs {
     // with the lumped FV1 mass M_e = diag(|SCV_i|); with b, the rhs of one
     // previous time point: sa0 f_e - sm1 M_e u_old - sa1 A_e u_old + sa1 f_e
     int inst = 0;
-    int k_uniform = 0;        // K holds one value for all elements
+    int k_uniform = 0;        // K holds one value for all elements: k_value
+    double k_value = 0.0;
     double sm0 = 0.0, sa0 = 1.0, sm1 = 0.0, sa1 = 0.0;
     const double *u_old = nullptr;
     // defect assembly (launch_defect): d += per-element defect of u
