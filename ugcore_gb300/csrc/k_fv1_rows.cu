@@ -446,54 +446,31 @@ __global__ void __launch_bounds__(256) k_assemble_boundary_rows(AsmArgs a, Class
 }
 
 // One coefficient K for all elements and no convection: every interior row
-// holds the same stencil.  One block per grid line (fixed j, k) of the
-// level, whose rows (and values) are contiguous in the CRS.  On a line
-// inside the box, thread 0 gathers the stencil of the interior row (1, 1, 1)
-// with the arithmetic of k_assemble_rows (so the values are the same; the
-// coefficient, a.K's value everywhere, comes as a parameter) while the other
-// threads write the right-hand side and warps 1 and 2 the line's two end
-// rows on the boundary; then the block writes the interior values with
+// holds the same stencil.  A block takes kLinesPerBlock consecutive grid lines
+// (fixed j, k) of the level; the rows (and values) of a line are contiguous
+// in the CRS.  Thread 0 first gathers the stencil of the interior row
+// (1, 1, 1) with the arithmetic of k_assemble_rows (so the values are the
+// same; the coefficient, a.K's value everywhere, comes as a parameter).  On a
+// line inside the box, warps 1 and 2 write the line's two end rows on the
+// boundary, all threads the right-hand side and then the interior values,
 // consecutive threads on consecutive values.  A line on the box surface
 // consists of boundary rows: the block sweeps the line's values with
 // consecutive threads (the row of a value from the line's row pointers in
 // shared memory), writing the identity rows of Dirichlet vertices; any other
 // row of the line is assembled by one lane afterwards.  Dynamic shared
 // memory: nx + 1 row pointers.
+constexpr int kLinesPerBlock = 4;
+
 template <int T>
 __global__ void __launch_bounds__(128) k_assemble_lines_uniform(AsmArgs a, ClassData<T> cd, double volsum, double kval,
-                                                                const unsigned char *__restrict__ bnd)
+                                                                const unsigned char *__restrict__ bnd, int nlines)
 {
     using S = Stencil<T>;
     __shared__ double st[S::N];
     extern __shared__ int srp[];
     const int nx = a.cx + 1, ny = a.cy + 1, nz = (S::DIM == 3) ? a.cz + 1 : 1;
-    const int j = (int)(blockIdx.x % (unsigned)ny), k = (int)(blockIdx.x / (unsigned)ny);
-    const int rl = nx * (j + ny * k);   // row of (0, j, k)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    if (j == 0 || j == ny - 1 || (S::DIM == 3 && (k == 0 || k == nz - 1))) {
-        for (int i = threadIdx.x; i <= nx; i += blockDim.x) srp[i] = __ldg(a.rowptr + rl + i);
-        __syncthreads();
-        const int q0 = srp[0], q1 = srp[nx];
-        for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
-            // the row of value q: the last row pointer <= q
-            int lo = 0, hi = nx - 1;
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (srp[mid] <= q) lo = mid; else hi = mid - 1;
-            }
-            const int r = rl + lo;
-            if (bnd[r]) a.val[q] = (__ldg(a.col + q) == r) ? 1.0 : 0.0;
-        }
-        for (int i = threadIdx.x; i < nx; i += blockDim.x)
-            if (a.b && bnd[rl + i]) a.b[rl + i] = 0.0;
-        // rows without the Dirichlet flag (none where the whole boundary is
-        // Dirichlet)
-        for (int i = warp; i < nx; i += nwarps)
-            if (!bnd[rl + i] && lane == 0) boundary_row_general<T>(a, cd, nullptr, rl + i, srp[i], srp[i + 1]);
-        return;
-    }
     const int nix = a.cx - 1;
-    const int r0 = rl + 1;
     if (threadIdx.x == 0) {
         double acc[S::N];
 #pragma unroll
@@ -502,17 +479,45 @@ __global__ void __launch_bounds__(128) k_assemble_lines_uniform(AsmArgs a, Class
                       [](double) {}, kval);
 #pragma unroll
         for (int s = 0; s < S::N; ++s) st[s] = acc[s];
-    } else if (warp == 1) {
-        boundary_row<T>(a, cd, nullptr, bnd, rl, lane);
-    } else if (warp == 2) {
-        boundary_row<T>(a, cd, nullptr, bnd, rl + nx - 1, lane);
     }
-    double *line = a.val + __ldg(a.rowptr + r0);
-    if (a.b)
-        for (int i = threadIdx.x; i < nix; i += blockDim.x) a.b[r0 + i] = source_at(a, r0 + i) * volsum;
     __syncthreads();
-    const int len = S::N * nix;
-    for (int q = threadIdx.x; q < len; q += blockDim.x) line[q] = st[q % S::N];
+    for (int ln = 0; ln < kLinesPerBlock; ++ln) {
+        const int line_id = blockIdx.x * kLinesPerBlock + ln;
+        if (line_id >= nlines) return;
+        const int j = line_id % ny, k = line_id / ny;
+        const int rl = nx * (j + ny * k);   // row of (0, j, k)
+        if (j == 0 || j == ny - 1 || (S::DIM == 3 && (k == 0 || k == nz - 1))) {
+            __syncthreads();   // srp of the previous surface line is read
+            for (int i = threadIdx.x; i <= nx; i += blockDim.x) srp[i] = __ldg(a.rowptr + rl + i);
+            __syncthreads();
+            const int q0 = srp[0], q1 = srp[nx];
+            for (int q = q0 + threadIdx.x; q < q1; q += blockDim.x) {
+                // the row of value q: the last row pointer <= q
+                int lo = 0, hi = nx - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (srp[mid] <= q) lo = mid; else hi = mid - 1;
+                }
+                const int r = rl + lo;
+                if (bnd[r]) a.val[q] = (__ldg(a.col + q) == r) ? 1.0 : 0.0;
+            }
+            for (int i = threadIdx.x; i < nx; i += blockDim.x)
+                if (a.b && bnd[rl + i]) a.b[rl + i] = 0.0;
+            // rows without the Dirichlet flag (none where the whole boundary
+            // is Dirichlet)
+            for (int i = warp; i < nx; i += nwarps)
+                if (!bnd[rl + i] && lane == 0) boundary_row_general<T>(a, cd, nullptr, rl + i, srp[i], srp[i + 1]);
+            continue;
+        }
+        const int r0 = rl + 1;
+        if (warp == 1) boundary_row<T>(a, cd, nullptr, bnd, rl, lane);
+        else if (warp == 2) boundary_row<T>(a, cd, nullptr, bnd, rl + nx - 1, lane);
+        double *line = a.val + __ldg(a.rowptr + r0);
+        if (a.b)
+            for (int i = threadIdx.x; i < nix; i += blockDim.x) a.b[r0 + i] = source_at(a, r0 + i) * volsum;
+        const int len = S::N * nix;
+        for (int q = threadIdx.x; q < len; q += blockDim.x) line[q] = st[q % S::N];
+    }
 }
 
 }  // namespace
@@ -609,8 +614,8 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
         if (a.k_uniform && !flux && line_smem <= 32 * 1024) {
             // every grid line, the boundary rows with it
             const int nlines = L.ny * ((L.dim == 3) ? L.nz : 1);
-            UG_LAUNCH(c, k_assemble_lines_uniform<T>, nlines, 128, line_smem, a, cd, cache.volsum, a.k_value,
-                      L.bnd.p);
+            UG_LAUNCH(c, k_assemble_lines_uniform<T>, div_up(nlines, kLinesPerBlock), 128, line_smem, a, cd,
+                      cache.volsum, a.k_value, L.bnd.p, nlines);
         } else {
             UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux, cache.volsum);
             UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 8), 256, 0, a, cd, flux, L.bnd.p,
