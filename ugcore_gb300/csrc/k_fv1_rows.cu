@@ -447,7 +447,8 @@ __global__ void __launch_bounds__(256) k_assemble_boundary_rows(AsmArgs a, Class
 
 // One coefficient K for all elements and no convection: every interior row
 // holds the same stencil.  A block takes kLinesPerBlock consecutive grid lines
-// (fixed j, k) of the level; the rows (and values) of a line are contiguous
+// (fixed j, k) of the level (one: more lines per block serialise their
+// latencies and were slower); the rows (and values) of a line are contiguous
 // in the CRS.  Thread 0 first gathers the stencil of the interior row
 // (1, 1, 1) with the arithmetic of k_assemble_rows (so the values are the
 // same; the coefficient, a.K's value everywhere, comes as a parameter).  On a
@@ -459,7 +460,7 @@ __global__ void __launch_bounds__(256) k_assemble_boundary_rows(AsmArgs a, Class
 // shared memory), writing the identity rows of Dirichlet vertices; any other
 // row of the line is assembled by one lane afterwards.  Dynamic shared
 // memory: nx + 1 row pointers.
-constexpr int kLinesPerBlock = 4;
+constexpr int kLinesPerBlock = 1;
 
 template <int T>
 __global__ void __launch_bounds__(128) k_assemble_lines_uniform(AsmArgs a, ClassData<T> cd, double volsum, double kval,
@@ -481,10 +482,31 @@ __global__ void __launch_bounds__(128) k_assemble_lines_uniform(AsmArgs a, Class
         for (int s = 0; s < S::N; ++s) st[s] = acc[s];
     }
     __syncthreads();
+    // the lines on the box surface come first (they take longer: started
+    // first, they overlap the stream of interior lines instead of trailing
+    // it), then the interior lines
+    const int nsurf = (S::DIM == 3) ? 2 * ny + 2 * (nz - 2) : 2;
     for (int ln = 0; ln < kLinesPerBlock; ++ln) {
         const int line_id = blockIdx.x * kLinesPerBlock + ln;
         if (line_id >= nlines) return;
-        const int j = line_id % ny, k = line_id / ny;
+        int j, k;
+        if (line_id < nsurf) {
+            if (S::DIM != 3) {
+                j = line_id == 0 ? 0 : ny - 1;
+                k = 0;
+            } else if (line_id < 2 * ny) {
+                j = line_id % ny;
+                k = line_id < ny ? 0 : nz - 1;
+            } else {
+                const int t = line_id - 2 * ny;
+                j = (t & 1) ? ny - 1 : 0;
+                k = 1 + (t >> 1);
+            }
+        } else {
+            const int t = line_id - nsurf, ni = ny - 2;
+            j = 1 + t % ni;
+            k = (S::DIM == 3) ? 1 + t / ni : 0;
+        }
         const int rl = nx * (j + ny * k);   // row of (0, j, k)
         if (j == 0 || j == ny - 1 || (S::DIM == 3 && (k == 0 || k == nz - 1))) {
             __syncthreads();   // srp of the previous surface line is read
