@@ -246,9 +246,13 @@ int ug4gb_grid_create_structured(ug4gb_ctx *ctx, int elem_type, int mx, int my, 
         UG_REQUIRE(mx >= 1 && my >= 1 && (elem_type == UG4GB_QUAD || mz >= 1), UG4GB_ERR_INVALID,
                    "grid: coarse cell counts must be >= 1");
         UG_REQUIRE(nref >= 0 && nref <= 12, UG4GB_ERR_INVALID, "grid: refinement count out of range");
-        double nv = (double)(mx * (1 << nref) + 1) * (my * (1 << nref) + 1) *
-                    (elem_type == UG4GB_QUAD ? 1.0 : (double)(mz * (1 << nref) + 1));
+        const double fr = (double)(1 << nref);
+        double nv = ((double)mx * fr + 1) * ((double)my * fr + 1) * (elem_type == UG4GB_QUAD ? 1.0 : (double)mz * fr + 1);
         UG_REQUIRE(nv < 2.0e9, UG4GB_ERR_INVALID, "grid: too many vertices for 32-bit indices");
+        // element corner lists are indexed with 32 bits: ne * corners < 2^31
+        const double cells = (double)mx * fr * ((double)my * fr) * (elem_type == UG4GB_QUAD ? 1.0 : (double)mz * fr);
+        const double corners = cells * (elem_type == UG4GB_TET ? 6.0 * 4.0 : (elem_type == UG4GB_HEX ? 8.0 : 4.0));
+        UG_REQUIRE(corners < 2147483648.0, UG4GB_ERR_INVALID, "grid: too many element corners for 32-bit indices");
         g->ctx = ctx;
         g->elem_type = elem_type;
         g->lev.resize(nref + 1);
