@@ -246,4 +246,34 @@ wait
 $CXX $GFLAGS -c "$OUT/lib_grid_standin.cpp" -o "$OUT/obj/lib_grid_standin.o"
 $CXX $GFLAGS "$HERE/ref_fv1geom.cpp" $GOBJS "$OUT/obj/lib_grid_standin.o" $OBJS "$OUT/obj/crc32_stub.o" \
     -o "$OUT/ref_fv1geom"
-echo "build_ref: built $OUT/ref_driver $OUT/ref_io $OUT/ref_fv1geom"
+# ugcore's NewtonSolver and StandardLineSearch (lib_disc headers) over the
+# oracle's assembly: the Boost headers lib_disc names are replaced by the
+# stand-in tests/standins/boost/ug_boost_standin.hpp (the same as the bridge
+# compile test's), the string stand-ins above, and ugcore's own
+# registry/class_name_provider.cpp for the class-name statics.
+NSHIM="$OUT/shim_newton"
+for h in boost/mpl/at.hpp boost/mpl/empty.hpp boost/mpl/fold.hpp boost/mpl/for_each.hpp boost/mpl/front.hpp \
+         boost/mpl/if.hpp boost/mpl/list.hpp boost/mpl/map.hpp boost/mpl/min_max.hpp boost/mpl/pop_front.hpp \
+         boost/mpl/size.hpp boost/mpl/transform_view.hpp boost/optional.hpp boost/serialization/access.hpp \
+         boost/serialization/export.hpp boost/serialization/level.hpp boost/serialization/nvp.hpp \
+         boost/serialization/version.hpp; do
+    mkdir -p "$NSHIM/$(dirname "$h")"
+    echo '#include "boost/ug_boost_standin.hpp"' > "$NSHIM/$h"
+done
+mkdir -p "$NSHIM/boost/algorithm"
+cp "$OUT/shim/boost/algorithm/string.hpp" "$NSHIM/boost/algorithm/string.hpp"
+cp "$OUT/shim/boost/lexical_cast.hpp" "$NSHIM/boost/lexical_cast.hpp"
+NFLAGS="-std=c++17 -O2 -DNDEBUG -w -DUG_DIM_3 -I$NSHIM -I$HERE/../tests/standins -I$REF/ugbase -I$HERE"
+if [ ! -f "$OUT/obj/n_class_name_provider.o" ]; then
+    $CXX $NFLAGS -c "$REF/ugbase/registry/class_name_provider.cpp" -o "$OUT/obj/n_class_name_provider.o"
+fi
+stale=0
+for d in "$HERE/ref_newton.cpp" "$HERE"/ug4_oracle*.c "$HERE/ug4_oracle.h"; do
+    if [ ! -f "$OUT/ref_newton" ] || [ "$d" -nt "$OUT/ref_newton" ]; then stale=1; fi
+done
+if [ "$stale" = 1 ]; then
+    $CXX $NFLAGS "$HERE/ref_newton.cpp" "$OUT/obj/n_class_name_provider.o" $OBJS "$OUT/obj/crc32_stub.o" \
+        "$OUT/obj/ug4_oracle_grid.o" "$OUT/obj/ug4_oracle_fv1.o" "$OUT/obj/ug4_oracle_solve.o" \
+        "$OUT/obj/ug4_oracle_api.o" -o "$OUT/ref_newton" -lm
+fi
+echo "build_ref: built $OUT/ref_driver $OUT/ref_io $OUT/ref_fv1geom $OUT/ref_newton"

@@ -229,4 +229,42 @@ int orc_problem_coefficients(const orc_problem *P, const orc_hier *H, double **K
 #ifdef __cplusplus
 }
 #endif
+
+/* ------------------------------------------------------------ problems -- */
+/* Parameters of one assemble-and-solve problem (oracle.py Params mirrors
+   this layout). */
+typedef struct {
+    int elem_type, mx, my, mz, nref;
+    uint64_t seed;
+    int coef_kind;      /* 0: K=1, 1: exp(2g) field, 2: exp(m) given, 3: constant `diffusion` */
+    int coef_modes;
+    double coef_kmax;
+    int vel_kind;       /* 0: none, 1: curl of a random vector potential */
+    int vel_modes;
+    double vel_kmax, diffusion, peclet;
+    int solver;         /* 0: CG, 1: BiCGStab */
+    int smoother;       /* 0: Jacobi, 1: multicolour GS */
+    double damp;
+    int nu1, nu2, cycle, base;
+    int maxit;
+    double rel_red, min_defect;
+    int rap;            /* 1: Galerkin coarse operators R A P instead of re-assembly */
+    int bicg_restart;   /* BiCGStab::set_restart (0: off) */
+    double bicg_min_ortho; /* BiCGStab::set_min_orthogonality */
+    double damp_prol, damp_res; /* StdTransfer damping (both 1 = none) */
+    int post_smoother;  /* set_postsmoother: -1 = the pre-smoother */
+    double post_damp;
+    int base_steps;     /* set_base_solver: 0 = dense LU, k > 0 = k pre-smoother steps */
+} orc_params;
+typedef struct orc_prob orc_prob;
+orc_prob *orc_prob_create(const orc_params *p, const double *m_top, const double *f_top);
+int orc_prob_num_levels(const orc_prob *P);
+int orc_prob_level_nv(const orc_prob *P, int l);
+int orc_prob_level_ne(const orc_prob *P, int l);
+void orc_prob_level_elems(const orc_prob *P, int l, int *elems, double *coords, unsigned char *bnd);
+int orc_prob_defect(const orc_prob *P, double theta, double dt, const double *u_old, const double *u, double *d);
+int orc_prob_newton_gmg(orc_prob *P, double theta, double dt, orc_gmg *G, orc_crs *J);
+void orc_prob_newton_gmg_free(orc_prob *P, orc_gmg *G, orc_crs *J);
+void orc_prob_free(orc_prob *P);
+
 #endif

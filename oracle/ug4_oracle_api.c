@@ -20,31 +20,9 @@
 
 int orc_grad_logk(const orc_level *L, const double *K, const double *u, const double *lam, double *g);
 
-typedef struct {
-    int elem_type, mx, my, mz, nref;
-    uint64_t seed;
-    int coef_kind;      /* 0: K=1, 1: exp(2g) field, 2: exp(m) given, 3: constant `diffusion` */
-    int coef_modes;
-    double coef_kmax;
-    int vel_kind;       /* 0: none, 1: curl of a random vector potential */
-    int vel_modes;
-    double vel_kmax, diffusion, peclet;
-    int solver;         /* 0: CG, 1: BiCGStab */
-    int smoother;       /* 0: Jacobi, 1: multicolour GS */
-    double damp;
-    int nu1, nu2, cycle, base;
-    int maxit;
-    double rel_red, min_defect;
-    int rap;            /* 1: Galerkin coarse operators R A P instead of re-assembly */
-    int bicg_restart;   /* BiCGStab::set_restart (0: off) */
-    double bicg_min_ortho; /* BiCGStab::set_min_orthogonality */
-    double damp_prol, damp_res; /* StdTransfer damping (both 1 = none) */
-    int post_smoother;  /* set_postsmoother: -1 = the pre-smoother */
-    double post_damp;
-    int base_steps;     /* set_base_solver: 0 = dense LU, k > 0 = k pre-smoother steps */
-} orc_params;
+/* orc_params: ug4_oracle.h */
 
-typedef struct {
+struct orc_prob {
     orc_params p;
     orc_hier H;
     double **K;          /* per level per element */
@@ -58,7 +36,7 @@ typedef struct {
     orc_crs *AT;         /* transposed level operators (adjoint) */
     orc_gmg GT;
     int gmgT_ready;
-} orc_prob;
+};
 
 static int assemble_all(orc_prob *P)
 {
@@ -425,6 +403,34 @@ static int line_search(orc_prob *P, double theta, double dt, const double *u_old
     return 0;
 }
 
+/* The linear solver's multigrid for a Newton step: the jacobian of every
+   level (stationary, theta < 0, or the theta step's M + theta dt A; the FV1
+   operator is linear, so it does not depend on u) and the problem's GMG on
+   them.  J: nlev matrices, owned by the caller (orc_prob_newton_gmg_free). */
+int orc_prob_newton_gmg(orc_prob *P, double theta, double dt, orc_gmg *G, orc_crs *J)
+{
+    const int nl = P->H.nlev;
+    for (int l = 0; l < nl; ++l) {
+        orc_crs_free(&J[l]);
+        orc_disc D;
+        prob_disc(P, l, &D);
+        D.f = NULL;
+        if (theta >= 0.0) {
+            D.inst = 1;
+            D.sm0 = 1.0; D.sa0 = theta * dt; D.sm1 = 0.0; D.sa1 = 0.0;
+        }
+        if (orc_assemble(&P->H.lev[l], &D, &J[l], NULL)) return -1;
+    }
+    memset(G, 0, sizeof(*G));
+    return gmg_init_p(G, P, J) ? -2 : 0;
+}
+
+void orc_prob_newton_gmg_free(orc_prob *P, orc_gmg *G, orc_crs *J)
+{
+    orc_gmg_free(G);
+    for (int l = 0; l < P->H.nlev; ++l) orc_crs_free(&J[l]);
+}
+
 /* NewtonSolver::apply (newton_impl.h:171-340) with the problem's
    GMG-preconditioned Krylov solver as the linear solver (its own convergence
    parameters) on the stationary operator (theta < 0) or the theta step from
@@ -457,21 +463,10 @@ int orc_prob_newton_ls(orc_prob *P, double theta, double dt, const double *u_old
     while (!orc_conv_ended(&NC)) {
         memset(c, 0, sizeof(double) * (size_t)nv);
         /* jacobian of every level (the linear solver's multigrid is set up with it) */
-        for (int l = 0; l < nl; ++l) {
-            orc_crs_free(&J[l]);
-            orc_disc D;
-            prob_disc(P, l, &D);
-            D.f = NULL;
-            if (theta >= 0.0) {
-                D.inst = 1;
-                D.sm0 = 1.0; D.sa0 = theta * dt; D.sm1 = 0.0; D.sa1 = 0.0;
-            }
-            if (orc_assemble(&P->H.lev[l], &D, &J[l], NULL)) return -1;
-        }
         orc_gmg G;
-        memset(&G, 0, sizeof(G));
+        const int grc = orc_prob_newton_gmg(P, theta, dt, &G, J);
+        if (grc) return grc;
         const orc_params *p = &P->p;
-        if (gmg_init_p(&G, P, J)) return -2;
         memcpy(rhs, d, sizeof(double) * (size_t)nv);
         int ls = 0;
         const int lrc = run_solver(p, &J[top], &G, c, rhs, &ls, NULL, NULL, NULL, 0);

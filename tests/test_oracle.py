@@ -371,3 +371,50 @@ def test_backward_and_separate_smoothers_in_the_oracle(oracle_lib):
     P4 = o.Problem(o.make_params(**dict(base, smoother=4)))
     d = np.random.default_rng(0).standard_normal(P1.nv())
     assert not np.array_equal(P1.apply_gmg(d), P4.apply_gmg(d))
+
+
+NEWTON_GOLDEN = ["newton_quad_r4_ls", "newton_hex_r2_ls_accept_best", "newton_tet_lognormal_ls_check_all",
+                 "newton_hex_theta_half", "newton_quad_plain"]
+
+
+@pytest.mark.parametrize("name", NEWTON_GOLDEN)
+def test_newton_matches_ugcore_newton_solver(oracle_lib, name):
+    """The oracle's Newton loop (orc_prob_newton_ls) against ugcore's own
+    NewtonSolver + StandardLineSearch + AssembledOperator + CG + StdConvCheck
+    run on the same assembly and multigrid (tests/golden/make_newton_golden.py,
+    oracle/ref_newton.cpp): the same Newton steps and return, the same
+    accepted lambdas, the same total linear steps, the solution to 1e-12 and
+    the final defect to 1e-9 relative.  Stationary and theta-step operators;
+    plain steps, line searches that accept, that take the best of their
+    tries, and that fail after checking all tries."""
+    from ugcore_gb300 import fields
+    o = oracle_lib
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    (elem, mx, my, mz, nref, seed, coef, diff, theta, dt, maxit, mind, red, ls_max, ls_start, ls_red, ls_best,
+     ls_all, lin_red) = g["args"].tolist()
+    P = o.Problem(o.make_params(elem_type=int(elem), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref),
+                                seed=int(seed), coef_kind=int(coef), diffusion=diff, rel_red=lin_red))
+    nv = len(g["u"])
+    u0 = np.array([0.1 * (2.0 * fields.hash_uniform(int(seed) + 7, i) - 1.0) for i in range(nv)])
+    ls = None
+    if ls_max > 0:
+        ls = dict(max_steps=int(ls_max), lambda_start=ls_start, lambda_reduce=ls_red, accept_best=int(ls_best),
+                  check_all=int(ls_all))
+    out = P.newton(u0, maxit=int(maxit), min_defect=mind, reduction=red,
+                   theta=None if theta < 0 else theta, dt=dt, u_old=None if theta < 0 else np.zeros(nv),
+                   line_search=ls)
+    u, rc, steps, lin, defs = out[:5]
+    assert int(steps) == int(g["steps"])
+    assert (rc == 0) == (int(g["rc"]) == 0)
+    # ugcore counts the linear solve of a step whose line search fails, the
+    # oracle's per-step list stops before that step
+    if rc == 3:
+        assert int(np.sum(lin)) < int(g["linear_steps"])
+    else:
+        assert int(np.sum(lin)) == int(g["linear_steps"])
+    if ls is not None:
+        lams = np.array(out[5][1])
+        assert len(lams) == len(g["lambdas"])
+        assert np.abs(lams - g["lambdas"]).max() <= 1e-9
+    assert np.abs(u - g["u"]).max() <= 1e-12 * max(np.abs(g["u"]).max(), 1e-300)
+    assert abs(defs[-1] - g["d1"]) <= 1e-9 * g["d1"] or (rc != 0 and int(steps) == 0)
