@@ -260,7 +260,10 @@ for h in boost/mpl/at.hpp boost/mpl/empty.hpp boost/mpl/fold.hpp boost/mpl/for_e
     mkdir -p "$NSHIM/$(dirname "$h")"
     echo '#include "boost/ug_boost_standin.hpp"' > "$NSHIM/$h"
 done
-mkdir -p "$NSHIM/boost/algorithm"
+mkdir -p "$NSHIM/boost/algorithm" "$NSHIM/boost/graph"
+# the dense LU's ordering code names these; unused, empty as for the algebra build
+: > "$NSHIM/boost/graph/adjacency_list.hpp"
+: > "$NSHIM/boost/graph/graph_traits.hpp"
 cp "$OUT/shim/boost/algorithm/string.hpp" "$NSHIM/boost/algorithm/string.hpp"
 cp "$OUT/shim/boost/lexical_cast.hpp" "$NSHIM/boost/lexical_cast.hpp"
 NFLAGS="-std=c++17 -O2 -DNDEBUG -w -DUG_DIM_3 -I$NSHIM -I$HERE/../tests/standins -I$REF/ugbase -I$HERE"
@@ -276,4 +279,14 @@ if [ "$stale" = 1 ]; then
         "$OUT/obj/ug4_oracle_grid.o" "$OUT/obj/ug4_oracle_fv1.o" "$OUT/obj/ug4_oracle_solve.o" \
         "$OUT/obj/ug4_oracle_api.o" -o "$OUT/ref_newton" -lm
 fi
-echo "build_ref: built $OUT/ref_driver $OUT/ref_io $OUT/ref_fv1geom $OUT/ref_newton"
+# ugcore's ThetaTimeStep over the oracle's time-dependent assembly
+stale=0
+for d in "$HERE/ref_theta.cpp" "$HERE"/ug4_oracle*.c "$HERE/ug4_oracle.h"; do
+    if [ ! -f "$OUT/ref_theta" ] || [ "$d" -nt "$OUT/ref_theta" ]; then stale=1; fi
+done
+if [ "$stale" = 1 ]; then
+    $CXX $NFLAGS "$HERE/ref_theta.cpp" "$OUT/obj/n_class_name_provider.o" $OBJS "$OUT/obj/crc32_stub.o" \
+        "$OUT/obj/ug4_oracle_grid.o" "$OUT/obj/ug4_oracle_fv1.o" "$OUT/obj/ug4_oracle_solve.o" \
+        "$OUT/obj/ug4_oracle_api.o" -o "$OUT/ref_theta" -lm
+fi
+echo "build_ref: built $OUT/ref_driver $OUT/ref_io $OUT/ref_fv1geom $OUT/ref_newton $OUT/ref_theta"

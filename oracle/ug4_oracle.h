@@ -263,6 +263,12 @@ int orc_prob_level_nv(const orc_prob *P, int l);
 int orc_prob_level_ne(const orc_prob *P, int l);
 void orc_prob_level_elems(const orc_prob *P, int l, int *elems, double *coords, unsigned char *bnd);
 int orc_prob_defect(const orc_prob *P, double theta, double dt, const double *u_old, const double *u, double *d);
+int orc_prob_scaled_defect(const orc_prob *P, double sm0, double sa0, double sm1, double sa1, const double *u_old,
+                           const double *u, double *d);
+int orc_prob_scaled_system(const orc_prob *P, double sm0, double sa0, double sm1, double sa1, const double *u_old,
+                           int *rowptr, int *col, double *val, double *b);
+int64_t orc_prob_level_nnz(const orc_prob *P, int l);
+void orc_prob_level_matrix(const orc_prob *P, int l, int *rowptr, int *col, double *val);
 int orc_prob_newton_gmg(orc_prob *P, double theta, double dt, orc_gmg *G, orc_crs *J);
 void orc_prob_newton_gmg_free(orc_prob *P, orc_gmg *G, orc_crs *J);
 void orc_prob_free(orc_prob *P);

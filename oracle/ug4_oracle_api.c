@@ -240,10 +240,13 @@ int orc_prob_solve(orc_prob *P, double *x, int *steps, double *d0, double *d1, d
 }
 
 /* ---- ThetaTimeStep ------------------------------------------------------ */
-/* the time-discrete operator of level l (M + theta dt A) and, with b, the
-   right-hand side of one step from u_old (top level) */
-static int theta_assemble(const orc_prob *P, int l, double theta, double dt, const double *u_old, orc_crs *A,
-                          double *b)
+/* the time-discrete operator of level l (sm0 M + sa0 A) and, with b, the
+   right-hand side of one step from u_old (top level) for the time scalings
+   vScaleMass = (sm0, sm1), vScaleStiff = (sa0, sa1) a multi-step
+   discretisation passes to the domain discretisation
+   (IDomainDiscretization::assemble_linear, domain_disc_interface.h) */
+static int scaled_assemble(const orc_prob *P, int l, double sm0, double sa0, double sm1, double sa1,
+                           const double *u_old, orc_crs *A, double *b)
 {
     const int top = P->H.nlev - 1;
     orc_disc D;
@@ -254,9 +257,28 @@ static int theta_assemble(const orc_prob *P, int l, double theta, double dt, con
     D.f = (l == top) ? P->f : NULL;
     D.dirichlet = 1;
     D.inst = 1;
-    D.sm0 = 1.0; D.sa0 = theta * dt; D.sm1 = -1.0; D.sa1 = (1.0 - theta) * dt;
+    D.sm0 = sm0; D.sa0 = sa0; D.sm1 = sm1; D.sa1 = sa1;
     D.u_old = u_old;
     return orc_assemble(&P->H.lev[l], &D, A, b);
+}
+
+/* the theta step's scalings (ThetaTimeStep::update_scaling,
+   theta_time_step.h): s_m = (1, -1), s_a = (theta dt, (1 - theta) dt) */
+static int theta_assemble(const orc_prob *P, int l, double theta, double dt, const double *u_old, orc_crs *A,
+                          double *b)
+{
+    return scaled_assemble(P, l, 1.0, theta * dt, -1.0, (1.0 - theta) * dt, u_old, A, b);
+}
+
+int orc_prob_scaled_system(const orc_prob *P, double sm0, double sa0, double sm1, double sa1, const double *u_old,
+                           int *rowptr, int *col, double *val, double *b)
+{
+    orc_crs A;
+    memset(&A, 0, sizeof(A));
+    if (scaled_assemble(P, P->H.nlev - 1, sm0, sa0, sm1, sa1, u_old, &A, b)) return -1;
+    crs_out(&A, rowptr, col, val);
+    orc_crs_free(&A);
+    return 0;
 }
 
 /* top-level time-discrete system of one step (CRS pattern = the level's) */
@@ -336,17 +358,27 @@ static void prob_disc(const orc_prob *P, int l, orc_disc *D)
 /* top-level defect of u: stationary (theta < 0) or of one theta step from
    u_old (ThetaTimeStep::assemble_defect, s_m = (1, -1),
    s_a = (theta dt, (1 - theta) dt)) */
-int orc_prob_defect(const orc_prob *P, double theta, double dt, const double *u_old, const double *u, double *d)
+/* the time-discrete defect of u for the scalings s_m = (sm0, sm1),
+   s_a = (sa0, sa1) from u_old (IDomainDiscretization::assemble_defect) */
+int orc_prob_scaled_defect(const orc_prob *P, double sm0, double sa0, double sm1, double sa1, const double *u_old,
+                           const double *u, double *d)
 {
     const int top = P->H.nlev - 1;
     orc_disc D;
     prob_disc(P, top, &D);
-    if (theta >= 0.0) {
-        if (!u_old) return -1;
-        D.inst = 1;
-        D.sm0 = 1.0; D.sa0 = theta * dt; D.sm1 = -1.0; D.sa1 = (1.0 - theta) * dt;
-        D.u_old = u_old;
-    }
+    if (!u_old) return -1;
+    D.inst = 1;
+    D.sm0 = sm0; D.sa0 = sa0; D.sm1 = sm1; D.sa1 = sa1;
+    D.u_old = u_old;
+    return orc_assemble_defect(&P->H.lev[top], &D, u, d);
+}
+
+int orc_prob_defect(const orc_prob *P, double theta, double dt, const double *u_old, const double *u, double *d)
+{
+    const int top = P->H.nlev - 1;
+    if (theta >= 0.0) return orc_prob_scaled_defect(P, 1.0, theta * dt, -1.0, (1.0 - theta) * dt, u_old, u, d);
+    orc_disc D;
+    prob_disc(P, top, &D);
     return orc_assemble_defect(&P->H.lev[top], &D, u, d);
 }
 

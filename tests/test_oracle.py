@@ -418,3 +418,39 @@ def test_newton_matches_ugcore_newton_solver(oracle_lib, name):
         assert np.abs(lams - g["lambdas"]).max() <= 1e-9
     assert np.abs(u - g["u"]).max() <= 1e-12 * max(np.abs(g["u"]).max(), 1e-300)
     assert abs(defs[-1] - g["d1"]) <= 1e-9 * g["d1"] or (rc != 0 and int(steps) == 0)
+
+
+THETA_GOLDEN = ["theta_quad_cn", "theta_hex_implicit_euler", "theta_tet_lognormal_explicit",
+                "theta_quad_lognormal_0.7"]
+
+
+@pytest.mark.parametrize("name", THETA_GOLDEN)
+def test_theta_step_matches_ugcore_theta_time_step(oracle_lib, name):
+    """The oracle's theta step against ugcore's own ThetaTimeStep
+    (tests/golden/make_theta_golden.py, oracle/ref_theta.cpp): the time
+    scalings ugcore passes to the domain discretisation are the restated
+    ones, s_m = (1, -1), s_a = (theta dt, (1 - theta) dt), bit for bit; for
+    every step of the series (advanced by ugcore's dense LU) the oracle's
+    operator and right-hand side from the same previous solution, the defect
+    of a perturbed iterate and the jacobian M + theta dt A equal what
+    ThetaTimeStep assembled, bit for bit.  Crank-Nicolson, implicit and
+    explicit Euler, theta = 0.7; quadrilaterals, hexahedra, lognormal
+    tetrahedra."""
+    from ugcore_gb300 import fields
+    o = oracle_lib
+    g = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    elem, mx, my, mz, nref, seed, coef, theta, dt, ns = g["args"].tolist()
+    P = o.Problem(o.make_params(elem_type=int(elem), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref),
+                                seed=int(seed), coef_kind=int(coef)))
+    top = P.nlev - 1
+    for s in range(int(ns)):
+        sc = g["scales"][s]
+        assert sc.tolist() == [1.0, theta * dt, -1.0, (1.0 - theta) * dt]
+        u_old = g["u_old"][s]
+        (_, _, va), b = P.theta_system(theta, dt, u_old)
+        assert np.array_equal(va, g["A"][s]) and np.array_equal(b, g["b"][s]), s
+        w = u_old + np.array([0.01 * (2.0 * fields.hash_uniform(int(seed) + 11, i) - 1.0) for i in range(len(u_old))])
+        d = P.defect(w, theta=theta, dt=dt, u_old=u_old)
+        assert np.array_equal(d, g["d"][s]), s
+        _, _, jv = P.theta_jacobian(top, theta, dt)
+        assert np.array_equal(jv, g["J"][s]), s
