@@ -25,22 +25,35 @@ namespace ug4gb {
 void disc_assemble(ug4gb_disc *d, int level, ug4gb_matrix *A, double *b, const TimeScale *ts);
 
 // ------------------------------------------------------------- helpers ---
+// Jacobi factors of a level in FP64 and in the level precision V (one
+// launch: the re-initialisation of small levels is bound by launches)
+template <class V>
 __global__ void k_diag_inv(const int *rowptr, const int *col, const double *val, int n, double damp, int smoother,
-                           double *dinv, double *dfac)
+                           double *dinv, double *dfac, V *dinv_v, V *dfac_v)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double a = 0.0;
     for (int q = rowptr[i]; q < rowptr[i + 1]; ++q)
         if (col[q] == i) a = val[q];
+    double di, df;
     if (smoother == UG4GB_SMOOTHER_JACOBI) {
         // Jacobi::preprocess (jacobi.h:196-208): diagInv = 1 / (a_ii * (1/damp))
         double m = a * (1. / damp);
-        dinv[i] = 1. / m;
-        dfac[i] = m;
+        di = 1. / m;
+        df = m;
     } else {
-        dinv[i] = damp / a;
-        dfac[i] = 1.0;
+        di = damp / a;
+        df = 1.0;
+    }
+    dinv[i] = di;
+    if (dfac) dfac[i] = df;
+    if constexpr (sizeof(V) == 4) {
+        dinv_v[i] = f64_to_f32(di);
+        if (dfac_v) dfac_v[i] = f64_to_f32(df);
+    } else {
+        dinv_v[i] = (V)di;
+        if (dfac_v) dfac_v[i] = (V)df;
     }
 }
 
@@ -228,19 +241,16 @@ struct GmgT : GmgBase {
         L.w.alloc(n);
         L.dinv64.alloc(n);
         L.dfac64.alloc(n);
-        UG_LAUNCH(c, k_diag_inv, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp, smoother,
-                  L.dinv64.p, L.dfac64.p);
         L.dinv.alloc(n);
         L.dfac.alloc(n);
-        UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, L.dinv64.p, L.dinv.p, n);
-        UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, L.dfac64.p, L.dfac.p, n);
+        UG_LAUNCH(c, k_diag_inv<V>, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp, smoother,
+                  L.dinv64.p, L.dfac64.p, L.dinv.p, L.dfac.p);
         // a Gauss-Seidel post-smoother with its own relaxation
         if (smoother2 != UG4GB_SMOOTHER_JACOBI && smoother2 != UG4GB_SMOOTHER_ILU && damp2 != damp) {
             L.dinv2_64.alloc(n);
             L.dinv2.alloc(n);
-            UG_LAUNCH(c, k_diag_inv, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp2, smoother2,
-                      L.dinv2_64.p, L.dfac64.p);
-            UG_LAUNCH(c, k_to_v<V>, div_up(n, 256), 256, 0, L.dinv2_64.p, L.dinv2.p, n);
+            UG_LAUNCH(c, k_diag_inv<V>, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp2,
+                      smoother2, L.dinv2_64.p, (double *)nullptr, L.dinv2.p, (V *)nullptr);
         }
         if (smoother == UG4GB_SMOOTHER_JACOBI) {
             op_from_csr_cached<V>(c, L.A, L.At, L.dinv64.p, c.allow_dia, L.At_lay);

@@ -418,19 +418,46 @@ __device__ __noinline__ void boundary_row_general(const AsmArgs &a, const ClassD
     if (a.b) a.b[r] = vsum;
 }
 
-// one boundary row by the lanes of a warp: a Dirichlet row is the identity
-// row with b = 0, any other row is assembled by lane 0
+// one boundary row by nlanes threads (lane 0..nlanes-1; a warp, or one
+// thread with nlanes = 1): a Dirichlet row is the identity row with b = 0,
+// any other row is assembled by lane 0
 template <int T>
 __device__ __forceinline__ void boundary_row(const AsmArgs &a, const ClassData<T> &cd, const double *__restrict__ flux,
-                                             const unsigned char *__restrict__ bnd, int r, int lane)
+                                             const unsigned char *__restrict__ bnd, int r, int lane, int nlanes = 32)
 {
     const int r0 = a.rowptr[r], r1 = a.rowptr[r + 1];
     if (bnd[r]) {
-        for (int q = r0 + lane; q < r1; q += 32) a.val[q] = (a.col[q] == r) ? 1.0 : 0.0;
+        for (int q = r0 + lane; q < r1; q += nlanes) a.val[q] = (a.col[q] == r) ? 1.0 : 0.0;
         if (a.b && lane == 0) a.b[r] = 0.0;
         return;
     }
     if (lane == 0) boundary_row_general<T>(a, cd, flux, r, r0, r1);
+}
+
+// small levels (launch-bound): every row of the level in one launch, one
+// thread per row, interior rows as k_assemble_rows, boundary rows as
+// k_assemble_boundary_rows
+template <int T>
+__global__ void __launch_bounds__(128) k_assemble_rows_all(AsmArgs a, ClassData<T> cd, const double *__restrict__ flux,
+                                                           double volsum, const unsigned char *__restrict__ bnd)
+{
+    using S = Stencil<T>;
+    const int nx = a.cx + 1, ny = a.cy + 1, nz = (S::DIM == 3) ? a.cz + 1 : 1;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nx * ny * nz) return;
+    const int i = r % nx, j = (r / nx) % ny, k = r / (nx * ny);
+    if (i == 0 || i == nx - 1 || j == 0 || j == ny - 1 || (S::DIM == 3 && (k == 0 || k == nz - 1))) {
+        boundary_row<T>(a, cd, flux, bnd, r, 0, 1);
+        return;
+    }
+    double acc[S::N];
+#pragma unroll
+    for (int s = 0; s < S::N; ++s) acc[s] = 0.0;
+    gather_row<T>(cd, a, i, j, k, flux, [&](int s, double v) { acc[s] += v; }, [](double) {});
+    double *row = a.val + __ldg(a.rowptr + r);
+#pragma unroll
+    for (int s = 0; s < S::N; ++s) row[s] = acc[s];
+    if (a.b) a.b[r] = source_at(a, r) * volsum;
 }
 
 // the rows of a list (the box surface), one warp per row
@@ -544,6 +571,10 @@ __global__ void __launch_bounds__(128) k_assemble_lines_uniform(AsmArgs a, Class
 
 }  // namespace
 
+// levels up to this size are assembled in one launch (k_assemble_rows_all):
+// their assembly is bound by the launches, not by the rows
+constexpr int kSmallLevelRows = 1 << 16;
+
 // Assembles level L row by row when it is a structured level and the
 // assembly is stationary; returns false (nothing launched) otherwise.
 bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCache &cache)
@@ -639,9 +670,13 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
             UG_LAUNCH(c, k_assemble_lines_uniform<T>, div_up(nlines, kLinesPerBlock), 128, line_smem, a, cd,
                       cache.volsum, a.k_value, L.bnd.p, nlines);
         } else {
-            UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux, cache.volsum);
-            UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 8), 256, 0, a, cd, flux, L.bnd.p,
-                      cache.brows.p, cache.nbrows);
+            if (L.nv <= kSmallLevelRows) {
+                UG_LAUNCH(c, k_assemble_rows_all<T>, div_up(L.nv, 128), 128, 0, a, cd, flux, cache.volsum, L.bnd.p);
+            } else {
+                UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux, cache.volsum);
+                UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 8), 256, 0, a, cd, flux, L.bnd.p,
+                          cache.brows.p, cache.nbrows);
+            }
         }
         done = true;
     };
