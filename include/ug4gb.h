@@ -8,7 +8,13 @@
  *     No C++ exception crosses this boundary.
  *   - Array arguments may be host or device pointers (the library detects
  *     which); the caller owns them.  The library owns all device memory of a
- *     handle and frees it in the matching *_destroy.
+ *     handle and frees it in the matching *_destroy.  A host output array is
+ *     complete when the call returns, and a host input array may be reused
+ *     then.  Device arrays are read and written in stream order on the
+ *     context's stream (ug4gb_stream): a device input must stay unchanged,
+ *     and a device output be read, only after that stream has passed the
+ *     call (an event, or ug4gb_synchronize).  Work on the library's own
+ *     objects (matrices, vectors, multigrids) is ordered on that stream.
  *   - One CUDA stream per context; calls on one context are not thread-safe
  *     (ugcore's hot path is single-threaded per process).
  *   - Indices are 0-based 32-bit ints; DoF numbering is lexicographic per

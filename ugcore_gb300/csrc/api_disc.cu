@@ -220,7 +220,9 @@ int ug4gb_disc_set_log_diffusion_elements(ug4gb_disc *d, const double *m_top)
         D.coef_kind = COEF_LOG_ELEMS;
         D.m_top.alloc(ne);
         copy_in(d->ctx->c, D.m_top.p, m_top, sizeof(double) * (size_t)ne);
-        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+        // a device array is read in stream order (the caller keeps it
+        // unchanged until the context's stream has passed this point)
+        if (!is_device_ptr(m_top)) UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
         invalidate(d);
     });
 }
@@ -263,7 +265,7 @@ int ug4gb_disc_set_source_vertices(ug4gb_disc *d, const double *f)
         int nv = d->g->lev.back().nv;
         d->d.f_top.alloc(nv);
         copy_in(d->ctx->c, d->d.f_top.p, f, sizeof(double) * (size_t)nv);
-        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
+        if (!is_device_ptr(f)) UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
         d->d.f_kind = 1;
     });
 }
@@ -284,20 +286,15 @@ int ug4gb_disc_assemble_linear(ug4gb_disc *d, int level, ug4gb_matrix *A, ug4gb_
         d->ctx->c.err = "assemble_linear: rhs size mismatch";
         return UG4GB_ERR_INVALID;
     }
-    return guarded(d->ctx, [&] {
-        disc_assemble(d, level, A, b->d, nullptr);
-        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
-    });
+    // queued on the context's stream (the matrix and rhs are device objects)
+    return guarded(d->ctx, [&] { disc_assemble(d, level, A, b->d, nullptr); });
 }
 
 int ug4gb_disc_assemble_jacobian(ug4gb_disc *d, int level, ug4gb_matrix *A)
 {
     ug4gb::NvtxRange nvtx_("ug4gb:disc_assemble_jacobian");
     if (!d || !A || level < 0 || level >= (int)d->g->lev.size()) return UG4GB_ERR_INVALID;
-    return guarded(d->ctx, [&] {
-        disc_assemble(d, level, A, nullptr, nullptr);
-        UG_CUDA(cudaStreamSynchronize(d->ctx->c.stream));
-    });
+    return guarded(d->ctx, [&] { disc_assemble(d, level, A, nullptr, nullptr); });
 }
 
 int ug4gb_disc_assemble_defect(ug4gb_disc *d, int level, const ug4gb_vector *u, ug4gb_vector *dvec)
@@ -504,8 +501,8 @@ int ug4gb_disc_grad_logk(ug4gb_disc *d, const ug4gb_vector *u, const ug4gb_vecto
         Ctx &c = d->ctx->c;
         const double *K = disc_coefficients(d, (int)d->g->lev.size() - 1);
         if (is_device_ptr(grad)) {
+            // in stream order on the context's stream
             launch_grad_logk(c, L, K, u->d, lam->d, grad);
-            UG_CUDA(cudaStreamSynchronize(c.stream));
         } else {
             DevBuf<double> g;
             g.alloc(L.ne);
