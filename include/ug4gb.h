@@ -127,6 +127,17 @@ UG4GB_API int ug4gb_set_operator_format(ug4gb_ctx *ctx, int format);
    UG4GB_ERR_CUDA ("a kernel's bounded wait ... ran out") and the context
    stays usable.  Never set outside such a test. */
 #define UG4GB_TUNE_SWEEP_WAIT_TEST 5
+/* UG4GB_TUNE_COARSE_LEVELS (-1..7; default -1): the coarse end of a V-cycle
+   (Jacobi smoothers on both sides, dense LU base solver, structured levels
+   with grid transfers) run by one block in one launch: the base level and
+   up to this many levels above it (never the top level), their operators,
+   Jacobi factors and vectors in shared memory.  -1: the levels where this
+   was measured faster on GB300 (a Jacobi sweep of at most about 4000 FP64
+   row-operations, rows x (stencil width + 3), an FP32 one counting a
+   quarter; a base level of at most 32 rows); 0: every level by separate
+   launches.  Corrections are bit-identical either way.  Applies to
+   multigrids set up after the call. */
+#define UG4GB_TUNE_COARSE_LEVELS 6
 UG4GB_API int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value);
 /* per-launch CUDA-event timing of every kernel until profile_end, which
    writes "tag|kernel<TAB>launches<TAB>total_ms" lines into buf.  While it is

@@ -24,6 +24,7 @@ TUNE_SWEEP_FUSION = 2
 TUNE_SWEEP_PLANES = 3
 TUNE_ROW_ASSEMBLY = 4
 TUNE_SWEEP_WAIT_TEST = 5
+TUNE_COARSE_LEVELS = 6
 
 _ERRNAMES = {ERR_INVALID: "invalid argument", ERR_CUDA: "CUDA error", ERR_NOMEM: "out of device memory",
              ERR_SINGULAR: "singular base matrix", ERR_NOT_CONVERGED: "not converged",

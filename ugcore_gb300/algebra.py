@@ -78,7 +78,8 @@ class Context:
         """'auto' (diagonal layout for structured operators) or 'sell'."""
         check(lib().ug4gb_set_operator_format(self.h, {"auto": 0, "sell": 1}[fmt]), self.h)
 
-    def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None, row_assembly=None, sweep_wait_test=None):
+    def set_tuning(self, pdl=None, sweep_fusion=None, sweep_planes=None, row_assembly=None, sweep_wait_test=None,
+                   coarse_levels=None):
         """performance switches:
         pdl: programmatic dependent launch of the solve kernels;
         sweep_fusion: bit mask (1 on, 2 every level size) of the
@@ -89,7 +90,10 @@ class Context:
         from the per-class element geometry (True or 1), in addition from
         the one interior stencil when the coefficient is constant and there
         is no convection (2, the default), or element by element (False or
-        0); the same values to rounding."""
+        0); the same values to rounding;
+        coarse_levels: levels above the base that one launch cycles at the
+        coarse end of a V-cycle (-1 as many as pay, the default; 0 none;
+        bit-identical corrections; multigrids set up afterwards)."""
         if sweep_wait_test is not None:
             # failure test of the fused sweeps' bounded waits only
             check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_SWEEP_WAIT_TEST, int(sweep_wait_test)), self.h)
@@ -101,6 +105,8 @@ class Context:
             check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_SWEEP_FUSION, int(sweep_fusion)), self.h)
         if sweep_planes is not None:
             check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_SWEEP_PLANES, int(sweep_planes)), self.h)
+        if coarse_levels is not None:
+            check(lib().ug4gb_set_tuning(self.h, _lib.TUNE_COARSE_LEVELS, int(coarse_levels)), self.h)
 
     def profile_begin(self):
         check(lib().ug4gb_profile_begin(self.h), self.h)

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libug4gb.so")
 
-SOURCES = ["k_grid.cu", "k_fv1.cu", "k_fv1_rows.cu", "k_solve.cu", "k_sweep2.cu", "k_rap.cu", "api.cu", "api_disc.cu", "api_gmg.cu", "api_solver.cu",
+SOURCES = ["k_grid.cu", "k_fv1.cu", "k_fv1_rows.cu", "k_solve.cu", "k_coarse.cu", "k_sweep2.cu", "k_rap.cu", "api.cu", "api_disc.cu", "api_gmg.cu", "api_solver.cu",
            "api_noalloc.cu", "api_perm.cu", "api_io.cu", "api_newton.cu",
            "grid_unstructured.cu", "grid_refine_device.cu", "k_ilu.cu", "api_algebra.cu", "guard.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -174,6 +174,10 @@ int ug4gb_set_tuning(ug4gb_ctx *ctx, int knob, int value)
         if (value < 0 || value > 4096 || value % 16) return UG4GB_ERR_INVALID;
         ctx->c.sweep_wait_test = value;
         return UG4GB_OK;
+    case UG4GB_TUNE_COARSE_LEVELS:
+        if (value < -1 || value > 7) return UG4GB_ERR_INVALID;
+        ctx->c.coarse_levels = value;
+        return UG4GB_OK;
     case UG4GB_TUNE_ROW_ASSEMBLY:
         if (value < 0 || value > 2) return UG4GB_ERR_INVALID;
         ctx->c.row_assembly = value;

@@ -197,6 +197,12 @@ struct GmgT : GmgBase {
     uint64_t top_key = 0;        // pattern key of the top operator of the last set-up
     int nbase = 0;
     bool top_converted = false;  // this apply: the FP32 top defect is already in dA of the top level
+    // the coarse end of the V-cycle in one launch (k_coarse.cu): levels
+    // base .. coarse_top, or none (coarse_top < 0)
+    int coarse_top = -1;
+    size_t coarse_smem = 0;
+    CoarsePlan<V> coarse_host{};
+    DevBuf<CoarsePlan<V>> coarse_plan;
 
     int top() const override { return (int)lev.size() - 1; }
     bool is_fp32() const override { return sizeof(V) == 4; }
@@ -224,6 +230,9 @@ struct GmgT : GmgBase {
         }
         mix(Ainv.p);
         mix(z64.p);
+        mix(coarse_plan.p);
+        h ^= (uint64_t)(coarse_top + 2);
+        h *= 1099511628211ULL;
         return h;
     }
 
@@ -380,6 +389,91 @@ struct GmgT : GmgBase {
         nbase = n;
     }
 
+    // Which coarse levels the one-block kernel cycles (Ctx::coarse_levels),
+    // and its shared-memory layout (CoarsePlan).  Inside the one block every
+    // phase is a chain of dependent FMAs on one SM; on GB300 an FP64 chain
+    // issues at a small fraction of the FP32 rate, so the block only pays
+    // where a phase is shorter than a separate launch (about 1.5 us).
+    // Measured on GB300 (c0/c3 quads, c1 hexes, c2 Kuhn tets, c4 upwind
+    // hexes): levels whose Jacobi sweep is at most about 4000 FP64 row-
+    // operations, rows x (S + 3), an FP32 one counting a quarter, gain
+    // (9-point 2D levels up to 17^2 in FP64 and 33^2 in FP32: 8-15% of a
+    // solve); a base level of more than 32 rows loses (its dense solve, one
+    // warp per row with a five-step warp sum, is FP64 bound on one SM).
+    void setup_coarse(Ctx &c)
+    {
+        coarse_top = -1;
+        coarse_smem = 0;
+        if (c.coarse_levels == 0 || cycle != 1 || smoother != UG4GB_SMOOTHER_JACOBI ||
+            smoother2 != UG4GB_SMOOTHER_JACOBI || base_kind != UG4GB_BASE_LU)
+            return;
+        constexpr double kSweepWork = 4000.0;
+        constexpr int kBaseRows = 32;
+        constexpr size_t kSmemMax = 216 * 1024;
+        constexpr int kAlign = 16 / (int)sizeof(V);   // elements per 16 bytes
+        auto up = [](size_t v, size_t a) { return (v + a - 1) / a * a; };
+        if (c.coarse_levels < 0 && nbase > kBaseRows) return;
+        CoarsePlan<V> &P = coarse_host;
+        P = CoarsePlan<V>{};
+        P.vbase = (int)up((size_t)(nbase + 1) * nbase * sizeof(double), 16);
+        size_t e = up(2 * (size_t)lev[base].n, kAlign);   // level-precision elements so far
+        P.lev[0].n = lev[base].n;
+        P.lev[0].vofs = 0;
+        int best = -1;
+        size_t best_bytes = 0;
+        const int last = std::min(top() - 1, base + kCoarseMaxLevels - 1);
+        for (int l = base + 1; l <= last; ++l) {
+            const GLevel<V> &L = lev[l];
+            const GridPair &gp = L.gp;
+            if (!L.grid_transfer || L.At.kind != 1 || L.At.nrows != L.n || L.At.ncols != L.n ||
+                gp.nx * gp.ny * gp.nz != L.n || gp.cnx * gp.cny * gp.cnz != lev[l - 1].n ||
+                !coarse_width_ok(L.At.dia.S) || L.At.dia.S != lev[base + 1].At.dia.S)
+                break;
+            const Dia<V> &D = L.At.dia;
+            CoarseLevel<V> &Q = P.lev[l - base];
+            Q.n = L.n;
+            Q.val = D.vals();
+            Q.dinv = L.dinv.p;
+            Q.dfac = L.dfac.p;
+            Q.ncols = D.ncols;
+            Q.ld = D.ld;
+            Q.S = D.S;
+            for (int k = 0; k < D.S; ++k) Q.off[k] = D.off.o[k];
+            Q.gp = gp;
+            Q.aofs = (int)e;
+            e = up(e + (size_t)D.S * D.ld, kAlign);
+            Q.iofs = (int)e;
+            e = up(e + (size_t)L.n, kAlign);
+            Q.fofs = (int)e;
+            e = up(e + (size_t)L.n, kAlign);
+            Q.vofs = (int)e;
+            e = up(e + 4 * (size_t)L.n, kAlign);
+            const size_t bytes = (size_t)P.vbase + e * sizeof(V);
+            if (bytes > kSmemMax) break;
+            if (c.coarse_levels > 0) {
+                if (l - base > c.coarse_levels) break;
+            } else if ((double)L.n * (D.S + 3) * (sizeof(V) == 8 ? 1.0 : 0.25) > kSweepWork) {
+                break;
+            }
+            best = l;
+            best_bytes = bytes;
+        }
+        if (best < 0) return;
+        P.m = best - base + 1;
+        P.nu1 = nu1;
+        P.nu2 = nu2;
+        P.nbase = nbase;
+        P.Ainv = Ainv.p;
+        P.d_in = lev[best].dA.p;
+        P.sc_out = lev[best].sc.p;
+        coarse_smem = best_bytes;
+        coarse_plan.alloc(1);
+        copy_in(c, coarse_plan.p, &P, sizeof(P));
+        coarse_prepare<V>(kSmemMax);   // the most any multigrid asks for
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        coarse_top = best;
+    }
+
     // ------------------------------------------------------------ cycle --
     // level l; dtop = FP64 defect of the top level (r), first = first visit.
     // In mixed precision the top defect is converted to FP32 once, and the
@@ -443,6 +537,10 @@ struct GmgT : GmgBase {
         if (l - 1 == base) {
             c.prof_tag = "L" + std::to_string(l - 1);
             base_correct(c, C, C.dA.p, skip);
+        } else if (l - 1 == coarse_top) {
+            // V-cycle below: the coarse end in one launch (setup_coarse)
+            c.prof_tag = "L" + std::to_string(base) + "-" + std::to_string(l - 1);
+            coarse_cycle<V>(c, coarse_plan.p, coarse_host.lev[1].S, coarse_smem, skip);
         } else {
             const int visits = (ctype == -1) ? 2 : ctype;
             for (int i = 0; i < visits; ++i) {
@@ -668,6 +766,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
         }
     }
     G->setup_base(c);
+    G->setup_coarse(c);
     if (sizeof(V) != sizeof(double)) G->z64.alloc(g->lev[nl - 1].nv);
     G->top_key = A_top->pattern_key();
     return guard.release();

@@ -130,6 +130,9 @@ struct Ctx {
     int sweep_fusion_min_rows = 1 << 18;
     int sweep_fusion_tz = 8;    // z planes per block
     int sweep_wait_test = 0;    // failure test only: bytes no copy delivers (fused sweeps' bounded waits run out)
+    // levels above the base cycled by the one-block coarse kernel (-1: as
+    // many as its cost model finds faster than separate launches, 0: none)
+    int coarse_levels = -1;
     std::string prof_tag;       // set by the orchestration (level / phase)
     std::vector<ProfRec> prof;
     std::vector<cudaEvent_t> ev_pool;

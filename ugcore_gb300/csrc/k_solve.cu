@@ -498,38 +498,6 @@ __device__ __forceinline__ void prolong_row(const GridPair &g, const V *__restri
     if (w) w[f] = mul_rn(t, dfac[f]);
 }
 
-// dc = R d for coarse vertex (I, J, K): R = P^T, Dirichlet coarse rows =
-// injection (k_restrict on the assembled R); children in increasing fine index
-template <class V>
-__device__ __forceinline__ void restrict_row(const GridPair &g, const V *__restrict__ d, V *__restrict__ dc, int I,
-                                             int J, int K)
-{
-    const int c = I + g.cnx * (J + g.cny * K);
-    const int fv = 2 * I + g.nx * (2 * J + g.ny * 2 * K);
-    if (on_box_boundary(I, J, K, g.cnx, g.cny, g.cnz, g.dim)) {
-        const V v = (V)0 + (V)1 * d[fv];
-        dc[c] = (g.dres != 1.0) ? mul_rn(v, (V)g.dres) : v;
-        return;
-    }
-    const int kr = (g.dim == 3) ? 1 : 0;
-    V acc = (V)0;
-    for (int dk = -kr; dk <= kr; ++dk)
-        for (int dj = -1; dj <= 1; ++dj)
-            for (int di = -1; di <= 1; ++di) {
-                const int nodd = (di != 0) + (dj != 0) + (dk != 0);
-                V wt;
-                if (g.tet) {
-                    const bool pos = di > 0 || dj > 0 || dk > 0, neg = di < 0 || dj < 0 || dk < 0;
-                    if (pos && neg) continue;   // not a Kuhn edge through this vertex
-                    wt = nodd ? (V)0.5 : (V)1;
-                } else {
-                    wt = grid_weight<V>(nodd);
-                }
-                acc += wt * d[fv + di + g.nx * (dj + g.ny * dk)];
-            }
-    dc[c] = (g.dres != 1.0) ? mul_rn(acc, (V)g.dres) : acc;
-}
-
 template <class V, bool TILED>
 __global__ void __launch_bounds__(NT) k_prolong_grid(GridPair g, const V *__restrict__ scc, V *__restrict__ sc,
                                                      const V *__restrict__ dfac, V *__restrict__ w, const int *skip)
@@ -604,7 +572,9 @@ template void restrict_grid<float>(Ctx &, const GridPair &, const float *, float
 // dense base solve with the LU-factored inverse, FP64: one warp per row of
 // Ainv, eight rows per block.  Each lane's first entries of its row are read
 // before the launch wait (Ainv is set up once), the defect is staged in
-// shared memory, and the row sum is a fixed-order warp reduction.
+// shared memory, and the row sum is a fixed-order warp reduction of the
+// lanes' explicitly fused partial sums (the fused coarse cycle, k_coarse.cu,
+// repeats them).
 constexpr int kBaseRowsPerBlock = NT / 32;
 constexpr int kBasePre = 8;   // entries per lane read before the wait (rows up to 256 wide)
 
@@ -632,9 +602,9 @@ __global__ void __launch_bounds__(NT) k_base_solve(const double *__restrict__ Ai
 #pragma unroll
     for (int t = 0; t < kBasePre; ++t) {
         const int j = lane + 32 * t;
-        if (j < n) s += a[t] * dsh[j];
+        if (j < n) s = fma_rn(a[t], dsh[j], s);
     }
-    for (int j = lane + 32 * kBasePre; j < n; j += 32) s += __ldg(arow + j) * dsh[j];
+    for (int j = lane + 32 * kBasePre; j < n; j += 32) s = fma_rn(__ldg(arow + j), dsh[j], s);
     s = warp_sum(s);
     if (lane == 0) sc[row] = (V)s;
 }

@@ -149,12 +149,86 @@ __device__ __forceinline__ V prolong_value(const GridPair &g, const V *__restric
     return t;
 }
 
+// dc = R d for coarse vertex (I, J, K): R = P^T, Dirichlet coarse rows =
+// injection (k_restrict on the assembled R); children in increasing fine index
+template <class V>
+__device__ __forceinline__ void restrict_row(const GridPair &g, const V *__restrict__ d, V *__restrict__ dc, int I,
+                                             int J, int K)
+{
+    const int c = I + g.cnx * (J + g.cny * K);
+    const int fv = 2 * I + g.nx * (2 * J + g.ny * 2 * K);
+    if (on_box_boundary(I, J, K, g.cnx, g.cny, g.cnz, g.dim)) {
+        const V v = (V)0 + (V)1 * d[fv];
+        dc[c] = (g.dres != 1.0) ? mul_rn(v, (V)g.dres) : v;
+        return;
+    }
+    const int kr = (g.dim == 3) ? 1 : 0;
+    V acc = (V)0;
+    for (int dk = -kr; dk <= kr; ++dk)
+        for (int dj = -1; dj <= 1; ++dj)
+            for (int di = -1; di <= 1; ++di) {
+                const int nodd = (di != 0) + (dj != 0) + (dk != 0);
+                V wt;
+                if (g.tet) {
+                    const bool pos = di > 0 || dj > 0 || dk > 0, neg = di < 0 || dj < 0 || dk < 0;
+                    if (pos && neg) continue;   // not a Kuhn edge through this vertex
+                    wt = nodd ? (V)0.5 : (V)1;
+                } else {
+                    wt = grid_weight<V>(nodd);
+                }
+                acc += wt * d[fv + di + g.nx * (dj + g.ny * dk)];
+            }
+    dc[c] = (g.dres != 1.0) ? mul_rn(acc, (V)g.dres) : acc;
+}
+
 template <class V>
 void prolong_grid(Ctx &c, const GridPair &g, const V *scc, V *sc, const V *dfac, V *w, const int *skip);
 template <class V>
 void restrict_grid(Ctx &c, const GridPair &g, const V *d, V *dc, const int *skip);
 template <class V>
 void base_solve(Ctx &c, const double *Ainv, int n, const V *d, V *sc, const int *skip);
+
+// ---- the coarse end of a V-cycle in one launch (k_coarse.cu) ----
+// Levels [0] (the base, dense LU inverse) .. [m-1] (the entry level) of a
+// structured hierarchy with damped-Jacobi smoothing on diagonal-layout
+// operators and grid transfers; the entry level's defect arrives in d_in
+// (its dA) and its correction leaves in sc_out (its sc), bit-identical to
+// the separate launches of lmgc.  The kernel keeps everything in shared
+// memory: Ainv (nbase^2 doubles) at byte 0 followed by the base defect in
+// FP64 (nbase doubles), then the level-precision region
+// at byte vbase holding, per level, the operator (S x ld), the Jacobi
+// factors and the vectors, at the element offsets below (the operator and
+// the factors 16-byte aligned).
+constexpr int kCoarseMaxLevels = 8;
+template <class V>
+struct alignas(16) CoarseLevel {
+    const V *val;           // column-scaled operator At, diagonal layout (Dia::vals(), S x ld)
+    const V *dinv, *dfac;   // Jacobi factors (unused on the base level)
+    int n, ncols, ld, S;
+    int off[kMaxDiag];
+    GridPair gp;            // this level and the next coarser one (unused on the base level)
+    int aofs;               // operator values (S * ld elements)
+    int iofs, fofs;         // dinv, dfac (n elements each)
+    int vofs;               // vectors sc, dA[, dB, w] (n elements each)
+};
+template <class V>
+struct alignas(16) CoarsePlan {
+    int m, nu1, nu2, nbase;
+    const double *Ainv;     // nbase x nbase, row-major
+    const V *d_in;
+    V *sc_out;
+    int vbase;              // byte offset of the level-precision region
+    CoarseLevel<V> lev[kCoarseMaxLevels];
+};
+// plan_dev: the plan in device memory (written at set-up); S: the stencil
+// width of every level above the base (coarse_width_ok); smem_bytes: the
+// extent of the layout above
+template <class V>
+void coarse_cycle(Ctx &c, const CoarsePlan<V> *plan_dev, int S, size_t smem_bytes, const int *skip);
+bool coarse_width_ok(int S);
+// set-up: allows launches with up to smem_bytes of dynamic shared memory
+template <class V>
+void coarse_prepare(size_t smem_bytes);
 template <class V>
 void mcgs_colour(Ctx &c, const OpMat<V> &A, const int *rows, int nrows_c, const V *dinv_relax, const V *d, V *t,
                  const int *skip);
