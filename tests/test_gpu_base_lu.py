@@ -1,0 +1,58 @@
+"""The dense LU base solver: bases of at most 64 unknowns are factorised on
+the device (one block, no host round trip in a re-initialisation), larger
+ones on the host.  Both follow LUDecomp's partial pivoting (lib_algebra/
+small_algebra/no_lapack/lu_decomp.h); the multigrid application must match
+the oracle on either side of the limit, and a singular base matrix must be
+reported by the initialisation on either path.
+"""
+import numpy as np
+import pytest
+
+from helpers import oracle_params
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    ("c3", dict(nref=4, base=0)),            # 9 unknowns: device
+    ("c3", dict(nref=4, base=1)),            # 25: device
+    ("c3", dict(nref=4, base=2)),            # 81: host
+    ("c1", dict(nref=2, mx=3, my=3, mz=3)),  # 64: device, the limit
+    ("c1", dict(nref=2, mx=4, my=4, mz=4)),  # 125: host
+    ("c4", dict(nref=2, precision="fp64")),  # 64, upwind convection: device
+]
+
+
+@pytest.mark.parametrize("name,over", CASES)
+def test_gmg_apply_matches_oracle_on_both_paths(ctx, oracle_lib, name, over):
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    cfg = problems.config(name, **over)
+    p = problems.Problem(ctx, cfg)
+    op = oracle_lib.Problem(oracle_params(oracle_lib, cfg), m_top=getattr(p, "m_top", None))
+    d = np.random.default_rng(3).standard_normal(p.n)
+    _, _, bnd = p.hier.export()
+    d[bnd.astype(bool)] = 0.0
+    c_ref = op.apply_gmg(d)
+    dv = ug.GPUVector(ctx, p.n).copy_from(d)
+    cv = ug.GPUVector(ctx, p.n)
+    p.gmg.apply(cv, dv)
+    err = np.abs(cv.numpy() - c_ref).max() / np.abs(c_ref).max()
+    assert err < 1e-12, err
+    # a re-initialisation on new values refactorises (same results again)
+    p.gmg.init(p.A)
+    p.gmg.apply(cv, dv)
+    assert np.abs(cv.numpy() - c_ref).max() / np.abs(c_ref).max() < 1e-12
+
+
+@pytest.mark.parametrize("name,over", [("c0", dict(nref=3)), ("c3", dict(nref=4, base=2))])
+def test_singular_base_is_reported_by_init(ctx, name, over):
+    """zero diffusion: every interior row of the base operator vanishes"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    with pytest.raises(ug.UG4GBError) as ei:
+        p = problems.Problem(ctx, problems.config(name, coef="const", diffusion=0.0, **over))
+        p.gmg.init(p.A)
+    assert ei.value.code == -4
+    # the context stays usable
+    q = problems.Problem(ctx, problems.config("c0", nref=3))
+    assert q.solve()["converged"]

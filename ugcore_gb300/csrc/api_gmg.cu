@@ -185,6 +185,105 @@ static void dense_lu_inverse(int n, std::vector<double> &M, std::vector<double> 
     }
 }
 
+// The same factorisation on the device for bases of at most kDeviceLuMax
+// unknowns (no host round trip in a re-initialisation): one block, M and the
+// inverse X in shared memory.  Partial pivoting as above (the first row of
+// the largest magnitude), row swaps applied to X = I as they happen, products
+// and differences rounded separately; the substitutions run over all columns
+// at once, right-looking: the forward one subtracts in increasing, the
+// backward one in decreasing column order.  *status = 1 on a pivot below
+// 1e-10 (the inverse is then not written).
+constexpr int kDeviceLuMax = 64;
+constexpr int kLuThreads = 256;
+
+__global__ void __launch_bounds__(kLuThreads) k_base_lu(const int *__restrict__ rowptr, const int *__restrict__ col,
+                                                        const double *__restrict__ val, int n,
+                                                        double *__restrict__ inv, int *__restrict__ status)
+{
+    extern __shared__ double lu_sh[];
+    __shared__ int big_sh;
+    double *M = lu_sh, *X = lu_sh + n * n;
+    const int tid = threadIdx.x, nt = blockDim.x, nn = n * n;
+    for (int i = tid; i < nn; i += nt) {
+        M[i] = 0.0;
+        X[i] = 0.0;
+    }
+    __syncthreads();
+    for (int r = tid; r < n; r += nt) {
+        for (int a = rowptr[r]; a < rowptr[r + 1]; ++a) M[r * n + col[a]] = val[a];
+        X[r * n + r] = 1.0;
+    }
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        if (tid < 32) {
+            // each lane: the first largest |M[j][k]| of its rows j >= k; then
+            // the larger value wins, a tie goes to the smaller row
+            double bv = -1.0;
+            int bi = n;
+            for (int j = k + tid; j < n; j += 32) {
+                const double v = fabs(M[j * n + k]);
+                if (v > bv) {
+                    bv = v;
+                    bi = j;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ov > bv || (ov == bv && oi < bi)) {
+                    bv = ov;
+                    bi = oi;
+                }
+            }
+            if (tid == 0) big_sh = bi < n ? bi : k;
+        }
+        __syncthreads();
+        const int big = big_sh;
+        if (big != k)
+            for (int j = tid; j < n; j += nt) {
+                const double t = M[k * n + j];
+                M[k * n + j] = M[big * n + j];
+                M[big * n + j] = t;
+                const double u = X[k * n + j];
+                X[k * n + j] = X[big * n + j];
+                X[big * n + j] = u;
+            }
+        __syncthreads();
+        const double p = M[k * n + k];
+        if (!(fabs(p) >= 1e-10)) {
+            if (tid == 0) *status = 1;
+            return;
+        }
+        for (int i = k + 1 + tid; i < n; i += nt) M[i * n + k] = __ddiv_rn(M[i * n + k], p);
+        __syncthreads();
+        const int m = n - k - 1;
+        for (int t = tid; t < m * m; t += nt) {
+            const int i = k + 1 + t / m, j = k + 1 + t % m;
+            M[i * n + j] = __dsub_rn(M[i * n + j], __dmul_rn(M[i * n + k], M[k * n + j]));
+        }
+        __syncthreads();
+    }
+    for (int k = 0; k < n; ++k) {
+        const int m = n - k - 1;
+        for (int t = tid; t < m * n; t += nt) {
+            const int i = k + 1 + t / n, c = t % n;
+            X[i * n + c] = __dsub_rn(X[i * n + c], __dmul_rn(M[i * n + k], X[k * n + c]));
+        }
+        __syncthreads();
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        for (int c = tid; c < n; c += nt) X[k * n + c] = __ddiv_rn(X[k * n + c], M[k * n + k]);
+        __syncthreads();
+        for (int t = tid; t < k * n; t += nt) {
+            const int i = t / n, c = t % n;
+            X[i * n + c] = __dsub_rn(X[i * n + c], __dmul_rn(M[i * n + k], X[k * n + c]));
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < nn; i += nt) inv[i] = X[i];
+    if (tid == 0) *status = 0;
+}
+
 // ---------------------------------------------------------------- GmgT ---
 template <class V>
 struct GmgT : GmgBase {
@@ -193,6 +292,7 @@ struct GmgT : GmgBase {
     int base_kind = UG4GB_BASE_LU, base_steps = 0;
     double damp = 1.0, damp2 = 1.0;
     DevBuf<double> Ainv;
+    DevBuf<int> lu_status;       // device factorisation of the base: 1 = singular
     DevBuf<double> z64;          // mixed precision: FP64 copy of the top correction
     uint64_t top_key = 0;        // pattern key of the top operator of the last set-up
     int nbase = 0;
@@ -374,6 +474,19 @@ struct GmgT : GmgBase {
         const Csr &A = lev[base].A;
         int n = A.nrows;
         UG_REQUIRE(n <= 4096, UG4GB_ERR_INVALID, "GMG base level larger than 4096 unknowns (dense LU limit)");
+        if (n <= kDeviceLuMax) {
+            const size_t smem = 2 * (size_t)kDeviceLuMax * kDeviceLuMax * sizeof(double);
+            UG_CUDA(cudaFuncSetAttribute(k_base_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            Ainv.alloc((size_t)n * n);
+            lu_status.alloc(1);
+            UG_LAUNCH(c, k_base_lu, 1, kLuThreads, 2 * (size_t)n * n * sizeof(double), A.rowptr.p, A.col.p, A.val.p,
+                      n, Ainv.p, lu_status.p);
+            int st = 0;
+            copy_out(c, &st, lu_status.p, sizeof(int));   // the one wait of a re-initialisation
+            UG_REQUIRE(st == 0, UG4GB_ERR_SINGULAR, "GMG base solver: LU pivot below 1e-10 (singular base matrix)");
+            nbase = n;
+            return;
+        }
         std::vector<int> rp(n + 1), ci(A.nnz);
         std::vector<double> va(A.nnz);
         copy_out(c, rp.data(), A.rowptr.p, sizeof(int) * (n + 1));
@@ -384,8 +497,7 @@ struct GmgT : GmgBase {
             for (int a = rp[r]; a < rp[r + 1]; ++a) M[(size_t)r * n + ci[a]] = va[a];
         dense_lu_inverse(n, M, inv);
         Ainv.alloc((size_t)n * n);
-        copy_in(c, Ainv.p, inv.data(), sizeof(double) * inv.size());
-        UG_CUDA(cudaStreamSynchronize(c.stream));
+        copy_in(c, Ainv.p, inv.data(), sizeof(double) * inv.size());   // from pageable memory: staged on return
         nbase = n;
     }
 
@@ -468,9 +580,8 @@ struct GmgT : GmgBase {
         P.sc_out = lev[best].sc.p;
         coarse_smem = best_bytes;
         coarse_plan.alloc(1);
-        copy_in(c, coarse_plan.p, &P, sizeof(P));
+        copy_in(c, coarse_plan.p, &P, sizeof(P));   // from pageable memory: staged on return
         coarse_prepare<V>(kSmemMax);   // the most any multigrid asks for
-        UG_CUDA(cudaStreamSynchronize(c.stream));
         coarse_top = best;
     }
 

@@ -1,11 +1,14 @@
 // api_solver.cu -- CG / BiCGStab drivers with StdConvCheck on the device.
 //
-// The iteration loop is captured once as a CUDA graph with a conditional
-// WHILE node (body: one Krylov iteration, preconditioner cycle included) and
-// launched once per solve; all scalars (alpha, beta, rho, omega, defects)
+// A solve is captured once as a CUDA graph: the prologue (r = b - A x, the
+// first defect and, for CG, the first step), a kernel that tests the
+// convergence flag, and a conditional WHILE node (body: one Krylov
+// iteration, preconditioner cycle included, and the same test); it is
+// launched once per solve.  All scalars (alpha, beta, rho, omega, defects)
 // stay in device memory, the device-side convergence check ends the loop,
 // and every kernel returns at once when the convergence flag is set.  The
-// host synchronises twice per solve.  The iteration count, defect
+// host waits once per solve, for the scalars and the defect history
+// together.  The iteration count, defect
 // history and stopping rule are those of the reference loop
 // (lib_algebra/operator/linear_solver/cg.h:103-230,
 //  lib_algebra/operator/linear_solver/bicgstab.h:112-400,
@@ -55,6 +58,13 @@ static void drop_graph(ug4gb_solver *s)
     if (s->iter_graph) cudaGraphExecDestroy(s->iter_graph);
     s->iter_graph = nullptr;
     s->graph_x = nullptr;
+}
+
+static void free_pinned(ug4gb_solver *s)
+{
+    if (s->pinned) cudaFreeHost(s->pinned);
+    s->pinned = nullptr;
+    s->pinned_bytes = 0;
 }
 
 namespace {
@@ -118,7 +128,8 @@ void bicg_iteration(ug4gb_solver *s, double *x, double *r)
     bicg_x_r<double>(c, n, x, q, s->s.p, s->t.p, r, red);
 }
 
-// last node of the loop body: keep iterating while the check has not ended
+// the entry test after the prologue and the last node of the loop body:
+// (keep) iterating while the check has not ended
 __global__ void k_loop_cond(cudaGraphConditionalHandle h, const KScal *ks)
 {
     PDL_ENTRY();
@@ -131,10 +142,22 @@ void iteration(ug4gb_solver *s, double *x, double *r)
     else bicg_iteration(s, x, r);
 }
 
-// The whole iteration loop as one graph: a conditional WHILE node whose body
-// is one Krylov iteration (multigrid cycle included) followed by
-// k_loop_cond.  The loop ends when the device-side StdConvCheck (or a
-// breakdown) sets done, at the latest after max_steps iterations.
+// r = b - A x starts the check; CG also does its first step
+void prologue(ug4gb_solver *s, double *x, double *r)
+{
+    Ctx &c = s->ctx->c;
+    RedArgs red = red_of(s);
+    c.prof_tag = "K";
+    krylov_start(c, s->A->op, x, r, red,
+                 s->kind == UG4GB_SOLVER_CG && s->pre ? s->pre->impl->top_defect_buffer() : nullptr);
+    if (s->kind == UG4GB_SOLVER_CG) cg_iteration(s, x, r, true);
+}
+
+// The whole solve as one graph: the prologue and k_loop_cond (captured), then
+// a conditional WHILE node whose body is one Krylov iteration (multigrid
+// cycle included) followed by k_loop_cond.  The loop ends when the
+// device-side StdConvCheck (or a breakdown) sets done, at the latest after
+// max_steps iterations; a solve that ends in the prologue skips it.
 void build_loop_graph(ug4gb_solver *s, double *x, double *r)
 {
     Ctx &c = s->ctx->c;
@@ -145,14 +168,45 @@ void build_loop_graph(ug4gb_solver *s, double *x, double *r)
     int64_t before = c.launches;
     try {
         UG_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+        UG_CUDA(cudaStreamBeginCaptureToGraph(c.stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+        try {
+            prologue(s, x, r);
+            UG_LAUNCH_PDL(c, k_loop_cond, 1, 1, 0, h, (const KScal *)s->ks.p);
+        } catch (...) {
+            cudaGraph_t tmp;
+            cudaStreamEndCapture(c.stream, &tmp);
+            throw;
+        }
+        {
+            cudaGraph_t tmp;
+            UG_CUDA(cudaStreamEndCapture(c.stream, &tmp));
+        }
+        s->prologue_kernels = c.launches - before;
+        // the loop follows the captured chain's last node (the entry test)
+        size_t nn = 0;
+        UG_CUDA(cudaGraphGetNodes(g, nullptr, &nn));
+        std::vector<cudaGraphNode_t> nodes(nn);
+        UG_CUDA(cudaGraphGetNodes(g, nodes.data(), &nn));
+        cudaGraphNode_t leaf = nullptr;
+        int leaves = 0;
+        for (cudaGraphNode_t nd : nodes) {
+            size_t nout = 0;
+            UG_CUDA(cudaGraphNodeGetDependentNodes(nd, nullptr, nullptr, &nout));
+            if (nout == 0) {
+                leaf = nd;
+                ++leaves;
+            }
+        }
+        UG_REQUIRE(leaves == 1, UG4GB_ERR_CUDA, "solver graph: the captured prologue is not one chain");
         cudaGraphNodeParams cp = {};
         cp.type = cudaGraphNodeTypeConditional;
         cp.conditional.handle = h;
         cp.conditional.type = cudaGraphCondTypeWhile;
         cp.conditional.size = 1;
         cudaGraphNode_t node;
-        UG_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+        UG_CUDA(cudaGraphAddNode(&node, g, &leaf, nullptr, 1, &cp));
         cudaGraph_t body = cp.conditional.phGraph_out[0];
+        const int64_t body_start = c.launches;
         UG_CUDA(cudaStreamBeginCaptureToGraph(c.stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
         try {
             iteration(s, x, r);
@@ -164,6 +218,7 @@ void build_loop_graph(ug4gb_solver *s, double *x, double *r)
         }
         cudaGraph_t tmp;
         UG_CUDA(cudaStreamEndCapture(c.stream, &tmp));
+        s->iter_kernels = c.launches - body_start;
         UG_CUDA(cudaGraphInstantiate(&exec, g, 0));
     } catch (...) {
         c.launches = before;
@@ -171,7 +226,6 @@ void build_loop_graph(ug4gb_solver *s, double *x, double *r)
         throw;
     }
     cudaGraphDestroy(g);
-    s->iter_kernels = c.launches - before;
     c.launches = before;
     s->iter_graph = exec;
 }
@@ -201,22 +255,16 @@ void run(ug4gb_solver *s, double *x, double *r)
     s->hist.alloc(h.hist_cap);
     h.hist = s->hist.p;
     UG_CUDA(cudaMemcpyAsync(s->ks.p, &h, sizeof(KScal), cudaMemcpyHostToDevice, c.stream));
-    RedArgs red = red_of(s);
-    // prologue: r = b - A x, start the check; CG also does the first step
-    c.prof_tag = "K";
-    krylov_start(c, s->A->op, x, r, red,
-                 s->kind == UG4GB_SOLVER_CG && s->pre ? s->pre->impl->top_defect_buffer() : nullptr);
-    if (s->kind == UG4GB_SOLVER_CG) cg_iteration(s, x, r, true);
-    int done = 0;
-    read_flags(s, &done);
-    if (!done && c.profiling) {
+    if (c.profiling) {
         // profiled run: direct launches, each one timed with events
+        prologue(s, x, r);
+        int done = 0;
+        read_flags(s, &done);
         while (!done) {
             iteration(s, x, r);
             read_flags(s, &done);
         }
-    }
-    if (!done) {
+    } else {
         int pre_gen = s->pre ? s->pre->gen : -1;
         if (!s->iter_graph || s->graph_x != x || s->graph_r != r || s->graph_pre_gen != pre_gen) {
             drop_graph(s);
@@ -236,18 +284,34 @@ void run(ug4gb_solver *s, double *x, double *r)
         }
         UG_CUDA(cudaGraphLaunch(s->iter_graph, c.stream));
     }
-    int steps_before = s->kind == UG4GB_SOLVER_CG ? 1 : 0;
-    UG_CUDA(cudaMemcpyAsync(&s->host_ks, s->ks.p, sizeof(KScal), cudaMemcpyDeviceToHost, c.stream));
+    // the scalars and the whole history buffer in one wait
+    const size_t hist_off = (sizeof(KScal) + 15) / 16 * 16;
+    const size_t need = hist_off + sizeof(double) * (size_t)h.hist_cap;
+    if (s->pinned_bytes < need) {
+        UG_CUDA(cudaStreamSynchronize(c.stream));
+        free_pinned(s);
+        UG_CUDA(cudaMallocHost(&s->pinned, need));
+        s->pinned_bytes = need;
+    }
+    UG_CUDA(cudaMemcpyAsync(s->pinned, s->ks.p, sizeof(KScal), cudaMemcpyDeviceToHost, c.stream));
+    UG_CUDA(cudaMemcpyAsync((char *)s->pinned + hist_off, s->hist.p, sizeof(double) * (size_t)h.hist_cap,
+                            cudaMemcpyDeviceToHost, c.stream));
     UG_CUDA(cudaStreamSynchronize(c.stream));
+    std::memcpy(&s->host_ks, s->pinned, sizeof(KScal));
     check_device_error(c);
-    if (!c.profiling && s->iter_graph && s->host_ks.step > steps_before) {
-        // the loop body ran once per CG step / per BiCGStab pair of half steps
-        int64_t runs = s->kind == UG4GB_SOLVER_CG ? s->host_ks.step - steps_before : (s->host_ks.step + 1) / 2;
-        c.launches += runs * s->iter_kernels;
+    int steps_before = s->kind == UG4GB_SOLVER_CG ? 1 : 0;
+    if (!c.profiling && s->iter_graph) {
+        // the graph's prologue, and its loop body once per CG step / per
+        // BiCGStab pair of half steps
+        c.launches += s->prologue_kernels;
+        if (s->host_ks.step > steps_before) {
+            int64_t runs = s->kind == UG4GB_SOLVER_CG ? s->host_ks.step - steps_before : (s->host_ks.step + 1) / 2;
+            c.launches += runs * s->iter_kernels;
+        }
     }
     int nh = s->host_ks.step + 1 < h.hist_cap ? s->host_ks.step + 1 : h.hist_cap;
     s->host_hist.resize(nh);
-    copy_out(c, s->host_hist.data(), s->hist.p, sizeof(double) * nh);
+    std::memcpy(s->host_hist.data(), (const char *)s->pinned + hist_off, sizeof(double) * nh);
     const KScal &k = s->host_ks;
     bool converged = (k.dcur < k.min_def) || (k.dcur / k.d0 < k.rel_red);
     if (k.fail) {
@@ -406,6 +470,7 @@ void ug4gb_solver_destroy(ug4gb_solver *s)
     ug4gb_ctx *ctx = s->ctx;
     cudaStreamSynchronize(ctx->c.stream);
     drop_graph(s);
+    free_pinned(s);
     delete s;
     ug4gb_ctx_release(ctx);
 }

@@ -244,9 +244,12 @@ struct ug4gb_solver {
     ug4gb::DevBuf<double> hist;
     ug4gb::KScal host_ks{};
     std::vector<double> host_hist;
-    // captured iteration graph
+    // captured solve graph: the prologue, then the iteration loop
     cudaGraphExec_t iter_graph = nullptr;
-    int64_t iter_kernels = 0;
+    int64_t iter_kernels = 0;       // kernels of one loop body
+    int64_t prologue_kernels = 0;   // kernels before the loop (entry test included)
+    void *pinned = nullptr;         // page-locked read-back of the scalars and the history
+    size_t pinned_bytes = 0;
     const double *graph_x = nullptr;
     const double *graph_r = nullptr;
     int graph_pre_gen = -1;
