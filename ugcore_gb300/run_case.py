@@ -12,6 +12,11 @@ row-wise kernel also with a constant coefficient, 2 the default):
 
     python -m ugcore_gb300.run_case --config c1 --solves 0 --assemblies 3
 
+--coarse-levels K cycles the base and K levels above it in one launch (-1
+the default choice, 0 none):
+
+    python -m ugcore_gb300.run_case --config c3 --direct --coarse-levels 3
+
 --ugx FILE runs an unstructured hierarchy instead (the UGX coarse grid refined
 --nref times, Dirichlet subsets --dirichlet, lognormal K, CG, Jacobi V(2,2)):
 
@@ -84,6 +89,7 @@ def main():
     ap.add_argument("--dirichlet", default=None)
     ap.add_argument("--assemblies", type=int, default=0)
     ap.add_argument("--row-assembly", type=int, default=None)
+    ap.add_argument("--coarse-levels", type=int, default=None)
     args = ap.parse_args()
 
     import ugcore_gb300 as ug
@@ -99,7 +105,7 @@ def main():
     ctx = ug.Context(0)
     ctx.set_operator_format(args.format)
     ctx.set_tuning(sweep_fusion=args.sweep_fusion, sweep_planes=args.sweep_planes,
-                   row_assembly=args.row_assembly)
+                   row_assembly=args.row_assembly, coarse_levels=args.coarse_levels)
     t0 = time.perf_counter()
     p = ugx_problem(ctx, args) if args.ugx else problems.Problem(ctx, problems.config(args.config, **over))
     ctx.synchronize()
