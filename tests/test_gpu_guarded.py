@@ -26,7 +26,7 @@ FILES = ["tests/test_gpu_parity.py", "tests/test_gpu_algebra_ops.py", "tests/tes
          "tests/test_gpu_fv1_pins.py", "tests/test_gpu_gmg_reinit.py", "tests/test_gpu_io.py",
          "tests/test_gpu_newton.py", "tests/test_gpu_perm.py", "tests/test_gpu_rap.py", "tests/test_gpu_refine.py",
          "tests/test_gpu_sweep_fusion.py", "tests/test_gpu_time_step.py", "tests/test_gpu_unstructured.py",
-         "tests/test_gpu_adjoint.py"]
+         "tests/test_gpu_adjoint.py", "tests/test_gpu_coarse_cycle.py", "tests/test_gpu_base_lu.py"]
 # full-size cases (193^3 and 129^3 problems) are left to the normal build
 SKIP = "not full_size"
 

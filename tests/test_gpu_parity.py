@@ -9,6 +9,8 @@ Bars (stated by the benchmark spec for this path):
   oracle solution stated per case); mixed precision: relative residual
   < 1e-10 in FP64 and error against the FP64 oracle solution reported.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -512,3 +514,28 @@ def test_cycle_types_match_oracle(ctx, oracle_lib, name, cycle, over):
         assert np.abs(p.x.numpy() - rs["x"]).max() <= 1e-8 * np.abs(rs["x"]).max()
     else:
         assert abs(st["steps"] - rs["steps"]) <= 1
+
+
+@pytest.mark.parametrize("name", ["ilu_quad_r4", "ilu_hex_r2", "ilu_tet_lognormal_r1", "ilu_hex_convection_r1"])
+def test_ilu_is_ugcore_ilu_with_that_ordering(ctx, name):
+    """the GPU's multicolour ILU(0) smoother against ugcore's own ILU given the
+    same (colour, index) row ordering (tests/golden/make_ilu_golden.py):
+    ILU as the one-step base solver of a one-level cycle returns (LU)^{-1} d"""
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import problems
+    from helpers import GOLDEN
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    mx, my, mz, nref, seed, ck, vk, diffusion, peclet = z["params"]
+    over = dict(elem=str(z["elem"]), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
+                coef={0: "const", 1: "lognormal", 3: "const"}[int(ck)], diffusion=float(diffusion),
+                vel="curl" if int(vk) else None, peclet=float(peclet), smoother="ilu", damp=1.0, base=int(nref),
+                base_solver="smoother", base_steps=1, precision="fp64")
+    p = problems.Problem(ctx, problems.config("c0", **over))
+    _, ci, va = p.A.export_csr()
+    assert ci.size == int(z["nnz"])
+    assert abs(np.abs(va).sum() - float(z["val_sum"])) <= 1e-12 * float(z["val_sum"])
+    for d, c in zip(z["d"], z["c"]):
+        dv = ug.GPUVector(ctx, p.n).copy_from(d)
+        cv = ug.GPUVector(ctx, p.n)
+        p.gmg.apply(cv, dv)
+        assert np.abs(cv.numpy() - c).max() <= 1e-12 * np.abs(c).max()

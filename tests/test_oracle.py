@@ -454,3 +454,34 @@ def test_theta_step_matches_ugcore_theta_time_step(oracle_lib, name):
         assert np.array_equal(d, g["d"][s]), s
         _, _, jv = P.theta_jacobian(top, theta, dt)
         assert np.array_equal(jv, g["J"][s]), s
+
+
+# ---- multicolour ILU(0) against ugcore's ILU with that ordering ------------
+# (tests/golden/make_ilu_golden.py: ug::ILU<CPUAlgebra> given the (colour,
+# index) row ordering through ILU::set_ordering_algorithm, ilu.h:396)
+ILU_GOLDEN = ["ilu_quad_r4", "ilu_hex_r2", "ilu_tet_lognormal_r1", "ilu_hex_convection_r1"]
+
+
+def ilu_golden_problem(orc, z):
+    """the oracle problem of an ILU fixture, with ILU as the one-step base
+    solver of a one-level cycle (so the cycle returns (LU)^{-1} d)"""
+    elem = str(z["elem"])
+    mx, my, mz, nref, seed, ck, vk, diffusion, peclet = z["params"]
+    et = {"quad": orc.ORC_QUAD, "hex": orc.ORC_HEX, "tet": orc.ORC_TET}[elem]
+    p = orc.make_params(elem_type=et, mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
+                        coef_kind=int(ck), vel_kind=int(vk), diffusion=float(diffusion), peclet=float(peclet),
+                        smoother=3, damp=1.0, base=int(nref), base_steps=1)
+    return orc.Problem(p)
+
+
+@pytest.mark.parametrize("name", ILU_GOLDEN)
+def test_multicolour_ilu_is_ugcore_ilu_with_that_ordering(oracle_lib, name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    P = ilu_golden_problem(oracle_lib, z)
+    rp, ci, va = P.matrix()
+    assert ci.size == int(z["nnz"])
+    assert abs(np.abs(va).sum() - float(z["val_sum"])) <= 1e-13 * float(z["val_sum"])
+    for d, c in zip(z["d"], z["c"]):
+        co = P.apply_gmg(d)
+        # ugcore divides by U_ii where the restatement multiplies by 1/U_ii
+        assert np.abs(co - c).max() <= 1e-14 * np.abs(c).max()
