@@ -54,9 +54,11 @@ extern "C" {
 
 /* smoothers, precisions, solvers */
 #define UG4GB_SMOOTHER_JACOBI 0     /* damped Jacobi (lib_algebra/operator/preconditioner/jacobi.h:90) */
-#define UG4GB_SMOOTHER_MCGS 1       /* multicolour Gauss-Seidel (opt-in; no ugcore counterpart) */
-#define UG4GB_SMOOTHER_MCSGS 2      /* symmetric multicolour Gauss-Seidel: forward colour sweep, then
-                                       backward (SymmetricGaussSeidel, gauss_seidel.h:350, in colour order) */
+#define UG4GB_SMOOTHER_MCGS 1       /* multicolour Gauss-Seidel (GaussSeidel, gauss_seidel.h:271, in
+                                       colour order); damp = the SOR factor (set_sor_relax) */
+#define UG4GB_SMOOTHER_MCSGS 2      /* symmetric multicolour Gauss-Seidel, (D/w + U)^-1 D (D/w + L)^-1
+                                       (SymmetricGaussSeidel, gauss_seidel.h:350, in colour order);
+                                       damp = w, 0 < w < 2 */
 #define UG4GB_SMOOTHER_ILU 3        /* ILU(0) in multicolour order (ILU, ilu.h:109-290, of the colour-
                                        permuted operator); damp scales the correction */
 #define UG4GB_SMOOTHER_MCBGS 4      /* backward multicolour Gauss-Seidel: colours in decreasing order

@@ -142,8 +142,9 @@ done
 $CXX $FLAGS "$HERE/ref_driver.cpp" $OBJS "$OUT/obj/crc32_stub.o" \
     "$OUT/obj/ug4_oracle_grid.o" "$OUT/obj/ug4_oracle_fv1.o" "$OUT/obj/ug4_oracle_solve.o" \
     "$OUT/obj/ug4_oracle_api.o" -o "$OUT/ref_driver" -lm
-# ugcore's ILU(0) with a given row ordering (pins the oracle's multicolour ILU)
-$CXX $FLAGS "$HERE/ref_ilu.cpp" $OBJS "$OUT/obj/crc32_stub.o" -o "$OUT/ref_ilu"
+# ugcore's ILU(0) and Gauss-Seidel smoothers with a given row ordering (pins
+# the oracle's multicolour smoothers)
+$CXX $FLAGS "$HERE/ref_smoothers.cpp" $OBJS "$OUT/obj/crc32_stub.o" -o "$OUT/ref_smoothers"
 # ugcore's matrix / vector file writers and readers (MatrixIOMtx, ConnectionViewer)
 IOSRCS="common/util/file_util.cpp common/util/os_dependent_impl/file_util_posix.cpp \
 common/util/os_dependent_impl/os_info_linux.cpp lib_algebra/common/matrixio/matrix_io.cpp \

@@ -382,7 +382,28 @@ static void mcgs_apply(const orc_crs *A, const int *color, int ncolor, double re
         }
 }
 
-/* backward multicolour sweep on c (SymmetricGaussSeidel, gauss_seidel.h:350,
+/* the symmetric sweep's second half (sgs_step, lib_algebra/algebra_common/
+   core_smoothers.h:189-206, in colour order): c2 = D c1, then gs_step_UR
+   (:150-172) in place, c_i = relax (c2_i - sum over later colours of
+   a_ij c_j) / a_ii, colours descending */
+static void mcsgs_backward(const orc_crs *A, const int *color, int ncolor, double relax, double *c)
+{
+    int n = A->n_rows;
+    for (int i = 0; i < n; ++i) c[i] = 1.0 * A->val[orc_crs_find(A, i, i)] * c[i];
+    for (int col = ncolor - 1; col >= 0; --col)
+        for (int i = 0; i < n; ++i) {
+            if (color[i] != col) continue;
+            double s = c[i], diag = 1.0;
+            for (int a = A->rowptr[i]; a < A->rowptr[i + 1]; ++a) {
+                const int j = A->col[a];
+                if (j == i) diag = A->val[a];
+                else if (color[j] > col) s -= A->val[a] * c[j];
+            }
+            c[i] = relax * s / diag;
+        }
+}
+
+/* backward multicolour sweep on c (BackwardGaussSeidel, gauss_seidel.h:316,
    in colour order): c_i += relax (d_i - (A c)_i) / a_ii, colours descending */
 static void mcgs_backward(const orc_crs *A, const int *color, int ncolor, double relax, double *c, const double *d)
 {
@@ -422,7 +443,7 @@ static void smooth(orc_gmg *G, int l, double *c, const double *d, int post)
             return;
         }
         mcgs_apply(&G->A[l], G->color[l], G->ncolor[l], damp, c, d);
-        if (kind == ORC_SMOOTH_MCSGS) mcgs_backward(&G->A[l], G->color[l], G->ncolor[l], damp, c, d);
+        if (kind == ORC_SMOOTH_MCSGS) mcsgs_backward(&G->A[l], G->color[l], G->ncolor[l], damp, c);
     }
 }
 

@@ -516,26 +516,33 @@ def test_cycle_types_match_oracle(ctx, oracle_lib, name, cycle, over):
         assert abs(st["steps"] - rs["steps"]) <= 1
 
 
-@pytest.mark.parametrize("name", ["ilu_quad_r4", "ilu_hex_r2", "ilu_tet_lognormal_r1", "ilu_hex_convection_r1"])
-def test_ilu_is_ugcore_ilu_with_that_ordering(ctx, name):
-    """the GPU's multicolour ILU(0) smoother against ugcore's own ILU given the
-    same (colour, index) row ordering (tests/golden/make_ilu_golden.py):
-    ILU as the one-step base solver of a one-level cycle returns (LU)^{-1} d"""
+@pytest.mark.parametrize("name", ["smoothers_quad_r4", "smoothers_hex_r2", "smoothers_tet_lognormal_r1",
+                                  "smoothers_hex_convection_r1"])
+def test_smoothers_are_ugcore_smoothers_in_that_order(ctx, name):
+    """the GPU's multicolour ILU(0) and Gauss-Seidel smoothers against ugcore's
+    own ILU (given the same (colour, index) row ordering) and GaussSeidel /
+    SymmetricGaussSeidel / BackwardGaussSeidel with set_sor_relax (on the
+    system permuted to that order) (tests/golden/make_smoother_golden.py):
+    the smoother as the one-step base solver of a one-level cycle returns
+    c = B d"""
     import ugcore_gb300 as ug
     from ugcore_gb300 import problems
     from helpers import GOLDEN
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     mx, my, mz, nref, seed, ck, vk, diffusion, peclet = z["params"]
-    over = dict(elem=str(z["elem"]), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
-                coef={0: "const", 1: "lognormal", 3: "const"}[int(ck)], diffusion=float(diffusion),
-                vel="curl" if int(vk) else None, peclet=float(peclet), smoother="ilu", damp=1.0, base=int(nref),
-                base_solver="smoother", base_steps=1, precision="fp64")
-    p = problems.Problem(ctx, problems.config("c0", **over))
-    _, ci, va = p.A.export_csr()
-    assert ci.size == int(z["nnz"])
-    assert abs(np.abs(va).sum() - float(z["val_sum"])) <= 1e-12 * float(z["val_sum"])
-    for d, c in zip(z["d"], z["c"]):
-        dv = ug.GPUVector(ctx, p.n).copy_from(d)
-        cv = ug.GPUVector(ctx, p.n)
-        p.gmg.apply(cv, dv)
-        assert np.abs(cv.numpy() - c).max() <= 1e-12 * np.abs(c).max()
+    kinds = {"ilu": "ilu", "gs": "mcgs", "sgs": "mcsgs", "bgs": "mcbgs"}
+    for key in ("ilu", "gs_1.0", "gs_1.3", "sgs_1.0", "sgs_1.3", "sgs_0.7", "bgs_1.0", "bgs_0.8"):
+        kind, relax = (key, 1.0) if key == "ilu" else (key.split("_")[0], float(key.split("_")[1]))
+        over = dict(elem=str(z["elem"]), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
+                    coef={0: "const", 1: "lognormal", 3: "const"}[int(ck)], diffusion=float(diffusion),
+                    vel="curl" if int(vk) else None, peclet=float(peclet), smoother=kinds[kind], damp=relax,
+                    base=int(nref), base_solver="smoother", base_steps=1, precision="fp64")
+        p = problems.Problem(ctx, problems.config("c0", **over))
+        _, ci, va = p.A.export_csr()
+        assert ci.size == int(z["nnz"])
+        assert abs(np.abs(va).sum() - float(z["val_sum"])) <= 1e-12 * float(z["val_sum"])
+        for d, c in zip(z["d"], z["c_" + key]):
+            dv = ug.GPUVector(ctx, p.n).copy_from(d)
+            cv = ug.GPUVector(ctx, p.n)
+            p.gmg.apply(cv, dv)
+            assert np.abs(cv.numpy() - c).max() <= 1e-12 * np.abs(c).max(), key

@@ -456,32 +456,39 @@ def test_theta_step_matches_ugcore_theta_time_step(oracle_lib, name):
         assert np.array_equal(jv, g["J"][s]), s
 
 
-# ---- multicolour ILU(0) against ugcore's ILU with that ordering ------------
-# (tests/golden/make_ilu_golden.py: ug::ILU<CPUAlgebra> given the (colour,
-# index) row ordering through ILU::set_ordering_algorithm, ilu.h:396)
-ILU_GOLDEN = ["ilu_quad_r4", "ilu_hex_r2", "ilu_tet_lognormal_r1", "ilu_hex_convection_r1"]
+# ---- multicolour smoothers against ugcore's own smoothers in that order ----
+# (tests/golden/make_smoother_golden.py: ug::ILU given the (colour, index)
+# row ordering through ILU::set_ordering_algorithm, ilu.h:396; ug::GaussSeidel,
+# SymmetricGaussSeidel, BackwardGaussSeidel with set_sor_relax on the system
+# permuted to that order)
+SMOOTHER_GOLDEN = ["smoothers_quad_r4", "smoothers_hex_r2", "smoothers_tet_lognormal_r1",
+                   "smoothers_hex_convection_r1"]
+# fixture key -> (oracle smoother kind, SOR factor)
+SMOOTHER_KEYS = {"ilu": (3, 1.0), "gs_1.0": (1, 1.0), "gs_1.3": (1, 1.3), "sgs_1.0": (2, 1.0), "sgs_1.3": (2, 1.3),
+                 "sgs_0.7": (2, 0.7), "bgs_1.0": (4, 1.0), "bgs_0.8": (4, 0.8)}
 
 
-def ilu_golden_problem(orc, z):
-    """the oracle problem of an ILU fixture, with ILU as the one-step base
-    solver of a one-level cycle (so the cycle returns (LU)^{-1} d)"""
+def smoother_golden_problem(orc, z, kind, relax):
+    """the oracle problem of a smoother fixture, the smoother as the one-step
+    base solver of a one-level cycle (so the cycle returns c = B d)"""
     elem = str(z["elem"])
     mx, my, mz, nref, seed, ck, vk, diffusion, peclet = z["params"]
     et = {"quad": orc.ORC_QUAD, "hex": orc.ORC_HEX, "tet": orc.ORC_TET}[elem]
     p = orc.make_params(elem_type=et, mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
                         coef_kind=int(ck), vel_kind=int(vk), diffusion=float(diffusion), peclet=float(peclet),
-                        smoother=3, damp=1.0, base=int(nref), base_steps=1)
+                        smoother=kind, damp=relax, base=int(nref), base_steps=1)
     return orc.Problem(p)
 
 
-@pytest.mark.parametrize("name", ILU_GOLDEN)
-def test_multicolour_ilu_is_ugcore_ilu_with_that_ordering(oracle_lib, name):
+@pytest.mark.parametrize("name", SMOOTHER_GOLDEN)
+def test_multicolour_smoothers_are_ugcore_smoothers_in_that_order(oracle_lib, name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
-    P = ilu_golden_problem(oracle_lib, z)
-    rp, ci, va = P.matrix()
-    assert ci.size == int(z["nnz"])
-    assert abs(np.abs(va).sum() - float(z["val_sum"])) <= 1e-13 * float(z["val_sum"])
-    for d, c in zip(z["d"], z["c"]):
-        co = P.apply_gmg(d)
-        # ugcore divides by U_ii where the restatement multiplies by 1/U_ii
-        assert np.abs(co - c).max() <= 1e-14 * np.abs(c).max()
+    for key, (kind, relax) in SMOOTHER_KEYS.items():
+        P = smoother_golden_problem(oracle_lib, z, kind, relax)
+        rp, ci, va = P.matrix()
+        assert ci.size == int(z["nnz"])
+        assert abs(np.abs(va).sum() - float(z["val_sum"])) <= 1e-13 * float(z["val_sum"])
+        for d, c in zip(z["d"], z["c_" + key]):
+            co = P.apply_gmg(d)
+            # ugcore divides by U_ii where the ILU restatement multiplies by 1/U_ii
+            assert np.abs(co - c).max() <= 5e-15 * np.abs(c).max(), key

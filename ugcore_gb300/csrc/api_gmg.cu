@@ -138,6 +138,15 @@ __global__ void k_vadd(int n, V *a, const V *b, const int *skip)
 }
 
 template <class V>
+__global__ void k_vscale(int n, V *a, V f, const int *skip)
+{
+    PDL_ENTRY();
+    if (skip && *skip) return;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] *= f;
+}
+
+template <class V>
 __global__ void k_zero(int n, V *a, const int *skip)
 {
     PDL_ENTRY();
@@ -754,6 +763,12 @@ struct GmgT : GmgBase {
         if (kind == UG4GB_SMOOTHER_MCSGS || kind == UG4GB_SMOOTHER_MCBGS)
             for (size_t q = L.crow.size(); q-- > 0;)
                 if (L.ncrow[q] > 0) mcgs_colour<V>(c, L.At, L.crow[q].p, L.ncrow[q], dinv, dv, L.t.p, skip);
+        // SymmetricGaussSeidel (sgs_step, core_smoothers.h:189-206) is
+        // (D/w + U)^{-1} D (D/w + L)^{-1}; the backward sweep above, which
+        // updates the forward result by w/a_ii times the defect, gives
+        // (2/w - 1) times that: with relaxation the result is rescaled
+        if (kind == UG4GB_SMOOTHER_MCSGS && dmp != 1.0)
+            UG_LAUNCH_PDL(c, k_vscale<V>, div_up(L.n, 256), 256, 0, L.n, L.t.p, (V)(dmp / (2.0 - dmp)), skip);
     }
 
     const double *apply(Ctx &c, const double *dtop, const int *skip, const double *r_rho, RedArgs *red,
@@ -923,6 +938,8 @@ int ug4gb_gmg_create(ug4gb_ctx *ctx, ug4gb_disc *disc, ug4gb_gmg **out)
 
 static bool smoother_ok(int kind, double damp)
 {
+    // the symmetric sweep is an SSOR step: its factor lies in (0, 2)
+    if (kind == UG4GB_SMOOTHER_MCSGS && !(damp < 2.0)) return false;
     return kind >= UG4GB_SMOOTHER_JACOBI && kind <= UG4GB_SMOOTHER_MCBGS && damp > 0.0 && std::isfinite(damp);
 }
 
