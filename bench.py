@@ -389,7 +389,7 @@ def run_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu,
     }
     if not args.no_extras:
-        line["north_star"] = north_star_summary(mixed, target, adj, conv, asm, cpu, cpu_c2, cpu_c3)
+        line["headline"] = headline_summary(mixed, target, adj, conv, asm, cpu, cpu_c2, cpu_c3)
     return line
 
 
@@ -397,7 +397,7 @@ def _r(x, nd=4):
     return None if x is None else float("%.*g" % (nd, x))
 
 
-def north_star_summary(mixed, target, adj, conv, asm, cpu_c1, cpu_c2, cpu_c3):
+def headline_summary(mixed, target, adj, conv, asm, cpu_c1, cpu_c2, cpu_c3):
     """the numbers the target of this path is stated in, in one compact
     object at the end of the line: the 3D variable-coefficient problem with
     the FP32 multigrid (time, HBM fraction of the whole solve, speed-up over
