@@ -3,7 +3,9 @@ the device (one block, no host round trip in a re-initialisation), larger
 ones on the host.  Both follow LUDecomp's partial pivoting (lib_algebra/
 small_algebra/no_lapack/lu_decomp.h); the multigrid application must match
 the oracle on either side of the limit, and a singular base matrix must be
-reported by the initialisation on either path.
+reported on either path (by the initialisation on the host path, by the next
+application or solve on the device path, whose factorisation is not waited
+for).
 """
 import numpy as np
 import pytest
@@ -44,15 +46,26 @@ def test_gmg_apply_matches_oracle_on_both_paths(ctx, oracle_lib, name, over):
     assert np.abs(cv.numpy() - c_ref).max() / np.abs(c_ref).max() < 1e-12
 
 
-@pytest.mark.parametrize("name,over", [("c0", dict(nref=3)), ("c3", dict(nref=4, base=2))])
-def test_singular_base_is_reported_by_init(ctx, name, over):
-    """zero diffusion: every interior row of the base operator vanishes"""
+@pytest.mark.parametrize("name,over,at_init", [("c0", dict(nref=3), False), ("c3", dict(nref=4, base=2), True)])
+def test_singular_base_is_reported(ctx, name, over, at_init):
+    """zero diffusion: every interior row of the base operator vanishes.  The
+    host factorisation (81 unknowns) reports it from the init; the device one
+    (9 unknowns) from the next application, which waits anyway"""
     import ugcore_gb300 as ug
     from ugcore_gb300 import problems
     with pytest.raises(ug.UG4GBError) as ei:
         p = problems.Problem(ctx, problems.config(name, coef="const", diffusion=0.0, **over))
         p.gmg.init(p.A)
+        assert not at_init, "the host factorisation reports from the init"
+        cv, dv = ug.GPUVector(ctx, p.n), ug.GPUVector(ctx, p.n).copy_from(np.ones(p.n))
+        p.gmg.apply(cv, dv)
     assert ei.value.code == -4
+    if not at_init:
+        # a solve with it reports the same
+        with pytest.raises(ug.UG4GBError) as ei:
+            p2 = problems.Problem(ctx, problems.config(name, coef="const", diffusion=0.0, **over))
+            p2.solve()
+        assert ei.value.code == -4
     # the context stays usable
     q = problems.Problem(ctx, problems.config("c0", nref=3))
     assert q.solve()["converged"]

@@ -302,6 +302,18 @@ struct GmgT : GmgBase {
     double damp = 1.0, damp2 = 1.0;
     DevBuf<double> Ainv;
     DevBuf<int> lu_status;       // device factorisation of the base: 1 = singular
+    int *lu_host = nullptr;      // its page-locked copy, read after the next wait
+    bool lu_pending = false;
+    ~GmgT() override
+    {
+        if (lu_host) cudaFreeHost(lu_host);
+    }
+    void check_base() override
+    {
+        if (!lu_pending) return;
+        lu_pending = false;
+        UG_REQUIRE(*lu_host == 0, UG4GB_ERR_SINGULAR, "GMG base solver: LU pivot below 1e-10 (singular base matrix)");
+    }
     DevBuf<double> z64;          // mixed precision: FP64 copy of the top correction
     uint64_t top_key = 0;        // pattern key of the top operator of the last set-up
     int nbase = 0;
@@ -490,9 +502,11 @@ struct GmgT : GmgBase {
             lu_status.alloc(1);
             UG_LAUNCH(c, k_base_lu, 1, kLuThreads, 2 * (size_t)n * n * sizeof(double), A.rowptr.p, A.col.p, A.val.p,
                       n, Ainv.p, lu_status.p);
-            int st = 0;
-            copy_out(c, &st, lu_status.p, sizeof(int));   // the one wait of a re-initialisation
-            UG_REQUIRE(st == 0, UG4GB_ERR_SINGULAR, "GMG base solver: LU pivot below 1e-10 (singular base matrix)");
+            // no wait: the status is read back behind the factorisation and
+            // checked after the next apply's or solve's own wait (check_base)
+            if (!lu_host) UG_CUDA(cudaMallocHost((void **)&lu_host, sizeof(int)));
+            UG_CUDA(cudaMemcpyAsync(lu_host, lu_status.p, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            lu_pending = true;
             nbase = n;
             return;
         }
@@ -1105,6 +1119,7 @@ int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
             const double *z = m->impl->apply(c, d->d, nullptr, nullptr, nullptr, 0, rd);
             copy_z<double>(c, m->n_top, z, cvec->d, nullptr);
             UG_CUDA(cudaStreamSynchronize(c.stream));
+            m->impl->check_base();
             check_device_error(c);
             return;
         }
@@ -1132,6 +1147,7 @@ int ug4gb_gmg_apply(ug4gb_gmg *m, ug4gb_vector *cvec, const ug4gb_vector *d)
         UG_CUDA(cudaGraphLaunch(m->graph, c.stream));
         c.launches += m->graph_kernels;
         UG_CUDA(cudaStreamSynchronize(c.stream));
+        m->impl->check_base();
         check_device_error(c);
     });
 }

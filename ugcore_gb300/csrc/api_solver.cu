@@ -298,6 +298,7 @@ void run(ug4gb_solver *s, double *x, double *r)
                             cudaMemcpyDeviceToHost, c.stream));
     UG_CUDA(cudaStreamSynchronize(c.stream));
     std::memcpy(&s->host_ks, s->pinned, sizeof(KScal));
+    if (s->pre && s->pre->impl) s->pre->impl->check_base();
     check_device_error(c);
     int steps_before = s->kind == UG4GB_SOLVER_CG ? 1 : 0;
     if (!c.profiling && s->iter_graph) {

@@ -137,6 +137,9 @@ struct GmgBase {
                                 int rho_kind, bool &rho_done, bool top_ready = false) = 0;
     // FP32 buffer a producer of d_top may fill (mixed precision), else null
     virtual float *top_defect_buffer() = 0;
+    // a base factorisation done on the device without a wait reports a
+    // singular matrix here: called after the caller's stream was synchronised
+    virtual void check_base() {}
     virtual const Csr &P(int l) const = 0;
     virtual const Csr &R(int l) const = 0;
     virtual const Csr &levelA(int l) const = 0;   // FP64 operator of level l (re-assembled or R A P)
