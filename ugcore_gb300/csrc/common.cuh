@@ -491,7 +491,8 @@ void sell_from_csr(Ctx &c, const Csr &A, Sell<T> &S, const double *col_scale /* 
 // distinct column offsets (col - row) of A, sorted; false if more than max_s
 bool csr_offsets(Ctx &c, const Csr &A, int max_s, std::vector<int> &offs);
 template <class T>
-void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs, const double *col_scale);
+void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs, const double *col_scale,
+                  bool refill = false);
 // solve format: diagonal when A is square with <= 27 offsets and allow_dia, else SELL-32
 template <class T>
 void op_from_csr(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_scale, bool allow_dia);

@@ -499,10 +499,16 @@ __global__ void k_dia_fill(const int *rowptr, const int *col, const double *val,
     }
 }
 
+// refill: D already holds this pattern's layout (the same offsets, the same
+// CSR pattern): only the pattern's positions are rewritten, the zeros of the
+// absent entries, the padding rows and the guards are kept
 template <class T>
-void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs, const double *col_scale)
+void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs, const double *col_scale,
+                  bool refill)
 {
     UG_REQUIRE((int)offs.size() <= kMaxDiag, UG4GB_ERR_INVALID, "dia_from_csr: too many offsets");
+    const size_t want = (size_t)offs.size() * ((A.nrows + 31) / 32 * 32) + 2 * Dia<T>::kGuard;
+    refill = refill && D.val.p && D.val.n == want && D.S == (int)offs.size() && D.nrows == A.nrows;
     D.nrows = A.nrows;
     D.ncols = A.ncols;
     D.S = (int)offs.size();
@@ -510,7 +516,7 @@ void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs,
     D.ld = (A.nrows + 31) / 32 * 32;
     D.val.alloc((size_t)D.S * D.ld + 2 * Dia<T>::kGuard);
     // absent entries, the padding rows and the guards stay 0
-    UG_CUDA(cudaMemsetAsync(D.val.p, 0, D.val.bytes(), c.stream));
+    if (!refill) UG_CUDA(cudaMemsetAsync(D.val.p, 0, D.val.bytes(), c.stream));
     UG_LAUNCH(c, k_dia_fill<T>, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows, D.ld, D.off,
               D.S, col_scale, D.vals());
 }
@@ -557,7 +563,7 @@ void op_from_csr_cached(Ctx &c, const Csr &A, OpMat<T> &M, const double *col_sca
 {
     if (lay.known && lay.nrows == A.nrows && lay.nnz == A.nnz && (lay.kind == 0 || allow_dia)) {
         if (lay.kind == 1) {
-            dia_from_csr<T>(c, A, M.dia, lay.offs, col_scale);
+            dia_from_csr<T>(c, A, M.dia, lay.offs, col_scale, M.kind == 1);
         } else {
             UG_LAUNCH(c, k_sell_fill<T>, div_up((size_t)M.sell.nslices * kSliceH, 256), 256, 0, A.rowptr.p, A.col.p,
                       A.val.p, A.nrows, M.sell.sptr.p, M.sell.swidth.p, col_scale, M.sell.col.p, M.sell.val.p);
@@ -711,8 +717,10 @@ void transpose_values(Ctx &c, const Csr &A, Csr &T, const DevBuf<int> &perm)
     if (T.nnz) UG_LAUNCH(c, k_gather_perm, div_up(T.nnz, (int64_t)256), 256, 0, T.nnz, perm.p, A.val.p, T.val.p);
 }
 
-template void dia_from_csr<double>(Ctx &, const Csr &, Dia<double> &, const std::vector<int> &, const double *);
-template void dia_from_csr<float>(Ctx &, const Csr &, Dia<float> &, const std::vector<int> &, const double *);
+template void dia_from_csr<double>(Ctx &, const Csr &, Dia<double> &, const std::vector<int> &, const double *,
+                                   bool);
+template void dia_from_csr<float>(Ctx &, const Csr &, Dia<float> &, const std::vector<int> &, const double *,
+                                  bool);
 template void op_from_csr<double>(Ctx &, const Csr &, OpMat<double> &, const double *, bool);
 template void op_from_csr<float>(Ctx &, const Csr &, OpMat<float> &, const double *, bool);
 
