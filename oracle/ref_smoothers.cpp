@@ -20,15 +20,21 @@
  *       set_sor_relax (:96).  Their serial step sweeps in index order and does
  *       not use an ordering algorithm, so they are run on the permuted system
  *       (SetMatrixAsPermutation, SetVectorAsPermutation) and the correction
- *       is permuted back here.
+ *       is permuted back here;
+ *   ug::Jacobi (jacobi.h:90) with its damping, in any order;
+ *   and, with steps = k > 0, each of them as the base solver a script sets
+ *       with gmg:set_base_solver: ug::LinearSolver (linear_solver/
+ *       linear_solver.h:114-190) with StdConvCheck(k, 0, 0, false, true)
+ *       (convergence_check.h:185): k corrections c = B d, x += c, d -= A c.
  *
  * Usage: ref_smoothers <in.bin> <out.bin>
  * in.bin (little-endian): int32 n, int64 nnz, int32 rowptr[n+1],
  *   int32 col[nnz], float64 val[nnz], int64 perm[n] (old index i -> new
  *   index perm[i]), int32 kind (0 ILU, 1 GaussSeidel, 2 SymmetricGaussSeidel,
- *   3 BackwardGaussSeidel), float64 relax (Gauss-Seidel kinds), int32 nvec,
- *   float64 d[nvec][n].
- * out.bin: float64 c[nvec][n], c = B d of that smoother.
+ *   3 BackwardGaussSeidel, 4 Jacobi), float64 relax (SOR factor / Jacobi
+ *   damping), int32 steps (0: one application), int32 nvec, float64 d[nvec][n].
+ * out.bin: float64 c[nvec][n], c = B d of that smoother (steps = 0) or the
+ *   LinearSolver's x after k steps from x = 0.
  */
 #include <cstdio>
 #include <cstdint>
@@ -40,6 +46,9 @@
 #include "lib_algebra/operator/preconditioner/ilu.h"
 #include "lib_algebra/operator/preconditioner/gauss_seidel.h"
 #include "lib_algebra/algebra_common/permutation_util.h"
+#include "lib_algebra/operator/preconditioner/jacobi.h"
+#include "lib_algebra/operator/linear_solver/linear_solver.h"
+#include "lib_algebra/operator/convergence_check.h"
 
 using namespace ug;
 typedef CPUAlgebra::matrix_type Mat;
@@ -93,10 +102,11 @@ int main(int argc, char **argv)
     rd(f, ci.data(), ci.size());
     rd(f, va.data(), va.size());
     rd(f, perm.data(), perm.size());
-    int32_t kind;
+    int32_t kind, steps;
     double relax;
     rd(f, &kind, 1);
     rd(f, &relax, 1);
+    rd(f, &steps, 1);
     int32_t nvec;
     rd(f, &nvec, 1);
     std::vector<double> d((size_t)nvec * n);
@@ -130,11 +140,41 @@ int main(int argc, char **argv)
             SmartPtr<SymmetricGaussSeidel<CPUAlgebra> > gs = make_sp(new SymmetricGaussSeidel<CPUAlgebra>());
             gs->set_sor_relax(relax);
             sm = gs;
+        } else if (kind == 4) {
+            sm = make_sp(new Jacobi<CPUAlgebra>(relax));
         } else {
             SmartPtr<BackwardGaussSeidel<CPUAlgebra> > gs = make_sp(new BackwardGaussSeidel<CPUAlgebra>());
             gs->set_sor_relax(relax);
             sm = gs;
         }
+    }
+    if (steps > 0) {
+        /* the smoother as the base solver: k steps of a LinearSolver */
+        SmartPtr<LinearSolver<Vec> > ls = make_sp(new LinearSolver<Vec>());
+        ls->set_preconditioner(sm);
+        ls->set_convergence_check(make_sp(new StdConvCheck<Vec>(steps, 0.0, 0.0, false, true)));
+        if (!ls->init(run_op)) {
+            fprintf(stderr, "ref_smoothers: LinearSolver::init failed\n");
+            return 1;
+        }
+        FILE *g = fopen(argv[2], "wb");
+        if (!g) return 2;
+        Vec dv(n), cv(n), pd(n), pc(n);
+        for (int v = 0; v < nvec; ++v) {
+            for (int i = 0; i < n; ++i) dv[i] = d[(size_t)v * n + i];
+            if (kind == 0) {
+                cv.set(0.0);
+                if (!ls->apply(cv, dv)) return 1;
+            } else {
+                SetVectorAsPermutation(pd, dv, ord);
+                pc.set(0.0);
+                if (!ls->apply(pc, pd)) return 1;
+                for (int i = 0; i < n; ++i) cv[i] = pc[ord[i]];
+            }
+            for (int i = 0; i < n; ++i) fwrite(&cv[i], sizeof(double), 1, g);
+        }
+        fclose(g);
+        return 0;
     }
     /* through the public interface a linear solver uses */
     SmartPtr<ILinearOperator<Vec> > lop = run_op;

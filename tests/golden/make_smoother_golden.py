@@ -33,18 +33,22 @@ CASES = {
     "smoothers_tet_lognormal_r1": ("tet", 4, 4, 4, 1, 1, 1, 0, 1.0, 10.0),
     "smoothers_hex_convection_r1": ("hex", 3, 3, 3, 1, 1, 3, 1, 1e-2, 10.0),
 }
-# (key, ref_smoothers kind, oracle smoother kind, SOR factor)
-SMOOTHERS = [("ilu", 0, 3, 1.0), ("gs_1.0", 1, 1, 1.0), ("gs_1.3", 1, 1, 1.3), ("sgs_1.0", 2, 2, 1.0),
-             ("sgs_1.3", 2, 2, 1.3), ("sgs_0.7", 2, 2, 0.7), ("bgs_1.0", 3, 4, 1.0), ("bgs_0.8", 3, 4, 0.8)]
+# (key, ref_smoothers kind, oracle smoother kind, SOR factor / damping,
+#  steps: 0 one application, k > 0 the smoother as a k-step base solver)
+SMOOTHERS = [("ilu", 0, 3, 1.0, 0), ("gs_1.0", 1, 1, 1.0, 0), ("gs_1.3", 1, 1, 1.3, 0), ("sgs_1.0", 2, 2, 1.0, 0),
+             ("sgs_1.3", 2, 2, 1.3, 0), ("sgs_0.7", 2, 2, 0.7, 0), ("bgs_1.0", 3, 4, 1.0, 0), ("bgs_0.8", 3, 4, 0.8, 0),
+             ("jacobi_0.6", 4, 0, 0.6, 0), ("ls5_jacobi_0.6", 4, 0, 0.6, 5), ("ls2_gs_1.0", 1, 1, 1.0, 2),
+             ("ls3_sgs_1.3", 2, 2, 1.3, 3), ("ls3_bgs_0.8", 3, 4, 0.8, 3), ("ls4_ilu", 0, 3, 1.0, 4)]
 
 
-def oracle_problem(orc, case, smoother=3, relax=1.0):
+def oracle_problem(orc, case, smoother=3, relax=1.0, steps=1):
     elem, mx, my, mz, nref, seed, ck, vk, diffusion, peclet = case
     et = {"quad": orc.ORC_QUAD, "hex": orc.ORC_HEX, "tet": orc.ORC_TET}[elem]
     # the smoother as the base solver of a one-level cycle: one step from
-    # zero gives c = B d
+    # zero gives c = B d, k steps the base solver's k corrections
     p = orc.make_params(elem_type=et, mx=mx, my=my, mz=mz, nref=nref, seed=seed, coef_kind=ck, vel_kind=vk,
-                        diffusion=diffusion, peclet=peclet, smoother=smoother, damp=relax, base=nref, base_steps=1)
+                        diffusion=diffusion, peclet=peclet, smoother=smoother, damp=relax, base=nref,
+                        base_steps=steps)
     return orc.Problem(p)
 
 
@@ -71,7 +75,7 @@ def run(name, case):
     assert perm.size == n
     d = np.random.default_rng(17).standard_normal((3, n))
     out = {}
-    for key, kind, _, relax in SMOOTHERS:
+    for key, kind, _, relax, steps in SMOOTHERS:
         inp, res = "/tmp/smoothers_%s.in" % name, "/tmp/smoothers_%s.out" % name
         with open(inp, "wb") as f:
             np.asarray([n], np.int32).tofile(f)
@@ -82,6 +86,7 @@ def run(name, case):
             perm.tofile(f)
             np.asarray([kind], np.int32).tofile(f)
             np.asarray([relax], np.float64).tofile(f)
+            np.asarray([steps], np.int32).tofile(f)
             np.asarray([d.shape[0]], np.int32).tofile(f)
             d.astype(np.float64).tofile(f)
         r = subprocess.run([DRIVER, inp, res], capture_output=True, text=True)

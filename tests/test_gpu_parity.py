@@ -522,21 +522,25 @@ def test_smoothers_are_ugcore_smoothers_in_that_order(ctx, name):
     """the GPU's multicolour ILU(0) and Gauss-Seidel smoothers against ugcore's
     own ILU (given the same (colour, index) row ordering) and GaussSeidel /
     SymmetricGaussSeidel / BackwardGaussSeidel with set_sor_relax (on the
-    system permuted to that order) (tests/golden/make_smoother_golden.py):
-    the smoother as the one-step base solver of a one-level cycle returns
-    c = B d"""
+    system permuted to that order) and Jacobi, alone and as a k-step
+    LinearSolver base solver (tests/golden/make_smoother_golden.py): the
+    smoother as the base solver of a one-level cycle returns c = B d"""
     import ugcore_gb300 as ug
     from ugcore_gb300 import problems
     from helpers import GOLDEN
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     mx, my, mz, nref, seed, ck, vk, diffusion, peclet = z["params"]
-    kinds = {"ilu": "ilu", "gs": "mcgs", "sgs": "mcsgs", "bgs": "mcbgs"}
-    for key in ("ilu", "gs_1.0", "gs_1.3", "sgs_1.0", "sgs_1.3", "sgs_0.7", "bgs_1.0", "bgs_0.8"):
-        kind, relax = (key, 1.0) if key == "ilu" else (key.split("_")[0], float(key.split("_")[1]))
+    kinds = {"ilu": "ilu", "gs": "mcgs", "sgs": "mcsgs", "bgs": "mcbgs", "jacobi": "jacobi"}
+    for key in ("ilu", "gs_1.0", "gs_1.3", "sgs_1.0", "sgs_1.3", "sgs_0.7", "bgs_1.0", "bgs_0.8", "jacobi_0.6",
+                "ls5_jacobi_0.6", "ls2_gs_1.0", "ls3_sgs_1.3", "ls3_bgs_0.8", "ls4_ilu"):
+        # "lsK_...": ugcore's LinearSolver with that smoother and StdConvCheck(K, 0, 0)
+        parts = key.split("_")
+        steps = int(parts.pop(0)[2:]) if parts[0].startswith("ls") else 1
+        kind, relax = parts[0], float(parts[1]) if len(parts) > 1 else 1.0
         over = dict(elem=str(z["elem"]), mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
                     coef={0: "const", 1: "lognormal", 3: "const"}[int(ck)], diffusion=float(diffusion),
                     vel="curl" if int(vk) else None, peclet=float(peclet), smoother=kinds[kind], damp=relax,
-                    base=int(nref), base_solver="smoother", base_steps=1, precision="fp64")
+                    base=int(nref), base_solver="smoother", base_steps=steps, precision="fp64")
         p = problems.Problem(ctx, problems.config("c0", **over))
         _, ci, va = p.A.export_csr()
         assert ci.size == int(z["nnz"])

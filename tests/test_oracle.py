@@ -463,28 +463,32 @@ def test_theta_step_matches_ugcore_theta_time_step(oracle_lib, name):
 # permuted to that order)
 SMOOTHER_GOLDEN = ["smoothers_quad_r4", "smoothers_hex_r2", "smoothers_tet_lognormal_r1",
                    "smoothers_hex_convection_r1"]
-# fixture key -> (oracle smoother kind, SOR factor)
-SMOOTHER_KEYS = {"ilu": (3, 1.0), "gs_1.0": (1, 1.0), "gs_1.3": (1, 1.3), "sgs_1.0": (2, 1.0), "sgs_1.3": (2, 1.3),
-                 "sgs_0.7": (2, 0.7), "bgs_1.0": (4, 1.0), "bgs_0.8": (4, 0.8)}
+# fixture key -> (oracle smoother kind, SOR factor / damping, base-solver steps);
+# keys "lsK_..." are ugcore's LinearSolver with that smoother and
+# StdConvCheck(K, 0, 0), as gmg:set_base_solver sets it
+SMOOTHER_KEYS = {"ilu": (3, 1.0, 1), "gs_1.0": (1, 1.0, 1), "gs_1.3": (1, 1.3, 1), "sgs_1.0": (2, 1.0, 1),
+                 "sgs_1.3": (2, 1.3, 1), "sgs_0.7": (2, 0.7, 1), "bgs_1.0": (4, 1.0, 1), "bgs_0.8": (4, 0.8, 1),
+                 "jacobi_0.6": (0, 0.6, 1), "ls5_jacobi_0.6": (0, 0.6, 5), "ls2_gs_1.0": (1, 1.0, 2),
+                 "ls3_sgs_1.3": (2, 1.3, 3), "ls3_bgs_0.8": (4, 0.8, 3), "ls4_ilu": (3, 1.0, 4)}
 
 
-def smoother_golden_problem(orc, z, kind, relax):
-    """the oracle problem of a smoother fixture, the smoother as the one-step
-    base solver of a one-level cycle (so the cycle returns c = B d)"""
+def smoother_golden_problem(orc, z, kind, relax, steps=1):
+    """the oracle problem of a smoother fixture, the smoother as the base
+    solver of a one-level cycle (one step from zero returns c = B d)"""
     elem = str(z["elem"])
     mx, my, mz, nref, seed, ck, vk, diffusion, peclet = z["params"]
     et = {"quad": orc.ORC_QUAD, "hex": orc.ORC_HEX, "tet": orc.ORC_TET}[elem]
     p = orc.make_params(elem_type=et, mx=int(mx), my=int(my), mz=int(mz), nref=int(nref), seed=int(seed),
                         coef_kind=int(ck), vel_kind=int(vk), diffusion=float(diffusion), peclet=float(peclet),
-                        smoother=kind, damp=relax, base=int(nref), base_steps=1)
+                        smoother=kind, damp=relax, base=int(nref), base_steps=steps)
     return orc.Problem(p)
 
 
 @pytest.mark.parametrize("name", SMOOTHER_GOLDEN)
 def test_multicolour_smoothers_are_ugcore_smoothers_in_that_order(oracle_lib, name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
-    for key, (kind, relax) in SMOOTHER_KEYS.items():
-        P = smoother_golden_problem(oracle_lib, z, kind, relax)
+    for key, (kind, relax, steps) in SMOOTHER_KEYS.items():
+        P = smoother_golden_problem(oracle_lib, z, kind, relax, steps)
         rp, ci, va = P.matrix()
         assert ci.size == int(z["nnz"])
         assert abs(np.abs(va).sum() - float(z["val_sum"])) <= 1e-13 * float(z["val_sum"])
