@@ -449,6 +449,20 @@ def test_edge_cases(ctx):
     p.b.set(0.0)
     st = p.solve()
     assert st["steps"] == 0 and np.all(p.x.numpy() == 0.0)
+    # the same solve graph (its entry test skipped the loop) runs the loop for
+    # a real right-hand side, and skips it again for zero
+    p.disc.assemble_linear(p.A, p.b)
+    st = p.solve()
+    assert st["converged"] and st["steps"] > 1
+    assert _rel_residual(p, p.x.numpy()) < 1e-10
+    p.b.set(0.0)
+    st = p.solve()
+    assert st["steps"] == 0 and np.all(p.x.numpy() == 0.0)
+    # BiCGStab ends in its prologue as well
+    q = problems.Problem(ctx, problems.config("c4", nref=2, precision="fp64"))
+    q.b.set(0.0)
+    st = q.solve()
+    assert st["steps"] == 0 and np.all(q.x.numpy() == 0.0)
     for over in [dict(nref=0), dict(nref=4, cycle=2), dict(nref=4, nu1=0), dict(nref=4, base=2),
                  dict(nref=4, nu1=1, nu2=3)]:
         cfg = problems.config("c0", **over)

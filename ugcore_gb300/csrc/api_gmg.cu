@@ -31,6 +31,7 @@ template <class V>
 __global__ void k_diag_inv(const int *rowptr, const int *col, const double *val, int n, double damp, int smoother,
                            double *dinv, double *dfac, V *dinv_v, V *dfac_v)
 {
+    PDL_ENTRY();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double a = 0.0;
@@ -110,6 +111,7 @@ __global__ void k_adjust_R(const int *npar, const int *par, const unsigned char 
 // transposed operator: Dirichlet rows reset to identity
 __global__ void k_dirichlet_identity(const unsigned char *bnd, int n, const int *rowptr, const int *col, double *val)
 {
+    PDL_ENTRY();
     int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n || !bnd[v]) return;
     for (int a = rowptr[v]; a < rowptr[v + 1]; ++a) val[a] = (col[a] == v) ? 1.0 : 0.0;
@@ -209,6 +211,7 @@ __global__ void __launch_bounds__(kLuThreads) k_base_lu(const int *__restrict__ 
                                                         const double *__restrict__ val, int n,
                                                         double *__restrict__ inv, int *__restrict__ status)
 {
+    PDL_ENTRY();
     extern __shared__ double lu_sh[];
     __shared__ int big_sh;
     double *M = lu_sh, *X = lu_sh + n * n;
@@ -373,13 +376,13 @@ struct GmgT : GmgBase {
         L.dfac64.alloc(n);
         L.dinv.alloc(n);
         L.dfac.alloc(n);
-        UG_LAUNCH(c, k_diag_inv<V>, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp, smoother,
+        UG_LAUNCH_PDL(c, k_diag_inv<V>, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp, smoother,
                   L.dinv64.p, L.dfac64.p, L.dinv.p, L.dfac.p);
         // a Gauss-Seidel post-smoother with its own relaxation
         if (smoother2 != UG4GB_SMOOTHER_JACOBI && smoother2 != UG4GB_SMOOTHER_ILU && damp2 != damp) {
             L.dinv2_64.alloc(n);
             L.dinv2.alloc(n);
-            UG_LAUNCH(c, k_diag_inv<V>, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp2,
+            UG_LAUNCH_PDL(c, k_diag_inv<V>, div_up(n, 256), 256, 0, L.A.rowptr.p, L.A.col.p, L.A.val.p, n, damp2,
                       smoother2, L.dinv2_64.p, (double *)nullptr, L.dinv2.p, (V *)nullptr);
         }
         if (smoother == UG4GB_SMOOTHER_JACOBI) {
@@ -500,7 +503,7 @@ struct GmgT : GmgBase {
             UG_CUDA(cudaFuncSetAttribute(k_base_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             Ainv.alloc((size_t)n * n);
             lu_status.alloc(1);
-            UG_LAUNCH(c, k_base_lu, 1, kLuThreads, 2 * (size_t)n * n * sizeof(double), A.rowptr.p, A.col.p, A.val.p,
+            UG_LAUNCH_PDL(c, k_base_lu, 1, kLuThreads, 2 * (size_t)n * n * sizeof(double), A.rowptr.p, A.col.p, A.val.p,
                       n, Ainv.p, lu_status.p);
             // no wait: the status is read back behind the factorisation and
             // checked after the next apply's or solve's own wait (check_base)
@@ -846,7 +849,7 @@ static GmgBase *build_gmg(ug4gb_gmg *m, const ug4gb_matrix *A_top, GmgT<V> *reus
             csr_transpose(c, L.A, T, true);
             L.A = std::move(T);
         }
-        UG_LAUNCH(c, k_dirichlet_identity, div_up(L.A.nrows, 256), 256, 0, g->lev[l].bnd.p, L.A.nrows, L.A.rowptr.p,
+        UG_LAUNCH_PDL(c, k_dirichlet_identity, div_up(L.A.nrows, 256), 256, 0, g->lev[l].bnd.p, L.A.nrows, L.A.rowptr.p,
                   L.A.col.p, L.A.val.p);
     };
     if (!m->rap) {

@@ -369,6 +369,7 @@ __device__ __forceinline__ int kuhn_perm_of(const double *off)
 __global__ void k_coarsen_log(int elem_type, const double *fcoords, const int *felems, int fnx, int fny, int cnx,
                               int cny, int cne, const double *logf, double *logc)
 {
+    PDL_ENTRY();
     int ce = blockIdx.x * blockDim.x + threadIdx.x;
     if (ce >= cne) return;
     const int fx = fnx - 1, fy = fny - 1, cx = cnx - 1, cy = cny - 1;
@@ -418,13 +419,14 @@ __global__ void k_coarsen_log(int elem_type, const double *fcoords, const int *f
 
 __global__ void k_exp(const double *m, int n, double *K)
 {
+    PDL_ENTRY();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e < n) K[e] = exp(m[e]);
 }
 
 void coarsen_log(Ctx &c, const Level &F, const Level &Cl, const double *logf, double *logc)
 {
-    UG_LAUNCH(c, k_coarsen_log, div_up(Cl.ne, 128), 128, 0, F.elem_type, F.coords.p, F.elems.p, F.nx, F.ny, Cl.nx,
+    UG_LAUNCH_PDL(c, k_coarsen_log, div_up(Cl.ne, 128), 128, 0, F.elem_type, F.coords.p, F.elems.p, F.nx, F.ny, Cl.nx,
               Cl.ny, Cl.ne, logf, logc);
 }
 
@@ -448,7 +450,7 @@ void coarsen_log_children(Ctx &c, const Level &F, const Level &Cl, const double 
 
 void exp_elements(Ctx &c, const double *m, int n, double *K)
 {
-    UG_LAUNCH(c, k_exp, div_up(n, 256), 256, 0, m, n, K);
+    UG_LAUNCH_PDL(c, k_exp, div_up(n, 256), 256, 0, m, n, K);
 }
 
 // ------------------------------------------------------------ adjoint ----

@@ -338,6 +338,7 @@ template <int T>
 __global__ void __launch_bounds__(128) k_assemble_rows(AsmArgs a, ClassData<T> cd, const double *__restrict__ flux,
                                                        double volsum)
 {
+    PDL_ENTRY();
     using S = Stencil<T>;
     const int nix = a.cx - 1, niy = a.cy - 1, niz = (S::DIM == 3) ? a.cz - 1 : 1;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -441,6 +442,7 @@ template <int T>
 __global__ void __launch_bounds__(128) k_assemble_rows_all(AsmArgs a, ClassData<T> cd, const double *__restrict__ flux,
                                                            double volsum, const unsigned char *__restrict__ bnd)
 {
+    PDL_ENTRY();
     using S = Stencil<T>;
     const int nx = a.cx + 1, ny = a.cy + 1, nz = (S::DIM == 3) ? a.cz + 1 : 1;
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
@@ -467,6 +469,7 @@ __global__ void __launch_bounds__(256) k_assemble_boundary_rows(AsmArgs a, Class
                                                                 const unsigned char *__restrict__ bnd,
                                                                 const int *__restrict__ brows, int nbrows)
 {
+    PDL_ENTRY();
     const int t = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     if (t >= nbrows) return;
     boundary_row<T>(a, cd, flux, bnd, brows[t], threadIdx.x & 31);
@@ -493,6 +496,7 @@ template <int T>
 __global__ void __launch_bounds__(128) k_assemble_lines_uniform(AsmArgs a, ClassData<T> cd, double volsum, double kval,
                                                                 const unsigned char *__restrict__ bnd, int nlines)
 {
+    PDL_ENTRY();
     using S = Stencil<T>;
     __shared__ double st[S::N];
     extern __shared__ int srp[];
@@ -667,14 +671,14 @@ bool launch_assemble_rows(Ctx &c, const Level &L, const AsmArgs &a_in, RowAsmCac
         if (a.k_uniform && !flux && line_smem <= 32 * 1024) {
             // every grid line, the boundary rows with it
             const int nlines = L.ny * ((L.dim == 3) ? L.nz : 1);
-            UG_LAUNCH(c, k_assemble_lines_uniform<T>, div_up(nlines, kLinesPerBlock), 128, line_smem, a, cd,
+            UG_LAUNCH_PDL(c, k_assemble_lines_uniform<T>, div_up(nlines, kLinesPerBlock), 128, line_smem, a, cd,
                       cache.volsum, a.k_value, L.bnd.p, nlines);
         } else {
             if (L.nv <= kSmallLevelRows) {
-                UG_LAUNCH(c, k_assemble_rows_all<T>, div_up(L.nv, 128), 128, 0, a, cd, flux, cache.volsum, L.bnd.p);
+                UG_LAUNCH_PDL(c, k_assemble_rows_all<T>, div_up(L.nv, 128), 128, 0, a, cd, flux, cache.volsum, L.bnd.p);
             } else {
-                UG_LAUNCH(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux, cache.volsum);
-                UG_LAUNCH(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 8), 256, 0, a, cd, flux, L.bnd.p,
+                UG_LAUNCH_PDL(c, k_assemble_rows<T>, div_up(nint, 128), 128, 0, a, cd, flux, cache.volsum);
+                UG_LAUNCH_PDL(c, k_assemble_boundary_rows<T>, div_up(cache.nbrows, 8), 256, 0, a, cd, flux, L.bnd.p,
                           cache.brows.p, cache.nbrows);
             }
         }

@@ -486,6 +486,7 @@ template <class T>
 __global__ void k_dia_fill(const int *rowptr, const int *col, const double *val, int nrows, int ld, Offs off, int S,
                            const double *col_scale, T *dval)
 {
+    PDL_ENTRY();
     int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nrows) return;
     for (int a = rowptr[r]; a < rowptr[r + 1]; ++a) {
@@ -517,7 +518,7 @@ void dia_from_csr(Ctx &c, const Csr &A, Dia<T> &D, const std::vector<int> &offs,
     D.val.alloc((size_t)D.S * D.ld + 2 * Dia<T>::kGuard);
     // absent entries, the padding rows and the guards stay 0
     if (!refill) UG_CUDA(cudaMemsetAsync(D.val.p, 0, D.val.bytes(), c.stream));
-    UG_LAUNCH(c, k_dia_fill<T>, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows, D.ld, D.off,
+    UG_LAUNCH_PDL(c, k_dia_fill<T>, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows, D.ld, D.off,
               D.S, col_scale, D.vals());
 }
 
@@ -599,6 +600,7 @@ __global__ void k_perm_gather(int64_t n, const double *tidx, int *perm, const do
 
 __global__ void k_gather_perm(int64_t n, const int *perm, const double *aval, double *tval)
 {
+    PDL_ENTRY();
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) tval[k] = aval[perm[k]];
 }
@@ -680,6 +682,7 @@ __global__ void k_check_symmetric(const int *rowptr, const int *col, int n, int 
 // entry (i, j) swapped with (j, i), each pair by the row with the smaller index
 __global__ void k_transpose_symmetric(const int *rowptr, const int *col, double *val, int n)
 {
+    PDL_ENTRY();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     for (int a = rowptr[i]; a < rowptr[i + 1]; ++a) {
@@ -709,12 +712,12 @@ bool csr_pattern_symmetric(Ctx &c, const Csr &A)
 
 void csr_transpose_symmetric_inplace(Ctx &c, Csr &A)
 {
-    if (A.nrows) UG_LAUNCH(c, k_transpose_symmetric, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows);
+    if (A.nrows) UG_LAUNCH_PDL(c, k_transpose_symmetric, div_up(A.nrows, 256), 256, 0, A.rowptr.p, A.col.p, A.val.p, A.nrows);
 }
 
 void transpose_values(Ctx &c, const Csr &A, Csr &T, const DevBuf<int> &perm)
 {
-    if (T.nnz) UG_LAUNCH(c, k_gather_perm, div_up(T.nnz, (int64_t)256), 256, 0, T.nnz, perm.p, A.val.p, T.val.p);
+    if (T.nnz) UG_LAUNCH_PDL(c, k_gather_perm, div_up(T.nnz, (int64_t)256), 256, 0, T.nnz, perm.p, A.val.p, T.val.p);
 }
 
 template void dia_from_csr<double>(Ctx &, const Csr &, Dia<double> &, const std::vector<int> &, const double *,
