@@ -437,7 +437,7 @@ UG4GB_API int ug4gb_gmg_set_rap(ug4gb_gmg *m, int rap);
 UG4GB_API int ug4gb_gmg_set_time_disc(ug4gb_gmg *m, ug4gb_timedisc *td);
 /* AssembledMultiGridCycle::init (mg_solver_impl.hpp:380): copies the top
    operator, re-assembles coarser levels (or forms R A P), builds P/R,
-   smoothers and the LU.  A base level of at most 64 unknowns is factorised
+   smoothers and the LU.  A base level of at most 160 unknowns is factorised
    on the device and the call does not wait for it: a singular base matrix
    (LU pivot below 1e-10) is then reported as UG4GB_ERR_SINGULAR by the next
    ug4gb_gmg_apply or solve with this multigrid; a larger base is factorised

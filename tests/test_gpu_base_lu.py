@@ -1,4 +1,4 @@
-"""The dense LU base solver: bases of at most 64 unknowns are factorised on
+"""The dense LU base solver: bases of at most 160 unknowns are factorised on
 the device (one block, no host round trip in a re-initialisation), larger
 ones on the host.  Both follow LUDecomp's partial pivoting (lib_algebra/
 small_algebra/no_lapack/lu_decomp.h); the multigrid application must match
@@ -17,10 +17,12 @@ pytestmark = pytest.mark.gpu
 CASES = [
     ("c3", dict(nref=4, base=0)),            # 9 unknowns: device
     ("c3", dict(nref=4, base=1)),            # 25: device
-    ("c3", dict(nref=4, base=2)),            # 81: host
-    ("c1", dict(nref=2, mx=3, my=3, mz=3)),  # 64: device, the limit
-    ("c1", dict(nref=2, mx=4, my=4, mz=4)),  # 125: host
+    ("c3", dict(nref=4, base=2)),            # 81: device
+    ("c1", dict(nref=2, mx=3, my=3, mz=3)),  # 64: device
+    ("c1", dict(nref=2, mx=4, my=4, mz=4)),  # 125: device
     ("c4", dict(nref=2, precision="fp64")),  # 64, upwind convection: device
+    ("c3", dict(nref=4, base=3)),            # 289: host
+    ("c1", dict(nref=1, mx=5, my=5, mz=5)),  # 216: host
 ]
 
 
@@ -46,11 +48,12 @@ def test_gmg_apply_matches_oracle_on_both_paths(ctx, oracle_lib, name, over):
     assert np.abs(cv.numpy() - c_ref).max() / np.abs(c_ref).max() < 1e-12
 
 
-@pytest.mark.parametrize("name,over,at_init", [("c0", dict(nref=3), False), ("c3", dict(nref=4, base=2), True)])
+@pytest.mark.parametrize("name,over,at_init", [("c0", dict(nref=3), False), ("c3", dict(nref=4, base=2), False),
+                                               ("c3", dict(nref=4, base=3), True)])
 def test_singular_base_is_reported(ctx, name, over, at_init):
     """zero diffusion: every interior row of the base operator vanishes.  The
-    host factorisation (81 unknowns) reports it from the init; the device one
-    (9 unknowns) from the next application, which waits anyway"""
+    host factorisation (289 unknowns) reports it from the init; the device
+    one (9 and 81 unknowns) from the next application, which waits anyway"""
     import ugcore_gb300 as ug
     from ugcore_gb300 import problems
     with pytest.raises(ug.UG4GBError) as ei:

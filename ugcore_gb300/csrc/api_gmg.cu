@@ -197,14 +197,15 @@ static void dense_lu_inverse(int n, std::vector<double> &M, std::vector<double> 
 }
 
 // The same factorisation on the device for bases of at most kDeviceLuMax
-// unknowns (no host round trip in a re-initialisation): one block, M and the
-// inverse X in shared memory.  Partial pivoting as above (the first row of
-// the largest magnitude), row swaps applied to X = I as they happen, products
-// and differences rounded separately; the substitutions run over all columns
-// at once, right-looking: the forward one subtracts in increasing, the
-// backward one in decreasing column order.  *status = 1 on a pivot below
-// 1e-10 (the inverse is then not written).
-constexpr int kDeviceLuMax = 64;
+// unknowns (no host round trip in a re-initialisation): one block, M in
+// shared memory, the inverse X built in place in the output array.  Partial
+// pivoting as above (the first row of the largest magnitude), row swaps
+// applied to X = I as they happen, products and differences rounded
+// separately; the substitutions run over all columns at once, right-looking:
+// the forward one subtracts in increasing, the backward one in decreasing
+// column order.  *status = 1 on a pivot below 1e-10 (the output is then not
+// an inverse).
+constexpr int kDeviceLuMax = 160;
 constexpr int kLuThreads = 256;
 
 __global__ void __launch_bounds__(kLuThreads) k_base_lu(const int *__restrict__ rowptr, const int *__restrict__ col,
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(kLuThreads) k_base_lu(const int *__restrict__ 
     PDL_ENTRY();
     extern __shared__ double lu_sh[];
     __shared__ int big_sh;
-    double *M = lu_sh, *X = lu_sh + n * n;
+    double *M = lu_sh, *X = inv;
     const int tid = threadIdx.x, nt = blockDim.x, nn = n * n;
     for (int i = tid; i < nn; i += nt) {
         M[i] = 0.0;
@@ -292,7 +293,6 @@ __global__ void __launch_bounds__(kLuThreads) k_base_lu(const int *__restrict__ 
         }
         __syncthreads();
     }
-    for (int i = tid; i < nn; i += nt) inv[i] = X[i];
     if (tid == 0) *status = 0;
 }
 
@@ -499,11 +499,11 @@ struct GmgT : GmgBase {
         int n = A.nrows;
         UG_REQUIRE(n <= 4096, UG4GB_ERR_INVALID, "GMG base level larger than 4096 unknowns (dense LU limit)");
         if (n <= kDeviceLuMax) {
-            const size_t smem = 2 * (size_t)kDeviceLuMax * kDeviceLuMax * sizeof(double);
+            const size_t smem = (size_t)kDeviceLuMax * kDeviceLuMax * sizeof(double);
             UG_CUDA(cudaFuncSetAttribute(k_base_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
             Ainv.alloc((size_t)n * n);
             lu_status.alloc(1);
-            UG_LAUNCH_PDL(c, k_base_lu, 1, kLuThreads, 2 * (size_t)n * n * sizeof(double), A.rowptr.p, A.col.p, A.val.p,
+            UG_LAUNCH_PDL(c, k_base_lu, 1, kLuThreads, (size_t)n * n * sizeof(double), A.rowptr.p, A.col.p, A.val.p,
                       n, Ainv.p, lu_status.p);
             // no wait: the status is read back behind the factorisation and
             // checked after the next apply's or solve's own wait (check_base)
