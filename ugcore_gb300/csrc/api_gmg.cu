@@ -176,23 +176,33 @@ static void dense_lu_inverse(int n, std::vector<double> &M, std::vector<double> 
             for (int j = k + 1; j < n; ++j) M[(size_t)i * n + j] -= M[(size_t)i * n + k] * M[(size_t)k * n + j];
         }
     }
+    // the n solves with the unit vectors, all columns at once (X row-major,
+    // each element with the operations of one solve, in the same order):
+    // X = P I, then X(i,:) -= M(i,k) X(k,:) for k < i in increasing k, then
+    // X(i,:) -= M(i,k) X(k,:) for k > i in increasing k and X(i,:) /= M(i,i)
     inv.assign((size_t)n * n, 0.0);
-    std::vector<double> x(n);
-    for (int col = 0; col < n; ++col) {
-        for (int i = 0; i < n; ++i) x[i] = (i == col) ? 1.0 : 0.0;
-        for (int i = 0; i < n; ++i)
-            if (i < piv[i]) std::swap(x[i], x[piv[i]]);
-        for (int i = 0; i < n; ++i) {
-            double s = x[i];
-            for (int k = 0; k < i; ++k) s -= M[(size_t)i * n + k] * x[k];
-            x[i] = s;
+    double *X = inv.data();
+    for (int i = 0; i < n; ++i) X[(size_t)i * n + i] = 1.0;
+    for (int i = 0; i < n; ++i)
+        if (i < piv[i])
+            for (int c = 0; c < n; ++c) std::swap(X[(size_t)i * n + c], X[(size_t)piv[i] * n + c]);
+    for (int i = 0; i < n; ++i) {
+        double *xi = X + (size_t)i * n;
+        for (int k = 0; k < i; ++k) {
+            const double m = M[(size_t)i * n + k];
+            const double *xk = X + (size_t)k * n;
+            for (int c = 0; c < n; ++c) xi[c] -= m * xk[c];
         }
-        for (int i = n - 1; i >= 0; --i) {
-            double s = x[i];
-            for (int k = i + 1; k < n; ++k) s -= M[(size_t)i * n + k] * x[k];
-            x[i] = s / M[(size_t)i * n + i];
+    }
+    for (int i = n - 1; i >= 0; --i) {
+        double *xi = X + (size_t)i * n;
+        for (int k = i + 1; k < n; ++k) {
+            const double m = M[(size_t)i * n + k];
+            const double *xk = X + (size_t)k * n;
+            for (int c = 0; c < n; ++c) xi[c] -= m * xk[c];
         }
-        for (int i = 0; i < n; ++i) inv[(size_t)i * n + col] = x[i];
+        const double d = M[(size_t)i * n + i];
+        for (int c = 0; c < n; ++c) xi[c] = xi[c] / d;
     }
 }
 
@@ -201,10 +211,11 @@ static void dense_lu_inverse(int n, std::vector<double> &M, std::vector<double> 
 // shared memory, the inverse X built in place in the output array.  Partial
 // pivoting as above (the first row of the largest magnitude), row swaps
 // applied to X = I as they happen, products and differences rounded
-// separately; the substitutions run over all columns at once, right-looking:
-// the forward one subtracts in increasing, the backward one in decreasing
-// column order.  *status = 1 on a pivot below 1e-10 (the output is then not
-// an inverse).
+// separately; the forward substitution runs over all columns at once,
+// right-looking (subtracting in increasing column order), the backward one
+// column by column in the order of SolveLU, so that each element of the
+// inverse takes the operations of the host statement above.  *status = 1 on a
+// pivot below 1e-10 (the output is then not an inverse).
 constexpr int kDeviceLuMax = 160;
 constexpr int kLuThreads = 256;
 
@@ -284,15 +295,14 @@ __global__ void __launch_bounds__(kLuThreads) k_base_lu(const int *__restrict__ 
         }
         __syncthreads();
     }
-    for (int k = n - 1; k >= 0; --k) {
-        for (int c = tid; c < n; c += nt) X[k * n + c] = __ddiv_rn(X[k * n + c], M[k * n + k]);
-        __syncthreads();
-        for (int t = tid; t < k * n; t += nt) {
-            const int i = t / n, c = t % n;
-            X[i * n + c] = __dsub_rn(X[i * n + c], __dmul_rn(M[i * n + k], X[k * n + c]));
+    // backward: one thread per column, each row's sum in increasing column
+    // order as SolveLU (the columns are independent: no barrier)
+    for (int c = tid; c < n; c += nt)
+        for (int i = n - 1; i >= 0; --i) {
+            double v = X[i * n + c];
+            for (int k = i + 1; k < n; ++k) v = __dsub_rn(v, __dmul_rn(M[i * n + k], X[k * n + c]));
+            X[i * n + c] = __ddiv_rn(v, M[i * n + i]);
         }
-        __syncthreads();
-    }
     if (tid == 0) *status = 0;
 }
 
