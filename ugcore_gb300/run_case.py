@@ -17,6 +17,12 @@ the default choice, 0 none):
 
     python -m ugcore_gb300.run_case --config c3 --direct --coarse-levels 3
 
+--gradients N times N adjoint gradients dJ/dm of J = 0.5 |u(m)|^2 through
+torch.autograd (forward assembly and solve, transposed solve, element
+gradient) on the configuration's problem with a per-element log coefficient:
+
+    python -m ugcore_gb300.run_case --config c3 --solves 0 --gradients 5
+
 --ugx FILE runs an unstructured hierarchy instead (the UGX coarse grid refined
 --nref times, Dirichlet subsets --dirichlet, lognormal K, CG, Jacobi V(2,2)):
 
@@ -90,6 +96,7 @@ def main():
     ap.add_argument("--assemblies", type=int, default=0)
     ap.add_argument("--row-assembly", type=int, default=None)
     ap.add_argument("--coarse-levels", type=int, default=None)
+    ap.add_argument("--gradients", type=int, default=0)
     args = ap.parse_args()
 
     import ugcore_gb300 as ug
@@ -127,6 +134,22 @@ def main():
             p.disc.assemble_linear(p.A, p.b)
         ctx.synchronize()
         res["assembly_ms"] = (time.perf_counter() - t0) * 1e3 / args.assemblies
+    if args.gradients:
+        import torch
+        from ugcore_gb300 import adjoint
+        prob = adjoint.DifferentiableProblem(ctx, problems.config(args.config, **over))
+        m0 = torch.tensor(prob.m_top, device="cuda")
+        f = torch.ones(prob.n, dtype=torch.float64, device="cuda")
+        times = []
+        for r in range(args.gradients):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mm = (m0 * (1.0 + 0.01 * r)).clone().requires_grad_(True)
+            u = adjoint.fv1_solve(mm, f, prob)
+            (0.5 * (u ** 2).sum()).backward()
+            torch.cuda.synchronize()
+            times.append((time.perf_counter() - t0) * 1e3)
+        res["gradient_ms"] = times
     if args.direct:
         prof = ctx.profile_end()
         res["kernels"] = {k: [v[0], round(v[1], 4)] for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])[:12]}
