@@ -121,3 +121,31 @@ def test_adjoint_gradient_identical():
         out.append((u.detach().cpu().numpy(), m.grad.cpu().numpy()))
     assert np.array_equal(out[0][0], out[1][0])
     assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_reinitialisations_keep_bit_identity():
+    """re-initialisations of the same multigrid (new coefficients; changed
+    smoothing counts and cycle type) refresh the one-launch cycle's plan: its
+    corrections stay bit-identical to the separate launches"""
+    import torch
+    import ugcore_gb300 as ug
+    from ugcore_gb300 import adjoint, problems
+    cfg = problems.config("c3", nref=5)
+    pr, pf = [], []
+    for levels, out in ((0, pr), (-1, pf)):
+        ctx = ug.Context(0)
+        ctx.set_tuning(coarse_levels=levels)
+        out.append(adjoint.DifferentiableProblem(ctx, cfg))
+    d = np.random.default_rng(5).uniform(-1.0, 1.0, pr[0].n)
+    m0 = torch.tensor(pr[0].m_top, device="cuda")
+    f = torch.ones(pr[0].n, dtype=torch.float64, device="cuda")
+    for step, (nu1, nu2, cycle) in enumerate([(2, 2, 1), (2, 2, 1), (1, 3, 1), (3, 0, 1), (2, 2, 2), (2, 2, 1)]):
+        res = []
+        for p in (pr[0], pf[0]):
+            p.gmg.set_num_presmooth(nu1)
+            p.gmg.set_num_postsmooth(nu2)
+            p.gmg.set_cycle_type(cycle)
+            p.update(m0 * (1.0 + 0.05 * step), f)
+            cv, dv = _apply(p, d)
+            res.append(cv.numpy())
+        assert np.array_equal(res[0], res[1]), (step, float(np.abs(res[0] - res[1]).max()))
